@@ -1,0 +1,334 @@
+"""Benchmark of the GB300 timestep: particle-steps/s on the 2-D production
+workload (N = 1e7 particles, grid 128x128x1x32x1, box 40x40, Dt 0.1, Dr 1.0,
+active stress -2, dt 0.005, 1 % sinusoidal density perturbation along x),
+plain FP64 path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+One JSON line on stdout (rank 0).  --impl reference times the CPU path of the
+same workload instead: the FP64 C restatement of the reference timestep
+(oracle/), parallel like the reference (serial histogram and stress
+contraction, parallel FFT components and particle loop) on all host threads.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BASELINE_METRIC = "particle-steps/s on 1 GB300 at fixed L2 field error vs FP64 oracle; plain vs denoised/FP32"
+UNIT = "particle-steps/s"
+GRID = (128, 128, 1, 32, 1)
+BOX = (40.0, 40.0, 1.0)
+N = 10_000_000
+PARAMS = dict(timestep=0.005, trans_diffusion=0.1, rot_diffusion=1.0, stress_active=-2.0)
+WORKLOAD = "2-D production size, plain FP64: N=1e7, grid 128x128x1x32x1, box 40x40, 1% sin(2 pi x/40) density"
+TWOPI = 2 * np.pi
+
+
+def c1_particles(n, seed=1):
+    rng = np.random.default_rng(seed)
+    L = BOX[0]
+    u = rng.random(n)
+    x = u * L
+    for _ in range(30):
+        f = x / L + 0.01 * (1 - np.cos(TWOPI * x / L)) / TWOPI - u
+        x -= f / ((1 + 0.01 * np.sin(TWOPI * x / L)) / L)
+    return np.column_stack([np.mod(x, L), BOX[1] * rng.random(n), np.zeros(n), TWOPI * rng.random(n),
+                            np.full(n, np.pi / 2)])
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi clock sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.lines = []
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_step_rate(n, steps, nthreads, seed=1):
+    """Time the oracle (the reference restatement) on n particles of the
+    workload: returns (particle-steps/s, seconds)."""
+    from oracle import oracle as O
+    s = O.make_settings(GRID, BOX, timestep=PARAMS["timestep"], trans_diff=PARAMS["trans_diffusion"],
+                        rot_diff=PARAMS["rot_diffusion"], active=PARAMS["stress_active"], quasi2d=True, seed=seed)
+    sim = O.Simulation(s, n, nthreads=nthreads)
+    sim.init(c1_particles(n, seed))
+    sim.do_timestep()  # warm
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.do_timestep()
+    dt = time.perf_counter() - t0
+    return n * steps / dt, dt
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the CPU path of the workload on all host threads."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    nthreads = os.cpu_count() or 1
+    # size the per-step sample so the whole run ends within a few minutes
+    probe_n = 1_000_000
+    rate, _ = cpu_step_rate(probe_n, 1, nthreads)
+    budget_s = 150.0
+    n_sample = int(min(N, max(100_000, rate * budget_s / max(1, args.steps + args.warmup))))
+    from oracle import oracle as O2
+    s = O2.make_settings(GRID, BOX, timestep=PARAMS["timestep"], trans_diff=PARAMS["trans_diffusion"],
+                         rot_diff=PARAMS["rot_diffusion"], active=PARAMS["stress_active"], quasi2d=True)
+    sim = O2.Simulation(s, n_sample, nthreads=nthreads)
+    sim.init(c1_particles(n_sample))
+    for _ in range(args.warmup):
+        sim.do_timestep()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sim.do_timestep()
+    dt = time.perf_counter() - t0
+    value = n_sample * args.steps / dt
+    sample = (f"{n_sample} particles of the workload (grid 128x128x1x32x1) per step, {args.steps} timed steps "
+              f"after {args.warmup} warm-up; FP64 C restatement of do_timestep on {nthreads} threads "
+              f"({cpu_model()})")
+    line = {
+        "impl": "reference", "metric": BASELINE_METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "particles_per_step": n_sample, "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world, dist):
+    import torch
+
+    import stochasticsampling_gb300 as ss
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    params = dict(PARAMS, number_of_particles=N, seed=1 + rank)
+    p0 = c1_particles(N, seed=1 + rank)
+    sim = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True, stream=stream.cuda_stream)
+    sim.init(p0)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    with torch.cuda.stream(stream):
+        sim.run(args.warmup)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        l0 = sim.launch_count()
+        clocks = Clocks(local)
+        clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.run(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        ms = e0.elapsed_time(e1)
+        launches = sim.launch_count() - l0
+    sim.synchronize()
+    t = torch.tensor([ms], dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t[0])
+    value = world * N * args.steps / (ms_max / 1e3)
+
+    # per-stage CUDA events over K direct-launch steps (same stream, same workload)
+    sim.profile(True)
+    sim.run(args.steps)
+    stage_ms, nprof = sim.profile_read()
+    sim.profile(False)
+    stage_avg = {k: v / max(1, nprof) for k, v in stage_ms.items()}
+
+    # end to end through the C ABI with pinned host buffers: per step the host
+    # particle array goes in (ss_resume), the step runs, the particles come out
+    host_in = torch.empty((N, 5), dtype=torch.float64, pin_memory=True).numpy()
+    host_out = torch.empty((N, 5), dtype=torch.float64, pin_memory=True).numpy()
+    host_in[:] = sim.get_particles()
+    ts = sim.get_timestep()
+    e2e_steps = max(1, min(args.steps, 10))
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        sim.resume(host_in, ts + k)
+        sim.do_timestep()
+        sim.get_particles(out=host_out)
+        host_in, host_out = host_out, host_in
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    te = torch.tensor([t_e2e], dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = world * N * e2e_steps / float(te[0])
+    sim.close()
+
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    gx, gy, gz, gp, gt = GRID
+    ncell, nbins = gx * gy * gz, gx * gy * gz * gp * gt
+    # update kernel, algorithmic bytes per launch: state read + written (5 f64),
+    # cell key read + written, particle id read, the field table once, the
+    # next histogram once (u32)
+    upd_bytes = N * (40 + 40 + 4 + 4 + 4) + ncell * 16 * 8 + nbins * 4
+    upd_ms = stage_avg["update"]
+    achieved = upd_bytes / (upd_ms / 1e3) / 1e9
+    # whole step, SURVEY-style algorithmic bytes: particles 80 B, histogram 12 B
+    # per bin, 21 FFT components read+written as 16 B complex, field table
+    step_bytes = N * 80 + nbins * 12 + ncell * 16 * 2 * 21 + ncell * 13 * 8
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            traffic = json.load(f).get("k_update_c1_bytes_per_launch")
+    except Exception:
+        pass
+    cpu = None
+    if not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        n_cpu = N
+        rate, secs = cpu_step_rate(1_000_000, 1, nthreads)
+        steps_cpu = max(2, min(10, int(20.0 / max(1e-9, N / rate))))
+        if N / rate * steps_cpu > 40:
+            n_cpu = int(rate * 20 / steps_cpu)
+        v, secs = cpu_step_rate(n_cpu, steps_cpu, nthreads)
+        cpu = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"{steps_cpu} steps of {n_cpu} particles of the workload, FP64 C restatement of "
+                         f"do_timestep, OpenMP on {nthreads} threads ({cpu_model()}), {secs:.1f} s"}
+    line = {
+        "metric": BASELINE_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "particles": N, "grid": list(GRID), "box": list(BOX), **PARAMS,
+                   "noise": "on-device Philox4x32-10", "execution": "CUDA graph per step, counting sort by cell",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   "l2": "inputs larger than L2 (400 MB particle state per step)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "k_update (fused Langevin step + next-step binning)",
+                     "peak_source": peak_kind, "bytes_per_launch": upd_bytes, "avg_launch_ms": upd_ms,
+                     "note": "FP64-issue bound on GB300 (low FP64 rate); HBM fraction reported as required"},
+        "step_roofline": {"algorithmic_bytes": step_bytes,
+                          "achieved_gbs": step_bytes / (ms_max / args.steps / 1e3) / 1e9},
+        "stage_ms": stage_avg,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N * 5 * 8, "d2h_bytes_per_step": N * 5 * 8,
+                "steps": e2e_steps, "api": "ss_resume(host) + ss_do_timestep + ss_get_particles(host), pinned"},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        if backend == "nccl":
+            import torch
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend)
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            run_gpu(args, rank, world, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

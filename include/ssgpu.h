@@ -1,0 +1,184 @@
+/*
+ * ssgpu.h -- C ABI of the GB300 (sm_103a) timestep for stochasticsampling.
+ *
+ * One context (ss_ctx) holds one simulation on one GPU: the particle state in
+ * HBM, the histogram, the spectral solvers (cuFFT plans) and the per-cell
+ * field table.  Every entry point returns an int status (SS_OK = 0); no C++
+ * exception or CUDA error crosses the ABI.  ss_last_error() returns the text
+ * of the last failure on a context.  A context is used by one host thread at
+ * a time; its GPU work runs in order on its stream.
+ *
+ * All particle arrays at this boundary use the reference's serialised layout,
+ * [n][5] doubles (x, y, z, phi, theta) -- src/particle.rs:363-395 -- in HOST
+ * memory (pageable or pinned).  Fields use the reference's ndarray C order.
+ * Complex arrays are interleaved (re, im) doubles, the layout of
+ * num_complex::Complex<f64> and of cufftDoubleComplex.
+ */
+#ifndef SSGPU_H
+#define SSGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SS_OK 0
+#define SS_ERR_INVALID_ARGUMENT 1 /* bad pointer, size or parameter (host-side check) */
+#define SS_ERR_CUDA 2             /* a CUDA runtime call failed */
+#define SS_ERR_CUFFT 3            /* a cuFFT call failed */
+#define SS_ERR_STATE 4            /* call out of order (e.g. a step before ss_init) */
+#define SS_ERR_PARTICLE_COUNT 5   /* n differs from number_of_particles */
+#define SS_ERR_RANGE 6            /* a device bounds check fired (non-finite state) */
+
+/* GridSize, src/lib.rs:52-61 */
+typedef struct {
+    uint64_t x, y, z, phi, theta;
+} ss_grid;
+
+/* BoxSize, src/lib.rs:44-51 */
+typedef struct {
+    double x, y, z;
+} ss_box;
+
+/* The numeric part of Settings (src/bin/simulation/settings/mod.rs:24-118)
+ * that the timestep reads. */
+typedef struct {
+    double timestep;               /* simulation.timestep */
+    double trans_diffusion;        /* parameters.diffusion.translational */
+    double rot_diffusion;          /* parameters.diffusion.rotational */
+    double stress_active;          /* parameters.stress.active */
+    double stress_magnetic;        /* parameters.stress.magnetic */
+    double shape;                  /* parameters.shape */
+    double magnetic_drag;          /* parameters.magnetic_drag */
+    double hydro_screening;        /* parameters.hydro_screening */
+    double volume_exclusion;       /* parameters.volume_exclusion */
+    double magnetic_reorientation; /* parameters.magnetic_reorientation */
+    double magnetic_dipole_dipole; /* parameters.magnetic_dipole.magnetic_dipole_dipole */
+    uint64_t number_of_particles;  /* simulation.number_of_particles */
+    uint64_t seed;                 /* simulation.seed (Philox key) */
+} ss_params;
+
+/* flags for ss_create */
+#define SS_FLAG_QUASI2D 1u         /* cargo feature quasi2d: grid z = 1, after each step z = 0, theta = pi/2 */
+#define SS_FLAG_ALWAYS_MAGNETIC 2u /* run the dipolar solver even when its couplings are zero */
+#define SS_FLAG_NO_SORT 4u         /* keep particles in input order (no counting sort by cell) */
+#define SS_FLAG_NO_GRAPH 8u        /* launch kernels directly instead of replaying a CUDA graph */
+
+typedef struct ss_ctx ss_ctx;
+
+/* Simulation::new, src/bin/simulation/mod.rs:91-160.  Builds the stress kernel
+ * (closure :100-104), the k meshes and the cuFFT plans, allocates HBM.
+ * stream: a cudaStream_t to run on, or NULL for a stream owned by the context. */
+int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, uint32_t flags,
+              void *stream, ss_ctx **out);
+/* Drop for Simulation, src/bin/simulation/mod.rs:377-381 */
+int ss_destroy(ss_ctx *ctx);
+
+/* Simulation::init, src/bin/simulation/mod.rs:163-196: sanitises every
+ * particle with Particle::new (src/particle.rs:186-201) and samples the
+ * distribution (x box volume).  n must equal number_of_particles. */
+int ss_init(ss_ctx *ctx, const double *particles, uint64_t n);
+/* Simulation::resume, src/bin/simulation/mod.rs:199-207.  The noise stream is
+ * counter based (Philox4x32-10 keyed by seed, counter = (particle, timestep)),
+ * so restoring the timestep restores the noise exactly. */
+int ss_resume(ss_ctx *ctx, const double *particles, uint64_t n, uint64_t timestep);
+
+/* Simulation::do_timestep, src/bin/simulation/mod.rs:251-374.
+ * noise: NULL -> on-device Philox noise; otherwise [n][5] host doubles
+ * (x, y, z, axis_angle, rotate_angle) = RandomVector (:51-57), the
+ * verification mode that takes the reference's host-generated noise.
+ * timestep_out (may be NULL) receives the incremented step counter. */
+int ss_do_timestep(ss_ctx *ctx, const double *noise, uint64_t *timestep_out);
+/* `steps` calls of do_timestep with Philox noise (the driver loop,
+ * src/bin/main.rs:182-262, without IO); replays a captured CUDA graph. */
+int ss_run(ss_ctx *ctx, uint64_t steps, uint64_t *timestep_out);
+/* The on-device noise of step `timestep` as the RandomVector array the
+ * verification mode takes: out[n][5] host doubles (x, y, z, axis_angle,
+ * rotate_angle) in the caller's particle order (src/bin/simulation/mod.rs:
+ * 272-286).  axis_angle is reported as 2*pi*U; the step itself uses
+ * sincospi(2U), the same angle without the rounding of 2*pi*U. */
+int ss_noise(ss_ctx *ctx, uint64_t timestep, double *out);
+/* Wait for the context's stream. */
+int ss_synchronize(ss_ctx *ctx);
+
+/* Simulation::get_particles / get_particles_head (:221-228): [n][5] */
+int ss_get_particles(ss_ctx *ctx, double *out, uint64_t n);
+/* Simulation::get_distribution (:231-233): dist[x][y][z][phi][theta] as
+ * sampled at the start of the last step (after init: the initial sample),
+ * normalised like Distribution::sample_from x box volume. */
+int ss_get_distribution(ss_ctx *ctx, double *out);
+/* the integer histogram behind ss_get_distribution (bit-exact counts) */
+int ss_get_counts(ss_ctx *ctx, uint32_t *out);
+/* Simulation::get_flow_field (:236-238): Re(u), [3][x][y][z] */
+int ss_get_flow_field(ss_ctx *ctx, double *out);
+/* Simulation::get_magnetic_field (:241-243): Re(B), [3][x][y][z]
+ * (zeros while the dipolar solver is skipped) */
+int ss_get_magnetic_field(ss_ctx *ctx, double *out);
+/* the complex views returned by SpectralSolver::mean_flow_field
+ * (src/flowfield/spectral_solver.rs:233-254): u [3][x][y][z], grad [3][3][x][y][z] */
+int ss_get_flow_complex(ss_ctx *ctx, double *u, double *grad);
+/* the complex views returned by MagneticSolver::mean_magnetic_field
+ * (src/magnetic_interaction/magnetic_solver.rs:139-161) */
+int ss_get_magnetic_complex(ss_ctx *ctx, double *b, double *gradb);
+/* Simulation::get_timestep (:246-248) */
+int ss_get_timestep(ss_ctx *ctx, uint64_t *out);
+
+/* Library seams on an explicit distribution dist[x][y][z][phi][theta] (host):
+ * SpectralSolver::mean_flow_field(screening, &Distribution) and
+ * MagneticSolver::mean_magnetic_field(&Distribution).  Outputs as
+ * ss_get_flow_complex / ss_get_magnetic_complex.  They overwrite the
+ * context's field buffers; the particle state is untouched. */
+int ss_mean_flow_field(ss_ctx *ctx, double screening, const double *dist, double *u, double *grad);
+int ss_mean_magnetic_field(ss_ctx *ctx, const double *dist, double *b, double *gradb);
+
+/* LangevinBuilder chain (src/integrators/langevin_builder/mod.rs:25-125,
+ * modifiers.rs:39-231) on n independent particles with shared arguments,
+ * run by the same device code as the timestep.  mask selects modifiers
+ * (bit k = k-th modifier of the chain in do_timestep order:
+ * self_propulsion, convection, magnetic_dipole_dipole_force,
+ * external_field_alignment, magnetic_dipole_dipole_rotation,
+ * jeffrey_vorticity, jeffrey_strain, step, translational_diffusion,
+ * rotational_diffusion).  particles/out: host [n][5]. */
+typedef struct {
+    double flow[3];
+    double drag;
+    double gradb[9];
+    double reorientation;
+    double b[3]; /* magnetic field already times magnetic_dipole_dipole */
+    double vort[9];
+    double shape;
+    double strain[9];
+    double dt;
+    double xi[3];
+    double diff;
+    double axis_angle, rotate_angle;
+    double box_x, box_y, box_z;
+} ss_langevin_args;
+int ss_langevin(const double *particles, uint64_t n, uint32_t mask, const ss_langevin_args *args,
+                double *out);
+
+/* Per-stage timing (CUDA events on the context stream).  enable != 0 starts
+ * recording; ss_profile_read fills ms[SS_NUM_STAGES] with the summed time of
+ * each stage since enabling and count with the number of steps. */
+#define SS_NUM_STAGES 8
+/* stage order: 0 contract, 1 fft forward, 2 k-space, 3 fft inverse, 4 field table,
+ * 5 particle update, 6 sort, 7 other */
+int ss_profile_enable(ss_ctx *ctx, int enable);
+int ss_profile_read(ss_ctx *ctx, double *ms, uint64_t *count);
+/* number of this library's kernels launched on the context so far
+ * (cuFFT's own kernels excluded) */
+int ss_launch_count(ss_ctx *ctx, uint64_t *out);
+
+/* copy the last error message of ctx (or the last context-free error when
+ * ctx is NULL) into buf, NUL terminated */
+int ss_last_error(ss_ctx *ctx, char *buf, size_t len);
+/* library version string */
+const char *ss_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

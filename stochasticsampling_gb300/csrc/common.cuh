@@ -1,0 +1,352 @@
+// common.cuh -- device-side definitions shared by the timestep kernels.
+//
+// Data layout in HBM (one simulation per context):
+//   particles   SoA doubles x[N], y[N], z[N], phi[N], theta[N]; uint32 key[N]
+//               (spatial cell of the particle, index (ix*gy+iy)*gz+iz) and
+//               uint32 id[N] (position in the caller's particle list).
+//   counts      uint32 histogram [gx][gy][gz][gphi][gtheta] (two buffers:
+//               the one this step's fields are built from, and the one the
+//               particle update fills for the next step).
+//   spectra     complex [9 stress (+3 polarisation)][ncell] forward buffer,
+//               complex [9 grad u, 3 u (+9 grad B, 3 B)][ncell] inverse buffer.
+//   table       one row of doubles per spatial cell with everything the
+//               particle update gathers (TABLE_* offsets below).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ss {
+
+constexpr double kPi = 3.14159265358979323846;  // std::f64::consts::PI
+constexpr double kTwoPi = 2.0 * kPi;             // src/consts.rs:8
+constexpr double kPiHalf = kPi / 2.0;            // src/particle.rs:24
+
+// ---- per-cell field table (doubles) ------------------------------------
+constexpr int T_U = 0;      // Re u[3]                      (mod.rs:324)
+constexpr int T_W01 = 3;    // Re W = (G - G^T)/2, W01 W02 W12 (mod.rs:302-306,325)
+constexpr int T_W02 = 4;
+constexpr int T_W12 = 5;
+constexpr int T_E00 = 6;    // Re E = (G + G^T)/2, E00 E01 E02 E11 E12 E22 (mod.rs:307,326)
+constexpr int T_E01 = 7;
+constexpr int T_E02 = 8;
+constexpr int T_E11 = 9;
+constexpr int T_E12 = 10;
+constexpr int T_E22 = 11;
+constexpr int T_DIFF = 12;  // sqrt(2 dt (Dt + volume_exclusion*density)) (mod.rs:333-346)
+constexpr int T_B = 13;     // Re B * magnetic_dipole_dipole [3]  (mod.rs:337-338)
+constexpr int T_GB = 16;    // Re grad B [3][3]                   (mod.rs:339)
+constexpr int TABLE_STRIDE = 16;      // without the dipolar solver
+constexpr int TABLE_STRIDE_MAG = 32;  // with it
+
+// Langevin modifier bits, in the chain order of src/bin/simulation/mod.rs:348-363
+enum : uint32_t {
+    M_SELF_PROPULSION = 1u << 0,
+    M_CONVECTION = 1u << 1,
+    M_MDD_FORCE = 1u << 2,
+    M_EXTERNAL_FIELD = 1u << 3,
+    M_MDD_ROTATION = 1u << 4,
+    M_JEFFREY_VORTICITY = 1u << 5,
+    M_JEFFREY_STRAIN = 1u << 6,
+    M_STEP = 1u << 7,
+    M_TRANS_DIFFUSION = 1u << 8,
+    M_ROT_DIFFUSION = 1u << 9,
+    M_ALL = (1u << 10) - 1
+};
+
+// device error flags (host reads them after a synchronising call)
+enum : uint32_t { ERR_BIN_RANGE = 1u, ERR_NONFINITE = 2u };
+
+struct DevParams {
+    int gx, gy, gz, gphi, gtheta;
+    int ncell, nang;
+    long long nbins;
+    unsigned long long n;
+    double bx, by, bz;
+    double gw[5];    // GridWidth, src/mesh/grid_width.rs:23-31
+    double igw[5];   // 1 / gw (only as a first guess for the bin index)
+    double dt, Dt, Dr;
+    double shape, drag, reorient, mdd, volex;
+    double dist_den;   // gwx*gwy*gwz*gwphi*gwtheta*N (distribution/mod.rs:183)
+    double volume;     // Lx*Ly*Lz (simulation/mod.rs:255-257)
+    double measure;    // gwphi*gwtheta  (stress.rs:83, director.rs:237)
+    double dthph;      // gwtheta*gwphi  (simulation/mod.rs:315)
+    double sigma_rot;  // sqrt(2 Dr dt)  (simulation/mod.rs:267-270)
+    double cos_half_pi, sin_half_pi;  // cos/sin of kPiHalf as evaluated on this device
+    unsigned long long seed;
+    int quasi2d;
+    uint32_t mask;     // Langevin modifiers that can change the state
+};
+
+// ---- reference arithmetic helpers -------------------------------------
+
+// modulo, src/particle.rs:26-35.  fmod(x, m) is exact; for x in (-m, 2m) it
+// equals x, x - m (exact by Sterbenz) or x (then + m), so the fast path gives
+// the identical double without the fmod loop.
+__device__ __forceinline__ double ref_modulo(double f, double m) {
+    if (f > -m && f < 2.0 * m) {
+        if (f >= m) return f - m;
+        if (f < 0.0) return f + m;
+        return f;
+    }
+    double r = fmod(f, m);
+    return (r < 0.0) ? r + fabs(m) : r;
+}
+
+// ang_pbc, src/particle.rs:37-44
+__device__ __forceinline__ void ref_ang_pbc(double &phi, double &theta) {
+    double t = ref_modulo(theta, kTwoPi);
+    if (t > kPi) {
+        phi = ref_modulo(phi + kPi, kTwoPi);
+        theta = kTwoPi - t;
+    } else {
+        phi = ref_modulo(phi, kTwoPi);
+        theta = t;
+    }
+}
+
+// floor(v / w) as usize with the `== n -> n-1` clamp of
+// Distribution::coord_to_grid (distribution/mod.rs:112-137) and
+// get_cell_index (mesh/mod.rs:49-63).  v * (1/w) is within two ulps of the
+// correctly rounded v / w; unless it lies within 2^-20 of an integer the two
+// floors agree, otherwise the exact division decides.  Indices outside
+// [0, n] (only reachable from non-finite or unwrapped input) are clamped and
+// flagged.
+__device__ __forceinline__ int ref_bin(double v, double w, double iw, int n, uint32_t &err) {
+    double q = v * iw;
+    double f = floor(q);
+    double fr = q - f;
+    if (fr < 0x1p-20 || fr > 1.0 - 0x1p-20) f = floor(v / w);
+    int i;
+    if (!(f >= 0.0)) {  // negative or NaN: Rust saturates to 0
+        if (f != f || f < 0.0) err |= ERR_BIN_RANGE;
+        i = 0;
+    } else if (f >= (double)n) {
+        if (f > (double)n) err |= ERR_BIN_RANGE;
+        i = n - 1;
+    } else {
+        i = (int)f;
+    }
+    return i;
+}
+
+// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -----------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+    constexpr uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    constexpr uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+        uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += W0;
+        k.y += W1;
+    }
+    return c;
+}
+
+// 53-bit uniform in [0, 1) from two 32-bit words
+__device__ __forceinline__ double u53(uint32_t hi, uint32_t lo) {
+    unsigned long long m = ((unsigned long long)hi << 21) ^ (unsigned long long)(lo >> 11);
+    return (double)m * 0x1p-53;
+}
+
+// Noise of particle `id` at step `t`: the RandomVector of
+// src/bin/simulation/mod.rs:272-286 (x, y, z ~ N(0,1), axis_angle = 2 pi U,
+// rotate_angle = sigma sqrt(-2 ln(1-U))), drawn from Philox with counter
+// (id, t_lo, t_hi, draw) and key = seed.  Normals by Box-Muller; the axis angle
+// is returned as its cosine and sine (sincospi(2U) = sincos(2 pi U)).
+template <bool Q2D, bool WANT_ALPHA = false>
+__device__ __forceinline__ void philox_noise(unsigned long long seed, uint32_t id, unsigned long long t,
+                                             double sigma, double xi[3], double &ca, double &sa,
+                                             double &rot, double *alpha = nullptr) {
+    uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+    uint32_t tl = (uint32_t)t, th = (uint32_t)(t >> 32);
+    uint4 r0 = philox4x32_10(make_uint4(id, tl, th, 0u), key);
+    uint4 r1 = philox4x32_10(make_uint4(id, tl, th, 1u), key);
+    double u1 = u53(r0.x, r0.y), u2 = u53(r0.z, r0.w);
+    double rad = sqrt(-2.0 * log(1.0 - u1));
+    double s, c;
+    sincospi(2.0 * u2, &s, &c);
+    xi[0] = rad * c;
+    xi[1] = rad * s;
+    if (Q2D) {
+        xi[2] = 0.0;  // overwritten position z: never read
+    } else {
+        uint4 r2 = philox4x32_10(make_uint4(id, tl, th, 2u), key);
+        double u5 = u53(r2.x, r2.y), u6 = u53(r2.z, r2.w);
+        double rad2 = sqrt(-2.0 * log(1.0 - u5));
+        xi[2] = rad2 * cospi(2.0 * u6);
+    }
+    double u3 = u53(r1.x, r1.y), u4 = u53(r1.z, r1.w);
+    sincospi(2.0 * u3, &sa, &ca);
+    rot = sigma * sqrt(-2.0 * log(1.0 - u4));
+    if (WANT_ALPHA) *alpha = kTwoPi * u3;
+}
+
+// ---- the Langevin chain ------------------------------------------------
+// Field access for the chain.  TableFields reads one row of the per-cell
+// table; MatrixFields carries full 3x3 matrices (used by ss_langevin).
+struct TableFields {
+    const double *r;
+    __device__ double flow(int k) const { return r[T_U + k]; }
+    __device__ double diff() const { return r[T_DIFF]; }
+    __device__ double b(int k) const { return r[T_B + k]; }
+    // Array2.dot(Array1) row a, then * (-1): ((0 + W[a][0]n0) + W[a][1]n1) + W[a][2]n2
+    // with W[a][a] == 0 exactly and W[b][a] == -W[a][b] exactly.
+    __device__ void vort_dot(const double n[3], double f[3]) const {
+        double w01 = r[T_W01], w02 = r[T_W02], w12 = r[T_W12];
+        f[0] = w01 * n[1] + w02 * n[2];
+        f[1] = (-w01) * n[0] + w12 * n[2];
+        f[2] = (-w02) * n[0] + (-w12) * n[1];
+    }
+    __device__ void strain_dot(const double n[3], double f[3]) const {
+        double e00 = r[T_E00], e01 = r[T_E01], e02 = r[T_E02], e11 = r[T_E11], e12 = r[T_E12],
+               e22 = r[T_E22];
+        f[0] = (e00 * n[0] + e01 * n[1]) + e02 * n[2];
+        f[1] = (e01 * n[0] + e11 * n[1]) + e12 * n[2];
+        f[2] = (e02 * n[0] + e12 * n[1]) + e22 * n[2];
+    }
+    __device__ void gradb_dot(const double n[3], double f[3]) const {
+        const double *g = r + T_GB;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) f[a] = (g[3 * a] * n[0] + g[3 * a + 1] * n[1]) + g[3 * a + 2] * n[2];
+    }
+};
+
+struct MatrixFields {
+    const double *flow_, *gradb_, *b_, *vort_, *strain_;
+    double diff_;
+    __device__ double flow(int k) const { return flow_[k]; }
+    __device__ double diff() const { return diff_; }
+    __device__ double b(int k) const { return b_[k]; }
+    static __device__ void rowdot(const double *m, const double n[3], double f[3]) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) f[a] = (m[3 * a] * n[0] + m[3 * a + 1] * n[1]) + m[3 * a + 2] * n[2];
+    }
+    __device__ void vort_dot(const double n[3], double f[3]) const { rowdot(vort_, n, f); }
+    __device__ void strain_dot(const double n[3], double f[3]) const { rowdot(strain_, n, f); }
+    __device__ void gradb_dot(const double n[3], double f[3]) const { rowdot(gradb_, n, f); }
+};
+
+// One particle through LangevinBuilder::new -> modifiers -> step -> noise ->
+// finalize (src/integrators/langevin_builder/mod.rs:25-125,
+// modifiers.rs:39-231, particle.rs:106-121,219-222), then the quasi2d override
+// (simulation/mod.rs:365-368).  Terms whose coefficient is exactly zero are
+// masked off by the caller: they add an exact +-0 in the reference.
+//   cth/sth: cos/sin of theta when the caller knows them (quasi2d), else pass
+//   have_theta = false.  (ca, sa): cos/sin of the rotation axis angle.
+template <bool Q2D, class F>
+__device__ __forceinline__ void langevin(double &x, double &y, double &z, double &phi, double &theta,
+                                         const F &fld, const double xi[3], double ca, double sa, double rot,
+                                         uint32_t mask, double dt, double reorient, double shape, double drag,
+                                         double bx, double by, double bz, bool have_theta, double cth,
+                                         double sth) {
+    double sp, cp, ct, st;
+    sincos(phi, &sp, &cp);
+    if (have_theta) {
+        ct = cth;
+        st = sth;
+    } else {
+        sincos(theta, &st, &ct);
+    }
+    // CosSinOrientation::to_orientation_vector, particle.rs:165-172
+    double n[3] = {st * cp, st * sp, ct};
+    double dp[3] = {0.0, 0.0, 0.0}, dn[3] = {0.0, 0.0, 0.0};
+
+    if (mask & M_SELF_PROPULSION) {  // modifiers.rs:39-46
+        dp[0] = n[0]; dp[1] = n[1]; dp[2] = n[2];
+    }
+    if (mask & M_CONVECTION) {  // modifiers.rs:49-56
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dp[k] = dp[k] + fld.flow(k);
+    }
+    if (mask & M_MDD_FORCE) {  // modifiers.rs:59-70
+        double f[3];
+        fld.gradb_dot(n, f);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dp[k] = dp[k] + f[k] * drag;
+    }
+    if (mask & M_EXTERNAL_FIELD) {  // modifiers.rs:103-119 (field along y)
+        double b[3] = {0.0, reorient, 0.0};
+        double d = (n[0] * b[0] + n[1] * b[1]) + n[2] * b[2];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dn[k] = dn[k] + (b[k] - n[k] * d);
+    }
+    if (mask & M_MDD_ROTATION) {  // modifiers.rs:172-187
+        double b[3] = {fld.b(0), fld.b(1), fld.b(2)};
+        double d = (n[0] * b[0] + n[1] * b[1]) + n[2] * b[2];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dn[k] = dn[k] + (b[k] - n[k] * d);
+    }
+    if (mask & M_JEFFREY_VORTICITY) {  // modifiers.rs:123-143
+        double f[3];
+        fld.vort_dot(n, f);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dn[k] = dn[k] + (-f[k]);
+    }
+    if (mask & M_JEFFREY_STRAIN) {  // modifiers.rs:147-170
+        double f[3];
+        fld.strain_dot(n, f);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) f[k] = f[k] * shape;
+        double fn = (f[0] * n[0] + f[1] * n[1]) + f[2] * n[2];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dn[k] = dn[k] + (f[k] - n[k] * fn);
+    }
+    if (mask & M_STEP) {  // mod.rs:114-119
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            dp[k] = dp[k] * dt;
+            dn[k] = dn[k] * dt;
+        }
+    }
+    if (mask & M_TRANS_DIFFUSION) {  // modifiers.rs:86-99
+        double diff = fld.diff();
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dp[k] = dp[k] + xi[k] * diff;
+    }
+    if (mask & M_ROT_DIFFUSION) {  // modifiers.rs:199-231, quaternion 0.3.1
+        double ax0 = (cp * ct) * sa - ca * sp;
+        double ax1 = ca * cp + (ct * sa) * sp;
+        double ax2 = (-sa) * st;
+        double sh, ch;
+        sincos(rot / 2.0, &sh, &ch);  // axis_angle: half angle
+        double q0 = ch, q1 = ax0 * sh, q2 = ax1 * sh, q3 = ax2 * sh;
+        // t = q * (0, n):  (q0*0 - q.n,  (n*q0 + q*0) + q x n)
+        double t0 = q0 * 0.0 - ((q1 * n[0] + q2 * n[1]) + q3 * n[2]);
+        double t1 = (n[0] * q0 + q1 * 0.0) + (q2 * n[2] - q3 * n[1]);
+        double t2 = (n[1] * q0 + q2 * 0.0) + (q3 * n[0] - q1 * n[2]);
+        double t3 = (n[2] * q0 + q3 * 0.0) + (q1 * n[1] - q2 * n[0]);
+        // r = t * conj(q), conj(q) = (q0, -q):  ((-q)*t0 + t*q0) + t x (-q)
+        double c1 = -q1, c2 = -q2, c3 = -q3;
+        double r1 = (c1 * t0 + t1 * q0) + (t2 * c3 - t3 * c2);
+        double r2 = (c2 * t0 + t2 * q0) + (t3 * c1 - t1 * c3);
+        double r3 = (c3 * t0 + t3 * q0) + (t1 * c2 - t2 * c1);
+        dn[0] = dn[0] + (r1 - n[0]);
+        dn[1] = dn[1] + (r2 - n[1]);
+        dn[2] = dn[2] + (r3 - n[2]);
+    }
+    // finalize: Particle::from(old + delta) then pbc (mod.rs:121-125)
+    double px = x + dp[0], py = y + dp[1], pz = z + dp[2];
+    double v0 = n[0] + dn[0], v1 = n[1] + dn[1], v2 = n[2] + dn[2];
+    double nphi = atan2(v1, v0);  // Orientation::from_vector, particle.rs:106-121
+    x = ref_modulo(px, bx);
+    y = ref_modulo(py, by);
+    if (Q2D) {
+        // theta = pi/2 - atan2(v2, rxy) lies in [0, pi] (rxy >= 0), so
+        // ang_pbc only wraps phi; z and theta are overwritten (mod.rs:365-368).
+        phi = ref_modulo(nphi, kTwoPi);
+        z = 0.0;
+        theta = kPiHalf;
+    } else {
+        double rxy = sqrt(v0 * v0 + v1 * v1);
+        double nth = kPiHalf - atan2(v2, rxy);
+        z = ref_modulo(pz, bz);
+        ref_ang_pbc(nphi, nth);
+        phi = nphi;
+        theta = nth;
+    }
+}
+
+}  // namespace ss

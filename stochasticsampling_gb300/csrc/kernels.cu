@@ -1,0 +1,545 @@
+// kernels.cu -- the timestep kernels (sm_103a) and their launch wrappers.
+//
+// Step pipeline (one simulation, all on one stream):
+//   contract  counts -> stress sigma_ij, polarisation P_c (complex, im = 0),
+//             per-cell diffusion length, particles per cell
+//   [sort]    counting sort of the particle arrays by spatial cell
+//   cuFFT     forward Z2Z of 9 (+3) components
+//   kspace    Oseen projection + screening, dipolar projection, gradients
+//   cuFFT     inverse Z2Z of 12 (+12) components
+//   table     per-cell row: Re u, W, E, B*mdd, grad B
+//   update    gather row by cell, Langevin step, wrap, bin into next histogram
+#include "kernels.cuh"
+
+#include <cstdio>
+
+namespace ss {
+
+// ------------------------------------------------------------------------
+// small helpers
+// ------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ uint32_t warp_sum_u(uint32_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// k value of FFT index i on an axis of n cells and box length L:
+// get_k_sampling (src/mesh/fft_helper.rs:26-51): index i < ceil(n/2) -> i,
+// else i - n (the Nyquist mode of an even n is negative), times 2 pi / L.
+__device__ __forceinline__ double kval(int i, int n, double step) {
+    int b = (n % 2 == 0) ? n / 2 : n / 2 + 1;
+    return (double)(i < b ? i : i - n) * step;
+}
+
+// ------------------------------------------------------------------------
+// particle ingest / egest / binning
+// ------------------------------------------------------------------------
+
+// Particle::new (src/particle.rs:186-201): modulo on positions and ang_pbc on
+// angles, then pbc once more; AoS [n][5] -> SoA.
+__global__ void k_ingest(const double *__restrict__ aos, unsigned long long n, DevParams P, double *__restrict__ x,
+                         double *__restrict__ y, double *__restrict__ z, double *__restrict__ phi,
+                         double *__restrict__ theta, uint32_t *__restrict__ id) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *p = aos + 5 * i;
+    double px = ref_modulo(p[0], P.bx), py = ref_modulo(p[1], P.by), pz = ref_modulo(p[2], P.bz);
+    double ph = p[3], th = p[4];
+    ref_ang_pbc(ph, th);
+    px = ref_modulo(px, P.bx);
+    py = ref_modulo(py, P.by);
+    pz = ref_modulo(pz, P.bz);
+    ref_ang_pbc(ph, th);
+    x[i] = px; y[i] = py; z[i] = pz; phi[i] = ph; theta[i] = th;
+    id[i] = (uint32_t)i;
+}
+
+// SoA slot i -> AoS row id[i] (the caller's order)
+__global__ void k_egest(unsigned long long n, const double *__restrict__ x, const double *__restrict__ y,
+                        const double *__restrict__ z, const double *__restrict__ phi,
+                        const double *__restrict__ theta, const uint32_t *__restrict__ id,
+                        double *__restrict__ aos) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double *p = aos + 5 * (unsigned long long)id[i];
+    p[0] = x[i]; p[1] = y[i]; p[2] = z[i]; p[3] = phi[i]; p[4] = theta[i];
+}
+
+__device__ __forceinline__ void bin_particle(const DevParams &P, double x, double y, double z, double phi,
+                                             double theta, uint32_t &cell, unsigned long long &bin,
+                                             uint32_t &err) {
+    int ix = ref_bin(x, P.gw[0], P.igw[0], P.gx, err);
+    int iy = ref_bin(y, P.gw[1], P.igw[1], P.gy, err);
+    int iz = ref_bin(z, P.gw[2], P.igw[2], P.gz, err);
+    int ip = ref_bin(phi, P.gw[3], P.igw[3], P.gphi, err);
+    int it = ref_bin(theta, P.gw[4], P.igw[4], P.gtheta, err);
+    cell = (uint32_t)((ix * P.gy + iy) * P.gz + iz);
+    bin = (unsigned long long)cell * (unsigned long long)P.nang + (unsigned long long)(ip * P.gtheta + it);
+}
+
+// Distribution::histogram_from (src/distribution/mod.rs:146-160) with
+// integer counts; also records each particle's spatial cell.
+__global__ void k_bin(unsigned long long n, DevParams P, const double *__restrict__ x,
+                      const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ phi,
+                      const double *__restrict__ theta, uint32_t *__restrict__ key, uint32_t *__restrict__ counts,
+                      uint32_t *__restrict__ errflag) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t err = 0, cell;
+    unsigned long long bin;
+    bin_particle(P, x[i], y[i], z[i], phi[i], theta[i], cell, bin, err);
+    atomicAdd(counts + bin, 1u);
+    key[i] = cell;
+    if (err) atomicOr(errflag, err);
+}
+
+// counts -> normalised distribution, (c / D) * V exactly as
+// sample_from + the box-volume rescale (distribution/mod.rs:183,
+// simulation/mod.rs:255-257)
+__global__ void k_counts_to_dist(const uint32_t *__restrict__ counts, long long nbins, DevParams P,
+                                 double *__restrict__ dist) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nbins) return;
+    dist[i] = ((double)counts[i] / P.dist_den) * P.volume;
+}
+
+// ------------------------------------------------------------------------
+// angular contraction: average_stress (src/flowfield/stress.rs:60-96),
+// DirectorField::from_distribution (src/polarization/director.rs:36-61) and
+// the density of src/bin/simulation/mod.rs:312-316.  One warp per cell,
+// lanes over angle bins.
+// kern rows: 0..8 stress kernel K_ij, 9..11 orientation kernel n_c.
+// ------------------------------------------------------------------------
+template <bool STRESS, bool MAG, bool FROM_DIST>
+__global__ void __launch_bounds__(256) k_contract(const uint32_t *__restrict__ counts,
+                                                  const double *__restrict__ dist,
+                                                  const double *__restrict__ lut, int lut_n,
+                                                  const double *__restrict__ kern, DevParams P,
+                                                  double2 *__restrict__ fwd, double *__restrict__ table,
+                                                  int tstride, uint32_t *__restrict__ cellcount) {
+    int cell = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+    int lane = threadIdx.x & 31;
+    if (cell >= P.ncell) return;
+    const int na = P.nang;
+    double acc[13];
+#pragma unroll
+    for (int j = 0; j < 13; ++j) acc[j] = 0.0;
+    uint32_t csum = 0;
+    for (int a = lane; a < na; a += 32) {
+        double f;
+        if (FROM_DIST) {
+            f = dist[(long long)cell * na + a];
+        } else {
+            uint32_t c = counts[(long long)cell * na + a];
+            csum += c;
+            f = ((int)c < lut_n) ? __ldg(lut + c) : ((double)c / P.dist_den) * P.volume;
+        }
+        if (STRESS) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) acc[j] = fma(__ldg(kern + j * na + a), f, acc[j]);
+        }
+        if (MAG) {
+#pragma unroll
+            for (int j = 9; j < 12; ++j) acc[j] = fma(__ldg(kern + j * na + a), f, acc[j]);
+        }
+        acc[12] += f;
+    }
+#pragma unroll
+    for (int j = 0; j < 13; ++j) {
+        if ((j < 9 && STRESS) || (j >= 9 && j < 12 && MAG) || j == 12) acc[j] = warp_sum(acc[j]);
+    }
+    if (!FROM_DIST) csum = warp_sum_u(csum);
+    if (lane == 0) {
+        const int nc = P.ncell;
+        if (STRESS) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = make_double2(acc[j] * P.measure, 0.0);
+        }
+        if (MAG) {
+#pragma unroll
+            for (int j = 0; j < 3; ++j) fwd[(long long)(9 + j) * nc + cell] = make_double2(acc[9 + j] * P.measure, 0.0);
+        }
+        double dens = acc[12] * P.dthph;
+        double volex = P.volex * dens;
+        table[(long long)cell * tstride + T_DIFF] = sqrt(2.0 * P.dt * (P.Dt + volex));
+        if (!FROM_DIST) cellcount[cell] = csum;
+    }
+}
+
+// ------------------------------------------------------------------------
+// k space: SpectralSolver::fft_mean_flow_field (spectral_solver.rs:133-189),
+// MagneticSolver::fft_mean_magnetic_field (magnetic_solver.rs:71-95) and both
+// update_gradient (spectral_solver.rs:192-229, magnetic_solver.rs:98-135).
+// fwd: [0..9) sigma_k, [9..12) P_k.  inv: [0..9) G_k = i k_a u_b, [9..12) u_k,
+// [12..21) grad B_k, [21..24) B_k.  Complex products with k (imaginary part
+// zero) reduce exactly to real scalings.
+// ------------------------------------------------------------------------
+template <bool FLOW, bool MAG>
+__global__ void k_kspace(const double2 *__restrict__ fwd, double2 *__restrict__ inv, DevParams P,
+                         double screening, double stepx, double stepy, double stepz) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nc = P.ncell;
+    if (c >= nc) return;
+    int iz = c % P.gz;
+    int iy = (c / P.gz) % P.gy;
+    int ix = c / (P.gz * P.gy);
+    double k[3] = {kval(ix, P.gx, stepx), kval(iy, P.gy, stepy), kval(iz, P.gz, stepz)};
+    // |k|^2 = ((0 + kx^2) + ky^2) + kz^2 (fft_helper.rs:80-82)
+    double s = (k[0] * k[0] + k[1] * k[1]);
+    s = s + k[2] * k[2];
+    // 1/|k|^2 via num-complex's real/complex division: s / (s*s); 1/|k| for k-hat;
+    // both zero at k = 0 (fft_helper.rs:84-85, 96-97)
+    double ik2 = (c == 0) ? 0.0 : s / (s * s);
+    double inrm = (c == 0) ? 0.0 : 1.0 / sqrt(s);
+    double kn[3] = {k[0] * inrm, k[1] * inrm, k[2] * inrm};
+    const double norm = (double)nc;
+    if (FLOW) {
+        double2 sg[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            double2 a0 = fwd[(long long)(3 * r + 0) * nc + c];
+            double2 a1 = fwd[(long long)(3 * r + 1) * nc + c];
+            double2 a2 = fwd[(long long)(3 * r + 2) * nc + c];
+            sg[r].x = (a0.x * k[0] + a1.x * k[1]) + a2.x * k[2];
+            sg[r].y = (a0.y * k[0] + a1.y * k[1]) + a2.y * k[2];
+        }
+        double ksr = (kn[0] * sg[0].x + kn[1] * sg[1].x) + kn[2] * sg[2].x;
+        double ksi = (kn[0] * sg[0].y + kn[1] * sg[1].y) + kn[2] * sg[2].y;
+        double fac = (ik2 + screening) / norm;
+        double2 u[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            double tr = (sg[r].x - kn[r] * ksr) * fac;
+            double ti = (sg[r].y - kn[r] * ksi) * fac;
+            u[r] = make_double2(-ti, tr);  // times i
+            inv[(long long)(9 + r) * nc + c] = u[r];
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+                inv[(long long)(3 * a + b) * nc + c] = make_double2(-(k[a] * u[b].y), k[a] * u[b].x);
+    }
+    if (MAG) {
+        double2 p[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) p[r] = fwd[(long long)(9 + r) * nc + c];
+        double dr = (kn[0] * p[0].x + kn[1] * p[1].x) + kn[2] * p[2].x;
+        double di = (kn[0] * p[0].y + kn[1] * p[1].y) + kn[2] * p[2].y;
+        double2 b[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            b[r] = make_double2((p[r].x - kn[r] * dr) / norm, (p[r].y - kn[r] * di) / norm);
+            inv[(long long)(21 + r) * nc + c] = b[r];
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int bb = 0; bb < 3; ++bb)
+                inv[(long long)(12 + 3 * a + bb) * nc + c] = make_double2(-(k[a] * b[bb].y), k[a] * b[bb].x);
+    }
+}
+
+// ------------------------------------------------------------------------
+// per-cell table: W = (G - G^T) * 0.5, E = (G + G^T) * 0.5 on real parts
+// (simulation/mod.rs:302-308), Re u, Re B * mdd, Re grad B (:323-339)
+// ------------------------------------------------------------------------
+template <bool FLOW, bool MAG>
+__global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__restrict__ table, int tstride) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nc = P.ncell;
+    if (c >= nc) return;
+    double *row = table + (long long)c * tstride;
+    if (FLOW) {
+        double g[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) g[j] = inv[(long long)j * nc + c].x;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) row[T_U + r] = inv[(long long)(9 + r) * nc + c].x;
+        row[T_W01] = (g[1] - g[3]) * 0.5;
+        row[T_W02] = (g[2] - g[6]) * 0.5;
+        row[T_W12] = (g[5] - g[7]) * 0.5;
+        row[T_E00] = (g[0] + g[0]) * 0.5;
+        row[T_E01] = (g[1] + g[3]) * 0.5;
+        row[T_E02] = (g[2] + g[6]) * 0.5;
+        row[T_E11] = (g[4] + g[4]) * 0.5;
+        row[T_E12] = (g[5] + g[7]) * 0.5;
+        row[T_E22] = (g[8] + g[8]) * 0.5;
+    }
+    if (MAG) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) row[T_B + r] = inv[(long long)(21 + r) * nc + c].x * P.mdd;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) row[T_GB + j] = inv[(long long)(12 + j) * nc + c].x;
+    }
+}
+
+// ------------------------------------------------------------------------
+// particle update: the loop of src/bin/simulation/mod.rs:318-369 fused with
+// the next step's binning (histogram_from) so each step reads and writes the
+// particle state once.  NOISE: 0 = Philox on device, 1 = host array [N][5]
+// indexed by the caller's particle order.
+// ------------------------------------------------------------------------
+template <bool Q2D, bool MAG, int NOISE>
+__global__ void __launch_bounds__(256) k_update(DevParams P, double *__restrict__ x, double *__restrict__ y,
+                                                double *__restrict__ z, double *__restrict__ phi,
+                                                double *__restrict__ theta, uint32_t *__restrict__ key,
+                                                const uint32_t *__restrict__ id, const double *__restrict__ table,
+                                                const double *__restrict__ noise,
+                                                const unsigned long long *__restrict__ d_step,
+                                                uint32_t *__restrict__ counts_next, uint32_t *__restrict__ errflag) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const int ts = MAG ? TABLE_STRIDE_MAG : TABLE_STRIDE;
+    uint32_t cell = key[i];
+    uint32_t pid = id[i];
+    double px = x[i], py = y[i], pz = z[i], pph = phi[i], pth = theta[i];
+    TableFields F{table + (long long)cell * ts};
+    double xi[3], ca, sa, rot;
+    if (NOISE == 0) {
+        philox_noise<Q2D>(P.seed, pid, *d_step, P.sigma_rot, xi, ca, sa, rot);
+    } else {
+        const double *r = noise + 5ull * pid;
+        xi[0] = r[0]; xi[1] = r[1]; xi[2] = r[2];
+        sincos(r[3], &sa, &ca);
+        rot = r[4];
+    }
+    bool have_theta = Q2D && (pth == kPiHalf);
+    langevin<Q2D>(px, py, pz, pph, pth, F, xi, ca, sa, rot, P.mask, P.dt, P.reorient, P.shape, P.drag, P.bx,
+                  P.by, P.bz, have_theta, P.cos_half_pi, P.sin_half_pi);
+    uint32_t err = 0, ncell;
+    unsigned long long bin;
+    bin_particle(P, px, py, pz, pph, pth, ncell, bin, err);
+    atomicAdd(counts_next + bin, 1u);
+    key[i] = ncell;
+    x[i] = px; y[i] = py; z[i] = pz; phi[i] = pph; theta[i] = pth;
+    if (err) atomicOr(errflag, err);
+}
+
+__global__ void k_step_inc(unsigned long long *d_step) { *d_step += 1ull; }
+
+// the Philox noise of step t for every particle, as RandomVector rows in the
+// caller's order
+template <bool Q2D>
+__global__ void k_noise(DevParams P, unsigned long long t, double *__restrict__ out) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    double xi[3], ca, sa, rot, alpha;
+    philox_noise<Q2D, true>(P.seed, (uint32_t)i, t, P.sigma_rot, xi, ca, sa, rot, &alpha);
+    double *r = out + 5 * i;
+    r[0] = xi[0]; r[1] = xi[1]; r[2] = xi[2]; r[3] = alpha; r[4] = rot;
+}
+
+// ------------------------------------------------------------------------
+// counting sort by cell
+// ------------------------------------------------------------------------
+// exclusive scan of cellcount into cursor (one block)
+__global__ void __launch_bounds__(1024) k_scan(const uint32_t *__restrict__ cnt, int n, uint32_t *__restrict__ out) {
+    __shared__ uint32_t part[1024];
+    int t = threadIdx.x;
+    int per = (n + 1023) / 1024;
+    int lo = t * per, hi = min(n, lo + per);
+    uint32_t s = 0;
+    for (int i = lo; i < hi; ++i) s += cnt[i];
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        uint32_t v = (t >= o) ? part[t - o] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[t] - s;
+    for (int i = lo; i < hi; ++i) {
+        uint32_t c = cnt[i];
+        out[i] = run;
+        run += c;
+    }
+}
+
+// scatter slot i to cursor[key] + rank; ranks handed out with one atomic per
+// group of lanes sharing a cell (warp-aggregated)
+__global__ void __launch_bounds__(256) k_scatter(unsigned long long n, const double *__restrict__ x,
+                                                 const double *__restrict__ y, const double *__restrict__ z,
+                                                 const double *__restrict__ phi, const double *__restrict__ theta,
+                                                 const uint32_t *__restrict__ key, const uint32_t *__restrict__ id,
+                                                 double *__restrict__ x2, double *__restrict__ y2,
+                                                 double *__restrict__ z2, double *__restrict__ phi2,
+                                                 double *__restrict__ theta2, uint32_t *__restrict__ key2,
+                                                 uint32_t *__restrict__ id2, uint32_t *__restrict__ cursor) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int lane = threadIdx.x & 31;
+    uint32_t k = key[i];
+    unsigned act = __activemask();
+    unsigned same = __match_any_sync(act, k);
+    int leader = __ffs(same) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(cursor + k, (uint32_t)__popc(same));
+    base = __shfl_sync(same, base, leader);
+    uint32_t dst = base + (uint32_t)__popc(same & ((1u << lane) - 1u));
+    x2[dst] = x[i]; y2[dst] = y[i]; z2[dst] = z[i]; phi2[dst] = phi[i]; theta2[dst] = theta[i];
+    key2[dst] = k; id2[dst] = id[i];
+}
+
+// ------------------------------------------------------------------------
+// misc
+// ------------------------------------------------------------------------
+__global__ void k_zero_u32(uint32_t *__restrict__ p, long long n) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) p[i] = 0u;
+}
+
+__global__ void k_real_parts(const double2 *__restrict__ src, long long count, double *__restrict__ dst) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    dst[i] = src[i].x;
+}
+
+__global__ void k_half_pi(double *out) {
+    double s, c;
+    sincos(kPiHalf, &s, &c);
+    out[0] = c;
+    out[1] = s;
+}
+
+// the Langevin chain on independent particles with shared arguments
+template <bool Q2D>
+__global__ void k_langevin_args(const double *__restrict__ in, unsigned long long n, uint32_t mask,
+                                const double *__restrict__ a /* ss_langevin_args as doubles */,
+                                double *__restrict__ out) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    // field offsets inside ss_langevin_args (all doubles)
+    const double *flow = a + 0, *gradb = a + 4, *b = a + 14, *vort = a + 17, *strain = a + 27;
+    double drag = a[3], reorient = a[13], shape = a[26], dt = a[36], diff = a[40];
+    const double *xi = a + 37;
+    double alpha = a[41], rot = a[42], bx = a[43], by = a[44], bz = a[45];
+    MatrixFields F{flow, gradb, b, vort, strain, diff};
+    double px = in[5 * i], py = in[5 * i + 1], pz = in[5 * i + 2], pph = in[5 * i + 3], pth = in[5 * i + 4];
+    double sa, ca, xv[3] = {xi[0], xi[1], xi[2]};
+    sincos(alpha, &sa, &ca);
+    langevin<false>(px, py, pz, pph, pth, F, xv, ca, sa, rot, mask, dt, reorient, shape, drag, bx, by, bz, false,
+                    0.0, 0.0);
+    out[5 * i] = px; out[5 * i + 1] = py; out[5 * i + 2] = pz; out[5 * i + 3] = pph; out[5 * i + 4] = pth;
+}
+
+// ========================================================================
+// launch wrappers
+// ========================================================================
+static inline unsigned nblocks(unsigned long long n, unsigned bs) { return (unsigned)((n + bs - 1) / bs); }
+
+void launch_ingest(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P, double *const xs[5],
+                   uint32_t *id) {
+    if (!n) return;
+    k_ingest<<<nblocks(n, 256), 256, 0, s>>>(aos, n, P, xs[0], xs[1], xs[2], xs[3], xs[4], id);
+}
+
+void launch_egest(cudaStream_t s, unsigned long long n, double *const xs[5], const uint32_t *id, double *aos) {
+    if (!n) return;
+    k_egest<<<nblocks(n, 256), 256, 0, s>>>(n, xs[0], xs[1], xs[2], xs[3], xs[4], id, aos);
+}
+
+void launch_bin(cudaStream_t s, unsigned long long n, const DevParams &P, double *const xs[5], uint32_t *key,
+                uint32_t *counts, uint32_t *err) {
+    if (!n) return;
+    k_bin<<<nblocks(n, 256), 256, 0, s>>>(n, P, xs[0], xs[1], xs[2], xs[3], xs[4], key, counts, err);
+}
+
+void launch_counts_to_dist(cudaStream_t s, const uint32_t *counts, const DevParams &P, double *dist) {
+    k_counts_to_dist<<<nblocks(P.nbins, 256), 256, 0, s>>>(counts, P.nbins, P, dist);
+}
+
+void launch_contract(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const double *dist,
+                     const double *lut, int lut_n, const double *kern, const DevParams &P, double2 *fwd,
+                     double *table, int tstride, uint32_t *cellcount) {
+    unsigned blocks = nblocks((unsigned long long)P.ncell * 32ull, 256);
+#define SS_CONTRACT(S, M, D) \
+    k_contract<S, M, D><<<blocks, 256, 0, s>>>(counts, dist, lut, lut_n, kern, P, fwd, table, tstride, cellcount)
+    bool fd = dist != nullptr;
+    if (stress && mag) { if (fd) SS_CONTRACT(true, true, true); else SS_CONTRACT(true, true, false); }
+    else if (stress) { if (fd) SS_CONTRACT(true, false, true); else SS_CONTRACT(true, false, false); }
+    else { if (fd) SS_CONTRACT(false, true, true); else SS_CONTRACT(false, true, false); }
+#undef SS_CONTRACT
+}
+
+void launch_kspace(cudaStream_t s, bool flow, bool mag, const double2 *fwd, double2 *inv, const DevParams &P,
+                   double screening) {
+    double sx = kTwoPi / P.bx, sy = kTwoPi / P.by, sz = kTwoPi / P.bz;
+    unsigned b = nblocks(P.ncell, 128);
+    if (flow && mag) k_kspace<true, true><<<b, 128, 0, s>>>(fwd, inv, P, screening, sx, sy, sz);
+    else if (flow) k_kspace<true, false><<<b, 128, 0, s>>>(fwd, inv, P, screening, sx, sy, sz);
+    else k_kspace<false, true><<<b, 128, 0, s>>>(fwd, inv, P, screening, sx, sy, sz);
+}
+
+void launch_table(cudaStream_t s, bool flow, bool mag, const double2 *inv, const DevParams &P, double *table,
+                  int tstride) {
+    unsigned b = nblocks(P.ncell, 128);
+    if (flow && mag) k_table<true, true><<<b, 128, 0, s>>>(inv, P, table, tstride);
+    else if (flow) k_table<true, false><<<b, 128, 0, s>>>(inv, P, table, tstride);
+    else k_table<false, true><<<b, 128, 0, s>>>(inv, P, table, tstride);
+}
+
+void launch_update(cudaStream_t s, bool q2d, bool mag, bool host_noise, const DevParams &P, double *const xs[5],
+                   uint32_t *key, const uint32_t *id, const double *table, const double *noise,
+                   const unsigned long long *d_step, uint32_t *counts_next, uint32_t *err) {
+    if (!P.n) return;
+    unsigned b = nblocks(P.n, 256);
+#define SS_UPD(Q, M, N) \
+    k_update<Q, M, N><<<b, 256, 0, s>>>(P, xs[0], xs[1], xs[2], xs[3], xs[4], key, id, table, noise, d_step, \
+                                        counts_next, err)
+    if (q2d) {
+        if (mag) { if (host_noise) SS_UPD(true, true, 1); else SS_UPD(true, true, 0); }
+        else { if (host_noise) SS_UPD(true, false, 1); else SS_UPD(true, false, 0); }
+    } else {
+        if (mag) { if (host_noise) SS_UPD(false, true, 1); else SS_UPD(false, true, 0); }
+        else { if (host_noise) SS_UPD(false, false, 1); else SS_UPD(false, false, 0); }
+    }
+#undef SS_UPD
+}
+
+void launch_step_inc(cudaStream_t s, unsigned long long *d_step) { k_step_inc<<<1, 1, 0, s>>>(d_step); }
+
+void launch_noise(cudaStream_t s, bool q2d, const DevParams &P, unsigned long long t, double *out) {
+    if (!P.n) return;
+    if (q2d) k_noise<true><<<nblocks(P.n, 256), 256, 0, s>>>(P, t, out);
+    else k_noise<false><<<nblocks(P.n, 256), 256, 0, s>>>(P, t, out);
+}
+
+void launch_scan(cudaStream_t s, const uint32_t *cnt, int n, uint32_t *out) { k_scan<<<1, 1024, 0, s>>>(cnt, n, out); }
+
+void launch_scatter(cudaStream_t s, unsigned long long n, double *const src[5], const uint32_t *key,
+                    const uint32_t *id, double *const dst[5], uint32_t *key2, uint32_t *id2, uint32_t *cursor) {
+    if (!n) return;
+    k_scatter<<<nblocks(n, 256), 256, 0, s>>>(n, src[0], src[1], src[2], src[3], src[4], key, id, dst[0], dst[1],
+                                              dst[2], dst[3], dst[4], key2, id2, cursor);
+}
+
+void launch_zero_u32(cudaStream_t s, uint32_t *p, long long n) {
+    if (n <= 0) return;
+    long long b = (n + 255) / 256;
+    if (b > 152 * 64) b = 152 * 64;
+    k_zero_u32<<<(unsigned)b, 256, 0, s>>>(p, n);
+}
+
+void launch_real_parts(cudaStream_t s, const double2 *src, long long count, double *dst) {
+    if (count <= 0) return;
+    k_real_parts<<<nblocks(count, 256), 256, 0, s>>>(src, count, dst);
+}
+
+void launch_half_pi(cudaStream_t s, double *out) { k_half_pi<<<1, 1, 0, s>>>(out); }
+
+void launch_langevin_args(cudaStream_t s, const double *in, unsigned long long n, uint32_t mask, const double *args,
+                          double *out) {
+    if (!n) return;
+    k_langevin_args<false><<<nblocks(n, 128), 128, 0, s>>>(in, n, mask, args, out);
+}
+
+}  // namespace ss

@@ -1,0 +1,37 @@
+// kernels.cuh -- launch wrappers of the timestep kernels (kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace ss {
+
+void launch_ingest(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P, double *const xs[5],
+                   uint32_t *id);
+void launch_egest(cudaStream_t s, unsigned long long n, double *const xs[5], const uint32_t *id, double *aos);
+void launch_bin(cudaStream_t s, unsigned long long n, const DevParams &P, double *const xs[5], uint32_t *key,
+                uint32_t *counts, uint32_t *err);
+void launch_counts_to_dist(cudaStream_t s, const uint32_t *counts, const DevParams &P, double *dist);
+void launch_contract(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const double *dist,
+                     const double *lut, int lut_n, const double *kern, const DevParams &P, double2 *fwd,
+                     double *table, int tstride, uint32_t *cellcount);
+void launch_kspace(cudaStream_t s, bool flow, bool mag, const double2 *fwd, double2 *inv, const DevParams &P,
+                   double screening);
+void launch_table(cudaStream_t s, bool flow, bool mag, const double2 *inv, const DevParams &P, double *table,
+                  int tstride);
+void launch_update(cudaStream_t s, bool q2d, bool mag, bool host_noise, const DevParams &P, double *const xs[5],
+                   uint32_t *key, const uint32_t *id, const double *table, const double *noise,
+                   const unsigned long long *d_step, uint32_t *counts_next, uint32_t *err);
+void launch_step_inc(cudaStream_t s, unsigned long long *d_step);
+void launch_noise(cudaStream_t s, bool q2d, const DevParams &P, unsigned long long t, double *out);
+void launch_scan(cudaStream_t s, const uint32_t *cnt, int n, uint32_t *out);
+void launch_scatter(cudaStream_t s, unsigned long long n, double *const src[5], const uint32_t *key,
+                    const uint32_t *id, double *const dst[5], uint32_t *key2, uint32_t *id2, uint32_t *cursor);
+void launch_zero_u32(cudaStream_t s, uint32_t *p, long long n);
+void launch_real_parts(cudaStream_t s, const double2 *src, long long count, double *dst);
+void launch_half_pi(cudaStream_t s, double *out);
+void launch_langevin_args(cudaStream_t s, const double *in, unsigned long long n, uint32_t mask, const double *args,
+                          double *out);
+
+}  // namespace ss

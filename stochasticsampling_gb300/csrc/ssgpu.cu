@@ -1,0 +1,823 @@
+// ssgpu.cu -- the simulation context and the C ABI declared in include/ssgpu.h.
+//
+// ss_ctx mirrors the reference's Simulation (src/bin/simulation/mod.rs:60-77):
+// it owns the particle state, the distribution (as an integer histogram), the
+// spectral solvers (cuFFT plans + k-space kernel) and the per-cell field table,
+// all resident in HBM.  Host code here only validates, allocates, launches and
+// copies; every arithmetic stage runs in kernels.cu.
+#include <cufft.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/ssgpu.h"
+#include "kernels.cuh"
+
+using namespace ss;
+
+namespace {
+
+constexpr int kLutN = 4096;
+
+thread_local std::string g_last_error;
+
+struct Timing {
+    bool on = false;
+    cudaEvent_t ev[SS_NUM_STAGES + 1] = {};
+    double ms[SS_NUM_STAGES] = {};
+    uint64_t steps = 0;
+};
+
+}  // namespace
+
+struct ss_ctx {
+    ss_grid grid{};
+    ss_box box{};
+    ss_params prm{};
+    uint32_t flags = 0;
+    DevParams P{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    bool q2d = false, mag_step = false, sort = true, use_graph = true;
+    bool initialized = false;
+    uint64_t timestep = 0;
+    int pcur = 0, ccur = 0, dist_idx = 0;
+    bool fields_mag_valid = false;  // inverse buffer holds B of the last solve
+    bool solved = false;            // a step ran since the last init
+
+    double *px[2][5] = {};
+    uint32_t *key[2] = {}, *pid[2] = {};
+    uint32_t *counts[2] = {};
+    double2 *fwd = nullptr, *inv = nullptr;
+    double *table = nullptr;
+    uint32_t *cellcount = nullptr, *cursor = nullptr;
+    double *kern = nullptr, *lut = nullptr;
+    double *staging = nullptr, *noise_dev = nullptr, *dist_dev = nullptr, *realbuf = nullptr;
+    unsigned long long *d_step = nullptr;
+    uint32_t *d_err = nullptr;
+    double *d_halfpi = nullptr;
+
+    std::map<int, cufftHandle> plans;
+    int fft_rank = 0;
+    int fft_n[3] = {1, 1, 1};
+
+    cudaGraphExec_t graph[2][2] = {};
+    uint64_t launches = 0;
+    uint64_t launches_per_step = 0;
+    Timing timing;
+    std::string err;
+};
+
+// ---------------------------------------------------------------------------
+// error helpers
+// ---------------------------------------------------------------------------
+static int fail(ss_ctx *c, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    g_last_error = buf;
+    return code;
+}
+
+#define CK(call)                                                                                    \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) return fail(c, SS_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+#define CKF(call)                                                                     \
+    do {                                                                              \
+        cufftResult r_ = (call);                                                      \
+        if (r_ != CUFFT_SUCCESS) return fail(c, SS_ERR_CUFFT, "%s: cufft error %d", #call, (int)r_); \
+    } while (0)
+#define CKR(expr)                   \
+    do {                            \
+        int rc_ = (expr);           \
+        if (rc_ != SS_OK) return rc_; \
+    } while (0)
+
+static int check_launch(ss_ctx *c, const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(c, SS_ERR_CUDA, "launch of %s: %s", what, cudaGetErrorString(e));
+    return SS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// angle kernels (init only): stress_kernel (src/flowfield/stress.rs:29-56)
+// with the closure of src/bin/simulation/mod.rs:100-104, and
+// orientation_kernel (src/polarization/director.rs:69-92).  Angles at cell
+// centres by ndarray's linspace: start + step * i, step = (end-start)/(n-1).
+// ---------------------------------------------------------------------------
+static double linspace_at(double a, double b, uint64_t n, uint64_t i) {
+    double step = (n > 1) ? (b - a) / ((double)n - 1.0) : 0.0;
+    return a + step * (double)i;
+}
+
+static double host_modulo(double f, double m) {
+    double r = std::fmod(f, m);
+    return r < 0.0 ? r + std::fabs(m) : r;
+}
+
+static void build_angle_kernels(const ss_ctx *c, std::vector<double> &K) {
+    const uint64_t gp = c->grid.phi, gt = c->grid.theta, na = gp * gt;
+    const double gwp = kTwoPi / (double)gp, gwt = kPi / (double)gt;
+    const double hp = gwp / 2., ht = gwt / 2.;
+    K.assign(12 * na, 0.0);
+    for (uint64_t i = 0; i < gp; ++i) {
+        double phi = linspace_at(0. + hp, kTwoPi - hp, gp, i);
+        for (uint64_t j = 0; j < gt; ++j) {
+            double theta = linspace_at(0. + ht, kPi - ht, gt, j);
+            double cp = std::cos(phi), sp = std::sin(phi), ct = std::cos(theta), st = std::sin(theta);
+            // stress_active (stress.rs:103-119)
+            double sa[9] = {-(1. / 3.) + cp * cp * st * st, cp * st * st * sp, ct * cp * st,
+                            cp * st * st * sp, -(1. / 3.) + st * st * sp * sp, ct * st * sp,
+                            ct * cp * st, ct * st * sp, -(1. / 3.) + ct * ct};
+            // stress_magnetic (stress.rs:125-141), field along y
+            double sm[9] = {0., cp * st, 0., -cp * st, 0., -ct, 0., ct, 0.};
+            // stress_magnetic_rods (stress.rs:144-159)
+            double c2p = std::cos(2. * phi), c2t = std::cos(2. * theta), s2t = std::sin(2. * theta);
+            double sr[9] = {2. * ct * (cp * cp) * (st * st), ct * (st * st) * c2p, c2t * cp * st,
+                            ct * (st * st) * c2p, st * s2t * (sp * sp), c2t * st * sp,
+                            c2t * cp * st, c2t * st * sp, -2. * ct * (st * st)};
+            for (int k = 0; k < 9; ++k) {
+                sm[k] = sm[k] * 0.5;
+                sr[k] = sr[k] * 0.5;
+                K[k * na + i * gt + j] =
+                    c->prm.stress_active * sa[k] + c->prm.stress_magnetic * sm[k] + c->prm.shape * sr[k];
+            }
+            // orientation kernel: Orientation::new (ang_pbc) then to_vector
+            double th = host_modulo(theta, kTwoPi), ph;
+            if (th > kPi) {
+                ph = host_modulo(phi + kPi, kTwoPi);
+                th = kTwoPi - th;
+            } else {
+                ph = host_modulo(phi, kTwoPi);
+            }
+            double ocp = std::cos(ph), osp = std::sin(ph), oct = std::cos(th), ost = std::sin(th);
+            K[9 * na + i * gt + j] = ost * ocp;
+            K[10 * na + i * gt + j] = ost * osp;
+            K[11 * na + i * gt + j] = oct;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// cuFFT plans (c2c Z2Z, unnormalised; the FFTW plans of
+// spectral_solver.rs:44-68 and magnetic_solver.rs:38-52).  Axes of length 1
+// are dropped: they do not change the memory layout of [comp][x][y][z].
+// ---------------------------------------------------------------------------
+static int get_plan(ss_ctx *c, int batch, cufftHandle *out) {
+    auto it = c->plans.find(batch);
+    if (it != c->plans.end()) {
+        *out = it->second;
+        return SS_OK;
+    }
+    cufftHandle h;
+    int nc = c->P.ncell;
+    CKF(cufftPlanMany(&h, c->fft_rank, c->fft_n, nullptr, 1, nc, nullptr, 1, nc, CUFFT_Z2Z, batch));
+    CKF(cufftSetStream(h, c->stream));
+    c->plans[batch] = h;
+    *out = h;
+    return SS_OK;
+}
+
+static int fft(ss_ctx *c, double2 *data, int batch, int dir) {
+    if (c->fft_rank == 0 || batch == 0) return SS_OK;  // 1-cell grid: the DFT is the identity
+    cufftHandle h;
+    CKR(get_plan(c, batch, &h));
+    CKF(cufftExecZ2Z(h, reinterpret_cast<cufftDoubleComplex *>(data), reinterpret_cast<cufftDoubleComplex *>(data),
+                     dir));
+    return SS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// timing helpers
+// ---------------------------------------------------------------------------
+static void mark(ss_ctx *c, int stage) {
+    if (c->timing.on) cudaEventRecord(c->timing.ev[stage], c->stream);
+}
+
+// ---------------------------------------------------------------------------
+// the field solve: contraction -> FFT -> k space -> inverse FFT -> table
+// ---------------------------------------------------------------------------
+static int enqueue_solve(ss_ctx *c, bool flow, bool mag, const uint32_t *counts, const double *dist, double screening,
+                         int pcur, bool sort_now, uint64_t *nl) {
+    const int ts = c->mag_step ? TABLE_STRIDE_MAG : TABLE_STRIDE;
+    mark(c, 0);
+    launch_contract(c->stream, flow, mag, counts, dist, c->lut, kLutN, c->kern, c->P, c->fwd, c->table, ts,
+                    c->cellcount);
+    ++*nl;
+    CKR(check_launch(c, "contract"));
+    mark(c, 6);
+    if (sort_now) {
+        launch_scan(c->stream, c->cellcount, c->P.ncell, c->cursor);
+        launch_scatter(c->stream, c->P.n, c->px[pcur], c->key[pcur], c->pid[pcur], c->px[1 - pcur],
+                       c->key[1 - pcur], c->pid[1 - pcur], c->cursor);
+        *nl += 2;
+        CKR(check_launch(c, "sort"));
+    }
+    mark(c, 1);
+    if (flow && mag) CKR(fft(c, c->fwd, 12, CUFFT_FORWARD));
+    else if (flow) CKR(fft(c, c->fwd, 9, CUFFT_FORWARD));
+    else CKR(fft(c, c->fwd + 9ll * c->P.ncell, 3, CUFFT_FORWARD));
+    mark(c, 2);
+    launch_kspace(c->stream, flow, mag, c->fwd, c->inv, c->P, screening);
+    ++*nl;
+    CKR(check_launch(c, "kspace"));
+    mark(c, 3);
+    if (flow && mag) CKR(fft(c, c->inv, 24, CUFFT_INVERSE));
+    else if (flow) CKR(fft(c, c->inv, 12, CUFFT_INVERSE));
+    else CKR(fft(c, c->inv + 12ll * c->P.ncell, 12, CUFFT_INVERSE));
+    mark(c, 4);
+    // the table has rows for the dipolar terms only when the step uses them
+    const bool table_mag = mag && c->mag_step;
+    if (flow || table_mag) {
+        launch_table(c->stream, flow, table_mag, c->inv, c->P, c->table, ts);
+        ++*nl;
+        CKR(check_launch(c, "table"));
+    }
+    return SS_OK;
+}
+
+// One do_timestep for the state (pcur, ccur); does not touch host-side state.
+static int enqueue_step(ss_ctx *c, int pcur, int ccur, bool host_noise, uint64_t *nl) {
+    const bool sort_now = c->sort;
+    CKR(enqueue_solve(c, true, c->mag_step, c->counts[ccur], nullptr, c->prm.hydro_screening, pcur, sort_now, nl));
+    const int p = sort_now ? 1 - pcur : pcur;
+    mark(c, 5);
+    launch_zero_u32(c->stream, c->counts[1 - ccur], c->P.nbins);
+    launch_update(c->stream, c->q2d, c->mag_step, host_noise, c->P, c->px[p], c->key[p], c->pid[p], c->table,
+                  c->noise_dev, c->d_step, c->counts[1 - ccur], c->d_err);
+    launch_step_inc(c->stream, c->d_step);
+    *nl += 3;
+    CKR(check_launch(c, "update"));
+    mark(c, 7);
+    return SS_OK;
+}
+
+static void advance(ss_ctx *c) {
+    if (c->sort) c->pcur ^= 1;
+    c->dist_idx = c->ccur;
+    c->ccur ^= 1;
+    c->timestep += 1;
+    c->fields_mag_valid = c->mag_step;
+    c->solved = true;
+}
+
+static void accumulate_timing(ss_ctx *c) {
+    if (!c->timing.on) return;
+    cudaEventSynchronize(c->timing.ev[7]);
+    // stage intervals: 0->6 contract, 6->1 sort, 1->2 fft fwd, 2->3 kspace, 3->4 fft inv, 4->5 table, 5->7 update
+    const int from[7] = {0, 6, 1, 2, 3, 4, 5};
+    const int to[7] = {6, 1, 2, 3, 4, 5, 7};
+    const int slot[7] = {0, 6, 1, 2, 3, 4, 5};
+    for (int k = 0; k < 7; ++k) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->timing.ev[from[k]], c->timing.ev[to[k]]);
+        c->timing.ms[slot[k]] += ms;
+    }
+    c->timing.steps += 1;
+}
+
+static int direct_step(ss_ctx *c, bool host_noise) {
+    uint64_t nl = 0;
+    CKR(enqueue_step(c, c->pcur, c->ccur, host_noise, &nl));
+    c->launches += nl;
+    c->launches_per_step = nl;
+    accumulate_timing(c);
+    advance(c);
+    return SS_OK;
+}
+
+static int graph_step(ss_ctx *c) {
+    cudaGraphExec_t &g = c->graph[c->pcur][c->ccur];
+    if (!g) {
+        cudaGraph_t graph;
+        uint64_t nl = 0;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_step(c, c->pcur, c->ccur, false, &nl);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+        if (rc != SS_OK) return rc;
+        if (e != cudaSuccess) return fail(c, SS_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&g, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(c, SS_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        c->launches_per_step = nl;
+    }
+    CK(cudaGraphLaunch(g, c->stream));
+    c->launches += c->launches_per_step;
+    advance(c);
+    return SS_OK;
+}
+
+static int read_device_error(ss_ctx *c) {
+    uint32_t e = 0;
+    CK(cudaMemcpyAsync(&e, c->d_err, sizeof e, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (e) {
+        return fail(c, SS_ERR_RANGE,
+                    "device bounds check fired (flags %u): a particle coordinate was non-finite or outside the "
+                    "box after wrapping",
+                    e);
+    }
+    return SS_OK;
+}
+
+static bool is_finite(double v) { return std::isfinite(v); }
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char *ss_version(void) { return "ssgpu 0.1 (sm_103a)"; }
+
+int ss_last_error(ss_ctx *ctx, char *buf, size_t len) {
+    if (!buf || len == 0) return SS_ERR_INVALID_ARGUMENT;
+    const std::string &s = ctx ? ctx->err : g_last_error;
+    std::snprintf(buf, len, "%s", s.c_str());
+    return SS_OK;
+}
+
+static void destroy_impl(ss_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &kv : c->plans) cufftDestroy(kv.second);
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b)
+            if (c->graph[a][b]) cudaGraphExecDestroy(c->graph[a][b]);
+    for (int b = 0; b < 2; ++b) {
+        for (int k = 0; k < 5; ++k) cudaFree(c->px[b][k]);
+        cudaFree(c->key[b]);
+        cudaFree(c->pid[b]);
+        cudaFree(c->counts[b]);
+    }
+    cudaFree(c->fwd); cudaFree(c->inv); cudaFree(c->table); cudaFree(c->cellcount); cudaFree(c->cursor);
+    cudaFree(c->kern); cudaFree(c->lut); cudaFree(c->staging); cudaFree(c->noise_dev); cudaFree(c->dist_dev);
+    cudaFree(c->realbuf); cudaFree(c->d_step); cudaFree(c->d_err); cudaFree(c->d_halfpi);
+    for (auto &e : c->timing.ev)
+        if (e) cudaEventDestroy(e);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int ss_destroy(ss_ctx *ctx) {
+    destroy_impl(ctx);
+    return SS_OK;
+}
+
+int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, uint32_t flags, void *stream,
+              ss_ctx **out) {
+    ss_ctx *c = nullptr;
+    if (!grid || !box || !params || !out) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "ss_create: null argument");
+    *out = nullptr;
+    const uint64_t lim = 1ull << 20;
+    if (grid->x < 1 || grid->y < 1 || grid->z < 1 || grid->phi < 1 || grid->theta < 1 || grid->x > lim ||
+        grid->y > lim || grid->z > lim || grid->phi > lim || grid->theta > lim)
+        return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "grid sizes must lie in [1, 2^20]");
+    const uint64_t ncell = grid->x * grid->y * grid->z, nang = grid->phi * grid->theta;
+    if (ncell > 0x7fffffffull || nang > 0x7fffffffull || ncell * nang > (1ull << 36))
+        return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "grid too large (cells %llu, angle bins %llu)",
+                    (unsigned long long)ncell, (unsigned long long)nang);
+    // check_settings (settings/mod.rs:185-205)
+    if (!(box->x > 0.) || !(box->y > 0.) || !(box->z > 0.) || !is_finite(box->x) || !is_finite(box->y) ||
+        !is_finite(box->z))
+        return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "Box size is invalid. Must be bigger than 0: (%g, %g, %g)",
+                    box->x, box->y, box->z);
+    if ((flags & SS_FLAG_QUASI2D) && grid->z != 1)
+        return fail(nullptr, SS_ERR_INVALID_ARGUMENT,
+                    "z-direction must only contain 1 cell if feature 'quasi2d' is activated.");
+    if (params->number_of_particles < 1 || params->number_of_particles > 0xffffffffull)
+        return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "number_of_particles must lie in [1, 2^32-1]");
+    const double vals[] = {params->timestep, params->trans_diffusion, params->rot_diffusion, params->stress_active,
+                           params->stress_magnetic, params->shape, params->magnetic_drag, params->hydro_screening,
+                           params->volume_exclusion, params->magnetic_reorientation,
+                           params->magnetic_dipole_dipole};
+    for (double v : vals)
+        if (!is_finite(v)) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "parameters must be finite");
+    if (params->rot_diffusion * params->timestep < 0.0)
+        return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "2 * rotational diffusion * timestep must be >= 0");
+
+    c = new ss_ctx();
+    c->grid = *grid;
+    c->box = *box;
+    c->prm = *params;
+    c->flags = flags;
+    c->q2d = (flags & SS_FLAG_QUASI2D) != 0;
+    c->sort = (flags & SS_FLAG_NO_SORT) == 0;
+    c->use_graph = (flags & SS_FLAG_NO_GRAPH) == 0;
+    c->mag_step = (flags & SS_FLAG_ALWAYS_MAGNETIC) || params->magnetic_dipole_dipole != 0.0 ||
+                  params->magnetic_drag != 0.0;
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e != cudaSuccess) {
+        destroy_impl(c);
+        return fail(nullptr, SS_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+    }
+    if (stream) {
+        c->stream = (cudaStream_t)stream;
+    } else {
+        e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            destroy_impl(c);
+            return fail(nullptr, SS_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+        }
+        c->own_stream = true;
+    }
+
+    DevParams &P = c->P;
+    P.gx = (int)grid->x; P.gy = (int)grid->y; P.gz = (int)grid->z; P.gphi = (int)grid->phi;
+    P.gtheta = (int)grid->theta;
+    P.ncell = (int)ncell;
+    P.nang = (int)nang;
+    P.nbins = (long long)(ncell * nang);
+    P.n = params->number_of_particles;
+    P.bx = box->x; P.by = box->y; P.bz = box->z;
+    // GridWidth::new (src/mesh/grid_width.rs:23-31)
+    P.gw[0] = box->x / (double)grid->x;
+    P.gw[1] = box->y / (double)grid->y;
+    P.gw[2] = box->z / (double)grid->z;
+    P.gw[3] = kTwoPi / (double)grid->phi;
+    P.gw[4] = kPi / (double)grid->theta;
+    for (int k = 0; k < 5; ++k) P.igw[k] = 1.0 / P.gw[k];
+    P.dt = params->timestep;
+    P.Dt = params->trans_diffusion;
+    P.Dr = params->rot_diffusion;
+    P.shape = params->shape;
+    P.drag = params->magnetic_drag;
+    P.reorient = params->magnetic_reorientation;
+    P.mdd = params->magnetic_dipole_dipole;
+    P.volex = params->volume_exclusion;
+    P.dist_den = P.gw[0] * P.gw[1] * P.gw[2] * P.gw[3] * P.gw[4] * (double)P.n;
+    P.volume = box->x * box->y * box->z;
+    P.measure = P.gw[3] * P.gw[4];
+    P.dthph = P.gw[4] * P.gw[3];
+    P.sigma_rot = std::sqrt(2. * params->rot_diffusion * params->timestep);
+    P.seed = params->seed;
+    P.quasi2d = c->q2d ? 1 : 0;
+    uint32_t mask = M_ALL;
+    if (params->magnetic_reorientation == 0.0) mask &= ~M_EXTERNAL_FIELD;
+    if (params->shape == 0.0) mask &= ~M_JEFFREY_STRAIN;
+    if (!c->mag_step || params->magnetic_drag == 0.0) mask &= ~M_MDD_FORCE;
+    if (!c->mag_step || params->magnetic_dipole_dipole == 0.0) mask &= ~M_MDD_ROTATION;
+    P.mask = mask;
+
+    // FFT geometry: drop axes of length 1
+    {
+        int dims[3] = {P.gx, P.gy, P.gz}, r = 0;
+        for (int k = 0; k < 3; ++k)
+            if (dims[k] > 1) c->fft_n[r++] = dims[k];
+        c->fft_rank = r;
+    }
+
+    auto alloc = [&](void **p, size_t bytes) -> int {
+        cudaError_t err = cudaMalloc(p, bytes ? bytes : 16);
+        if (err != cudaSuccess)
+            return fail(c, SS_ERR_CUDA, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(err));
+        return SS_OK;
+    };
+    int rc = SS_OK;
+    const size_t N = (size_t)P.n;
+    const int nbuf = c->sort ? 2 : 1;
+    for (int b = 0; b < nbuf && rc == SS_OK; ++b) {
+        for (int k = 0; k < 5 && rc == SS_OK; ++k) rc = alloc((void **)&c->px[b][k], N * sizeof(double));
+        if (rc == SS_OK) rc = alloc((void **)&c->key[b], N * sizeof(uint32_t));
+        if (rc == SS_OK) rc = alloc((void **)&c->pid[b], N * sizeof(uint32_t));
+    }
+    for (int b = 0; b < 2 && rc == SS_OK; ++b) rc = alloc((void **)&c->counts[b], (size_t)P.nbins * sizeof(uint32_t));
+    if (rc == SS_OK) rc = alloc((void **)&c->fwd, 12 * ncell * sizeof(double2));
+    if (rc == SS_OK) rc = alloc((void **)&c->inv, 24 * ncell * sizeof(double2));
+    if (rc == SS_OK) rc = alloc((void **)&c->table, ncell * TABLE_STRIDE_MAG * sizeof(double));
+    if (rc == SS_OK) rc = alloc((void **)&c->cellcount, ncell * sizeof(uint32_t));
+    if (rc == SS_OK) rc = alloc((void **)&c->cursor, ncell * sizeof(uint32_t));
+    if (rc == SS_OK) rc = alloc((void **)&c->kern, 12 * nang * sizeof(double));
+    if (rc == SS_OK) rc = alloc((void **)&c->lut, kLutN * sizeof(double));
+    if (rc == SS_OK) rc = alloc((void **)&c->staging, 5 * N * sizeof(double));
+    if (rc == SS_OK) rc = alloc((void **)&c->d_step, sizeof(unsigned long long));
+    if (rc == SS_OK) rc = alloc((void **)&c->d_err, sizeof(uint32_t));
+    if (rc == SS_OK) rc = alloc((void **)&c->d_halfpi, 2 * sizeof(double));
+    if (rc != SS_OK) {
+        std::string m = c->err;
+        destroy_impl(c);
+        return fail(nullptr, rc, "%s", m.c_str());
+    }
+#define CKC(call)                                                                                     \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) {                                                                      \
+            std::string m_ = std::string(#call) + ": " + cudaGetErrorString(e_);                      \
+            destroy_impl(c);                                                                          \
+            return fail(nullptr, SS_ERR_CUDA, "%s", m_.c_str());                                      \
+        }                                                                                             \
+    } while (0)
+    CKC(cudaMemsetAsync(c->fwd, 0, 12 * ncell * sizeof(double2), c->stream));
+    CKC(cudaMemsetAsync(c->inv, 0, 24 * ncell * sizeof(double2), c->stream));
+    CKC(cudaMemsetAsync(c->table, 0, ncell * TABLE_STRIDE_MAG * sizeof(double), c->stream));
+    CKC(cudaMemsetAsync(c->counts[0], 0, (size_t)P.nbins * sizeof(uint32_t), c->stream));
+    CKC(cudaMemsetAsync(c->counts[1], 0, (size_t)P.nbins * sizeof(uint32_t), c->stream));
+    CKC(cudaMemsetAsync(c->d_step, 0, sizeof(unsigned long long), c->stream));
+    CKC(cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream));
+
+    std::vector<double> K;
+    build_angle_kernels(c, K);
+    std::vector<double> lut(kLutN);
+    for (int i = 0; i < kLutN; ++i) lut[i] = ((double)i / P.dist_den) * P.volume;
+    CKC(cudaMemcpyAsync(c->kern, K.data(), K.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CKC(cudaMemcpyAsync(c->lut, lut.data(), lut.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    launch_half_pi(c->stream, c->d_halfpi);
+    double hp[2];
+    CKC(cudaMemcpyAsync(hp, c->d_halfpi, sizeof hp, cudaMemcpyDeviceToHost, c->stream));
+    CKC(cudaStreamSynchronize(c->stream));
+    P.cos_half_pi = hp[0];
+    P.sin_half_pi = hp[1];
+    for (auto &ev : c->timing.ev) CKC(cudaEventCreate(&ev));
+#undef CKC
+    // plans for the step
+    {
+        cufftHandle h;
+        int r1 = get_plan(c, c->mag_step ? 12 : 9, &h);
+        int r2 = (r1 == SS_OK) ? get_plan(c, c->mag_step ? 24 : 12, &h) : r1;
+        if (r1 != SS_OK || r2 != SS_OK) {
+            std::string m = c->err;
+            destroy_impl(c);
+            return fail(nullptr, SS_ERR_CUFFT, "%s", m.c_str());
+        }
+    }
+    *out = c;
+    return SS_OK;
+}
+
+static int load_particles(ss_ctx *c, const double *particles, uint64_t n) {
+    if (!particles) return fail(c, SS_ERR_INVALID_ARGUMENT, "particles is NULL");
+    if (n != c->P.n)
+        return fail(c, SS_ERR_PARTICLE_COUNT,
+                    "Given initial condition has not the same number of particles (%llu) as given in the "
+                    "parameter file (%llu).",
+                    (unsigned long long)n, (unsigned long long)c->P.n);
+    for (uint64_t i = 0; i < 5 * n; ++i)
+        if (!is_finite(particles[i]))
+            return fail(c, SS_ERR_INVALID_ARGUMENT, "particle %llu has a non-finite coordinate",
+                        (unsigned long long)(i / 5));
+    CK(cudaSetDevice(c->device));
+    c->pcur = 0;
+    c->ccur = 0;
+    CK(cudaMemcpyAsync(c->staging, particles, 5 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    launch_ingest(c->stream, c->staging, n, c->P, c->px[0], c->pid[0]);
+    launch_zero_u32(c->stream, c->counts[0], c->P.nbins);
+    launch_bin(c->stream, n, c->P, c->px[0], c->key[0], c->counts[0], c->d_err);
+    c->launches += 3;
+    CKR(check_launch(c, "init"));
+    c->dist_idx = 0;
+    c->fields_mag_valid = false;
+    c->solved = false;
+    c->initialized = true;
+    CK(cudaStreamSynchronize(c->stream));
+    return SS_OK;
+}
+
+int ss_init(ss_ctx *c, const double *particles, uint64_t n) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    CKR(load_particles(c, particles, n));
+    c->timestep = 0;
+    CK(cudaMemsetAsync(c->d_step, 0, sizeof(unsigned long long), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SS_OK;
+}
+
+int ss_resume(ss_ctx *c, const double *particles, uint64_t n, uint64_t timestep) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    CKR(load_particles(c, particles, n));
+    c->timestep = timestep;
+    unsigned long long t = timestep;
+    CK(cudaMemcpyAsync(c->d_step, &t, sizeof t, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SS_OK;
+}
+
+int ss_do_timestep(ss_ctx *c, const double *noise, uint64_t *timestep_out) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    if (!c->initialized) return fail(c, SS_ERR_STATE, "ss_do_timestep before ss_init");
+    CK(cudaSetDevice(c->device));
+    if (noise) {
+        if (!c->noise_dev) CK(cudaMalloc((void **)&c->noise_dev, 5 * (size_t)c->P.n * sizeof(double)));
+        CK(cudaMemcpyAsync(c->noise_dev, noise, 5 * (size_t)c->P.n * sizeof(double), cudaMemcpyHostToDevice,
+                           c->stream));
+        CKR(direct_step(c, true));
+        // the caller may reuse its noise buffer once this returns
+        CK(cudaStreamSynchronize(c->stream));
+    } else if (c->use_graph && !c->timing.on) {
+        CKR(graph_step(c));
+    } else {
+        CKR(direct_step(c, false));
+    }
+    if (timestep_out) *timestep_out = c->timestep;
+    return SS_OK;
+}
+
+int ss_run(ss_ctx *c, uint64_t steps, uint64_t *timestep_out) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    if (!c->initialized) return fail(c, SS_ERR_STATE, "ss_run before ss_init");
+    CK(cudaSetDevice(c->device));
+    for (uint64_t s = 0; s < steps; ++s) {
+        if (c->use_graph && !c->timing.on) CKR(graph_step(c));
+        else CKR(direct_step(c, false));
+    }
+    if (timestep_out) *timestep_out = c->timestep;
+    return SS_OK;
+}
+
+int ss_noise(ss_ctx *c, uint64_t timestep, double *out) {
+    if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
+    CK(cudaSetDevice(c->device));
+    launch_noise(c->stream, c->q2d, c->P, timestep, c->staging);
+    c->launches += 1;
+    CKR(check_launch(c, "noise"));
+    CK(cudaMemcpyAsync(out, c->staging, 5 * (size_t)c->P.n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SS_OK;
+}
+
+int ss_synchronize(ss_ctx *c) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    CK(cudaStreamSynchronize(c->stream));
+    return read_device_error(c);
+}
+
+int ss_get_particles(ss_ctx *c, double *out, uint64_t n) {
+    if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->initialized) return fail(c, SS_ERR_STATE, "no particles before ss_init");
+    if (n > c->P.n) return fail(c, SS_ERR_INVALID_ARGUMENT, "asked for %llu of %llu particles",
+                                (unsigned long long)n, (unsigned long long)c->P.n);
+    CK(cudaSetDevice(c->device));
+    launch_egest(c->stream, c->P.n, c->px[c->pcur], c->pid[c->pcur], c->staging);
+    c->launches += 1;
+    CKR(check_launch(c, "egest"));
+    CK(cudaMemcpyAsync(out, c->staging, 5 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return read_device_error(c);
+}
+
+int ss_get_counts(ss_ctx *c, uint32_t *out) {
+    if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
+    CK(cudaSetDevice(c->device));
+    CK(cudaMemcpyAsync(out, c->counts[c->dist_idx], (size_t)c->P.nbins * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return read_device_error(c);
+}
+
+int ss_get_distribution(ss_ctx *c, double *out) {
+    if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
+    CK(cudaSetDevice(c->device));
+    if (!c->dist_dev) CK(cudaMalloc((void **)&c->dist_dev, (size_t)c->P.nbins * sizeof(double)));
+    launch_counts_to_dist(c->stream, c->counts[c->dist_idx], c->P, c->dist_dev);
+    c->launches += 1;
+    CKR(check_launch(c, "counts_to_dist"));
+    CK(cudaMemcpyAsync(out, c->dist_dev, (size_t)c->P.nbins * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return read_device_error(c);
+}
+
+static int copy_real(ss_ctx *c, const double2 *src, int comps, double *out) {
+    long long cnt = (long long)comps * c->P.ncell;
+    if (!c->realbuf) CK(cudaMalloc((void **)&c->realbuf, 24ull * c->P.ncell * sizeof(double)));
+    launch_real_parts(c->stream, src, cnt, c->realbuf);
+    c->launches += 1;
+    CKR(check_launch(c, "real_parts"));
+    CK(cudaMemcpyAsync(out, c->realbuf, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SS_OK;
+}
+
+// The dipolar field of the last solve, computed on demand when the step
+// skipped it (its couplings are zero).  The histogram it is built from is
+// still resident, so the result equals what the step would have produced.
+static int ensure_magnetic(ss_ctx *c) {
+    if (c->fields_mag_valid) return SS_OK;
+    if (!c->initialized || !c->solved) return SS_OK;  // nothing solved yet: zeros, like the reference
+    uint64_t nl = 0;
+    int pc = c->pcur;
+    CKR(enqueue_solve(c, false, true, c->counts[c->dist_idx], nullptr, 0.0, pc, false, &nl));
+    c->launches += nl;
+    c->fields_mag_valid = true;
+    return SS_OK;
+}
+
+int ss_get_flow_field(ss_ctx *c, double *out) {
+    if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
+    CK(cudaSetDevice(c->device));
+    return copy_real(c, c->inv + 9ll * c->P.ncell, 3, out);
+}
+
+int ss_get_magnetic_field(ss_ctx *c, double *out) {
+    if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
+    CK(cudaSetDevice(c->device));
+    CKR(ensure_magnetic(c));
+    return copy_real(c, c->inv + 21ll * c->P.ncell, 3, out);
+}
+
+int ss_get_flow_complex(ss_ctx *c, double *u, double *grad) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    CK(cudaSetDevice(c->device));
+    const size_t nc = c->P.ncell;
+    if (u) CK(cudaMemcpyAsync(u, c->inv + 9 * nc, 3 * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
+    if (grad) CK(cudaMemcpyAsync(grad, c->inv, 9 * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SS_OK;
+}
+
+int ss_get_magnetic_complex(ss_ctx *c, double *b, double *gradb) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    CK(cudaSetDevice(c->device));
+    CKR(ensure_magnetic(c));
+    const size_t nc = c->P.ncell;
+    if (b) CK(cudaMemcpyAsync(b, c->inv + 21 * nc, 3 * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
+    if (gradb) CK(cudaMemcpyAsync(gradb, c->inv + 12 * nc, 9 * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SS_OK;
+}
+
+int ss_get_timestep(ss_ctx *c, uint64_t *out) {
+    if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
+    *out = c->timestep;
+    return SS_OK;
+}
+
+static int seam_solve(ss_ctx *c, bool flow, bool mag, double screening, const double *dist) {
+    if (!dist) return fail(c, SS_ERR_INVALID_ARGUMENT, "dist is NULL");
+    CK(cudaSetDevice(c->device));
+    if (!c->dist_dev) CK(cudaMalloc((void **)&c->dist_dev, (size_t)c->P.nbins * sizeof(double)));
+    CK(cudaMemcpyAsync(c->dist_dev, dist, (size_t)c->P.nbins * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    uint64_t nl = 0;
+    CKR(enqueue_solve(c, flow, mag, nullptr, c->dist_dev, screening, c->pcur, false, &nl));
+    c->launches += nl;
+    if (mag) c->fields_mag_valid = true;
+    return SS_OK;
+}
+
+int ss_mean_flow_field(ss_ctx *c, double screening, const double *dist, double *u, double *grad) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    if (!is_finite(screening)) return fail(c, SS_ERR_INVALID_ARGUMENT, "screening must be finite");
+    CKR(seam_solve(c, true, false, screening, dist));
+    return ss_get_flow_complex(c, u, grad);
+}
+
+int ss_mean_magnetic_field(ss_ctx *c, const double *dist, double *b, double *gradb) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    CKR(seam_solve(c, false, true, 0.0, dist));
+    return ss_get_magnetic_complex(c, b, gradb);
+}
+
+int ss_langevin(const double *particles, uint64_t n, uint32_t mask, const ss_langevin_args *args, double *out) {
+    ss_ctx *c = nullptr;
+    if (!particles || !args || !out) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "ss_langevin: null argument");
+    if (n == 0) return SS_OK;
+    static_assert(sizeof(ss_langevin_args) == 46 * sizeof(double), "ss_langevin_args layout");
+    double *d_in = nullptr, *d_out = nullptr, *d_args = nullptr;
+    CK(cudaMalloc((void **)&d_in, 5 * n * sizeof(double)));
+    CK(cudaMalloc((void **)&d_out, 5 * n * sizeof(double)));
+    CK(cudaMalloc((void **)&d_args, sizeof(ss_langevin_args)));
+    CK(cudaMemcpy(d_in, particles, 5 * n * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_args, args, sizeof(ss_langevin_args), cudaMemcpyHostToDevice));
+    launch_langevin_args(nullptr, d_in, n, mask & M_ALL, d_args, d_out);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out, d_out, 5 * n * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(d_in);
+    cudaFree(d_out);
+    cudaFree(d_args);
+    if (e != cudaSuccess) return fail(nullptr, SS_ERR_CUDA, "ss_langevin: %s", cudaGetErrorString(e));
+    return SS_OK;
+}
+
+int ss_profile_enable(ss_ctx *c, int enable) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    CK(cudaStreamSynchronize(c->stream));
+    c->timing.on = enable != 0;
+    for (double &m : c->timing.ms) m = 0.0;
+    c->timing.steps = 0;
+    return SS_OK;
+}
+
+int ss_profile_read(ss_ctx *c, double *ms, uint64_t *count) {
+    if (!c || !ms) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
+    for (int k = 0; k < SS_NUM_STAGES; ++k) ms[k] = c->timing.ms[k];
+    if (count) *count = c->timing.steps;
+    return SS_OK;
+}
+
+int ss_launch_count(ss_ctx *c, uint64_t *out) {
+    if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
+    *out = c->launches;
+    return SS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,239 @@
+"""Host-side mirror of the reference's ``Simulation`` (src/bin/simulation/mod.rs)
+over the C ABI of libssgpu.so.
+
+    sim = Simulation(settings)          # Simulation::new        (:91-160)
+    sim.init(particles)                 # Simulation::init       (:163-196)
+    sim.do_timestep()                   # Simulation::do_timestep (:251-374)
+    sim.get_particles() / get_distribution() / get_flow_field() /
+    get_magnetic_field() / get_timestep() / get_snapshot() / resume()
+
+Particles are numpy arrays of shape (n, 5) with columns (x, y, z, phi, theta),
+the reference's serialised Particle layout (src/particle.rs:363-395).  All
+arithmetic runs on the GPU; there is no CPU fallback.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import Box, Grid, LangevinArgs, Params, check
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+class Simulation:
+    """One simulation on the current CUDA device."""
+
+    def __init__(self, settings=None, *, grid=None, box=None, params=None, quasi2d=False, sort=True, graph=True,
+                 always_magnetic=False, stream=None):
+        if settings is not None:
+            sim, par = settings.simulation, settings.parameters
+            grid = (sim.grid_size.x, sim.grid_size.y, sim.grid_size.z, sim.grid_size.phi, sim.grid_size.theta)
+            box = (sim.box_size.x, sim.box_size.y, sim.box_size.z)
+            params = dict(timestep=sim.timestep, trans_diffusion=par.diffusion.translational,
+                          rot_diffusion=par.diffusion.rotational, stress_active=par.stress.active,
+                          stress_magnetic=par.stress.magnetic, shape=par.shape, magnetic_drag=par.magnetic_drag,
+                          hydro_screening=par.hydro_screening, volume_exclusion=par.volume_exclusion,
+                          magnetic_reorientation=par.magnetic_reorientation,
+                          magnetic_dipole_dipole=par.magnetic_dipole.magnetic_dipole_dipole,
+                          number_of_particles=sim.number_of_particles, seed=sim.seed)
+        if grid is None or box is None or params is None:
+            raise ValueError("give settings, or grid, box and params")
+        self.lib = _lib.load()
+        self.grid = tuple(int(v) for v in grid)
+        self.box = tuple(float(v) for v in box)
+        self.params = dict(params)
+        g = Grid(*self.grid)
+        b = Box(*self.box)
+        p = Params()
+        for k, v in self.params.items():
+            setattr(p, k, v)
+        self.n = int(p.number_of_particles)
+        flags = 0
+        if quasi2d:
+            flags |= _lib.FLAG_QUASI2D
+        if not sort:
+            flags |= _lib.FLAG_NO_SORT
+        if not graph:
+            flags |= _lib.FLAG_NO_GRAPH
+        if always_magnetic:
+            flags |= _lib.FLAG_ALWAYS_MAGNETIC
+        self.flags = flags
+        h = ctypes.c_void_p()
+        rc = self.lib.ss_create(ctypes.byref(g), ctypes.byref(b), ctypes.byref(p), flags,
+                                ctypes.c_void_p(stream) if stream else None, ctypes.byref(h))
+        check(rc)
+        self._h = h
+        gx, gy, gz, gp, gt = self.grid
+        self.ncell = gx * gy * gz
+        self.dist_shape = (gx, gy, gz, gp, gt)
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self.lib.ss_destroy(h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        check(rc, self._h)
+
+    # --- Simulation API ---------------------------------------------------
+    def init(self, particles):
+        p = _f64(particles, (-1, 5))
+        self._check(self.lib.ss_init(self._h, _ptr(p), p.shape[0]))
+
+    def resume(self, particles, timestep):
+        p = _f64(particles, (-1, 5))
+        self._check(self.lib.ss_resume(self._h, _ptr(p), p.shape[0], int(timestep)))
+
+    def do_timestep(self, noise=None):
+        t = ctypes.c_uint64()
+        if noise is None:
+            self._check(self.lib.ss_do_timestep(self._h, None, ctypes.byref(t)))
+        else:
+            z = _f64(noise, (self.n, 5))
+            self._check(self.lib.ss_do_timestep(self._h, _ptr(z), ctypes.byref(t)))
+        return t.value
+
+    def run(self, steps):
+        t = ctypes.c_uint64()
+        self._check(self.lib.ss_run(self._h, int(steps), ctypes.byref(t)))
+        return t.value
+
+    def noise(self, timestep):
+        """The Philox noise step `timestep` uses, as RandomVector rows (n, 5)."""
+        out = np.empty((self.n, 5))
+        self._check(self.lib.ss_noise(self._h, int(timestep), _ptr(out)))
+        return out
+
+    def synchronize(self):
+        self._check(self.lib.ss_synchronize(self._h))
+
+    def get_particles(self, out=None):
+        out = np.empty((self.n, 5)) if out is None else out
+        self._check(self.lib.ss_get_particles(self._h, _ptr(out), self.n))
+        return out
+
+    def get_particles_head(self, n):
+        out = np.empty((int(n), 5))
+        self._check(self.lib.ss_get_particles(self._h, _ptr(out), int(n)))
+        return out
+
+    def get_distribution(self):
+        out = np.empty(self.dist_shape)
+        self._check(self.lib.ss_get_distribution(self._h, _ptr(out)))
+        return out
+
+    def get_counts(self):
+        out = np.empty(self.dist_shape, dtype=np.uint32)
+        self._check(self.lib.ss_get_counts(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
+        return out
+
+    def get_flow_field(self):
+        out = np.empty((3,) + self.grid[:3])
+        self._check(self.lib.ss_get_flow_field(self._h, _ptr(out)))
+        return out
+
+    def get_magnetic_field(self):
+        out = np.empty((3,) + self.grid[:3])
+        self._check(self.lib.ss_get_magnetic_field(self._h, _ptr(out)))
+        return out
+
+    def get_flow_complex(self):
+        u = np.empty((3,) + self.grid[:3], dtype=np.complex128)
+        g = np.empty((3, 3) + self.grid[:3], dtype=np.complex128)
+        self._check(self.lib.ss_get_flow_complex(self._h, _ptr(u.view(np.float64)), _ptr(g.view(np.float64))))
+        return u, g
+
+    def get_magnetic_complex(self):
+        b = np.empty((3,) + self.grid[:3], dtype=np.complex128)
+        g = np.empty((3, 3) + self.grid[:3], dtype=np.complex128)
+        self._check(self.lib.ss_get_magnetic_complex(self._h, _ptr(b.view(np.float64)),
+                                                     _ptr(g.view(np.float64))))
+        return b, g
+
+    def get_timestep(self):
+        t = ctypes.c_uint64()
+        self._check(self.lib.ss_get_timestep(self._h, ctypes.byref(t)))
+        return t.value
+
+    def get_snapshot(self):
+        """Snapshot (src/bin/simulation/mod.rs:80-86,210-217): the particles and
+        the step counter.  The noise is counter based (Philox keyed by seed), so
+        (seed, timestep) is the whole RNG state."""
+        return {"particles": self.get_particles(), "rng_state": {"philox_seed": int(self.params["seed"])},
+                "timestep": self.get_timestep()}
+
+    # --- library seams ----------------------------------------------------
+    def mean_flow_field(self, screening, dist):
+        d = _f64(dist, self.dist_shape)
+        u = np.empty((3,) + self.grid[:3], dtype=np.complex128)
+        g = np.empty((3, 3) + self.grid[:3], dtype=np.complex128)
+        self._check(self.lib.ss_mean_flow_field(self._h, float(screening), _ptr(d), _ptr(u.view(np.float64)),
+                                                _ptr(g.view(np.float64))))
+        return u, g
+
+    def mean_magnetic_field(self, dist):
+        d = _f64(dist, self.dist_shape)
+        b = np.empty((3,) + self.grid[:3], dtype=np.complex128)
+        g = np.empty((3, 3) + self.grid[:3], dtype=np.complex128)
+        self._check(self.lib.ss_mean_magnetic_field(self._h, _ptr(d), _ptr(b.view(np.float64)),
+                                                    _ptr(g.view(np.float64))))
+        return b, g
+
+    # --- instrumentation --------------------------------------------------
+    def profile(self, enable=True):
+        self._check(self.lib.ss_profile_enable(self._h, 1 if enable else 0))
+
+    def profile_read(self):
+        ms = np.zeros(_lib.NUM_STAGES)
+        n = ctypes.c_uint64()
+        self._check(self.lib.ss_profile_read(self._h, _ptr(ms), ctypes.byref(n)))
+        return dict(zip(_lib.STAGES, ms.tolist())), n.value
+
+    def launch_count(self):
+        n = ctypes.c_uint64()
+        self._check(self.lib.ss_launch_count(self._h, ctypes.byref(n)))
+        return n.value
+
+
+def langevin(particles, mask, **kw):
+    """Run the LangevinBuilder chain (modifier bits in do_timestep order) on
+    independent particles with shared arguments, on the GPU."""
+    lib = _lib.load()
+    a = LangevinArgs()
+    a.box_x, a.box_y, a.box_z = kw.pop("box", (10.0, 10.0, 10.0))
+    for k, v in kw.items():
+        cur = getattr(a, k)
+        if isinstance(cur, float):
+            setattr(a, k, float(v))
+        else:
+            for i, x in enumerate(np.asarray(v, dtype=np.float64).ravel()):
+                cur[i] = x
+    p = _f64(particles, (-1, 5))
+    out = np.empty_like(p)
+    check(lib.ss_langevin(_ptr(p), p.shape[0], int(mask), ctypes.byref(a), _ptr(out)))
+    return out

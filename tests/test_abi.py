@@ -1,0 +1,66 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every entry point
+that include/ssgpu.h declares.  No compute call is made here (no GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    text = open(os.path.join(ROOT, "include", "ssgpu.h")).read()
+    return sorted(set(re.findall(r"^(?:int|const char \*)\s*(ss_\w+)\(", text, flags=re.M)))
+
+
+def test_header_and_loader_agree():
+    from stochasticsampling_gb300 import _lib
+    assert _declared() == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol():
+    from stochasticsampling_gb300 import _lib
+    L = _lib.load()
+    for name in _declared():
+        assert hasattr(L, name), name
+    assert L.ss_version().startswith(b"ssgpu")
+
+
+def test_invalid_arguments_are_rejected_on_the_host():
+    from stochasticsampling_gb300 import _lib
+    from stochasticsampling_gb300._lib import Box, Grid, Params
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    p = Params(number_of_particles=10)
+    # quasi2d with z != 1 (src/bin/simulation/mod.rs:96-98)
+    rc = L.ss_create(ctypes.byref(Grid(4, 4, 2, 4, 1)), ctypes.byref(Box(1, 1, 1)), ctypes.byref(p),
+                     _lib.FLAG_QUASI2D, None, ctypes.byref(h))
+    assert rc == _lib.SS_ERR_INVALID_ARGUMENT and "quasi2d" in _lib.last_error()
+    # box <= 0 (check_settings)
+    rc = L.ss_create(ctypes.byref(Grid(4, 4, 1, 4, 1)), ctypes.byref(Box(0, 1, 1)), ctypes.byref(p), 0, None,
+                     ctypes.byref(h))
+    assert rc == _lib.SS_ERR_INVALID_ARGUMENT and "Box size" in _lib.last_error()
+    # zero particles, zero-sized grid
+    rc = L.ss_create(ctypes.byref(Grid(4, 4, 1, 4, 1)), ctypes.byref(Box(1, 1, 1)),
+                     ctypes.byref(Params(number_of_particles=0)), 0, None, ctypes.byref(h))
+    assert rc == _lib.SS_ERR_INVALID_ARGUMENT
+    rc = L.ss_create(ctypes.byref(Grid(0, 4, 1, 4, 1)), ctypes.byref(Box(1, 1, 1)), ctypes.byref(p), 0, None,
+                     ctypes.byref(h))
+    assert rc == _lib.SS_ERR_INVALID_ARGUMENT
+    # non-finite parameters
+    bad = Params(number_of_particles=10, timestep=float("nan"))
+    rc = L.ss_create(ctypes.byref(Grid(4, 4, 1, 4, 1)), ctypes.byref(Box(1, 1, 1)), ctypes.byref(bad), 0, None,
+                     ctypes.byref(h))
+    assert rc == _lib.SS_ERR_INVALID_ARGUMENT
+    # null context
+    assert L.ss_do_timestep(None, None, None) == _lib.SS_ERR_INVALID_ARGUMENT
+
+
+def test_no_cpu_fallback_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from stochasticsampling_gb300 import SsError, Simulation
+    with pytest.raises(SsError):
+        Simulation(grid=(4, 4, 1, 4, 1), box=(1, 1, 1), params=dict(number_of_particles=8), quasi2d=True)

@@ -1,0 +1,326 @@
+"""The CPU oracle against the reference's own known-answer tests and golden
+fixtures.  Every expected value below is the one the cited reference test
+asserts; the oracle must reproduce it before it may judge the GPU path."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import EPS, GOLDEN, equal_floats, rel_l2
+
+PI = np.pi
+TWOPI = 2.0 * PI
+
+
+# ---------------------------------------------------------------- particle.rs
+def test_modulo(oracle):
+    # src/particle_test.rs:32-57
+    cases = [((TWOPI, TWOPI), 0.0), ((TWOPI + EPS, TWOPI), 0.0), ((7.0, 4.0), 3.0), ((7.0, -4.0), 3.0),
+             ((-7.0, 4.0), 1.0), ((-7.0, -4.0), 1.0)]
+    for (f, m), want in cases:
+        assert equal_floats(oracle.modulo(f, m), want), (f, m)
+    assert oracle.modulo(-EPS, TWOPI) != 0.9
+
+
+def test_ang_pbc(oracle):
+    # src/particle_test.rs:60-99
+    inp = [(1.0, 0.0), (1.0, PI), (1.0, -0.1), (1.0, PI + 0.1), (TWOPI, PI), (6.283185307179586, 1.5707963267948966),
+           (PI, PI + 1.0)]
+    exp = [(1.0, 0.0), (1.0, PI), (1.0 + PI, 0.09999999999999964), (1.0 + PI, PI - 0.1), (0.0, PI), (0.0, PI / 2.0),
+           (0.0, PI - 1.0)]
+    for i, e in zip(inp, exp):
+        phi, theta = oracle.ang_pbc(*i)
+        assert equal_floats(phi, e[0]), i
+        assert equal_floats(theta, e[1]), i
+
+
+def test_orientation_from_vector(oracle):
+    # src/particle_test.rs:114-165 (expected: [theta, phi])
+    inp = [[1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 0], [1, 0, 1], [-1, 0, 0], [0, -1, 0], [0, 0, -1], [-1, 1, 0],
+           [1, 0, -1], [15.23456, 0, 0]]
+    exp = [[PI / 2, 0], [PI / 2, PI / 2], [0, 0], [PI / 2, PI / 4], [PI / 4, 0], [PI / 2, PI], [PI / 2, -PI / 2],
+           [PI, 0], [PI / 2, 3 * PI / 4], [3 / 4 * PI, 0], [PI / 2, 0]]
+    for i, e in zip(inp, exp):
+        phi, theta = oracle.from_vector(np.array(i, dtype=float))
+        assert equal_floats(e[0], theta), i
+        assert equal_floats(e[1], phi), i
+
+
+# ------------------------------------------------------------ distribution
+def test_coord_to_grid(oracle):
+    # src/distribution/distribution_test.rs:118-184
+    s = oracle.make_settings((50, 50, 1, 10, 1), (1.0, 1.0, 1.0))
+    inp = [[0, 0, 0, 0, 0], [1, 0, 0, 0, 0], [0, 1, 0, 0, 0], [0, 0, 0, 0.5, 0], [0, 0, 0, 7, 0], [0, 0, 0, -1, 0],
+           [0.96, 0, 0, 0, 0], [0.5, 0.5, 0, -1, 0], [0.5, 0.5, 0, 0, 0], [0, 0, 0, 2 * PI, 0],
+           [0.51000000000000005, 0.5, 0, 6.283185307179584, 0]]
+    out = [[0, 0, 0, 0, 0], [0, 0, 0, 0, 0], [0, 0, 0, 0, 0], [0, 0, 0, 0, 0], [0, 0, 0, 1, 0], [0, 0, 0, 8, 0],
+           [48, 0, 0, 0, 0], [25, 25, 0, 8, 0], [25, 25, 0, 0, 0], [0, 0, 0, 0, 0], [25, 25, 0, 9, 0]]
+    for i, o in zip(inp, out):
+        p = oracle.particle_new(s, np.array(i, dtype=float))
+        assert list(oracle.coord_to_grid(s, p)) == o, i
+
+
+def test_histogram_bin_and_sum(oracle):
+    # src/distribution/distribution_test.rs:31-64: the sum over bins is the
+    # particle count; one particle at (0.6, 0.3, 0, 4, 1) lands in [2,1,0,1,0]
+    s = oracle.make_settings((5, 5, 1, 2, 2), (1.0, 1.0, 1.0))
+    rng = np.random.default_rng(1)
+    raw = np.column_stack([rng.random(1000), rng.random(1000), rng.random(1000), TWOPI * rng.random(1000),
+                           np.arccos(1 - 2 * rng.random(1000))])
+    p = np.array([oracle.particle_new(s, r) for r in raw])
+    d = oracle.histogram(s, p)
+    assert d.sum() == 1000.0
+    p2 = oracle.particle_new(s, np.array([0.6, 0.3, 0.0, 4.0, 1.0]))
+    d = oracle.histogram(s, p2[None])
+    assert d[2, 1, 0, 1, 0] == 1.0 and d.sum() == 1.0
+
+
+def test_sample_from_normalisation(oracle):
+    # src/distribution/distribution_test.rs:66-117
+    s = oracle.make_settings((5, 5, 1, 2, 2), (1.0, 1.0, 1.0))
+    rng = np.random.default_rng(2)
+    raw = np.column_stack([rng.random(1000), rng.random(1000), rng.random(1000), TWOPI * rng.random(1000),
+                           np.arccos(1 - 2 * rng.random(1000))])
+    p = np.array([oracle.particle_new(s, r) for r in raw])
+    gw = oracle.grid_width(s)
+    vol = gw[0] * gw[1] * gw[2] * gw[3] * gw[4]
+    d = oracle.sample_from(s, p)
+    assert equal_floats(vol * d.sum(), 1.0)
+    p2 = oracle.particle_new(s, np.array([0.6, 0.3, 0.0, 0.0, 0.0]))
+    d = oracle.sample_from(s, p2[None])
+    assert equal_floats(d[2, 1, 0, 0, 0] * vol, 1.0)
+
+
+# ---------------------------------------------------------------- k meshes
+def test_k_sampling(oracle):
+    # src/mesh/fft_helper_test.rs:13-60
+    e0 = [0., 1.0471975511965976, 2.0943951023931953, -3.1415926535897931, -2.0943951023931953, -1.0471975511965976]
+    e1 = [0., 0.8975979010256552, 1.7951958020513104, 2.6927937030769655, -2.6927937030769655, -1.7951958020513104,
+          -0.8975979010256552]
+    e2 = [0., 1., -1.]
+    for n, box, e in [(6, 6.0, e0), (7, 7.0, e1), (3, TWOPI, e2)]:
+        k = oracle.k_sampling(n, box)
+        for v, w in zip(k, e):
+            assert equal_floats(v, w)
+
+
+def test_k_mesh(oracle):
+    # src/mesh/fft_helper_test.rs:62-116: grid 4x3x2, box 2 pi (Nyquist negative)
+    s = oracle.make_settings((4, 3, 2, 1, 1), (TWOPI, TWOPI, TWOPI))
+    m = oracle.k_mesh(s)
+    kx, ky, kz = [0, 1, -2, -1], [0, 1, -1], [0, -1]
+    for i in range(4):
+        for j in range(3):
+            for l in range(2):
+                assert equal_floats(m[0, i, j, l], kx[i])
+                assert equal_floats(m[1, i, j, l], ky[j])
+                assert equal_floats(m[2, i, j, l], kz[l])
+
+
+def test_norm_k_mesh(oracle):
+    # src/mesh/fft_helper_test.rs:118-436: 4x4x4, box 2 pi, k/|k| with 0 at k = 0
+    s = oracle.make_settings((4, 4, 4, 1, 1), (TWOPI, TWOPI, TWOPI))
+    m = oracle.norm_k_mesh(s)
+    kk = np.array([0, 1, -2, -1], dtype=float)
+    K = np.stack(np.meshgrid(kk, kk, kk, indexing="ij"))
+    n2 = K[0] ** 2 + K[1] ** 2 + K[2] ** 2
+    with np.errstate(divide="ignore"):
+        inv = 1.0 / np.sqrt(n2)
+    inv[0, 0, 0] = 0.0
+    exp = K * inv
+    for v, e in zip(m.ravel(), exp.ravel()):
+        assert equal_floats(v, e)
+
+
+def test_inverse_norm_squared(oracle):
+    # src/mesh/fft_helper_test.rs:438-486
+    s = oracle.make_settings((4, 3, 2, 1, 1), (TWOPI, TWOPI, TWOPI))
+    got = oracle.inverse_norm_squared(s)
+    exp = np.array([[[0.0, 1.0], [1.0, 0.5], [1.0, 0.5]], [[1.0, 0.5], [0.5, 0.3333333333333333],
+                                                           [0.5, 0.3333333333333333]],
+                    [[0.25, 0.2], [0.2, 0.1666666666666667], [0.2, 0.1666666666666667]],
+                    [[1.0, 0.5], [0.5, 0.3333333333333333], [0.5, 0.3333333333333333]]])
+    for v, e in zip(got.ravel(), exp.ravel()):
+        assert equal_floats(v, e)
+
+
+# --------------------------------------------------------------- stress etc.
+def test_stress_kernel_golden(oracle):
+    # src/flowfield/stress_test.rs:82-122 + test/control/stress_kernel.bincode:
+    # active = magnetic = 1, 9 x 9 angle bins, compared after rounding x 1e12
+    s = oracle.make_settings((1, 1, 1, 9, 9), (1.0, 1.0, 1.0), active=1.0, magnetic=1.0)
+    sk = oracle.stress_kernel(s)
+    gold = np.load(os.path.join(GOLDEN, "stress_kernel.npy"))
+    for a, b in zip(sk.ravel(), gold.ravel()):
+        assert equal_floats(np.round(a * 1e12), np.round(b * 1e12))
+    assert np.abs(sk - gold).max() < 1e-30
+
+
+def test_flow_field_golden(oracle):
+    # src/flowfield/spectral_solver_test.rs:15-65 + test/flowfield/ff_test.bincode:
+    # one particle at the origin, phi = theta = pi/2, grid 11^5, box 11, active 1.
+    # The fixture was written before the screening term existed; it matches
+    # screening = 0 (the ignored reference test passes 1).
+    s = oracle.make_settings((11, 11, 11, 11, 11), (11.0, 11.0, 11.0), active=1.0)
+    p = oracle.particle_new(s, np.array([0.0, 0.0, 0.0, PI / 2, PI / 2]))
+    d = oracle.sample_from(s, p[None]) * (11.0 * 11.0 * 11.0)
+    u, _ = oracle.flow_field(s, d, 0.0)
+    gold = np.load(os.path.join(GOLDEN, "ff_test.npy"))
+    # FFT round-off (FFTW there, an own FFT here) leaves ~1e-16 of the field's
+    # maximum on every entry, so near-zero entries cannot agree relatively;
+    # the reference flags the test as non-deterministic for that reason.
+    assert rel_l2(u.real, gold) < 1e-15
+    assert np.abs(u.real - gold).max() < 1e-15 * np.abs(gold).max()
+
+
+def test_magnetic_golden_is_stale(oracle):
+    # test/magneticfield/b_test.bincode (magnetic_solver_test.rs:43-92, ignored
+    # in the reference) was produced by an older projection: P_k/3 - k^(k^.P_k)
+    # with the k = 0 mode zeroed.  The current code (magnetic_solver.rs:88-94)
+    # keeps k = 0 and has no 1/3.  This pins that reading of the fixture.
+    s = oracle.make_settings((11, 11, 11, 11, 11), (11.0, 11.0, 11.0))
+    p = oracle.particle_new(s, np.array([0.0, 0.0, 0.0, PI, PI / 2]))
+    d = oracle.sample_from(s, p[None]) * (11.0 ** 3)
+    gold = np.load(os.path.join(GOLDEN, "b_test.npy"))
+    b, _ = oracle.magnetic_field(s, d)
+    assert rel_l2(b.real, gold) > 1e-3  # the current code does not reproduce it
+    pol = oracle.director_field(s, d)
+    pk = np.stack([oracle.fft3d(pol[c], -1) for c in range(3)])
+    kn = oracle.norm_k_mesh(s)
+    old = pk / 3.0 - kn * (kn * pk).sum(axis=0)
+    old[:, 0, 0, 0] = 0.0
+    old = np.stack([oracle.fft3d(old[c], +1) for c in range(3)]) / 11.0 ** 3
+    assert rel_l2(old.real, gold) < 1e-14
+
+
+def test_polarization_two_particles(oracle):
+    # src/polarization/director_test.rs:9-73
+    s = oracle.make_settings((3, 3, 1, 35, 5), (3.0, 3.0, 1.0))
+    p1 = oracle.particle_new(s, np.array([0.0, 0.0, 0.0, PI, PI / 2]))
+    p2 = oracle.particle_new(s, np.array([1.5, 2.5, 0.0, 0.269279370307697, 0.942477796076938]))
+    d = oracle.sample_from(s, np.stack([p1, p2]))
+    f = oracle.director_field(s, d)
+    n = 2.0
+    assert f[0, 0, 0, 0].real == -1.0 / n
+    assert np.round(f[1, 0, 0, 0].real * 10e14) == 0.0
+    assert np.round(f[2, 0, 0, 0].real * 10e14) == 0.0
+    f[:, 0, 0, 0] = 0.0
+    assert equal_floats(f[0, 1, 2, 0].real, 0.7798623362492354 / n)
+    assert equal_floats(f[1, 1, 2, 0].real, 0.2152283291933436 / n)
+    assert equal_floats(f[2, 1, 2, 0].real, 0.5877852522924731 / n)
+    f[:, 1, 2, 0] = 0.0
+    assert np.all(f == 0.0)
+
+
+def test_magnetic_vector_gradient(oracle):
+    # src/magnetic_interaction/magnetic_solver_test.rs:94-156: the gradient of
+    # the cosine mode B_x = cos(x) on a 10^3 grid, box 2 pi
+    s = oracle.make_settings((10, 10, 10, 1, 1), (TWOPI, TWOPI, TWOPI))
+    b = np.zeros((3, 10, 10, 10), dtype=np.complex128)
+    b[0, 1, 0, 0] = -0.5j
+    b[0, 9, 0, 0] = 0.5j
+    g = oracle.vector_gradient(s, b)
+    exp = np.array([1., 0.8090169943749475, 0.30901699437494745, -0.30901699437494745, -0.8090169943749475, -1.,
+                    -0.8090169943749475, -0.30901699437494745, 0.30901699437494745, 0.8090169943749475])
+    # FFTW gives these exactly; the own FFT agrees to one ulp
+    assert np.abs(g[0, 0, :, 0, 0] - exp).max() <= 2 * EPS
+    for a, bb in [(1, 0), (0, 1), (1, 1)]:
+        assert np.abs(g[a, bb, :, 0, 0]).max() <= 1e-16
+        assert np.abs(g[a, bb, 0, :, 0]).max() <= 1e-16
+        assert np.abs(g[a, bb, 0, 0, :]).max() <= 1e-16
+    assert np.abs(g[0, 0, 0, :, 0] - 1.0).max() <= 2 * EPS
+    assert np.abs(g[0, 0, 0, 0, :] - 1.0).max() <= 2 * EPS
+
+
+# --------------------------------------------------------- Langevin modifiers
+BS = (10.0, 10.0, 10.0)
+
+
+def _p(oracle, *c):
+    return oracle.particle_new(oracle.make_settings((1, 1, 1, 1, 1), BS), np.array(c, dtype=float))
+
+
+MODIFIER_KATS = [
+    # (mask name, kwargs, start particle, expected particle); modifiers_test.rs:39-97
+    ("SELF_PROPULSION", {}, (0, 0, 0, 0, 0), (0., 0., 1., 0., 0.)),
+    ("CONVECTION", {"flow": [1., 1., 0.]}, (0, 0, 0, 0, 0), (1., 1., 0., 0., 0.)),
+    ("MDD_FORCE", {"drag": 0.1, "gradb": [[0, 0, 1], [0, 0, 1], [0, 0, 1]]}, (0, 0, 0, 0, 0), (0.1, 0.1, 0.1, 0., 0.)),
+    ("TRANS_DIFFUSION", {"xi": [1., 1., 0.], "diff": 1.0}, (0, 0, 0, 0, 0), (1., 1., 0., 0., 0.)),
+    ("EXTERNAL_FIELD", {"reorientation": 0.1}, (0, 0, 0, 0, PI / 2), (0., 0., 0., 0.09966865249116204, PI / 2)),
+    ("JEFFREY_VORTICITY", {"vort": [[0, 0, -0.01], [0, 0, 0], [0.01, 0, 0]]}, (0, 0, 0, 0, 0),
+     (0., 0., 0., 0., 0.009999666686665076)),
+    # the reference's "jeffrey_strain" test runs jeffrey_vorticity (modifiers_test.rs:81-82)
+    ("JEFFREY_VORTICITY", {"vort": [[0, 0, 0.01], [0, 0, 0.02], [0.01, 0.02, 0]]}, (0, 0, 0, 0, 0),
+     (0., 0., 0., 4.2487413713838835, 0.022356954112670246)),
+    ("MDD_ROTATION", {"b": [0.01, 0., 0.]}, (0, 0, 0, 0, 0), (0., 0., 0., 0., 0.009999666686665076)),
+    ("ROT_DIFFUSION", {"axis_angle": 0.0, "rotate_angle": 0.1}, (0, 0, 0, 0, 0), (0., 0., 0., 0., 0.09999999999999987)),
+]
+
+
+@pytest.mark.parametrize("name,kw,start,expect", MODIFIER_KATS)
+def test_modifier_kat(oracle, name, kw, start, expect):
+    got = oracle.langevin(_p(oracle, *start), getattr(oracle, name), box=BS, **kw)
+    want = _p(oracle, *expect)
+    assert np.array_equal(got, want), (got, want)
+
+
+def test_builder_conversion_identity(oracle):
+    # src/integrators/langevin_builder/mod_test.rs:13-56: new -> identity -> finalize == p
+    for c in [[0, 0, 0, 0, 0], [0, 0, 0, 0, PI / 2], [0, 0, 0, 0, PI], [1, 2, 3, 0, 0], [0, 5, 0, PI / 2, PI / 2]]:
+        p = _p(oracle, *c)
+        assert np.array_equal(oracle.langevin(p, 0, box=BS), p), c
+
+
+# ------------------------------------------------------------------- FFT
+@pytest.mark.parametrize("shape", [(11, 11, 11), (8, 6, 1), (20, 20, 20), (7, 3, 5), (1, 1, 1), (32, 32, 1), (2, 9, 4)])
+def test_fft_matches_numpy(oracle, shape):
+    rng = np.random.default_rng(sum(shape))
+    a = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    f = oracle.fft3d(a, -1)
+    assert rel_l2(f, np.fft.fftn(a)) < 1e-14
+    b = oracle.fft3d(a, +1)
+    assert rel_l2(b, np.fft.ifftn(a) * a.size) < 1e-14
+
+
+# ------------------------------------------------------------- a full step
+def test_step_reference_semantics(oracle):
+    """One oracle step against an independent numpy restatement of the same
+    step (numpy FFTs), for a small 3-D case with every term switched on."""
+    s = oracle.make_settings((6, 5, 4, 6, 4), (3.0, 2.5, 2.0), timestep=0.01, trans_diff=0.3, rot_diff=0.7,
+                             active=-1.3, magnetic=0.4, shape=0.6, magnetic_drag=0.2, hydro_screening=0.1,
+                             volume_exclusion=0.05, magnetic_reorientation=0.8, magnetic_dipole_dipole=0.5)
+    n = 400
+    rng = np.random.default_rng(7)
+    raw = np.column_stack([3 * rng.random(n), 2.5 * rng.random(n), 2 * rng.random(n), TWOPI * rng.random(n),
+                           np.arccos(1 - 2 * rng.random(n))])
+    noise = np.column_stack([rng.standard_normal((n, 3)), TWOPI * rng.random(n),
+                             np.sqrt(2 * 0.7 * 0.01) * np.sqrt(-2 * np.log(1 - rng.random(n)))])
+    sim = oracle.Simulation(s, n)
+    sim.init(raw)
+    p0 = sim.particles()
+    d = sim.distribution()
+    assert np.isclose(d.sum() * np.prod(oracle.grid_width(s)), 3.0 * 2.5 * 2.0)
+    sim.do_timestep(noise)
+    u, g = oracle.flow_field(s, d, 0.1)
+    assert rel_l2(sim.flow(), u) == 0.0
+    assert rel_l2(sim.flow_grad(), g) == 0.0
+    # numpy restatement of the flow solve
+    gw = oracle.grid_width(s)
+    K = oracle.stress_kernel(s).reshape(9, -1)
+    dd = d.reshape(s.gx * s.gy * s.gz, -1)
+    sig = (K @ dd.T * (gw[3] * gw[4])).reshape(3, 3, s.gx, s.gy, s.gz)
+    sk = np.fft.fftn(sig, axes=(2, 3, 4))
+    k = oracle.k_mesh(s)
+    kn = oracle.norm_k_mesh(s)
+    ik2 = oracle.inverse_norm_squared(s)
+    sk_k = np.einsum("ijxyz,jxyz->ixyz", sk, k)
+    ks = (kn * sk_k).sum(0)
+    uk = 1j * (sk_k - kn * ks) * (ik2 + 0.1) / (s.gx * s.gy * s.gz)
+    gk = 1j * k[:, None] * uk[None, :]
+    u_np = np.fft.ifftn(uk, axes=(1, 2, 3)) * (s.gx * s.gy * s.gz)
+    g_np = np.fft.ifftn(gk, axes=(2, 3, 4)) * (s.gx * s.gy * s.gz)
+    assert rel_l2(u, u_np) < 1e-13
+    assert rel_l2(g, g_np) < 1e-13
+    p1 = sim.particles()
+    assert p1.shape == p0.shape and np.all(np.isfinite(p1))
+    assert np.all((p1[:, 0] >= 0) & (p1[:, 0] < 3.0)) and np.all((p1[:, 4] >= 0) & (p1[:, 4] <= PI))
