@@ -15,7 +15,7 @@ EXPORTS = [
     "ss_get_particles", "ss_get_distribution", "ss_get_counts", "ss_get_flow_field", "ss_get_magnetic_field",
     "ss_get_flow_complex", "ss_get_magnetic_complex", "ss_get_timestep", "ss_mean_flow_field",
     "ss_mean_magnetic_field", "ss_langevin", "ss_profile_enable", "ss_profile_read", "ss_launch_count",
-    "ss_last_error", "ss_version",
+    "ss_sample_distribution_noalloc", "ss_last_error", "ss_version",
 ]
 
 SS_OK = 0
@@ -115,6 +115,7 @@ def load(build_if_missing=True):
         "ss_profile_enable": [vp, ci],
         "ss_profile_read": [vp, dp, u64p],
         "ss_launch_count": [vp, u64p],
+        "ss_sample_distribution_noalloc": [ctypes.POINTER(Grid), ctypes.POINTER(Box), vp, u64, vp, vp],
         "ss_last_error": [vp, ctypes.c_char_p, ctypes.c_size_t],
     }
     for name, args in sig.items():

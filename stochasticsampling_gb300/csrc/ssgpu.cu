@@ -36,6 +36,11 @@ struct Timing {
 
 }  // namespace
 
+namespace ss {
+// context-free error text for entry points outside this file
+void record_error(const char *msg) { g_last_error = msg; }
+}  // namespace ss
+
 struct ss_ctx {
     ss_grid grid{};
     ss_box box{};
