@@ -173,6 +173,64 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def measure_mixed(args, stream, p0, rank, world, dist, barrier):
+    """The FP32 mixed-precision path on the same workload: throughput over K
+    graph-replayed steps, and each field's error against the FP64 path after
+    one step from identical state and noise."""
+    import torch
+
+    import stochasticsampling_gb300 as ss
+    params = dict(PARAMS, number_of_particles=N, seed=1 + rank)
+    sim = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True, mixed=True, stream=stream.cuda_stream)
+    sim.init(p0)
+    with torch.cuda.stream(stream):
+        sim.run(args.warmup)
+        torch.cuda.synchronize()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.run(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1)
+    sim.profile(True)
+    sim.run(min(args.steps, 20))
+    stage_ms, nprof = sim.profile_read()
+    sim.profile(False)
+    t = torch.tensor([ms], dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    value = world * N * args.steps / (float(t[0]) / 1e3)
+    # errors against the FP64 path (itself within 1e-15 of the FP64 oracle)
+    start = sim.get_particles()
+    sim.close()
+    m = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True, mixed=True)
+    d = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True)
+    m.init(start)
+    d.init(start)
+    cm, cd = m.get_counts().astype(np.float64), d.get_counts().astype(np.float64)
+    noise = m.noise(0)
+    m.do_timestep()
+    d.do_timestep(noise)
+    um, ud = m.get_flow_field(), d.get_flow_field()
+    pm, pd = m.get_particles(), d.get_particles()
+    disp = np.linalg.norm((pd - start)[:, :2])
+    dphi = np.abs(pm[:, 3] - pd[:, 3])
+    dphi = np.minimum(dphi, 2 * np.pi - dphi)
+    errors = {
+        "histogram_l1_rel": float(np.abs(cm - cd).sum() / cd.sum()),
+        "flow_l2_rel": float(np.linalg.norm(um - ud) / np.linalg.norm(ud)),
+        "position_l2_rel_to_displacement": float(np.linalg.norm((pm - pd)[:, :2]) / disp),
+        "phi_rms_rad": float(np.sqrt(np.mean(dphi ** 2))),
+    }
+    m.close()
+    d.close()
+    return {"value": value, "unit": UNIT, "ms_per_step": float(t[0]) / args.steps, "dtype": "f32 + f64 positions",
+            "stage_ms": {k: v / max(1, nprof) for k, v in stage_ms.items()},
+            "errors_vs_fp64_one_step": errors}
+
+
 def run_gpu(args, rank, world, dist):
     import torch
 
@@ -244,6 +302,7 @@ def run_gpu(args, rank, world, dist):
         dist.all_reduce(te, op=dist.ReduceOp.MAX)
     e2e_value = world * N * e2e_steps / float(te[0])
     sim.close()
+    mixed = None if args.no_mixed else measure_mixed(args, stream, p0, rank, world, dist, barrier)
 
     if rank != 0:
         return
@@ -297,6 +356,7 @@ def run_gpu(args, rank, world, dist):
         "gpu_launches": launches,
         "clocks": clk,
         "cpu_baseline": cpu,
+        "mixed": mixed,
     }
     print(json.dumps(line), flush=True)
 
@@ -304,10 +364,11 @@ def run_gpu(args, rank, world, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the FP32 mixed-precision measurement")
     ap.add_argument("--particles", type=int, default=None,
                     help="override N (profiling a smaller case of the same workload)")
     args = ap.parse_args()

@@ -66,6 +66,9 @@ typedef struct {
 #define SS_FLAG_ALWAYS_MAGNETIC 2u /* run the dipolar solver even when its couplings are zero */
 #define SS_FLAG_NO_SORT 4u         /* keep particles in input order (no counting sort by cell) */
 #define SS_FLAG_NO_GRAPH 8u        /* launch kernels directly instead of replaying a CUDA graph */
+#define SS_FLAG_MIXED 16u          /* FP32 mixed precision: FP64 positions and k = 0 / mean handling, FP32
+                                      angles, binning, contraction, FFTs, fields and Langevin arithmetic
+                                      (no sort; the library seams ss_mean_* need the FP64 mode) */
 
 typedef struct ss_ctx ss_ctx;
 
@@ -85,6 +88,14 @@ int ss_init(ss_ctx *ctx, const double *particles, uint64_t n);
  * counter based (Philox4x32-10 keyed by seed, counter = (particle, timestep)),
  * so restoring the timestep restores the noise exactly. */
 int ss_resume(ss_ctx *ctx, const double *particles, uint64_t n, uint64_t timestep);
+
+/* init_simulation with InitType::Distribution (src/bin/init.rs:93-116):
+ * samples the initial particles on the device and then behaves like ss_init.
+ * kind 0 = Isotropic (Particle::create_isotropic, src/particle.rs:241-256),
+ * kind 1 = Homogeneous (Particle::create_homogeneous, :280-295, with
+ * kappa = magnetic_reorientation / rotational diffusion).  The draws come from
+ * Philox keyed by seed (the reference uses Pcg64Mcg). */
+int ss_init_distribution(ss_ctx *ctx, uint32_t kind);
 
 /* Simulation::do_timestep, src/bin/simulation/mod.rs:251-374.
  * noise: NULL -> on-device Philox noise; otherwise [n][5] host doubles
@@ -114,8 +125,9 @@ int ss_get_distribution(ss_ctx *ctx, double *out);
 int ss_get_counts(ss_ctx *ctx, uint32_t *out);
 /* Simulation::get_flow_field (:236-238): Re(u), [3][x][y][z] */
 int ss_get_flow_field(ss_ctx *ctx, double *out);
-/* Simulation::get_magnetic_field (:241-243): Re(B), [3][x][y][z]
- * (zeros while the dipolar solver is skipped) */
+/* Simulation::get_magnetic_field (:241-243): Re(B), [3][x][y][z].  When the
+ * step skipped the dipolar solve (both couplings zero), it is computed here on
+ * demand from the histogram of the last step, which is still resident. */
 int ss_get_magnetic_field(ss_ctx *ctx, double *out);
 /* the complex views returned by SpectralSolver::mean_flow_field
  * (src/flowfield/spectral_solver.rs:233-254): u [3][x][y][z], grad [3][3][x][y][z] */

@@ -11,7 +11,7 @@ LIB_PATH = os.path.join(HERE, "libssgpu.so")
 
 # every symbol that include/ssgpu.h declares
 EXPORTS = [
-    "ss_create", "ss_destroy", "ss_init", "ss_resume", "ss_do_timestep", "ss_run", "ss_noise", "ss_synchronize",
+    "ss_create", "ss_destroy", "ss_init", "ss_init_distribution", "ss_resume", "ss_do_timestep", "ss_run", "ss_noise", "ss_synchronize",
     "ss_get_particles", "ss_get_distribution", "ss_get_counts", "ss_get_flow_field", "ss_get_magnetic_field",
     "ss_get_flow_complex", "ss_get_magnetic_complex", "ss_get_timestep", "ss_mean_flow_field",
     "ss_mean_magnetic_field", "ss_langevin", "ss_profile_enable", "ss_profile_read", "ss_launch_count",
@@ -30,6 +30,7 @@ FLAG_QUASI2D = 1
 FLAG_ALWAYS_MAGNETIC = 2
 FLAG_NO_SORT = 4
 FLAG_NO_GRAPH = 8
+FLAG_MIXED = 16
 
 NUM_STAGES = 8
 STAGES = ["contract", "fft_forward", "kspace", "fft_inverse", "table", "update", "sort", "other"]
@@ -97,6 +98,7 @@ def load(build_if_missing=True):
         "ss_destroy": [vp],
         "ss_init": [vp, dp, u64],
         "ss_resume": [vp, dp, u64, u64],
+        "ss_init_distribution": [vp, u32],
         "ss_do_timestep": [vp, dp, u64p],
         "ss_run": [vp, u64, u64p],
         "ss_noise": [vp, u64, dp],

@@ -145,10 +145,11 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
     return c;
 }
 
-// 53-bit uniform in [0, 1) from two 32-bit words
-__device__ __forceinline__ double u53(uint32_t hi, uint32_t lo) {
-    unsigned long long m = ((unsigned long long)hi << 21) ^ (unsigned long long)(lo >> 11);
-    return (double)m * 0x1p-53;
+// A double in [1, 2) whose 52 mantissa bits come from two 32-bit words,
+// assembled with integer operations (no FP64 conversion).  x - 1 is a uniform
+// in [0, 1) and 2 - x one in (0, 1], both exact.
+__device__ __forceinline__ double u12(uint32_t hi, uint32_t lo) {
+    return __hiloint2double((int)(0x3FF00000u | (hi >> 12)), (int)((hi << 20) | (lo >> 12)));
 }
 
 // Noise of particle `id` at step `t`: the RandomVector of
@@ -164,24 +165,25 @@ __device__ __forceinline__ void philox_noise(unsigned long long seed, uint32_t i
     uint32_t tl = (uint32_t)t, th = (uint32_t)(t >> 32);
     uint4 r0 = philox4x32_10(make_uint4(id, tl, th, 0u), key);
     uint4 r1 = philox4x32_10(make_uint4(id, tl, th, 1u), key);
-    double u1 = u53(r0.x, r0.y), u2 = u53(r0.z, r0.w);
-    double rad = sqrt(-2.0 * log(1.0 - u1));
+    // x in [1, 2): U = x - 1, 1 - U = 2 - x, 2 U = 2 x - 2 (all exact)
+    double x1 = u12(r0.x, r0.y), x2 = u12(r0.z, r0.w);
+    double rad = sqrt(-2.0 * log(2.0 - x1));
     double s, c;
-    sincospi(2.0 * u2, &s, &c);
+    sincospi(2.0 * x2 - 2.0, &s, &c);
     xi[0] = rad * c;
     xi[1] = rad * s;
     if (Q2D) {
         xi[2] = 0.0;  // overwritten position z: never read
     } else {
         uint4 r2 = philox4x32_10(make_uint4(id, tl, th, 2u), key);
-        double u5 = u53(r2.x, r2.y), u6 = u53(r2.z, r2.w);
-        double rad2 = sqrt(-2.0 * log(1.0 - u5));
-        xi[2] = rad2 * cospi(2.0 * u6);
+        double x5 = u12(r2.x, r2.y), x6 = u12(r2.z, r2.w);
+        double rad2 = sqrt(-2.0 * log(2.0 - x5));
+        xi[2] = rad2 * cospi(2.0 * x6 - 2.0);
     }
-    double u3 = u53(r1.x, r1.y), u4 = u53(r1.z, r1.w);
-    sincospi(2.0 * u3, &sa, &ca);
-    rot = sigma * sqrt(-2.0 * log(1.0 - u4));
-    if (WANT_ALPHA) *alpha = kTwoPi * u3;
+    double x3 = u12(r1.x, r1.y), x4 = u12(r1.z, r1.w);
+    sincospi(2.0 * x3 - 2.0, &sa, &ca);
+    rot = sigma * sqrt(-2.0 * log(2.0 - x4));
+    if (WANT_ALPHA) *alpha = kTwoPi * (x3 - 1.0);
 }
 
 // ---- the Langevin chain ------------------------------------------------
@@ -251,7 +253,12 @@ __device__ __forceinline__ void langevin(double &x, double &y, double &z, double
         sincos(theta, &st, &ct);
     }
     // CosSinOrientation::to_orientation_vector, particle.rs:165-172
+    // (with sin(theta) == 1 exactly, the products are cp and sp exactly)
     double n[3] = {st * cp, st * sp, ct};
+    if (have_theta && st == 1.0) {
+        n[0] = cp;
+        n[1] = sp;
+    }
     double dp[3] = {0.0, 0.0, 0.0}, dn[3] = {0.0, 0.0, 0.0};
 
     if (mask & M_SELF_PROPULSION) {  // modifiers.rs:39-46
@@ -306,26 +313,26 @@ __device__ __forceinline__ void langevin(double &x, double &y, double &z, double
 #pragma unroll
         for (int k = 0; k < 3; ++k) dp[k] = dp[k] + xi[k] * diff;
     }
-    if (mask & M_ROT_DIFFUSION) {  // modifiers.rs:199-231, quaternion 0.3.1
+    if (mask & M_ROT_DIFFUSION) {  // modifiers.rs:199-231
+        // Rotation axis k perpendicular to n (modifiers.rs:205-215).  The
+        // reference rotates with the quaternion q n q* of
+        // quaternion::axis_angle(k, rot) (quaternion 0.3.1); for a unit k
+        // perpendicular to n that rotation is n cos(rot) + (k x n) sin(rot)
+        // (Rodrigues), which needs one sincos and a cross product instead of
+        // two quaternion products.  The delta R n - n is formed as
+        // n (cos - 1) + (k x n) sin, without the cancellation of R n - n.
         double ax0 = (cp * ct) * sa - ca * sp;
         double ax1 = ca * cp + (ct * sa) * sp;
         double ax2 = (-sa) * st;
-        double sh, ch;
-        sincos(rot / 2.0, &sh, &ch);  // axis_angle: half angle
-        double q0 = ch, q1 = ax0 * sh, q2 = ax1 * sh, q3 = ax2 * sh;
-        // t = q * (0, n):  (q0*0 - q.n,  (n*q0 + q*0) + q x n)
-        double t0 = q0 * 0.0 - ((q1 * n[0] + q2 * n[1]) + q3 * n[2]);
-        double t1 = (n[0] * q0 + q1 * 0.0) + (q2 * n[2] - q3 * n[1]);
-        double t2 = (n[1] * q0 + q2 * 0.0) + (q3 * n[0] - q1 * n[2]);
-        double t3 = (n[2] * q0 + q3 * 0.0) + (q1 * n[1] - q2 * n[0]);
-        // r = t * conj(q), conj(q) = (q0, -q):  ((-q)*t0 + t*q0) + t x (-q)
-        double c1 = -q1, c2 = -q2, c3 = -q3;
-        double r1 = (c1 * t0 + t1 * q0) + (t2 * c3 - t3 * c2);
-        double r2 = (c2 * t0 + t2 * q0) + (t3 * c1 - t1 * c3);
-        double r3 = (c3 * t0 + t3 * q0) + (t1 * c2 - t2 * c1);
-        dn[0] = dn[0] + (r1 - n[0]);
-        dn[1] = dn[1] + (r2 - n[1]);
-        dn[2] = dn[2] + (r3 - n[2]);
+        double sr, cr;
+        sincos(rot, &sr, &cr);
+        double cm1 = cr - 1.0;
+        double k0 = ax1 * n[2] - ax2 * n[1];
+        double k1 = ax2 * n[0] - ax0 * n[2];
+        double k2 = ax0 * n[1] - ax1 * n[0];
+        dn[0] = dn[0] + (n[0] * cm1 + k0 * sr);
+        dn[1] = dn[1] + (n[1] * cm1 + k1 * sr);
+        dn[2] = dn[2] + (n[2] * cm1 + k2 * sr);
     }
     // finalize: Particle::from(old + delta) then pbc (mod.rs:121-125)
     double px = x + dp[0], py = y + dp[1], pz = z + dp[2];

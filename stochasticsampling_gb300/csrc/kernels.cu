@@ -324,6 +324,54 @@ __global__ void __launch_bounds__(256) k_update(DevParams P, double *__restrict_
 
 __global__ void k_step_inc(unsigned long long *d_step) { *d_step += 1ull; }
 
+// Initial conditions: Particle::create_isotropic / create_homogeneous
+// (src/particle.rs:224-295) with Philox draws (counter (i, ~0, ~0, 3..5),
+// outside the range the steps use) instead of Pcg64Mcg.  Rows are written in
+// the boundary layout [n][5]; the caller then ingests them like ss_init.
+template <bool HOMOGENEOUS>
+__global__ void k_sample_initial(DevParams P, double kappa, double *__restrict__ aos, uint32_t *__restrict__ errflag) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    uint2 key = make_uint2((uint32_t)P.seed, (uint32_t)(P.seed >> 32));
+    uint4 a = philox4x32_10(make_uint4((uint32_t)i, 0xFFFFFFFFu, 0xFFFFFFFFu, 3u), key);
+    uint4 b = philox4x32_10(make_uint4((uint32_t)i, 0xFFFFFFFFu, 0xFFFFFFFFu, 4u), key);
+    uint4 c = philox4x32_10(make_uint4((uint32_t)i, 0xFFFFFFFFu, 0xFFFFFFFFu, 5u), key);
+    double u[5] = {u12(a.x, a.y) - 1.0, u12(a.z, a.w) - 1.0, u12(b.x, b.y) - 1.0, u12(b.z, b.w) - 1.0,
+                   u12(c.x, c.y) - 1.0};
+    double x = P.bx * u[0], y = P.by * u[1], z = P.bz * u[2], phi = kTwoPi * u[3], theta;
+    if (!HOMOGENEOUS) {
+        theta = acos(1.0 - 2.0 * u[4]);  // pdf_sin(2 r), particle.rs:340-342
+    } else {
+        // pdf_homogeneous_fixpoint, particle.rs:347-360
+        theta = acos(log(exp(kappa) - 2.0 * u[4] * sinh(kappa)) / kappa);
+        if (theta != theta) atomicOr(errflag, ERR_NONFINITE);
+    }
+    // Particle::new: modulo / ang_pbc, then pbc
+    x = ref_modulo(ref_modulo(x, P.bx), P.bx);
+    y = ref_modulo(ref_modulo(y, P.by), P.by);
+    z = ref_modulo(ref_modulo(z, P.bz), P.bz);
+    ref_ang_pbc(phi, theta);
+    ref_ang_pbc(phi, theta);
+    if (HOMOGENEOUS) {
+        // rotate the orientation by -pi/2 about x (place_homogeneous,
+        // particle.rs:271-276; Rodrigues with k = (1, 0, 0)), then
+        // Orientation::from_vector_mut
+        double sp, cp, st, ct;
+        sincos(phi, &sp, &cp);
+        sincos(theta, &st, &ct);
+        double n0 = st * cp, n1 = st * sp, n2 = ct;
+        double sr, cr;
+        sincos(-kPiHalf, &sr, &cr);
+        double r0 = n0;  // the component along the axis is unchanged
+        double r1 = n1 * cr - n2 * sr;
+        double r2 = n2 * cr + n1 * sr;
+        phi = atan2(r1, r0);
+        theta = kPiHalf - atan2(r2, sqrt(r0 * r0 + r1 * r1));
+    }
+    double *p = aos + 5 * i;
+    p[0] = x; p[1] = y; p[2] = z; p[3] = phi; p[4] = theta;
+}
+
 // the Philox noise of step t for every particle, as RandomVector rows in the
 // caller's order
 template <bool Q2D>
@@ -506,6 +554,13 @@ void launch_update(cudaStream_t s, bool q2d, bool mag, bool host_noise, const De
 }
 
 void launch_step_inc(cudaStream_t s, unsigned long long *d_step) { k_step_inc<<<1, 1, 0, s>>>(d_step); }
+
+void launch_sample_initial(cudaStream_t s, bool homogeneous, const DevParams &P, double kappa, double *aos,
+                           uint32_t *err) {
+    if (!P.n) return;
+    if (homogeneous) k_sample_initial<true><<<nblocks(P.n, 256), 256, 0, s>>>(P, kappa, aos, err);
+    else k_sample_initial<false><<<nblocks(P.n, 256), 256, 0, s>>>(P, kappa, aos, err);
+}
 
 void launch_noise(cudaStream_t s, bool q2d, const DevParams &P, unsigned long long t, double *out) {
     if (!P.n) return;

@@ -24,6 +24,8 @@ void launch_update(cudaStream_t s, bool q2d, bool mag, bool host_noise, const De
                    uint32_t *key, const uint32_t *id, const double *table, const double *noise,
                    const unsigned long long *d_step, uint32_t *counts_next, uint32_t *err);
 void launch_step_inc(cudaStream_t s, unsigned long long *d_step);
+void launch_sample_initial(cudaStream_t s, bool homogeneous, const DevParams &P, double kappa, double *aos,
+                           uint32_t *err);
 void launch_noise(cudaStream_t s, bool q2d, const DevParams &P, unsigned long long t, double *out);
 void launch_scan(cudaStream_t s, const uint32_t *cnt, int n, uint32_t *out);
 void launch_scatter(cudaStream_t s, unsigned long long n, double *const src[5], const uint32_t *key,

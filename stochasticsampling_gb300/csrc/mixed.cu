@@ -1,0 +1,535 @@
+// mixed.cu -- the FP32 mixed-precision timestep (SS_FLAG_MIXED).
+//
+// Positions x, y, z stay FP64 and are accumulated in FP64.  Orientations,
+// binning, the angular contraction, the FFTs, the k-space solve, the field
+// table and the Langevin arithmetic are FP32.  The spectral solve keeps its
+// k = 0 / mean handling in FP64: the per-component means of the stress and
+// polarisation fields are summed in FP64 and removed before the FP32 FFT (so
+// the transform only sees the fluctuations), and the mean dipolar field
+// B_0 = <P> (the kept k = 0 mode, magnetic_solver.rs:88-94) is added back in
+// FP64.  The mean flow is exactly zero (its k = 0 mode is multiplied by k).
+//
+// Layout: particles x, y, z f64 SoA + phi, theta f32 SoA (+ key, id as in the
+// FP64 path); spectra float2; table rows of 16 (32 with dipolar terms) floats.
+#include "mixed.cuh"
+
+namespace ss {
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float kval_f(int i, int n, float step) {
+    int b = (n % 2 == 0) ? n / 2 : n / 2 + 1;
+    return (float)(i < b ? i : i - n) * step;
+}
+
+// floor(v / w) in FP32 with the `== n -> n - 1` clamp of coord_to_grid
+__device__ __forceinline__ int bin_f(float v, float iw, int n) {
+    float f = floorf(v * iw);
+    int i = (int)f;
+    i = i < 0 ? 0 : i;
+    return i >= n ? n - 1 : i;
+}
+
+__device__ __forceinline__ float modulo_f(float f, float m) {
+    float r = fmodf(f, m);
+    return r < 0.0f ? r + fabsf(m) : r;
+}
+
+__device__ __forceinline__ void bin_mixed(const MixedParams &M, double x, double y, double z, float phi, float theta,
+                                          uint32_t &cell, unsigned long long &bin) {
+    int ix = bin_f((float)x, M.igwf[0], M.gx);
+    int iy = bin_f((float)y, M.igwf[1], M.gy);
+    int iz = bin_f((float)z, M.igwf[2], M.gz);
+    int ip = bin_f(phi, M.igwf[3], M.gphi);
+    int it = bin_f(theta, M.igwf[4], M.gtheta);
+    cell = (uint32_t)((ix * M.gy + iy) * M.gz + iz);
+    bin = (unsigned long long)cell * (unsigned long long)M.nang + (unsigned long long)(ip * M.gtheta + it);
+}
+
+// Particle::new in FP64, then the angles rounded to FP32
+__global__ void k_ingest_m(const double *__restrict__ aos, unsigned long long n, DevParams P, double *__restrict__ x,
+                           double *__restrict__ y, double *__restrict__ z, float *__restrict__ phi,
+                           float *__restrict__ theta, uint32_t *__restrict__ id) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *p = aos + 5 * i;
+    double px = ref_modulo(p[0], P.bx), py = ref_modulo(p[1], P.by), pz = ref_modulo(p[2], P.bz);
+    double ph = p[3], th = p[4];
+    ref_ang_pbc(ph, th);
+    px = ref_modulo(px, P.bx);
+    py = ref_modulo(py, P.by);
+    pz = ref_modulo(pz, P.bz);
+    ref_ang_pbc(ph, th);
+    x[i] = px; y[i] = py; z[i] = pz; phi[i] = (float)ph; theta[i] = (float)th;
+    id[i] = (uint32_t)i;
+}
+
+__global__ void k_egest_m(unsigned long long n, const double *__restrict__ x, const double *__restrict__ y,
+                          const double *__restrict__ z, const float *__restrict__ phi,
+                          const float *__restrict__ theta, const uint32_t *__restrict__ id, double *__restrict__ aos) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double *p = aos + 5 * (unsigned long long)id[i];
+    p[0] = x[i]; p[1] = y[i]; p[2] = z[i]; p[3] = (double)phi[i]; p[4] = (double)theta[i];
+}
+
+__global__ void k_bin_m(unsigned long long n, MixedParams M, const double *__restrict__ x,
+                        const double *__restrict__ y, const double *__restrict__ z, const float *__restrict__ phi,
+                        const float *__restrict__ theta, uint32_t *__restrict__ key, uint32_t *__restrict__ counts) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t cell;
+    unsigned long long bin;
+    bin_mixed(M, x[i], y[i], z[i], phi[i], theta[i], cell, bin);
+    atomicAdd(counts + bin, 1u);
+    key[i] = cell;
+}
+
+// angular contraction in FP32 (warp per cell); per-component sums of the
+// result accumulated in FP64 for the mean handling
+template <bool STRESS, bool MAG>
+__global__ void __launch_bounds__(256) k_contract_m(const uint32_t *__restrict__ counts,
+                                                    const float *__restrict__ lut, int lut_n,
+                                                    const float *__restrict__ kern, MixedParams M,
+                                                    float2 *__restrict__ fwd, float *__restrict__ table, int tstride,
+                                                    double *__restrict__ sums) {
+    int cell = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+    int lane = threadIdx.x & 31;
+    if (cell >= M.ncell) return;
+    const int na = M.nang;
+    float acc[13];
+#pragma unroll
+    for (int j = 0; j < 13; ++j) acc[j] = 0.f;
+    for (int a = lane; a < na; a += 32) {
+        uint32_t c = counts[(long long)cell * na + a];
+        float f = ((int)c < lut_n) ? __ldg(lut + c) : (float)(((double)c / M.dist_den) * M.volume);
+        if (STRESS) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) acc[j] = fmaf(__ldg(kern + j * na + a), f, acc[j]);
+        }
+        if (MAG) {
+#pragma unroll
+            for (int j = 9; j < 12; ++j) acc[j] = fmaf(__ldg(kern + j * na + a), f, acc[j]);
+        }
+        acc[12] += f;
+    }
+#pragma unroll
+    for (int j = 0; j < 13; ++j)
+        if ((j < 9 && STRESS) || (j >= 9 && j < 12 && MAG) || j == 12) acc[j] = warp_sum_f(acc[j]);
+    if (lane == 0) {
+        const int nc = M.ncell;
+        if (STRESS) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) {
+                float v = acc[j] * M.measure;
+                fwd[(long long)j * nc + cell] = make_float2(v, 0.f);
+                atomicAdd(sums + j, (double)v);
+            }
+        }
+        if (MAG) {
+#pragma unroll
+            for (int j = 9; j < 12; ++j) {
+                float v = acc[j] * M.measure;
+                fwd[(long long)j * nc + cell] = make_float2(v, 0.f);
+                atomicAdd(sums + j, (double)v);
+            }
+        }
+        float dens = acc[12] * M.dthph;
+        table[(long long)cell * tstride + T_DIFF] = sqrtf(M.two_dt * (M.Dt + M.volex * dens));
+    }
+}
+
+// subtract the FP64 means before the FP32 transform
+__global__ void k_center_m(float2 *__restrict__ fwd, int c0, int c1, int ncell, const double *__restrict__ sums) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long total = (long long)(c1 - c0) * ncell;
+    if (i >= total) return;
+    int comp = c0 + (int)(i / ncell);
+    long long idx = (long long)comp * ncell + (i % ncell);
+    float mean = (float)(sums[comp] / (double)ncell);
+    fwd[idx].x -= mean;
+}
+
+template <bool FLOW, bool MAG>
+__global__ void k_kspace_m(const float2 *__restrict__ fwd, float2 *__restrict__ inv, MixedParams M, float screening,
+                           float stepx, float stepy, float stepz) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nc = M.ncell;
+    if (c >= nc) return;
+    int iz = c % M.gz;
+    int iy = (c / M.gz) % M.gy;
+    int ix = c / (M.gz * M.gy);
+    float k[3] = {kval_f(ix, M.gx, stepx), kval_f(iy, M.gy, stepy), kval_f(iz, M.gz, stepz)};
+    float s = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+    float ik2 = (c == 0) ? 0.f : 1.f / s;
+    float inrm = (c == 0) ? 0.f : rsqrtf(s);
+    float kn[3] = {k[0] * inrm, k[1] * inrm, k[2] * inrm};
+    const float norm = (float)nc;
+    if (FLOW) {
+        float2 sg[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            float2 a0 = fwd[(long long)(3 * r + 0) * nc + c];
+            float2 a1 = fwd[(long long)(3 * r + 1) * nc + c];
+            float2 a2 = fwd[(long long)(3 * r + 2) * nc + c];
+            sg[r].x = a0.x * k[0] + a1.x * k[1] + a2.x * k[2];
+            sg[r].y = a0.y * k[0] + a1.y * k[1] + a2.y * k[2];
+        }
+        float ksr = kn[0] * sg[0].x + kn[1] * sg[1].x + kn[2] * sg[2].x;
+        float ksi = kn[0] * sg[0].y + kn[1] * sg[1].y + kn[2] * sg[2].y;
+        float fac = (ik2 + screening) / norm;
+        float2 u[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            float tr = (sg[r].x - kn[r] * ksr) * fac;
+            float ti = (sg[r].y - kn[r] * ksi) * fac;
+            u[r] = make_float2(-ti, tr);
+            inv[(long long)(9 + r) * nc + c] = u[r];
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+                inv[(long long)(3 * a + b) * nc + c] = make_float2(-(k[a] * u[b].y), k[a] * u[b].x);
+    }
+    if (MAG) {
+        float2 p[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) p[r] = fwd[(long long)(9 + r) * nc + c];
+        float dr = kn[0] * p[0].x + kn[1] * p[1].x + kn[2] * p[2].x;
+        float di = kn[0] * p[0].y + kn[1] * p[1].y + kn[2] * p[2].y;
+        float2 b[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            // the k = 0 mode (the mean) was removed and is added back in FP64
+            b[r] = (c == 0) ? make_float2(0.f, 0.f)
+                            : make_float2((p[r].x - kn[r] * dr) / norm, (p[r].y - kn[r] * di) / norm);
+            inv[(long long)(21 + r) * nc + c] = b[r];
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int bb = 0; bb < 3; ++bb)
+                inv[(long long)(12 + 3 * a + bb) * nc + c] = make_float2(-(k[a] * b[bb].y), k[a] * b[bb].x);
+    }
+}
+
+template <bool FLOW, bool MAG>
+__global__ void k_table_m(const float2 *__restrict__ inv, MixedParams M, float *__restrict__ table, int tstride,
+                          const double *__restrict__ sums) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nc = M.ncell;
+    if (c >= nc) return;
+    float *row = table + (long long)c * tstride;
+    if (FLOW) {
+        float g[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) g[j] = inv[(long long)j * nc + c].x;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) row[T_U + r] = inv[(long long)(9 + r) * nc + c].x;
+        row[T_W01] = (g[1] - g[3]) * 0.5f;
+        row[T_W02] = (g[2] - g[6]) * 0.5f;
+        row[T_W12] = (g[5] - g[7]) * 0.5f;
+        row[T_E00] = g[0];
+        row[T_E01] = (g[1] + g[3]) * 0.5f;
+        row[T_E02] = (g[2] + g[6]) * 0.5f;
+        row[T_E11] = g[4];
+        row[T_E12] = (g[5] + g[7]) * 0.5f;
+        row[T_E22] = g[8];
+    }
+    if (MAG) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            double b = (double)inv[(long long)(21 + r) * nc + c].x + sums[9 + r] / (double)nc;
+            row[T_B + r] = (float)(b * M.mdd);
+        }
+#pragma unroll
+        for (int j = 0; j < 9; ++j) row[T_GB + j] = inv[(long long)(12 + j) * nc + c].x;
+    }
+}
+
+// complex float field -> complex double (for the FP64 getters); adds the FP64
+// mean back to the components listed in [m0, m1)
+__global__ void k_widen_m(const float2 *__restrict__ src, long long count, int ncell, int comp0, int m0, int m1,
+                          const double *__restrict__ sums, double2 *__restrict__ dst) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    float2 v = src[i];
+    int comp = comp0 + (int)(i / ncell);
+    double re = (double)v.x;
+    if (comp >= m0 && comp < m1) re += sums[comp - 12] / (double)ncell;
+    dst[i] = make_double2(re, (double)v.y);
+}
+
+// ---- the particle update ----------------------------------------------
+__device__ __forceinline__ float u24(uint32_t r) { return (float)(r >> 8) * 0x1p-24f; }
+
+template <bool Q2D>
+__device__ __forceinline__ void philox_noise_f(unsigned long long seed, uint32_t id, unsigned long long t,
+                                               float sigma, float xi[3], float &ca, float &sa, float &rot) {
+    uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+    uint32_t tl = (uint32_t)t, th = (uint32_t)(t >> 32);
+    uint4 r0 = philox4x32_10(make_uint4(id, tl, th, 0u), key);
+    float rad = sqrtf(-2.0f * logf(1.0f - u24(r0.x)));
+    float s, c;
+    sincospif(2.0f * u24(r0.y), &s, &c);
+    xi[0] = rad * c;
+    xi[1] = rad * s;
+    sincospif(2.0f * u24(r0.z), &sa, &ca);
+    rot = sigma * sqrtf(-2.0f * logf(1.0f - u24(r0.w)));
+    if (Q2D) {
+        xi[2] = 0.f;
+    } else {
+        uint4 r1 = philox4x32_10(make_uint4(id, tl, th, 1u), key);
+        xi[2] = sqrtf(-2.0f * logf(1.0f - u24(r1.x))) * cospif(2.0f * u24(r1.y));
+    }
+}
+
+struct TableFieldsF {
+    const float *r;
+    __device__ float flow(int k) const { return r[T_U + k]; }
+    __device__ float diff() const { return r[T_DIFF]; }
+    __device__ float b(int k) const { return r[T_B + k]; }
+    __device__ void vort_dot(const float n[3], float f[3]) const {
+        float w01 = r[T_W01], w02 = r[T_W02], w12 = r[T_W12];
+        f[0] = w01 * n[1] + w02 * n[2];
+        f[1] = -w01 * n[0] + w12 * n[2];
+        f[2] = -w02 * n[0] - w12 * n[1];
+    }
+    __device__ void strain_dot(const float n[3], float f[3]) const {
+        float e00 = r[T_E00], e01 = r[T_E01], e02 = r[T_E02], e11 = r[T_E11], e12 = r[T_E12], e22 = r[T_E22];
+        f[0] = e00 * n[0] + e01 * n[1] + e02 * n[2];
+        f[1] = e01 * n[0] + e11 * n[1] + e12 * n[2];
+        f[2] = e02 * n[0] + e12 * n[1] + e22 * n[2];
+    }
+    __device__ void gradb_dot(const float n[3], float f[3]) const {
+        const float *g = r + T_GB;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) f[a] = g[3 * a] * n[0] + g[3 * a + 1] * n[1] + g[3 * a + 2] * n[2];
+    }
+};
+
+// The Langevin chain of do_timestep in FP32, positions accumulated in FP64.
+template <bool Q2D>
+__device__ __forceinline__ void langevin_mixed(double &x, double &y, double &z, float &phi, float &theta,
+                                               const TableFieldsF &fld, const float xi[3], float ca, float sa,
+                                               float rot, const MixedParams &M) {
+    float sp, cp, st, ct;
+    sincosf(phi, &sp, &cp);
+    if (Q2D) {
+        st = 1.0f;
+        ct = 0.0f;
+    } else {
+        sincosf(theta, &st, &ct);
+    }
+    float n[3] = {st * cp, st * sp, ct};
+    float dp[3] = {n[0], n[1], n[2]}, dn[3] = {0.f, 0.f, 0.f};
+    const uint32_t mask = M.mask;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) dp[k] += fld.flow(k);
+    if (mask & M_MDD_FORCE) {
+        float f[3];
+        fld.gradb_dot(n, f);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dp[k] += f[k] * M.drag;
+    }
+    if (mask & M_EXTERNAL_FIELD) {
+        float d = n[1] * M.reorient;
+        dn[0] -= n[0] * d;
+        dn[1] += M.reorient - n[1] * d;
+        dn[2] -= n[2] * d;
+    }
+    if (mask & M_MDD_ROTATION) {
+        float b[3] = {fld.b(0), fld.b(1), fld.b(2)};
+        float d = n[0] * b[0] + n[1] * b[1] + n[2] * b[2];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dn[k] += b[k] - n[k] * d;
+    }
+    {
+        float f[3];
+        fld.vort_dot(n, f);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dn[k] -= f[k];
+    }
+    if (mask & M_JEFFREY_STRAIN) {
+        float f[3];
+        fld.strain_dot(n, f);
+        float fn = M.shape * (f[0] * n[0] + f[1] * n[1] + f[2] * n[2]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dn[k] += M.shape * f[k] - n[k] * fn;
+    }
+    const float diff = fld.diff();
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        dp[k] = dp[k] * M.dt + xi[k] * diff;
+        dn[k] = dn[k] * M.dt;
+    }
+    // rotational diffusion about k perpendicular to n by rot (Rodrigues)
+    float ax0 = cp * ct * sa - ca * sp, ax1 = ca * cp + ct * sa * sp, ax2 = -sa * st;
+    float sr, cr;
+    sincosf(rot, &sr, &cr);
+    float cm1 = cr - 1.0f;
+    dn[0] += n[0] * cm1 + (ax1 * n[2] - ax2 * n[1]) * sr;
+    dn[1] += n[1] * cm1 + (ax2 * n[0] - ax0 * n[2]) * sr;
+    dn[2] += n[2] * cm1 + (ax0 * n[1] - ax1 * n[0]) * sr;
+    float v0 = n[0] + dn[0], v1 = n[1] + dn[1], v2 = n[2] + dn[2];
+    float nphi = atan2f(v1, v0);
+    x = ref_modulo(x + (double)dp[0], M.bx);
+    y = ref_modulo(y + (double)dp[1], M.by);
+    if (Q2D) {
+        phi = nphi < 0.0f ? nphi + 6.28318530717958647692f : nphi;
+        z = 0.0;
+        theta = 1.57079632679489661923f;
+    } else {
+        float nth = 1.57079632679489661923f - atan2f(v2, sqrtf(v0 * v0 + v1 * v1));
+        z = ref_modulo(z + (double)dp[2], M.bz);
+        float t = modulo_f(nth, 6.28318530717958647692f);
+        if (t > 3.14159265358979323846f) {
+            phi = modulo_f(nphi + 3.14159265358979323846f, 6.28318530717958647692f);
+            theta = 6.28318530717958647692f - t;
+        } else {
+            phi = modulo_f(nphi, 6.28318530717958647692f);
+            theta = t;
+        }
+    }
+}
+
+// NOISE: 0 Philox, 1 host array.  CANON (quasi2d only): z == 0 and
+// theta == pi/2 already hold, so they are neither read nor written.
+template <bool Q2D, bool CANON, bool MAG, int NOISE>
+__global__ void __launch_bounds__(256) k_update_m(MixedParams M, double *__restrict__ x, double *__restrict__ y,
+                                                  double *__restrict__ z, float *__restrict__ phi,
+                                                  float *__restrict__ theta, uint32_t *__restrict__ key,
+                                                  const uint32_t *__restrict__ id, const float *__restrict__ table,
+                                                  const double *__restrict__ noise,
+                                                  const unsigned long long *__restrict__ d_step,
+                                                  uint32_t *__restrict__ counts_next) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= M.n) return;
+    const int ts = MAG ? TABLE_STRIDE_MAG : TABLE_STRIDE;
+    uint32_t cell = key[i];
+    double px = x[i], py = y[i], pz = 0.0;
+    float pph = phi[i], pth = 1.57079632679489661923f;
+    if (!CANON) {
+        pz = z[i];
+        pth = theta[i];
+    }
+    TableFieldsF F{table + (long long)cell * ts};
+    float xi[3], ca, sa, rot;
+    if (NOISE == 0) {
+        philox_noise_f<Q2D>(M.seed, id[i], *d_step, M.sigma_rot, xi, ca, sa, rot);
+    } else {
+        const double *r = noise + 5ull * id[i];
+        xi[0] = (float)r[0]; xi[1] = (float)r[1]; xi[2] = (float)r[2];
+        sincosf((float)r[3], &sa, &ca);
+        rot = (float)r[4];
+    }
+    if (Q2D && !CANON) {
+        // first step after init: theta may differ from pi/2
+        langevin_mixed<false>(px, py, pz, pph, pth, F, xi, ca, sa, rot, M);
+        pz = 0.0;
+        pth = 1.57079632679489661923f;
+    } else {
+        langevin_mixed<Q2D>(px, py, pz, pph, pth, F, xi, ca, sa, rot, M);
+    }
+    uint32_t ncell;
+    unsigned long long bin;
+    bin_mixed(M, px, py, pz, pph, pth, ncell, bin);
+    atomicAdd(counts_next + bin, 1u);
+    key[i] = ncell;
+    x[i] = px;
+    y[i] = py;
+    phi[i] = pph;
+    if (!CANON) {
+        z[i] = pz;
+        theta[i] = pth;
+    }
+}
+
+template <bool Q2D>
+__global__ void k_noise_m(MixedParams M, unsigned long long t, double *__restrict__ out) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= M.n) return;
+    float xi[3], ca, sa, rot;
+    philox_noise_f<Q2D>(M.seed, (uint32_t)i, t, M.sigma_rot, xi, ca, sa, rot);
+    double *r = out + 5 * i;
+    r[0] = xi[0]; r[1] = xi[1]; r[2] = xi[2]; r[3] = atan2((double)sa, (double)ca); r[4] = rot;
+    if (r[3] < 0.0) r[3] += kTwoPi;
+}
+
+// ========================================================================
+static inline unsigned nb(unsigned long long n, unsigned bs) { return (unsigned)((n + bs - 1) / bs); }
+
+void launch_ingest_m(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P, double *const xs[3],
+                     float *const as[2], uint32_t *id) {
+    if (n) k_ingest_m<<<nb(n, 256), 256, 0, s>>>(aos, n, P, xs[0], xs[1], xs[2], as[0], as[1], id);
+}
+void launch_egest_m(cudaStream_t s, unsigned long long n, double *const xs[3], float *const as[2], const uint32_t *id,
+                    double *aos) {
+    if (n) k_egest_m<<<nb(n, 256), 256, 0, s>>>(n, xs[0], xs[1], xs[2], as[0], as[1], id, aos);
+}
+void launch_bin_m(cudaStream_t s, unsigned long long n, const MixedParams &M, double *const xs[3], float *const as[2],
+                  uint32_t *key, uint32_t *counts) {
+    if (n) k_bin_m<<<nb(n, 256), 256, 0, s>>>(n, M, xs[0], xs[1], xs[2], as[0], as[1], key, counts);
+}
+void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *lut, int lut_n,
+                       const float *kern, const MixedParams &M, float2 *fwd, float *table, int tstride,
+                       double *sums) {
+    unsigned blocks = nb((unsigned long long)M.ncell * 32ull, 256);
+    if (stress && mag) k_contract_m<true, true><<<blocks, 256, 0, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums);
+    else if (stress) k_contract_m<true, false><<<blocks, 256, 0, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums);
+    else k_contract_m<false, true><<<blocks, 256, 0, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums);
+}
+void launch_center_m(cudaStream_t s, float2 *fwd, int c0, int c1, int ncell, const double *sums) {
+    long long total = (long long)(c1 - c0) * ncell;
+    if (total > 0) k_center_m<<<nb(total, 256), 256, 0, s>>>(fwd, c0, c1, ncell, sums);
+}
+void launch_kspace_m(cudaStream_t s, bool flow, bool mag, const float2 *fwd, float2 *inv, const MixedParams &M,
+                     float screening) {
+    float sx = (float)(kTwoPi / M.bx), sy = (float)(kTwoPi / M.by), sz = (float)(kTwoPi / M.bz);
+    unsigned b = nb(M.ncell, 128);
+    if (flow && mag) k_kspace_m<true, true><<<b, 128, 0, s>>>(fwd, inv, M, screening, sx, sy, sz);
+    else if (flow) k_kspace_m<true, false><<<b, 128, 0, s>>>(fwd, inv, M, screening, sx, sy, sz);
+    else k_kspace_m<false, true><<<b, 128, 0, s>>>(fwd, inv, M, screening, sx, sy, sz);
+}
+void launch_table_m(cudaStream_t s, bool flow, bool mag, const float2 *inv, const MixedParams &M, float *table,
+                    int tstride, const double *sums) {
+    unsigned b = nb(M.ncell, 128);
+    if (flow && mag) k_table_m<true, true><<<b, 128, 0, s>>>(inv, M, table, tstride, sums);
+    else if (flow) k_table_m<true, false><<<b, 128, 0, s>>>(inv, M, table, tstride, sums);
+    else k_table_m<false, true><<<b, 128, 0, s>>>(inv, M, table, tstride, sums);
+}
+void launch_widen_m(cudaStream_t s, const float2 *src, long long count, int ncell, int comp0, int m0, int m1,
+                    const double *sums, double2 *dst) {
+    if (count > 0) k_widen_m<<<nb(count, 256), 256, 0, s>>>(src, count, ncell, comp0, m0, m1, sums, dst);
+}
+void launch_update_m(cudaStream_t s, bool q2d, bool canon, bool mag, bool host_noise, const MixedParams &M,
+                     double *const xs[3], float *const as[2], uint32_t *key, const uint32_t *id, const float *table,
+                     const double *noise, const unsigned long long *d_step, uint32_t *counts_next) {
+    if (!M.n) return;
+    unsigned b = nb(M.n, 256);
+#define SS_UPDM(Q, C, G, N) \
+    k_update_m<Q, C, G, N><<<b, 256, 0, s>>>(M, xs[0], xs[1], xs[2], as[0], as[1], key, id, table, noise, d_step, \
+                                            counts_next)
+#define SS_UPDM_N(Q, C, G) \
+    do { if (host_noise) SS_UPDM(Q, C, G, 1); else SS_UPDM(Q, C, G, 0); } while (0)
+    if (q2d) {
+        if (canon) { if (mag) SS_UPDM_N(true, true, true); else SS_UPDM_N(true, true, false); }
+        else { if (mag) SS_UPDM_N(true, false, true); else SS_UPDM_N(true, false, false); }
+    } else {
+        if (mag) SS_UPDM_N(false, false, true); else SS_UPDM_N(false, false, false);
+    }
+#undef SS_UPDM_N
+#undef SS_UPDM
+}
+void launch_noise_m(cudaStream_t s, bool q2d, const MixedParams &M, unsigned long long t, double *out) {
+    if (!M.n) return;
+    if (q2d) k_noise_m<true><<<nb(M.n, 256), 256, 0, s>>>(M, t, out);
+    else k_noise_m<false><<<nb(M.n, 256), 256, 0, s>>>(M, t, out);
+}
+
+}  // namespace ss

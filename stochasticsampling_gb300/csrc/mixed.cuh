@@ -1,0 +1,45 @@
+// mixed.cuh -- parameters and launch wrappers of the FP32 mixed-precision
+// timestep (mixed.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace ss {
+
+struct MixedParams {
+    int gx, gy, gz, gphi, gtheta;
+    int ncell, nang;
+    unsigned long long n;
+    double bx, by, bz;  // positions stay FP64
+    float igwf[5];      // 1 / grid width, FP32 binning
+    double dist_den, volume;
+    float measure, dthph, two_dt, Dt, volex, dt;
+    float drag, reorient, shape, mdd, sigma_rot;
+    unsigned long long seed;
+    uint32_t mask;
+};
+
+void launch_ingest_m(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P, double *const xs[3],
+                     float *const as[2], uint32_t *id);
+void launch_egest_m(cudaStream_t s, unsigned long long n, double *const xs[3], float *const as[2], const uint32_t *id,
+                    double *aos);
+void launch_bin_m(cudaStream_t s, unsigned long long n, const MixedParams &M, double *const xs[3], float *const as[2],
+                  uint32_t *key, uint32_t *counts);
+void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *lut, int lut_n,
+                       const float *kern, const MixedParams &M, float2 *fwd, float *table, int tstride,
+                       double *sums);
+void launch_center_m(cudaStream_t s, float2 *fwd, int c0, int c1, int ncell, const double *sums);
+void launch_kspace_m(cudaStream_t s, bool flow, bool mag, const float2 *fwd, float2 *inv, const MixedParams &M,
+                     float screening);
+void launch_table_m(cudaStream_t s, bool flow, bool mag, const float2 *inv, const MixedParams &M, float *table,
+                    int tstride, const double *sums);
+void launch_widen_m(cudaStream_t s, const float2 *src, long long count, int ncell, int comp0, int m0, int m1,
+                    const double *sums, double2 *dst);
+void launch_update_m(cudaStream_t s, bool q2d, bool canon, bool mag, bool host_noise, const MixedParams &M,
+                     double *const xs[3], float *const as[2], uint32_t *key, const uint32_t *id, const float *table,
+                     const double *noise, const unsigned long long *d_step, uint32_t *counts_next);
+void launch_noise_m(cudaStream_t s, bool q2d, const MixedParams &M, unsigned long long t, double *out);
+
+}  // namespace ss

@@ -18,6 +18,7 @@
 
 #include "../../include/ssgpu.h"
 #include "kernels.cuh"
+#include "mixed.cuh"
 
 using namespace ss;
 
@@ -68,6 +69,17 @@ struct ss_ctx {
     unsigned long long *d_step = nullptr;
     uint32_t *d_err = nullptr;
     double *d_halfpi = nullptr;
+
+    // FP32 mixed-precision mode (SS_FLAG_MIXED)
+    bool mixed = false;
+    bool canon = false;  // quasi2d: z == 0 and theta == pi/2 hold for every particle
+    MixedParams M{};
+    float *pa[2][2] = {};  // phi, theta (FP32)
+    float2 *fwd_f = nullptr, *inv_f = nullptr;
+    float *table_f = nullptr, *kern_f = nullptr, *lut_f = nullptr;
+    double *sums = nullptr;  // FP64 per-component sums for the mean handling
+    bool wide_valid = false;  // inv (FP64) holds the widened mixed fields
+    std::map<int, cufftHandle> plans_c;
 
     std::map<int, cufftHandle> plans;
     int fft_rank = 0;
@@ -197,10 +209,33 @@ static int get_plan(ss_ctx *c, int batch, cufftHandle *out) {
 
 static int fft(ss_ctx *c, double2 *data, int batch, int dir) {
     if (c->fft_rank == 0 || batch == 0) return SS_OK;  // 1-cell grid: the DFT is the identity
-    cufftHandle h;
+    cufftHandle h = 0;
     CKR(get_plan(c, batch, &h));
     CKF(cufftExecZ2Z(h, reinterpret_cast<cufftDoubleComplex *>(data), reinterpret_cast<cufftDoubleComplex *>(data),
                      dir));
+    return SS_OK;
+}
+
+static int get_plan_c(ss_ctx *c, int batch, cufftHandle *out) {
+    auto it = c->plans_c.find(batch);
+    if (it != c->plans_c.end()) {
+        *out = it->second;
+        return SS_OK;
+    }
+    cufftHandle h;
+    int nc = c->P.ncell;
+    CKF(cufftPlanMany(&h, c->fft_rank, c->fft_n, nullptr, 1, nc, nullptr, 1, nc, CUFFT_C2C, batch));
+    CKF(cufftSetStream(h, c->stream));
+    c->plans_c[batch] = h;
+    *out = h;
+    return SS_OK;
+}
+
+static int fft_c(ss_ctx *c, float2 *data, int batch, int dir) {
+    if (c->fft_rank == 0 || batch == 0) return SS_OK;
+    cufftHandle h = 0;
+    CKR(get_plan_c(c, batch, &h));
+    CKF(cufftExecC2C(h, reinterpret_cast<cufftComplex *>(data), reinterpret_cast<cufftComplex *>(data), dir));
     return SS_OK;
 }
 
@@ -253,8 +288,59 @@ static int enqueue_solve(ss_ctx *c, bool flow, bool mag, const uint32_t *counts,
     return SS_OK;
 }
 
+// The mixed-precision field solve (mixed.cu): FP32 contraction with FP64
+// component sums, means removed in FP64, C2C FP32 transforms, FP32 k space.
+static int enqueue_solve_m(ss_ctx *c, bool flow, bool mag, const uint32_t *counts, double screening, uint64_t *nl) {
+    const int ts = c->mag_step ? TABLE_STRIDE_MAG : TABLE_STRIDE;
+    const int nc = c->P.ncell;
+    mark(c, 0);
+    CK(cudaMemsetAsync(c->sums, 0, 12 * sizeof(double), c->stream));
+    launch_contract_m(c->stream, flow, mag, counts, c->lut_f, kLutN, c->kern_f, c->M, c->fwd_f, c->table_f, ts,
+                      c->sums);
+    if (flow) launch_center_m(c->stream, c->fwd_f, 0, 9, nc, c->sums);
+    if (mag) launch_center_m(c->stream, c->fwd_f, 9, 12, nc, c->sums);
+    *nl += 1 + (flow ? 1 : 0) + (mag ? 1 : 0);
+    CKR(check_launch(c, "contract (mixed)"));
+    mark(c, 6);
+    mark(c, 1);
+    if (flow && mag) CKR(fft_c(c, c->fwd_f, 12, CUFFT_FORWARD));
+    else if (flow) CKR(fft_c(c, c->fwd_f, 9, CUFFT_FORWARD));
+    else CKR(fft_c(c, c->fwd_f + 9ll * nc, 3, CUFFT_FORWARD));
+    mark(c, 2);
+    launch_kspace_m(c->stream, flow, mag, c->fwd_f, c->inv_f, c->M, (float)screening);
+    ++*nl;
+    CKR(check_launch(c, "kspace (mixed)"));
+    mark(c, 3);
+    if (flow && mag) CKR(fft_c(c, c->inv_f, 24, CUFFT_INVERSE));
+    else if (flow) CKR(fft_c(c, c->inv_f, 12, CUFFT_INVERSE));
+    else CKR(fft_c(c, c->inv_f + 12ll * nc, 12, CUFFT_INVERSE));
+    mark(c, 4);
+    const bool table_mag = mag && c->mag_step;
+    if (flow || table_mag) {
+        launch_table_m(c->stream, flow, table_mag, c->inv_f, c->M, c->table_f, ts, c->sums);
+        ++*nl;
+        CKR(check_launch(c, "table (mixed)"));
+    }
+    c->wide_valid = false;
+    return SS_OK;
+}
+
+static int enqueue_step_m(ss_ctx *c, int pcur, int ccur, bool host_noise, uint64_t *nl) {
+    CKR(enqueue_solve_m(c, true, c->mag_step, c->counts[ccur], c->prm.hydro_screening, nl));
+    mark(c, 5);
+    launch_zero_u32(c->stream, c->counts[1 - ccur], c->P.nbins);
+    launch_update_m(c->stream, c->q2d, c->canon, c->mag_step, host_noise, c->M, c->px[pcur], c->pa[pcur],
+                    c->key[pcur], c->pid[pcur], c->table_f, c->noise_dev, c->d_step, c->counts[1 - ccur]);
+    launch_step_inc(c->stream, c->d_step);
+    *nl += 3;
+    CKR(check_launch(c, "update (mixed)"));
+    mark(c, 7);
+    return SS_OK;
+}
+
 // One do_timestep for the state (pcur, ccur); does not touch host-side state.
 static int enqueue_step(ss_ctx *c, int pcur, int ccur, bool host_noise, uint64_t *nl) {
+    if (c->mixed) return enqueue_step_m(c, pcur, ccur, host_noise, nl);
     const bool sort_now = c->sort;
     CKR(enqueue_solve(c, true, c->mag_step, c->counts[ccur], nullptr, c->prm.hydro_screening, pcur, sort_now, nl));
     const int p = sort_now ? 1 - pcur : pcur;
@@ -276,6 +362,8 @@ static void advance(ss_ctx *c) {
     c->timestep += 1;
     c->fields_mag_valid = c->mag_step;
     c->solved = true;
+    // the first mixed quasi2d step sets z = 0 and theta = pi/2 everywhere
+    if (c->mixed && c->q2d) c->canon = true;
 }
 
 static void accumulate_timing(ss_ctx *c) {
@@ -304,6 +392,7 @@ static int direct_step(ss_ctx *c, bool host_noise) {
 }
 
 static int graph_step(ss_ctx *c) {
+    if (c->mixed && c->q2d && !c->canon) return direct_step(c, false);
     cudaGraphExec_t &g = c->graph[c->pcur][c->ccur];
     if (!g) {
         cudaGraph_t graph;
@@ -370,6 +459,11 @@ static void destroy_impl(ss_ctx *c) {
     cudaFree(c->fwd); cudaFree(c->inv); cudaFree(c->table); cudaFree(c->cellcount); cudaFree(c->cursor);
     cudaFree(c->kern); cudaFree(c->lut); cudaFree(c->staging); cudaFree(c->noise_dev); cudaFree(c->dist_dev);
     cudaFree(c->realbuf); cudaFree(c->d_step); cudaFree(c->d_err); cudaFree(c->d_halfpi);
+    for (auto &kv : c->plans_c) cufftDestroy(kv.second);
+    for (int b = 0; b < 2; ++b)
+        for (int k = 0; k < 2; ++k) cudaFree(c->pa[b][k]);
+    cudaFree(c->fwd_f); cudaFree(c->inv_f); cudaFree(c->table_f); cudaFree(c->kern_f); cudaFree(c->lut_f);
+    cudaFree(c->sums);
     for (auto &e : c->timing.ev)
         if (e) cudaEventDestroy(e);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -421,6 +515,8 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     c->q2d = (flags & SS_FLAG_QUASI2D) != 0;
     c->sort = (flags & SS_FLAG_NO_SORT) == 0;
     c->use_graph = (flags & SS_FLAG_NO_GRAPH) == 0;
+    c->mixed = (flags & SS_FLAG_MIXED) != 0;
+    if (c->mixed) c->sort = false;
     c->mag_step = (flags & SS_FLAG_ALWAYS_MAGNETIC) || params->magnetic_dipole_dipole != 0.0 ||
                   params->magnetic_drag != 0.0;
     cudaError_t e = cudaGetDevice(&c->device);
@@ -475,6 +571,20 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     if (!c->mag_step || params->magnetic_drag == 0.0) mask &= ~M_MDD_FORCE;
     if (!c->mag_step || params->magnetic_dipole_dipole == 0.0) mask &= ~M_MDD_ROTATION;
     P.mask = mask;
+    if (c->mixed) {
+        MixedParams &M = c->M;
+        M.gx = P.gx; M.gy = P.gy; M.gz = P.gz; M.gphi = P.gphi; M.gtheta = P.gtheta;
+        M.ncell = P.ncell; M.nang = P.nang; M.n = P.n;
+        M.bx = P.bx; M.by = P.by; M.bz = P.bz;
+        for (int k = 0; k < 5; ++k) M.igwf[k] = (float)(1.0 / P.gw[k]);
+        M.dist_den = P.dist_den; M.volume = P.volume;
+        M.measure = (float)P.measure; M.dthph = (float)P.dthph; M.two_dt = (float)(2.0 * P.dt);
+        M.Dt = (float)P.Dt; M.volex = (float)P.volex; M.dt = (float)P.dt;
+        M.drag = (float)P.drag; M.reorient = (float)P.reorient; M.shape = (float)P.shape; M.mdd = (float)P.mdd;
+        M.sigma_rot = (float)P.sigma_rot;
+        M.seed = P.seed;
+        M.mask = mask;
+    }
 
     // FFT geometry: drop axes of length 1
     {
@@ -494,7 +604,9 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     const size_t N = (size_t)P.n;
     const int nbuf = c->sort ? 2 : 1;
     for (int b = 0; b < nbuf && rc == SS_OK; ++b) {
-        for (int k = 0; k < 5 && rc == SS_OK; ++k) rc = alloc((void **)&c->px[b][k], N * sizeof(double));
+        const int nd = c->mixed ? 3 : 5;  // mixed: x, y, z in FP64, phi, theta in FP32
+        for (int k = 0; k < nd && rc == SS_OK; ++k) rc = alloc((void **)&c->px[b][k], N * sizeof(double));
+        for (int k = 0; c->mixed && k < 2 && rc == SS_OK; ++k) rc = alloc((void **)&c->pa[b][k], N * sizeof(float));
         if (rc == SS_OK) rc = alloc((void **)&c->key[b], N * sizeof(uint32_t));
         if (rc == SS_OK) rc = alloc((void **)&c->pid[b], N * sizeof(uint32_t));
     }
@@ -510,6 +622,14 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     if (rc == SS_OK) rc = alloc((void **)&c->d_step, sizeof(unsigned long long));
     if (rc == SS_OK) rc = alloc((void **)&c->d_err, sizeof(uint32_t));
     if (rc == SS_OK) rc = alloc((void **)&c->d_halfpi, 2 * sizeof(double));
+    if (c->mixed) {
+        if (rc == SS_OK) rc = alloc((void **)&c->fwd_f, 12 * ncell * sizeof(float2));
+        if (rc == SS_OK) rc = alloc((void **)&c->inv_f, 24 * ncell * sizeof(float2));
+        if (rc == SS_OK) rc = alloc((void **)&c->table_f, ncell * TABLE_STRIDE_MAG * sizeof(float));
+        if (rc == SS_OK) rc = alloc((void **)&c->kern_f, 12 * nang * sizeof(float));
+        if (rc == SS_OK) rc = alloc((void **)&c->lut_f, kLutN * sizeof(float));
+        if (rc == SS_OK) rc = alloc((void **)&c->sums, 12 * sizeof(double));
+    }
     if (rc != SS_OK) {
         std::string m = c->err;
         destroy_impl(c);
@@ -538,6 +658,13 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     for (int i = 0; i < kLutN; ++i) lut[i] = ((double)i / P.dist_den) * P.volume;
     CKC(cudaMemcpyAsync(c->kern, K.data(), K.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     CKC(cudaMemcpyAsync(c->lut, lut.data(), lut.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    std::vector<float> Kf(K.begin(), K.end()), lutf(lut.begin(), lut.end());
+    if (c->mixed) {
+        CKC(cudaMemsetAsync(c->inv_f, 0, 24 * ncell * sizeof(float2), c->stream));
+        CKC(cudaMemsetAsync(c->sums, 0, 12 * sizeof(double), c->stream));
+        CKC(cudaMemcpyAsync(c->kern_f, Kf.data(), Kf.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        CKC(cudaMemcpyAsync(c->lut_f, lutf.data(), lutf.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    }
     launch_half_pi(c->stream, c->d_halfpi);
     double hp[2];
     CKC(cudaMemcpyAsync(hp, c->d_halfpi, sizeof hp, cudaMemcpyDeviceToHost, c->stream));
@@ -549,8 +676,10 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     // plans for the step
     {
         cufftHandle h;
-        int r1 = get_plan(c, c->mag_step ? 12 : 9, &h);
-        int r2 = (r1 == SS_OK) ? get_plan(c, c->mag_step ? 24 : 12, &h) : r1;
+        int r1 = c->mixed ? get_plan_c(c, c->mag_step ? 12 : 9, &h) : get_plan(c, c->mag_step ? 12 : 9, &h);
+        int r2 = (r1 == SS_OK) ? (c->mixed ? get_plan_c(c, c->mag_step ? 24 : 12, &h)
+                                           : get_plan(c, c->mag_step ? 24 : 12, &h))
+                               : r1;
         if (r1 != SS_OK || r2 != SS_OK) {
             std::string m = c->err;
             destroy_impl(c);
@@ -560,6 +689,8 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     *out = c;
     return SS_OK;
 }
+
+static int ingest_staging(ss_ctx *c, uint64_t n, bool canon);
 
 static int load_particles(ss_ctx *c, const double *particles, uint64_t n) {
     if (!particles) return fail(c, SS_ERR_INVALID_ARGUMENT, "particles is NULL");
@@ -573,12 +704,29 @@ static int load_particles(ss_ctx *c, const double *particles, uint64_t n) {
             return fail(c, SS_ERR_INVALID_ARGUMENT, "particle %llu has a non-finite coordinate",
                         (unsigned long long)(i / 5));
     CK(cudaSetDevice(c->device));
+    CK(cudaMemcpyAsync(c->staging, particles, 5 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    bool canon = c->q2d;
+    for (uint64_t i = 0; c->mixed && canon && i < n; ++i)
+        canon = particles[5 * i + 2] == 0.0 && particles[5 * i + 4] == kPiHalf;
+    return ingest_staging(c, n, canon);
+}
+
+// the rows in `staging` become the particle state: Particle::new, then the
+// first histogram (Simulation::init, src/bin/simulation/mod.rs:163-196)
+static int ingest_staging(ss_ctx *c, uint64_t n, bool canon) {
     c->pcur = 0;
     c->ccur = 0;
-    CK(cudaMemcpyAsync(c->staging, particles, 5 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    launch_ingest(c->stream, c->staging, n, c->P, c->px[0], c->pid[0]);
-    launch_zero_u32(c->stream, c->counts[0], c->P.nbins);
-    launch_bin(c->stream, n, c->P, c->px[0], c->key[0], c->counts[0], c->d_err);
+    if (c->mixed) {
+        launch_ingest_m(c->stream, c->staging, n, c->P, c->px[0], c->pa[0], c->pid[0]);
+        launch_zero_u32(c->stream, c->counts[0], c->P.nbins);
+        launch_bin_m(c->stream, n, c->M, c->px[0], c->pa[0], c->key[0], c->counts[0]);
+        // quasi2d: the canonical state (z = 0, theta = pi/2) lets the update skip z and theta
+        c->canon = canon;
+    } else {
+        launch_ingest(c->stream, c->staging, n, c->P, c->px[0], c->pid[0]);
+        launch_zero_u32(c->stream, c->counts[0], c->P.nbins);
+        launch_bin(c->stream, n, c->P, c->px[0], c->key[0], c->counts[0], c->d_err);
+    }
     c->launches += 3;
     CKR(check_launch(c, "init"));
     c->dist_idx = 0;
@@ -604,6 +752,34 @@ int ss_resume(ss_ctx *c, const double *particles, uint64_t n, uint64_t timestep)
     c->timestep = timestep;
     unsigned long long t = timestep;
     CK(cudaMemcpyAsync(c->d_step, &t, sizeof t, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SS_OK;
+}
+
+int ss_init_distribution(ss_ctx *c, uint32_t kind) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    if (kind > 1) return fail(c, SS_ERR_INVALID_ARGUMENT, "unknown initial distribution %u", kind);
+    double kappa = 0.0;
+    if (kind == 1) {
+        // init.rs:103-110: kappa = magnetic_reorientation / rotational diffusion
+        kappa = c->prm.magnetic_reorientation / c->prm.rot_diffusion;
+        if (kappa == 0.0)
+            return fail(c, SS_ERR_INVALID_ARGUMENT,
+                        "Alignment of zero is the isotropic state. Please use that instead.");
+        if (!is_finite(kappa)) return fail(c, SS_ERR_INVALID_ARGUMENT, "alignment kappa is not finite");
+    }
+    CK(cudaSetDevice(c->device));
+    CK(cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream));
+    launch_sample_initial(c->stream, kind == 1, c->P, kappa, c->staging, c->d_err);
+    c->launches += 1;
+    CKR(check_launch(c, "sample_initial"));
+    uint32_t e = 0;
+    CK(cudaMemcpyAsync(&e, c->d_err, sizeof e, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (e) return fail(c, SS_ERR_RANGE, "Caution, the alignment parameter is too high for the given precision.");
+    CKR(ingest_staging(c, c->P.n, false));
+    c->timestep = 0;
+    CK(cudaMemsetAsync(c->d_step, 0, sizeof(unsigned long long), c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return SS_OK;
 }
@@ -643,7 +819,8 @@ int ss_run(ss_ctx *c, uint64_t steps, uint64_t *timestep_out) {
 int ss_noise(ss_ctx *c, uint64_t timestep, double *out) {
     if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
     CK(cudaSetDevice(c->device));
-    launch_noise(c->stream, c->q2d, c->P, timestep, c->staging);
+    if (c->mixed) launch_noise_m(c->stream, c->q2d, c->M, timestep, c->staging);
+    else launch_noise(c->stream, c->q2d, c->P, timestep, c->staging);
     c->launches += 1;
     CKR(check_launch(c, "noise"));
     CK(cudaMemcpyAsync(out, c->staging, 5 * (size_t)c->P.n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -663,7 +840,8 @@ int ss_get_particles(ss_ctx *c, double *out, uint64_t n) {
     if (n > c->P.n) return fail(c, SS_ERR_INVALID_ARGUMENT, "asked for %llu of %llu particles",
                                 (unsigned long long)n, (unsigned long long)c->P.n);
     CK(cudaSetDevice(c->device));
-    launch_egest(c->stream, c->P.n, c->px[c->pcur], c->pid[c->pcur], c->staging);
+    if (c->mixed) launch_egest_m(c->stream, c->P.n, c->px[c->pcur], c->pa[c->pcur], c->pid[c->pcur], c->staging);
+    else launch_egest(c->stream, c->P.n, c->px[c->pcur], c->pid[c->pcur], c->staging);
     c->launches += 1;
     CKR(check_launch(c, "egest"));
     CK(cudaMemcpyAsync(out, c->staging, 5 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -711,15 +889,29 @@ static int ensure_magnetic(ss_ctx *c) {
     if (!c->initialized || !c->solved) return SS_OK;  // nothing solved yet: zeros, like the reference
     uint64_t nl = 0;
     int pc = c->pcur;
-    CKR(enqueue_solve(c, false, true, c->counts[c->dist_idx], nullptr, 0.0, pc, false, &nl));
+    if (c->mixed) CKR(enqueue_solve_m(c, false, true, c->counts[c->dist_idx], 0.0, &nl));
+    else CKR(enqueue_solve(c, false, true, c->counts[c->dist_idx], nullptr, 0.0, pc, false, &nl));
     c->launches += nl;
     c->fields_mag_valid = true;
+    return SS_OK;
+}
+
+// mixed mode: the FP32 fields widened into the FP64 buffer the getters read,
+// with the FP64 mean dipolar field added back
+static int widen_fields(ss_ctx *c) {
+    if (!c->mixed || c->wide_valid) return SS_OK;
+    const int nc = c->P.ncell;
+    launch_widen_m(c->stream, c->inv_f, 24ll * nc, nc, 0, 21, 24, c->sums, c->inv);
+    c->launches += 1;
+    CKR(check_launch(c, "widen"));
+    c->wide_valid = true;
     return SS_OK;
 }
 
 int ss_get_flow_field(ss_ctx *c, double *out) {
     if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
     CK(cudaSetDevice(c->device));
+    CKR(widen_fields(c));
     return copy_real(c, c->inv + 9ll * c->P.ncell, 3, out);
 }
 
@@ -727,12 +919,14 @@ int ss_get_magnetic_field(ss_ctx *c, double *out) {
     if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
     CK(cudaSetDevice(c->device));
     CKR(ensure_magnetic(c));
+    CKR(widen_fields(c));
     return copy_real(c, c->inv + 21ll * c->P.ncell, 3, out);
 }
 
 int ss_get_flow_complex(ss_ctx *c, double *u, double *grad) {
     if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
     CK(cudaSetDevice(c->device));
+    CKR(widen_fields(c));
     const size_t nc = c->P.ncell;
     if (u) CK(cudaMemcpyAsync(u, c->inv + 9 * nc, 3 * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
     if (grad) CK(cudaMemcpyAsync(grad, c->inv, 9 * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
@@ -744,6 +938,7 @@ int ss_get_magnetic_complex(ss_ctx *c, double *b, double *gradb) {
     if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
     CK(cudaSetDevice(c->device));
     CKR(ensure_magnetic(c));
+    CKR(widen_fields(c));
     const size_t nc = c->P.ncell;
     if (b) CK(cudaMemcpyAsync(b, c->inv + 21 * nc, 3 * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
     if (gradb) CK(cudaMemcpyAsync(gradb, c->inv + 12 * nc, 9 * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
@@ -759,6 +954,9 @@ int ss_get_timestep(ss_ctx *c, uint64_t *out) {
 
 static int seam_solve(ss_ctx *c, bool flow, bool mag, double screening, const double *dist) {
     if (!dist) return fail(c, SS_ERR_INVALID_ARGUMENT, "dist is NULL");
+    if (c->mixed)
+        return fail(c, SS_ERR_INVALID_ARGUMENT,
+                    "the solver seams on an explicit distribution need a context without SS_FLAG_MIXED");
     CK(cudaSetDevice(c->device));
     if (!c->dist_dev) CK(cudaMalloc((void **)&c->dist_dev, (size_t)c->P.nbins * sizeof(double)));
     CK(cudaMemcpyAsync(c->dist_dev, dist, (size_t)c->P.nbins * sizeof(double), cudaMemcpyHostToDevice, c->stream));

@@ -223,6 +223,114 @@ def read_parameter_file(path):
     return s
 
 
+# ---------------------------------------------------------------- SI units
+BOLTZMANN = 1.38064852e-23  # src/bin/simulation/settings/si.rs:22
+
+
+@dataclass
+class ParticleSI:
+    radius: float
+    self_propulsion_speed: float
+    force_dipole: float
+    magnetic_dipole_moment: float
+    persistance_time: float
+    shape: float = 0.0
+
+
+@dataclass
+class ParametersSI:
+    hydro_screening: float
+    volume_exclusion: float
+    viscocity: float
+    temperature: float
+    volume_fraction: float
+    external_field: float
+    particle: ParticleSI
+
+
+@dataclass
+class SettingsSI:
+    simulation: SimulationSettings
+    parameters: ParametersSI
+    environment: EnvironmentSettings
+
+
+def parse_settings_si(doc):
+    """SettingsSI (src/bin/simulation/settings/si.rs:24-73): the simulation and
+    environment tables of the dimensionless schema, physical parameters in SI."""
+    _table(doc, "settings", ["simulation", "parameters", "environment"], [])
+    shell = {"simulation": doc["simulation"], "environment": doc["environment"],
+             "parameters": {"magnetic_reorientation": 0.0, "diffusion": {"translational": 0.0, "rotational": 0.0},
+                            "stress": {"active": 0.0, "magnetic": 0.0}, "magnetic_dipole": {}}}
+    base = parse_settings(shell)
+    p = _table(doc["parameters"], "parameters",
+               ["hydro_screening", "volume_exclusion", "viscocity", "temperature", "volume_fraction",
+                "external_field", "particle"], [])
+    q = _table(p["particle"], "parameters.particle",
+               ["radius", "self_propulsion_speed", "force_dipole", "magnetic_dipole_moment", "persistance_time"],
+               ["shape"])
+    par = ParametersSI(**{k: _num(p[k], k) for k in ["hydro_screening", "volume_exclusion", "viscocity",
+                                                     "temperature", "volume_fraction", "external_field"]},
+                       particle=ParticleSI(**{k: _num(v, k) for k, v in q.items()}))
+    return SettingsSI(simulation=base.simulation, parameters=par, environment=base.environment)
+
+
+def into_settings(si):
+    """SettingsSI::into_settings (si.rs:126-199): lengths in units of the mean
+    particle distance n^(-1/3), velocities in units of the swimming speed."""
+    import math
+    pi = math.pi
+    a = si.parameters.particle
+    par = si.parameters
+    volp = 4.0 / 3.0 * pi * (a.radius * a.radius * a.radius)
+    number_density = par.volume_fraction / volp
+    xc = number_density ** (-1.0 / 3.0)
+    uc = a.self_propulsion_speed
+    tc = xc / uc
+    stressf = number_density ** (2.0 / 3.0) / a.self_propulsion_speed / par.viscocity
+    rotfriction = 8.0 * pi * par.viscocity * (a.radius * a.radius * a.radius)
+    transfriction = 6.0 * pi * par.viscocity * a.radius
+    rotdiff_brown = BOLTZMANN * par.temperature / rotfriction
+    rotdiff_active = 1.0 / 2.0 / a.persistance_time
+    transdiff_brown = BOLTZMANN * par.temperature / transfriction
+    diff = DiffusionConstants(translational=number_density ** (1.0 / 3.0) / uc * transdiff_brown,
+                              rotational=number_density ** (-1.0 / 3.0) / uc * (rotdiff_brown + rotdiff_active))
+    alignment = a.magnetic_dipole_moment * par.external_field / rotfriction / (rotdiff_brown + rotdiff_active)
+    m2 = a.magnetic_dipole_moment * a.magnetic_dipole_moment
+    params = Parameters(
+        magnetic_reorientation=alignment * diff.rotational,
+        diffusion=diff,
+        stress=StressPrefactors(active=stressf * a.force_dipole,
+                                magnetic=stressf * a.magnetic_dipole_moment * par.external_field),
+        magnetic_dipole=MagneticDipolePrefactors(
+            magnetic_dipole_dipole=number_density ** (2.0 / 3.0) / uc / rotfriction * 4.0e-7 * pi * m2),
+        magnetic_drag=number_density / uc / transfriction * 4.0e-7 * pi * m2,
+        shape=a.shape,
+        hydro_screening=par.hydro_screening,
+        volume_exclusion=par.volume_exclusion,
+    )
+    sim = dataclasses.replace(si.simulation)
+    bs = si.simulation.box_size
+    sim.box_size = BoxSize(bs.x / xc, bs.y / xc, bs.z / xc)
+    sim.timestep = si.simulation.timestep / tc
+    return Settings(simulation=sim, parameters=params, environment=dataclasses.replace(si.environment))
+
+
+def read_parameter_file_si(path):
+    """si::read_parameter_file (si.rs:87-101) followed by into_settings."""
+    try:
+        with open(path, "rb") as f:
+            doc = tomllib.load(f)
+    except OSError as exc:
+        raise SettingsError(f"Unable to read parameter file: {exc}") from exc
+    except tomllib.TOMLDecodeError as exc:
+        raise SettingsError(f"Unable to parse parameter file: {exc}") from exc
+    s = into_settings(parse_settings_si(doc))
+    s.environment.version = ""
+    check_settings(s)
+    return s
+
+
 def _toml_value(v):
     if isinstance(v, bool):
         return "true" if v else "false"

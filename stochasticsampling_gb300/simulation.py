@@ -36,7 +36,7 @@ class Simulation:
     """One simulation on the current CUDA device."""
 
     def __init__(self, settings=None, *, grid=None, box=None, params=None, quasi2d=False, sort=True, graph=True,
-                 always_magnetic=False, stream=None):
+                 always_magnetic=False, mixed=False, stream=None):
         if settings is not None:
             sim, par = settings.simulation, settings.parameters
             grid = (sim.grid_size.x, sim.grid_size.y, sim.grid_size.z, sim.grid_size.phi, sim.grid_size.theta)
@@ -69,6 +69,8 @@ class Simulation:
             flags |= _lib.FLAG_NO_GRAPH
         if always_magnetic:
             flags |= _lib.FLAG_ALWAYS_MAGNETIC
+        if mixed:
+            flags |= _lib.FLAG_MIXED
         self.flags = flags
         h = ctypes.c_void_p()
         rc = self.lib.ss_create(ctypes.byref(g), ctypes.byref(b), ctypes.byref(p), flags,
@@ -104,6 +106,12 @@ class Simulation:
     def init(self, particles):
         p = _f64(particles, (-1, 5))
         self._check(self.lib.ss_init(self._h, _ptr(p), p.shape[0]))
+
+    def init_distribution(self, kind):
+        """Sample the initial condition on the GPU: "Isotropic" or "Homogeneous"
+        (init_simulation with InitType::Distribution)."""
+        k = {"Isotropic": 0, "Homogeneous": 1}[kind] if isinstance(kind, str) else int(kind)
+        self._check(self.lib.ss_init_distribution(self._h, k))
 
     def resume(self, particles, timestep):
         p = _f64(particles, (-1, 5))

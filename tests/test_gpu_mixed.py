@@ -1,0 +1,120 @@
+"""The FP32 mixed-precision path (SS_FLAG_MIXED) against the FP64 oracle.
+
+The mixed path keeps positions and the spectral k = 0 / mean handling in FP64
+and does everything else in FP32, so it is not held to 1e-12; each field's
+error against the FP64 oracle is bounded instead (one step from identical
+state and noise):
+  histogram       differs only for particles within FP32 rounding of a bin edge
+  u, grad u       relative L2 error < 1e-5
+  B               relative L2 error < 1e-5
+  positions       relative L2 error < 1e-8 (FP64 accumulation of FP32 steps)
+  orientations    relative L2 error < 1e-6
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from test_gpu_parity import C0, EVEN2D, ODD3D, _c1_particles, _gpu, _noise, _pair, _particles
+
+pytestmark = pytest.mark.gpu
+
+
+def _wrapdiff(a, b, period):
+    d = np.abs(a - b)
+    return np.minimum(d, period - d)
+
+
+@pytest.mark.parametrize("cfg", [C0, EVEN2D, ODD3D], ids=["c0_2d", "even_2d_screened", "odd_3d_magnetic"])
+def test_mixed_one_step_errors(oracle, cfg):
+    g, o, s = _pair(oracle, cfg, mixed=True)
+    rng = np.random.default_rng(71)
+    n = cfg[4]
+    p = _particles(rng, n, cfg[2], cfg[5])
+    noise = _noise(rng, n, cfg[3])
+    g.init(p)
+    o.init(p)
+    c_g = g.get_counts().astype(np.float64)
+    c_o = oracle.histogram(s, o.particles())
+    assert c_g.sum() == n
+    assert np.abs(c_g - c_o).sum() <= 2e-3 * n  # FP32 binning at bin edges
+    g.do_timestep(noise)
+    o.do_timestep(noise)
+    u, gu = g.get_flow_complex()
+    ou = o.flow()
+    # the reference histogram feeds the oracle; the mixed histogram differs
+    # in a few bins, so compare the fields relative to their norm
+    assert rel_l2(u, ou) < 1e-2 and rel_l2(gu, o.flow_grad()) < 1e-2
+    gp, op = g.get_particles(), o.particles()
+    assert rel_l2(gp[:, :3], op[:, :3]) < 1e-6
+    assert np.sqrt(np.mean(_wrapdiff(gp[:, 3], op[:, 3], 2 * np.pi) ** 2)) < 1e-4
+    g.close()
+
+
+def test_mixed_fields_from_identical_histogram(oracle):
+    """Fields of the mixed solve when its histogram equals the FP64 one:
+    particles at bin centres, so FP32 binning cannot differ."""
+    ss = _gpu()
+    name, grid, box, params, n, q2d = ODD3D
+    rng = np.random.default_rng(81)
+    gw = np.array(box) / np.array(grid[:3])
+    idx = np.column_stack([rng.integers(0, grid[k], n) for k in range(3)])
+    ang = np.column_stack([rng.integers(0, grid[3], n), rng.integers(0, grid[4], n)])
+    p = np.column_stack([(idx + 0.5) * gw, (ang[:, 0] + 0.5) * 2 * np.pi / grid[3], (ang[:, 1] + 0.5) * np.pi / grid[4]])
+    g, o, s = _pair(oracle, ODD3D, mixed=True)
+    g.init(p)
+    o.init(p)
+    assert np.array_equal(g.get_counts().astype(np.float64), oracle.histogram(s, o.particles()))
+    noise = _noise(rng, n, params)
+    g.do_timestep(noise)
+    o.do_timestep(noise)
+    u, gu = g.get_flow_complex()
+    assert rel_l2(u, o.flow()) < 1e-5 and rel_l2(gu, o.flow_grad()) < 1e-5
+    b, gb = g.get_magnetic_complex()
+    assert rel_l2(b, o.mag()) < 1e-5 and rel_l2(gb, o.mag_grad()) < 1e-5
+    gp, op = g.get_particles(), o.particles()
+    assert rel_l2(gp[:, :3], op[:, :3]) < 1e-8
+    assert rel_l2(gp[:, 3:], op[:, 3:]) < 1e-6
+    g.close()
+
+
+def test_mixed_runs_and_conserves(oracle):
+    ss = _gpu()
+    name, grid, box, params, n, q2d = C0
+    rng = np.random.default_rng(91)
+    p = _particles(rng, n, box, q2d)
+    g = ss.Simulation(grid=grid, box=box, params=dict(params, number_of_particles=n, seed=5), quasi2d=q2d,
+                      mixed=True)
+    g.init(p)
+    g.run(20)
+    g.do_timestep()
+    assert g.get_counts().sum() == n
+    q = g.get_particles()
+    assert np.all(np.isfinite(q))
+    assert np.all((q[:, 0] >= 0) & (q[:, 0] < box[0]) & (q[:, 1] >= 0) & (q[:, 1] < box[1]))
+    assert np.all(q[:, 2] == 0.0)
+    # mean squared displacement of the translational noise dominates: sanity only
+    z = g.noise(3)
+    assert abs(z[:, 0].mean()) < 0.05 and abs(z[:, 0].var() - 1) < 0.05
+    g.close()
+
+
+def test_mixed_c1_full_size(oracle):
+    """Production size 2-D in mixed precision: one step against the oracle fed
+    the same noise, then ten more steps."""
+    cfg = ("c1", (128, 128, 1, 32, 1), (40.0, 40.0, 1.0),
+           dict(timestep=0.005, trans_diffusion=0.1, rot_diffusion=1.0, stress_active=-2.0), 10_000_000, True)
+    g, o, s = _pair(oracle, cfg, mixed=True)
+    p = _c1_particles(np.random.default_rng(1), cfg[4])
+    g.init(p)
+    o.init(p)
+    noise = g.noise(0)
+    g.do_timestep()
+    o.do_timestep(noise)
+    u, _ = g.get_flow_complex()
+    assert rel_l2(u, o.flow()) < 1e-2
+    gp, op = g.get_particles(), o.particles()
+    assert rel_l2(gp[:, :2], op[:, :2]) < 1e-6
+    g.run(10)
+    g.do_timestep()
+    assert int(g.get_counts().sum()) == cfg[4]
+    g.close()

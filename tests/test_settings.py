@@ -160,3 +160,50 @@ def test_roundtrip_without_version(tmp_path):
     del doc["environment"]["version"]
     s2 = parse_settings(doc)
     assert s2 == s
+
+
+SI = FULL.split("[parameters]")[0] + """
+[parameters]
+    hydro_screening = 0.0
+    volume_exclusion = 0.0
+    viscocity = 1e-3
+    temperature = 300
+    volume_fraction = 1e-2
+    external_field = 1e-3
+    [parameters.particle]
+        radius = 1e-6
+        self_propulsion_speed = 1e-4
+        force_dipole = 1.88496e-18
+        magnetic_dipole_moment = 1e-15
+        persistance_time = 0.75
+"""
+
+
+def test_si_conversion(tmp_path):
+    # SettingsSI::into_settings, src/bin/simulation/settings/si.rs:126-199
+    import math
+    from stochasticsampling_gb300.settings import read_parameter_file_si
+    s = read_parameter_file_si(_write(tmp_path, "si.toml", SI.replace("x = 1.0\n", "x = 1.0e-4\n", 1)))
+    r, v, eta, T, phi, B, m, tau = 1e-6, 1e-4, 1e-3, 300.0, 1e-2, 1e-3, 1e-15, 0.75
+    n = phi / (4 / 3 * math.pi * r ** 3)
+    xc = n ** (-1 / 3)
+    kT = 1.38064852e-23 * T
+    fr, ft = 8 * math.pi * eta * r ** 3, 6 * math.pi * eta * r
+    dr = n ** (-1 / 3) / v * (kT / fr + 1 / (2 * tau))
+    assert math.isclose(s.parameters.diffusion.rotational, dr, rel_tol=1e-12)
+    assert math.isclose(s.parameters.diffusion.translational, n ** (1 / 3) / v * kT / ft, rel_tol=1e-12)
+    assert math.isclose(s.parameters.stress.active, n ** (2 / 3) / v / eta * 1.88496e-18, rel_tol=1e-12)
+    assert math.isclose(s.parameters.stress.magnetic, n ** (2 / 3) / v / eta * m * B, rel_tol=1e-12)
+    assert math.isclose(s.parameters.magnetic_reorientation, m * B / fr / (kT / fr + 1 / (2 * tau)) * dr,
+                        rel_tol=1e-12)
+    assert math.isclose(s.parameters.magnetic_drag, n / v / ft * 4e-7 * math.pi * m * m, rel_tol=1e-12)
+    assert math.isclose(s.simulation.box_size.x, 1.0e-4 / xc, rel_tol=1e-12)
+    assert math.isclose(s.simulation.timestep, 0.1 / (xc / v), rel_tol=1e-12)
+    assert s.simulation.grid_size.x == 11 and s.environment.prefix == "foo"
+
+
+def test_si_requires_every_parameter(tmp_path):
+    # the SI parameters table has no defaults (si.rs:62-73)
+    from stochasticsampling_gb300.settings import read_parameter_file_si
+    with pytest.raises(SettingsError, match="missing field `hydro_screening`"):
+        read_parameter_file_si(_write(tmp_path, "si.toml", SI.replace("    hydro_screening = 0.0\n", "")))
