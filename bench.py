@@ -173,6 +173,20 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def aggregate(ms_local, n_local, steps, world, dist):
+    """Replicas: every rank steps its own n_local particles.  The job's time
+    is the slowest rank's (max over ranks) and its throughput all particles
+    of all ranks over that time.  Returns (particle-steps/s, ms)."""
+    import torch
+    t = torch.tensor([float(ms_local)], dtype=torch.float64)
+    n = torch.tensor([float(n_local)], dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    ms = float(t[0])
+    return float(n[0]) * steps / (ms / 1e3), ms
+
+
 def measure_mixed(args, stream, p0, rank, world, dist, barrier):
     """The FP32 mixed-precision path on the same workload: throughput over K
     graph-replayed steps, and each field's error against the FP64 path after
@@ -198,10 +212,7 @@ def measure_mixed(args, stream, p0, rank, world, dist, barrier):
     sim.run(min(args.steps, 20))
     stage_ms, nprof = sim.profile_read()
     sim.profile(False)
-    t = torch.tensor([ms], dtype=torch.float64)
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    value = world * N * args.steps / (float(t[0]) / 1e3)
+    value, ms_max = aggregate(ms, N, args.steps, world, dist)
     # errors against the FP64 path (itself within 1e-15 of the FP64 oracle)
     start = sim.get_particles()
     sim.close()
@@ -226,7 +237,7 @@ def measure_mixed(args, stream, p0, rank, world, dist, barrier):
     }
     m.close()
     d.close()
-    return {"value": value, "unit": UNIT, "ms_per_step": float(t[0]) / args.steps, "dtype": "f32 + f64 positions",
+    return {"value": value, "unit": UNIT, "ms_per_step": ms_max / args.steps, "dtype": "f32 + f64 positions",
             "stage_ms": {k: v / max(1, nprof) for k, v in stage_ms.items()},
             "errors_vs_fp64_one_step": errors}
 
@@ -267,11 +278,7 @@ def run_gpu(args, rank, world, dist):
         ms = e0.elapsed_time(e1)
         launches = sim.launch_count() - l0
     sim.synchronize()
-    t = torch.tensor([ms], dtype=torch.float64)
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t[0])
-    value = world * N * args.steps / (ms_max / 1e3)
+    value, ms_max = aggregate(ms, N, args.steps, world, dist)
 
     # per-stage CUDA events over K direct-launch steps (same stream, same workload)
     sim.profile(True)
@@ -297,10 +304,7 @@ def run_gpu(args, rank, world, dist):
         host_in, host_out = host_out, host_in
     torch.cuda.synchronize()
     t_e2e = time.perf_counter() - t0
-    te = torch.tensor([t_e2e], dtype=torch.float64)
-    if dist is not None:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = world * N * e2e_steps / float(te[0])
+    e2e_value, _ = aggregate(1e3 * t_e2e, N, e2e_steps, world, dist)
     sim.close()
     mixed = None if args.no_mixed else measure_mixed(args, stream, p0, rank, world, dist, barrier)
 

@@ -69,6 +69,11 @@ typedef struct {
 #define SS_FLAG_MIXED 16u          /* FP32 mixed precision: FP64 positions and k = 0 / mean handling, FP32
                                       angles, binning, contraction, FFTs, fields and Langevin arithmetic
                                       (no sort; the library seams ss_mean_* need the FP64 mode) */
+#define SS_FLAG_TRILINEAR 32u      /* gather every field by trilinear interpolation at the particle position
+                                      (src/mesh/interpolate.rs:11-119) instead of the nearest cell that
+                                      do_timestep uses (FP64 mode) */
+#define SS_FLAG_TRILINEAR_ZFROMY 64u /* as SS_FLAG_TRILINEAR, with the reference's z fraction computed from
+                                        y (interpolate.rs:22), for comparisons with that code */
 
 typedef struct ss_ctx ss_ctx;
 

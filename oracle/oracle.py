@@ -31,7 +31,7 @@ class Settings(ctypes.Structure):
         ("shape", ctypes.c_double), ("magnetic_drag", ctypes.c_double),
         ("hydro_screening", ctypes.c_double), ("volume_exclusion", ctypes.c_double),
         ("magnetic_reorientation", ctypes.c_double), ("magnetic_dipole_dipole", ctypes.c_double),
-        ("quasi2d", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("quasi2d", ctypes.c_int32), ("gather", ctypes.c_int32),
         ("seed", ctypes.c_uint64),
     ]
 
@@ -87,6 +87,7 @@ def lib():
         L.orc_flow_field.argtypes = [sp, c_double_p, ctypes.c_double, c_double_p, c_double_p, ctypes.c_int]
         L.orc_magnetic_field.argtypes = [sp, c_double_p, c_double_p, c_double_p, ctypes.c_int]
         L.orc_vector_gradient.argtypes = [sp, c_double_p, c_double_p]
+        L.orc_interpolate.argtypes = [sp, c_double_p, ctypes.c_int, c_double_p, ctypes.c_int, c_double_p]
         L.orc_langevin.argtypes = [c_double_p, ctypes.c_uint32, ctypes.POINTER(LangevinArgs), c_double_p]
         L.orc_sim_new.restype = ctypes.c_void_p
         L.orc_sim_new.argtypes = [sp, ctypes.c_uint64, ctypes.c_int]
@@ -113,7 +114,7 @@ def _p(a):
 
 def make_settings(grid, box, timestep=0.0, trans_diff=0.0, rot_diff=0.0, active=0.0, magnetic=0.0,
                   shape=0.0, magnetic_drag=0.0, hydro_screening=0.0, volume_exclusion=0.0,
-                  magnetic_reorientation=0.0, magnetic_dipole_dipole=0.0, quasi2d=False, seed=1):
+                  magnetic_reorientation=0.0, magnetic_dipole_dipole=0.0, quasi2d=False, seed=1, gather=0):
     s = Settings()
     s.gx, s.gy, s.gz, s.gphi, s.gtheta = [int(v) for v in grid]
     s.bx, s.by, s.bz = [float(v) for v in box]
@@ -122,6 +123,7 @@ def make_settings(grid, box, timestep=0.0, trans_diff=0.0, rot_diff=0.0, active=
     s.magnetic_drag, s.hydro_screening, s.volume_exclusion = magnetic_drag, hydro_screening, volume_exclusion
     s.magnetic_reorientation, s.magnetic_dipole_dipole = magnetic_reorientation, magnetic_dipole_dipole
     s.quasi2d = 1 if quasi2d else 0
+    s.gather = int(gather)
     s.seed = seed
     return s
 
@@ -262,6 +264,15 @@ def vector_gradient(s, bk):
     g = np.zeros((3, 3, s.gx, s.gy, s.gz), dtype=np.complex128)
     lib().orc_vector_gradient(ctypes.byref(s), b.ctypes.data_as(c_double_p), g.ctypes.data_as(c_double_p))
     return g
+
+
+def interpolate(s, field, p, zbug=False):
+    f = np.ascontiguousarray(field, dtype=np.float64)
+    ncomp = f.shape[0]
+    q = np.ascontiguousarray(p, dtype=np.float64)
+    o = np.zeros(ncomp)
+    lib().orc_interpolate(ctypes.byref(s), _p(f), ncomp, _p(q), 1 if zbug else 0, _p(o))
+    return o
 
 
 def langevin(p, mask, box=(10.0, 10.0, 10.0), **kw):

@@ -626,6 +626,48 @@ void orc_magnetic_field(const orc_settings *s, const double *dist, double *b, do
 }
 
 /* ===================================================================== */
+/* trilinear interpolation, src/mesh/interpolate.rs                      */
+/* ===================================================================== */
+
+/* lerp 0.2.0: a * (1 - t) + b * t */
+static double lerp(double a, double b, double t) { return a * (1.0 - t) + b * t; }
+
+static uint64_t wrap_idx(int64_t i, uint64_t n) { return (uint64_t)((i + (int64_t)n) % (int64_t)n); }
+
+void orc_interpolate(const orc_settings *s, const double *field, int ncomp, const double p[3], int zbug,
+                     double *out) {
+    double gw[5];
+    orc_grid_width(s, gw);
+    uint64_t nc = s->gx * s->gy * s->gz;
+    /* relative position, interpolate.rs:19-23 (Rust % on f64 is fmod) */
+    double fx = fmod(p[0] / gw[0] + 0.5, 1.0);
+    double fy = fmod(p[1] / gw[1] + 0.5, 1.0);
+    double fz = fmod((zbug ? p[1] : p[2]) / gw[2] + 0.5, 1.0);
+    /* lower corner, get_neighbouring_cell_values :68-78: floor(p / gw - 0.5) */
+    int64_t ix = (int64_t)floor(p[0] / gw[0] - 0.5);
+    int64_t iy = (int64_t)floor(p[1] / gw[1] - 0.5);
+    int64_t iz = (int64_t)floor(p[2] / gw[2] - 0.5);
+    for (int c = 0; c < ncomp; ++c) {
+        const double *f = field + (uint64_t)c * nc;
+        double v[2][2][2];
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b)
+                for (int d = 0; d < 2; ++d) {
+                    uint64_t i = wrap_idx(ix + a, s->gx), j = wrap_idx(iy + b, s->gy), k = wrap_idx(iz + d, s->gz);
+                    v[a][b][d] = f[(i * s->gy + j) * s->gz + k];
+                }
+        /* trilinear_interpolation :104-119 */
+        double c00 = lerp(v[0][0][0], v[1][0][0], fx);
+        double c01 = lerp(v[0][0][1], v[1][0][1], fx);
+        double c10 = lerp(v[0][1][0], v[1][1][0], fx);
+        double c11 = lerp(v[0][1][1], v[1][1][1], fx);
+        double c0 = lerp(c00, c10, fy);
+        double c1 = lerp(c01, c11, fy);
+        out[c] = lerp(c0, c1, fz);
+    }
+}
+
+/* ===================================================================== */
 /* Langevin builder, src/integrators/langevin_builder/{mod.rs,modifiers.rs} */
 /* ===================================================================== */
 
@@ -744,6 +786,7 @@ struct orc_sim {
     double *particles, *dist, *noise;
     double *u, *grad, *b, *gradb, *dens;
     double *vort, *strain;  /* real parts of W and E, [3][3][ncell] */
+    double *re_u, *re_b, *re_gradb;  /* real parts for the trilinear gather */
     uint64_t *rng;          /* PCG32 state per thread (baseline noise only) */
 };
 
@@ -772,6 +815,9 @@ orc_sim *orc_sim_new(const orc_settings *s, uint64_t n, int nthreads) {
     sim->dens = (double *)calloc(sim->ncell, sizeof(double));
     sim->vort = (double *)calloc(9 * sim->ncell, sizeof(double));
     sim->strain = (double *)calloc(9 * sim->ncell, sizeof(double));
+    sim->re_u = (double *)calloc(3 * sim->ncell, sizeof(double));
+    sim->re_b = (double *)calloc(3 * sim->ncell, sizeof(double));
+    sim->re_gradb = (double *)calloc(9 * sim->ncell, sizeof(double));
     /* every thread's generator seeded with the same seed, like
      * src/bin/simulation/mod.rs:126-128 */
     sim->rng = (uint64_t *)calloc(2 * (uint64_t)sim->nthreads, sizeof(uint64_t));
@@ -786,6 +832,7 @@ void orc_sim_free(orc_sim *sim) {
     if (!sim) return;
     free(sim->particles); free(sim->noise); free(sim->dist); free(sim->u); free(sim->grad);
     free(sim->b); free(sim->gradb); free(sim->dens); free(sim->vort); free(sim->strain);
+    free(sim->re_u); free(sim->re_b); free(sim->re_gradb);
     free(sim->rng);
     free(sim);
 }
@@ -871,6 +918,13 @@ uint64_t orc_sim_step(orc_sim *sim, const double *noise) {
                 sim->vort[(uint64_t)(a * 3 + b) * nc + c] = (gab - gba) * 0.5;
                 sim->strain[(uint64_t)(a * 3 + b) * nc + c] = (gab + gba) * 0.5;
             }
+    for (uint64_t c = 0; c < nc; ++c) {
+        for (int k = 0; k < 3; ++k) {
+            sim->re_u[k * nc + c] = sim->u[2 * (k * nc + c)];
+            sim->re_b[k * nc + c] = sim->b[2 * (k * nc + c)];
+        }
+        for (int k = 0; k < 9; ++k) sim->re_gradb[k * nc + c] = sim->gradb[2 * (k * nc + c)];
+    }
     /* dens = sum over angles (sequential) * dtheta*dphi, mod.rs:312-316 */
     double dthph = gw[4] * gw[3];
     for (uint64_t c = 0; c < nc; ++c) {
@@ -889,17 +943,32 @@ uint64_t orc_sim_step(orc_sim *sim, const double *noise) {
         orc_cell_index(s, p, g);
         uint64_t c = (g[0] * s->gy + g[1]) * s->gz + g[2];
         orc_langevin_args a;
-        for (int k = 0; k < 3; ++k) {
-            a.flow[k] = sim->u[2 * (k * nc + c)];
-            a.b[k] = sim->b[2 * (k * nc + c)] * s->magnetic_dipole_dipole;
-            a.xi[k] = r[k];
+        double dens;
+        if (s->gather == 0) {
+            for (int k = 0; k < 3; ++k) {
+                a.flow[k] = sim->u[2 * (k * nc + c)];
+                a.b[k] = sim->b[2 * (k * nc + c)] * s->magnetic_dipole_dipole;
+            }
+            for (int k = 0; k < 9; ++k) {
+                a.vort[k] = sim->vort[(uint64_t)k * nc + c];
+                a.strain[k] = sim->strain[(uint64_t)k * nc + c];
+                a.gradb[k] = sim->gradb[2 * ((uint64_t)k * nc + c)];
+            }
+            dens = sim->dens[c];
+        } else {
+            /* every gathered field interpolated at the particle position */
+            int zb = s->gather == 2;
+            double bi[3];
+            orc_interpolate(s, sim->re_u, 3, p, zb, a.flow);
+            orc_interpolate(s, sim->vort, 9, p, zb, a.vort);
+            orc_interpolate(s, sim->strain, 9, p, zb, a.strain);
+            orc_interpolate(s, sim->re_b, 3, p, zb, bi);
+            orc_interpolate(s, sim->re_gradb, 9, p, zb, a.gradb);
+            orc_interpolate(s, sim->dens, 1, p, zb, &dens);
+            for (int k = 0; k < 3; ++k) a.b[k] = bi[k] * s->magnetic_dipole_dipole;
         }
-        for (int k = 0; k < 9; ++k) {
-            a.vort[k] = sim->vort[(uint64_t)k * nc + c];
-            a.strain[k] = sim->strain[(uint64_t)k * nc + c];
-            a.gradb[k] = sim->gradb[2 * ((uint64_t)k * nc + c)];
-        }
-        double volex = s->volume_exclusion * sim->dens[c];
+        for (int k = 0; k < 3; ++k) a.xi[k] = r[k];
+        double volex = s->volume_exclusion * dens;
         a.drag = s->magnetic_drag;
         a.reorientation = s->magnetic_reorientation;
         a.shape = s->shape;

@@ -47,7 +47,9 @@ typedef struct {
     double magnetic_reorientation;       /* parameters.magnetic_reorientation */
     double magnetic_dipole_dipole;       /* parameters.magnetic_dipole.magnetic_dipole_dipole */
     int32_t quasi2d;                     /* cargo feature quasi2d as a runtime flag */
-    int32_t reserved;
+    int32_t gather;                      /* 0 nearest cell (the step), 1 trilinear
+                                            (src/mesh/interpolate.rs), 2 trilinear with
+                                            the reference's z fraction from y (:22) */
     uint64_t seed;                       /* simulation.seed */
 } orc_settings;
 
@@ -94,6 +96,12 @@ void orc_magnetic_field(const orc_settings *s, const double *dist,
 /* MagneticSolver::update_gradient on a given k-space field (no inverse of b) */
 void orc_vector_gradient(const orc_settings *s, const double *bk /* cplx [3][ncell] */,
                          double *grad /* cplx [3][3][ncell], inverse-transformed */);
+
+/* interpolate_vector_field (src/mesh/interpolate.rs:11-40) of `ncomp`
+ * real fields [ncomp][gx][gy][gz] at position p; zbug != 0 keeps the
+ * reference's z fraction computed from p.y (:22) */
+void orc_interpolate(const orc_settings *s, const double *field, int ncomp, const double p[3], int zbug,
+                     double *out);
 
 /* ---- Langevin builder ------------------------------------------------- */
 enum {

@@ -31,6 +31,8 @@ FLAG_ALWAYS_MAGNETIC = 2
 FLAG_NO_SORT = 4
 FLAG_NO_GRAPH = 8
 FLAG_MIXED = 16
+FLAG_TRILINEAR = 32
+FLAG_TRILINEAR_ZFROMY = 64
 
 NUM_STAGES = 8
 STAGES = ["contract", "fft_forward", "kspace", "fft_inverse", "table", "update", "sort", "other"]

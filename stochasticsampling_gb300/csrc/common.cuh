@@ -36,8 +36,9 @@ constexpr int T_E22 = 11;
 constexpr int T_DIFF = 12;  // sqrt(2 dt (Dt + volume_exclusion*density)) (mod.rs:333-346)
 constexpr int T_B = 13;     // Re B * magnetic_dipole_dipole [3]  (mod.rs:337-338)
 constexpr int T_GB = 16;    // Re grad B [3][3]                   (mod.rs:339)
+constexpr int T_DENS = 25;  // density, sum_a f * dtheta dphi (rows of stride 32 only)
 constexpr int TABLE_STRIDE = 16;      // without the dipolar solver
-constexpr int TABLE_STRIDE_MAG = 32;  // with it
+constexpr int TABLE_STRIDE_MAG = 32;  // with it, or with the trilinear gather
 
 // Langevin modifier bits, in the chain order of src/bin/simulation/mod.rs:348-363
 enum : uint32_t {
@@ -75,6 +76,7 @@ struct DevParams {
     double cos_half_pi, sin_half_pi;  // cos/sin of kPiHalf as evaluated on this device
     unsigned long long seed;
     int quasi2d;
+    int gather;        // 0 nearest cell, 1 trilinear, 2 trilinear with the z fraction from y
     uint32_t mask;     // Langevin modifiers that can change the state
 };
 
@@ -230,6 +232,56 @@ struct MatrixFields {
     __device__ void strain_dot(const double n[3], double f[3]) const { rowdot(strain_, n, f); }
     __device__ void gradb_dot(const double n[3], double f[3]) const { rowdot(gradb_, n, f); }
 };
+
+// Trilinear gather (src/mesh/interpolate.rs:11-119): the fields at the
+// particle position from the eight surrounding cell centres, periodic.
+// q = position / grid width; fraction fmod(q + 0.5, 1) (:19-23, with the
+// reference's y in place of z when zbug), lower corner floor(q - 0.5)
+// (:68-78), lerp a (1 - t) + b t (lerp 0.2.0) along x, then y, then z
+// (:104-119).  The interpolated row holds u, W, E, B mdd, grad B and the
+// density; the diffusion length is formed from the interpolated density.
+template <bool MAG>
+__device__ __forceinline__ void trilinear_row(const double *__restrict__ table, const DevParams &P, double x,
+                                              double y, double z, double *row) {
+    double qx = x / P.gw[0], qy = y / P.gw[1], qz = z / P.gw[2];
+    double ax = qx + 0.5, ay = qy + 0.5, az = (P.gather == 2 ? y / P.gw[2] : qz) + 0.5;
+    double t[3] = {ax - floor(ax), ay - floor(ay), az - floor(az)};  // fmod(., 1) for a >= 0, exact
+    int n[3] = {P.gx, P.gy, P.gz};
+    double lo[3] = {floor(qx - 0.5), floor(qy - 0.5), floor(qz - 0.5)};
+    int c[3][2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        int i = (int)lo[k];
+        c[k][0] = (i + n[k]) % n[k];
+        c[k][1] = (i + 1 + n[k]) % n[k];
+    }
+    const double *r[2][2][2];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int d = 0; d < 2; ++d)
+                r[a][b][d] = table + (long long)((c[0][a] * P.gy + c[1][b]) * P.gz + c[2][d]) * TABLE_STRIDE_MAG;
+    const double sx = 1.0 - t[0], sy = 1.0 - t[1], sz = 1.0 - t[2];
+    auto lerp3 = [&](int j) {
+        double c00 = r[0][0][0][j] * sx + r[1][0][0][j] * t[0];
+        double c01 = r[0][0][1][j] * sx + r[1][0][1][j] * t[0];
+        double c10 = r[0][1][0][j] * sx + r[1][1][0][j] * t[0];
+        double c11 = r[0][1][1][j] * sx + r[1][1][1][j] * t[0];
+        double c0 = c00 * sy + c10 * t[1];
+        double c1 = c01 * sy + c11 * t[1];
+        return c0 * sz + c1 * t[2];
+    };
+#pragma unroll
+    for (int j = 0; j < 12; ++j) row[j] = lerp3(j);
+    if (MAG) {
+#pragma unroll
+        for (int j = T_B; j < T_GB + 9; ++j) row[j] = lerp3(j);
+    }
+    double dens = lerp3(T_DENS);
+    row[T_DIFF] = sqrt(2.0 * P.dt * (P.Dt + P.volex * dens));
+}
 
 // One particle through LangevinBuilder::new -> modifiers -> step -> noise ->
 // finalize (src/integrators/langevin_builder/mod.rs:25-125,

@@ -168,6 +168,7 @@ __global__ void __launch_bounds__(256) k_contract(const uint32_t *__restrict__ c
         double dens = acc[12] * P.dthph;
         double volex = P.volex * dens;
         table[(long long)cell * tstride + T_DIFF] = sqrt(2.0 * P.dt * (P.Dt + volex));
+        if (tstride == TABLE_STRIDE_MAG) table[(long long)cell * tstride + T_DENS] = dens;
         if (!FROM_DIST) cellcount[cell] = csum;
     }
 }
@@ -286,7 +287,7 @@ __global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__
 // particle state once.  NOISE: 0 = Philox on device, 1 = host array [N][5]
 // indexed by the caller's particle order.
 // ------------------------------------------------------------------------
-template <bool Q2D, bool MAG, int NOISE>
+template <bool Q2D, bool MAG, int NOISE, bool TRI>
 __global__ void __launch_bounds__(256) k_update(DevParams P, double *__restrict__ x, double *__restrict__ y,
                                                 double *__restrict__ z, double *__restrict__ phi,
                                                 double *__restrict__ theta, uint32_t *__restrict__ key,
@@ -296,11 +297,16 @@ __global__ void __launch_bounds__(256) k_update(DevParams P, double *__restrict_
                                                 uint32_t *__restrict__ counts_next, uint32_t *__restrict__ errflag) {
     unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    const int ts = MAG ? TABLE_STRIDE_MAG : TABLE_STRIDE;
+    const int ts = (MAG || TRI) ? TABLE_STRIDE_MAG : TABLE_STRIDE;
     uint32_t cell = key[i];
     uint32_t pid = id[i];
     double px = x[i], py = y[i], pz = z[i], pph = phi[i], pth = theta[i];
     TableFields F{table + (long long)cell * ts};
+    double trow[TABLE_STRIDE_MAG];
+    if (TRI) {
+        trilinear_row<MAG>(table, P, px, py, pz, trow);
+        F.r = trow;
+    }
     double xi[3], ca, sa, rot;
     if (NOISE == 0) {
         philox_noise<Q2D>(P.seed, pid, *d_step, P.sigma_rot, xi, ca, sa, rot);
@@ -540,16 +546,19 @@ void launch_update(cudaStream_t s, bool q2d, bool mag, bool host_noise, const De
                    const unsigned long long *d_step, uint32_t *counts_next, uint32_t *err) {
     if (!P.n) return;
     unsigned b = nblocks(P.n, 256);
-#define SS_UPD(Q, M, N) \
-    k_update<Q, M, N><<<b, 256, 0, s>>>(P, xs[0], xs[1], xs[2], xs[3], xs[4], key, id, table, noise, d_step, \
-                                        counts_next, err)
+#define SS_UPD(Q, M, N, T)                                                                                   \
+    k_update<Q, M, N, T><<<b, 256, 0, s>>>(P, xs[0], xs[1], xs[2], xs[3], xs[4], key, id, table, noise, d_step, \
+                                           counts_next, err)
+#define SS_UPD_T(Q, M, N) \
+    do { if (P.gather) SS_UPD(Q, M, N, true); else SS_UPD(Q, M, N, false); } while (0)
     if (q2d) {
-        if (mag) { if (host_noise) SS_UPD(true, true, 1); else SS_UPD(true, true, 0); }
-        else { if (host_noise) SS_UPD(true, false, 1); else SS_UPD(true, false, 0); }
+        if (mag) { if (host_noise) SS_UPD_T(true, true, 1); else SS_UPD_T(true, true, 0); }
+        else { if (host_noise) SS_UPD_T(true, false, 1); else SS_UPD_T(true, false, 0); }
     } else {
-        if (mag) { if (host_noise) SS_UPD(false, true, 1); else SS_UPD(false, true, 0); }
-        else { if (host_noise) SS_UPD(false, false, 1); else SS_UPD(false, false, 0); }
+        if (mag) { if (host_noise) SS_UPD_T(false, true, 1); else SS_UPD_T(false, true, 0); }
+        else { if (host_noise) SS_UPD_T(false, false, 1); else SS_UPD_T(false, false, 0); }
     }
+#undef SS_UPD_T
 #undef SS_UPD
 }
 

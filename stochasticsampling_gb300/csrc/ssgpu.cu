@@ -251,7 +251,7 @@ static void mark(ss_ctx *c, int stage) {
 // ---------------------------------------------------------------------------
 static int enqueue_solve(ss_ctx *c, bool flow, bool mag, const uint32_t *counts, const double *dist, double screening,
                          int pcur, bool sort_now, uint64_t *nl) {
-    const int ts = c->mag_step ? TABLE_STRIDE_MAG : TABLE_STRIDE;
+    const int ts = (c->mag_step || c->P.gather) ? TABLE_STRIDE_MAG : TABLE_STRIDE;
     mark(c, 0);
     launch_contract(c->stream, flow, mag, counts, dist, c->lut, kLutN, c->kern, c->P, c->fwd, c->table, ts,
                     c->cellcount);
@@ -516,6 +516,10 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     c->sort = (flags & SS_FLAG_NO_SORT) == 0;
     c->use_graph = (flags & SS_FLAG_NO_GRAPH) == 0;
     c->mixed = (flags & SS_FLAG_MIXED) != 0;
+    if (c->mixed && (flags & (SS_FLAG_TRILINEAR | SS_FLAG_TRILINEAR_ZFROMY))) {
+        destroy_impl(c);
+        return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "the trilinear gather is available in the FP64 mode only");
+    }
     if (c->mixed) c->sort = false;
     c->mag_step = (flags & SS_FLAG_ALWAYS_MAGNETIC) || params->magnetic_dipole_dipole != 0.0 ||
                   params->magnetic_drag != 0.0;
@@ -565,6 +569,7 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     P.sigma_rot = std::sqrt(2. * params->rot_diffusion * params->timestep);
     P.seed = params->seed;
     P.quasi2d = c->q2d ? 1 : 0;
+    P.gather = (flags & SS_FLAG_TRILINEAR_ZFROMY) ? 2 : (flags & SS_FLAG_TRILINEAR) ? 1 : 0;
     uint32_t mask = M_ALL;
     if (params->magnetic_reorientation == 0.0) mask &= ~M_EXTERNAL_FIELD;
     if (params->shape == 0.0) mask &= ~M_JEFFREY_STRAIN;

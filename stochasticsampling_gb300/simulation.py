@@ -36,7 +36,7 @@ class Simulation:
     """One simulation on the current CUDA device."""
 
     def __init__(self, settings=None, *, grid=None, box=None, params=None, quasi2d=False, sort=True, graph=True,
-                 always_magnetic=False, mixed=False, stream=None):
+                 always_magnetic=False, mixed=False, gather="nearest", stream=None):
         if settings is not None:
             sim, par = settings.simulation, settings.parameters
             grid = (sim.grid_size.x, sim.grid_size.y, sim.grid_size.z, sim.grid_size.phi, sim.grid_size.theta)
@@ -71,6 +71,8 @@ class Simulation:
             flags |= _lib.FLAG_ALWAYS_MAGNETIC
         if mixed:
             flags |= _lib.FLAG_MIXED
+        flags |= {"nearest": 0, "trilinear": _lib.FLAG_TRILINEAR,
+                  "trilinear_zfromy": _lib.FLAG_TRILINEAR_ZFROMY}[gather]
         self.flags = flags
         h = ctypes.c_void_p()
         rc = self.lib.ss_create(ctypes.byref(g), ctypes.byref(b), ctypes.byref(p), flags,

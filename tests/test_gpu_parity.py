@@ -290,6 +290,39 @@ def test_lazy_magnetic_field(oracle):
         g.close()
 
 
+# ------------------------------------------------------ trilinear gather
+@pytest.mark.parametrize("gather", [1, 2], ids=["trilinear", "trilinear_zfromy"])
+@pytest.mark.parametrize("cfg", [SMALL3D, EVEN2D], ids=["small_3d_all_terms", "even_2d_screened"])
+def test_trilinear_gather_matches_oracle(oracle, cfg, gather):
+    """The gather of src/mesh/interpolate.rs (periodic trilinear between cell
+    centres) in place of the nearest cell, on every gathered field."""
+    ss = _gpu()
+    name, grid, box, params, n, q2d = cfg
+    p_ = dict(params, number_of_particles=n, seed=1)
+    g = ss.Simulation(grid=grid, box=box, params=p_, quasi2d=q2d, always_magnetic=True,
+                      gather={1: "trilinear", 2: "trilinear_zfromy"}[gather])
+    s = oracle.make_settings(grid, box, timestep=p_["timestep"], trans_diff=p_.get("trans_diffusion", 0.0),
+                             rot_diff=p_.get("rot_diffusion", 0.0), active=p_.get("stress_active", 0.0),
+                             magnetic=p_.get("stress_magnetic", 0.0), shape=p_.get("shape", 0.0),
+                             magnetic_drag=p_.get("magnetic_drag", 0.0),
+                             hydro_screening=p_.get("hydro_screening", 0.0),
+                             volume_exclusion=p_.get("volume_exclusion", 0.0),
+                             magnetic_reorientation=p_.get("magnetic_reorientation", 0.0),
+                             magnetic_dipole_dipole=p_.get("magnetic_dipole_dipole", 0.0), quasi2d=q2d,
+                             gather=gather)
+    o = oracle.Simulation(s, n, nthreads=8)
+    rng = np.random.default_rng(101)
+    p = _particles(rng, n, box, q2d)
+    noise = _noise(rng, n, params)
+    g.init(p)
+    o.init(p)
+    g.do_timestep(noise)
+    o.do_timestep(noise)
+    gp, op = g.get_particles(), o.particles()
+    assert rel_l2(gp[:, :3], op[:, :3]) < TOL and rel_l2(gp[:, 3:], op[:, 3:]) < TOL
+    g.close()
+
+
 # ---------------------------------------------------------------- errors
 def test_error_paths(oracle):
     ss = _gpu()

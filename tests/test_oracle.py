@@ -324,3 +324,31 @@ def test_step_reference_semantics(oracle):
     p1 = sim.particles()
     assert p1.shape == p0.shape and np.all(np.isfinite(p1))
     assert np.all((p1[:, 0] >= 0) & (p1[:, 0] < 3.0)) and np.all((p1[:, 4] >= 0) & (p1[:, 4] <= PI))
+
+
+# ------------------------------------------------ trilinear interpolation
+def test_interpolate_reproduces_cell_values_and_linear_fields(oracle):
+    # src/mesh/interpolate.rs: cell-centred samples, periodic neighbours
+    s = oracle.make_settings((6, 5, 4, 1, 1), (3.0, 2.5, 2.0))
+    gw = oracle.grid_width(s)
+    rng = np.random.default_rng(3)
+    f = rng.random((2, 6, 5, 4))
+    for i, j, k in [(0, 0, 0), (2, 3, 1), (5, 4, 3)]:
+        c = np.array([(i + 0.5) * gw[0], (j + 0.5) * gw[1], (k + 0.5) * gw[2]])
+        assert np.allclose(oracle.interpolate(s, f, c), f[:, i, j, k], rtol=0, atol=1e-15)
+    x = (np.arange(6) + 0.5) * gw[0]
+    lin = np.broadcast_to((1.0 + 2.0 * x)[:, None, None], (6, 5, 4))[None].copy()
+    for px in [0.9, 1.3, 2.2]:  # between the first and last centre: no periodic wrap
+        got = oracle.interpolate(s, lin, np.array([px, 1.1, 0.7]))
+        assert abs(got[0] - (1.0 + 2.0 * px)) < 1e-14
+
+
+def test_interpolate_z_fraction_from_y(oracle):
+    # interpolate.rs:22 takes the z fraction from position.y; only the
+    # compatibility flag reproduces that
+    s = oracle.make_settings((4, 4, 4, 1, 1), (4.0, 4.0, 4.0))
+    z = (np.arange(4) + 0.5)
+    f = np.broadcast_to(z[None, None, :], (4, 4, 4))[None].copy()
+    p = np.array([1.5, 1.75, 1.25])
+    assert abs(oracle.interpolate(s, f, p)[0] - 1.25) < 1e-15
+    assert oracle.interpolate(s, f, p, zbug=True)[0] != oracle.interpolate(s, f, p)[0]
