@@ -112,65 +112,66 @@ __global__ void k_counts_to_dist(const uint32_t *__restrict__ counts, long long 
 // ------------------------------------------------------------------------
 // angular contraction: average_stress (src/flowfield/stress.rs:60-96),
 // DirectorField::from_distribution (src/polarization/director.rs:36-61) and
-// the density of src/bin/simulation/mod.rs:312-316.  One warp per cell,
-// lanes over angle bins.
-// kern rows: 0..8 stress kernel K_ij, 9..11 orientation kernel n_c.
+// the density of src/bin/simulation/mod.rs:312-316.  One thread per cell runs
+// over that cell's angle row (one cache line per thread for 32 angles,
+// reused from L1), with the angle kernels broadcast from shared memory; the
+// sums run in angle order, like sum_axis.  kern rows: 0..8 stress kernel
+// K_ij, 9..11 orientation kernel n_c.
 // ------------------------------------------------------------------------
-template <bool STRESS, bool MAG, bool FROM_DIST>
-__global__ void __launch_bounds__(256) k_contract(const uint32_t *__restrict__ counts,
-                                                  const double *__restrict__ dist,
-                                                  const double *__restrict__ lut, int lut_n,
-                                                  const double *__restrict__ kern, DevParams P,
-                                                  double2 *__restrict__ fwd, double *__restrict__ table,
-                                                  int tstride, uint32_t *__restrict__ cellcount) {
-    int cell = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-    int lane = threadIdx.x & 31;
-    if (cell >= P.ncell) return;
+template <bool STRESS, bool MAG, bool FROM_DIST, bool SMEM>
+__global__ void __launch_bounds__(64) k_contract(const uint32_t *__restrict__ counts,
+                                                 const double *__restrict__ dist,
+                                                 const double *__restrict__ lut, int lut_n,
+                                                 const double *__restrict__ kern, DevParams P,
+                                                 double2 *__restrict__ fwd, double *__restrict__ table,
+                                                 int tstride, uint32_t *__restrict__ cellcount) {
+    extern __shared__ double sk[];
     const int na = P.nang;
+    if (SMEM) {
+        for (int i = threadIdx.x; i < 12 * na; i += blockDim.x) sk[i] = kern[i];
+        __syncthreads();
+    }
+    const double *K = SMEM ? sk : kern;
+    int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.ncell) return;
     double acc[13];
 #pragma unroll
     for (int j = 0; j < 13; ++j) acc[j] = 0.0;
     uint32_t csum = 0;
-    for (int a = lane; a < na; a += 32) {
+    const long long row = (long long)cell * na;
+    for (int a = 0; a < na; ++a) {
         double f;
         if (FROM_DIST) {
-            f = dist[(long long)cell * na + a];
+            f = dist[row + a];
         } else {
-            uint32_t c = counts[(long long)cell * na + a];
+            uint32_t c = counts[row + a];
             csum += c;
             f = ((int)c < lut_n) ? __ldg(lut + c) : ((double)c / P.dist_den) * P.volume;
         }
         if (STRESS) {
 #pragma unroll
-            for (int j = 0; j < 9; ++j) acc[j] = fma(__ldg(kern + j * na + a), f, acc[j]);
+            for (int j = 0; j < 9; ++j) acc[j] = fma(K[j * na + a], f, acc[j]);
         }
         if (MAG) {
 #pragma unroll
-            for (int j = 9; j < 12; ++j) acc[j] = fma(__ldg(kern + j * na + a), f, acc[j]);
+            for (int j = 9; j < 12; ++j) acc[j] = fma(K[j * na + a], f, acc[j]);
         }
         acc[12] += f;
     }
+    const int nc = P.ncell;
+    if (STRESS) {
 #pragma unroll
-    for (int j = 0; j < 13; ++j) {
-        if ((j < 9 && STRESS) || (j >= 9 && j < 12 && MAG) || j == 12) acc[j] = warp_sum(acc[j]);
+        for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = make_double2(acc[j] * P.measure, 0.0);
     }
-    if (!FROM_DIST) csum = warp_sum_u(csum);
-    if (lane == 0) {
-        const int nc = P.ncell;
-        if (STRESS) {
+    if (MAG) {
 #pragma unroll
-            for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = make_double2(acc[j] * P.measure, 0.0);
-        }
-        if (MAG) {
-#pragma unroll
-            for (int j = 0; j < 3; ++j) fwd[(long long)(9 + j) * nc + cell] = make_double2(acc[9 + j] * P.measure, 0.0);
-        }
-        double dens = acc[12] * P.dthph;
-        double volex = P.volex * dens;
-        table[(long long)cell * tstride + T_DIFF] = sqrt(2.0 * P.dt * (P.Dt + volex));
-        if (tstride == TABLE_STRIDE_MAG) table[(long long)cell * tstride + T_DENS] = dens;
-        if (!FROM_DIST) cellcount[cell] = csum;
+        for (int j = 0; j < 3; ++j) fwd[(long long)(9 + j) * nc + cell] = make_double2(acc[9 + j] * P.measure, 0.0);
     }
+    double dens = acc[12] * P.dthph;
+    double volex = P.volex * dens;
+    table[(long long)cell * tstride + T_DIFF] = sqrt(2.0 * P.dt * (P.Dt + volex));
+    if (tstride == TABLE_STRIDE_MAG) table[(long long)cell * tstride + T_DENS] = dens;
+    if (!FROM_DIST) cellcount[cell] = csum;
 }
 
 // ------------------------------------------------------------------------
@@ -514,9 +515,19 @@ void launch_counts_to_dist(cudaStream_t s, const uint32_t *counts, const DevPara
 void launch_contract(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const double *dist,
                      const double *lut, int lut_n, const double *kern, const DevParams &P, double2 *fwd,
                      double *table, int tstride, uint32_t *cellcount) {
-    unsigned blocks = nblocks((unsigned long long)P.ncell * 32ull, 256);
-#define SS_CONTRACT(S, M, D) \
-    k_contract<S, M, D><<<blocks, 256, 0, s>>>(counts, dist, lut, lut_n, kern, P, fwd, table, tstride, cellcount)
+    unsigned blocks = nblocks((unsigned long long)P.ncell, 64);
+    const size_t smem = 12ull * P.nang * sizeof(double);
+    const bool use_smem = smem <= 48 * 1024;
+    const size_t sm = use_smem ? smem : 0;
+#define SS_CONTRACT(S, M, D)                                                                                     \
+    do {                                                                                                         \
+        if (use_smem)                                                                                            \
+            k_contract<S, M, D, true><<<blocks, 64, sm, s>>>(counts, dist, lut, lut_n, kern, P, fwd, table,     \
+                                                             tstride, cellcount);                                \
+        else                                                                                                     \
+            k_contract<S, M, D, false><<<blocks, 64, 0, s>>>(counts, dist, lut, lut_n, kern, P, fwd, table,     \
+                                                             tstride, cellcount);                                \
+    } while (0)
     bool fd = dist != nullptr;
     if (stress && mag) { if (fd) SS_CONTRACT(true, true, true); else SS_CONTRACT(true, true, false); }
     else if (stress) { if (fd) SS_CONTRACT(true, false, true); else SS_CONTRACT(true, false, false); }

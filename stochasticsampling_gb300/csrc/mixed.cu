@@ -89,57 +89,62 @@ __global__ void k_bin_m(unsigned long long n, MixedParams M, const double *__res
     key[i] = cell;
 }
 
-// angular contraction in FP32 (warp per cell); per-component sums of the
-// result accumulated in FP64 for the mean handling
+// angular contraction in FP32 (thread per cell, angle kernels in shared
+// memory); per-component sums of the result accumulated in FP64 for the
+// mean handling (one FP64 atomic per component per warp)
 template <bool STRESS, bool MAG>
-__global__ void __launch_bounds__(256) k_contract_m(const uint32_t *__restrict__ counts,
-                                                    const float *__restrict__ lut, int lut_n,
-                                                    const float *__restrict__ kern, MixedParams M,
-                                                    float2 *__restrict__ fwd, float *__restrict__ table, int tstride,
-                                                    double *__restrict__ sums) {
-    int cell = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-    int lane = threadIdx.x & 31;
-    if (cell >= M.ncell) return;
+__global__ void __launch_bounds__(64) k_contract_m(const uint32_t *__restrict__ counts,
+                                                   const float *__restrict__ lut, int lut_n,
+                                                   const float *__restrict__ kern, MixedParams M,
+                                                   float2 *__restrict__ fwd, float *__restrict__ table, int tstride,
+                                                   double *__restrict__ sums) {
+    extern __shared__ float skf[];
     const int na = M.nang;
+    for (int i = threadIdx.x; i < 12 * na; i += blockDim.x) skf[i] = kern[i];
+    __syncthreads();
+    int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = cell < M.ncell;
     float acc[13];
 #pragma unroll
     for (int j = 0; j < 13; ++j) acc[j] = 0.f;
-    for (int a = lane; a < na; a += 32) {
-        uint32_t c = counts[(long long)cell * na + a];
-        float f = ((int)c < lut_n) ? __ldg(lut + c) : (float)(((double)c / M.dist_den) * M.volume);
-        if (STRESS) {
+    if (live) {
+        const long long row = (long long)cell * na;
+        for (int a = 0; a < na; ++a) {
+            uint32_t c = counts[row + a];
+            float f = ((int)c < lut_n) ? __ldg(lut + c) : (float)(((double)c / M.dist_den) * M.volume);
+            if (STRESS) {
 #pragma unroll
-            for (int j = 0; j < 9; ++j) acc[j] = fmaf(__ldg(kern + j * na + a), f, acc[j]);
-        }
-        if (MAG) {
+                for (int j = 0; j < 9; ++j) acc[j] = fmaf(skf[j * na + a], f, acc[j]);
+            }
+            if (MAG) {
 #pragma unroll
-            for (int j = 9; j < 12; ++j) acc[j] = fmaf(__ldg(kern + j * na + a), f, acc[j]);
+                for (int j = 9; j < 12; ++j) acc[j] = fmaf(skf[j * na + a], f, acc[j]);
+            }
+            acc[12] += f;
         }
-        acc[12] += f;
     }
-#pragma unroll
-    for (int j = 0; j < 13; ++j)
-        if ((j < 9 && STRESS) || (j >= 9 && j < 12 && MAG) || j == 12) acc[j] = warp_sum_f(acc[j]);
-    if (lane == 0) {
-        const int nc = M.ncell;
+    const int nc = M.ncell;
+    if (live) {
         if (STRESS) {
 #pragma unroll
-            for (int j = 0; j < 9; ++j) {
-                float v = acc[j] * M.measure;
-                fwd[(long long)j * nc + cell] = make_float2(v, 0.f);
-                atomicAdd(sums + j, (double)v);
-            }
+            for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = make_float2(acc[j] * M.measure, 0.f);
         }
         if (MAG) {
 #pragma unroll
-            for (int j = 9; j < 12; ++j) {
-                float v = acc[j] * M.measure;
-                fwd[(long long)j * nc + cell] = make_float2(v, 0.f);
-                atomicAdd(sums + j, (double)v);
-            }
+            for (int j = 9; j < 12; ++j) fwd[(long long)j * nc + cell] = make_float2(acc[j] * M.measure, 0.f);
         }
         float dens = acc[12] * M.dthph;
         table[(long long)cell * tstride + T_DIFF] = sqrtf(M.two_dt * (M.Dt + M.volex * dens));
+    }
+    // FP64 component sums: warp partials in FP64, one atomic per warp
+#pragma unroll
+    for (int j = 0; j < 12; ++j) {
+        if ((j < 9 && STRESS) || (j >= 9 && MAG)) {
+            double v = live ? (double)(acc[j] * M.measure) : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if ((threadIdx.x & 31) == 0) atomicAdd(sums + j, v);
+        }
     }
 }
 
@@ -479,10 +484,11 @@ void launch_bin_m(cudaStream_t s, unsigned long long n, const MixedParams &M, do
 void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *lut, int lut_n,
                        const float *kern, const MixedParams &M, float2 *fwd, float *table, int tstride,
                        double *sums) {
-    unsigned blocks = nb((unsigned long long)M.ncell * 32ull, 256);
-    if (stress && mag) k_contract_m<true, true><<<blocks, 256, 0, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums);
-    else if (stress) k_contract_m<true, false><<<blocks, 256, 0, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums);
-    else k_contract_m<false, true><<<blocks, 256, 0, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums);
+    unsigned blocks = nb((unsigned long long)M.ncell, 64);
+    const size_t sm = 12ull * M.nang * sizeof(float);
+    if (stress && mag) k_contract_m<true, true><<<blocks, 64, sm, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums);
+    else if (stress) k_contract_m<true, false><<<blocks, 64, sm, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums);
+    else k_contract_m<false, true><<<blocks, 64, sm, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums);
 }
 void launch_center_m(cudaStream_t s, float2 *fwd, int c0, int c1, int ncell, const double *sums) {
     long long total = (long long)(c1 - c0) * ncell;

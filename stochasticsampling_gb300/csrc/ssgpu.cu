@@ -520,6 +520,10 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
         destroy_impl(c);
         return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "the trilinear gather is available in the FP64 mode only");
     }
+    if (c->mixed && nang > 1024) {  // the FP32 contraction keeps 12 angle kernels in 48 KB of shared memory
+        destroy_impl(c);
+        return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "the mixed-precision mode supports at most 1024 angle bins");
+    }
     if (c->mixed) c->sort = false;
     c->mag_step = (flags & SS_FLAG_ALWAYS_MAGNETIC) || params->magnetic_dipole_dipole != 0.0 ||
                   params->magnetic_drag != 0.0;
