@@ -187,7 +187,7 @@ def aggregate(ms_local, n_local, steps, world, dist):
     return float(n[0]) * steps / (ms / 1e3), ms
 
 
-def measure_mixed(args, stream, p0, rank, world, dist, barrier):
+def measure_mixed(args, stream, p0, rank, world, dist, barrier, mode=True):
     """The FP32 mixed-precision path on the same workload: throughput over K
     graph-replayed steps, and each field's error against the FP64 path after
     one step from identical state and noise."""
@@ -195,7 +195,7 @@ def measure_mixed(args, stream, p0, rank, world, dist, barrier):
 
     import stochasticsampling_gb300 as ss
     params = dict(PARAMS, number_of_particles=N, seed=1 + rank)
-    sim = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True, mixed=True, stream=stream.cuda_stream)
+    sim = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True, mixed=mode, stream=stream.cuda_stream)
     sim.init(p0)
     with torch.cuda.stream(stream):
         sim.run(args.warmup)
@@ -216,7 +216,7 @@ def measure_mixed(args, stream, p0, rank, world, dist, barrier):
     # errors against the FP64 path (itself within 1e-15 of the FP64 oracle)
     start = sim.get_particles()
     sim.close()
-    m = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True, mixed=True)
+    m = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True, mixed=mode)
     d = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True)
     m.init(start)
     d.init(start)
@@ -237,7 +237,8 @@ def measure_mixed(args, stream, p0, rank, world, dist, barrier):
     }
     m.close()
     d.close()
-    return {"value": value, "unit": UNIT, "ms_per_step": ms_max / args.steps, "dtype": "f32 + f64 positions",
+    dtype = "f32 + 64-bit fixed-point positions" if mode == "fixed64" else "f32 + f64 positions"
+    return {"value": value, "unit": UNIT, "ms_per_step": ms_max / args.steps, "dtype": dtype,
             "stage_ms": {k: v / max(1, nprof) for k, v in stage_ms.items()},
             "errors_vs_fp64_one_step": errors}
 
@@ -307,6 +308,7 @@ def run_gpu(args, rank, world, dist):
     e2e_value, _ = aggregate(1e3 * t_e2e, N, e2e_steps, world, dist)
     sim.close()
     mixed = None if args.no_mixed else measure_mixed(args, stream, p0, rank, world, dist, barrier)
+    mixed_fixed = None if args.no_mixed else measure_mixed(args, stream, p0, rank, world, dist, barrier, "fixed64")
 
     if rank != 0:
         return
@@ -361,6 +363,7 @@ def run_gpu(args, rank, world, dist):
         "clocks": clk,
         "cpu_baseline": cpu,
         "mixed": mixed,
+        "mixed_fixed64": mixed_fixed,
     }
     print(json.dumps(line), flush=True)
 

@@ -69,6 +69,9 @@ typedef struct {
 #define SS_FLAG_MIXED 16u          /* FP32 mixed precision: FP64 positions and k = 0 / mean handling, FP32
                                       angles, binning, contraction, FFTs, fields and Langevin arithmetic
                                       (no sort; the library seams ss_mean_* need the FP64 mode) */
+#define SS_FLAG_FIXED64 128u       /* as SS_FLAG_MIXED, with positions accumulated in 64-bit fixed point
+                                      (units of L / 2^64: periodic wrap by integer overflow, exact binning by
+                                      a 64-bit high multiply, no FP64 instruction in the step) */
 #define SS_FLAG_TRILINEAR 32u      /* gather every field by trilinear interpolation at the particle position
                                       (src/mesh/interpolate.rs:11-119) instead of the nearest cell that
                                       do_timestep uses (FP64 mode) */

@@ -50,7 +50,35 @@ __device__ __forceinline__ void bin_mixed(const MixedParams &M, double x, double
     bin = (unsigned long long)cell * (unsigned long long)M.nang + (unsigned long long)(ip * M.gtheta + it);
 }
 
-// Particle::new in FP64, then the angles rounded to FP32
+// ---- 64-bit fixed-point positions (SS_FLAG_FIXED64) ----------------------
+// A coordinate x in [0, L) is stored as X = x / L * 2^64 in a u64 (the same
+// 8 bytes as the double it replaces).  Adding a step is a 64-bit integer add;
+// leaving the box on either side wraps modulo 2^64, which is the periodic
+// boundary.  The cell is floor(X * n / 2^64), the high word of a 64-bit
+// product, exact.  The resolution, L / 2^64, is 2^11 times finer than FP64
+// near x = L.
+__device__ __forceinline__ unsigned long long to_fixed(double x, double L) {
+    double q = x / L;  // in [0, 1)
+    unsigned long long X = (unsigned long long)(q * 0x1p64 >= 0x1p64 ? 0x1p64 - 2048.0 : q * 0x1p64);
+    return X;
+}
+__device__ __forceinline__ double from_fixed(unsigned long long X, double unit) { return (double)X * unit; }
+// FP32 step -> signed fixed-point increment, in two 32-bit halves (no FP64)
+__device__ __forceinline__ unsigned long long step_fixed(float dx, float s32) {
+    float s = dx * s32;            // the step in units of 2^-32 L
+    s = fminf(fmaxf(s, -0x1p31f + 256.f), 0x1p31f - 256.f);  // |step| < L / 2
+    float hf = floorf(s);
+    int hi = (int)hf;
+    uint32_t lo = (uint32_t)((s - hf) * 0x1p32f);
+    return ((unsigned long long)(long long)hi << 32) + (unsigned long long)lo;
+}
+__device__ __forceinline__ int cell_fixed(unsigned long long X, int n) {
+    return (int)__umul64hi(X, (unsigned long long)n);
+}
+
+// Particle::new in FP64, then the angles rounded to FP32 (and the position
+// converted to fixed point when FIX)
+template <bool FIX>
 __global__ void k_ingest_m(const double *__restrict__ aos, unsigned long long n, DevParams P, double *__restrict__ x,
                            double *__restrict__ y, double *__restrict__ z, float *__restrict__ phi,
                            float *__restrict__ theta, uint32_t *__restrict__ id) {
@@ -64,19 +92,52 @@ __global__ void k_ingest_m(const double *__restrict__ aos, unsigned long long n,
     py = ref_modulo(py, P.by);
     pz = ref_modulo(pz, P.bz);
     ref_ang_pbc(ph, th);
-    x[i] = px; y[i] = py; z[i] = pz; phi[i] = (float)ph; theta[i] = (float)th;
+    if (FIX) {
+        reinterpret_cast<unsigned long long *>(x)[i] = to_fixed(px, P.bx);
+        reinterpret_cast<unsigned long long *>(y)[i] = to_fixed(py, P.by);
+        reinterpret_cast<unsigned long long *>(z)[i] = to_fixed(pz, P.bz);
+    } else {
+        x[i] = px; y[i] = py; z[i] = pz;
+    }
+    phi[i] = (float)ph; theta[i] = (float)th;
     id[i] = (uint32_t)i;
 }
 
-__global__ void k_egest_m(unsigned long long n, const double *__restrict__ x, const double *__restrict__ y,
-                          const double *__restrict__ z, const float *__restrict__ phi,
+template <bool FIX>
+__global__ void k_egest_m(unsigned long long n, MixedParams M, const double *__restrict__ x,
+                          const double *__restrict__ y, const double *__restrict__ z, const float *__restrict__ phi,
                           const float *__restrict__ theta, const uint32_t *__restrict__ id, double *__restrict__ aos) {
     unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
     if (i >= n) return;
     double *p = aos + 5 * (unsigned long long)id[i];
-    p[0] = x[i]; p[1] = y[i]; p[2] = z[i]; p[3] = (double)phi[i]; p[4] = (double)theta[i];
+    if (FIX) {
+        p[0] = from_fixed(reinterpret_cast<const unsigned long long *>(x)[i], M.unit[0]);
+        p[1] = from_fixed(reinterpret_cast<const unsigned long long *>(y)[i], M.unit[1]);
+        p[2] = from_fixed(reinterpret_cast<const unsigned long long *>(z)[i], M.unit[2]);
+    } else {
+        p[0] = x[i]; p[1] = y[i]; p[2] = z[i];
+    }
+    p[3] = (double)phi[i]; p[4] = (double)theta[i];
 }
 
+template <bool FIX>
+__device__ __forceinline__ void bin_any(const MixedParams &M, const double *x, const double *y, const double *z,
+                                        unsigned long long i, float phi, float theta, uint32_t &cell,
+                                        unsigned long long &bin) {
+    if (FIX) {
+        int ix = cell_fixed(reinterpret_cast<const unsigned long long *>(x)[i], M.gx);
+        int iy = cell_fixed(reinterpret_cast<const unsigned long long *>(y)[i], M.gy);
+        int iz = cell_fixed(reinterpret_cast<const unsigned long long *>(z)[i], M.gz);
+        int ip = bin_f(phi, M.igwf[3], M.gphi);
+        int it = bin_f(theta, M.igwf[4], M.gtheta);
+        cell = (uint32_t)((ix * M.gy + iy) * M.gz + iz);
+        bin = (unsigned long long)cell * (unsigned long long)M.nang + (unsigned long long)(ip * M.gtheta + it);
+    } else {
+        bin_mixed(M, x[i], y[i], z[i], phi, theta, cell, bin);
+    }
+}
+
+template <bool FIX>
 __global__ void k_bin_m(unsigned long long n, MixedParams M, const double *__restrict__ x,
                         const double *__restrict__ y, const double *__restrict__ z, const float *__restrict__ phi,
                         const float *__restrict__ theta, uint32_t *__restrict__ key, uint32_t *__restrict__ counts) {
@@ -84,7 +145,7 @@ __global__ void k_bin_m(unsigned long long n, MixedParams M, const double *__res
     if (i >= n) return;
     uint32_t cell;
     unsigned long long bin;
-    bin_mixed(M, x[i], y[i], z[i], phi[i], theta[i], cell, bin);
+    bin_any<FIX>(M, x, y, z, i, phi[i], theta[i], cell, bin);
     atomicAdd(counts + bin, 1u);
     key[i] = cell;
 }
@@ -320,9 +381,9 @@ struct TableFieldsF {
 
 // The Langevin chain of do_timestep in FP32, positions accumulated in FP64.
 template <bool Q2D>
-__device__ __forceinline__ void langevin_mixed(double &x, double &y, double &z, float &phi, float &theta,
-                                               const TableFieldsF &fld, const float xi[3], float ca, float sa,
-                                               float rot, const MixedParams &M) {
+__device__ __forceinline__ void langevin_mixed(float &phi, float &theta, float step[3], const TableFieldsF &fld,
+                                               const float xi[3], float ca, float sa, float rot,
+                                               const MixedParams &M) {
     float sp, cp, st, ct;
     sincosf(phi, &sp, &cp);
     if (Q2D) {
@@ -383,15 +444,14 @@ __device__ __forceinline__ void langevin_mixed(double &x, double &y, double &z, 
     dn[2] += n[2] * cm1 + (ax0 * n[1] - ax1 * n[0]) * sr;
     float v0 = n[0] + dn[0], v1 = n[1] + dn[1], v2 = n[2] + dn[2];
     float nphi = atan2f(v1, v0);
-    x = ref_modulo(x + (double)dp[0], M.bx);
-    y = ref_modulo(y + (double)dp[1], M.by);
+    step[0] = dp[0];
+    step[1] = dp[1];
+    step[2] = dp[2];
     if (Q2D) {
         phi = nphi < 0.0f ? nphi + 6.28318530717958647692f : nphi;
-        z = 0.0;
         theta = 1.57079632679489661923f;
     } else {
         float nth = 1.57079632679489661923f - atan2f(v2, sqrtf(v0 * v0 + v1 * v1));
-        z = ref_modulo(z + (double)dp[2], M.bz);
         float t = modulo_f(nth, 6.28318530717958647692f);
         if (t > 3.14159265358979323846f) {
             phi = modulo_f(nphi + 3.14159265358979323846f, 6.28318530717958647692f);
@@ -403,9 +463,26 @@ __device__ __forceinline__ void langevin_mixed(double &x, double &y, double &z, 
     }
 }
 
+// FP64 position advance: x + dx wrapped into [0, L) (modulo of
+// src/particle.rs:26-35 with 2L precomputed).  From an interior cell a step
+// shorter than one cell cannot leave the box, so only particles in the first
+// or last cell of the axis, or with long steps, pay for the wrap tests.
+__device__ __forceinline__ double advance64(double x, float dx, int cell, int n, float w, double L, double L2) {
+    double xn = x + (double)dx;
+    if (cell > 0 && cell < n - 1 && fabsf(dx) < w) return xn;
+    if (xn > -L && xn < L2) {
+        if (xn >= L) return xn - L;
+        if (xn < 0.0) return xn + L;
+        return xn;
+    }
+    double r = fmod(xn, L);
+    return r < 0.0 ? r + L : r;
+}
+
 // NOISE: 0 Philox, 1 host array.  CANON (quasi2d only): z == 0 and
-// theta == pi/2 already hold, so they are neither read nor written.
-template <bool Q2D, bool CANON, bool MAG, int NOISE>
+// theta == pi/2 already hold, so they are neither read nor written.  FIX:
+// positions in 64-bit fixed point.
+template <bool Q2D, bool CANON, bool MAG, int NOISE, bool FIX>
 __global__ void __launch_bounds__(256) k_update_m(MixedParams M, double *__restrict__ x, double *__restrict__ y,
                                                   double *__restrict__ z, float *__restrict__ phi,
                                                   float *__restrict__ theta, uint32_t *__restrict__ key,
@@ -417,12 +494,8 @@ __global__ void __launch_bounds__(256) k_update_m(MixedParams M, double *__restr
     if (i >= M.n) return;
     const int ts = MAG ? TABLE_STRIDE_MAG : TABLE_STRIDE;
     uint32_t cell = key[i];
-    double px = x[i], py = y[i], pz = 0.0;
     float pph = phi[i], pth = 1.57079632679489661923f;
-    if (!CANON) {
-        pz = z[i];
-        pth = theta[i];
-    }
+    if (!CANON) pth = theta[i];
     TableFieldsF F{table + (long long)cell * ts};
     float xi[3], ca, sa, rot;
     if (NOISE == 0) {
@@ -433,26 +506,47 @@ __global__ void __launch_bounds__(256) k_update_m(MixedParams M, double *__restr
         sincosf((float)r[3], &sa, &ca);
         rot = (float)r[4];
     }
+    float st[3];
     if (Q2D && !CANON) {
         // first step after init: theta may differ from pi/2
-        langevin_mixed<false>(px, py, pz, pph, pth, F, xi, ca, sa, rot, M);
-        pz = 0.0;
+        langevin_mixed<false>(pph, pth, st, F, xi, ca, sa, rot, M);
         pth = 1.57079632679489661923f;
     } else {
-        langevin_mixed<Q2D>(px, py, pz, pph, pth, F, xi, ca, sa, rot, M);
+        langevin_mixed<Q2D>(pph, pth, st, F, xi, ca, sa, rot, M);
     }
     uint32_t ncell;
     unsigned long long bin;
-    bin_mixed(M, px, py, pz, pph, pth, ncell, bin);
+    if (FIX) {
+        unsigned long long *X = reinterpret_cast<unsigned long long *>(x);
+        unsigned long long *Y = reinterpret_cast<unsigned long long *>(y);
+        unsigned long long *Z = reinterpret_cast<unsigned long long *>(z);
+        unsigned long long px = X[i] + step_fixed(st[0], M.s32[0]);
+        unsigned long long py = Y[i] + step_fixed(st[1], M.s32[1]);
+        unsigned long long pz = 0ull;
+        if (!Q2D) pz = Z[i] + step_fixed(st[2], M.s32[2]);
+        int ix = cell_fixed(px, M.gx), iy = cell_fixed(py, M.gy), iz = Q2D ? 0 : cell_fixed(pz, M.gz);
+        int ip = bin_f(pph, M.igwf[3], M.gphi), it = bin_f(pth, M.igwf[4], M.gtheta);
+        ncell = (uint32_t)((ix * M.gy + iy) * M.gz + iz);
+        bin = (unsigned long long)ncell * (unsigned long long)M.nang + (unsigned long long)(ip * M.gtheta + it);
+        X[i] = px;
+        Y[i] = py;
+        if (!CANON) Z[i] = pz;
+    } else {
+        const int gyz = M.gy * M.gz;
+        const int cx = (int)cell / gyz, cy = ((int)cell / M.gz) % M.gy, cz = (int)cell % M.gz;
+        double px = advance64(x[i], st[0], cx, M.gx, M.gwf[0], M.bx, M.bx2);
+        double py = advance64(y[i], st[1], cy, M.gy, M.gwf[1], M.by, M.by2);
+        double pz = 0.0;
+        if (!Q2D) pz = advance64(z[i], st[2], cz, M.gz, M.gwf[2], M.bz, M.bz2);
+        bin_mixed(M, px, py, pz, pph, pth, ncell, bin);
+        x[i] = px;
+        y[i] = py;
+        if (!CANON) z[i] = pz;
+    }
     atomicAdd(counts_next + bin, 1u);
     key[i] = ncell;
-    x[i] = px;
-    y[i] = py;
     phi[i] = pph;
-    if (!CANON) {
-        z[i] = pz;
-        theta[i] = pth;
-    }
+    if (!CANON) theta[i] = pth;
 }
 
 template <bool Q2D>
@@ -469,17 +563,24 @@ __global__ void k_noise_m(MixedParams M, unsigned long long t, double *__restric
 // ========================================================================
 static inline unsigned nb(unsigned long long n, unsigned bs) { return (unsigned)((n + bs - 1) / bs); }
 
-void launch_ingest_m(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P, double *const xs[3],
-                     float *const as[2], uint32_t *id) {
-    if (n) k_ingest_m<<<nb(n, 256), 256, 0, s>>>(aos, n, P, xs[0], xs[1], xs[2], as[0], as[1], id);
+void launch_ingest_m(cudaStream_t s, bool fixed, const double *aos, unsigned long long n, const DevParams &P,
+                     const MixedParams &M, double *const xs[3], float *const as[2], uint32_t *id) {
+    (void)M;
+    if (!n) return;
+    if (fixed) k_ingest_m<true><<<nb(n, 256), 256, 0, s>>>(aos, n, P, xs[0], xs[1], xs[2], as[0], as[1], id);
+    else k_ingest_m<false><<<nb(n, 256), 256, 0, s>>>(aos, n, P, xs[0], xs[1], xs[2], as[0], as[1], id);
 }
-void launch_egest_m(cudaStream_t s, unsigned long long n, double *const xs[3], float *const as[2], const uint32_t *id,
-                    double *aos) {
-    if (n) k_egest_m<<<nb(n, 256), 256, 0, s>>>(n, xs[0], xs[1], xs[2], as[0], as[1], id, aos);
+void launch_egest_m(cudaStream_t s, bool fixed, unsigned long long n, const MixedParams &M, double *const xs[3],
+                    float *const as[2], const uint32_t *id, double *aos) {
+    if (!n) return;
+    if (fixed) k_egest_m<true><<<nb(n, 256), 256, 0, s>>>(n, M, xs[0], xs[1], xs[2], as[0], as[1], id, aos);
+    else k_egest_m<false><<<nb(n, 256), 256, 0, s>>>(n, M, xs[0], xs[1], xs[2], as[0], as[1], id, aos);
 }
-void launch_bin_m(cudaStream_t s, unsigned long long n, const MixedParams &M, double *const xs[3], float *const as[2],
-                  uint32_t *key, uint32_t *counts) {
-    if (n) k_bin_m<<<nb(n, 256), 256, 0, s>>>(n, M, xs[0], xs[1], xs[2], as[0], as[1], key, counts);
+void launch_bin_m(cudaStream_t s, bool fixed, unsigned long long n, const MixedParams &M, double *const xs[3],
+                  float *const as[2], uint32_t *key, uint32_t *counts) {
+    if (!n) return;
+    if (fixed) k_bin_m<true><<<nb(n, 256), 256, 0, s>>>(n, M, xs[0], xs[1], xs[2], as[0], as[1], key, counts);
+    else k_bin_m<false><<<nb(n, 256), 256, 0, s>>>(n, M, xs[0], xs[1], xs[2], as[0], as[1], key, counts);
 }
 void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *lut, int lut_n,
                        const float *kern, const MixedParams &M, float2 *fwd, float *table, int tstride,
@@ -513,14 +614,20 @@ void launch_widen_m(cudaStream_t s, const float2 *src, long long count, int ncel
                     const double *sums, double2 *dst) {
     if (count > 0) k_widen_m<<<nb(count, 256), 256, 0, s>>>(src, count, ncell, comp0, m0, m1, sums, dst);
 }
-void launch_update_m(cudaStream_t s, bool q2d, bool canon, bool mag, bool host_noise, const MixedParams &M,
+void launch_update_m(cudaStream_t s, bool fixed, bool q2d, bool canon, bool mag, bool host_noise, const MixedParams &M,
                      double *const xs[3], float *const as[2], uint32_t *key, const uint32_t *id, const float *table,
                      const double *noise, const unsigned long long *d_step, uint32_t *counts_next) {
     if (!M.n) return;
     unsigned b = nb(M.n, 256);
-#define SS_UPDM(Q, C, G, N) \
-    k_update_m<Q, C, G, N><<<b, 256, 0, s>>>(M, xs[0], xs[1], xs[2], as[0], as[1], key, id, table, noise, d_step, \
-                                            counts_next)
+#define SS_UPDM(Q, C, G, N)                                                                                 \
+    do {                                                                                                    \
+        if (fixed)                                                                                          \
+            k_update_m<Q, C, G, N, true><<<b, 256, 0, s>>>(M, xs[0], xs[1], xs[2], as[0], as[1], key, id,   \
+                                                           table, noise, d_step, counts_next);              \
+        else                                                                                                \
+            k_update_m<Q, C, G, N, false><<<b, 256, 0, s>>>(M, xs[0], xs[1], xs[2], as[0], as[1], key, id,  \
+                                                            table, noise, d_step, counts_next);             \
+    } while (0)
 #define SS_UPDM_N(Q, C, G) \
     do { if (host_noise) SS_UPDM(Q, C, G, 1); else SS_UPDM(Q, C, G, 0); } while (0)
     if (q2d) {

@@ -12,8 +12,12 @@ struct MixedParams {
     int gx, gy, gz, gphi, gtheta;
     int ncell, nang;
     unsigned long long n;
-    double bx, by, bz;  // positions stay FP64
+    double bx, by, bz;  // positions stay FP64 (or 64-bit fixed point)
+    double bx2, by2, bz2;  // 2 L, for the exact wrap
     float igwf[5];      // 1 / grid width, FP32 binning
+    float gwf[3];       // grid width (FP32), to skip the wrap test in interior cells
+    float s32[3];       // 2^32 / L: FP32 step -> fixed-point increment
+    double unit[3];     // L / 2^64: fixed point -> FP64
     double dist_den, volume;
     float measure, dthph, two_dt, Dt, volex, dt;
     float drag, reorient, shape, mdd, sigma_rot;
@@ -21,12 +25,12 @@ struct MixedParams {
     uint32_t mask;
 };
 
-void launch_ingest_m(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P, double *const xs[3],
-                     float *const as[2], uint32_t *id);
-void launch_egest_m(cudaStream_t s, unsigned long long n, double *const xs[3], float *const as[2], const uint32_t *id,
-                    double *aos);
-void launch_bin_m(cudaStream_t s, unsigned long long n, const MixedParams &M, double *const xs[3], float *const as[2],
-                  uint32_t *key, uint32_t *counts);
+void launch_ingest_m(cudaStream_t s, bool fixed, const double *aos, unsigned long long n, const DevParams &P,
+                     const MixedParams &M, double *const xs[3], float *const as[2], uint32_t *id);
+void launch_egest_m(cudaStream_t s, bool fixed, unsigned long long n, const MixedParams &M, double *const xs[3],
+                    float *const as[2], const uint32_t *id, double *aos);
+void launch_bin_m(cudaStream_t s, bool fixed, unsigned long long n, const MixedParams &M, double *const xs[3],
+                  float *const as[2], uint32_t *key, uint32_t *counts);
 void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *lut, int lut_n,
                        const float *kern, const MixedParams &M, float2 *fwd, float *table, int tstride,
                        double *sums);
@@ -37,7 +41,7 @@ void launch_table_m(cudaStream_t s, bool flow, bool mag, const float2 *inv, cons
                     int tstride, const double *sums);
 void launch_widen_m(cudaStream_t s, const float2 *src, long long count, int ncell, int comp0, int m0, int m1,
                     const double *sums, double2 *dst);
-void launch_update_m(cudaStream_t s, bool q2d, bool canon, bool mag, bool host_noise, const MixedParams &M,
+void launch_update_m(cudaStream_t s, bool fixed, bool q2d, bool canon, bool mag, bool host_noise, const MixedParams &M,
                      double *const xs[3], float *const as[2], uint32_t *key, const uint32_t *id, const float *table,
                      const double *noise, const unsigned long long *d_step, uint32_t *counts_next);
 void launch_noise_m(cudaStream_t s, bool q2d, const MixedParams &M, unsigned long long t, double *out);

@@ -72,6 +72,7 @@ struct ss_ctx {
 
     // FP32 mixed-precision mode (SS_FLAG_MIXED)
     bool mixed = false;
+    bool fixed = false;  // positions in 64-bit fixed point (SS_FLAG_FIXED64)
     bool canon = false;  // quasi2d: z == 0 and theta == pi/2 hold for every particle
     MixedParams M{};
     float *pa[2][2] = {};  // phi, theta (FP32)
@@ -329,7 +330,7 @@ static int enqueue_step_m(ss_ctx *c, int pcur, int ccur, bool host_noise, uint64
     CKR(enqueue_solve_m(c, true, c->mag_step, c->counts[ccur], c->prm.hydro_screening, nl));
     mark(c, 5);
     launch_zero_u32(c->stream, c->counts[1 - ccur], c->P.nbins);
-    launch_update_m(c->stream, c->q2d, c->canon, c->mag_step, host_noise, c->M, c->px[pcur], c->pa[pcur],
+    launch_update_m(c->stream, c->fixed, c->q2d, c->canon, c->mag_step, host_noise, c->M, c->px[pcur], c->pa[pcur],
                     c->key[pcur], c->pid[pcur], c->table_f, c->noise_dev, c->d_step, c->counts[1 - ccur]);
     launch_step_inc(c->stream, c->d_step);
     *nl += 3;
@@ -515,7 +516,8 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     c->q2d = (flags & SS_FLAG_QUASI2D) != 0;
     c->sort = (flags & SS_FLAG_NO_SORT) == 0;
     c->use_graph = (flags & SS_FLAG_NO_GRAPH) == 0;
-    c->mixed = (flags & SS_FLAG_MIXED) != 0;
+    c->fixed = (flags & SS_FLAG_FIXED64) != 0;
+    c->mixed = (flags & (SS_FLAG_MIXED | SS_FLAG_FIXED64)) != 0;
     if (c->mixed && (flags & (SS_FLAG_TRILINEAR | SS_FLAG_TRILINEAR_ZFROMY))) {
         destroy_impl(c);
         return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "the trilinear gather is available in the FP64 mode only");
@@ -585,7 +587,14 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
         M.gx = P.gx; M.gy = P.gy; M.gz = P.gz; M.gphi = P.gphi; M.gtheta = P.gtheta;
         M.ncell = P.ncell; M.nang = P.nang; M.n = P.n;
         M.bx = P.bx; M.by = P.by; M.bz = P.bz;
+        M.bx2 = 2.0 * P.bx; M.by2 = 2.0 * P.by; M.bz2 = 2.0 * P.bz;
         for (int k = 0; k < 5; ++k) M.igwf[k] = (float)(1.0 / P.gw[k]);
+        const double L[3] = {P.bx, P.by, P.bz};
+        for (int k = 0; k < 3; ++k) {
+            M.gwf[k] = (float)P.gw[k];
+            M.s32[k] = (float)(0x1p32 / L[k]);
+            M.unit[k] = L[k] * 0x1p-64;
+        }
         M.dist_den = P.dist_den; M.volume = P.volume;
         M.measure = (float)P.measure; M.dthph = (float)P.dthph; M.two_dt = (float)(2.0 * P.dt);
         M.Dt = (float)P.Dt; M.volex = (float)P.volex; M.dt = (float)P.dt;
@@ -726,9 +735,9 @@ static int ingest_staging(ss_ctx *c, uint64_t n, bool canon) {
     c->pcur = 0;
     c->ccur = 0;
     if (c->mixed) {
-        launch_ingest_m(c->stream, c->staging, n, c->P, c->px[0], c->pa[0], c->pid[0]);
+        launch_ingest_m(c->stream, c->fixed, c->staging, n, c->P, c->M, c->px[0], c->pa[0], c->pid[0]);
         launch_zero_u32(c->stream, c->counts[0], c->P.nbins);
-        launch_bin_m(c->stream, n, c->M, c->px[0], c->pa[0], c->key[0], c->counts[0]);
+        launch_bin_m(c->stream, c->fixed, n, c->M, c->px[0], c->pa[0], c->key[0], c->counts[0]);
         // quasi2d: the canonical state (z = 0, theta = pi/2) lets the update skip z and theta
         c->canon = canon;
     } else {
@@ -849,7 +858,8 @@ int ss_get_particles(ss_ctx *c, double *out, uint64_t n) {
     if (n > c->P.n) return fail(c, SS_ERR_INVALID_ARGUMENT, "asked for %llu of %llu particles",
                                 (unsigned long long)n, (unsigned long long)c->P.n);
     CK(cudaSetDevice(c->device));
-    if (c->mixed) launch_egest_m(c->stream, c->P.n, c->px[c->pcur], c->pa[c->pcur], c->pid[c->pcur], c->staging);
+    if (c->mixed)
+        launch_egest_m(c->stream, c->fixed, c->P.n, c->M, c->px[c->pcur], c->pa[c->pcur], c->pid[c->pcur], c->staging);
     else launch_egest(c->stream, c->P.n, c->px[c->pcur], c->pid[c->pcur], c->staging);
     c->launches += 1;
     CKR(check_launch(c, "egest"));

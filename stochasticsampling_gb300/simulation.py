@@ -69,7 +69,9 @@ class Simulation:
             flags |= _lib.FLAG_NO_GRAPH
         if always_magnetic:
             flags |= _lib.FLAG_ALWAYS_MAGNETIC
-        if mixed:
+        if mixed == "fixed64":
+            flags |= _lib.FLAG_FIXED64
+        elif mixed:
             flags |= _lib.FLAG_MIXED
         flags |= {"nearest": 0, "trilinear": _lib.FLAG_TRILINEAR,
                   "trilinear_zfromy": _lib.FLAG_TRILINEAR_ZFROMY}[gather]

@@ -1,4 +1,5 @@
-"""The FP32 mixed-precision path (SS_FLAG_MIXED) against the FP64 oracle.
+"""The FP32 mixed-precision path against the FP64 oracle, with positions
+accumulated in FP64 (SS_FLAG_MIXED) or in 64-bit fixed point (SS_FLAG_FIXED64).
 
 The mixed path keeps positions and the spectral k = 0 / mean handling in FP64
 and does everything else in FP32, so it is not held to 1e-12; each field's
@@ -19,14 +20,18 @@ from test_gpu_parity import C0, EVEN2D, ODD3D, _c1_particles, _gpu, _noise, _pai
 pytestmark = pytest.mark.gpu
 
 
+MODES = pytest.mark.parametrize("mode", [True, "fixed64"], ids=["fp64_positions", "fixed64_positions"])
+
+
 def _wrapdiff(a, b, period):
     d = np.abs(a - b)
     return np.minimum(d, period - d)
 
 
+@MODES
 @pytest.mark.parametrize("cfg", [C0, EVEN2D, ODD3D], ids=["c0_2d", "even_2d_screened", "odd_3d_magnetic"])
-def test_mixed_one_step_errors(oracle, cfg):
-    g, o, s = _pair(oracle, cfg, mixed=True)
+def test_mixed_one_step_errors(oracle, cfg, mode):
+    g, o, s = _pair(oracle, cfg, mixed=mode)
     rng = np.random.default_rng(71)
     n = cfg[4]
     p = _particles(rng, n, cfg[2], cfg[5])
@@ -50,7 +55,8 @@ def test_mixed_one_step_errors(oracle, cfg):
     g.close()
 
 
-def test_mixed_fields_from_identical_histogram(oracle):
+@MODES
+def test_mixed_fields_from_identical_histogram(oracle, mode):
     """Fields of the mixed solve when its histogram equals the FP64 one:
     particles at bin centres, so FP32 binning cannot differ."""
     ss = _gpu()
@@ -60,7 +66,7 @@ def test_mixed_fields_from_identical_histogram(oracle):
     idx = np.column_stack([rng.integers(0, grid[k], n) for k in range(3)])
     ang = np.column_stack([rng.integers(0, grid[3], n), rng.integers(0, grid[4], n)])
     p = np.column_stack([(idx + 0.5) * gw, (ang[:, 0] + 0.5) * 2 * np.pi / grid[3], (ang[:, 1] + 0.5) * np.pi / grid[4]])
-    g, o, s = _pair(oracle, ODD3D, mixed=True)
+    g, o, s = _pair(oracle, ODD3D, mixed=mode)
     g.init(p)
     o.init(p)
     assert np.array_equal(g.get_counts().astype(np.float64), oracle.histogram(s, o.particles()))
@@ -77,13 +83,14 @@ def test_mixed_fields_from_identical_histogram(oracle):
     g.close()
 
 
-def test_mixed_runs_and_conserves(oracle):
+@MODES
+def test_mixed_runs_and_conserves(oracle, mode):
     ss = _gpu()
     name, grid, box, params, n, q2d = C0
     rng = np.random.default_rng(91)
     p = _particles(rng, n, box, q2d)
     g = ss.Simulation(grid=grid, box=box, params=dict(params, number_of_particles=n, seed=5), quasi2d=q2d,
-                      mixed=True)
+                      mixed=mode)
     g.init(p)
     g.run(20)
     g.do_timestep()
@@ -98,12 +105,13 @@ def test_mixed_runs_and_conserves(oracle):
     g.close()
 
 
-def test_mixed_c1_full_size(oracle):
+@MODES
+def test_mixed_c1_full_size(oracle, mode):
     """Production size 2-D in mixed precision: one step against the oracle fed
     the same noise, then ten more steps."""
     cfg = ("c1", (128, 128, 1, 32, 1), (40.0, 40.0, 1.0),
            dict(timestep=0.005, trans_diffusion=0.1, rot_diffusion=1.0, stress_active=-2.0), 10_000_000, True)
-    g, o, s = _pair(oracle, cfg, mixed=True)
+    g, o, s = _pair(oracle, cfg, mixed=mode)
     p = _c1_particles(np.random.default_rng(1), cfg[4])
     g.init(p)
     o.init(p)
@@ -118,3 +126,30 @@ def test_mixed_c1_full_size(oracle):
     g.do_timestep()
     assert int(g.get_counts().sum()) == cfg[4]
     g.close()
+
+
+def test_fixed64_wraps_and_bins_exactly(oracle):
+    """64-bit fixed point: crossing the box faces wraps by integer overflow and
+    the histogram of the stored positions is the FP64 binning of them."""
+    ss = _gpu()
+    grid, box = (16, 12, 1, 8, 1), (8.0, 6.0, 1.0)
+    n = 50_000
+    rng = np.random.default_rng(5)
+    p = _particles(rng, n, box, True)
+    p[:1000, 0] = box[0] - 1e-9  # next to the face: most cross it in one step
+    g = ss.Simulation(grid=grid, box=box, params=dict(number_of_particles=n, timestep=0.01, trans_diffusion=0.5,
+                                                      rot_diffusion=0.5, stress_active=-1.0), quasi2d=True,
+                      mixed="fixed64")
+    g.init(p)
+    g.run(5)
+    g.do_timestep()
+    q = g.get_particles()
+    assert np.all((q[:, 0] >= 0) & (q[:, 0] < box[0]) & (q[:, 1] >= 0) & (q[:, 1] < box[1]))
+    s = oracle.make_settings(grid, box, quasi2d=True)
+    # the counts of the last step were binned from the positions before it
+    g2 = ss.Simulation(grid=grid, box=box, params=dict(number_of_particles=n), quasi2d=True, mixed="fixed64")
+    g2.init(q)
+    hist = oracle.histogram(s, np.column_stack([q[:, :3], q[:, 3], np.full(n, np.pi / 2)]))
+    assert np.abs(g2.get_counts().astype(np.float64) - hist).sum() <= 1e-4 * n  # FP32 angle bins only
+    g.close()
+    g2.close()
