@@ -243,6 +243,86 @@ def measure_mixed(args, stream, p0, rank, world, dist, barrier, mode=True):
             "errors_vs_fp64_one_step": errors}
 
 
+def measure_ensemble(args, stream, rank, world, dist, barrier):
+    """The batched ensemble: 64 independent 2-D simulations (particle counts
+    log-uniform in [50k, 2M], grid edges {32, 64, 128}, 16 or 32 phi bins,
+    active stress uniform in [-3, 0], own Philox seed each) stepped by one
+    CUDA graph per step; against the same members as 64 separate mixed
+    contexts stepped one after the other."""
+    import torch
+
+    import stochasticsampling_gb300 as ss
+    from stochasticsampling_gb300.ensemble import parameter_scan, uniform_particles
+    members = parameter_scan(64, seed=1 + rank)
+    rows = uniform_particles(members, seed=2 + rank)
+    ntot = int(rows.shape[0])
+    ens = ss.Ensemble(members, stream=stream.cuda_stream)
+    ens.init(rows)
+    t0 = time.perf_counter()
+    cfg = ens.autotune()
+    tune_s = time.perf_counter() - t0
+    steps = args.steps
+    with torch.cuda.stream(stream):
+        ens.run(args.warmup)
+        torch.cuda.synchronize()
+        barrier()
+        _, _, l0 = ens.info()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ens.run(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        _, groups, l1 = ens.info()
+    ens.close()
+    value, ms_max = aggregate(ms, ntot, steps, world, dist)
+    # the same members as separate contexts, one after the other per step
+    sep_steps = max(3, min(steps, 20))
+    off = np.cumsum([0] + [m["params"]["number_of_particles"] for m in members])
+    sims = []
+    for i, m in enumerate(members):
+        s_ = ss.Simulation(grid=m["grid"], box=m["box"], params=m["params"], quasi2d=True, mixed=True,
+                           stream=stream.cuda_stream)
+        s_.init(rows[off[i]:off[i + 1]])
+        sims.append(s_)
+    with torch.cuda.stream(stream):
+        for s_ in sims:
+            s_.run(args.warmup)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(sep_steps):
+            for s_ in sims:
+                s_.run(1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sep_ms = e0.elapsed_time(e1) / sep_steps
+    for s_ in sims:
+        s_.close()
+    nbins = sum(m["grid"][0] * m["grid"][1] * m["grid"][3] for m in members)
+    ncell = sum(m["grid"][0] * m["grid"][1] for m in members)
+    # algorithmic bytes per step: particles x, y (f64), phi, cell key (f32/u32)
+    # read and written; both histograms (zero, count, contract read); 9 + 12
+    # complex FP32 spectra read and written by the FFTs and their neighbours;
+    # the table (16 floats per cell) written and read
+    step_bytes = ntot * 48 + nbins * 12 + ncell * 21 * 8 * 4 + ncell * 16 * 4 * 2
+    ns = [m["params"]["number_of_particles"] for m in members]
+    return {"value": value, "unit": UNIT, "ms_per_step": ms_max / steps, "steps": steps,
+            "dtype": "f32 + f64 positions",
+            "workload": "64 independent 2-D simulations, N log-uniform in [50k, 2M], grid edge in {32, 64, 128}, "
+                        "16 or 32 phi bins, box edge = 0.3125 x grid edge, active stress U[-3, 0], Dt 0.1, Dr 1.0, "
+                        "dt 0.005, own Philox seed per member",
+            "particles": ntot, "particles_min_max": [min(ns), max(ns)], "grid_shapes": groups,
+            "autotune": {"threads": cfg[0], "blocks_per_sm": cfg[1], "particles_per_unit": cfg[2],
+                         "seconds": tune_s},
+            "gpu_launches_per_step": (l1 - l0) / steps,
+            "step_algorithmic_bytes": step_bytes,
+            "step_achieved_gbs": step_bytes / (ms_max / steps / 1e3) / 1e9,
+            "separate_contexts": {"ms_per_step": sep_ms, "value": ntot / (sep_ms / 1e3),
+                                  "note": "the same 64 members as SS_FLAG_MIXED contexts, each graph-stepped, "
+                                          "one after the other"}}
+
+
 def run_gpu(args, rank, world, dist):
     import torch
 
@@ -309,6 +389,7 @@ def run_gpu(args, rank, world, dist):
     sim.close()
     mixed = None if args.no_mixed else measure_mixed(args, stream, p0, rank, world, dist, barrier)
     mixed_fixed = None if args.no_mixed else measure_mixed(args, stream, p0, rank, world, dist, barrier, "fixed64")
+    ensemble = None if args.no_ensemble else measure_ensemble(args, stream, rank, world, dist, barrier)
 
     if rank != 0:
         return
@@ -364,6 +445,7 @@ def run_gpu(args, rank, world, dist):
         "cpu_baseline": cpu,
         "mixed": mixed,
         "mixed_fixed64": mixed_fixed,
+        "ensemble": ensemble,
     }
     print(json.dumps(line), flush=True)
 
@@ -376,6 +458,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32 mixed-precision measurement")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--particles", type=int, default=None,
                     help="override N (profiling a smaller case of the same workload)")
     args = ap.parse_args()

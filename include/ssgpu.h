@@ -221,6 +221,48 @@ int ss_launch_count(ss_ctx *ctx, uint64_t *out);
 int ss_sample_distribution_noalloc(const ss_grid *grid, const ss_box *box, const double *particles, uint64_t n,
                                    double *dist, void *stream);
 
+/* ---- batched ensembles ---------------------------------------------------
+ * Many independent quasi-2-D simulations stepped together on one GPU, the
+ * batched form of running the reference binary once per parameter set
+ * (src/bin/simulation/main.rs) -- a parameter scan or an ensemble average.
+ * Member m has its own grid, box and parameters (particle count, seed,
+ * activity, diffusion, ...).  Every member is stepped with the arithmetic of
+ * a single context created with SS_FLAG_QUASI2D | SS_FLAG_MIXED and the same
+ * grid, box and parameters, with the same Philox stream, so member m follows
+ * that context's trajectory up to the round-off of the differently batched
+ * FP32 FFTs.  Members of one grid shape share one batched cuFFT plan; each
+ * step is one CUDA graph of 6 kernels plus 2 FFT calls per grid shape.
+ * Dipolar coupling is not supported (magnetic_dipole_dipole and
+ * magnetic_drag must be 0).  Errors are reported by ss_last_error(NULL, ...). */
+typedef struct ss_ens ss_ens;
+
+/* count members; grids[m].z == grids[m].theta == 1; flags: SS_FLAG_QUASI2D,
+ * optionally | SS_FLAG_MIXED (implied).  stream as in ss_create. */
+int ss_ensemble_create(const ss_grid *grids, const ss_box *boxes, const ss_params *params, uint32_t count,
+                       uint32_t flags, void *stream, ss_ens **out);
+int ss_ensemble_destroy(ss_ens *ens);
+/* Simulation::init for every member: particles holds the members' rows one
+ * after the other ([sum n_m][5] doubles, host memory); every row must have
+ * z = 0 and theta = pi/2.  Resets every member's timestep to 0. */
+int ss_ensemble_init(ss_ens *ens, const double *particles, uint64_t total);
+/* times the particle update's launch shapes on the ensemble's own data and
+ * keeps the fastest; config (optional, 3 entries) receives threads per
+ * block, blocks per SM and particles per work unit.  ss_ensemble_run calls
+ * it before its first step when it has not run. */
+int ss_ensemble_autotune(ss_ens *ens, uint32_t *config);
+/* steps do_timestep calls of every member (asynchronous) */
+int ss_ensemble_run(ss_ens *ens, uint64_t steps);
+int ss_ensemble_synchronize(ss_ens *ens);
+/* member's particles, [n_m][5] doubles (x, y, 0, phi, pi/2), host memory */
+int ss_ensemble_get_particles(ss_ens *ens, uint32_t member, double *out);
+/* member's histogram the last step solved from (after init: the initial
+ * one), as ss_get_counts */
+int ss_ensemble_get_counts(ss_ens *ens, uint32_t member, uint32_t *out);
+/* member's flow field of the last step, [3][x][y] doubles, as ss_get_flow_field */
+int ss_ensemble_get_flow_field(ss_ens *ens, uint32_t member, double *out);
+/* total particles, grid-shape groups and kernel launches so far (each optional) */
+int ss_ensemble_info(ss_ens *ens, uint64_t *particles, uint32_t *groups, uint64_t *launches);
+
 /* copy the last error message of ctx (or the last context-free error when
  * ctx is NULL) into buf, NUL terminated */
 int ss_last_error(ss_ctx *ctx, char *buf, size_t len);

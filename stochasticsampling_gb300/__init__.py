@@ -10,8 +10,9 @@ from . import _lib
 from ._lib import SsError
 from .settings import read_parameter_file, parse_settings, Settings, SettingsError
 from .simulation import Simulation, langevin
+from .ensemble import Ensemble
 
-__all__ = ["Simulation", "langevin", "read_parameter_file", "parse_settings", "Settings", "SettingsError",
+__all__ = ["Simulation", "Ensemble", "langevin", "read_parameter_file", "parse_settings", "Settings", "SettingsError",
            "SsError", "load_library"]
 
 

@@ -15,7 +15,9 @@ EXPORTS = [
     "ss_get_particles", "ss_get_distribution", "ss_get_counts", "ss_get_flow_field", "ss_get_magnetic_field",
     "ss_get_flow_complex", "ss_get_magnetic_complex", "ss_get_timestep", "ss_mean_flow_field",
     "ss_mean_magnetic_field", "ss_langevin", "ss_profile_enable", "ss_profile_read", "ss_launch_count",
-    "ss_sample_distribution_noalloc", "ss_last_error", "ss_version",
+    "ss_sample_distribution_noalloc", "ss_ensemble_create", "ss_ensemble_destroy", "ss_ensemble_init",
+    "ss_ensemble_autotune", "ss_ensemble_run", "ss_ensemble_synchronize", "ss_ensemble_get_particles",
+    "ss_ensemble_get_counts", "ss_ensemble_get_flow_field", "ss_ensemble_info", "ss_last_error", "ss_version",
 ]
 
 SS_OK = 0
@@ -121,6 +123,17 @@ def load(build_if_missing=True):
         "ss_profile_read": [vp, dp, u64p],
         "ss_launch_count": [vp, u64p],
         "ss_sample_distribution_noalloc": [ctypes.POINTER(Grid), ctypes.POINTER(Box), vp, u64, vp, vp],
+        "ss_ensemble_create": [ctypes.POINTER(Grid), ctypes.POINTER(Box), ctypes.POINTER(Params), u32, u32, vp,
+                               ctypes.POINTER(vp)],
+        "ss_ensemble_destroy": [vp],
+        "ss_ensemble_init": [vp, dp, u64],
+        "ss_ensemble_autotune": [vp, ctypes.POINTER(ctypes.c_uint32)],
+        "ss_ensemble_run": [vp, u64],
+        "ss_ensemble_synchronize": [vp],
+        "ss_ensemble_get_particles": [vp, u32, dp],
+        "ss_ensemble_get_counts": [vp, u32, ctypes.POINTER(ctypes.c_uint32)],
+        "ss_ensemble_get_flow_field": [vp, u32, dp],
+        "ss_ensemble_info": [vp, u64p, ctypes.POINTER(ctypes.c_uint32), u64p],
         "ss_last_error": [vp, ctypes.c_char_p, ctypes.c_size_t],
     }
     for name, args in sig.items():

@@ -12,69 +12,9 @@
 // Layout: particles x, y, z f64 SoA + phi, theta f32 SoA (+ key, id as in the
 // FP64 path); spectra float2; table rows of 16 (32 with dipolar terms) floats.
 #include "mixed.cuh"
+#include "mixed_device.cuh"
 
 namespace ss {
-
-__device__ __forceinline__ float warp_sum_f(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-__device__ __forceinline__ float kval_f(int i, int n, float step) {
-    int b = (n % 2 == 0) ? n / 2 : n / 2 + 1;
-    return (float)(i < b ? i : i - n) * step;
-}
-
-// floor(v / w) in FP32 with the `== n -> n - 1` clamp of coord_to_grid
-__device__ __forceinline__ int bin_f(float v, float iw, int n) {
-    float f = floorf(v * iw);
-    int i = (int)f;
-    i = i < 0 ? 0 : i;
-    return i >= n ? n - 1 : i;
-}
-
-__device__ __forceinline__ float modulo_f(float f, float m) {
-    float r = fmodf(f, m);
-    return r < 0.0f ? r + fabsf(m) : r;
-}
-
-__device__ __forceinline__ void bin_mixed(const MixedParams &M, double x, double y, double z, float phi, float theta,
-                                          uint32_t &cell, unsigned long long &bin) {
-    int ix = bin_f((float)x, M.igwf[0], M.gx);
-    int iy = bin_f((float)y, M.igwf[1], M.gy);
-    int iz = bin_f((float)z, M.igwf[2], M.gz);
-    int ip = bin_f(phi, M.igwf[3], M.gphi);
-    int it = bin_f(theta, M.igwf[4], M.gtheta);
-    cell = (uint32_t)((ix * M.gy + iy) * M.gz + iz);
-    bin = (unsigned long long)cell * (unsigned long long)M.nang + (unsigned long long)(ip * M.gtheta + it);
-}
-
-// ---- 64-bit fixed-point positions (SS_FLAG_FIXED64) ----------------------
-// A coordinate x in [0, L) is stored as X = x / L * 2^64 in a u64 (the same
-// 8 bytes as the double it replaces).  Adding a step is a 64-bit integer add;
-// leaving the box on either side wraps modulo 2^64, which is the periodic
-// boundary.  The cell is floor(X * n / 2^64), the high word of a 64-bit
-// product, exact.  The resolution, L / 2^64, is 2^11 times finer than FP64
-// near x = L.
-__device__ __forceinline__ unsigned long long to_fixed(double x, double L) {
-    double q = x / L;  // in [0, 1)
-    unsigned long long X = (unsigned long long)(q * 0x1p64 >= 0x1p64 ? 0x1p64 - 2048.0 : q * 0x1p64);
-    return X;
-}
-__device__ __forceinline__ double from_fixed(unsigned long long X, double unit) { return (double)X * unit; }
-// FP32 step -> signed fixed-point increment, in two 32-bit halves (no FP64)
-__device__ __forceinline__ unsigned long long step_fixed(float dx, float s32) {
-    float s = dx * s32;            // the step in units of 2^-32 L
-    s = fminf(fmaxf(s, -0x1p31f + 256.f), 0x1p31f - 256.f);  // |step| < L / 2
-    float hf = floorf(s);
-    int hi = (int)hf;
-    uint32_t lo = (uint32_t)((s - hf) * 0x1p32f);
-    return ((unsigned long long)(long long)hi << 32) + (unsigned long long)lo;
-}
-__device__ __forceinline__ int cell_fixed(unsigned long long X, int n) {
-    return (int)__umul64hi(X, (unsigned long long)n);
-}
 
 // Particle::new in FP64, then the angles rounded to FP32 (and the position
 // converted to fixed point when FIX)
@@ -329,154 +269,6 @@ __global__ void k_widen_m(const float2 *__restrict__ src, long long count, int n
     double re = (double)v.x;
     if (comp >= m0 && comp < m1) re += sums[comp - 12] / (double)ncell;
     dst[i] = make_double2(re, (double)v.y);
-}
-
-// ---- the particle update ----------------------------------------------
-__device__ __forceinline__ float u24(uint32_t r) { return (float)(r >> 8) * 0x1p-24f; }
-
-template <bool Q2D>
-__device__ __forceinline__ void philox_noise_f(unsigned long long seed, uint32_t id, unsigned long long t,
-                                               float sigma, float xi[3], float &ca, float &sa, float &rot) {
-    uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
-    uint32_t tl = (uint32_t)t, th = (uint32_t)(t >> 32);
-    uint4 r0 = philox4x32_10(make_uint4(id, tl, th, 0u), key);
-    float rad = sqrtf(-2.0f * logf(1.0f - u24(r0.x)));
-    float s, c;
-    sincospif(2.0f * u24(r0.y), &s, &c);
-    xi[0] = rad * c;
-    xi[1] = rad * s;
-    sincospif(2.0f * u24(r0.z), &sa, &ca);
-    rot = sigma * sqrtf(-2.0f * logf(1.0f - u24(r0.w)));
-    if (Q2D) {
-        xi[2] = 0.f;
-    } else {
-        uint4 r1 = philox4x32_10(make_uint4(id, tl, th, 1u), key);
-        xi[2] = sqrtf(-2.0f * logf(1.0f - u24(r1.x))) * cospif(2.0f * u24(r1.y));
-    }
-}
-
-struct TableFieldsF {
-    const float *r;
-    __device__ float flow(int k) const { return r[T_U + k]; }
-    __device__ float diff() const { return r[T_DIFF]; }
-    __device__ float b(int k) const { return r[T_B + k]; }
-    __device__ void vort_dot(const float n[3], float f[3]) const {
-        float w01 = r[T_W01], w02 = r[T_W02], w12 = r[T_W12];
-        f[0] = w01 * n[1] + w02 * n[2];
-        f[1] = -w01 * n[0] + w12 * n[2];
-        f[2] = -w02 * n[0] - w12 * n[1];
-    }
-    __device__ void strain_dot(const float n[3], float f[3]) const {
-        float e00 = r[T_E00], e01 = r[T_E01], e02 = r[T_E02], e11 = r[T_E11], e12 = r[T_E12], e22 = r[T_E22];
-        f[0] = e00 * n[0] + e01 * n[1] + e02 * n[2];
-        f[1] = e01 * n[0] + e11 * n[1] + e12 * n[2];
-        f[2] = e02 * n[0] + e12 * n[1] + e22 * n[2];
-    }
-    __device__ void gradb_dot(const float n[3], float f[3]) const {
-        const float *g = r + T_GB;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) f[a] = g[3 * a] * n[0] + g[3 * a + 1] * n[1] + g[3 * a + 2] * n[2];
-    }
-};
-
-// The Langevin chain of do_timestep in FP32, positions accumulated in FP64.
-template <bool Q2D>
-__device__ __forceinline__ void langevin_mixed(float &phi, float &theta, float step[3], const TableFieldsF &fld,
-                                               const float xi[3], float ca, float sa, float rot,
-                                               const MixedParams &M) {
-    float sp, cp, st, ct;
-    sincosf(phi, &sp, &cp);
-    if (Q2D) {
-        st = 1.0f;
-        ct = 0.0f;
-    } else {
-        sincosf(theta, &st, &ct);
-    }
-    float n[3] = {st * cp, st * sp, ct};
-    float dp[3] = {n[0], n[1], n[2]}, dn[3] = {0.f, 0.f, 0.f};
-    const uint32_t mask = M.mask;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) dp[k] += fld.flow(k);
-    if (mask & M_MDD_FORCE) {
-        float f[3];
-        fld.gradb_dot(n, f);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) dp[k] += f[k] * M.drag;
-    }
-    if (mask & M_EXTERNAL_FIELD) {
-        float d = n[1] * M.reorient;
-        dn[0] -= n[0] * d;
-        dn[1] += M.reorient - n[1] * d;
-        dn[2] -= n[2] * d;
-    }
-    if (mask & M_MDD_ROTATION) {
-        float b[3] = {fld.b(0), fld.b(1), fld.b(2)};
-        float d = n[0] * b[0] + n[1] * b[1] + n[2] * b[2];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) dn[k] += b[k] - n[k] * d;
-    }
-    {
-        float f[3];
-        fld.vort_dot(n, f);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) dn[k] -= f[k];
-    }
-    if (mask & M_JEFFREY_STRAIN) {
-        float f[3];
-        fld.strain_dot(n, f);
-        float fn = M.shape * (f[0] * n[0] + f[1] * n[1] + f[2] * n[2]);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) dn[k] += M.shape * f[k] - n[k] * fn;
-    }
-    const float diff = fld.diff();
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        dp[k] = dp[k] * M.dt + xi[k] * diff;
-        dn[k] = dn[k] * M.dt;
-    }
-    // rotational diffusion about k perpendicular to n by rot (Rodrigues)
-    float ax0 = cp * ct * sa - ca * sp, ax1 = ca * cp + ct * sa * sp, ax2 = -sa * st;
-    float sr, cr;
-    sincosf(rot, &sr, &cr);
-    float cm1 = cr - 1.0f;
-    dn[0] += n[0] * cm1 + (ax1 * n[2] - ax2 * n[1]) * sr;
-    dn[1] += n[1] * cm1 + (ax2 * n[0] - ax0 * n[2]) * sr;
-    dn[2] += n[2] * cm1 + (ax0 * n[1] - ax1 * n[0]) * sr;
-    float v0 = n[0] + dn[0], v1 = n[1] + dn[1], v2 = n[2] + dn[2];
-    float nphi = atan2f(v1, v0);
-    step[0] = dp[0];
-    step[1] = dp[1];
-    step[2] = dp[2];
-    if (Q2D) {
-        phi = nphi < 0.0f ? nphi + 6.28318530717958647692f : nphi;
-        theta = 1.57079632679489661923f;
-    } else {
-        float nth = 1.57079632679489661923f - atan2f(v2, sqrtf(v0 * v0 + v1 * v1));
-        float t = modulo_f(nth, 6.28318530717958647692f);
-        if (t > 3.14159265358979323846f) {
-            phi = modulo_f(nphi + 3.14159265358979323846f, 6.28318530717958647692f);
-            theta = 6.28318530717958647692f - t;
-        } else {
-            phi = modulo_f(nphi, 6.28318530717958647692f);
-            theta = t;
-        }
-    }
-}
-
-// FP64 position advance: x + dx wrapped into [0, L) (modulo of
-// src/particle.rs:26-35 with 2L precomputed).  From an interior cell a step
-// shorter than one cell cannot leave the box, so only particles in the first
-// or last cell of the axis, or with long steps, pay for the wrap tests.
-__device__ __forceinline__ double advance64(double x, float dx, int cell, int n, float w, double L, double L2) {
-    double xn = x + (double)dx;
-    if (cell > 0 && cell < n - 1 && fabsf(dx) < w) return xn;
-    if (xn > -L && xn < L2) {
-        if (xn >= L) return xn - L;
-        if (xn < 0.0) return xn + L;
-        return xn;
-    }
-    double r = fmod(xn, L);
-    return r < 0.0 ? r + L : r;
 }
 
 // NOISE: 0 Philox, 1 host array.  CANON (quasi2d only): z == 0 and

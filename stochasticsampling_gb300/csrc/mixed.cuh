@@ -4,6 +4,9 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
+#include "../../include/ssgpu.h"
 #include "common.cuh"
 
 namespace ss {
@@ -45,5 +48,11 @@ void launch_update_m(cudaStream_t s, bool fixed, bool q2d, bool canon, bool mag,
                      double *const xs[3], float *const as[2], uint32_t *key, const uint32_t *id, const float *table,
                      const double *noise, const unsigned long long *d_step, uint32_t *counts_next);
 void launch_noise_m(cudaStream_t s, bool q2d, const MixedParams &M, unsigned long long t, double *out);
+
+// host side, defined in ssgpu.cu and shared with the ensemble: the FP64 angle
+// kernels [component][phi][theta], 9 stress components then the 3
+// orientation components, and the context-free error of ss_last_error
+void build_angle_kernels(const ss_grid &grid, const ss_params &prm, std::vector<double> &K);
+void record_error(const char *msg);
 
 }  // namespace ss

@@ -145,8 +145,8 @@ static double host_modulo(double f, double m) {
     return r < 0.0 ? r + std::fabs(m) : r;
 }
 
-static void build_angle_kernels(const ss_ctx *c, std::vector<double> &K) {
-    const uint64_t gp = c->grid.phi, gt = c->grid.theta, na = gp * gt;
+void ss::build_angle_kernels(const ss_grid &grid, const ss_params &prm, std::vector<double> &K) {
+    const uint64_t gp = grid.phi, gt = grid.theta, na = gp * gt;
     const double gwp = kTwoPi / (double)gp, gwt = kPi / (double)gt;
     const double hp = gwp / 2., ht = gwt / 2.;
     K.assign(12 * na, 0.0);
@@ -170,7 +170,7 @@ static void build_angle_kernels(const ss_ctx *c, std::vector<double> &K) {
                 sm[k] = sm[k] * 0.5;
                 sr[k] = sr[k] * 0.5;
                 K[k * na + i * gt + j] =
-                    c->prm.stress_active * sa[k] + c->prm.stress_magnetic * sm[k] + c->prm.shape * sr[k];
+                    prm.stress_active * sa[k] + prm.stress_magnetic * sm[k] + prm.shape * sr[k];
             }
             // orientation kernel: Orientation::new (ang_pbc) then to_vector
             double th = host_modulo(theta, kTwoPi), ph;
@@ -671,7 +671,7 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     CKC(cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream));
 
     std::vector<double> K;
-    build_angle_kernels(c, K);
+    build_angle_kernels(c->grid, c->prm, K);
     std::vector<double> lut(kLutN);
     for (int i = 0; i < kLutN; ++i) lut[i] = ((double)i / P.dist_den) * P.volume;
     CKC(cudaMemcpyAsync(c->kern, K.data(), K.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));

@@ -32,22 +32,29 @@ def _f64(a, shape=None):
     return a
 
 
+def geometry_from_settings(settings):
+    """(grid, box, params) of a Settings object, the ss_grid / ss_box /
+    ss_params triple of the C ABI."""
+    sim, par = settings.simulation, settings.parameters
+    grid = (sim.grid_size.x, sim.grid_size.y, sim.grid_size.z, sim.grid_size.phi, sim.grid_size.theta)
+    box = (sim.box_size.x, sim.box_size.y, sim.box_size.z)
+    params = dict(timestep=sim.timestep, trans_diffusion=par.diffusion.translational,
+                  rot_diffusion=par.diffusion.rotational, stress_active=par.stress.active,
+                  stress_magnetic=par.stress.magnetic, shape=par.shape, magnetic_drag=par.magnetic_drag,
+                  hydro_screening=par.hydro_screening, volume_exclusion=par.volume_exclusion,
+                  magnetic_reorientation=par.magnetic_reorientation,
+                  magnetic_dipole_dipole=par.magnetic_dipole.magnetic_dipole_dipole,
+                  number_of_particles=sim.number_of_particles, seed=sim.seed)
+    return grid, box, params
+
+
 class Simulation:
     """One simulation on the current CUDA device."""
 
     def __init__(self, settings=None, *, grid=None, box=None, params=None, quasi2d=False, sort=True, graph=True,
                  always_magnetic=False, mixed=False, gather="nearest", stream=None):
         if settings is not None:
-            sim, par = settings.simulation, settings.parameters
-            grid = (sim.grid_size.x, sim.grid_size.y, sim.grid_size.z, sim.grid_size.phi, sim.grid_size.theta)
-            box = (sim.box_size.x, sim.box_size.y, sim.box_size.z)
-            params = dict(timestep=sim.timestep, trans_diffusion=par.diffusion.translational,
-                          rot_diffusion=par.diffusion.rotational, stress_active=par.stress.active,
-                          stress_magnetic=par.stress.magnetic, shape=par.shape, magnetic_drag=par.magnetic_drag,
-                          hydro_screening=par.hydro_screening, volume_exclusion=par.volume_exclusion,
-                          magnetic_reorientation=par.magnetic_reorientation,
-                          magnetic_dipole_dipole=par.magnetic_dipole.magnetic_dipole_dipole,
-                          number_of_particles=sim.number_of_particles, seed=sim.seed)
+            grid, box, params = geometry_from_settings(settings)
         if grid is None or box is None or params is None:
             raise ValueError("give settings, or grid, box and params")
         self.lib = _lib.load()
