@@ -130,12 +130,20 @@ class Ensemble:
     def synchronize(self):
         check(self.lib.ss_ensemble_synchronize(self._h))
 
+    def _member(self, member):
+        member = int(member)
+        if not 0 <= member < len(self.members):
+            raise IndexError(f"member {member} of an ensemble of {len(self.members)}")
+        return member
+
     def get_particles(self, member):
+        member = self._member(member)
         out = np.empty((self.n[member], 5))
         check(self.lib.ss_ensemble_get_particles(self._h, int(member), out.ctypes.data_as(_dp)))
         return out
 
     def get_counts(self, member):
+        member = self._member(member)
         g = self.members[member][0]
         out = np.empty(g, dtype=np.uint32)
         check(self.lib.ss_ensemble_get_counts(self._h, int(member),
@@ -143,6 +151,7 @@ class Ensemble:
         return out
 
     def get_flow_field(self, member):
+        member = self._member(member)
         gx, gy, gz = self.members[member][0][:3]
         out = np.empty((3, gx, gy, gz))
         check(self.lib.ss_ensemble_get_flow_field(self._h, int(member), out.ctypes.data_as(_dp)))

@@ -159,8 +159,12 @@ def test_ensemble_errors():
         ens.run(1)  # not initialised
     ens.init(rows)
     ens.run(1)
-    with pytest.raises(ss.SsError):
+    with pytest.raises(IndexError):
         ens.get_particles(len(members))
+    from stochasticsampling_gb300 import _lib
+    out = np.empty((10, 5))
+    rc = ens.lib.ss_ensemble_get_particles(ens._h, len(members), out.ctypes.data_as(_lib.ctypes.POINTER(_lib.ctypes.c_double)))
+    assert rc == _lib.SS_ERR_INVALID_ARGUMENT
     ens.close()
 
 
