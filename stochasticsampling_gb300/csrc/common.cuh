@@ -154,11 +154,29 @@ __device__ __forceinline__ double u12(uint32_t hi, uint32_t lo) {
     return __hiloint2double((int)(0x3FF00000u | (hi >> 12)), (int)((hi << 20) | (lo >> 12)));
 }
 
+// -2 ln(1 - U) in FP32 with full relative precision over all of (0, 1],
+// from x = 1 + U in [1, 2) (52 random bits): -U = 1 - x and 1 - U = 2 - x
+// are exact in FP64; log1p takes -U below U = 1/2 (the radius near 0), log
+// takes 1 - U above it (the tail, down to 1 - U = 2^-52).
+__device__ __forceinline__ float neg2log1m(double x) {
+    const float l = (x < 1.5) ? log1pf((float)(1.0 - x)) : logf((float)(2.0 - x));
+    return -2.0f * l;
+}
+
 // Noise of particle `id` at step `t`: the RandomVector of
 // src/bin/simulation/mod.rs:272-286 (x, y, z ~ N(0,1), axis_angle = 2 pi U,
 // rotate_angle = sigma sqrt(-2 ln(1-U))), drawn from Philox with counter
-// (id, t_lo, t_hi, draw) and key = seed.  Normals by Box-Muller; the axis angle
-// is returned as its cosine and sine (sincospi(2U) = sincos(2 pi U)).
+// (id, t_lo, t_hi, draw) and key = seed.  Normals by Box-Muller.
+//
+// The transcendentals of the noise run in FP32 (the FP64 pipe is the scarce
+// unit of the update); every value handed to the FP64 step is an exact double
+// of that FP32 result, and ss_noise returns the same doubles, so the FP64
+// oracle fed ss_noise sees exactly what the update used.  Radii take 52-bit
+// uniforms through neg2log1m (tails to 8.5 sigma); angles take 24-bit
+// uniforms.  The axis angle is returned as its cosine and sine, rounded to
+// FP32 and renormalised in FP64 to unit length (to 1e-21: the second-order
+// expansion of 1/sqrt(1 + d) with |d| < 2^-22), so that
+// sincos(atan2(sa, ca)) reproduces (ca, sa) to FP64 rounding.
 template <bool Q2D, bool WANT_ALPHA = false>
 __device__ __forceinline__ void philox_noise(unsigned long long seed, uint32_t id, unsigned long long t,
                                              double sigma, double xi[3], double &ca, double &sa,
@@ -167,25 +185,63 @@ __device__ __forceinline__ void philox_noise(unsigned long long seed, uint32_t i
     uint32_t tl = (uint32_t)t, th = (uint32_t)(t >> 32);
     uint4 r0 = philox4x32_10(make_uint4(id, tl, th, 0u), key);
     uint4 r1 = philox4x32_10(make_uint4(id, tl, th, 1u), key);
-    // x in [1, 2): U = x - 1, 1 - U = 2 - x, 2 U = 2 x - 2 (all exact)
-    double x1 = u12(r0.x, r0.y), x2 = u12(r0.z, r0.w);
-    double rad = sqrt(-2.0 * log(2.0 - x1));
-    double s, c;
-    sincospi(2.0 * x2 - 2.0, &s, &c);
-    xi[0] = rad * c;
-    xi[1] = rad * s;
+    const float rad = sqrtf(neg2log1m(u12(r0.x, r0.y)));
+    float s, c;
+    sincospif(2.0f * (float)(r0.z >> 8) * 0x1p-24f, &s, &c);
+    xi[0] = (double)(rad * c);
+    xi[1] = (double)(rad * s);
     if (Q2D) {
         xi[2] = 0.0;  // overwritten position z: never read
     } else {
         uint4 r2 = philox4x32_10(make_uint4(id, tl, th, 2u), key);
-        double x5 = u12(r2.x, r2.y), x6 = u12(r2.z, r2.w);
-        double rad2 = sqrt(-2.0 * log(2.0 - x5));
-        xi[2] = rad2 * cospi(2.0 * x6 - 2.0);
+        const float rad2 = sqrtf(neg2log1m(u12(r2.x, r2.y)));
+        xi[2] = (double)(rad2 * cospif(2.0f * (float)(r2.z >> 8) * 0x1p-24f));
     }
-    double x3 = u12(r1.x, r1.y), x4 = u12(r1.z, r1.w);
-    sincospi(2.0 * x3 - 2.0, &sa, &ca);
-    rot = sigma * sqrt(-2.0 * log(2.0 - x4));
-    if (WANT_ALPHA) *alpha = kTwoPi * (x3 - 1.0);
+    float saf, caf;
+    sincospif(2.0f * (float)(r1.x >> 8) * 0x1p-24f, &saf, &caf);
+    const double c0 = (double)caf, s0 = (double)saf;
+    const double d = fma(c0, c0, fma(s0, s0, -1.0));        // |c0, s0|^2 - 1
+    const double inv = fma(d, fma(0.375, d, -0.5), 1.0);     // 1 / sqrt(1 + d)
+    ca = c0 * inv;
+    sa = s0 * inv;
+    rot = sigma * (double)sqrtf(neg2log1m(u12(r1.z, r1.w)));
+    if (WANT_ALPHA) {
+        double a = atan2(sa, ca);
+        *alpha = a < 0.0 ? a + kTwoPi : a;
+    }
+}
+
+// sin r and cos r - 1.  For |r| <= 0.8 (every rotation angle below 8
+// sigma at sigma = 0.1) by their Taylor series to r^17 and r^18, Horner in
+// r^2 (the first omitted terms are below 1.3e-19 relative); the series of
+// cos r - 1 has no cancellation.  Other r through sincos.
+__device__ __forceinline__ void sin_cosm1(double r, double &s, double &cm1) {
+    if (fabs(r) <= 0.8) {
+        const double z = r * r;
+        double p = 1.0 / 355687428096000.0;  // 1/17!
+        p = fma(p, z, -1.0 / 1307674368000.0);
+        p = fma(p, z, 1.0 / 6227020800.0);
+        p = fma(p, z, -1.0 / 39916800.0);
+        p = fma(p, z, 1.0 / 362880.0);
+        p = fma(p, z, -1.0 / 5040.0);
+        p = fma(p, z, 1.0 / 120.0);
+        p = fma(p, z, -1.0 / 6.0);
+        s = fma(r * z, p, r);
+        double q = -1.0 / 6402373705728000.0;  // -1/18!
+        q = fma(q, z, 1.0 / 20922789888000.0);
+        q = fma(q, z, -1.0 / 87178291200.0);
+        q = fma(q, z, 1.0 / 479001600.0);
+        q = fma(q, z, -1.0 / 3628800.0);
+        q = fma(q, z, 1.0 / 40320.0);
+        q = fma(q, z, -1.0 / 720.0);
+        q = fma(q, z, 1.0 / 24.0);
+        q = fma(q, z, -0.5);
+        cm1 = z * q;
+    } else {
+        double c;
+        sincos(r, &s, &c);
+        cm1 = c - 1.0;
+    }
 }
 
 // ---- the Langevin chain ------------------------------------------------
@@ -376,9 +432,8 @@ __device__ __forceinline__ void langevin(double &x, double &y, double &z, double
         double ax0 = (cp * ct) * sa - ca * sp;
         double ax1 = ca * cp + (ct * sa) * sp;
         double ax2 = (-sa) * st;
-        double sr, cr;
-        sincos(rot, &sr, &cr);
-        double cm1 = cr - 1.0;
+        double sr, cm1;
+        sin_cosm1(rot, sr, cm1);
         double k0 = ax1 * n[2] - ax2 * n[1];
         double k1 = ax2 * n[0] - ax0 * n[2];
         double k2 = ax0 * n[1] - ax1 * n[0];
