@@ -117,8 +117,10 @@ int ss_run(ss_ctx *ctx, uint64_t steps, uint64_t *timestep_out);
 /* The on-device noise of step `timestep` as the RandomVector array the
  * verification mode takes: out[n][5] host doubles (x, y, z, axis_angle,
  * rotate_angle) in the caller's particle order (src/bin/simulation/mod.rs:
- * 272-286).  axis_angle is reported as 2*pi*U; the step itself uses
- * sincospi(2U), the same angle without the rounding of 2*pi*U. */
+ * 272-286).  The step uses the axis as its cosine and sine (rounded from
+ * FP32 and renormalised to unit length in FP64); axis_angle is reported as
+ * their atan2 in [0, 2 pi), whose sine and cosine give them back to FP64
+ * rounding. */
 int ss_noise(ss_ctx *ctx, uint64_t timestep, double *out);
 /* Wait for the context's stream. */
 int ss_synchronize(ss_ctx *ctx);
@@ -246,10 +248,14 @@ int ss_ensemble_destroy(ss_ens *ens);
  * z = 0 and theta = pi/2.  Resets every member's timestep to 0. */
 int ss_ensemble_init(ss_ens *ens, const double *particles, uint64_t total);
 /* times the particle update's launch shapes on the ensemble's own data and
- * keeps the fastest; config (optional, 3 entries) receives threads per
- * block, blocks per SM and particles per work unit.  ss_ensemble_run calls
- * it before its first step when it has not run. */
+ * keeps the fastest; config (optional, 4 entries) receives threads per
+ * block, resident blocks per SM, particles per work unit and the register
+ * plan (1: 72, 2: 64, 3: 40 registers per thread).  ss_ensemble_run calls it
+ * before its first step when neither it nor ss_ensemble_set_config has run. */
 int ss_ensemble_autotune(ss_ens *ens, uint32_t *config);
+/* sets the update's launch shape (the 4 entries ss_ensemble_autotune
+ * reports), e.g. one tuned earlier for the same ensemble shape */
+int ss_ensemble_set_config(ss_ens *ens, const uint32_t *config);
 /* steps do_timestep calls of every member (asynchronous) */
 int ss_ensemble_run(ss_ens *ens, uint64_t steps);
 int ss_ensemble_synchronize(ss_ens *ens);

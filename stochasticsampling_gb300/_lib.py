@@ -16,7 +16,7 @@ EXPORTS = [
     "ss_get_flow_complex", "ss_get_magnetic_complex", "ss_get_timestep", "ss_mean_flow_field",
     "ss_mean_magnetic_field", "ss_langevin", "ss_profile_enable", "ss_profile_read", "ss_launch_count",
     "ss_sample_distribution_noalloc", "ss_ensemble_create", "ss_ensemble_destroy", "ss_ensemble_init",
-    "ss_ensemble_autotune", "ss_ensemble_run", "ss_ensemble_synchronize", "ss_ensemble_get_particles",
+    "ss_ensemble_autotune", "ss_ensemble_set_config", "ss_ensemble_run", "ss_ensemble_synchronize", "ss_ensemble_get_particles",
     "ss_ensemble_get_counts", "ss_ensemble_get_flow_field", "ss_ensemble_info", "ss_last_error", "ss_version",
 ]
 
@@ -128,6 +128,7 @@ def load(build_if_missing=True):
         "ss_ensemble_destroy": [vp],
         "ss_ensemble_init": [vp, dp, u64],
         "ss_ensemble_autotune": [vp, ctypes.POINTER(ctypes.c_uint32)],
+        "ss_ensemble_set_config": [vp, ctypes.POINTER(ctypes.c_uint32)],
         "ss_ensemble_run": [vp, u64],
         "ss_ensemble_synchronize": [vp],
         "ss_ensemble_get_particles": [vp, u32, dp],

@@ -53,15 +53,27 @@ struct EnsMember {
     float stepx, stepy;
 };
 
-struct WorkUnit {
+struct WorkUnit {  // a tile of one member's particles
     unsigned long long start;
     uint32_t count;
     uint32_t member;
 };
 
+struct CellChunk {  // up to kChunkCells consecutive cells of one member
+    uint32_t member;
+    int cell0;  // member-local
+    int count;
+};
+
 constexpr int kEnsRow = TABLE_STRIDE;  // no dipolar terms in the ensemble
 constexpr int kEnsLut = 4096;          // the count -> value table of the single context
 constexpr uint32_t kEnsMaxMembers = 4096;
+constexpr int kEnsMaxPhi = 256;
+constexpr int kChunkCells = 128;                // threads of the cell kernels
+constexpr int kChunkCountBytes = 36 * 1024;     // shared-memory budget for one chunk's counts
+
+// cells per chunk of a member with `na` angle bins (the chunk's counts fit the budget)
+inline int chunk_cells(int na) { return std::min(kChunkCells, kChunkCountBytes / (4 * na)); }
 
 // ---------------------------------------------------------------------------
 // kernels
@@ -83,89 +95,119 @@ __global__ void k_ens_ingest(const double *__restrict__ aos, unsigned long long 
     phi[i] = (float)ph;
 }
 
+// the 2-D bin of bin_mixed (z = 0 and theta = pi/2 fall in bin 0 of their
+// one-bin axes): cell = ix * gy + iy, bin = cell * gphi + iphi
+__device__ __forceinline__ void bin2d(const MixedParams &M, double x, double y, float phi, int &cell, int &bin) {
+    const int ix = bin_f(d2f_pos(x), M.igwf[0], M.gx), iy = bin_f(d2f_pos(y), M.igwf[1], M.gy);
+    cell = ix * M.gy + iy;
+    bin = cell * M.gphi + bin_f(phi, M.igwf[3], M.gphi);
+}
+
 __global__ void k_ens_bin(const WorkUnit *__restrict__ units, int nunits, const EnsMember *__restrict__ mem,
                           const double *__restrict__ x, const double *__restrict__ y, const float *__restrict__ phi,
-                          uint32_t *__restrict__ key, uint32_t *__restrict__ counts) {
+                          uint32_t *__restrict__ counts) {
     for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
         const WorkUnit w = units[u];
         const EnsMember &E = mem[w.member];
         for (uint32_t t = threadIdx.x; t < w.count; t += blockDim.x) {
-            unsigned long long i = w.start + t;
-            uint32_t cell;
-            unsigned long long bin;
-            bin_mixed(E.M, x[i], y[i], 0.0, phi[i], 1.57079632679489661923f, cell, bin);
+            const unsigned long long i = w.start + t;
+            int cell, bin;
+            bin2d(E.M, x[i], y[i], phi[i], cell, bin);
             atomicAdd(counts + E.bin_off + bin, 1u);
-            key[i] = (uint32_t)E.cell_off + cell;
         }
     }
 }
 
-// FP64 atomic add of a warp's sum by lane 0 (all lanes of the warp call it)
-__device__ __forceinline__ void warp_add(double *dst, double v) {
+// Angular contraction, one block per cell chunk of one member: the chunk's
+// counts (contiguous) and the member's 9 x nang stress kernel are staged in
+// shared memory with coalesced loads; thread c then sums its cell's row,
+// visiting the angles from a = c mod nang on so that a warp's shared-memory
+// reads fall in different banks.  The chunk's 9 component sums are added to
+// the member's FP64 sums with one atomic each.
+__global__ void __launch_bounds__(kChunkCells) k_ens_contract(const CellChunk *__restrict__ chunks,
+                                                              const EnsMember *__restrict__ mem,
+                                                              const uint32_t *__restrict__ counts,
+                                                              const float *__restrict__ kern,
+                                                              const float *__restrict__ lut,
+                                                              float2 *__restrict__ fwd, float *__restrict__ diff,
+                                                              double *__restrict__ sums) {
+    extern __shared__ uint32_t s_counts[];
+    __shared__ float s_kern[9 * kEnsMaxPhi];
+    __shared__ double s_red[kChunkCells / 32][9];
+    const CellChunk ch = chunks[blockIdx.x];
+    const EnsMember &E = mem[ch.member];
+    const int na = E.M.nang, tid = threadIdx.x;
+    const uint32_t *src = counts + E.bin_off + (long long)ch.cell0 * na;
+    for (int e = tid; e < ch.count * na; e += blockDim.x) s_counts[e] = src[e];
+    for (int e = tid; e < 9 * na; e += blockDim.x) s_kern[e] = kern[E.kern_off + e];
+    __syncthreads();
+    float acc[9];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(dst, v);
-}
-
-__global__ void __launch_bounds__(128) k_ens_contract(const uint32_t *__restrict__ counts,
-                                                      const uint16_t *__restrict__ cell_member,
-                                                      const EnsMember *__restrict__ mem, const float *__restrict__ kern,
-                                                      const float *__restrict__ lut, int total_cells,
-                                                      float2 *__restrict__ fwd, float *__restrict__ table,
-                                                      double *__restrict__ sums) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = c < total_cells;
-    int m = live ? cell_member[c] : 0;
-    float acc[10];
-#pragma unroll
-    for (int j = 0; j < 10; ++j) acc[j] = 0.f;
-    const EnsMember &E = mem[m];
+    for (int j = 0; j < 9; ++j) acc[j] = 0.f;
+    const bool live = tid < ch.count;
     if (live) {
-        const int na = E.M.nang, local = c - E.cell_off;
-        const float *K = kern + E.kern_off;
+        const uint32_t *row = s_counts + tid * na;
         const float *L = lut + E.lut_off;
-        const uint32_t *row = counts + E.bin_off + (long long)local * na;
-        for (int a = 0; a < na; ++a) {
+        float dens = 0.f;
+        int a = tid % na;
+        for (int i = 0; i < na; ++i) {
             const uint32_t n = row[a];
-            float f = (n < (uint32_t)kEnsLut) ? __ldg(L + n) : (float)(((double)n / E.M.dist_den) * E.M.volume);
+            const float f = (n < (uint32_t)kEnsLut) ? __ldg(L + n) : (float)(((double)n / E.M.dist_den) * E.M.volume);
 #pragma unroll
-            for (int j = 0; j < 9; ++j) acc[j] = fmaf(__ldg(K + j * na + a), f, acc[j]);
-            acc[9] += f;
+            for (int j = 0; j < 9; ++j) acc[j] = fmaf(s_kern[j * na + a], f, acc[j]);
+            dens += f;
+            a = (a + 1 == na) ? 0 : a + 1;
         }
-        const int nc = E.M.ncell;
+        const int nc = E.M.ncell, local = ch.cell0 + tid;
 #pragma unroll
         for (int j = 0; j < 9; ++j) fwd[E.fwd_off + (long long)j * nc + local] = make_float2(acc[j] * E.M.measure, 0.f);
-        float dens = acc[9] * E.M.dthph;
-        table[(long long)c * kEnsRow + T_DIFF] = sqrtf(E.M.two_dt * (E.M.Dt + E.M.volex * dens));
+        diff[E.cell_off + local] = sqrtf(E.M.two_dt * (E.M.Dt + E.M.volex * (dens * E.M.dthph)));
     }
-    // FP64 component sums: one atomic per warp when the warp's cells belong
-    // to one member (the same value on every lane), else one per cell
-    const bool uniform = __match_any_sync(0xffffffffu, live ? m : -1) == 0xffffffffu && live;
+    // warp partials in FP32 (32 terms), the block's and the member's sums in
+    // FP64 (the FP64 pipe is too slow for a per-thread tree)
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
-        double v = live ? (double)(acc[j] * E.M.measure) : 0.0;
-        if (uniform) warp_add(sums + 9 * m + j, v);
-        else if (live) atomicAdd(sums + 9 * m + j, v);
+        float v = live ? acc[j] * E.M.measure : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((tid & 31) == 0) s_red[tid >> 5][j] = (double)v;
+    }
+    __syncthreads();
+    if (tid < 9) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += s_red[w][tid];
+        atomicAdd(sums + 9 * ch.member + tid, v);
     }
 }
 
-__global__ void k_ens_center(float2 *__restrict__ fwd, const uint16_t *__restrict__ cell_member,
-                             const EnsMember *__restrict__ mem, int total_cells, const double *__restrict__ sums) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= total_cells) return;
-    const EnsMember &E = mem[cell_member[c]];
-    const int nc = E.M.ncell, local = c - E.cell_off, m = cell_member[c];
-#pragma unroll
-    for (int j = 0; j < 9; ++j) fwd[E.fwd_off + (long long)j * nc + local].x -= (float)(sums[9 * m + j] / (double)nc);
+// per member and component: the FP64 mean rounded to FP32
+__global__ void k_ens_means(const EnsMember *__restrict__ mem, int nm, const double *__restrict__ sums,
+                            float *__restrict__ means) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 9 * nm) means[i] = (float)(sums[i] / (double)mem[i / 9].M.ncell);
 }
 
-__global__ void k_ens_kspace(const float2 *__restrict__ fwd, float2 *__restrict__ inv,
-                             const uint16_t *__restrict__ cell_member, const EnsMember *__restrict__ mem,
-                             int total_cells) {
-    int cg = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cg >= total_cells) return;
-    const EnsMember &E = mem[cell_member[cg]];
-    const int nc = E.M.ncell, c = cg - E.cell_off;
+// subtract the means before the FP32 transform (the k_center_m of a single context)
+__global__ void __launch_bounds__(kChunkCells) k_ens_center(const CellChunk *__restrict__ chunks,
+                                                            const EnsMember *__restrict__ mem,
+                                                            const float *__restrict__ means,
+                                                            float2 *__restrict__ fwd) {
+    const CellChunk ch = chunks[blockIdx.x];
+    if ((int)threadIdx.x >= ch.count) return;
+    const EnsMember &E = mem[ch.member];
+    const int nc = E.M.ncell, local = ch.cell0 + threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < 9; ++j) fwd[E.fwd_off + (long long)j * nc + local].x -= means[9 * ch.member + j];
+}
+
+__global__ void __launch_bounds__(kChunkCells) k_ens_kspace(const CellChunk *__restrict__ chunks,
+                                                            const EnsMember *__restrict__ mem,
+                                                            const float2 *__restrict__ fwd,
+                                                            float2 *__restrict__ inv) {
+    const CellChunk ch = chunks[blockIdx.x];
+    if ((int)threadIdx.x >= ch.count) return;
+    const EnsMember &E = mem[ch.member];
+    const int nc = E.M.ncell, c = ch.cell0 + threadIdx.x;
     const int iy = c % E.M.gy, ix = c / E.M.gy;
     float k[3] = {kval_f(ix, E.M.gx, E.stepx), kval_f(iy, E.M.gy, E.stepy), 0.f};
     float s = k[0] * k[0] + k[1] * k[1];
@@ -197,35 +239,55 @@ __global__ void k_ens_kspace(const float2 *__restrict__ fwd, float2 *__restrict_
             inv[E.inv_off + (long long)(3 * a + b) * nc + c] = make_float2(-(k[a] * u[b].y), k[a] * u[b].x);
 }
 
-__global__ void k_ens_table(const float2 *__restrict__ inv, const uint16_t *__restrict__ cell_member,
-                            const EnsMember *__restrict__ mem, int total_cells, float *__restrict__ table) {
-    int cg = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cg >= total_cells) return;
-    const EnsMember &E = mem[cell_member[cg]];
-    const int nc = E.M.ncell, c = cg - E.cell_off;
-    float g[9];
+// the per-cell row (u, W, E, diffusion length) of k_table_m, assembled in
+// shared memory and written as whole rows (coalesced)
+__global__ void __launch_bounds__(kChunkCells) k_ens_table(const CellChunk *__restrict__ chunks,
+                                                           const EnsMember *__restrict__ mem,
+                                                           const float2 *__restrict__ inv,
+                                                           const float *__restrict__ diff,
+                                                           float *__restrict__ table) {
+    __shared__ float s_rows[kChunkCells][kEnsRow + 1];
+    const CellChunk ch = chunks[blockIdx.x];
+    const EnsMember &E = mem[ch.member];
+    const int tid = threadIdx.x;
+    if (tid < ch.count) {
+        const int nc = E.M.ncell, c = ch.cell0 + tid;
+        float g[9];
 #pragma unroll
-    for (int j = 0; j < 9; ++j) g[j] = inv[E.inv_off + (long long)j * nc + c].x;
-    float *row = table + (long long)cg * kEnsRow;
+        for (int j = 0; j < 9; ++j) g[j] = inv[E.inv_off + (long long)j * nc + c].x;
+        float *row = s_rows[tid];
 #pragma unroll
-    for (int r = 0; r < 3; ++r) row[T_U + r] = inv[E.inv_off + (long long)(9 + r) * nc + c].x;
-    row[T_W01] = (g[1] - g[3]) * 0.5f;
-    row[T_W02] = (g[2] - g[6]) * 0.5f;
-    row[T_W12] = (g[5] - g[7]) * 0.5f;
-    row[T_E00] = g[0];
-    row[T_E01] = (g[1] + g[3]) * 0.5f;
-    row[T_E02] = (g[2] + g[6]) * 0.5f;
-    row[T_E11] = g[4];
-    row[T_E12] = (g[5] + g[7]) * 0.5f;
-    row[T_E22] = g[8];
+        for (int r = 0; r < 3; ++r) row[T_U + r] = inv[E.inv_off + (long long)(9 + r) * nc + c].x;
+        row[T_W01] = (g[1] - g[3]) * 0.5f;
+        row[T_W02] = (g[2] - g[6]) * 0.5f;
+        row[T_W12] = (g[5] - g[7]) * 0.5f;
+        row[T_E00] = g[0];
+        row[T_E01] = (g[1] + g[3]) * 0.5f;
+        row[T_E02] = (g[2] + g[6]) * 0.5f;
+        row[T_E11] = g[4];
+        row[T_E12] = (g[5] + g[7]) * 0.5f;
+        row[T_E22] = g[8];
+        row[T_DIFF] = diff[E.cell_off + c];
+        row[13] = row[14] = row[15] = 0.f;
+    }
+    __syncthreads();
+    float *dst = table + (long long)(E.cell_off + ch.cell0) * kEnsRow;
+    for (int e = tid; e < ch.count * kEnsRow; e += blockDim.x) dst[e] = s_rows[e / kEnsRow][e % kEnsRow];
 }
 
-// the persistent update: each block takes work units (a tile of one member's
-// particles) round robin; the member's parameters are block-uniform
-__global__ void k_ens_update(const WorkUnit *__restrict__ units, int nunits, const EnsMember *__restrict__ mem,
-                             double *__restrict__ x, double *__restrict__ y, float *__restrict__ phi,
-                             uint32_t *__restrict__ key, const float *__restrict__ table,
-                             const unsigned long long *__restrict__ d_step, uint32_t *__restrict__ counts_next) {
+// The persistent update: each block takes work units (a tile of one member's
+// particles) round robin; the member's parameters are block-uniform and
+// staged in shared memory.  The cell a particle sits in is recomputed from
+// its position (the bin2d of the previous step's binning, so the same cell),
+// which saves a stored cell key.  MINB (blocks per SM the compiler plans
+// registers for) is one of the autotuner's choices.
+template <int MINB>
+__global__ void __launch_bounds__(512, MINB) k_ens_update(const WorkUnit *__restrict__ units, int nunits,
+                                                          const EnsMember *__restrict__ mem,
+                                                          double *__restrict__ x, double *__restrict__ y,
+                                                          float *__restrict__ phi, const float *__restrict__ table,
+                                                          const unsigned long long *__restrict__ d_step,
+                                                          uint32_t *__restrict__ counts_next) {
     __shared__ EnsMember E;
     const unsigned long long t = *d_step;
     for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
@@ -235,30 +297,34 @@ __global__ void k_ens_update(const WorkUnit *__restrict__ units, int nunits, con
         __syncthreads();
         const MixedParams &M = E.M;
         for (uint32_t k = threadIdx.x; k < w.count; k += blockDim.x) {
+            // the member's parameters are re-read from shared memory in every
+            // iteration instead of being held in registers across the loop
+            asm volatile("" ::: "memory");
             const unsigned long long i = w.start + k;
-            const uint32_t local_id = (uint32_t)(i - E.part_off);
-            const uint32_t gcell = key[i];
+            double px = x[i], py = y[i];
             float pph = phi[i], pth = 1.57079632679489661923f;
-            TableFieldsF F{table + (long long)gcell * kEnsRow};
+            const int cx = bin_f(d2f_pos(px), M.igwf[0], M.gx), cy = bin_f(d2f_pos(py), M.igwf[1], M.gy);
+            TableFieldsF F(table + (long long)(E.cell_off + cx * M.gy + cy) * kEnsRow);
             float xi[3], ca, sa, rot;
-            philox_noise_f<true>(M.seed, local_id, t, M.sigma_rot, xi, ca, sa, rot);
+            philox_noise_f<true>(M.seed, (uint32_t)(i - E.part_off), t, M.sigma_rot, xi, ca, sa, rot);
             float st[3];
             langevin_mixed<true>(pph, pth, st, F, xi, ca, sa, rot, M);
-            const int lcell = (int)gcell - E.cell_off;
-            const int cx = lcell / M.gy, cy = lcell % M.gy;
-            double px = advance64(x[i], st[0], cx, M.gx, M.gwf[0], M.bx, M.bx2);
-            double py = advance64(y[i], st[1], cy, M.gy, M.gwf[1], M.by, M.by2);
-            uint32_t ncell;
-            unsigned long long bin;
-            bin_mixed(M, px, py, 0.0, pph, pth, ncell, bin);
+            px = advance64(px, st[0], cx, M.gx, M.gwf[0], M.bx, M.bx2);
+            py = advance64(py, st[1], cy, M.gy, M.gwf[1], M.by, M.by2);
+            int cell, bin;
+            bin2d(M, px, py, pph, cell, bin);
             atomicAdd(counts_next + E.bin_off + bin, 1u);
-            key[i] = (uint32_t)E.cell_off + ncell;
             x[i] = px;
             y[i] = py;
             phi[i] = pph;
         }
     }
 }
+
+using UpdateKernel = void (*)(const WorkUnit *, int, const EnsMember *, double *, double *, float *, const float *,
+                              const unsigned long long *, uint32_t *);
+constexpr int kUpdateVariants = 3;
+const UpdateKernel kUpdate[kUpdateVariants] = {k_ens_update<1>, k_ens_update<2>, k_ens_update<3>};
 
 __global__ void k_ens_step_inc(unsigned long long *d_step) { *d_step += 1ull; }
 
@@ -284,7 +350,6 @@ __global__ void k_ens_real(const float2 *__restrict__ src, long long count, doub
 struct ss_ens {
     uint32_t nm = 0;
     std::vector<EnsMember> mem;
-    std::vector<int> shape_of;  // member -> shape group
     struct Group {
         int gx, gy;
         std::vector<uint32_t> members;
@@ -305,14 +370,16 @@ struct ss_ens {
     EnsMember *d_mem = nullptr;
     WorkUnit *d_units = nullptr;
     int nunits = 0;
-    int threads = 256, blocks_per_sm = 4, unit = 16384;
+    int variant = 1, threads = 256, blocks_per_sm = 4, unit = 16384;  // the update's launch shape
     bool tuned = false;
-    uint16_t *cell_member = nullptr;
+    CellChunk *d_chunks = nullptr;
+    int nchunks = 0;
+    size_t chunk_smem = 0;  // dynamic shared memory of k_ens_contract
     double *x = nullptr, *y = nullptr, *staging = nullptr, *realbuf = nullptr;
     float *phi = nullptr;
-    uint32_t *key = nullptr, *counts[2] = {};
+    uint32_t *counts[2] = {};
     float2 *fwd = nullptr, *inv = nullptr;
-    float *table = nullptr, *kern = nullptr, *lut = nullptr;
+    float *table = nullptr, *kern = nullptr, *lut = nullptr, *diff = nullptr, *means = nullptr;
     double *sums = nullptr;
     unsigned long long *d_step = nullptr;
     cudaGraphExec_t graph[2] = {};
@@ -371,23 +438,30 @@ unsigned nb(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 // the field solve of one step: histogram counts[ccur] -> table
 int enqueue_solve(ss_ens *e, int ccur, uint64_t *nl) {
     cudaStream_t s = e->stream;
-    const unsigned b = nb(e->total_cells, 128);
+    const unsigned nc = (unsigned)e->nchunks;
     ECK(cudaMemsetAsync(e->sums, 0, 9ull * e->nm * sizeof(double), s));
-    k_ens_contract<<<b, 128, 0, s>>>(e->counts[ccur], e->cell_member, e->d_mem, e->kern, e->lut, e->total_cells,
-                                     e->fwd, e->table, e->sums);
-    k_ens_center<<<b, 128, 0, s>>>(e->fwd, e->cell_member, e->d_mem, e->total_cells, e->sums);
+    k_ens_contract<<<nc, kChunkCells, e->chunk_smem, s>>>(e->d_chunks, e->d_mem, e->counts[ccur], e->kern, e->lut,
+                                                           e->fwd, e->diff, e->sums);
+    k_ens_means<<<nb(9ll * e->nm, 128), 128, 0, s>>>(e->d_mem, (int)e->nm, e->sums, e->means);
+    k_ens_center<<<nc, kChunkCells, 0, s>>>(e->d_chunks, e->d_mem, e->means, e->fwd);
     for (auto &g : e->groups)
         ECKF(cufftExecC2C(g.fwd_plan, reinterpret_cast<cufftComplex *>(e->fwd + g.fwd_off),
                           reinterpret_cast<cufftComplex *>(e->fwd + g.fwd_off), CUFFT_FORWARD));
-    k_ens_kspace<<<b, 128, 0, s>>>(e->fwd, e->inv, e->cell_member, e->d_mem, e->total_cells);
+    k_ens_kspace<<<nc, kChunkCells, 0, s>>>(e->d_chunks, e->d_mem, e->fwd, e->inv);
     for (auto &g : e->groups)
         ECKF(cufftExecC2C(g.inv_plan, reinterpret_cast<cufftComplex *>(e->inv + g.inv_off),
                           reinterpret_cast<cufftComplex *>(e->inv + g.inv_off), CUFFT_INVERSE));
-    k_ens_table<<<b, 128, 0, s>>>(e->inv, e->cell_member, e->d_mem, e->total_cells, e->table);
-    *nl += 4;
+    k_ens_table<<<nc, kChunkCells, 0, s>>>(e->d_chunks, e->d_mem, e->inv, e->diff, e->table);
+    *nl += 5;
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return efail(e, SS_ERR_CUDA, "ensemble solve launch: %s", cudaGetErrorString(err));
     return SS_OK;
+}
+
+void launch_update(ss_ens *e, int variant, int threads, int bps, double *x, double *y, float *phi,
+                   uint32_t *counts_next) {
+    kUpdate[variant]<<<(unsigned)(e->sms * bps), threads, 0, e->stream>>>(e->d_units, e->nunits, e->d_mem, x, y, phi,
+                                                                         e->table, e->d_step, counts_next);
 }
 
 // one do_timestep of every member: solve from counts[ccur], move the
@@ -396,8 +470,7 @@ int enqueue_step(ss_ens *e, int ccur, uint64_t *nl) {
     cudaStream_t s = e->stream;
     ECKR(enqueue_solve(e, ccur, nl));
     ECK(cudaMemsetAsync(e->counts[1 - ccur], 0, (size_t)e->total_bins * sizeof(uint32_t), s));
-    k_ens_update<<<(unsigned)(e->sms * e->blocks_per_sm), e->threads, 0, s>>>(
-        e->d_units, e->nunits, e->d_mem, e->x, e->y, e->phi, e->key, e->table, e->d_step, e->counts[1 - ccur]);
+    launch_update(e, e->variant, e->threads, e->blocks_per_sm, e->x, e->y, e->phi, e->counts[1 - ccur]);
     k_ens_step_inc<<<1, 1, 0, s>>>(e->d_step);
     *nl += 2;
     cudaError_t err = cudaGetLastError();
@@ -405,17 +478,19 @@ int enqueue_step(ss_ens *e, int ccur, uint64_t *nl) {
     return SS_OK;
 }
 
-// Autotuner for the persistent update: every (threads, blocks per SM,
-// particles per unit) candidate runs the update kernel on a scratch copy of
-// the ensemble's particles and fields; the fastest median of three wins.
-// The candidates do not change the ensemble's state.
+// Autotuner for the persistent update: every candidate (register plan of
+// 1, 2 or 3 blocks per SM; threads per block; resident blocks per SM;
+// particles per work unit) runs the update on a scratch copy of the
+// ensemble's particles through the fields of the current histogram; the
+// fastest median of three wins.  The candidates do not change the
+// ensemble's state.
 struct TuneScratch {
     double *x = nullptr, *y = nullptr;
     float *phi = nullptr;
-    uint32_t *key = nullptr, *counts = nullptr;
+    uint32_t *counts = nullptr;
     cudaEvent_t a = nullptr, b = nullptr;
     ~TuneScratch() {
-        cudaFree(x); cudaFree(y); cudaFree(phi); cudaFree(key); cudaFree(counts);
+        cudaFree(x); cudaFree(y); cudaFree(phi); cudaFree(counts);
         if (a) cudaEventDestroy(a);
         if (b) cudaEventDestroy(b);
     }
@@ -436,51 +511,49 @@ int autotune(ss_ens *e) {
     ECK(cudaMalloc((void **)&S.x, N * sizeof(double)));
     ECK(cudaMalloc((void **)&S.y, N * sizeof(double)));
     ECK(cudaMalloc((void **)&S.phi, N * sizeof(float)));
-    ECK(cudaMalloc((void **)&S.key, N * sizeof(uint32_t)));
     ECK(cudaMalloc((void **)&S.counts, (size_t)e->total_bins * sizeof(uint32_t)));
     ECK(cudaEventCreate(&S.a));
     ECK(cudaEventCreate(&S.b));
-    // the candidates move the particles through the fields of the current histogram
     uint64_t nl = 0;
     ECKR(enqueue_solve(e, e->ccur, &nl));
     e->launches += nl;
     float best = 1e30f;
-    int bt = e->threads, bb = e->blocks_per_sm, bu = e->unit;
+    int bv = e->variant, bt = e->threads, bb = e->blocks_per_sm, bu = e->unit;
     for (int unit : un) {
         ECKR(build_units(e, unit));
-        for (int t : th)
-            for (int k : bps) {
-                float ms[3];
-                for (int r = 0; r < 3; ++r) {
-                    ECK(cudaMemcpyAsync(S.x, e->x, N * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
-                    ECK(cudaMemcpyAsync(S.y, e->y, N * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
-                    ECK(cudaMemcpyAsync(S.phi, e->phi, N * sizeof(float), cudaMemcpyDeviceToDevice, e->stream));
-                    ECK(cudaMemcpyAsync(S.key, e->key, N * sizeof(uint32_t), cudaMemcpyDeviceToDevice, e->stream));
-                    ECK(cudaMemsetAsync(S.counts, 0, (size_t)e->total_bins * sizeof(uint32_t), e->stream));
-                    ECK(cudaEventRecord(S.a, e->stream));
-                    k_ens_update<<<(unsigned)(e->sms * k), t, 0, e->stream>>>(e->d_units, e->nunits, e->d_mem, S.x,
-                                                                              S.y, S.phi, S.key, e->table, e->d_step,
-                                                                              S.counts);
-                    cudaError_t le = cudaGetLastError();
-                    if (le == cudaErrorLaunchOutOfResources || le == cudaErrorInvalidConfiguration) {
-                        ms[r] = 1e30f;  // shape not launchable on this device: never chosen
-                        continue;
+        for (int v = 0; v < kUpdateVariants; ++v)
+            for (int t : th)
+                for (int k : bps) {
+                    float ms[3];
+                    for (int r = 0; r < 3; ++r) {
+                        ECK(cudaMemcpyAsync(S.x, e->x, N * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
+                        ECK(cudaMemcpyAsync(S.y, e->y, N * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
+                        ECK(cudaMemcpyAsync(S.phi, e->phi, N * sizeof(float), cudaMemcpyDeviceToDevice, e->stream));
+                        ECK(cudaMemsetAsync(S.counts, 0, (size_t)e->total_bins * sizeof(uint32_t), e->stream));
+                        ECK(cudaEventRecord(S.a, e->stream));
+                        launch_update(e, v, t, k, S.x, S.y, S.phi, S.counts);
+                        cudaError_t le = cudaGetLastError();
+                        if (le == cudaErrorLaunchOutOfResources || le == cudaErrorInvalidConfiguration) {
+                            ms[r] = 1e30f;  // shape not launchable on this device: never chosen
+                            continue;
+                        }
+                        if (le != cudaSuccess) return efail(e, SS_ERR_CUDA, "autotune: %s", cudaGetErrorString(le));
+                        e->launches += 1;
+                        ECK(cudaEventRecord(S.b, e->stream));
+                        ECK(cudaEventSynchronize(S.b));
+                        ECK(cudaEventElapsedTime(&ms[r], S.a, S.b));
                     }
-                    if (le != cudaSuccess) return efail(e, SS_ERR_CUDA, "autotune: %s", cudaGetErrorString(le));
-                    e->launches += 1;
-                    ECK(cudaEventRecord(S.b, e->stream));
-                    ECK(cudaEventSynchronize(S.b));
-                    ECK(cudaEventElapsedTime(&ms[r], S.a, S.b));
+                    std::sort(ms, ms + 3);
+                    if (ms[1] < best) {
+                        best = ms[1];
+                        bv = v;
+                        bt = t;
+                        bb = k;
+                        bu = unit;
+                    }
                 }
-                std::sort(ms, ms + 3);
-                if (ms[1] < best) {
-                    best = ms[1];
-                    bt = t;
-                    bb = k;
-                    bu = unit;
-                }
-            }
     }
+    e->variant = bv;
     e->threads = bt;
     e->blocks_per_sm = bb;
     ECKR(build_units(e, bu));
@@ -498,8 +571,9 @@ void destroy(ss_ens *e) {
     }
     for (auto &g : e->graph)
         if (g) cudaGraphExecDestroy(g);
-    cudaFree(e->d_mem); cudaFree(e->d_units); cudaFree(e->cell_member); cudaFree(e->x); cudaFree(e->y);
-    cudaFree(e->staging); cudaFree(e->realbuf); cudaFree(e->phi); cudaFree(e->key); cudaFree(e->counts[0]);
+    cudaFree(e->d_mem); cudaFree(e->d_units); cudaFree(e->d_chunks); cudaFree(e->x); cudaFree(e->y);
+    cudaFree(e->staging); cudaFree(e->realbuf); cudaFree(e->phi); cudaFree(e->diff); cudaFree(e->means);
+    cudaFree(e->counts[0]);
     cudaFree(e->counts[1]); cudaFree(e->fwd); cudaFree(e->inv); cudaFree(e->table); cudaFree(e->kern); cudaFree(e->lut);
     cudaFree(e->sums); cudaFree(e->d_step);
     if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
@@ -527,9 +601,10 @@ int ss_ensemble_create(const ss_grid *grids, const ss_box *boxes, const ss_param
         const ss_box &b = boxes[m];
         const ss_params &p = params[m];
         if (g.x < 2 || g.y < 2 || g.z != 1 || g.theta != 1 || g.phi < 1 || g.x > 4096 || g.y > 4096 ||
-            g.phi > 1024)
+            g.phi > (uint64_t)kEnsMaxPhi)
             return efail(nullptr, SS_ERR_INVALID_ARGUMENT,
-                         "member %u: grid must be quasi-2-D (z = theta = 1, 2 <= x, y <= 4096, 1 <= phi <= 1024)", m);
+                         "member %u: grid must be quasi-2-D (z = theta = 1, 2 <= x, y <= 4096, 1 <= phi <= %d)", m,
+                         kEnsMaxPhi);
         if (!(b.x > 0) || !(b.y > 0) || !(b.z > 0) || !std::isfinite(b.x) || !std::isfinite(b.y) ||
             !std::isfinite(b.z))
             return efail(nullptr, SS_ERR_INVALID_ARGUMENT, "member %u: box sizes must be positive and finite", m);
@@ -643,9 +718,14 @@ int ss_ensemble_create(const ss_grid *grids, const ss_box *boxes, const ss_param
         for (int i = 0; i < kEnsLut; ++i)
             lut[(size_t)m * kEnsLut + i] = (float)(((double)i / e->mem[m].M.dist_den) * e->mem[m].M.volume);
     }
-    std::vector<uint16_t> cm((size_t)e->total_cells);
-    for (uint32_t m = 0; m < count; ++m)
-        for (int c = 0; c < e->mem[m].M.ncell; ++c) cm[(size_t)e->mem[m].cell_off + c] = (uint16_t)m;
+    // cell chunks: member-aligned blocks of the cell kernels
+    std::vector<CellChunk> chunks;
+    for (uint32_t m = 0; m < count; ++m) {
+        const int nc = e->mem[m].M.ncell, per = chunk_cells(e->mem[m].M.nang);
+        for (int c0 = 0; c0 < nc; c0 += per) chunks.push_back({m, c0, std::min(per, nc - c0)});
+        e->chunk_smem = std::max(e->chunk_smem, (size_t)per * e->mem[m].M.nang * sizeof(uint32_t));
+    }
+    e->nchunks = (int)chunks.size();
 
     cudaError_t err = cudaGetDevice(&e->device);
     if (err == cudaSuccess) err = cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, e->device);
@@ -662,11 +742,12 @@ int ss_ensemble_create(const ss_grid *grids, const ss_box *boxes, const ss_param
         if (err == cudaSuccess) err = cudaMalloc(p, std::max<size_t>(bytes, 16));
     };
     A((void **)&e->d_mem, count * sizeof(EnsMember));
-    A((void **)&e->cell_member, cm.size() * sizeof(uint16_t));
+    A((void **)&e->d_chunks, chunks.size() * sizeof(CellChunk));
+    A((void **)&e->diff, (size_t)e->total_cells * sizeof(float));
+    A((void **)&e->means, 9ull * count * sizeof(float));
     A((void **)&e->x, N * sizeof(double));
     A((void **)&e->y, N * sizeof(double));
     A((void **)&e->phi, N * sizeof(float));
-    A((void **)&e->key, N * sizeof(uint32_t));
     A((void **)&e->counts[0], (size_t)e->total_bins * sizeof(uint32_t));
     A((void **)&e->counts[1], (size_t)e->total_bins * sizeof(uint32_t));
     A((void **)&e->fwd, (size_t)fo * sizeof(float2));
@@ -684,7 +765,8 @@ int ss_ensemble_create(const ss_grid *grids, const ss_box *boxes, const ss_param
     if (err == cudaSuccess)
         err = cudaMemcpyAsync(e->d_mem, e->mem.data(), count * sizeof(EnsMember), cudaMemcpyHostToDevice, st);
     if (err == cudaSuccess)
-        err = cudaMemcpyAsync(e->cell_member, cm.data(), cm.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, st);
+        err = cudaMemcpyAsync(e->d_chunks, chunks.data(), chunks.size() * sizeof(CellChunk), cudaMemcpyHostToDevice,
+                              st);
     if (err == cudaSuccess)
         err = cudaMemcpyAsync(e->kern, kern.data(), kern.size() * sizeof(float), cudaMemcpyHostToDevice, st);
     if (err == cudaSuccess)
@@ -751,7 +833,7 @@ int ss_ensemble_init(ss_ens *e, const double *particles, uint64_t total) {
     }
     ECK(cudaMemsetAsync(e->counts[0], 0, (size_t)e->total_bins * sizeof(uint32_t), e->stream));
     k_ens_bin<<<(unsigned)(e->sms * 4), 256, 0, e->stream>>>(e->d_units, e->nunits, e->d_mem, e->x, e->y, e->phi,
-                                                              e->key, e->counts[0]);
+                                                              e->counts[0]);
     ECK(cudaGetLastError());
     e->launches += e->nm + 1;
     ECK(cudaMemsetAsync(e->d_step, 0, sizeof(unsigned long long), e->stream));
@@ -771,7 +853,31 @@ int ss_ensemble_autotune(ss_ens *e, uint32_t *config) {
         config[0] = (uint32_t)e->threads;
         config[1] = (uint32_t)e->blocks_per_sm;
         config[2] = (uint32_t)e->unit;
+        config[3] = (uint32_t)e->variant + 1;
     }
+    return SS_OK;
+}
+
+int ss_ensemble_set_config(ss_ens *e, const uint32_t *config) {
+    if (!e || !config) return efail(e, SS_ERR_INVALID_ARGUMENT, "null argument");
+    const uint32_t t = config[0], k = config[1], u = config[2], v = config[3];
+    if (t == 0 || t > 512 || t % 32 != 0 || k < 1 || k > 32 || u < 32 || u > (1u << 24) || v < 1 ||
+        v > (uint32_t)kUpdateVariants)
+        return efail(e, SS_ERR_INVALID_ARGUMENT,
+                     "update config: threads a multiple of 32 in [32, 512], blocks per SM in [1, 32], "
+                     "particles per unit in [32, 2^24], register plan in [1, %d]",
+                     kUpdateVariants);
+    ECK(cudaSetDevice(e->device));
+    for (auto &g : e->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    e->threads = (int)t;
+    e->blocks_per_sm = (int)k;
+    e->variant = (int)v - 1;
+    ECKR(build_units(e, (int)u));
+    e->tuned = true;
     return SS_OK;
 }
 

@@ -288,12 +288,13 @@ __global__ void __launch_bounds__(256) k_update_m(MixedParams M, double *__restr
     uint32_t cell = key[i];
     float pph = phi[i], pth = 1.57079632679489661923f;
     if (!CANON) pth = theta[i];
-    TableFieldsF F{table + (long long)cell * ts};
+    TableFieldsF F(table + (long long)cell * ts);
     float xi[3], ca, sa, rot;
+    // the mixed mode never sorts, so particle i keeps caller index i (id[i] == i)
     if (NOISE == 0) {
-        philox_noise_f<Q2D>(M.seed, id[i], *d_step, M.sigma_rot, xi, ca, sa, rot);
+        philox_noise_f<Q2D>(M.seed, (uint32_t)i, *d_step, M.sigma_rot, xi, ca, sa, rot);
     } else {
-        const double *r = noise + 5ull * id[i];
+        const double *r = noise + 5ull * i;
         xi[0] = (float)r[0]; xi[1] = (float)r[1]; xi[2] = (float)r[2];
         sincosf((float)r[3], &sa, &ca);
         rot = (float)r[4];

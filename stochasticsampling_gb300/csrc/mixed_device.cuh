@@ -31,11 +31,41 @@ __device__ __forceinline__ float modulo_f(float f, float m) {
     return r < 0.0f ? r + fabsf(m) : r;
 }
 
+// FP64 <-> FP32 conversions in integer arithmetic.  This GPU's FP64 pipe
+// issues about one instruction per clock per SM and a conversion occupies it
+// like an FP64 add, while the integer pipes are many times wider; the
+// mixed step converts every position for binning and every FP32 step to
+// FP64 for the position update.
+//
+// d2f_pos: the float nearest a position d (ties to even), the same as
+// (float)d for d >= 2^-126; 0 for smaller or negative d (which bin to cell 0
+// either way).
+__device__ __forceinline__ float d2f_pos(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const uint32_t e = (uint32_t)(b >> 52);  // biased exponent; >= 2048 when negative
+    if (e < 1023u - 126u || e >= 2048u) return 0.0f;
+    uint32_t f = ((e - 896u) << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu);
+    const uint32_t rest = (uint32_t)b & 0x1FFFFFFFu;  // the 29 bits rounded off
+    if (rest > 0x10000000u || (rest == 0x10000000u && (f & 1u))) f += 1u;
+    return __uint_as_float(f);
+}
+
+// f2d: the exact double of a float (zero, subnormals, inf and nan through
+// the conversion instruction)
+__device__ __forceinline__ double f2d(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xFFu;
+    if (e == 0u || e == 0xFFu) return (double)f;
+    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                 ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
+    return __longlong_as_double((long long)b);
+}
+
 __device__ __forceinline__ void bin_mixed(const MixedParams &M, double x, double y, double z, float phi, float theta,
                                           uint32_t &cell, unsigned long long &bin) {
-    int ix = bin_f((float)x, M.igwf[0], M.gx);
-    int iy = bin_f((float)y, M.igwf[1], M.gy);
-    int iz = bin_f((float)z, M.igwf[2], M.gz);
+    int ix = bin_f(d2f_pos(x), M.igwf[0], M.gx);
+    int iy = bin_f(d2f_pos(y), M.igwf[1], M.gy);
+    int iz = bin_f(d2f_pos(z), M.igwf[2], M.gz);
     int ip = bin_f(phi, M.igwf[3], M.gphi);
     int it = bin_f(theta, M.igwf[4], M.gtheta);
     cell = (uint32_t)((ix * M.gy + iy) * M.gz + iz);
@@ -92,19 +122,34 @@ __device__ __forceinline__ void philox_noise_f(unsigned long long seed, uint32_t
     }
 }
 
+// One row of the FP32 field table: the first 16 floats (u, W, E, the
+// diffusion length, mdd B) are read with four 16-byte loads when the row is
+// opened; the dipolar gradient (floats 16-24 of a 32-float row) on demand.
 struct TableFieldsF {
     const float *r;
-    __device__ float flow(int k) const { return r[T_U + k]; }
-    __device__ float diff() const { return r[T_DIFF]; }
-    __device__ float b(int k) const { return r[T_B + k]; }
+    float v[16];
+    __device__ __forceinline__ explicit TableFieldsF(const float *row) : r(row) {
+        const float4 *q = reinterpret_cast<const float4 *>(row);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float4 t = __ldg(q + k);
+            v[4 * k] = t.x;
+            v[4 * k + 1] = t.y;
+            v[4 * k + 2] = t.z;
+            v[4 * k + 3] = t.w;
+        }
+    }
+    __device__ float flow(int k) const { return v[T_U + k]; }
+    __device__ float diff() const { return v[T_DIFF]; }
+    __device__ float b(int k) const { return v[T_B + k]; }
     __device__ void vort_dot(const float n[3], float f[3]) const {
-        float w01 = r[T_W01], w02 = r[T_W02], w12 = r[T_W12];
+        float w01 = v[T_W01], w02 = v[T_W02], w12 = v[T_W12];
         f[0] = w01 * n[1] + w02 * n[2];
         f[1] = -w01 * n[0] + w12 * n[2];
         f[2] = -w02 * n[0] - w12 * n[1];
     }
     __device__ void strain_dot(const float n[3], float f[3]) const {
-        float e00 = r[T_E00], e01 = r[T_E01], e02 = r[T_E02], e11 = r[T_E11], e12 = r[T_E12], e22 = r[T_E22];
+        float e00 = v[T_E00], e01 = v[T_E01], e02 = v[T_E02], e11 = v[T_E11], e12 = v[T_E12], e22 = v[T_E22];
         f[0] = e00 * n[0] + e01 * n[1] + e02 * n[2];
         f[1] = e01 * n[0] + e11 * n[1] + e12 * n[2];
         f[2] = e02 * n[0] + e12 * n[1] + e22 * n[2];
@@ -204,9 +249,9 @@ __device__ __forceinline__ void langevin_mixed(float &phi, float &theta, float s
 // src/particle.rs:26-35 with 2L precomputed).  From an interior cell a step
 // shorter than one cell cannot leave the box, so only particles in the first
 // or last cell of the axis, or with long steps, pay for the wrap tests.
-__device__ __forceinline__ double advance64(double x, float dx, int cell, int n, float w, double L, double L2) {
-    double xn = x + (double)dx;
-    if (cell > 0 && cell < n - 1 && fabsf(dx) < w) return xn;
+// The wrap is a called function so that the compiler does not evaluate its
+// FP64 compares (predicated) for the interior particles too.
+static __device__ __noinline__ double wrap64(double xn, double L, double L2) {
     if (xn > -L && xn < L2) {
         if (xn >= L) return xn - L;
         if (xn < 0.0) return xn + L;
@@ -214,6 +259,11 @@ __device__ __forceinline__ double advance64(double x, float dx, int cell, int n,
     }
     double r = fmod(xn, L);
     return r < 0.0 ? r + L : r;
+}
+__device__ __forceinline__ double advance64(double x, float dx, int cell, int n, float w, double L, double L2) {
+    const double xn = x + f2d(dx);
+    if (cell > 0 && cell < n - 1 && fabsf(dx) < w) return xn;
+    return wrap64(xn, L, L2);
 }
 
 }  // namespace ss

@@ -119,10 +119,16 @@ class Ensemble:
         check(self.lib.ss_ensemble_init(self._h, p.ctypes.data_as(_dp), p.shape[0]))
 
     def autotune(self):
-        """(threads per block, blocks per SM, particles per work unit) of the update"""
-        cfg = (ctypes.c_uint32 * 3)()
+        """Time the update's launch shapes and keep the fastest; returns
+        (threads per block, blocks per SM, particles per work unit, register plan)."""
+        cfg = (ctypes.c_uint32 * 4)()
         check(self.lib.ss_ensemble_autotune(self._h, cfg))
         return tuple(int(v) for v in cfg)
+
+    def set_config(self, config):
+        """Set the update's launch shape (the 4-tuple autotune returns)."""
+        cfg = (ctypes.c_uint32 * 4)(*[int(v) for v in config])
+        check(self.lib.ss_ensemble_set_config(self._h, cfg))
 
     def run(self, steps):
         check(self.lib.ss_ensemble_run(self._h, int(steps)))

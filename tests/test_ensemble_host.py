@@ -59,6 +59,7 @@ def test_create_rejects_bad_flags_and_sizes():
     # other entry points reject a null ensemble
     assert L.ss_ensemble_run(None, 1) == _lib.SS_ERR_INVALID_ARGUMENT
     assert L.ss_ensemble_autotune(None, None) == _lib.SS_ERR_INVALID_ARGUMENT
+    assert L.ss_ensemble_set_config(None, None) == _lib.SS_ERR_INVALID_ARGUMENT
     assert L.ss_ensemble_info(None, None, None, None) == _lib.SS_ERR_INVALID_ARGUMENT
     assert L.ss_ensemble_destroy(None) == _lib.SS_OK
 

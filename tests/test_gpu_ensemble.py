@@ -105,13 +105,15 @@ def test_ensemble_deterministic_and_autotune_leaves_state():
     a = ss.Ensemble(members)
     a.init(rows)
     before = [a.get_particles(i) for i in range(len(members))]
-    threads, bps, unit = a.autotune()
-    assert threads in (128, 256, 512) and bps in (2, 4, 8) and unit in (4096, 16384, 65536)
+    threads, bps, unit, plan = a.autotune()
+    assert threads in (128, 256, 512) and bps in (2, 4, 8) and unit in (4096, 16384, 65536) and plan in (1, 2, 3)
     for i in range(len(members)):
         assert np.array_equal(a.get_particles(i), before[i])
     a.run(3)
+    # another launch shape gives the same trajectory, bit for bit
     b = ss.Ensemble(members)
     b.init(rows)
+    b.set_config((128, 2, 4096, 3) if plan != 3 else (512, 8, 65536, 1))
     b.run(3)
     for i in range(len(members)):
         assert np.array_equal(a.get_particles(i), b.get_particles(i))
