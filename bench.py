@@ -46,6 +46,21 @@ def c1_particles(n, seed=1):
                             np.full(n, np.pi / 2)])
 
 
+def traffic_per_launch(key, n):
+    """DRAM bytes per launch of a kernel at n particles, from the ncu
+    figures in profiles/traffic.txt (bytes per particle, measured on a smaller
+    case of the same workload); None when absent."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.txt")) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 2 and parts[0] == key:
+                    return float(parts[1]) * n
+    except OSError:
+        pass
+    return None
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -238,8 +253,21 @@ def measure_mixed(args, stream, p0, rank, world, dist, barrier, mode=True):
     m.close()
     d.close()
     dtype = "f32 + 64-bit fixed-point positions" if mode == "fixed64" else "f32 + f64 positions"
+    stage = {k: v / max(1, nprof) for k, v in stage_ms.items()}
+    # k_update_m, algorithmic bytes per launch: x, y (8 B each), phi and the
+    # cell key (4 B each) read and written; the table (16 floats per cell)
+    # and the next histogram once
+    gx, gy, gz, gp, gt = GRID
+    upd_bytes = N * 48 + gx * gy * gz * 16 * 4 + gx * gy * gz * gp * gt * 4
+    peak, peak_kind = peaks()
+    achieved = upd_bytes / (stage["update"] / 1e3) / 1e9
+    key = "k_update_m_fixed64_c1" if mode == "fixed64" else "k_update_m_c1"
     return {"value": value, "unit": UNIT, "ms_per_step": ms_max / args.steps, "dtype": dtype,
-            "stage_ms": {k: v / max(1, nprof) for k, v in stage_ms.items()},
+            "stage_ms": stage,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic_per_launch(key, N),
+                         "kernel": "k_update_m", "peak_source": peak_kind, "bytes_per_launch": upd_bytes,
+                         "avg_launch_ms": stage["update"]},
             "errors_vs_fp64_one_step": errors}
 
 
@@ -253,13 +281,17 @@ def measure_ensemble(args, stream, rank, world, dist, barrier):
 
     import stochasticsampling_gb300 as ss
     from stochasticsampling_gb300.ensemble import parameter_scan, uniform_particles
-    members = parameter_scan(64, seed=1 + rank)
+    members = parameter_scan(args.ensemble_members, seed=1 + rank)
     rows = uniform_particles(members, seed=2 + rank)
     ntot = int(rows.shape[0])
     ens = ss.Ensemble(members, stream=stream.cuda_stream)
     ens.init(rows)
     t0 = time.perf_counter()
-    cfg = ens.autotune()
+    if args.ensemble_config:
+        cfg = tuple(int(v) for v in args.ensemble_config.split(","))
+        ens.set_config(cfg)
+    else:
+        cfg = ens.autotune()
     tune_s = time.perf_counter() - t0
     steps = args.steps
     with torch.cuda.stream(stream):
@@ -333,12 +365,22 @@ def run_gpu(args, rank, world, dist):
     stream = torch.cuda.Stream()
     params = dict(PARAMS, number_of_particles=N, seed=1 + rank)
     p0 = c1_particles(N, seed=1 + rank)
-    sim = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True, stream=stream.cuda_stream)
-    sim.init(p0)
 
     def barrier():
         if dist is not None:
             dist.barrier()
+
+    if args.only:
+        if args.only == "ensemble":
+            res = measure_ensemble(args, stream, rank, world, dist, barrier)
+        else:
+            res = measure_mixed(args, stream, p0, rank, world, dist, barrier,
+                                "fixed64" if args.only == "fixed64" else True)
+        if rank == 0:
+            print(json.dumps({"section": args.only, **res}), flush=True)
+        return
+    sim = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True, stream=stream.cuda_stream)
+    sim.init(p0)
 
     with torch.cuda.stream(stream):
         sim.run(args.warmup)
@@ -405,12 +447,7 @@ def run_gpu(args, rank, world, dist):
     # whole step, SURVEY-style algorithmic bytes: particles 80 B, histogram 12 B
     # per bin, 21 FFT components read+written as 16 B complex, field table
     step_bytes = N * 80 + nbins * 12 + ncell * 16 * 2 * 21 + ncell * 13 * 8
-    traffic = None
-    try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get("k_update_c1_bytes_per_launch")
-    except Exception:
-        pass
+    traffic = traffic_per_launch("k_update_c1", N)
     cpu = None
     if not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
@@ -459,6 +496,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32 mixed-precision measurement")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--only", choices=["mixed", "fixed64", "ensemble"], default=None,
+                    help="run one section alone (a smaller command for profiling); prints its JSON")
+    ap.add_argument("--ensemble-members", type=int, default=64)
+    ap.add_argument("--ensemble-config", default=None,
+                    help="threads,blocks_per_sm,unit,plan of the ensemble update instead of autotuning")
     ap.add_argument("--particles", type=int, default=None,
                     help="override N (profiling a smaller case of the same workload)")
     args = ap.parse_args()
