@@ -76,6 +76,7 @@ struct DevParams {
     double cos_half_pi, sin_half_pi;  // cos/sin of kPiHalf as evaluated on this device
     unsigned long long seed;
     int quasi2d;
+    int bin_theta_half;  // the theta bin of pi/2 (every particle after a quasi2d step)
     int gather;        // 0 nearest cell, 1 trilinear, 2 trilinear with the z fraction from y
     uint32_t mask;     // Langevin modifiers that can change the state
 };
@@ -107,6 +108,60 @@ __device__ __forceinline__ void ref_ang_pbc(double &phi, double &theta) {
     }
 }
 
+// ---- FP64 <-> FP32 and floor in integer arithmetic ---------------------
+// GB300 executes FP64 at 2 operations per clock per SM (FP32: 128), and a
+// conversion, floor or compare occupies the FP64 pipe like an add; the
+// integer pipes are many times wider.
+//
+// d2f_pos: the float nearest a double d (ties to even), the same as
+// (float)d for d >= 2^-126; 0 for smaller or negative d.
+__device__ __forceinline__ float d2f_pos(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const uint32_t e = (uint32_t)(b >> 52);  // biased exponent; >= 2048 when negative
+    if (e < 1023u - 126u || e >= 2048u) return 0.0f;
+    uint32_t f = ((e - 896u) << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu);
+    const uint32_t rest = (uint32_t)b & 0x1FFFFFFFu;  // the 29 bits rounded off
+    if (rest > 0x10000000u || (rest == 0x10000000u && (f & 1u))) f += 1u;
+    return __uint_as_float(f);
+}
+// d2f: as (float)d for |d| >= 2^-126 or d == 0 (round to nearest is symmetric)
+__device__ __forceinline__ float d2f(double d) {
+    const long long b = __double_as_longlong(d);
+    const float m = d2f_pos(__longlong_as_double(b & 0x7FFFFFFFFFFFFFFFll));
+    return (b < 0) ? -m : m;
+}
+// f2d: the exact double of a float (zero, subnormals, inf and nan through
+// the conversion instruction)
+__device__ __forceinline__ double f2d(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xFFu;
+    if (e == 0u || e == 0xFFu) return (double)f;
+    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                 ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
+    return __longlong_as_double((long long)b);
+}
+// For 0 <= q < 2^31: fl = floor(q), and near = q lies within 2^-20 of an
+// integer (fr = q - floor(q) < 2^-20 or fr > 1 - 2^-20), from q's bits.
+// Returns false for other q (negative, -0.0, NaN, large).
+__device__ __forceinline__ bool floor_near(double q, int &fl, bool &near) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(q);
+    if (b >> 63) return false;
+    const int e = (int)(b >> 52) - 1023;
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    if (e < 0) {  // [0, 1): floor 0; near 0 below 2^-20, near 1 above 1 - 2^-20
+        fl = 0;
+        near = e < -20 || (e == -1 && m > 0xFFFFFFFFFFFFFull - 0x1FFFFFFFFull);
+        return true;
+    }
+    if (e >= 31) return false;
+    const unsigned long long mant = m | (1ull << 52);
+    const int shift = 52 - e;  // 22 .. 52
+    fl = (int)(mant >> shift);
+    const unsigned long long frac = mant & ((1ull << shift) - 1ull), tol = 1ull << (shift - 20);
+    near = frac < tol || frac > (1ull << shift) - tol;
+    return true;
+}
+
 // floor(v / w) as usize with the `== n -> n-1` clamp of
 // Distribution::coord_to_grid (distribution/mod.rs:112-137) and
 // get_cell_index (mesh/mod.rs:49-63).  v * (1/w) is within two ulps of the
@@ -116,6 +171,17 @@ __device__ __forceinline__ void ref_ang_pbc(double &phi, double &theta) {
 // flagged.
 __device__ __forceinline__ int ref_bin(double v, double w, double iw, int n, uint32_t &err) {
     double q = v * iw;
+    {
+        int fl;
+        bool near;
+        if (floor_near(q, fl, near) && !near) {  // the common case, without FP64 compares
+            if (fl >= n) {
+                if (fl > n) err |= ERR_BIN_RANGE;
+                return n - 1;
+            }
+            return fl;
+        }
+    }
     double f = floor(q);
     double fr = q - f;
     if (fr < 0x1p-20 || fr > 1.0 - 0x1p-20) f = floor(v / w);
@@ -159,7 +225,9 @@ __device__ __forceinline__ double u12(uint32_t hi, uint32_t lo) {
 // are exact in FP64; log1p takes -U below U = 1/2 (the radius near 0), log
 // takes 1 - U above it (the tail, down to 1 - U = 2^-52).
 __device__ __forceinline__ float neg2log1m(double x) {
-    const float l = (x < 1.5) ? log1pf((float)(1.0 - x)) : logf((float)(2.0 - x));
+    // x < 1.5 <=> the top mantissa bit of x in [1, 2) is clear
+    const bool low = ((__double_as_longlong(x) >> 51) & 1) == 0;
+    const float l = low ? log1pf(d2f(1.0 - x)) : logf(d2f_pos(2.0 - x));
     return -2.0f * l;
 }
 
@@ -188,23 +256,23 @@ __device__ __forceinline__ void philox_noise(unsigned long long seed, uint32_t i
     const float rad = sqrtf(neg2log1m(u12(r0.x, r0.y)));
     float s, c;
     sincospif(2.0f * (float)(r0.z >> 8) * 0x1p-24f, &s, &c);
-    xi[0] = (double)(rad * c);
-    xi[1] = (double)(rad * s);
+    xi[0] = f2d(rad * c);
+    xi[1] = f2d(rad * s);
     if (Q2D) {
         xi[2] = 0.0;  // overwritten position z: never read
     } else {
         uint4 r2 = philox4x32_10(make_uint4(id, tl, th, 2u), key);
         const float rad2 = sqrtf(neg2log1m(u12(r2.x, r2.y)));
-        xi[2] = (double)(rad2 * cospif(2.0f * (float)(r2.z >> 8) * 0x1p-24f));
+        xi[2] = f2d(rad2 * cospif(2.0f * (float)(r2.z >> 8) * 0x1p-24f));
     }
     float saf, caf;
     sincospif(2.0f * (float)(r1.x >> 8) * 0x1p-24f, &saf, &caf);
-    const double c0 = (double)caf, s0 = (double)saf;
+    const double c0 = f2d(caf), s0 = f2d(saf);
     const double d = fma(c0, c0, fma(s0, s0, -1.0));        // |c0, s0|^2 - 1
     const double inv = fma(d, fma(0.375, d, -0.5), 1.0);     // 1 / sqrt(1 + d)
     ca = c0 * inv;
     sa = s0 * inv;
-    rot = sigma * (double)sqrtf(neg2log1m(u12(r1.z, r1.w)));
+    rot = sigma * f2d(sqrtf(neg2log1m(u12(r1.z, r1.w))));
     if (WANT_ALPHA) {
         double a = atan2(sa, ca);
         *alpha = a < 0.0 ? a + kTwoPi : a;

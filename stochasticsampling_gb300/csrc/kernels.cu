@@ -71,14 +71,17 @@ __global__ void k_egest(unsigned long long n, const double *__restrict__ x, cons
     p[0] = x[i]; p[1] = y[i]; p[2] = z[i]; p[3] = phi[i]; p[4] = theta[i];
 }
 
+// CANON: z == 0 and theta == pi/2 (every particle after a quasi2d step), so
+// their bins are 0 and the precomputed bin of pi/2.
+template <bool CANON = false>
 __device__ __forceinline__ void bin_particle(const DevParams &P, double x, double y, double z, double phi,
                                              double theta, uint32_t &cell, unsigned long long &bin,
                                              uint32_t &err) {
     int ix = ref_bin(x, P.gw[0], P.igw[0], P.gx, err);
     int iy = ref_bin(y, P.gw[1], P.igw[1], P.gy, err);
-    int iz = ref_bin(z, P.gw[2], P.igw[2], P.gz, err);
+    int iz = CANON ? 0 : ref_bin(z, P.gw[2], P.igw[2], P.gz, err);
     int ip = ref_bin(phi, P.gw[3], P.igw[3], P.gphi, err);
-    int it = ref_bin(theta, P.gw[4], P.igw[4], P.gtheta, err);
+    int it = CANON ? P.bin_theta_half : ref_bin(theta, P.gw[4], P.igw[4], P.gtheta, err);
     cell = (uint32_t)((ix * P.gy + iy) * P.gz + iz);
     bin = (unsigned long long)cell * (unsigned long long)P.nang + (unsigned long long)(ip * P.gtheta + it);
 }
@@ -322,7 +325,7 @@ __global__ void __launch_bounds__(256) k_update(DevParams P, double *__restrict_
                   P.by, P.bz, have_theta, P.cos_half_pi, P.sin_half_pi);
     uint32_t err = 0, ncell;
     unsigned long long bin;
-    bin_particle(P, px, py, pz, pph, pth, ncell, bin, err);
+    bin_particle<Q2D>(P, px, py, pz, pph, pth, ncell, bin, err);
     atomicAdd(counts_next + bin, 1u);
     key[i] = ncell;
     x[i] = px; y[i] = py; z[i] = pz; phi[i] = pph; theta[i] = pth;

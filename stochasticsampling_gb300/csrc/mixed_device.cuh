@@ -31,35 +31,7 @@ __device__ __forceinline__ float modulo_f(float f, float m) {
     return r < 0.0f ? r + fabsf(m) : r;
 }
 
-// FP64 <-> FP32 conversions in integer arithmetic.  This GPU's FP64 pipe
-// issues about one instruction per clock per SM and a conversion occupies it
-// like an FP64 add, while the integer pipes are many times wider; the
-// mixed step converts every position for binning and every FP32 step to
-// FP64 for the position update.
-//
-// d2f_pos: the float nearest a position d (ties to even), the same as
-// (float)d for d >= 2^-126; 0 for smaller or negative d (which bin to cell 0
-// either way).
-__device__ __forceinline__ float d2f_pos(double d) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-    const uint32_t e = (uint32_t)(b >> 52);  // biased exponent; >= 2048 when negative
-    if (e < 1023u - 126u || e >= 2048u) return 0.0f;
-    uint32_t f = ((e - 896u) << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu);
-    const uint32_t rest = (uint32_t)b & 0x1FFFFFFFu;  // the 29 bits rounded off
-    if (rest > 0x10000000u || (rest == 0x10000000u && (f & 1u))) f += 1u;
-    return __uint_as_float(f);
-}
-
-// f2d: the exact double of a float (zero, subnormals, inf and nan through
-// the conversion instruction)
-__device__ __forceinline__ double f2d(float f) {
-    const uint32_t u = __float_as_uint(f);
-    const uint32_t e = (u >> 23) & 0xFFu;
-    if (e == 0u || e == 0xFFu) return (double)f;
-    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
-                                 ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
-    return __longlong_as_double((long long)b);
-}
+// (d2f_pos and f2d, the integer-pipe conversions, are in common.cuh)
 
 __device__ __forceinline__ void bin_mixed(const MixedParams &M, double x, double y, double z, float phi, float theta,
                                           uint32_t &cell, unsigned long long &bin) {

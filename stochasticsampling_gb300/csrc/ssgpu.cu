@@ -575,6 +575,10 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     P.sigma_rot = std::sqrt(2. * params->rot_diffusion * params->timestep);
     P.seed = params->seed;
     P.quasi2d = c->q2d ? 1 : 0;
+    {  // floor((pi/2) / gw_theta) with the n -> n-1 clamp: the bin ref_bin gives pi/2
+        const double f = std::floor(kPiHalf / P.gw[4]);
+        P.bin_theta_half = f >= (double)P.gtheta ? P.gtheta - 1 : (int)f;
+    }
     P.gather = (flags & SS_FLAG_TRILINEAR_ZFROMY) ? 2 : (flags & SS_FLAG_TRILINEAR) ? 1 : 0;
     uint32_t mask = M_ALL;
     if (params->magnetic_reorientation == 0.0) mask &= ~M_EXTERNAL_FIELD;
