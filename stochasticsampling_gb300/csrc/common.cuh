@@ -86,10 +86,21 @@ struct DevParams {
 // modulo, src/particle.rs:26-35.  fmod(x, m) is exact; for x in (-m, 2m) it
 // equals x, x - m (exact by Sterbenz) or x (then + m), so the fast path gives
 // the identical double without the fmod loop.
+// Doubles as ordered 64-bit integers: sign-magnitude mapped to two's
+// complement, so key(a) < key(b) <=> a < b for non-NaN a, b, and
+// key(-0.0) == key(+0.0).  (Compares on the integer pipe; see d2f_pos.)
+__device__ __forceinline__ long long dkey(double d) {
+    const long long b = __double_as_longlong(d);
+    return b < 0 ? -(b & 0x7FFFFFFFFFFFFFFFll) : b;
+}
+
 __device__ __forceinline__ double ref_modulo(double f, double m) {
-    if (f > -m && f < 2.0 * m) {
-        if (f >= m) return f - m;
-        if (f < 0.0) return f + m;
+    // m > 0 finite (box sizes, 2 pi); a NaN f fails both range tests and
+    // goes through fmod as in the IEEE form of these compares
+    const long long kf = dkey(f), km = dkey(m);
+    if (kf > -km && kf < km + (1ll << 52)) {  // key(2 m): the exponent of m plus one
+        if (kf >= km) return f - m;
+        if (kf < 0) return f + m;
         return f;
     }
     double r = fmod(f, m);
@@ -431,7 +442,7 @@ __device__ __forceinline__ void langevin(double &x, double &y, double &z, double
     // CosSinOrientation::to_orientation_vector, particle.rs:165-172
     // (with sin(theta) == 1 exactly, the products are cp and sp exactly)
     double n[3] = {st * cp, st * sp, ct};
-    if (have_theta && st == 1.0) {
+    if (have_theta && __double_as_longlong(st) == __double_as_longlong(1.0)) {
         n[0] = cp;
         n[1] = sp;
     }

@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(256) k_update(DevParams P, double *__restrict_
         sincos(r[3], &sa, &ca);
         rot = r[4];
     }
-    bool have_theta = Q2D && (pth == kPiHalf);
+    bool have_theta = Q2D && (__double_as_longlong(pth) == __double_as_longlong(kPiHalf));
     langevin<Q2D>(px, py, pz, pph, pth, F, xi, ca, sa, rot, P.mask, P.dt, P.reorient, P.shape, P.drag, P.bx,
                   P.by, P.bz, have_theta, P.cos_half_pi, P.sin_half_pi);
     uint32_t err = 0, ncell;
