@@ -269,6 +269,19 @@ int ss_ensemble_get_flow_field(ss_ens *ens, uint32_t member, double *out);
 /* total particles, grid-shape groups and kernel launches so far (each optional) */
 int ss_ensemble_info(ss_ens *ens, uint64_t *particles, uint32_t *groups, uint64_t *launches);
 
+/* ---- learned histogram denoiser ------------------------------------------
+ * One 3x3x3 periodic convolution of 32 -> 32 channels on the tensor cores
+ * (tcgen05, BF16 operands, FP32 accumulation): the building block of the
+ * denoiser, exposed for tests.  x: DEVICE bf16 [nx][ny][np][32] (channels
+ * last); w: DEVICE float [27][32 out][32 in], tap = 9 (dx+1) + 3 (dy+1) +
+ * (dp+1) (the torch conv3d weight [out][in][dx+1][dy+1][dp+1] reordered);
+ * bias: DEVICE float[32].  mode 0: y = bf16 ReLU(conv(x) + bias); mode 1:
+ * y = float conv(x) + bias; mode 2: y = bf16 conv^T(x) * (ref > 0), the
+ * backward-data step through a ReLU (ref: DEVICE bf16, bias unused).
+ * nx ny np must be a positive multiple of 128.  Returns after completion. */
+int ss_dn_conv32(const void *x, const float *w, const float *bias, const void *ref, void *y, uint32_t nx,
+                 uint32_t ny, uint32_t np, uint32_t mode, void *stream);
+
 /* copy the last error message of ctx (or the last context-free error when
  * ctx is NULL) into buf, NUL terminated */
 int ss_last_error(ss_ctx *ctx, char *buf, size_t len);
