@@ -282,6 +282,34 @@ int ss_ensemble_info(ss_ens *ens, uint64_t *particles, uint32_t *groups, uint64_
 int ss_dn_conv32(const void *x, const float *w, const float *bias, const void *ref, void *y, uint32_t nx,
                  uint32_t ny, uint32_t np, uint32_t mode, void *stream);
 
+/* The denoiser network: input x (the histogram divided by its mean count,
+ * DEVICE float [nx][ny][np]) -> conv 1->32 + ReLU -> conv 32->32 + ReLU ->
+ * conv 32->32 + ReLU -> conv 32->1 -> y = x + that (DEVICE float).  All
+ * convolutions 3x3x3 with periodic padding; the 32->32 ones on the tensor
+ * cores (BF16 weights and activations, FP32 accumulation), the others on the
+ * CUDA cores in FP32.  57,121 FP32 parameters: w_in[27][32], b_in[32],
+ * w2[27][32][32], b2[32], w3[27][32][32], b3[32], w_out[27][32], b_out
+ * (w[tap][out][in], tap as for ss_dn_conv32).  Trained with Adam on the
+ * mean-square error against a target distribution. */
+typedef struct ss_dn ss_dn;
+/* He-initialised from seed (the output layer near zero: y ~ x at start);
+ * nx ny np a positive multiple of 128.  stream as in ss_create. */
+int ss_dn_create(uint32_t nx, uint32_t ny, uint32_t np, uint64_t seed, void *stream, ss_dn **out);
+int ss_dn_destroy(ss_dn *dn);
+/* parameter count (57121) and kernel launches so far (each optional) */
+int ss_dn_info(ss_dn *dn, uint64_t *nparams, uint64_t *launches);
+int ss_dn_get_params(ss_dn *dn, float *host, uint64_t count);
+int ss_dn_set_params(ss_dn *dn, const float *host, uint64_t count);
+/* y = network(x), DEVICE arrays; returns after completion */
+int ss_dn_forward(ss_dn *dn, const float *x, float *y);
+/* batch samples x[batch][V], t[batch][V] (DEVICE): loss = mean over the batch
+ * of mean_v (y - t)^2; with lr > 0 one Adam step (beta 0.9 / 0.999) on the
+ * batch-mean gradient, with lr = 0 the loss only */
+int ss_dn_train(ss_dn *dn, const float *x, const float *t, uint32_t batch, float lr, double *loss);
+/* the batch-mean gradient of that loss (host float[count]) without an update */
+int ss_dn_gradients(ss_dn *dn, const float *x, const float *t, uint32_t batch, float *grads, uint64_t count,
+                    double *loss);
+
 /* copy the last error message of ctx (or the last context-free error when
  * ctx is NULL) into buf, NUL terminated */
 int ss_last_error(ss_ctx *ctx, char *buf, size_t len);

@@ -17,8 +17,9 @@ EXPORTS = [
     "ss_mean_magnetic_field", "ss_langevin", "ss_profile_enable", "ss_profile_read", "ss_launch_count",
     "ss_sample_distribution_noalloc", "ss_ensemble_create", "ss_ensemble_destroy", "ss_ensemble_init",
     "ss_ensemble_autotune", "ss_ensemble_set_config", "ss_ensemble_run", "ss_ensemble_synchronize", "ss_ensemble_get_particles",
-    "ss_ensemble_get_counts", "ss_ensemble_get_flow_field", "ss_ensemble_info", "ss_dn_conv32", "ss_last_error",
-    "ss_version",
+    "ss_ensemble_get_counts", "ss_ensemble_get_flow_field", "ss_ensemble_info", "ss_dn_conv32", "ss_dn_create",
+    "ss_dn_destroy", "ss_dn_info", "ss_dn_get_params", "ss_dn_set_params", "ss_dn_forward", "ss_dn_train",
+    "ss_dn_gradients", "ss_last_error", "ss_version",
 ]
 
 SS_OK = 0
@@ -137,6 +138,14 @@ def load(build_if_missing=True):
         "ss_ensemble_get_flow_field": [vp, u32, dp],
         "ss_ensemble_info": [vp, u64p, ctypes.POINTER(ctypes.c_uint32), u64p],
         "ss_dn_conv32": [vp, vp, vp, vp, vp, u32, u32, u32, u32, vp],
+        "ss_dn_create": [u32, u32, u32, u64, vp, ctypes.POINTER(vp)],
+        "ss_dn_destroy": [vp],
+        "ss_dn_info": [vp, u64p, u64p],
+        "ss_dn_get_params": [vp, ctypes.POINTER(ctypes.c_float), u64],
+        "ss_dn_set_params": [vp, ctypes.POINTER(ctypes.c_float), u64],
+        "ss_dn_forward": [vp, vp, vp],
+        "ss_dn_train": [vp, vp, vp, u32, ctypes.c_float, dp],
+        "ss_dn_gradients": [vp, vp, vp, u32, ctypes.POINTER(ctypes.c_float), u64, dp],
         "ss_last_error": [vp, ctypes.c_char_p, ctypes.c_size_t],
     }
     for name, args in sig.items():

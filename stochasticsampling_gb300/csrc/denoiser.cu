@@ -24,8 +24,13 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <cmath>
+#include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <random>
+#include <string>
+#include <vector>
 
 #include "../../include/ssgpu.h"
 
@@ -286,6 +291,246 @@ __global__ void k_pack_weights(const float *__restrict__ W, uint8_t *__restrict_
 
 int g_sms = 0;
 
+// ---- the network's CUDA-core layers -----------------------------------
+// Parameters (FP32, one array): w_in[27][32], b_in[32], w2[27][32][32],
+// b2[32], w3[27][32][32], b3[32], w_out[27][32], b_out.
+constexpr int kOffWin = 0, kOffBin = kOffWin + kTaps * kC, kOffW2 = kOffBin + kC, kOffB2 = kOffW2 + kTaps * kC * kC,
+              kOffW3 = kOffB2 + kC, kOffB3 = kOffW3 + kTaps * kC * kC, kOffWout = kOffB3 + kC,
+              kOffBout = kOffWout + kTaps * kC, kParams = kOffBout + 1;
+
+__device__ __forceinline__ void store_bf16x32(__nv_bfloat16 *dst, const float (&a)[32]) {
+    uint32_t q[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        __nv_bfloat162 h = __floats2bfloat162_rn(a[2 * i], a[2 * i + 1]);
+        q[i] = *reinterpret_cast<uint32_t *>(&h);
+    }
+    uint4 *o = reinterpret_cast<uint4 *>(dst);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) o[i] = make_uint4(q[4 * i], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]);
+}
+__device__ __forceinline__ void load_bf16x32(const __nv_bfloat16 *src, float (&a)[32]) {
+    const uint4 *s = reinterpret_cast<const uint4 *>(src);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const uint4 u = s[i];
+        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162 *>(&w[j]);
+            a[8 * i + 2 * j] = __low2float(h);
+            a[8 * i + 2 * j + 1] = __high2float(h);
+        }
+    }
+}
+
+// input layer 1 -> 32 channels, ReLU: A1[v] = ReLU(b_in + sum_tap w_in[tap] x[nbr(v, tap)])
+__global__ void __launch_bounds__(128) k_dn_in(const float *__restrict__ x, const float *__restrict__ P,
+                                               __nv_bfloat16 *__restrict__ A1, Dims d, int nvox) {
+    __shared__ float sw[kTaps * kC + kC];
+    for (int i = threadIdx.x; i < kTaps * kC + kC; i += blockDim.x) sw[i] = P[kOffWin + i];
+    __syncthreads();
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nvox) return;
+    const Voxel vx(v, d);
+    float a[32];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) a[c] = sw[kTaps * kC + c];
+    for (int t = 0; t < kTaps; ++t) {
+        const float xv = x[vx.neighbour(t, d)];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) a[c] = fmaf(sw[t * kC + c], xv, a[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < kC; ++c) a[c] = fmaxf(a[c], 0.f);
+    store_bf16x32(A1 + (size_t)v * kC, a);
+}
+
+// output layer 32 -> 1 with the residual: y[v] = x[v] + b_out + sum_tap w_out[tap] . A3[nbr(v, tap)]
+__global__ void __launch_bounds__(128) k_dn_out(const __nv_bfloat16 *__restrict__ A3, const float *__restrict__ x,
+                                                const float *__restrict__ P, float *__restrict__ y, Dims d, int nvox) {
+    __shared__ float sw[kTaps * kC + 1];
+    for (int i = threadIdx.x; i < kTaps * kC + 1; i += blockDim.x) sw[i] = P[kOffWout + i];
+    __syncthreads();
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nvox) return;
+    const Voxel vx(v, d);
+    float acc = sw[kTaps * kC];
+    for (int t = 0; t < kTaps; ++t) {
+        float a[32];
+        load_bf16x32(A3 + (size_t)vx.neighbour(t, d) * kC, a);
+#pragma unroll
+        for (int c = 0; c < kC; ++c) acc = fmaf(sw[t * kC + c], a[c], acc);
+    }
+    y[v] = x[v] + acc;
+}
+
+// mean-square loss against the target and its gradient dy = 2 (y - t) / V;
+// sums (y - t)^2 / V and dy (the output bias gradient) in FP64
+__global__ void k_dn_loss(const float *__restrict__ y, const float *__restrict__ t, float *__restrict__ dy, int nvox,
+                          double *__restrict__ sums, float *__restrict__ db_out) {
+    double l = 0.0, g = 0.0;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += gridDim.x * blockDim.x) {
+        const float r = y[v] - t[v];
+        const float gv = 2.f * r / (float)nvox;
+        dy[v] = gv;
+        l += (double)(r * r);
+        g += (double)gv;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        l += __shfl_xor_sync(0xffffffffu, l, o);
+        g += __shfl_xor_sync(0xffffffffu, g, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&sums[0], l / (double)nvox);
+        if (db_out) atomicAdd(db_out, (float)g);
+    }
+}
+
+// backward of the output layer into its input: dZ3[u][c] = (sum_tap
+// w_out[tap][c] dy[nbr(u, 26 - tap)]) * (A3[u][c] > 0)
+__global__ void __launch_bounds__(128) k_dn_out_bwd(const float *__restrict__ dy, const float *__restrict__ P,
+                                                    const __nv_bfloat16 *__restrict__ A3,
+                                                    __nv_bfloat16 *__restrict__ dZ3, Dims d, int nvox) {
+    __shared__ float sw[kTaps * kC];
+    for (int i = threadIdx.x; i < kTaps * kC; i += blockDim.x) sw[i] = P[kOffWout + i];
+    __syncthreads();
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nvox) return;
+    const Voxel vx(u, d);
+    float g[32];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) g[c] = 0.f;
+    for (int t = 0; t < kTaps; ++t) {
+        const float dv = dy[vx.neighbour(kTaps - 1 - t, d)];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) g[c] = fmaf(sw[t * kC + c], dv, g[c]);
+    }
+    float a[32];
+    load_bf16x32(A3 + (size_t)u * kC, a);
+#pragma unroll
+    for (int c = 0; c < kC; ++c) g[c] = a[c] > 0.f ? g[c] : 0.f;
+    store_bf16x32(dZ3 + (size_t)u * kC, g);
+}
+
+// weight gradient of a 1-channel side: dW[tap][c] = sum_v S[v][c] * s[nbr(v, tap)]
+// (input layer: S = dZ1, s = x) or sum_v s[v] * S[nbr(v, tap)][c] (output
+// layer: S = A3, s = dy).  Grid (27 taps, blocks); 8 voxel lanes x 32 channels.
+template <bool OUT>
+__global__ void __launch_bounds__(256) k_dn_wgrad_c1(const __nv_bfloat16 *__restrict__ S, const float *__restrict__ sv,
+                                                     float *__restrict__ dW, Dims d, int nvox) {
+    __shared__ float red[8][kC];
+    const int tap = blockIdx.x, c = threadIdx.x & 31, lane8 = threadIdx.x >> 5;
+    float acc = 0.f;
+    for (int v = blockIdx.y * 8 + lane8; v < nvox; v += gridDim.y * 8) {
+        const int u = Voxel(v, d).neighbour(tap, d);
+        if (OUT) acc = fmaf(sv[v], __bfloat162float(S[(size_t)u * kC + c]), acc);
+        else acc = fmaf(__bfloat162float(S[(size_t)v * kC + c]), sv[u], acc);
+    }
+    red[lane8][c] = acc;
+    __syncthreads();
+    if (threadIdx.x < kC) {
+        float s = 0.f;
+        for (int i = 0; i < 8; ++i) s += red[i][threadIdx.x];
+        atomicAdd(&dW[tap * kC + threadIdx.x], s);
+    }
+}
+
+// bias gradient db[c] = sum_v D[v][c]
+__global__ void __launch_bounds__(256) k_dn_bgrad(const __nv_bfloat16 *__restrict__ D, float *__restrict__ db,
+                                                  int nvox) {
+    __shared__ float red[8][kC];
+    const int c = threadIdx.x & 31, lane8 = threadIdx.x >> 5;
+    float acc = 0.f;
+    for (int v = blockIdx.x * 8 + lane8; v < nvox; v += gridDim.x * 8) acc += __bfloat162float(D[(size_t)v * kC + c]);
+    red[lane8][c] = acc;
+    __syncthreads();
+    if (threadIdx.x < kC) {
+        float s = 0.f;
+        for (int i = 0; i < 8; ++i) s += red[i][threadIdx.x];
+        atomicAdd(&db[threadIdx.x], s);
+    }
+}
+
+// weight gradient of a 32 -> 32 layer: dW[tap][co][ci] = sum_v dZ[v][co] A[nbr(v, tap)][ci].
+// Grid (27 taps, blocks over voxel tiles of 128).  A tile of dZ and the
+// tap-shifted tile of A are staged in shared memory as FP32; each thread
+// accumulates a 4 x 4 block of (co, ci) over a quarter of the tile's voxels.
+__global__ void __launch_bounds__(256) k_dn_wgrad32(const __nv_bfloat16 *__restrict__ dZ,
+                                                    const __nv_bfloat16 *__restrict__ A, float *__restrict__ dW,
+                                                    Dims d, int ntiles) {
+    __shared__ __align__(16) float sZ[kTileM][kC + 4];
+    __shared__ __align__(16) float sA[kTileM][kC + 4];
+    const int tap = blockIdx.x, tid = threadIdx.x;
+    const int g = tid >> 6, lt = tid & 63, cb = lt >> 3, ib = lt & 7;
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    const int r = tid >> 1, h = tid & 1;
+    for (int tile = blockIdx.y; tile < ntiles; tile += gridDim.y) {
+        const int v = tile * kTileM + r;
+        const int u = Voxel(v, d).neighbour(tap, d);
+        const uint4 *zs = reinterpret_cast<const uint4 *>(dZ + (size_t)v * kC + 16 * h);
+        const uint4 *as = reinterpret_cast<const uint4 *>(A + (size_t)u * kC + 16 * h);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const uint4 zu = zs[q], au = as[q];
+            const uint32_t zw[4] = {zu.x, zu.y, zu.z, zu.w}, aw[4] = {au.x, au.y, au.z, au.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const __nv_bfloat162 zh = *reinterpret_cast<const __nv_bfloat162 *>(&zw[j]);
+                const __nv_bfloat162 ah = *reinterpret_cast<const __nv_bfloat162 *>(&aw[j]);
+                sZ[r][16 * h + 8 * q + 2 * j] = __low2float(zh);
+                sZ[r][16 * h + 8 * q + 2 * j + 1] = __high2float(zh);
+                sA[r][16 * h + 8 * q + 2 * j] = __low2float(ah);
+                sA[r][16 * h + 8 * q + 2 * j + 1] = __high2float(ah);
+            }
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int k = g; k < kTileM; k += 4) {
+            const float4 z = *reinterpret_cast<const float4 *>(&sZ[k][4 * cb]);
+            const float4 a = *reinterpret_cast<const float4 *>(&sA[k][4 * ib]);
+            const float zz[4] = {z.x, z.y, z.z, z.w}, aa[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(zz[i], aa[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+    // the four voxel groups' partial sums, then one atomic per (co, ci)
+    float *red = &sZ[0][0];  // 4 x 64 x 16 floats fit in sZ
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) red[(g * 64 + lt) * 16 + 4 * i + j] = acc[i][j];
+    __syncthreads();
+    for (int o = tid; o < kC * kC; o += blockDim.x) {
+        const int co = o >> 5, ci = o & 31;
+        const int l = (co >> 2) * 8 + (ci >> 2), e = (co & 3) * 4 + (ci & 3);
+        const float s = red[(0 * 64 + l) * 16 + e] + red[(1 * 64 + l) * 16 + e] + red[(2 * 64 + l) * 16 + e] +
+                        red[(3 * 64 + l) * 16 + e];
+        atomicAdd(&dW[(tap * kC + co) * kC + ci], s);
+    }
+}
+
+// Adam (Kingma and Ba, 2015) on the FP32 parameters
+__global__ void k_dn_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+                          float *__restrict__ s, int n, float gscale, float lr, float b1, float b2, float eps, float c1,
+                          float c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i] * gscale;
+    const float mi = b1 * m[i] + (1.f - b1) * gi, si = b2 * s[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    s[i] = si;
+    p[i] -= lr * (mi / c1) / (sqrtf(si / c2) + eps);
+}
+
 }  // namespace
 
 extern "C" int ss_dn_conv32(const void *x, const float *w, const float *bias, const void *ref, void *y,
@@ -342,3 +587,275 @@ extern "C" int ss_dn_conv32(const void *x, const float *w, const float *bias, co
     }
     return SS_OK;
 }
+
+// ---------------------------------------------------------------------------
+// host object
+// ---------------------------------------------------------------------------
+struct ss_dn {
+    Dims d{};
+    int nvox = 0, ntiles = 0, sms = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int device = 0;
+    float *P = nullptr, *G = nullptr, *M = nullptr, *S = nullptr, *dy = nullptr, *yb = nullptr;
+    uint8_t *Wp2 = nullptr, *Wp3 = nullptr, *Wm2 = nullptr, *Wm3 = nullptr;
+    __nv_bfloat16 *A1 = nullptr, *A2 = nullptr, *A3 = nullptr, *D1 = nullptr, *D2 = nullptr;
+    double *sums = nullptr;
+    unsigned *err = nullptr;
+    long long adam_t = 0;
+    uint64_t launches = 0;
+};
+
+namespace {
+
+int dnfail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    ss::record_error(buf);
+    return code;
+}
+#define DCK(call)                                                                                    \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return dnfail(SS_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+void conv_attrs() {
+    static bool done = false;
+    if (done) return;
+    cudaFuncSetAttribute(k_conv32<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
+    cudaFuncSetAttribute(k_conv32<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
+    cudaFuncSetAttribute(k_conv32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
+    done = true;
+}
+
+template <int MODE>
+void launch_conv(ss_dn *n, const __nv_bfloat16 *X, const uint8_t *W, const float *bias, const __nv_bfloat16 *ref,
+                 void *Y, cudaStream_t s) {
+    const int grid = n->ntiles < 2 * n->sms ? n->ntiles : 2 * n->sms;
+    k_conv32<MODE><<<grid, kTileM, kSmemConv, s>>>(X, W, bias, ref, Y, n->d, n->ntiles, n->err);
+}
+
+void pack_all(ss_dn *n, cudaStream_t s) {
+    const int nw = kTaps * kC * kC, b = (nw + 255) / 256;
+    k_pack_weights<false><<<b, 256, 0, s>>>(n->P + kOffW2, n->Wp2);
+    k_pack_weights<false><<<b, 256, 0, s>>>(n->P + kOffW3, n->Wp3);
+    k_pack_weights<true><<<b, 256, 0, s>>>(n->P + kOffW2, n->Wm2);
+    k_pack_weights<true><<<b, 256, 0, s>>>(n->P + kOffW3, n->Wm3);
+    n->launches += 4;
+}
+
+void enqueue_forward(ss_dn *n, const float *x, float *y, cudaStream_t s) {
+    const unsigned b = (unsigned)((n->nvox + 127) / 128);
+    k_dn_in<<<b, 128, 0, s>>>(x, n->P, n->A1, n->d, n->nvox);
+    launch_conv<0>(n, n->A1, n->Wp2, n->P + kOffB2, nullptr, n->A2, s);
+    launch_conv<0>(n, n->A2, n->Wp3, n->P + kOffB3, nullptr, n->A3, s);
+    k_dn_out<<<b, 128, 0, s>>>(n->A3, x, n->P, y, n->d, n->nvox);
+    n->launches += 4;
+}
+
+// loss of y against t, then the gradients of every parameter (accumulated into G)
+void enqueue_backward(ss_dn *n, const float *x, const float *t, const float *y, cudaStream_t s, bool grads) {
+    const unsigned b = (unsigned)((n->nvox + 127) / 128);
+    k_dn_loss<<<2 * n->sms, 256, 0, s>>>(y, t, n->dy, n->nvox, n->sums, grads ? n->G + kOffBout : nullptr);
+    n->launches += 1;
+    if (!grads) return;
+    const dim3 wg(kTaps, (unsigned)(n->sms > 0 ? (4 * n->sms + kTaps - 1) / kTaps : 8));
+    k_dn_out_bwd<<<b, 128, 0, s>>>(n->dy, n->P, n->A3, n->D1, n->d, n->nvox);
+    k_dn_wgrad_c1<true><<<wg, 256, 0, s>>>(n->A3, n->dy, n->G + kOffWout, n->d, n->nvox);
+    k_dn_wgrad32<<<wg, 256, 0, s>>>(n->D1, n->A2, n->G + kOffW3, n->d, n->ntiles);
+    k_dn_bgrad<<<2 * n->sms, 256, 0, s>>>(n->D1, n->G + kOffB3, n->nvox);
+    launch_conv<2>(n, n->D1, n->Wm3, nullptr, n->A2, n->D2, s);
+    k_dn_wgrad32<<<wg, 256, 0, s>>>(n->D2, n->A1, n->G + kOffW2, n->d, n->ntiles);
+    k_dn_bgrad<<<2 * n->sms, 256, 0, s>>>(n->D2, n->G + kOffB2, n->nvox);
+    launch_conv<2>(n, n->D2, n->Wm2, nullptr, n->A1, n->D1, s);
+    k_dn_wgrad_c1<false><<<wg, 256, 0, s>>>(n->D1, x, n->G + kOffWin, n->d, n->nvox);
+    k_dn_bgrad<<<2 * n->sms, 256, 0, s>>>(n->D1, n->G + kOffBin, n->nvox);
+    n->launches += 11;
+}
+
+int check_err(ss_dn *n) {
+    unsigned h = 0;
+    DCK(cudaMemcpyAsync(&h, n->err, sizeof h, cudaMemcpyDeviceToHost, n->stream));
+    DCK(cudaStreamSynchronize(n->stream));
+    if (h) return dnfail(SS_ERR_CUDA, "denoiser: a tensor-core convolution's mbarrier wait timed out");
+    return SS_OK;
+}
+
+void destroy_dn(ss_dn *n) {
+    if (!n) return;
+    cudaSetDevice(n->device);
+    if (n->stream) cudaStreamSynchronize(n->stream);
+    cudaFree(n->P); cudaFree(n->G); cudaFree(n->M); cudaFree(n->S); cudaFree(n->dy); cudaFree(n->yb);
+    cudaFree(n->Wp2); cudaFree(n->Wp3); cudaFree(n->Wm2); cudaFree(n->Wm3);
+    cudaFree(n->A1); cudaFree(n->A2); cudaFree(n->A3); cudaFree(n->D1); cudaFree(n->D2);
+    cudaFree(n->sums); cudaFree(n->err);
+    if (n->own_stream && n->stream) cudaStreamDestroy(n->stream);
+    delete n;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ss_dn_create(uint32_t nx, uint32_t ny, uint32_t np, uint64_t seed, void *stream, ss_dn **out) {
+    if (!out) return dnfail(SS_ERR_INVALID_ARGUMENT, "ss_dn_create: null output");
+    *out = nullptr;
+    const unsigned long long V = (unsigned long long)nx * ny * np;
+    if (nx < 1 || ny < 1 || np < 1 || V % kTileM != 0 || V > (1ull << 27))
+        return dnfail(SS_ERR_INVALID_ARGUMENT,
+                      "ss_dn_create: the voxel count nx ny np must be a positive multiple of 128 (at most 2^27)");
+    ss_dn *n = new ss_dn();
+    n->d = Dims{(int)nx, (int)ny, (int)np};
+    n->nvox = (int)V;
+    n->ntiles = (int)(V / kTileM);
+    cudaError_t e = cudaGetDevice(&n->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&n->sms, cudaDevAttrMultiProcessorCount, n->device);
+    if (e == cudaSuccess) {
+        if (stream) {
+            n->stream = (cudaStream_t)stream;
+        } else {
+            e = cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking);
+            n->own_stream = e == cudaSuccess;
+        }
+    }
+    auto A = [&](void **p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    };
+    const size_t pb = (size_t)kParams * sizeof(float), ab = (size_t)V * kC * sizeof(__nv_bfloat16);
+    A((void **)&n->P, pb); A((void **)&n->G, pb); A((void **)&n->M, pb); A((void **)&n->S, pb);
+    A((void **)&n->dy, V * sizeof(float)); A((void **)&n->yb, V * sizeof(float));
+    A((void **)&n->Wp2, kBAll); A((void **)&n->Wp3, kBAll); A((void **)&n->Wm2, kBAll); A((void **)&n->Wm3, kBAll);
+    A((void **)&n->A1, ab); A((void **)&n->A2, ab); A((void **)&n->A3, ab); A((void **)&n->D1, ab);
+    A((void **)&n->D2, ab);
+    A((void **)&n->sums, 2 * sizeof(double)); A((void **)&n->err, sizeof(unsigned));
+    // He initialisation of the convolutions; the output layer starts near
+    // zero so that the network starts as the identity (residual)
+    std::vector<float> h(kParams, 0.f);
+    std::mt19937_64 rng(seed);
+    std::normal_distribution<float> nd(0.f, 1.f);
+    for (int i = 0; i < kTaps * kC; ++i) h[kOffWin + i] = nd(rng) * std::sqrt(2.f / kTaps);
+    for (int i = 0; i < kTaps * kC * kC; ++i) h[kOffW2 + i] = nd(rng) * std::sqrt(2.f / (kTaps * kC));
+    for (int i = 0; i < kTaps * kC * kC; ++i) h[kOffW3 + i] = nd(rng) * std::sqrt(2.f / (kTaps * kC));
+    for (int i = 0; i < kTaps * kC; ++i) h[kOffWout + i] = nd(rng) * 1e-3f;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(n->P, h.data(), pb, cudaMemcpyHostToDevice, n->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(n->M, 0, pb, n->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(n->S, 0, pb, n->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(n->err, 0, sizeof(unsigned), n->stream);
+    if (e == cudaSuccess) {
+        conv_attrs();
+        pack_all(n, n->stream);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(n->stream);
+    if (e != cudaSuccess) {
+        const std::string m = cudaGetErrorString(e);
+        destroy_dn(n);
+        return dnfail(SS_ERR_CUDA, "ss_dn_create: %s", m.c_str());
+    }
+    *out = n;
+    return SS_OK;
+}
+
+int ss_dn_destroy(ss_dn *n) {
+    destroy_dn(n);
+    return SS_OK;
+}
+
+int ss_dn_info(ss_dn *n, uint64_t *nparams, uint64_t *launches) {
+    if (!n) return dnfail(SS_ERR_INVALID_ARGUMENT, "null denoiser");
+    if (nparams) *nparams = (uint64_t)kParams;
+    if (launches) *launches = n->launches;
+    return SS_OK;
+}
+
+int ss_dn_get_params(ss_dn *n, float *host, uint64_t count) {
+    if (!n || !host || count != (uint64_t)kParams)
+        return dnfail(SS_ERR_INVALID_ARGUMENT, "ss_dn_get_params: null argument or count != %d", kParams);
+    DCK(cudaSetDevice(n->device));
+    DCK(cudaMemcpyAsync(host, n->P, (size_t)kParams * sizeof(float), cudaMemcpyDeviceToHost, n->stream));
+    DCK(cudaStreamSynchronize(n->stream));
+    return SS_OK;
+}
+
+int ss_dn_set_params(ss_dn *n, const float *host, uint64_t count) {
+    if (!n || !host || count != (uint64_t)kParams)
+        return dnfail(SS_ERR_INVALID_ARGUMENT, "ss_dn_set_params: null argument or count != %d", kParams);
+    for (uint64_t i = 0; i < count; ++i)
+        if (!std::isfinite(host[i])) return dnfail(SS_ERR_INVALID_ARGUMENT, "ss_dn_set_params: non-finite parameter");
+    DCK(cudaSetDevice(n->device));
+    DCK(cudaMemcpyAsync(n->P, host, (size_t)kParams * sizeof(float), cudaMemcpyHostToDevice, n->stream));
+    pack_all(n, n->stream);
+    DCK(cudaGetLastError());
+    DCK(cudaStreamSynchronize(n->stream));
+    return SS_OK;
+}
+
+int ss_dn_forward(ss_dn *n, const float *x, float *y) {
+    if (!n || !x || !y) return dnfail(SS_ERR_INVALID_ARGUMENT, "ss_dn_forward: null argument");
+    DCK(cudaSetDevice(n->device));
+    enqueue_forward(n, x, y, n->stream);
+    DCK(cudaGetLastError());
+    return check_err(n);
+}
+
+// batch samples [batch][V] (DEVICE): loss averaged over the batch; with
+// lr > 0 one Adam step on the batch-mean gradient
+int ss_dn_train(ss_dn *n, const float *x, const float *t, uint32_t batch, float lr, double *loss) {
+    if (!n || !x || !t || batch == 0 || !(lr >= 0.f))
+        return dnfail(SS_ERR_INVALID_ARGUMENT, "ss_dn_train: null argument, empty batch or negative rate");
+    DCK(cudaSetDevice(n->device));
+    const bool update = lr > 0.f;
+    DCK(cudaMemsetAsync(n->sums, 0, 2 * sizeof(double), n->stream));
+    if (update) DCK(cudaMemsetAsync(n->G, 0, (size_t)kParams * sizeof(float), n->stream));
+    for (uint32_t b = 0; b < batch; ++b) {
+        const float *xb = x + (size_t)b * n->nvox, *tb = t + (size_t)b * n->nvox;
+        enqueue_forward(n, xb, n->yb, n->stream);
+        enqueue_backward(n, xb, tb, n->yb, n->stream, update);
+    }
+    if (update) {
+        n->adam_t += 1;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = 1.f - std::pow(b1, (float)n->adam_t), c2 = 1.f - std::pow(b2, (float)n->adam_t);
+        k_dn_adam<<<(kParams + 255) / 256, 256, 0, n->stream>>>(n->P, n->G, n->M, n->S, kParams, 1.f / (float)batch,
+                                                                lr, b1, b2, 1e-8f, c1, c2);
+        pack_all(n, n->stream);
+        n->launches += 1;
+    }
+    DCK(cudaGetLastError());
+    double h[2];
+    DCK(cudaMemcpyAsync(h, n->sums, sizeof h, cudaMemcpyDeviceToHost, n->stream));
+    const int rc = check_err(n);
+    if (rc != SS_OK) return rc;
+    if (loss) *loss = h[0] / (double)batch;
+    return SS_OK;
+}
+
+int ss_dn_gradients(ss_dn *n, const float *x, const float *t, uint32_t batch, float *grads, uint64_t count,
+                    double *loss) {
+    if (!n || !x || !t || !grads || batch == 0 || count != (uint64_t)kParams)
+        return dnfail(SS_ERR_INVALID_ARGUMENT, "ss_dn_gradients: null argument, empty batch or count != %d", kParams);
+    DCK(cudaSetDevice(n->device));
+    DCK(cudaMemsetAsync(n->sums, 0, 2 * sizeof(double), n->stream));
+    DCK(cudaMemsetAsync(n->G, 0, (size_t)kParams * sizeof(float), n->stream));
+    for (uint32_t b = 0; b < batch; ++b) {
+        const float *xb = x + (size_t)b * n->nvox, *tb = t + (size_t)b * n->nvox;
+        enqueue_forward(n, xb, n->yb, n->stream);
+        enqueue_backward(n, xb, tb, n->yb, n->stream, true);
+    }
+    DCK(cudaGetLastError());
+    std::vector<float> g(kParams);
+    double h[2];
+    DCK(cudaMemcpyAsync(g.data(), n->G, (size_t)kParams * sizeof(float), cudaMemcpyDeviceToHost, n->stream));
+    DCK(cudaMemcpyAsync(h, n->sums, sizeof h, cudaMemcpyDeviceToHost, n->stream));
+    const int rc = check_err(n);
+    if (rc != SS_OK) return rc;
+    for (int i = 0; i < kParams; ++i) grads[i] = g[i] / (float)batch;
+    if (loss) *loss = h[0] / (double)batch;
+    return SS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+"""The learned histogram denoiser over the C ABI (``ss_dn_*`` of
+include/ssgpu.h): a 3-D CNN on the (x, y, phi) grid whose 32 -> 32
+convolutions run on the tensor cores (tcgen05).  Inputs and outputs are CUDA
+float tensors of the grid's shape (torch is used only to hold device memory).
+
+    dn = Denoiser((128, 128, 32), seed=0)
+    y = dn.forward(x)                   # x: histogram / mean count
+    loss = dn.train(x_batch, t_batch, lr=1e-3)
+
+There is no CPU fallback.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+_fp = ctypes.POINTER(ctypes.c_float)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class Denoiser:
+    """The network on the current CUDA device for grids of `shape` = (nx, ny, nphi)."""
+
+    def __init__(self, shape, seed=0, stream=None):
+        self.lib = _lib.load()
+        self.shape = tuple(int(v) for v in shape)
+        h = ctypes.c_void_p()
+        check(self.lib.ss_dn_create(*self.shape, int(seed), ctypes.c_void_p(stream) if stream else None,
+                                    ctypes.byref(h)))
+        self._h = h
+        n = ctypes.c_uint64()
+        check(self.lib.ss_dn_info(self._h, ctypes.byref(n), None))
+        self.nparams = n.value
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self.lib.ss_dn_destroy(h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check_grid(self, t, batched=False):
+        import torch
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()):
+            raise TypeError("expected a contiguous CUDA float32 tensor")
+        n = int(np.prod(self.shape))
+        if batched:
+            if t.numel() % n or t.numel() == 0:
+                raise ValueError(f"expected a batch of grids of shape {self.shape}")
+            return t.numel() // n
+        if t.numel() != n:
+            raise ValueError(f"expected a grid of shape {self.shape}")
+        return 1
+
+    @property
+    def params(self):
+        out = np.empty(self.nparams, dtype=np.float32)
+        check(self.lib.ss_dn_get_params(self._h, out.ctypes.data_as(_fp), self.nparams))
+        return out
+
+    @params.setter
+    def params(self, values):
+        v = np.ascontiguousarray(values, dtype=np.float32).ravel()
+        check(self.lib.ss_dn_set_params(self._h, v.ctypes.data_as(_fp), v.size))
+
+    def forward(self, x, out=None):
+        import torch
+        self._check_grid(x)
+        y = torch.empty_like(x) if out is None else out
+        self._check_grid(y)
+        check(self.lib.ss_dn_forward(self._h, _ptr(x), _ptr(y)))
+        return y
+
+    def train(self, x, t, lr=1e-3):
+        """One Adam step on a batch (x, t: [batch, *shape]); returns the batch loss."""
+        b = self._check_grid(x, True)
+        if self._check_grid(t, True) != b:
+            raise ValueError("x and t differ in batch size")
+        loss = ctypes.c_double()
+        check(self.lib.ss_dn_train(self._h, _ptr(x), _ptr(t), b, float(lr), ctypes.byref(loss)))
+        return loss.value
+
+    def loss(self, x, t):
+        return self.train(x, t, lr=0.0)
+
+    def gradients(self, x, t):
+        """(batch-mean gradient as a numpy array, loss) without an update."""
+        b = self._check_grid(x, True)
+        g = np.empty(self.nparams, dtype=np.float32)
+        loss = ctypes.c_double()
+        check(self.lib.ss_dn_gradients(self._h, _ptr(x), _ptr(t), b, g.ctypes.data_as(_fp), self.nparams,
+                                       ctypes.byref(loss)))
+        return g, loss.value
+
+    def save(self, path):
+        np.save(path, self.params)
+
+    def load(self, path):
+        self.params = np.load(path)
+
+
+# parameter layout (offsets into the flat FP32 array)
+C, TAPS = 32, 27
+OFFSETS = {}
+_o = 0
+for _name, _size in [("w_in", TAPS * C), ("b_in", C), ("w2", TAPS * C * C), ("b2", C), ("w3", TAPS * C * C),
+                     ("b3", C), ("w_out", TAPS * C), ("b_out", 1)]:
+    OFFSETS[_name] = (_o, _size)
+    _o += _size
+NPARAMS = _o
+
+
+def split_params(p):
+    """dict of named views (w_in (27, 32), w2 (27, 32, 32), ...) into a flat parameter array."""
+    shapes = {"w_in": (TAPS, C), "b_in": (C,), "w2": (TAPS, C, C), "b2": (C,), "w3": (TAPS, C, C), "b3": (C,),
+              "w_out": (TAPS, C), "b_out": (1,)}
+    return {k: p[o:o + s].reshape(shapes[k]) for k, (o, s) in OFFSETS.items()}

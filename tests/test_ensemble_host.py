@@ -81,3 +81,15 @@ def test_parameter_scan_matches_its_ranges():
     assert rows.shape == (sum(m["params"]["number_of_particles"] for m in small), 5)
     assert np.all(rows[:, 2] == 0.0) and np.all(rows[:, 4] == np.pi / 2)
     assert np.all((rows[:, 3] >= 0) & (rows[:, 3] < 2 * np.pi))
+
+
+def test_denoiser_rejects_bad_shapes_on_the_host():
+    import ctypes
+    from stochasticsampling_gb300 import _lib
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    for shape in [(5, 5, 5), (0, 128, 1), (128, 128, 0)]:
+        assert L.ss_dn_create(*shape, 1, None, ctypes.byref(h)) == _lib.SS_ERR_INVALID_ARGUMENT
+        assert "multiple of 128" in _lib.last_error()
+    assert L.ss_dn_forward(None, None, None) == _lib.SS_ERR_INVALID_ARGUMENT
+    assert L.ss_dn_destroy(None) == _lib.SS_OK

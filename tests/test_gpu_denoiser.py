@@ -94,3 +94,115 @@ def test_conv32_rejects_bad_shapes():
     b = torch.zeros(32, device="cuda")
     with pytest.raises(ss.SsError):
         _call(ss, x, w, b, None, torch.empty_like(x), (5, 5, 5), 0)
+
+
+# ---------------------------------------------------------------- the network
+def _ref_net(torch, x, P, ste=False):
+    """The denoiser in torch fp32 with the kernel's BF16 roundings (weights
+    of the 32->32 layers, the three activations)."""
+    import torch.nn.functional as F
+    from stochasticsampling_gb300.denoiser import split_params
+    p = {k: torch.as_tensor(v.copy()) for k, v in split_params(P).items()}
+
+    def bf(t):
+        r = t.to(torch.bfloat16).float()
+        return t + (r - t).detach() if ste else r
+
+    def conv(a, w, b):  # a (in, nx, ny, np); w (27, out, in)
+        wt = w.reshape(3, 3, 3, w.shape[1], w.shape[2]).permute(3, 4, 0, 1, 2)
+        return F.conv3d(F.pad(a[None], (1, 1, 1, 1, 1, 1), mode="circular"), wt, b)[0]
+
+    a1 = bf(torch.relu(conv(x[None], p["w_in"][:, :, None], p["b_in"])))
+    a2 = bf(torch.relu(conv(a1, bf(p["w2"]), p["b2"])))
+    a3 = bf(torch.relu(conv(a2, bf(p["w3"]), p["b3"])))
+    return x + conv(a3, p["w_out"][:, None, :], p["b_out"])[0], p
+
+
+def _net(ss, shape, seed=3, out_scale=0.05):
+    from stochasticsampling_gb300.denoiser import Denoiser, split_params
+    dn = Denoiser(shape, seed=seed)
+    P = dn.params
+    rng = np.random.default_rng(seed)
+    split_params(P)["w_out"][:] = out_scale * rng.standard_normal((27, 32))
+    split_params(P)["b_in"][:] = 0.05 * rng.standard_normal(32)
+    dn.params = P
+    return dn, P
+
+
+def test_denoiser_forward_matches_torch():
+    ss = _gpu()
+    torch = _torch()
+    shape = (8, 8, 32)
+    dn, P = _net(ss, shape)
+    g = torch.Generator().manual_seed(1)
+    x = 1.0 + 0.3 * torch.randn(*shape, generator=g)
+    y = dn.forward(x.cuda()).cpu()
+    want, _ = _ref_net(torch, x, P)
+    corr, wcorr = y - x, want - x
+    assert (corr - wcorr).abs().max().item() <= 1e-2 * wcorr.abs().max().item()
+    dn.close()
+
+
+def test_denoiser_gradients_match_torch():
+    ss = _gpu()
+    torch = _torch()
+    from stochasticsampling_gb300.denoiser import split_params
+    shape = (8, 8, 32)
+    dn, P = _net(ss, shape, seed=4)
+    g = torch.Generator().manual_seed(2)
+    x = 1.0 + 0.3 * torch.randn(2, *shape, generator=g)
+    t = 1.0 + 0.1 * torch.randn(2, *shape, generator=g)
+    grads, loss = dn.gradients(x.cuda().contiguous(), t.cuda().contiguous())
+    # autograd through the network rebuilt with leaf parameters and
+    # straight-through BF16 roundings
+    import torch.nn.functional as F
+    P_t = {k: torch.as_tensor(v.copy(), dtype=torch.float32).requires_grad_(True)
+           for k, v in split_params(P).items()}
+
+    def bf(a):
+        return a + (a.to(torch.bfloat16).float() - a).detach()
+
+    def conv(a, w, bias):
+        wt = w.reshape(3, 3, 3, w.shape[1], w.shape[2]).permute(3, 4, 0, 1, 2)
+        return F.conv3d(F.pad(a[None], (1, 1, 1, 1, 1, 1), mode="circular"), wt, bias)[0]
+
+    lt = 0.0
+    for b in range(2):
+        a1 = bf(torch.relu(conv(x[b][None], P_t["w_in"][:, :, None], P_t["b_in"])))
+        a2 = bf(torch.relu(conv(a1, bf(P_t["w2"]), P_t["b2"])))
+        a3 = bf(torch.relu(conv(a2, bf(P_t["w3"]), P_t["b3"])))
+        yb = x[b] + conv(a3, P_t["w_out"][:, None, :], P_t["b_out"])[0]
+        lt = lt + ((yb - t[b]) ** 2).mean() / 2
+    lt.backward()
+    assert abs(loss - lt.item()) <= 1e-3 * lt.item()
+    got = split_params(grads)
+    for k, v in P_t.items():
+        want = v.grad.numpy()
+        err = np.linalg.norm(got[k] - want) / max(np.linalg.norm(want), 1e-30)
+        assert err < 3e-2, (k, err)
+    dn.close()
+
+
+def test_denoiser_training_reduces_loss():
+    ss = _gpu()
+    torch = _torch()
+    shape = (16, 16, 32)
+    from stochasticsampling_gb300.denoiser import Denoiser
+    dn = Denoiser(shape, seed=7)
+    g = torch.Generator().manual_seed(3)
+    X, Y, P_ = torch.meshgrid(torch.arange(16.0), torch.arange(16.0), torch.arange(32.0), indexing="ij")
+
+    def batch(n):
+        amp = 0.3 * torch.rand(n, 1, 1, 1, generator=g)
+        ph = 6.283 * torch.rand(n, 1, 1, 1, generator=g)
+        t = 1.0 + amp * torch.sin(6.283 * X / 16 + ph) * torch.cos(6.283 * P_ / 32)
+        x = t + 0.2 * torch.randn(n, *shape, generator=g)
+        return x.cuda().contiguous(), t.cuda().contiguous()
+
+    xv, tv = batch(4)
+    l0 = dn.loss(xv, tv)
+    for _ in range(150):
+        dn.train(*batch(4), lr=2e-3)
+    l1 = dn.loss(xv, tv)
+    assert np.isfinite(l1) and l1 < 0.5 * l0, (l0, l1)
+    dn.close()
