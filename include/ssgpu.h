@@ -310,6 +310,23 @@ int ss_dn_train(ss_dn *dn, const float *x, const float *t, uint32_t batch, float
 int ss_dn_gradients(ss_dn *dn, const float *x, const float *t, uint32_t batch, float *grads, uint64_t count,
                     double *loss);
 
+/* Training data for the denoiser: adds to hist (DEVICE float [nx][ny][np])
+ * the normalised histogram (nx ny np / n per particle, mean 1) of n particles
+ * drawn with density 1 + amp sin(2 pi s + phase) along axis (0: x, 1: y; s =
+ * position / box edge), uniform along the other axis and in phi -- the
+ * production workload's initial-condition family.  Philox keyed by seed.
+ * Asynchronous on stream. */
+int ss_dn_sample_histogram(uint32_t nx, uint32_t ny, uint32_t np, uint64_t n, double amp, double phase,
+                           uint32_t axis, uint64_t seed, float *hist, void *stream);
+
+/* Put the denoiser between the histogram and the stress contraction of a
+ * quasi2d SS_FLAG_MIXED / SS_FLAG_FIXED64 context whose grid (x, y, phi)
+ * equals the network's: every step then contracts network(counts / mean
+ * count) * mean count instead of the counts (the binning, the particles and
+ * ss_get_counts are unchanged).  dn = NULL removes it.  The context does not
+ * own dn; keep it alive while it is set. */
+int ss_set_denoiser(ss_ctx *ctx, ss_dn *dn);
+
 /* copy the last error message of ctx (or the last context-free error when
  * ctx is NULL) into buf, NUL terminated */
 int ss_last_error(ss_ctx *ctx, char *buf, size_t len);

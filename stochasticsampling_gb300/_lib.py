@@ -19,7 +19,7 @@ EXPORTS = [
     "ss_ensemble_autotune", "ss_ensemble_set_config", "ss_ensemble_run", "ss_ensemble_synchronize", "ss_ensemble_get_particles",
     "ss_ensemble_get_counts", "ss_ensemble_get_flow_field", "ss_ensemble_info", "ss_dn_conv32", "ss_dn_create",
     "ss_dn_destroy", "ss_dn_info", "ss_dn_get_params", "ss_dn_set_params", "ss_dn_forward", "ss_dn_train",
-    "ss_dn_gradients", "ss_last_error", "ss_version",
+    "ss_dn_gradients", "ss_dn_sample_histogram", "ss_set_denoiser", "ss_last_error", "ss_version",
 ]
 
 SS_OK = 0
@@ -146,6 +146,8 @@ def load(build_if_missing=True):
         "ss_dn_forward": [vp, vp, vp],
         "ss_dn_train": [vp, vp, vp, u32, ctypes.c_float, dp],
         "ss_dn_gradients": [vp, vp, vp, u32, ctypes.POINTER(ctypes.c_float), u64, dp],
+        "ss_set_denoiser": [vp, vp],
+        "ss_dn_sample_histogram": [u32, u32, u32, u64, ctypes.c_double, ctypes.c_double, u32, u64, vp, vp],
         "ss_last_error": [vp, ctypes.c_char_p, ctypes.c_size_t],
     }
     for name, args in sig.items():

@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "../../include/ssgpu.h"
+#include "common.cuh"
 
 namespace ss {
 void record_error(const char *msg);
@@ -588,6 +589,40 @@ extern "C" int ss_dn_conv32(const void *x, const float *w, const float *bias, co
     return SS_OK;
 }
 
+// Training data: the normalised histogram (mean 1 per bin) of n particles
+// drawn from the production workload's initial condition family: density
+// proportional to 1 + amp sin(2 pi s + phase) along one axis (s = position
+// / box edge), uniform along the other and in phi.  The profile is sampled
+// by inverting its CDF with FP32 Newton steps; Philox keyed by seed, counter
+// = particle index.  Each particle adds nbins / n to its bin.
+__global__ void k_dn_sample_hist(int nx, int ny, int np, unsigned long long n, float amp, float phase, int axis,
+                                 unsigned long long seed, float w, float *__restrict__ hist) {
+    const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint4 r = ss::philox4x32_10(make_uint4((uint32_t)i, (uint32_t)(i >> 32), 0x5EED0000u, 7u), key);
+        const float u = (float)(r.x >> 8) * 0x1p-24f, u2 = (float)(r.y >> 8) * 0x1p-24f,
+                    u3 = (float)(r.z >> 8) * 0x1p-24f;
+        // F(s) = s - amp / (2 pi) (cos(2 pi s + phase) - cos(phase)) = u, F' = 1 + amp sin(2 pi s + phase)
+        float sv = u;
+        const float c0 = cosf(phase), k = amp * 0.15915494309189535f;
+#pragma unroll
+        for (int it = 0; it < 4; ++it) {
+            float sn, cs;
+            sincosf(6.283185307179586f * sv + phase, &sn, &cs);
+            sv -= (sv - k * (cs - c0) - u) / (1.f + amp * sn);
+        }
+        sv = sv - floorf(sv);
+        const int na = axis == 0 ? nx : ny, nb = axis == 0 ? ny : nx;
+        int ia = (int)(sv * (float)na), ib = (int)(u2 * (float)nb), ip = (int)(u3 * (float)np);
+        ia = ia < 0 ? 0 : (ia >= na ? na - 1 : ia);
+        ib = ib >= nb ? nb - 1 : ib;
+        ip = ip >= np ? np - 1 : ip;
+        const int ix = axis == 0 ? ia : ib, iy = axis == 0 ? ib : ia;
+        atomicAdd(hist + ((size_t)ix * ny + iy) * np + ip, w);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // host object
 // ---------------------------------------------------------------------------
@@ -859,3 +894,41 @@ int ss_dn_gradients(ss_dn *n, const float *x, const float *t, uint32_t batch, fl
 }
 
 }  // extern "C"
+
+extern "C" int ss_dn_sample_histogram(uint32_t nx, uint32_t ny, uint32_t np, uint64_t n, double amp, double phase,
+                                      uint32_t axis, uint64_t seed, float *hist, void *stream) {
+    if (!hist || nx < 1 || ny < 1 || np < 1 || n < 1 || axis > 1 || !(amp >= 0.0 && amp < 1.0) ||
+        !std::isfinite(phase))
+        return dnfail(SS_ERR_INVALID_ARGUMENT,
+                      "ss_dn_sample_histogram: null histogram, empty grid, n = 0, axis > 1 or amp outside [0, 1)");
+    cudaStream_t s = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    DCK(cudaGetDevice(&dev));
+    DCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const double nbins = (double)nx * ny * np;
+    const unsigned long long want = (n + 255) / 256;
+    const unsigned grid = (unsigned)(want < (unsigned long long)(8 * sms) ? want : (unsigned long long)(8 * sms));
+    k_dn_sample_hist<<<grid, 256, 0, s>>>((int)nx, (int)ny, (int)np, n, (float)amp, (float)phase, (int)axis, seed,
+                                          (float)(nbins / (double)n), hist);
+    DCK(cudaGetLastError());
+    return SS_OK;
+}
+
+namespace ss {
+void dn_shape(const ss_dn *n, int *nx, int *ny, int *np) {
+    *nx = n->d.nx;
+    *ny = n->d.ny;
+    *np = n->d.np;
+}
+int dn_enqueue_forward(ss_dn *n, const float *x, float *y, cudaStream_t s) {
+    enqueue_forward(n, x, y, s);
+    return 4;
+}
+int dn_status(ss_dn *n, cudaStream_t s) {
+    unsigned h = 0;
+    DCK(cudaMemcpyAsync(&h, n->err, sizeof h, cudaMemcpyDeviceToHost, s));
+    DCK(cudaStreamSynchronize(s));
+    if (h) return dnfail(SS_ERR_CUDA, "denoiser: a tensor-core convolution's mbarrier wait timed out");
+    return SS_OK;
+}
+}  // namespace ss

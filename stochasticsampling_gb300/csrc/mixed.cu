@@ -93,12 +93,15 @@ __global__ void k_bin_m(unsigned long long n, MixedParams M, const double *__res
 // angular contraction in FP32 (thread per cell, angle kernels in shared
 // memory); per-component sums of the result accumulated in FP64 for the
 // mean handling (one FP64 atomic per component per warp)
+// dist != nullptr: the distribution comes from dist[bin] * fscale (the
+// denoised histogram) instead of the counts
 template <bool STRESS, bool MAG>
 __global__ void __launch_bounds__(64) k_contract_m(const uint32_t *__restrict__ counts,
                                                    const float *__restrict__ lut, int lut_n,
                                                    const float *__restrict__ kern, MixedParams M,
                                                    float2 *__restrict__ fwd, float *__restrict__ table, int tstride,
-                                                   double *__restrict__ sums) {
+                                                   double *__restrict__ sums, const float *__restrict__ dist,
+                                                   float fscale) {
     extern __shared__ float skf[];
     const int na = M.nang;
     for (int i = threadIdx.x; i < 12 * na; i += blockDim.x) skf[i] = kern[i];
@@ -111,8 +114,13 @@ __global__ void __launch_bounds__(64) k_contract_m(const uint32_t *__restrict__ 
     if (live) {
         const long long row = (long long)cell * na;
         for (int a = 0; a < na; ++a) {
-            uint32_t c = counts[row + a];
-            float f = ((int)c < lut_n) ? __ldg(lut + c) : (float)(((double)c / M.dist_den) * M.volume);
+            float f;
+            if (dist) {
+                f = dist[row + a] * fscale;
+            } else {
+                const uint32_t c = counts[row + a];
+                f = ((int)c < lut_n) ? __ldg(lut + c) : (float)(((double)c / M.dist_den) * M.volume);
+            }
             if (STRESS) {
 #pragma unroll
                 for (int j = 0; j < 9; ++j) acc[j] = fmaf(skf[j * na + a], f, acc[j]);
@@ -377,12 +385,28 @@ void launch_bin_m(cudaStream_t s, bool fixed, unsigned long long n, const MixedP
 }
 void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *lut, int lut_n,
                        const float *kern, const MixedParams &M, float2 *fwd, float *table, int tstride,
-                       double *sums) {
+                       double *sums, const float *dist, float fscale) {
     unsigned blocks = nb((unsigned long long)M.ncell, 64);
     const size_t sm = 12ull * M.nang * sizeof(float);
-    if (stress && mag) k_contract_m<true, true><<<blocks, 64, sm, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums);
-    else if (stress) k_contract_m<true, false><<<blocks, 64, sm, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums);
-    else k_contract_m<false, true><<<blocks, 64, sm, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums);
+    if (stress && mag)
+        k_contract_m<true, true><<<blocks, 64, sm, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums, dist,
+                                                        fscale);
+    else if (stress)
+        k_contract_m<true, false><<<blocks, 64, sm, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums, dist,
+                                                         fscale);
+    else
+        k_contract_m<false, true><<<blocks, 64, sm, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums, dist,
+                                                         fscale);
+}
+
+// counts -> the denoiser's input, counts / (N / nbins) (mean 1)
+__global__ void k_counts_to_unit(const uint32_t *__restrict__ counts, long long nbins, float inv_mean,
+                                 float *__restrict__ x) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < nbins) x[i] = (float)counts[i] * inv_mean;
+}
+void launch_counts_to_unit(cudaStream_t s, const uint32_t *counts, long long nbins, float inv_mean, float *x) {
+    if (nbins > 0) k_counts_to_unit<<<nb((unsigned long long)nbins, 256), 256, 0, s>>>(counts, nbins, inv_mean, x);
 }
 void launch_center_m(cudaStream_t s, float2 *fwd, int c0, int c1, int ncell, const double *sums) {
     long long total = (long long)(c1 - c0) * ncell;

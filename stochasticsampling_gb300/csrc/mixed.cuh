@@ -36,7 +36,8 @@ void launch_bin_m(cudaStream_t s, bool fixed, unsigned long long n, const MixedP
                   float *const as[2], uint32_t *key, uint32_t *counts);
 void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *lut, int lut_n,
                        const float *kern, const MixedParams &M, float2 *fwd, float *table, int tstride,
-                       double *sums);
+                       double *sums, const float *dist = nullptr, float fscale = 0.f);
+void launch_counts_to_unit(cudaStream_t s, const uint32_t *counts, long long nbins, float inv_mean, float *x);
 void launch_center_m(cudaStream_t s, float2 *fwd, int c0, int c1, int ncell, const double *sums);
 void launch_kspace_m(cudaStream_t s, bool flow, bool mag, const float2 *fwd, float2 *inv, const MixedParams &M,
                      float screening);

@@ -18,6 +18,7 @@
 
 #include "../../include/ssgpu.h"
 #include "kernels.cuh"
+#include "denoiser.cuh"
 #include "mixed.cuh"
 
 using namespace ss;
@@ -73,6 +74,10 @@ struct ss_ctx {
     // FP32 mixed-precision mode (SS_FLAG_MIXED)
     bool mixed = false;
     bool fixed = false;  // positions in 64-bit fixed point (SS_FLAG_FIXED64)
+    // learned denoiser between the histogram and the stress contraction (mixed quasi2d only)
+    ss_dn *dn = nullptr;
+    float *dn_x = nullptr, *dn_y = nullptr;
+    float dn_inv_mean = 0.f, dn_fscale = 0.f;
     bool canon = false;  // quasi2d: z == 0 and theta == pi/2 hold for every particle
     MixedParams M{};
     float *pa[2][2] = {};  // phi, theta (FP32)
@@ -296,8 +301,16 @@ static int enqueue_solve_m(ss_ctx *c, bool flow, bool mag, const uint32_t *count
     const int nc = c->P.ncell;
     mark(c, 0);
     CK(cudaMemsetAsync(c->sums, 0, 12 * sizeof(double), c->stream));
-    launch_contract_m(c->stream, flow, mag, counts, c->lut_f, kLutN, c->kern_f, c->M, c->fwd_f, c->table_f, ts,
-                      c->sums);
+    if (c->dn && flow) {
+        // the denoised histogram replaces the counts in the contraction
+        launch_counts_to_unit(c->stream, counts, c->P.nbins, c->dn_inv_mean, c->dn_x);
+        *nl += 1 + dn_enqueue_forward(c->dn, c->dn_x, c->dn_y, c->stream);
+        launch_contract_m(c->stream, flow, mag, counts, c->lut_f, kLutN, c->kern_f, c->M, c->fwd_f, c->table_f, ts,
+                          c->sums, c->dn_y, c->dn_fscale);
+    } else {
+        launch_contract_m(c->stream, flow, mag, counts, c->lut_f, kLutN, c->kern_f, c->M, c->fwd_f, c->table_f, ts,
+                          c->sums);
+    }
     if (flow) launch_center_m(c->stream, c->fwd_f, 0, 9, nc, c->sums);
     if (mag) launch_center_m(c->stream, c->fwd_f, 9, 12, nc, c->sums);
     *nl += 1 + (flow ? 1 : 0) + (mag ? 1 : 0);
@@ -357,6 +370,9 @@ static int enqueue_step(ss_ctx *c, int pcur, int ccur, bool host_noise, uint64_t
 }
 
 static void advance(ss_ctx *c) {
+    // a replayed graph does not run the host side of enqueue_solve_m: the
+    // widened FP64 copy of the mixed fields is stale after every step
+    c->wide_valid = false;
     if (c->sort) c->pcur ^= 1;
     c->dist_idx = c->ccur;
     c->ccur ^= 1;
@@ -464,6 +480,7 @@ static void destroy_impl(ss_ctx *c) {
     for (int b = 0; b < 2; ++b)
         for (int k = 0; k < 2; ++k) cudaFree(c->pa[b][k]);
     cudaFree(c->fwd_f); cudaFree(c->inv_f); cudaFree(c->table_f); cudaFree(c->kern_f); cudaFree(c->lut_f);
+    cudaFree(c->dn_x); cudaFree(c->dn_y);
     cudaFree(c->sums);
     for (auto &e : c->timing.ev)
         if (e) cudaEventDestroy(e);
@@ -853,7 +870,39 @@ int ss_noise(ss_ctx *c, uint64_t timestep, double *out) {
 int ss_synchronize(ss_ctx *c) {
     if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
     CK(cudaStreamSynchronize(c->stream));
+    if (c->dn) CKR(dn_status(c->dn, c->stream));
     return read_device_error(c);
+}
+
+int ss_set_denoiser(ss_ctx *c, ss_dn *dn) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    if (dn) {
+        int nx, ny, np;
+        dn_shape(dn, &nx, &ny, &np);
+        if (!c->mixed || !c->q2d || c->P.gz != 1 || c->P.gtheta != 1)
+            return fail(c, SS_ERR_INVALID_ARGUMENT, "the denoiser needs a quasi2d mixed-precision context");
+        if (nx != c->P.gx || ny != c->P.gy || np != c->P.gphi)
+            return fail(c, SS_ERR_INVALID_ARGUMENT, "denoiser grid %dx%dx%d differs from the histogram's %dx%dx%d", nx,
+                        ny, np, c->P.gx, c->P.gy, c->P.gphi);
+        if (!c->dn_x) {
+            CK(cudaMalloc((void **)&c->dn_x, (size_t)c->P.nbins * sizeof(float)));
+            CK(cudaMalloc((void **)&c->dn_y, (size_t)c->P.nbins * sizeof(float)));
+        }
+        const double mean = (double)c->P.n / (double)c->P.nbins;  // counts per bin
+        c->dn_inv_mean = (float)(1.0 / mean);
+        c->dn_fscale = (float)(mean / c->P.dist_den * c->P.volume);
+    }
+    c->dn = dn;
+    // the captured steps change: recapture on the next step
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b)
+            if (c->graph[a][b]) {
+                cudaGraphExecDestroy(c->graph[a][b]);
+                c->graph[a][b] = nullptr;
+            }
+    return SS_OK;
 }
 
 int ss_get_particles(ss_ctx *c, double *out, uint64_t n) {

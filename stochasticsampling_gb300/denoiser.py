@@ -53,6 +53,8 @@ class Denoiser:
         import torch
         if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()):
             raise TypeError("expected a contiguous CUDA float32 tensor")
+        # the network runs on its own stream: the tensor's producer must be done
+        torch.cuda.current_stream().synchronize()
         n = int(np.prod(self.shape))
         if batched:
             if t.numel() % n or t.numel() == 0:
@@ -125,3 +127,54 @@ def split_params(p):
     shapes = {"w_in": (TAPS, C), "b_in": (C,), "w2": (TAPS, C, C), "b2": (C,), "w3": (TAPS, C, C), "b3": (C,),
               "w_out": (TAPS, C), "b_out": (1,)}
     return {k: p[o:o + s].reshape(shapes[k]) for k, (o, s) in OFFSETS.items()}
+
+
+# ---------------------------------------------------------------- training data
+def sample_histogram(shape, n, amp, phase, axis, seed, out=None):
+    """Normalised histogram (mean 1) of n particles with density
+    1 + amp sin(2 pi s + phase) along `axis` (0: x, 1: y), uniform otherwise,
+    sampled on the device (ss_dn_sample_histogram); a CUDA float tensor."""
+    import torch
+    lib = _lib.load()
+    h = torch.zeros(shape, device="cuda", dtype=torch.float32) if out is None else out
+    check(lib.ss_dn_sample_histogram(*[int(v) for v in shape], int(n), float(amp), float(phase), int(axis),
+                                     int(seed), _ptr(h), None))
+    return h
+
+
+def make_pairs(npairs, shape=(128, 128, 32), n_in=1_000_000, n_target=64_000_000, amp_max=0.05, seed=0):
+    """Training pairs generated by the method: for each pair an initial
+    condition of the production family (perturbation amplitude uniform in
+    [0, amp_max], random phase and axis), histogrammed once with n_in and
+    once, independently, with n_target particles.  Returns (inputs,
+    targets), CUDA float tensors [npairs, *shape], both normalised to mean 1."""
+    import torch
+    rng = np.random.default_rng(seed)
+    X = torch.zeros((npairs, *shape), device="cuda", dtype=torch.float32)
+    T = torch.zeros_like(X)
+    for i in range(npairs):
+        amp, ph, ax = rng.uniform(0.0, amp_max), rng.uniform(0.0, 2 * np.pi), int(rng.integers(2))
+        sample_histogram(shape, n_in, amp, ph, ax, (seed << 32) + 2 * i, out=X[i])
+        sample_histogram(shape, n_target, amp, ph, ax, (seed << 32) + 2 * i + 1, out=T[i])
+    torch.cuda.synchronize()
+    return X, T
+
+
+def train(dn, X, T, epochs=1, batch=8, lr=1e-3, seed=0, val=None):
+    """Adam over shuffled minibatches of (X, T); returns the per-epoch mean
+    training loss and, when val = (Xv, Tv) is given, the validation loss."""
+    import torch
+    rng = np.random.default_rng(seed)
+    hist = []
+    n = X.shape[0]
+    for _ in range(epochs):
+        order = rng.permutation(n)
+        losses = []
+        for k in range(0, n - batch + 1, batch):
+            idx = torch.as_tensor(order[k:k + batch], device=X.device)
+            losses.append(dn.train(X[idx].contiguous(), T[idx].contiguous(), lr=lr))
+        rec = {"train": float(np.mean(losses))}
+        if val is not None:
+            rec["val"] = dn.loss(val[0], val[1])
+        hist.append(rec)
+    return hist

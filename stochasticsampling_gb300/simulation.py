@@ -114,6 +114,13 @@ class Simulation:
         check(rc, self._h)
 
     # --- Simulation API ---------------------------------------------------
+    def set_denoiser(self, denoiser):
+        """Contract the denoised histogram instead of the counts every step
+        (quasi2d mixed contexts; None removes it).  The simulation keeps a
+        reference to the denoiser while it is set."""
+        self._denoiser = denoiser
+        self._check(self.lib.ss_set_denoiser(self._h, denoiser._h if denoiser is not None else None))
+
     def init(self, particles):
         p = _f64(particles, (-1, 5))
         self._check(self.lib.ss_init(self._h, _ptr(p), p.shape[0]))

@@ -206,3 +206,59 @@ def test_denoiser_training_reduces_loss():
     l1 = dn.loss(xv, tv)
     assert np.isfinite(l1) and l1 < 0.5 * l0, (l0, l1)
     dn.close()
+
+
+def test_sample_histogram_profile():
+    _gpu()
+    torch = _torch()
+    from stochasticsampling_gb300.denoiser import sample_histogram
+    shape = (32, 32, 16)
+    h = sample_histogram(shape, 4_000_000, 0.05, 0.3, 0, seed=11).cpu().numpy()
+    assert abs(h.mean() - 1.0) < 1e-5
+    prof = h.mean(axis=(1, 2))
+    s = (np.arange(32) + 0.5) / 32
+    want = 1 + 0.05 * np.sin(2 * np.pi * s + 0.3) * np.sinc(1 / 32)  # bin average of the sine
+    assert np.abs(prof - want).max() < 0.02  # ~4 sigma of 4e6 / 32 particles per slab
+    hy = sample_histogram(shape, 4_000_000, 0.05, 0.3, 1, seed=12).cpu().numpy()
+    assert np.abs(hy.mean(axis=(0, 2)) - want).max() < 0.02
+
+
+def test_denoised_step_with_identity_network_matches_plain():
+    """With w_out = b_out = 0 the network is the identity, so the denoised
+    step contracts counts / mean * mean: the plain step up to FP32 rounding."""
+    ss = _gpu()
+    _torch()
+    from stochasticsampling_gb300.denoiser import Denoiser, split_params
+    from test_gpu_parity import C0, _particles
+    name, grid, box, params, n, q2d = C0
+    p = dict(params, number_of_particles=n, seed=5)
+    dn = Denoiser((grid[0], grid[1], grid[3]), seed=1)
+    P = dn.params
+    split_params(P)["w_out"][:] = 0.0
+    split_params(P)["b_out"][:] = 0.0
+    dn.params = P
+    rng = np.random.default_rng(2)
+    rows = _particles(rng, n, box, True)
+    a = ss.Simulation(grid=grid, box=box, params=p, quasi2d=True, mixed=True)
+    b = ss.Simulation(grid=grid, box=box, params=p, quasi2d=True, mixed=True)
+    a.init(rows)
+    b.init(rows)
+    b.set_denoiser(dn)
+    for _ in range(3):
+        a.do_timestep()
+        b.do_timestep()
+        ua, ub = a.get_flow_field(), b.get_flow_field()
+        assert np.linalg.norm(ua - ub) <= 1e-5 * np.linalg.norm(ua)
+    pa, pb = a.get_particles(), b.get_particles()
+    assert np.mean(np.abs(pa[:, 0] - pb[:, 0]) > 1e-6) < 1e-3
+    # a non-trivial network changes the contraction (a uniform output
+    # weight would only shift the mean, which the flow does not see)
+    split_params(P)["w_out"][:] = 0.05 * rng.standard_normal((27, 32))
+    dn.params = P
+    b.do_timestep()
+    a.do_timestep()
+    assert np.linalg.norm(a.get_flow_field() - b.get_flow_field()) > 1e-3 * np.linalg.norm(a.get_flow_field())
+    b.set_denoiser(None)
+    a.close()
+    b.close()
+    dn.close()
