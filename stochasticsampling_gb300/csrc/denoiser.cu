@@ -9,8 +9,9 @@
 // accumulator in tensor memory.  One elected thread issues tcgen05.mma
 // (M = 128, N = 32, K = 16, two per tap); the A rows of a tap (the periodic
 // neighbours of the tile's voxels, 64 bytes each, channels-last) are copied
-// into shared memory with cp.async into a 4-stage ring whose reuse is gated
-// by mbarriers that tcgen05.commit arrives on; the 27 weight taps stay in
+// into shared memory with cp.async into a 6-stage ring (3 taps in flight,
+// two CTAs per SM) whose reuse is gated by mbarriers that tcgen05.commit
+// arrives on; the 27 weight taps stay in
 // shared memory for the whole persistent CTA.  The epilogue reads the
 // accumulator with tcgen05.ld (one voxel's 32 channels per thread), adds the
 // bias and applies ReLU (or the ReLU derivative of a reference tensor for
@@ -44,11 +45,14 @@ namespace {
 constexpr int kC = 32;                       // channels
 constexpr int kTaps = 27;                    // 3 x 3 x 3
 constexpr int kTileM = 128;                  // voxels per tile (MMA M)
-constexpr int kStages = 4;                   // A ring
+constexpr int kStages = 6;                   // A ring (two CTAs per SM)
+constexpr int kAhead = 3;                    // taps in flight: a stage is refilled 3 MMAs after its use
 constexpr int kAStage = kTileM * kC * 2;     // 8 KB
 constexpr int kBTap = kC * kC * 2;           // 2 KB
 constexpr int kBAll = kTaps * kBTap;         // 54 KB
-constexpr int kSmemConv = kBAll + kStages * kAStage + 128;
+constexpr int kSmemTail = 8 * kStages + 8;   // the mbarriers, the tensor-memory slot and the failure flag
+constexpr int kSmemConv = kBAll + kStages * kAStage + ((kSmemTail + 127) / 128) * 128;
+static_assert(kSmemConv <= 227 * 1024, "the convolution's shared memory exceeds a CTA's limit");
 constexpr uint32_t kWaitLimit = 1u << 22;    // mbarrier polls before giving up
 constexpr unsigned kErrTimeout = 1u;
 
@@ -200,16 +204,21 @@ __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__res
             for (int j = 0; j < 4; ++j) cp_async16(dst + j * 128, src + j * 16);
             return true;
         };
-        bool ok = load_tap(0, it);
-        cp_async_commit();
+        // taps 0 .. kAhead - 1 in flight before the first MMA; then one new
+        // tap per MMA, kAhead ahead, into the stage the MMA kStages - kAhead
+        // taps back read (long complete, so the wait rarely stalls); empty
+        // groups past the last tap keep the group count uniform
+        const uint32_t base = it;
+        bool ok = true;
+        for (int q = 0; q < kAhead; ++q) {
+            ok = load_tap(q, base + q) && ok;
+            cp_async_commit();
+        }
         for (int t = 0; t < kTaps; ++t) {
-            if (t + 1 < kTaps) {
-                ok = load_tap(t + 1, it + 1) && ok;
-                cp_async_commit();
-                cp_async_wait<1>();
-            } else {
-                cp_async_wait<0>();
-            }
+            const int tn = t + kAhead;
+            if (tn < kTaps) ok = load_tap(tn, base + tn) && ok;
+            cp_async_commit();
+            cp_async_wait<kAhead>();  // tap t has landed
             if (!ok) *sfail = 1;
             fence_proxy_async();
             __syncthreads();
@@ -415,43 +424,70 @@ __global__ void __launch_bounds__(128) k_dn_out_bwd(const float *__restrict__ dy
     store_bf16x32(dZ3 + (size_t)u * kC, g);
 }
 
-// weight gradient of a 1-channel side: dW[tap][c] = sum_v S[v][c] * s[nbr(v, tap)]
-// (input layer: S = dZ1, s = x) or sum_v s[v] * S[nbr(v, tap)][c] (output
-// layer: S = A3, s = dy).  Grid (27 taps, blocks); 8 voxel lanes x 32 channels.
-template <bool OUT>
-__global__ void __launch_bounds__(256) k_dn_wgrad_c1(const __nv_bfloat16 *__restrict__ S, const float *__restrict__ sv,
-                                                     float *__restrict__ dW, Dims d, int nvox) {
-    __shared__ float red[8][kC];
-    const int tap = blockIdx.x, c = threadIdx.x & 31, lane8 = threadIdx.x >> 5;
-    float acc = 0.f;
-    for (int v = blockIdx.y * 8 + lane8; v < nvox; v += gridDim.y * 8) {
-        const int u = Voxel(v, d).neighbour(tap, d);
-        if (OUT) acc = fmaf(sv[v], __bfloat162float(S[(size_t)u * kC + c]), acc);
-        else acc = fmaf(__bfloat162float(S[(size_t)v * kC + c]), sv[u], acc);
+// Reduce-scatter across a warp: each lane holds v[0..31]; afterwards lane l
+// holds the sum over the warp of v[l] (31 shuffles instead of 32 x 5).
+__device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int half = 16; half >= 1; half >>= 1) {
+        const bool up = (lane & half) != 0;
+#pragma unroll
+        for (int j = 0; j < half; ++j) {
+            const float send = up ? v[j] : v[j + half];
+            const float keep = up ? v[j + half] : v[j];
+            v[j] = keep + __shfl_xor_sync(0xffffffffu, send, half);
+        }
     }
-    red[lane8][c] = acc;
-    __syncthreads();
-    if (threadIdx.x < kC) {
-        float s = 0.f;
-        for (int i = 0; i < 8; ++i) s += red[i][threadIdx.x];
-        atomicAdd(&dW[tap * kC + threadIdx.x], s);
-    }
+    return v[0];
 }
 
-// bias gradient db[c] = sum_v D[v][c]
-__global__ void __launch_bounds__(256) k_dn_bgrad(const __nv_bfloat16 *__restrict__ D, float *__restrict__ db,
-                                                  int nvox) {
-    __shared__ float red[8][kC];
-    const int c = threadIdx.x & 31, lane8 = threadIdx.x >> 5;
-    float acc = 0.f;
-    for (int v = blockIdx.x * 8 + lane8; v < nvox; v += gridDim.x * 8) acc += __bfloat162float(D[(size_t)v * kC + c]);
-    red[lane8][c] = acc;
+// Weight gradients of the 1-channel layers, one tile of 128 voxels per
+// block iteration (persistent grid):
+//   OUT: dW[tap][c] += sum_v dy[v] A3[nbr(v, tap)][c]   (S = A3, sv = dy)
+//   IN:  dW[tap][c] += sum_v dZ1[v][c] x[nbr(v, tap)]   (S = dZ1, sv = x),
+//        and db[c] += sum_v dZ1[v][c]
+// Per tap the warp's 32 x 32 products are reduce-scattered to one channel
+// per lane and added into the block's shared accumulator.
+template <bool OUT>
+__global__ void __launch_bounds__(128) k_dn_wgrad_c1(const __nv_bfloat16 *__restrict__ S, const float *__restrict__ sv,
+                                                     float *__restrict__ dW, float *__restrict__ db, Dims d,
+                                                     int ntiles) {
+    __shared__ float acc[kTaps * kC + kC];
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (int i = tid; i < kTaps * kC + kC; i += blockDim.x) acc[i] = 0.f;
     __syncthreads();
-    if (threadIdx.x < kC) {
-        float s = 0.f;
-        for (int i = 0; i < 8; ++i) s += red[i][threadIdx.x];
-        atomicAdd(&db[threadIdx.x], s);
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int v = tile * kTileM + tid;
+        const Voxel vx(v, d);
+        float own[32];
+        float s_own = 0.f;
+        if (OUT) {
+            s_own = sv[v];
+        } else {
+            load_bf16x32(S + (size_t)v * kC, own);
+            float t[32];
+#pragma unroll
+            for (int c = 0; c < kC; ++c) t[c] = own[c];
+            atomicAdd(&acc[kTaps * kC + lane], warp_reduce_scatter32(t));
+        }
+        for (int tap = 0; tap < kTaps; ++tap) {
+            const int u = vx.neighbour(tap, d);
+            float p[32];
+            if (OUT) {
+                load_bf16x32(S + (size_t)u * kC, p);
+#pragma unroll
+                for (int c = 0; c < kC; ++c) p[c] *= s_own;
+            } else {
+                const float xs = sv[u];
+#pragma unroll
+                for (int c = 0; c < kC; ++c) p[c] = own[c] * xs;
+            }
+            atomicAdd(&acc[tap * kC + lane], warp_reduce_scatter32(p));
+        }
     }
+    __syncthreads();
+    for (int i = tid; i < kTaps * kC; i += blockDim.x) atomicAdd(&dW[i], acc[i]);
+    if (!OUT && tid < kC) atomicAdd(&db[tid], acc[kTaps * kC + tid]);
 }
 
 // weight gradient of a 32 -> 32 layer: dW[tap][co][ci] = sum_v dZ[v][co] A[nbr(v, tap)][ci].
@@ -460,17 +496,18 @@ __global__ void __launch_bounds__(256) k_dn_bgrad(const __nv_bfloat16 *__restric
 // accumulates a 4 x 4 block of (co, ci) over a quarter of the tile's voxels.
 __global__ void __launch_bounds__(256) k_dn_wgrad32(const __nv_bfloat16 *__restrict__ dZ,
                                                     const __nv_bfloat16 *__restrict__ A, float *__restrict__ dW,
-                                                    Dims d, int ntiles) {
+                                                    float *__restrict__ db, Dims d, int ntiles) {
     __shared__ __align__(16) float sZ[kTileM][kC + 4];
     __shared__ __align__(16) float sA[kTileM][kC + 4];
     const int tap = blockIdx.x, tid = threadIdx.x;
     const int g = tid >> 6, lt = tid & 63, cb = lt >> 3, ib = lt & 7;
-    float acc[4][4];
+    float acc[4][4], bacc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
     const int r = tid >> 1, h = tid & 1;
+    const bool centre = tap == kTaps / 2 && ib == 0;  // these threads also sum dZ (the bias gradient)
     for (int tile = blockIdx.y; tile < ntiles; tile += gridDim.y) {
         const int v = tile * kTileM + r;
         const int u = Voxel(v, d).neighbour(tap, d);
@@ -500,6 +537,10 @@ __global__ void __launch_bounds__(256) k_dn_wgrad32(const __nv_bfloat16 *__restr
             for (int i = 0; i < 4; ++i)
 #pragma unroll
                 for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(zz[i], aa[j], acc[i][j]);
+            if (centre) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) bacc[i] += zz[i];
+            }
         }
         __syncthreads();
     }
@@ -516,6 +557,10 @@ __global__ void __launch_bounds__(256) k_dn_wgrad32(const __nv_bfloat16 *__restr
         const float s = red[(0 * 64 + l) * 16 + e] + red[(1 * 64 + l) * 16 + e] + red[(2 * 64 + l) * 16 + e] +
                         red[(3 * 64 + l) * 16 + e];
         atomicAdd(&dW[(tap * kC + co) * kC + ci], s);
+    }
+    if (centre) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) atomicAdd(&db[4 * cb + i], bacc[i]);
     }
 }
 
@@ -699,17 +744,15 @@ void enqueue_backward(ss_dn *n, const float *x, const float *t, const float *y, 
     n->launches += 1;
     if (!grads) return;
     const dim3 wg(kTaps, (unsigned)(n->sms > 0 ? (4 * n->sms + kTaps - 1) / kTaps : 8));
+    const unsigned pg = (unsigned)(n->ntiles < 2 * n->sms ? n->ntiles : 2 * n->sms);
     k_dn_out_bwd<<<b, 128, 0, s>>>(n->dy, n->P, n->A3, n->D1, n->d, n->nvox);
-    k_dn_wgrad_c1<true><<<wg, 256, 0, s>>>(n->A3, n->dy, n->G + kOffWout, n->d, n->nvox);
-    k_dn_wgrad32<<<wg, 256, 0, s>>>(n->D1, n->A2, n->G + kOffW3, n->d, n->ntiles);
-    k_dn_bgrad<<<2 * n->sms, 256, 0, s>>>(n->D1, n->G + kOffB3, n->nvox);
+    k_dn_wgrad_c1<true><<<pg, 128, 0, s>>>(n->A3, n->dy, n->G + kOffWout, nullptr, n->d, n->ntiles);
+    k_dn_wgrad32<<<wg, 256, 0, s>>>(n->D1, n->A2, n->G + kOffW3, n->G + kOffB3, n->d, n->ntiles);
     launch_conv<2>(n, n->D1, n->Wm3, nullptr, n->A2, n->D2, s);
-    k_dn_wgrad32<<<wg, 256, 0, s>>>(n->D2, n->A1, n->G + kOffW2, n->d, n->ntiles);
-    k_dn_bgrad<<<2 * n->sms, 256, 0, s>>>(n->D2, n->G + kOffB2, n->nvox);
+    k_dn_wgrad32<<<wg, 256, 0, s>>>(n->D2, n->A1, n->G + kOffW2, n->G + kOffB2, n->d, n->ntiles);
     launch_conv<2>(n, n->D2, n->Wm2, nullptr, n->A1, n->D1, s);
-    k_dn_wgrad_c1<false><<<wg, 256, 0, s>>>(n->D1, x, n->G + kOffWin, n->d, n->nvox);
-    k_dn_bgrad<<<2 * n->sms, 256, 0, s>>>(n->D1, n->G + kOffBin, n->nvox);
-    n->launches += 11;
+    k_dn_wgrad_c1<false><<<pg, 128, 0, s>>>(n->D1, x, n->G + kOffWin, n->G + kOffBin, n->d, n->ntiles);
+    n->launches += 8;
 }
 
 int check_err(ss_dn *n) {
