@@ -1,9 +1,12 @@
 """Benchmark of the GB300 timestep: particle-steps/s on the 2-D production
 workload (N = 1e7 particles, grid 128x128x1x32x1, box 40x40, Dt 0.1, Dr 1.0,
 active stress -2, dt 0.005, 1 % sinusoidal density perturbation along x),
-plain FP64 path.
+plain FP64 path (the headline `value`), with sections for the FP32 mixed
+path (FP64 and fixed-point positions), the batched ensemble of 64 parameter
+sets and the learned denoiser in the loop.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--no-mixed] [--no-ensemble] [--no-denoise] [--only SECTION]
 
 One JSON line on stdout (rank 0).  --impl reference times the CPU path of the
 same workload instead: the FP64 C restatement of the reference timestep
@@ -355,6 +358,28 @@ def measure_ensemble(args, stream, rank, world, dist, barrier):
                                           "one after the other"}}
 
 
+def measure_denoised(args, rank):
+    """The learned denoiser in the loop: trained on pairs (1e6-particle
+    histogram, independent 6.4e7-particle histogram) of the workload's
+    initial-condition family, then run for a number of steps beside plain
+    FP64 runs and a 6.4e7-particle FP64 reference from independent samples of
+    the workload's initial condition; errors of the distribution and flow
+    field against the reference, and the plain FP64 cost of the denoised
+    run's error."""
+    from stochasticsampling_gb300 import denoise_eval as de
+    dn, info = de.train_denoiser(pairs=args.denoise_pairs, epochs=args.denoise_epochs, seed=rank)
+    res = de.evaluate(dn, steps=args.denoise_steps, every=max(1, args.denoise_steps // 4), seed=10 + rank)
+    dn.close()
+    ms = res["ms_per_step"]["denoised"]
+    return {"value": res["n_low"] / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+            "dtype": "f32 step (fixed-point positions) + bf16 tensor-core CNN (fp32 accumulation)",
+            "particles": res["n_low"], "cnn_ms_per_step": ms - res["ms_per_step"]["fp32_plain"],
+            "training": {k: v for k, v in info.items() if k != "history"} | {"history": info["history"]},
+            "steps": res["steps"], "mean_errors_vs_64M_fp64": res["mean_errors"],
+            "plain_fp64_ms_per_step": {k: v for k, v in res["ms_per_step"].items() if k.startswith("plain") or k == "ref"},
+            "equal_error_cost": {"distribution": res["dist_fit"], "flow": res["flow_fit"]}}
+
+
 def run_gpu(args, rank, world, dist):
     import torch
 
@@ -373,6 +398,8 @@ def run_gpu(args, rank, world, dist):
     if args.only:
         if args.only == "ensemble":
             res = measure_ensemble(args, stream, rank, world, dist, barrier)
+        elif args.only == "denoised":
+            res = measure_denoised(args, rank)
         else:
             res = measure_mixed(args, stream, p0, rank, world, dist, barrier,
                                 "fixed64" if args.only == "fixed64" else True)
@@ -432,6 +459,7 @@ def run_gpu(args, rank, world, dist):
     mixed = None if args.no_mixed else measure_mixed(args, stream, p0, rank, world, dist, barrier)
     mixed_fixed = None if args.no_mixed else measure_mixed(args, stream, p0, rank, world, dist, barrier, "fixed64")
     ensemble = None if args.no_ensemble else measure_ensemble(args, stream, rank, world, dist, barrier)
+    denoised = None if args.no_denoise else measure_denoised(args, rank)
 
     if rank != 0:
         return
@@ -483,6 +511,7 @@ def run_gpu(args, rank, world, dist):
         "mixed": mixed,
         "mixed_fixed64": mixed_fixed,
         "ensemble": ensemble,
+        "denoised": denoised,
     }
     print(json.dumps(line), flush=True)
 
@@ -496,7 +525,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32 mixed-precision measurement")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
-    ap.add_argument("--only", choices=["mixed", "fixed64", "ensemble"], default=None,
+    ap.add_argument("--no-denoise", action="store_true", help="skip the learned-denoiser measurement")
+    ap.add_argument("--denoise-pairs", type=int, default=1000)
+    ap.add_argument("--denoise-epochs", type=int, default=1)
+    ap.add_argument("--denoise-steps", type=int, default=400)
+    ap.add_argument("--only", choices=["mixed", "fixed64", "ensemble", "denoised"], default=None,
                     help="run one section alone (a smaller command for profiling); prints its JSON")
     ap.add_argument("--ensemble-members", type=int, default=64)
     ap.add_argument("--ensemble-config", default=None,
