@@ -272,13 +272,14 @@ int ss_ensemble_info(ss_ens *ens, uint64_t *particles, uint32_t *groups, uint64_
 /* ---- learned histogram denoiser ------------------------------------------
  * One 3x3x3 periodic convolution of 32 -> 32 channels on the tensor cores
  * (tcgen05, BF16 operands, FP32 accumulation): the building block of the
- * denoiser, exposed for tests.  x: DEVICE bf16 [nx][ny][np][32] (channels
- * last); w: DEVICE float [27][32 out][32 in], tap = 9 (dx+1) + 3 (dy+1) +
- * (dp+1) (the torch conv3d weight [out][in][dx+1][dy+1][dp+1] reordered);
+ * denoiser, exposed for tests.  x: DEVICE bf16 [nx][np][ny][32] (the
+ * activation layout: channels last, y fastest); w: DEVICE float [27][32
+ * out][32 in], tap = 9 (dx+1) + 3 (dy+1) + (dp+1) (the torch conv3d weight
+ * [out][in][dx+1][dy+1][dp+1] reordered);
  * bias: DEVICE float[32].  mode 0: y = bf16 ReLU(conv(x) + bias); mode 1:
  * y = float conv(x) + bias; mode 2: y = bf16 conv^T(x) * (ref > 0), the
  * backward-data step through a ReLU (ref: DEVICE bf16, bias unused).
- * nx ny np must be a positive multiple of 128.  Returns after completion. */
+ * ny must be a positive multiple of 128.  Returns after completion. */
 int ss_dn_conv32(const void *x, const float *w, const float *bias, const void *ref, void *y, uint32_t nx,
                  uint32_t ny, uint32_t np, uint32_t mode, void *stream);
 
@@ -293,7 +294,7 @@ int ss_dn_conv32(const void *x, const float *w, const float *bias, const void *r
  * mean-square error against a target distribution. */
 typedef struct ss_dn ss_dn;
 /* He-initialised from seed (the output layer near zero: y ~ x at start);
- * nx ny np a positive multiple of 128.  stream as in ss_create. */
+ * ny a positive multiple of 128.  stream as in ss_create. */
 int ss_dn_create(uint32_t nx, uint32_t ny, uint32_t np, uint64_t seed, void *stream, ss_dn **out);
 int ss_dn_destroy(ss_dn *dn);
 /* parameter count (57121) and kernel launches so far (each optional) */

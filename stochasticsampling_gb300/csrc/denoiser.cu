@@ -3,25 +3,31 @@
 // low-particle-count histogram on the (x, y, phi) grid to an estimate of the
 // high-count distribution before the stress / Stokes solve.
 //
-// The 32 -> 32 convolutions are implicit GEMMs on the 5th-generation tensor
-// cores: per tile of 128 voxels, D[128 x 32] = sum over the 27 taps of
-// A_tap[128 x 32] * W_tap[32 x 32]^T with BF16 operands and an FP32
-// accumulator in tensor memory.  One elected thread issues tcgen05.mma
-// (M = 128, N = 32, K = 16, two per tap); the A rows of a tap (the periodic
-// neighbours of the tile's voxels, 64 bytes each, channels-last) are copied
-// into shared memory with cp.async into a 6-stage ring (3 taps in flight,
-// two CTAs per SM) whose reuse is gated by mbarriers that tcgen05.commit
-// arrives on; the 27 weight taps stay in
-// shared memory for the whole persistent CTA.  The epilogue reads the
+// Activations are BF16, channels last, in the layout [x][phi][y][32], so
+// that a line along y (the 128 voxels of one tile) is contiguous.  The
+// 32 -> 32 convolutions are implicit GEMMs on the 5th-generation tensor
+// cores: per tile (x, phi, 128 consecutive y), D[128 x 32] = sum over the 27
+// taps of A_tap[128 x 32] W_tap[32 x 32]^T, BF16 operands in shared memory,
+// FP32 accumulator in tensor memory, one elected thread issuing tcgen05.mma
+// (M = 128, N = 32, K = 16).  A CTA walks along phi: it keeps the lines
+// (x + dx, phi + dphi) of the current tile in a ring of 12 line buffers (3
+// x-planes x 4 positions along phi), each line with one halo row at either
+// end (130 rows), and loads only the 3 lines the next tile adds; the 27 taps
+// are descriptor offsets into those lines (the y shift is a 16-byte row
+// offset), so every activation row is read from global memory about 3 times
+// instead of 27.  Lines are copied with cp.async; a tile's 54 MMAs are issued
+// back to back and committed to an mbarrier.  The epilogue reads the
 // accumulator with tcgen05.ld (one voxel's 32 channels per thread), adds the
-// bias and applies ReLU (or the ReLU derivative of a reference tensor for
-// the backward pass) and stores channels-last.
+// bias and applies ReLU (or the ReLU derivative of a reference tensor, for
+// the backward pass).
 //
-// Shared-memory operand layout (K-major, no swizzle): core matrices of 8 rows
-// x 16 bytes; the 4 core matrices of a row group along K are contiguous
-// (leading-dimension offset 128 B), row groups are 512 B apart (stride
-// offset).  Every wait is bounded: on a timeout the kernel records an error,
-// waits for its own copies, frees its tensor memory and returns.
+// Shared-memory operand layouts (K-major, no swizzle).  A line: for each of
+// its 4 K chunks (8 channels, 16 bytes) the 130 rows at a 16-byte stride, so
+// row groups are 128 B apart (stride offset) and K chunks 2080 B (leading
+// offset).  Weights: per tap 32 rows x 4 chunks in 8 x 16 B core matrices,
+// leading offset 128 B, stride offset 512 B.  Every wait is bounded: on a
+// timeout the kernel records an error, waits for its own copies, frees its
+// tensor memory and returns.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -44,14 +50,15 @@ namespace {
 
 constexpr int kC = 32;                       // channels
 constexpr int kTaps = 27;                    // 3 x 3 x 3
-constexpr int kTileM = 128;                  // voxels per tile (MMA M)
-constexpr int kStages = 6;                   // A ring (two CTAs per SM)
-constexpr int kAhead = 3;                    // taps in flight: a stage is refilled 3 MMAs after its use
-constexpr int kAStage = kTileM * kC * 2;     // 8 KB
-constexpr int kBTap = kC * kC * 2;           // 2 KB
+constexpr int kTileM = 128;                  // voxels per tile (MMA M): one line segment along y
+constexpr int kBTap = kC * kC * 2;           // 2 KB of weights per tap
 constexpr int kBAll = kTaps * kBTap;         // 54 KB
-constexpr int kSmemTail = 8 * kStages + 8;   // the mbarriers, the tensor-memory slot and the failure flag
-constexpr int kSmemConv = kBAll + kStages * kAStage + ((kSmemTail + 127) / 128) * 128;
+constexpr int kLineRows = kTileM + 2;        // y = -1 .. 128 of a segment
+constexpr int kChunkBytes = kLineRows * 16;  // one 16-byte K chunk of every row of a line
+constexpr int kLineBytes = 4 * kChunkBytes;  // 8320 B
+constexpr int kSlots = 12;                   // 3 x-planes x 4 positions along phi
+constexpr int kPChunk = 4;                   // tiles along phi per work item
+constexpr int kSmemConv = kBAll + kSlots * kLineBytes + 128;  // + the mbarrier, tensor-memory slot, failure flag
 static_assert(kSmemConv <= 227 * 1024, "the convolution's shared memory exceeds a CTA's limit");
 constexpr uint32_t kWaitLimit = 1u << 22;    // mbarrier polls before giving up
 constexpr unsigned kErrTimeout = 1u;
@@ -64,19 +71,23 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-// voxel (x, y, p) <-> linear index (x ny + y) np + p.  A voxel's periodic
-// neighbour at tap = (dx + 1) 9 + (dy + 1) 3 + (dp + 1), from its
-// coordinates decoded once.
-struct Voxel {
+// A voxel (x, y, p) and its linear index in the activation layout
+// [x][phi][y] (every internal grid; the network's input and output are in
+// the histogram layout [x][y][phi], converted by k_dn_transpose).
+// moved(tap) is the periodic neighbour at tap = (dx + 1) 9 + (dy + 1) 3 + (dp + 1).
+struct Vox {
     int x, y, p;
-    __device__ __forceinline__ Voxel(int v, Dims d) : x(v / (d.np * d.ny)), y((v / d.np) % d.ny), p(v % d.np) {}
-    __device__ __forceinline__ int neighbour(int tap, Dims d) const {
+    __device__ __forceinline__ static Vox from_act(int a, Dims d) {
+        return Vox{a / (d.ny * d.np), a % d.ny, (a / d.ny) % d.np};
+    }
+    __device__ __forceinline__ Vox moved(int tap, Dims d) const {
         int a = x + tap / 9 - 1, b = y + (tap / 3) % 3 - 1, c = p + tap % 3 - 1;
         a = a < 0 ? a + d.nx : (a >= d.nx ? a - d.nx : a);
         b = b < 0 ? b + d.ny : (b >= d.ny ? b - d.ny : b);
         c = c < 0 ? c + d.np : (c >= d.np ? c - d.np : c);
-        return (a * d.ny + b) * d.np + c;
+        return Vox{a, b, c};
     }
+    __device__ __forceinline__ int act(Dims d) const { return (x * d.np + p) * d.ny + y; }
 };
 
 // ---- PTX wrappers ------------------------------------------------------
@@ -145,10 +156,11 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 }
 
-// shared-memory matrix descriptor: K-major, no swizzle, LBO 128 B, SBO 512 B
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(512u >> 4) << 32) |
-           (1ull << 46);
+// shared-memory matrix descriptor: K-major, no swizzle; lbo = byte offset
+// between K-adjacent core matrices, sbo = between 8-row groups
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 // instruction descriptor: D FP32, A and B BF16, both K-major, N = 32, M = 128
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kC >> 3) << 17) |
@@ -159,25 +171,26 @@ __host__ __device__ __forceinline__ int core_offset(int row, int k) {
     return (row >> 3) * 512 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
 }
 
-// MODE 0: bias + ReLU -> BF16; MODE 1: bias -> FP32; MODE 2: times ReLU'(ref) -> BF16
+// MODE 0: bias + ReLU -> BF16; MODE 1: bias -> FP32; MODE 2: times ReLU'(ref) -> BF16.
+// Work item = (x, y segment, kPChunk consecutive phi); ny a multiple of 128.
 template <int MODE>
 __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__restrict__ X,
                                                       const uint8_t *__restrict__ Wpacked,
                                                       const float *__restrict__ bias,
                                                       const __nv_bfloat16 *__restrict__ ref, void *__restrict__ Y,
-                                                      Dims d, int ntiles, unsigned *__restrict__ err) {
+                                                      Dims d, int nitems, unsigned *__restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *sB = smem;
-    uint8_t *sA = smem + kBAll;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(sA + kStages * kAStage);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + kStages);
+    uint8_t *sL = smem + kBAll;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(sL + kSlots * kLineBytes);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 1);
     volatile int *sfail = reinterpret_cast<volatile int *>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     for (int i = tid; i < kBAll / 16; i += kTileM)
         reinterpret_cast<uint4 *>(sB)[i] = reinterpret_cast<const uint4 *>(Wpacked)[i];
     if (tid == 0) {
-        for (int s = 0; s < kStages; ++s) mbar_init(smem_u32(&mbar[s]), 1);
+        mbar_init(smem_u32(mbar), 1);
         *sfail = 0;
         fence_mbar_init();
     }
@@ -187,97 +200,102 @@ __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__res
     __syncthreads();
     tc_after_sync();
     const uint32_t tmem = *tslot;
-    const uint32_t sA0 = smem_u32(sA), sB0 = smem_u32(sB);
-    const int row_off = (tid >> 3) * 512 + (tid & 7) * 16;  // this thread's row in an A stage
+    const uint32_t sL0 = smem_u32(sL), sB0 = smem_u32(sB);
+    const int nseg = d.ny / kTileM, npc = (d.np + kPChunk - 1) / kPChunk;
+    uint32_t phase = 0;
 
-    uint32_t it = 0;  // taps issued by this CTA (ring position)
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const Voxel vx(tile * kTileM + tid, d);
-        // copy the A rows of tap t into stage it % kStages, after the MMA
-        // that last read that stage has completed
-        auto load_tap = [&](int t, uint32_t pos) -> bool {
-            const uint32_t s = pos % kStages;
-            if (pos >= kStages && !mbar_wait(smem_u32(&mbar[s]), ((pos - kStages) / kStages) & 1u)) return false;
-            const uint8_t *src = reinterpret_cast<const uint8_t *>(X + (size_t)vx.neighbour(t, d) * kC);
-            const uint32_t dst = sA0 + s * kAStage + row_off;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) cp_async16(dst + j * 128, src + j * 16);
-            return true;
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const int pc = item % npc, ys = (item / npc) % nseg, x = item / (npc * nseg);
+        const int p0 = pc * kPChunk, pcount = min(kPChunk, d.np - p0), y0 = ys * kTileM;
+        // line (x + dx, p0 + q - 1) of this segment, rows y0 - 1 .. y0 + 128, into slot (dx + 1) 4 + q % 4
+        auto load_line = [&](int dx, int q) {
+            int xl = x + dx, pl = p0 + q - 1;
+            xl = xl < 0 ? xl + d.nx : (xl >= d.nx ? xl - d.nx : xl);
+            pl = ((pl % d.np) + d.np) % d.np;
+            const __nv_bfloat16 *line = X + (size_t)(xl * d.np + pl) * d.ny * kC;
+            const uint32_t dst0 = sL0 + (uint32_t)(((dx + 1) * 4 + (q & 3)) * kLineBytes);
+            for (int e = tid; e < kLineRows * 4; e += kTileM) {
+                const int r = e >> 2, j = e & 3;
+                int yl = y0 + r - 1;
+                yl = yl < 0 ? yl + d.ny : (yl >= d.ny ? yl - d.ny : yl);
+                cp_async16(dst0 + j * kChunkBytes + r * 16, line + (size_t)yl * kC + j * 8);
+            }
         };
-        // taps 0 .. kAhead - 1 in flight before the first MMA; then one new
-        // tap per MMA, kAhead ahead, into the stage the MMA kStages - kAhead
-        // taps back read (long complete, so the wait rarely stalls); empty
-        // groups past the last tap keep the group count uniform
-        const uint32_t base = it;
-        bool ok = true;
-        for (int q = 0; q < kAhead; ++q) {
-            ok = load_tap(q, base + q) && ok;
+        for (int q = 0; q < 3; ++q)
+            for (int dx = -1; dx <= 1; ++dx) load_line(dx, q);
+        cp_async_commit();
+        for (int k = 0; k < pcount; ++k) {
+            // the line the next tile adds goes where the line of tile k - 1's
+            // first phi row was (its MMAs completed before this iteration)
+            if (k + 3 <= pcount + 1)
+                for (int dx = -1; dx <= 1; ++dx) load_line(dx, k + 3);
             cp_async_commit();
-        }
-        for (int t = 0; t < kTaps; ++t) {
-            const int tn = t + kAhead;
-            if (tn < kTaps) ok = load_tap(tn, base + tn) && ok;
-            cp_async_commit();
-            cp_async_wait<kAhead>();  // tap t has landed
-            if (!ok) *sfail = 1;
+            cp_async_wait<1>();  // the lines of tile k have landed
             fence_proxy_async();
             __syncthreads();
             if (*sfail) break;
             if (tid == 0) {
                 tc_after_sync();
-                const uint32_t s = it % kStages;
+                uint32_t acc = 0;
+                for (int dx = -1; dx <= 1; ++dx)
+                    for (int dp = -1; dp <= 1; ++dp) {
+                        const uint32_t line = sL0 + (uint32_t)(((dx + 1) * 4 + ((k + 1 + dp) & 3)) * kLineBytes);
 #pragma unroll
-                for (int kk = 0; kk < 2; ++kk) {
-                    const uint64_t ad = smem_desc(sA0 + s * kAStage + kk * 256);
-                    const uint64_t bd = smem_desc(sB0 + t * kBTap + kk * 256);
-                    mma_bf16(tmem, ad, bd, kIdesc, (t > 0 || kk > 0) ? 1u : 0u);
-                }
-                mma_commit(smem_u32(&mbar[s]));
+                        for (int dy = -1; dy <= 1; ++dy) {
+                            const int tap = (dx + 1) * 9 + (dy + 1) * 3 + (dp + 1);
+#pragma unroll
+                            for (int kk = 0; kk < 2; ++kk) {
+                                const uint64_t ad = smem_desc(line + kk * 2 * kChunkBytes + (1 + dy) * 16, kChunkBytes, 128);
+                                const uint64_t bd = smem_desc(sB0 + tap * kBTap + kk * 256, 128, 512);
+                                mma_bf16(tmem, ad, bd, kIdesc, acc);
+                                acc = 1;
+                            }
+                        }
+                    }
+                mma_commit(smem_u32(mbar));
             }
-            ++it;
-        }
-        __syncthreads();
-        if (*sfail) break;
-        // the accumulator is complete when the tile's last MMA has completed
-        const uint32_t last = it - 1;
-        if (!mbar_wait(smem_u32(&mbar[last % kStages]), (last / kStages) & 1u)) *sfail = 1;
-        __syncthreads();
-        if (*sfail) break;
-        tc_after_sync();
-        uint32_t r[32];
-        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), r);
-        const int vo = tile * kTileM + warp * 32 + lane;  // this thread's accumulator row
-        if (MODE == 1) {
-            float4 *out = reinterpret_cast<float4 *>(reinterpret_cast<float *>(Y) + (size_t)vo * kC);
+            if (!mbar_wait(smem_u32(mbar), phase)) *sfail = 1;
+            phase ^= 1u;
+            __syncthreads();
+            if (*sfail) break;
+            tc_after_sync();
+            uint32_t r[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), r);
+            const size_t vo = (size_t)((x * d.np + p0 + k) * d.ny + y0 + warp * 32 + lane);  // this thread's row
+            if (MODE == 1) {
+                float4 *out = reinterpret_cast<float4 *>(reinterpret_cast<float *>(Y) + vo * kC);
 #pragma unroll
-            for (int q = 0; q < 8; ++q)
-                out[q] = make_float4(__uint_as_float(r[4 * q]) + bias[4 * q], __uint_as_float(r[4 * q + 1]) + bias[4 * q + 1],
-                                     __uint_as_float(r[4 * q + 2]) + bias[4 * q + 2],
-                                     __uint_as_float(r[4 * q + 3]) + bias[4 * q + 3]);
-        } else {
-            uint32_t packed[16];
-            const __nv_bfloat16 *rr = ref + (size_t)vo * kC;
+                for (int q = 0; q < 8; ++q)
+                    out[q] = make_float4(__uint_as_float(r[4 * q]) + bias[4 * q],
+                                         __uint_as_float(r[4 * q + 1]) + bias[4 * q + 1],
+                                         __uint_as_float(r[4 * q + 2]) + bias[4 * q + 2],
+                                         __uint_as_float(r[4 * q + 3]) + bias[4 * q + 3]);
+            } else {
+                uint32_t packed[16];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                float a = __uint_as_float(r[2 * q]), b = __uint_as_float(r[2 * q + 1]);
-                if (MODE == 0) {
-                    a = fmaxf(a + bias[2 * q], 0.f);
-                    b = fmaxf(b + bias[2 * q + 1], 0.f);
-                } else {
-                    a = __bfloat162float(rr[2 * q]) > 0.f ? a : 0.f;
-                    b = __bfloat162float(rr[2 * q + 1]) > 0.f ? b : 0.f;
+                for (int q = 0; q < 16; ++q) {
+                    float a = __uint_as_float(r[2 * q]), b = __uint_as_float(r[2 * q + 1]);
+                    if (MODE == 0) {
+                        a = fmaxf(a + bias[2 * q], 0.f);
+                        b = fmaxf(b + bias[2 * q + 1], 0.f);
+                    } else {
+                        const __nv_bfloat16 *rr = ref + vo * kC;
+                        a = __bfloat162float(rr[2 * q]) > 0.f ? a : 0.f;
+                        b = __bfloat162float(rr[2 * q + 1]) > 0.f ? b : 0.f;
+                    }
+                    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+                    packed[q] = *reinterpret_cast<uint32_t *>(&h);
                 }
-                __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-                packed[q] = *reinterpret_cast<uint32_t *>(&h);
-            }
-            uint4 *out = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(Y) + (size_t)vo * kC);
+                uint4 *out = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(Y) + vo * kC);
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-                out[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+                for (int q = 0; q < 4; ++q)
+                    out[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+            }
+            // every thread's tensor-memory reads finish before the next tile's MMAs overwrite it
+            tc_before_sync();
+            __syncthreads();
         }
-        // every thread's tensor-memory reads finish before the next tile's MMAs overwrite it
-        tc_before_sync();
-        __syncthreads();
+        if (*sfail) break;
     }
     if (*sfail && tid == 0) atomicOr(err, kErrTimeout);
     cp_async_wait<0>();
@@ -300,6 +318,9 @@ __global__ void k_pack_weights(const float *__restrict__ W, uint8_t *__restrict_
 }
 
 int g_sms = 0;
+
+// work items of the convolution: (x, y segment of 128, kPChunk positions along phi)
+int conv_items(Dims d) { return d.nx * (d.ny / kTileM) * ((d.np + kPChunk - 1) / kPChunk); }
 
 // ---- the network's CUDA-core layers -----------------------------------
 // Parameters (FP32, one array): w_in[27][32], b_in[32], w2[27][32][32],
@@ -334,20 +355,41 @@ __device__ __forceinline__ void load_bf16x32(const __nv_bfloat16 *src, float (&a
     }
 }
 
+// FP32 grids between the histogram layout [x][y][phi] and the activation
+// layout [x][phi][y]: per plane x a transpose in 32 x 32 tiles
+template <bool TO_ACT>
+__global__ void k_dn_transpose(const float *__restrict__ src, float *__restrict__ dst, Dims d) {
+    __shared__ float t[32][33];
+    const int R = TO_ACT ? d.ny : d.np, Cn = TO_ACT ? d.np : d.ny;  // source rows, columns
+    const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+    const float *sp = src + (size_t)blockIdx.z * d.ny * d.np;
+    float *op = dst + (size_t)blockIdx.z * d.ny * d.np;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int r = r0 + i, c = c0 + threadIdx.x;
+        if (r < R && c < Cn) t[i][threadIdx.x] = sp[(size_t)r * Cn + c];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int c = c0 + i, r = r0 + threadIdx.x;
+        if (c < Cn && r < R) op[(size_t)c * R + r] = t[threadIdx.x][i];
+    }
+}
+
 // input layer 1 -> 32 channels, ReLU: A1[v] = ReLU(b_in + sum_tap w_in[tap] x[nbr(v, tap)])
+// (x in the activation layout)
 __global__ void __launch_bounds__(128) k_dn_in(const float *__restrict__ x, const float *__restrict__ P,
                                                __nv_bfloat16 *__restrict__ A1, Dims d, int nvox) {
     __shared__ float sw[kTaps * kC + kC];
     for (int i = threadIdx.x; i < kTaps * kC + kC; i += blockDim.x) sw[i] = P[kOffWin + i];
     __syncthreads();
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;  // activation index
     if (v >= nvox) return;
-    const Voxel vx(v, d);
+    const Vox vx = Vox::from_act(v, d);
     float a[32];
 #pragma unroll
     for (int c = 0; c < kC; ++c) a[c] = sw[kTaps * kC + c];
     for (int t = 0; t < kTaps; ++t) {
-        const float xv = x[vx.neighbour(t, d)];
+        const float xv = x[vx.moved(t, d).act(d)];
 #pragma unroll
         for (int c = 0; c < kC; ++c) a[c] = fmaf(sw[t * kC + c], xv, a[c]);
     }
@@ -357,22 +399,33 @@ __global__ void __launch_bounds__(128) k_dn_in(const float *__restrict__ x, cons
 }
 
 // output layer 32 -> 1 with the residual: y[v] = x[v] + b_out + sum_tap w_out[tap] . A3[nbr(v, tap)]
+// (x and y in the activation layout).  Four threads per voxel, 8 channels
+// each (one 16-byte load per tap), summed with two shuffles.
 __global__ void __launch_bounds__(128) k_dn_out(const __nv_bfloat16 *__restrict__ A3, const float *__restrict__ x,
                                                 const float *__restrict__ P, float *__restrict__ y, Dims d, int nvox) {
     __shared__ float sw[kTaps * kC + 1];
     for (int i = threadIdx.x; i < kTaps * kC + 1; i += blockDim.x) sw[i] = P[kOffWout + i];
     __syncthreads();
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nvox) return;
-    const Voxel vx(v, d);
-    float acc = sw[kTaps * kC];
-    for (int t = 0; t < kTaps; ++t) {
-        float a[32];
-        load_bf16x32(A3 + (size_t)vx.neighbour(t, d) * kC, a);
+    const int g = blockIdx.x * blockDim.x + threadIdx.x, v = g >> 2, q = g & 3;
+    const bool live = v < nvox;
+    float acc = 0.f;
+    if (live) {
+        const Vox vx = Vox::from_act(v, d);
+        for (int t = 0; t < kTaps; ++t) {
+            const uint4 u = *reinterpret_cast<const uint4 *>(A3 + (size_t)vx.moved(t, d).act(d) * kC + 8 * q);
+            const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+            const float *wt = sw + t * kC + 8 * q;
 #pragma unroll
-        for (int c = 0; c < kC; ++c) acc = fmaf(sw[t * kC + c], a[c], acc);
+            for (int j = 0; j < 4; ++j) {
+                const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162 *>(&w[j]);
+                acc = fmaf(wt[2 * j], __low2float(h), acc);
+                acc = fmaf(wt[2 * j + 1], __high2float(h), acc);
+            }
+        }
     }
-    y[v] = x[v] + acc;
+    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+    if (live && q == 0) y[v] = x[v] + acc + sw[kTaps * kC];
 }
 
 // mean-square loss against the target and its gradient dy = 2 (y - t) / V;
@@ -406,14 +459,14 @@ __global__ void __launch_bounds__(128) k_dn_out_bwd(const float *__restrict__ dy
     __shared__ float sw[kTaps * kC];
     for (int i = threadIdx.x; i < kTaps * kC; i += blockDim.x) sw[i] = P[kOffWout + i];
     __syncthreads();
-    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;  // activation index
     if (u >= nvox) return;
-    const Voxel vx(u, d);
+    const Vox vx = Vox::from_act(u, d);
     float g[32];
 #pragma unroll
     for (int c = 0; c < kC; ++c) g[c] = 0.f;
     for (int t = 0; t < kTaps; ++t) {
-        const float dv = dy[vx.neighbour(kTaps - 1 - t, d)];
+        const float dv = dy[vx.moved(kTaps - 1 - t, d).act(d)];
 #pragma unroll
         for (int c = 0; c < kC; ++c) g[c] = fmaf(sw[t * kC + c], dv, g[c]);
     }
@@ -457,8 +510,8 @@ __global__ void __launch_bounds__(128) k_dn_wgrad_c1(const __nv_bfloat16 *__rest
     for (int i = tid; i < kTaps * kC + kC; i += blockDim.x) acc[i] = 0.f;
     __syncthreads();
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int v = tile * kTileM + tid;
-        const Voxel vx(v, d);
+        const int v = tile * kTileM + tid;  // activation index
+        const Vox vx = Vox::from_act(v, d);
         float own[32];
         float s_own = 0.f;
         if (OUT) {
@@ -471,14 +524,14 @@ __global__ void __launch_bounds__(128) k_dn_wgrad_c1(const __nv_bfloat16 *__rest
             atomicAdd(&acc[kTaps * kC + lane], warp_reduce_scatter32(t));
         }
         for (int tap = 0; tap < kTaps; ++tap) {
-            const int u = vx.neighbour(tap, d);
+            const Vox u = vx.moved(tap, d);
             float p[32];
             if (OUT) {
-                load_bf16x32(S + (size_t)u * kC, p);
+                load_bf16x32(S + (size_t)u.act(d) * kC, p);
 #pragma unroll
                 for (int c = 0; c < kC; ++c) p[c] *= s_own;
             } else {
-                const float xs = sv[u];
+                const float xs = sv[u.act(d)];
 #pragma unroll
                 for (int c = 0; c < kC; ++c) p[c] = own[c] * xs;
             }
@@ -509,8 +562,8 @@ __global__ void __launch_bounds__(256) k_dn_wgrad32(const __nv_bfloat16 *__restr
     const int r = tid >> 1, h = tid & 1;
     const bool centre = tap == kTaps / 2 && ib == 0;  // these threads also sum dZ (the bias gradient)
     for (int tile = blockIdx.y; tile < ntiles; tile += gridDim.y) {
-        const int v = tile * kTileM + r;
-        const int u = Voxel(v, d).neighbour(tap, d);
+        const int v = tile * kTileM + r;  // activation indices
+        const int u = Vox::from_act(v, d).moved(tap, d).act(d);
         const uint4 *zs = reinterpret_cast<const uint4 *>(dZ + (size_t)v * kC + 16 * h);
         const uint4 *as = reinterpret_cast<const uint4 *>(A + (size_t)u * kC + 16 * h);
 #pragma unroll
@@ -583,8 +636,8 @@ extern "C" int ss_dn_conv32(const void *x, const float *w, const float *bias, co
                             uint32_t nx, uint32_t ny, uint32_t np, uint32_t mode, void *stream) {
     char buf[256];
     if (!x || !w || !y || (mode != 2 && !bias) || (mode == 2 && !ref) || mode > 2 || nx < 1 || ny < 1 || np < 1 ||
-        ((unsigned long long)nx * ny * np) % kTileM != 0 || (unsigned long long)nx * ny * np > (1ull << 30)) {
-        ss::record_error("ss_dn_conv32: null pointer, mode > 2, or voxel count not a positive multiple of 128");
+        ny % kTileM != 0 || (unsigned long long)nx * ny * np > (1ull << 27)) {
+        ss::record_error("ss_dn_conv32: null pointer, mode > 2, or ny not a positive multiple of 128");
         return SS_ERR_INVALID_ARGUMENT;
     }
     cudaStream_t s = (cudaStream_t)stream;
@@ -607,14 +660,13 @@ extern "C" int ss_dn_conv32(const void *x, const float *w, const float *bias, co
         const int nw = kTaps * kC * kC;
         if (mode == 2) k_pack_weights<true><<<(nw + 255) / 256, 256, 0, s>>>(w, packed);
         else k_pack_weights<false><<<(nw + 255) / 256, 256, 0, s>>>(w, packed);
-        const int ntiles = (int)(((unsigned long long)nx * ny * np) / kTileM);
-        const int grid = ntiles < 2 * g_sms ? ntiles : 2 * g_sms;
         Dims d{(int)nx, (int)ny, (int)np};
+        const int items = conv_items(d), grid = items < g_sms ? items : g_sms;
         const __nv_bfloat16 *X = reinterpret_cast<const __nv_bfloat16 *>(x);
         const __nv_bfloat16 *R = reinterpret_cast<const __nv_bfloat16 *>(ref);
-        if (mode == 0) k_conv32<0><<<grid, kTileM, kSmemConv, s>>>(X, packed, bias, R, y, d, ntiles, derr);
-        else if (mode == 1) k_conv32<1><<<grid, kTileM, kSmemConv, s>>>(X, packed, bias, R, y, d, ntiles, derr);
-        else k_conv32<2><<<grid, kTileM, kSmemConv, s>>>(X, packed, bias, R, y, d, ntiles, derr);
+        if (mode == 0) k_conv32<0><<<grid, kTileM, kSmemConv, s>>>(X, packed, bias, R, y, d, items, derr);
+        else if (mode == 1) k_conv32<1><<<grid, kTileM, kSmemConv, s>>>(X, packed, bias, R, y, d, items, derr);
+        else k_conv32<2><<<grid, kTileM, kSmemConv, s>>>(X, packed, bias, R, y, d, items, derr);
         e = cudaGetLastError();
     }
     unsigned herr = 0;
@@ -677,7 +729,9 @@ struct ss_dn {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int device = 0;
-    float *P = nullptr, *G = nullptr, *M = nullptr, *S = nullptr, *dy = nullptr, *yb = nullptr;
+    // dy, yb, xa, ta: FP32 grids in the activation layout
+    float *P = nullptr, *G = nullptr, *M = nullptr, *S = nullptr, *dy = nullptr, *yb = nullptr, *xa = nullptr,
+          *ta = nullptr;
     uint8_t *Wp2 = nullptr, *Wp3 = nullptr, *Wm2 = nullptr, *Wm3 = nullptr;
     __nv_bfloat16 *A1 = nullptr, *A2 = nullptr, *A3 = nullptr, *D1 = nullptr, *D2 = nullptr;
     double *sums = nullptr;
@@ -715,8 +769,8 @@ void conv_attrs() {
 template <int MODE>
 void launch_conv(ss_dn *n, const __nv_bfloat16 *X, const uint8_t *W, const float *bias, const __nv_bfloat16 *ref,
                  void *Y, cudaStream_t s) {
-    const int grid = n->ntiles < 2 * n->sms ? n->ntiles : 2 * n->sms;
-    k_conv32<MODE><<<grid, kTileM, kSmemConv, s>>>(X, W, bias, ref, Y, n->d, n->ntiles, n->err);
+    const int items = conv_items(n->d), grid = items < n->sms ? items : n->sms;
+    k_conv32<MODE><<<grid, kTileM, kSmemConv, s>>>(X, W, bias, ref, Y, n->d, items, n->err);
 }
 
 void pack_all(ss_dn *n, cudaStream_t s) {
@@ -728,30 +782,46 @@ void pack_all(ss_dn *n, cudaStream_t s) {
     n->launches += 4;
 }
 
-void enqueue_forward(ss_dn *n, const float *x, float *y, cudaStream_t s) {
+template <bool TO_ACT>
+void transpose(ss_dn *n, const float *src, float *dst, cudaStream_t s) {
+    const int R = TO_ACT ? n->d.ny : n->d.np, Cn = TO_ACT ? n->d.np : n->d.ny;
+    k_dn_transpose<TO_ACT><<<dim3((Cn + 31) / 32, (R + 31) / 32, n->d.nx), dim3(32, 8), 0, s>>>(src, dst, n->d);
+}
+
+// the network on x (histogram layout), output ya in the activation layout
+void enqueue_forward_act(ss_dn *n, const float *x, float *ya, cudaStream_t s) {
     const unsigned b = (unsigned)((n->nvox + 127) / 128);
-    k_dn_in<<<b, 128, 0, s>>>(x, n->P, n->A1, n->d, n->nvox);
+    transpose<true>(n, x, n->xa, s);
+    k_dn_in<<<b, 128, 0, s>>>(n->xa, n->P, n->A1, n->d, n->nvox);
     launch_conv<0>(n, n->A1, n->Wp2, n->P + kOffB2, nullptr, n->A2, s);
     launch_conv<0>(n, n->A2, n->Wp3, n->P + kOffB3, nullptr, n->A3, s);
-    k_dn_out<<<b, 128, 0, s>>>(n->A3, x, n->P, y, n->d, n->nvox);
-    n->launches += 4;
+    k_dn_out<<<4 * b, 128, 0, s>>>(n->A3, n->xa, n->P, ya, n->d, n->nvox);
+    n->launches += 5;
+}
+
+void enqueue_forward(ss_dn *n, const float *x, float *y, cudaStream_t s) {
+    enqueue_forward_act(n, x, n->yb, s);
+    transpose<false>(n, n->yb, y, s);
+    n->launches += 1;
 }
 
 // loss of y against t, then the gradients of every parameter (accumulated into G)
-void enqueue_backward(ss_dn *n, const float *x, const float *t, const float *y, cudaStream_t s, bool grads) {
+// (after enqueue_forward_act: n->xa holds the input, ya the output, both in the activation layout)
+void enqueue_backward(ss_dn *n, const float *t, const float *ya, cudaStream_t s, bool grads) {
     const unsigned b = (unsigned)((n->nvox + 127) / 128);
-    k_dn_loss<<<2 * n->sms, 256, 0, s>>>(y, t, n->dy, n->nvox, n->sums, grads ? n->G + kOffBout : nullptr);
-    n->launches += 1;
+    transpose<true>(n, t, n->ta, s);
+    k_dn_loss<<<2 * n->sms, 256, 0, s>>>(ya, n->ta, n->dy, n->nvox, n->sums, grads ? n->G + kOffBout : nullptr);
+    n->launches += 2;
     if (!grads) return;
     const dim3 wg(kTaps, (unsigned)(n->sms > 0 ? (4 * n->sms + kTaps - 1) / kTaps : 8));
-    const unsigned pg = (unsigned)(n->ntiles < 2 * n->sms ? n->ntiles : 2 * n->sms);
+    const unsigned pg = (unsigned)(n->ntiles < 8 * n->sms ? n->ntiles : 8 * n->sms);
     k_dn_out_bwd<<<b, 128, 0, s>>>(n->dy, n->P, n->A3, n->D1, n->d, n->nvox);
     k_dn_wgrad_c1<true><<<pg, 128, 0, s>>>(n->A3, n->dy, n->G + kOffWout, nullptr, n->d, n->ntiles);
     k_dn_wgrad32<<<wg, 256, 0, s>>>(n->D1, n->A2, n->G + kOffW3, n->G + kOffB3, n->d, n->ntiles);
     launch_conv<2>(n, n->D1, n->Wm3, nullptr, n->A2, n->D2, s);
     k_dn_wgrad32<<<wg, 256, 0, s>>>(n->D2, n->A1, n->G + kOffW2, n->G + kOffB2, n->d, n->ntiles);
     launch_conv<2>(n, n->D2, n->Wm2, nullptr, n->A1, n->D1, s);
-    k_dn_wgrad_c1<false><<<pg, 128, 0, s>>>(n->D1, x, n->G + kOffWin, n->G + kOffBin, n->d, n->ntiles);
+    k_dn_wgrad_c1<false><<<pg, 128, 0, s>>>(n->D1, n->xa, n->G + kOffWin, n->G + kOffBin, n->d, n->ntiles);
     n->launches += 8;
 }
 
@@ -768,6 +838,7 @@ void destroy_dn(ss_dn *n) {
     cudaSetDevice(n->device);
     if (n->stream) cudaStreamSynchronize(n->stream);
     cudaFree(n->P); cudaFree(n->G); cudaFree(n->M); cudaFree(n->S); cudaFree(n->dy); cudaFree(n->yb);
+    cudaFree(n->xa); cudaFree(n->ta);
     cudaFree(n->Wp2); cudaFree(n->Wp3); cudaFree(n->Wm2); cudaFree(n->Wm3);
     cudaFree(n->A1); cudaFree(n->A2); cudaFree(n->A3); cudaFree(n->D1); cudaFree(n->D2);
     cudaFree(n->sums); cudaFree(n->err);
@@ -783,9 +854,9 @@ int ss_dn_create(uint32_t nx, uint32_t ny, uint32_t np, uint64_t seed, void *str
     if (!out) return dnfail(SS_ERR_INVALID_ARGUMENT, "ss_dn_create: null output");
     *out = nullptr;
     const unsigned long long V = (unsigned long long)nx * ny * np;
-    if (nx < 1 || ny < 1 || np < 1 || V % kTileM != 0 || V > (1ull << 27))
+    if (nx < 1 || ny < 1 || np < 1 || ny % kTileM != 0 || V > (1ull << 27))
         return dnfail(SS_ERR_INVALID_ARGUMENT,
-                      "ss_dn_create: the voxel count nx ny np must be a positive multiple of 128 (at most 2^27)");
+                      "ss_dn_create: ny must be a positive multiple of 128 (at most 2^27 voxels)");
     ss_dn *n = new ss_dn();
     n->d = Dims{(int)nx, (int)ny, (int)np};
     n->nvox = (int)V;
@@ -806,6 +877,7 @@ int ss_dn_create(uint32_t nx, uint32_t ny, uint32_t np, uint64_t seed, void *str
     const size_t pb = (size_t)kParams * sizeof(float), ab = (size_t)V * kC * sizeof(__nv_bfloat16);
     A((void **)&n->P, pb); A((void **)&n->G, pb); A((void **)&n->M, pb); A((void **)&n->S, pb);
     A((void **)&n->dy, V * sizeof(float)); A((void **)&n->yb, V * sizeof(float));
+    A((void **)&n->xa, V * sizeof(float)); A((void **)&n->ta, V * sizeof(float));
     A((void **)&n->Wp2, kBAll); A((void **)&n->Wp3, kBAll); A((void **)&n->Wm2, kBAll); A((void **)&n->Wm3, kBAll);
     A((void **)&n->A1, ab); A((void **)&n->A2, ab); A((void **)&n->A3, ab); A((void **)&n->D1, ab);
     A((void **)&n->D2, ab);
@@ -891,8 +963,8 @@ int ss_dn_train(ss_dn *n, const float *x, const float *t, uint32_t batch, float 
     if (update) DCK(cudaMemsetAsync(n->G, 0, (size_t)kParams * sizeof(float), n->stream));
     for (uint32_t b = 0; b < batch; ++b) {
         const float *xb = x + (size_t)b * n->nvox, *tb = t + (size_t)b * n->nvox;
-        enqueue_forward(n, xb, n->yb, n->stream);
-        enqueue_backward(n, xb, tb, n->yb, n->stream, update);
+        enqueue_forward_act(n, xb, n->yb, n->stream);
+        enqueue_backward(n, tb, n->yb, n->stream, update);
     }
     if (update) {
         n->adam_t += 1;
@@ -921,8 +993,8 @@ int ss_dn_gradients(ss_dn *n, const float *x, const float *t, uint32_t batch, fl
     DCK(cudaMemsetAsync(n->G, 0, (size_t)kParams * sizeof(float), n->stream));
     for (uint32_t b = 0; b < batch; ++b) {
         const float *xb = x + (size_t)b * n->nvox, *tb = t + (size_t)b * n->nvox;
-        enqueue_forward(n, xb, n->yb, n->stream);
-        enqueue_backward(n, xb, tb, n->yb, n->stream, true);
+        enqueue_forward_act(n, xb, n->yb, n->stream);
+        enqueue_backward(n, tb, n->yb, n->stream, true);
     }
     DCK(cudaGetLastError());
     std::vector<float> g(kParams);
@@ -965,7 +1037,7 @@ void dn_shape(const ss_dn *n, int *nx, int *ny, int *np) {
 }
 int dn_enqueue_forward(ss_dn *n, const float *x, float *y, cudaStream_t s) {
     enqueue_forward(n, x, y, s);
-    return 4;
+    return 6;
 }
 int dn_status(ss_dn *n, cudaStream_t s) {
     unsigned h = 0;
