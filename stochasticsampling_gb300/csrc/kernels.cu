@@ -41,6 +41,25 @@ __device__ __forceinline__ double kval(int i, int n, double step) {
 // particle ingest / egest / binning
 // ------------------------------------------------------------------------
 
+// Validation of caller rows [n][5] on the device (integer tests on the bits):
+// scan[0] = the first particle with a non-finite coordinate (atomicMin; left
+// at ~0 when there is none), scan[1] |= 1 when a particle is outside the
+// canonical quasi2d state z = 0, theta = pi/2.
+__global__ void k_scan_rows(const double *__restrict__ aos, unsigned long long n,
+                            unsigned long long *__restrict__ scan) {
+    const unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    bool bad = false, noncanon = false;
+    if (i < n) {
+        const unsigned long long *b = reinterpret_cast<const unsigned long long *>(aos + 5 * i);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) bad |= ((b[k] >> 52) & 0x7FFull) == 0x7FFull;
+        const unsigned long long half_pi = (unsigned long long)__double_as_longlong(kPiHalf);
+        noncanon = (b[2] << 1) != 0ull || b[4] != half_pi;
+    }
+    if (bad) atomicMin(&scan[0], i);
+    if (__any_sync(0xffffffffu, noncanon) && (threadIdx.x & 31) == 0) atomicOr(&scan[1], 1ull);
+}
+
 // Particle::new (src/particle.rs:186-201): modulo on positions and ang_pbc on
 // angles, then pbc once more; AoS [n][5] -> SoA.
 __global__ void k_ingest(const double *__restrict__ aos, unsigned long long n, DevParams P, double *__restrict__ x,
@@ -493,6 +512,10 @@ __global__ void k_langevin_args(const double *__restrict__ in, unsigned long lon
 // launch wrappers
 // ========================================================================
 static inline unsigned nblocks(unsigned long long n, unsigned bs) { return (unsigned)((n + bs - 1) / bs); }
+
+void launch_scan_rows(cudaStream_t s, const double *aos, unsigned long long n, unsigned long long *scan) {
+    if (n) k_scan_rows<<<nblocks(n, 256), 256, 0, s>>>(aos, n, scan);
+}
 
 void launch_ingest(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P, double *const xs[5],
                    uint32_t *id) {

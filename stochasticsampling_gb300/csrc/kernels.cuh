@@ -7,6 +7,7 @@
 
 namespace ss {
 
+void launch_scan_rows(cudaStream_t s, const double *aos, unsigned long long n, unsigned long long *scan);
 void launch_ingest(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P, double *const xs[5],
                    uint32_t *id);
 void launch_egest(cudaStream_t s, unsigned long long n, double *const xs[5], const uint32_t *id, double *aos);

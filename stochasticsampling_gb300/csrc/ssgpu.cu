@@ -69,6 +69,7 @@ struct ss_ctx {
     double *staging = nullptr, *noise_dev = nullptr, *dist_dev = nullptr, *realbuf = nullptr;
     unsigned long long *d_step = nullptr;
     uint32_t *d_err = nullptr;
+    unsigned long long *d_scan = nullptr;  // row validation: first non-finite particle, non-canonical flag
     double *d_halfpi = nullptr;
 
     // FP32 mixed-precision mode (SS_FLAG_MIXED)
@@ -475,7 +476,7 @@ static void destroy_impl(ss_ctx *c) {
     }
     cudaFree(c->fwd); cudaFree(c->inv); cudaFree(c->table); cudaFree(c->cellcount); cudaFree(c->cursor);
     cudaFree(c->kern); cudaFree(c->lut); cudaFree(c->staging); cudaFree(c->noise_dev); cudaFree(c->dist_dev);
-    cudaFree(c->realbuf); cudaFree(c->d_step); cudaFree(c->d_err); cudaFree(c->d_halfpi);
+    cudaFree(c->realbuf); cudaFree(c->d_step); cudaFree(c->d_err); cudaFree(c->d_scan); cudaFree(c->d_halfpi);
     for (auto &kv : c->plans_c) cufftDestroy(kv.second);
     for (int b = 0; b < 2; ++b)
         for (int k = 0; k < 2; ++k) cudaFree(c->pa[b][k]);
@@ -660,6 +661,7 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     if (rc == SS_OK) rc = alloc((void **)&c->staging, 5 * N * sizeof(double));
     if (rc == SS_OK) rc = alloc((void **)&c->d_step, sizeof(unsigned long long));
     if (rc == SS_OK) rc = alloc((void **)&c->d_err, sizeof(uint32_t));
+    if (rc == SS_OK) rc = alloc((void **)&c->d_scan, 2 * sizeof(unsigned long long));
     if (rc == SS_OK) rc = alloc((void **)&c->d_halfpi, 2 * sizeof(double));
     if (c->mixed) {
         if (rc == SS_OK) rc = alloc((void **)&c->fwd_f, 12 * ncell * sizeof(float2));
@@ -738,16 +740,20 @@ static int load_particles(ss_ctx *c, const double *particles, uint64_t n) {
                     "Given initial condition has not the same number of particles (%llu) as given in the "
                     "parameter file (%llu).",
                     (unsigned long long)n, (unsigned long long)c->P.n);
-    for (uint64_t i = 0; i < 5 * n; ++i)
-        if (!is_finite(particles[i]))
-            return fail(c, SS_ERR_INVALID_ARGUMENT, "particle %llu has a non-finite coordinate",
-                        (unsigned long long)(i / 5));
     CK(cudaSetDevice(c->device));
     CK(cudaMemcpyAsync(c->staging, particles, 5 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    bool canon = c->q2d;
-    for (uint64_t i = 0; c->mixed && canon && i < n; ++i)
-        canon = particles[5 * i + 2] == 0.0 && particles[5 * i + 4] == kPiHalf;
-    return ingest_staging(c, n, canon);
+    // the rows are checked on the device (finite; canonical quasi2d state)
+    // before they replace the particle state
+    static const unsigned long long scan_init[2] = {~0ull, 0ull};
+    unsigned long long scan[2];
+    CK(cudaMemcpyAsync(c->d_scan, scan_init, sizeof scan_init, cudaMemcpyHostToDevice, c->stream));
+    launch_scan_rows(c->stream, c->staging, n, c->d_scan);
+    CKR(check_launch(c, "scan_rows"));
+    CK(cudaMemcpyAsync(scan, c->d_scan, sizeof scan, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (scan[0] != ~0ull)
+        return fail(c, SS_ERR_INVALID_ARGUMENT, "particle %llu has a non-finite coordinate", scan[0]);
+    return ingest_staging(c, n, c->q2d && scan[1] == 0ull);
 }
 
 // the rows in `staging` become the particle state: Particle::new, then the
