@@ -79,18 +79,22 @@ __device__ __forceinline__ void philox_noise_f(unsigned long long seed, uint32_t
     uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
     uint32_t tl = (uint32_t)t, th = (uint32_t)(t >> 32);
     uint4 r0 = philox4x32_10(make_uint4(id, tl, th, 0u), key);
-    float rad = sqrtf(-2.0f * logf(1.0f - u24(r0.x)));
+    // the noise needs only statistical accuracy: the hardware approximations
+    // (__logf: relative error ~2^-21 on (2^-24, 1]; __sincosf: absolute
+    // error ~2^-21 on [-pi, pi], where the angles are drawn)
+    constexpr float kTwoPiF = 6.28318530717958647692f;
+    float rad = sqrtf(-2.0f * __logf(1.0f - u24(r0.x)));
     float s, c;
-    sincospif(2.0f * u24(r0.y), &s, &c);
+    __sincosf(kTwoPiF * (u24(r0.y) - 0.5f), &s, &c);
     xi[0] = rad * c;
     xi[1] = rad * s;
-    sincospif(2.0f * u24(r0.z), &sa, &ca);
-    rot = sigma * sqrtf(-2.0f * logf(1.0f - u24(r0.w)));
+    __sincosf(kTwoPiF * (u24(r0.z) - 0.5f), &sa, &ca);
+    rot = sigma * sqrtf(-2.0f * __logf(1.0f - u24(r0.w)));
     if (Q2D) {
         xi[2] = 0.f;
     } else {
         uint4 r1 = philox4x32_10(make_uint4(id, tl, th, 1u), key);
-        xi[2] = sqrtf(-2.0f * logf(1.0f - u24(r1.x))) * cospif(2.0f * u24(r1.y));
+        xi[2] = sqrtf(-2.0f * __logf(1.0f - u24(r1.x))) * __cosf(kTwoPiF * (u24(r1.y) - 0.5f));
     }
 }
 
