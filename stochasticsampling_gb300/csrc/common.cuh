@@ -290,37 +290,104 @@ __device__ __forceinline__ void philox_noise(unsigned long long seed, uint32_t i
     }
 }
 
-// sin r and cos r - 1.  For |r| <= 0.8 (every rotation angle below 8
-// sigma at sigma = 0.1) by their Taylor series to r^17 and r^18, Horner in
-// r^2 (the first omitted terms are below 1.3e-19 relative); the series of
-// cos r - 1 has no cancellation.  Other r through sincos.
+// ---- sin, cos and atan2 from a table of j / 128 -------------------------
+// kTrig[j] = (cos a_j, sin a_j) and kTrigCm1[j] = cos a_j - 1 at a_j = j / 128,
+// correctly rounded (gen_trig_table.py).  An angle a_j + b with |b| <= 2^-8
+// needs only short Taylor polynomials in b and the addition theorem: about
+// 12 FP64 operations for sin and cos and 15 for atan2, where the general
+// routines spend an argument reduction and long polynomials on the FP64
+// pipe (the bound of the update).  Results agree with the correctly rounded
+// values to about an ulp, like the library routines'.
+#include "trig_table.inc"
+
+// j = round(128 a) for +0 <= a < 6.3, from a's bits on the integer pipe;
+// -1 for other a (negative, -0.0, larger, NaN)
+__device__ __forceinline__ int trig_round(double a) {
+    const long long bits = __double_as_longlong(a);
+    if (bits < 0 || bits >= kTrigMaxKey) return -1;
+    const int e = (int)(bits >> 52) - 1023;
+    if (e < -9) return 0;  // a < 2^-9: 128 a < 1/4
+    const unsigned long long mant = (unsigned long long)(bits & 0xFFFFFFFFFFFFFll) | (1ull << 52);
+    const int shift = 45 - e;  // 128 a = mant 2^-shift, shift in 43 .. 54
+    return (int)((mant + (1ull << (shift - 1))) >> shift);
+}
+
+// a_j = j / 128 as a double, from j's bits (0 <= j < 2^20)
+__device__ __forceinline__ double trig_angle(int j) {
+    if (j == 0) return 0.0;
+    const int hb = 31 - __clz(j);
+    const unsigned long long b = ((unsigned long long)(1023 + hb - 7) << 52) |
+                                 (((unsigned long long)j << (52 - hb)) & 0xFFFFFFFFFFFFFull);
+    return __longlong_as_double((long long)b);
+}
+
+// sin b and cos b - 1 for |b| <= 2^-8 (+ a few FP32 ulps): Taylor to b^5 and
+// b^6 (the first omitted terms are below 4e-18 and 2e-19 relative)
+__device__ __forceinline__ void trig_small(double b, double &sb, double &cb) {
+    const double z = b * b;
+    sb = fma(b * z, fma(z, 1.0 / 120.0, -1.0 / 6.0), b);
+    cb = z * fma(z, fma(z, -1.0 / 720.0, 1.0 / 24.0), -0.5);
+}
+
+// sin a and cos a (sincos for a outside [0, 6.3))
+__device__ __forceinline__ void tab_sincos(double a, double &s, double &c) {
+    const int j = trig_round(a);
+    if (j < 0) {
+        sincos(a, &s, &c);
+        return;
+    }
+    const double b = a - trig_angle(j);  // exact: a_j is a multiple of ulp(a), |b| <= min(a, 2^-8)
+    const double2 t = __ldg(&kTrig[j]);
+    double sb, cb;
+    trig_small(b, sb, cb);
+    s = fma(t.x, sb, fma(t.y, cb, t.y));
+    c = fma(-t.y, sb, fma(t.x, cb, t.x));
+}
+
+// sin r and cos r - 1, the latter without the cancellation of cos r - 1
 __device__ __forceinline__ void sin_cosm1(double r, double &s, double &cm1) {
-    if (fabs(r) <= 0.8) {
-        const double z = r * r;
-        double p = 1.0 / 355687428096000.0;  // 1/17!
-        p = fma(p, z, -1.0 / 1307674368000.0);
-        p = fma(p, z, 1.0 / 6227020800.0);
-        p = fma(p, z, -1.0 / 39916800.0);
-        p = fma(p, z, 1.0 / 362880.0);
-        p = fma(p, z, -1.0 / 5040.0);
-        p = fma(p, z, 1.0 / 120.0);
-        p = fma(p, z, -1.0 / 6.0);
-        s = fma(r * z, p, r);
-        double q = -1.0 / 6402373705728000.0;  // -1/18!
-        q = fma(q, z, 1.0 / 20922789888000.0);
-        q = fma(q, z, -1.0 / 87178291200.0);
-        q = fma(q, z, 1.0 / 479001600.0);
-        q = fma(q, z, -1.0 / 3628800.0);
-        q = fma(q, z, 1.0 / 40320.0);
-        q = fma(q, z, -1.0 / 720.0);
-        q = fma(q, z, 1.0 / 24.0);
-        q = fma(q, z, -0.5);
-        cm1 = z * q;
-    } else {
+    const int j = trig_round(r);
+    if (j < 0) {
         double c;
         sincos(r, &s, &c);
         cm1 = c - 1.0;
+        return;
     }
+    const double b = r - trig_angle(j);
+    const double2 t = __ldg(&kTrig[j]);
+    const double tm = __ldg(&kTrigCm1[j]);
+    double sb, cb;
+    trig_small(b, sb, cb);
+    s = fma(t.x, sb, fma(t.y, cb, t.y));
+    cm1 = fma(t.x, cb, fma(-t.y, sb, tm));  // (cos a_j - 1) + cos a_j (cos b - 1) - sin a_j sin b
+}
+
+// atan2(y, x).  An FP32 estimate of the angle of (x, |y|) picks a_j; the
+// vector rotated by -a_j has the small angle eps = atan(e / d), |eps| <=
+// 2^-8 + 1e-6, from an FP64 quotient (FP32 reciprocal, two Newton steps)
+// and the series eps - eps^3/3 + eps^5/5 - eps^7/7 (omitted terms below
+// 1e-20 relative); the sign of y is applied last (atan2 is odd in y).
+// Inputs whose rotated length d is not a positive number in [2^-60, 2^61),
+// or whose |e| is not below d 2^-8 (zero, tiny, huge or non-finite vectors,
+// for which the FP32 estimate fails) go through atan2.
+__device__ __forceinline__ double tab_atan2(double y, double x) {
+    const float af = atan2f(fabsf(d2f(y)), d2f(x));  // [0, pi] to ~1e-7 (NaN -> j = 0)
+    const int j = __float2int_rn(af * 128.0f);       // 0 .. 402
+    const double2 t = __ldg(&kTrig[j]);
+    const double ay = fabs(y);
+    const double d = fma(ay, t.y, x * t.x);   // along a_j
+    const double e = fma(-x, t.y, ay * t.x);  // across it
+    const long long db = __double_as_longlong(d);
+    const int ed = (int)(db >> 52), ee = (int)((__double_as_longlong(e) >> 52) & 0x7FF);
+    if (db < 0x3C30000000000000ll || db >= 0x43C0000000000000ll || ee > ed - 8) return atan2(y, x);
+    const double r0 = f2d(__frcp_rn(d2f_pos(d)));
+    const double r = fma(r0, fma(-d, r0, 1.0), r0);  // 1 / d to ~2^-46
+    const double q = e * r;
+    const double eps = fma(r, fma(-d, q, e), q);     // e / d to about an ulp
+    const double z = eps * eps;
+    const double at = fma(eps * z, fma(z, fma(z, -1.0 / 7.0, 1.0 / 5.0), -1.0 / 3.0), eps);
+    const double ang = trig_angle(j) + at;
+    return (__double_as_longlong(y) < 0) ? -ang : ang;
 }
 
 // ---- the Langevin chain ------------------------------------------------
@@ -432,12 +499,12 @@ __device__ __forceinline__ void langevin(double &x, double &y, double &z, double
                                          double bx, double by, double bz, bool have_theta, double cth,
                                          double sth) {
     double sp, cp, ct, st;
-    sincos(phi, &sp, &cp);
+    tab_sincos(phi, sp, cp);
     if (have_theta) {
         ct = cth;
         st = sth;
     } else {
-        sincos(theta, &st, &ct);
+        tab_sincos(theta, st, ct);
     }
     // CosSinOrientation::to_orientation_vector, particle.rs:165-172
     // (with sin(theta) == 1 exactly, the products are cp and sp exactly)
@@ -523,7 +590,7 @@ __device__ __forceinline__ void langevin(double &x, double &y, double &z, double
     // finalize: Particle::from(old + delta) then pbc (mod.rs:121-125)
     double px = x + dp[0], py = y + dp[1], pz = z + dp[2];
     double v0 = n[0] + dn[0], v1 = n[1] + dn[1], v2 = n[2] + dn[2];
-    double nphi = atan2(v1, v0);  // Orientation::from_vector, particle.rs:106-121
+    double nphi = tab_atan2(v1, v0);  // Orientation::from_vector, particle.rs:106-121
     x = ref_modulo(px, bx);
     y = ref_modulo(py, by);
     if (Q2D) {
@@ -534,7 +601,7 @@ __device__ __forceinline__ void langevin(double &x, double &y, double &z, double
         theta = kPiHalf;
     } else {
         double rxy = sqrt(v0 * v0 + v1 * v1);
-        double nth = kPiHalf - atan2(v2, rxy);
+        double nth = kPiHalf - tab_atan2(v2, rxy);
         z = ref_modulo(pz, bz);
         ref_ang_pbc(nphi, nth);
         phi = nphi;
