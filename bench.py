@@ -64,6 +64,30 @@ def traffic_per_launch(key, n):
     return None
 
 
+def fp64_per_particle(key):
+    """FP64 thread-instructions (DFMA + DMUL + DADD) per particle of a kernel,
+    from the ncu instruction counts in profiles/fp64_inst.txt; None when absent."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "fp64_inst.txt")) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 2 and parts[0] == key:
+                    return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+def fp64_rate():
+    """Measured FP64 FMA rate of this GPU (thread-FMAs/s, ss_fp64_rate probe)."""
+    import ctypes
+
+    from stochasticsampling_gb300 import _lib
+    r = ctypes.c_double()
+    _lib.check(_lib.load().ss_fp64_rate(ctypes.byref(r)))
+    return r.value
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -493,16 +517,27 @@ def run_gpu(args, rank, world, dist):
     peak, peak_kind = peaks()
     gx, gy, gz, gp, gt = GRID
     ncell, nbins = gx * gy * gz, gx * gy * gz * gp * gt
-    # update kernel, algorithmic bytes per launch: state read + written (5 f64),
-    # cell key read + written, particle id read, the field table once, the
-    # next histogram once (u32)
-    upd_bytes = N * (40 + 40 + 4 + 4 + 4) + ncell * 16 * 8 + nbins * 4
+    # update kernel (the canonical quasi-2-D variant: every particle holds
+    # z = 0, theta = pi/2, which it neither reads nor writes), algorithmic
+    # bytes per launch: x, y, phi read + written (3 f64), cell key read +
+    # written, particle id read, the field table once, the next histogram
+    # once (u32)
+    upd_bytes = N * (24 + 24 + 4 + 4 + 4) + ncell * 16 * 8 + nbins * 4
     upd_ms = stage_avg["update"]
     achieved = upd_bytes / (upd_ms / 1e3) / 1e9
     # whole step, algorithmic bytes: particles 80 B, histogram 12 B
     # per bin, 21 FFT components read+written as 16 B complex, field table
     step_bytes = N * 80 + nbins * 12 + ncell * 16 * 2 * 21 + ncell * 13 * 8
     traffic = traffic_per_launch("k_update_c1", N)
+    # the bound of k_update on GB300: FP64 issue (instructions from ncu)
+    inst = fp64_per_particle("k_update_c1")
+    rate = fp64_rate()
+    fp64_roof = {"bound": "fp64", "achieved": inst * N / (upd_ms / 1e3) if inst else None, "peak": rate,
+                 "unit": "FP64 thread-instructions/s",
+                 "frac": inst * N / (upd_ms / 1e3) / rate if inst else None,
+                 "instructions_per_particle": inst,
+                 "peak_source": "ss_fp64_rate: independent FMA chains on every SM, measured in this run",
+                 "instructions_source": "DFMA + DMUL + DADD per particle, ncu (profiles/fp64_inst.txt)"}
     cpu = None
     if not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
@@ -527,6 +562,7 @@ def run_gpu(args, rank, world, dist):
                      "traffic": traffic, "kernel": "k_update (fused Langevin step + next-step binning)",
                      "peak_source": peak_kind, "bytes_per_launch": upd_bytes, "avg_launch_ms": upd_ms,
                      "note": "FP64-issue bound on GB300 (low FP64 rate); HBM fraction reported as required"},
+        "fp64_roofline": fp64_roof,
         "step_roofline": {"algorithmic_bytes": step_bytes,
                           "achieved_gbs": step_bytes / (ms_max / args.steps / 1e3) / 1e9},
         "stage_ms": stage_avg,

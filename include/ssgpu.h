@@ -193,6 +193,11 @@ int ss_profile_read(ss_ctx *ctx, double *ms, uint64_t *count);
 /* number of this library's kernels launched on the context so far
  * (cuFFT's own kernels excluded) */
 int ss_launch_count(ss_ctx *ctx, uint64_t *out);
+/* FP64 FMA throughput of the current device (thread-FMAs per second) from a
+ * probe kernel of independent FMA chains on every SM: the FP64 roofline of
+ * the particle update, whose bound on GB300 is the FP64 pipe.  Diagnostic; no
+ * counterpart in the reference. */
+int ss_fp64_rate(double *fma_per_second);
 
 /* The normalised distribution of a particle list, computed without any
  * allocation.  This entry point has no counterpart in the reference.

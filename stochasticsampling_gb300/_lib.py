@@ -19,7 +19,7 @@ EXPORTS = [
     "ss_ensemble_autotune", "ss_ensemble_set_config", "ss_ensemble_run", "ss_ensemble_synchronize", "ss_ensemble_get_particles",
     "ss_ensemble_get_counts", "ss_ensemble_get_flow_field", "ss_ensemble_info", "ss_dn_conv32", "ss_dn_create",
     "ss_dn_destroy", "ss_dn_info", "ss_dn_get_params", "ss_dn_set_params", "ss_dn_forward", "ss_dn_train",
-    "ss_dn_gradients", "ss_dn_sample_histogram", "ss_set_denoiser", "ss_last_error", "ss_version",
+    "ss_dn_gradients", "ss_dn_sample_histogram", "ss_set_denoiser", "ss_fp64_rate", "ss_last_error", "ss_version",
 ]
 
 SS_OK = 0
@@ -124,6 +124,7 @@ def load(build_if_missing=True):
         "ss_profile_enable": [vp, ci],
         "ss_profile_read": [vp, dp, u64p],
         "ss_launch_count": [vp, u64p],
+        "ss_fp64_rate": [dp],
         "ss_sample_distribution_noalloc": [ctypes.POINTER(Grid), ctypes.POINTER(Box), vp, u64, vp, vp],
         "ss_ensemble_create": [ctypes.POINTER(Grid), ctypes.POINTER(Box), ctypes.POINTER(Params), u32, u32, vp,
                                ctypes.POINTER(vp)],

@@ -99,9 +99,10 @@ __device__ __forceinline__ double ref_modulo(double f, double m) {
     // goes through fmod as in the IEEE form of these compares
     const long long kf = dkey(f), km = dkey(m);
     if (kf > -km && kf < km + (1ll << 52)) {  // key(2 m): the exponent of m plus one
-        if (kf >= km) return f - m;
-        if (kf < 0) return f + m;
-        return f;
+        // f - m, f + m or f, as one addition (f + -0.0 == f for every f,
+        // signed zeros included); the choice is made on the integer pipe
+        const long long mb = __double_as_longlong(m), sign = (long long)0x8000000000000000ull;
+        return f + __longlong_as_double((kf >= km) ? (mb ^ sign) : ((kf < 0) ? mb : sign));
     }
     double r = fmod(f, m);
     return (r < 0.0) ? r + fabs(m) : r;
@@ -141,15 +142,39 @@ __device__ __forceinline__ float d2f(double d) {
     const float m = d2f_pos(__longlong_as_double(b & 0x7FFFFFFFFFFFFFFFll));
     return (b < 0) ? -m : m;
 }
-// f2d: the exact double of a float (zero, subnormals, inf and nan through
-// the conversion instruction)
+// f2d: the exact double of a float, all from its bits (zero, subnormals,
+// inf and NaN included; a NaN keeps its payload bits)
 __device__ __forceinline__ double f2d(float f) {
     const uint32_t u = __float_as_uint(f);
-    const uint32_t e = (u >> 23) & 0xFFu;
-    if (e == 0u || e == 0xFFu) return (double)f;
-    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
-                                 ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
-    return __longlong_as_double((long long)b);
+    const uint32_t e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+    unsigned long long body;
+    if (e == 0xFFu) {
+        body = (0x7FFull << 52) | ((unsigned long long)m << 29);
+    } else if (e != 0u) {
+        body = ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+    } else if (m == 0u) {
+        body = 0ull;
+    } else {  // subnormal m 2^-149 = 2^(p - 149) 1.f, p the highest set bit of m
+        const int p = 31 - __clz(m);
+        body = ((unsigned long long)(p + 874) << 52) | (((unsigned long long)m << (52 - p)) & 0xFFFFFFFFFFFFFull);
+    }
+    return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) | body));
+}
+// m 2^-52 rounded to the nearest float (ties to even) for 0 < m < 2^53,
+// from m's bits (the value is a normal float, 2^-52 .. 2)
+__device__ __forceinline__ float u52_to_float(unsigned long long m) {
+    const int p = 63 - __clzll(m);  // 2^(p - 52) <= m 2^-52 < 2^(p - 51)
+    unsigned long long q;
+    if (p <= 23) {
+        q = m << (23 - p);  // exact, the leading one at bit 23
+    } else {
+        const int sh = p - 23;
+        q = m >> sh;
+        const unsigned long long rest = m & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        if (rest > half || (rest == half && (q & 1ull))) q += 1ull;  // a carry to 2^24 raises the exponent below
+    }
+    // exponent field p + 75, minus one for the leading one that q adds
+    return __uint_as_float(((uint32_t)(p + 74) << 23) + (uint32_t)q);
 }
 // For 0 <= q < 2^31: fl = floor(q), and near = q lies within 2^-20 of an
 // integer (fr = q - floor(q) < 2^-20 or fr > 1 - 2^-20), from q's bits.
@@ -232,13 +257,15 @@ __device__ __forceinline__ double u12(uint32_t hi, uint32_t lo) {
 }
 
 // -2 ln(1 - U) in FP32 with full relative precision over all of (0, 1],
-// from x = 1 + U in [1, 2) (52 random bits): -U = 1 - x and 1 - U = 2 - x
-// are exact in FP64; log1p takes -U below U = 1/2 (the radius near 0), log
-// takes 1 - U above it (the tail, down to 1 - U = 2^-52).
+// from x = 1 + U in [1, 2) (52 random bits, U = m 2^-52 with m the mantissa
+// of x): log1p takes -U below U = 1/2 (the radius near 0), log takes
+// 1 - U = (2^52 - m) 2^-52 above it (the tail, down to 1 - U = 2^-52).  Both
+// arguments are the float nearest the exact value, formed from m's bits
+// (the same floats as rounding the exact FP64 differences 1 - x and 2 - x).
 __device__ __forceinline__ float neg2log1m(double x) {
-    // x < 1.5 <=> the top mantissa bit of x in [1, 2) is clear
-    const bool low = ((__double_as_longlong(x) >> 51) & 1) == 0;
-    const float l = low ? log1pf(d2f(1.0 - x)) : logf(d2f_pos(2.0 - x));
+    const unsigned long long m = (unsigned long long)__double_as_longlong(x) & 0xFFFFFFFFFFFFFull;
+    const float l = (m >> 51) == 0ull ? log1pf(m ? -u52_to_float(m) : 0.0f)
+                                      : logf(u52_to_float((1ull << 52) - m));
     return -2.0f * l;
 }
 
@@ -387,7 +414,7 @@ __device__ __forceinline__ double tab_atan2(double y, double x) {
     const double z = eps * eps;
     const double at = fma(eps * z, fma(z, fma(z, -1.0 / 7.0, 1.0 / 5.0), -1.0 / 3.0), eps);
     const double ang = trig_angle(j) + at;
-    return (__double_as_longlong(y) < 0) ? -ang : ang;
+    return __longlong_as_double(__double_as_longlong(ang) ^ (__double_as_longlong(y) & (long long)0x8000000000000000ull));
 }
 
 // ---- the Langevin chain ------------------------------------------------
@@ -508,11 +535,15 @@ __device__ __forceinline__ void langevin(double &x, double &y, double &z, double
     }
     // CosSinOrientation::to_orientation_vector, particle.rs:165-172
     // (with sin(theta) == 1 exactly, the products are cp and sp exactly)
-    double n[3] = {st * cp, st * sp, ct};
+    double n[3];
     if (have_theta && __double_as_longlong(st) == __double_as_longlong(1.0)) {
         n[0] = cp;
         n[1] = sp;
+    } else {
+        n[0] = st * cp;
+        n[1] = st * sp;
     }
+    n[2] = ct;
     double dp[3] = {0.0, 0.0, 0.0}, dn[3] = {0.0, 0.0, 0.0};
 
     if (mask & M_SELF_PROPULSION) {  // modifiers.rs:39-46
@@ -607,6 +638,73 @@ __device__ __forceinline__ void langevin(double &x, double &y, double &z, double
         phi = nphi;
         theta = nth;
     }
+}
+
+// The chain of `langevin` for a quasi-2-D particle in the canonical state
+// (theta = pi/2 and z = 0, which every particle holds after a quasi2d step)
+// and no magnetic modifiers: n = (cos phi, sin phi, cos(pi/2)) with
+// cos(pi/2) (6.1e-17 in FP64) taken as 0 and sin(pi/2) == 1 exactly, so the
+// products with n_z and every z component drop out; the rotation axis then
+// enters only through k x n = (sa sin phi, -sa cos phi).  Each dropped term
+// is below half an ulp of the sum it joins, so the results can differ from
+// the full chain's in the last bit, like the rounding of sin / cos / atan2.
+// z and theta are not produced (the quasi2d step overwrites them with 0 and
+// pi/2, which the canonical state already holds).
+template <class F>
+__device__ __forceinline__ void langevin_canon(double &x, double &y, double &phi, const F &fld, const double xi[3],
+                                               double sa, double rot, uint32_t mask, double dt, double reorient,
+                                               double shape, double bx, double by) {
+    double sp, cp;
+    tab_sincos(phi, sp, cp);
+    double dp0 = 0.0, dp1 = 0.0, dn0 = 0.0, dn1 = 0.0;
+    if (mask & M_SELF_PROPULSION) {
+        dp0 = cp;
+        dp1 = sp;
+    }
+    if (mask & M_CONVECTION) {
+        dp0 = dp0 + fld.flow(0);
+        dp1 = dp1 + fld.flow(1);
+    }
+    if (mask & M_EXTERNAL_FIELD) {  // b = (0, reorient, 0): b - n (n . b)
+        const double d = sp * reorient;
+        dn0 = dn0 + (0.0 - cp * d);
+        dn1 = dn1 + (reorient - sp * d);
+    }
+    if (mask & M_JEFFREY_VORTICITY) {  // -(W n), W n = (w01 n1, -w01 n0)
+        const double w01 = fld.r[T_W01];
+        dn0 = dn0 + (-(w01 * sp));
+        dn1 = dn1 + (-((-w01) * cp));
+    }
+    if (mask & M_JEFFREY_STRAIN) {  // f = shape E n, f - n (f . n)
+        const double e00 = fld.r[T_E00], e01 = fld.r[T_E01], e11 = fld.r[T_E11];
+        const double f0 = (e00 * cp + e01 * sp) * shape, f1 = (e01 * cp + e11 * sp) * shape;
+        const double fn = f0 * cp + f1 * sp;
+        dn0 = dn0 + (f0 - cp * fn);
+        dn1 = dn1 + (f1 - sp * fn);
+    }
+    if (mask & M_STEP) {
+        dp0 = dp0 * dt;
+        dp1 = dp1 * dt;
+        dn0 = dn0 * dt;
+        dn1 = dn1 * dt;
+    }
+    if (mask & M_TRANS_DIFFUSION) {
+        const double diff = fld.diff();
+        dp0 = dp0 + xi[0] * diff;
+        dp1 = dp1 + xi[1] * diff;
+    }
+    if (mask & M_ROT_DIFFUSION) {  // n (cos rot - 1) + (k x n) sin rot
+        double sr, cm1;
+        sin_cosm1(rot, sr, cm1);
+        const double k0 = sa * sp, k1 = (-sa) * cp;
+        dn0 = dn0 + (cp * cm1 + k0 * sr);
+        dn1 = dn1 + (sp * cm1 + k1 * sr);
+    }
+    const double px = x + dp0, py = y + dp1;
+    const double v0 = cp + dn0, v1 = sp + dn1;
+    x = ref_modulo(px, bx);
+    y = ref_modulo(py, by);
+    phi = ref_modulo(tab_atan2(v1, v0), kTwoPi);
 }
 
 }  // namespace ss

@@ -54,7 +54,7 @@ __global__ void k_scan_rows(const double *__restrict__ aos, unsigned long long n
 #pragma unroll
         for (int k = 0; k < 5; ++k) bad |= ((b[k] >> 52) & 0x7FFull) == 0x7FFull;
         const unsigned long long half_pi = (unsigned long long)__double_as_longlong(kPiHalf);
-        noncanon = (b[2] << 1) != 0ull || b[4] != half_pi;
+        noncanon = b[2] != 0ull || b[4] != half_pi;  // z == +0.0 (the value a quasi2d step writes)
     }
     if (bad) atomicMin(&scan[0], i);
     if (__any_sync(0xffffffffu, noncanon) && (threadIdx.x & 31) == 0) atomicOr(&scan[1], 1ull);
@@ -308,9 +308,12 @@ __global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__
 // particle update: the loop of src/bin/simulation/mod.rs:318-369 fused with
 // the next step's binning (histogram_from) so each step reads and writes the
 // particle state once.  NOISE: 0 = Philox on device, 1 = host array [N][5]
-// indexed by the caller's particle order.
+// indexed by the caller's particle order.  CANON (quasi2d, every particle in
+// the canonical state z = 0, theta = pi/2, no magnetic step, nearest-cell
+// gather): the chain of langevin_canon, and z and theta are neither read nor
+// written.
 // ------------------------------------------------------------------------
-template <bool Q2D, bool MAG, int NOISE, bool TRI>
+template <bool Q2D, bool MAG, int NOISE, bool TRI, bool CANON = false>
 __global__ void __launch_bounds__(256) k_update(DevParams P, double *__restrict__ x, double *__restrict__ y,
                                                 double *__restrict__ z, double *__restrict__ phi,
                                                 double *__restrict__ theta, uint32_t *__restrict__ key,
@@ -323,7 +326,8 @@ __global__ void __launch_bounds__(256) k_update(DevParams P, double *__restrict_
     const int ts = (MAG || TRI) ? TABLE_STRIDE_MAG : TABLE_STRIDE;
     uint32_t cell = key[i];
     uint32_t pid = id[i];
-    double px = x[i], py = y[i], pz = z[i], pph = phi[i], pth = theta[i];
+    double px = x[i], py = y[i], pph = phi[i];
+    double pz = CANON ? 0.0 : z[i], pth = CANON ? kPiHalf : theta[i];
     TableFields F{table + (long long)cell * ts};
     double trow[TABLE_STRIDE_MAG];
     if (TRI) {
@@ -339,15 +343,23 @@ __global__ void __launch_bounds__(256) k_update(DevParams P, double *__restrict_
         sincos(r[3], &sa, &ca);
         rot = r[4];
     }
-    bool have_theta = Q2D && (__double_as_longlong(pth) == __double_as_longlong(kPiHalf));
-    langevin<Q2D>(px, py, pz, pph, pth, F, xi, ca, sa, rot, P.mask, P.dt, P.reorient, P.shape, P.drag, P.bx,
-                  P.by, P.bz, have_theta, P.cos_half_pi, P.sin_half_pi);
+    if (CANON) {
+        langevin_canon(px, py, pph, F, xi, sa, rot, P.mask, P.dt, P.reorient, P.shape, P.bx, P.by);
+    } else {
+        bool have_theta = Q2D && (__double_as_longlong(pth) == __double_as_longlong(kPiHalf));
+        langevin<Q2D>(px, py, pz, pph, pth, F, xi, ca, sa, rot, P.mask, P.dt, P.reorient, P.shape, P.drag, P.bx,
+                      P.by, P.bz, have_theta, P.cos_half_pi, P.sin_half_pi);
+    }
     uint32_t err = 0, ncell;
     unsigned long long bin;
     bin_particle<Q2D>(P, px, py, pz, pph, pth, ncell, bin, err);
     atomicAdd(counts_next + bin, 1u);
     key[i] = ncell;
-    x[i] = px; y[i] = py; z[i] = pz; phi[i] = pph; theta[i] = pth;
+    x[i] = px; y[i] = py; phi[i] = pph;
+    if (!CANON) {
+        z[i] = pz;
+        theta[i] = pth;
+    }
     if (err) atomicOr(errflag, err);
 }
 
@@ -508,6 +520,23 @@ __global__ void k_langevin_args(const double *__restrict__ in, unsigned long lon
     out[5 * i] = px; out[5 * i + 1] = py; out[5 * i + 2] = pz; out[5 * i + 3] = pph; out[5 * i + 4] = pth;
 }
 
+// FP64 FMA throughput probe: every thread runs 8 independent FMA chains of
+// `iters` steps (x <- x a + b with |a| < 1, so the chains stay finite); the
+// sum is written so that the chains are not removed.
+__global__ void __launch_bounds__(256) k_fp64_rate(int iters, double a, double b, double *__restrict__ out) {
+    double x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = (double)(threadIdx.x + k);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+    }
+    double sum = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) sum += x[k];
+    out[blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x] = sum;
+}
+
 // ========================================================================
 // launch wrappers
 // ========================================================================
@@ -578,11 +607,20 @@ void launch_table(cudaStream_t s, bool flow, bool mag, const double2 *inv, const
     else k_table<false, true><<<b, 128, 0, s>>>(inv, P, table, tstride);
 }
 
-void launch_update(cudaStream_t s, bool q2d, bool mag, bool host_noise, const DevParams &P, double *const xs[5],
-                   uint32_t *key, const uint32_t *id, const double *table, const double *noise,
+void launch_update(cudaStream_t s, bool q2d, bool canon, bool mag, bool host_noise, const DevParams &P,
+                   double *const xs[5], uint32_t *key, const uint32_t *id, const double *table, const double *noise,
                    const unsigned long long *d_step, uint32_t *counts_next, uint32_t *err) {
     if (!P.n) return;
     unsigned b = nblocks(P.n, 256);
+    if (q2d && canon && !mag && !P.gather && !(P.mask & (M_MDD_FORCE | M_MDD_ROTATION))) {
+        if (host_noise)
+            k_update<true, false, 1, false, true><<<b, 256, 0, s>>>(P, xs[0], xs[1], xs[2], xs[3], xs[4], key, id,
+                                                                    table, noise, d_step, counts_next, err);
+        else
+            k_update<true, false, 0, false, true><<<b, 256, 0, s>>>(P, xs[0], xs[1], xs[2], xs[3], xs[4], key, id,
+                                                                    table, noise, d_step, counts_next, err);
+        return;
+    }
 #define SS_UPD(Q, M, N, T)                                                                                   \
     k_update<Q, M, N, T><<<b, 256, 0, s>>>(P, xs[0], xs[1], xs[2], xs[3], xs[4], key, id, table, noise, d_step, \
                                            counts_next, err)
@@ -641,6 +679,10 @@ void launch_langevin_args(cudaStream_t s, const double *in, unsigned long long n
                           double *out) {
     if (!n) return;
     k_langevin_args<false><<<nblocks(n, 128), 128, 0, s>>>(in, n, mask, args, out);
+}
+
+void launch_fp64_rate(cudaStream_t s, unsigned blocks, int iters, double *out) {
+    k_fp64_rate<<<blocks, 256, 0, s>>>(iters, 0.999999, 1e-3, out);
 }
 
 }  // namespace ss

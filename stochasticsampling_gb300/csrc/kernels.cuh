@@ -21,8 +21,9 @@ void launch_kspace(cudaStream_t s, bool flow, bool mag, const double2 *fwd, doub
                    double screening);
 void launch_table(cudaStream_t s, bool flow, bool mag, const double2 *inv, const DevParams &P, double *table,
                   int tstride);
-void launch_update(cudaStream_t s, bool q2d, bool mag, bool host_noise, const DevParams &P, double *const xs[5],
-                   uint32_t *key, const uint32_t *id, const double *table, const double *noise,
+// canon: quasi2d with every particle in the canonical state (z = 0, theta = pi/2)
+void launch_update(cudaStream_t s, bool q2d, bool canon, bool mag, bool host_noise, const DevParams &P,
+                   double *const xs[5], uint32_t *key, const uint32_t *id, const double *table, const double *noise,
                    const unsigned long long *d_step, uint32_t *counts_next, uint32_t *err);
 void launch_step_inc(cudaStream_t s, unsigned long long *d_step);
 void launch_sample_initial(cudaStream_t s, bool homogeneous, const DevParams &P, double kappa, double *aos,
@@ -36,5 +37,7 @@ void launch_real_parts(cudaStream_t s, const double2 *src, long long count, doub
 void launch_half_pi(cudaStream_t s, double *out);
 void launch_langevin_args(cudaStream_t s, const double *in, unsigned long long n, uint32_t mask, const double *args,
                           double *out);
+// blocks x 256 threads, 8 FMA chains of iters steps each; out[blocks * 256]
+void launch_fp64_rate(cudaStream_t s, unsigned blocks, int iters, double *out);
 
 }  // namespace ss

@@ -361,7 +361,7 @@ static int enqueue_step(ss_ctx *c, int pcur, int ccur, bool host_noise, uint64_t
     const int p = sort_now ? 1 - pcur : pcur;
     mark(c, 5);
     launch_zero_u32(c->stream, c->counts[1 - ccur], c->P.nbins);
-    launch_update(c->stream, c->q2d, c->mag_step, host_noise, c->P, c->px[p], c->key[p], c->pid[p], c->table,
+    launch_update(c->stream, c->q2d, c->canon, c->mag_step, host_noise, c->P, c->px[p], c->key[p], c->pid[p], c->table,
                   c->noise_dev, c->d_step, c->counts[1 - ccur], c->d_err);
     launch_step_inc(c->stream, c->d_step);
     *nl += 3;
@@ -380,8 +380,8 @@ static void advance(ss_ctx *c) {
     c->timestep += 1;
     c->fields_mag_valid = c->mag_step;
     c->solved = true;
-    // the first mixed quasi2d step sets z = 0 and theta = pi/2 everywhere
-    if (c->mixed && c->q2d) c->canon = true;
+    // the first quasi2d step sets z = 0 and theta = pi/2 everywhere
+    if (c->q2d) c->canon = true;
 }
 
 static void accumulate_timing(ss_ctx *c) {
@@ -410,7 +410,8 @@ static int direct_step(ss_ctx *c, bool host_noise) {
 }
 
 static int graph_step(ss_ctx *c) {
-    if (c->mixed && c->q2d && !c->canon) return direct_step(c, false);
+    // the step after non-canonical quasi2d rows runs directly (graphs hold the canonical update)
+    if (c->q2d && !c->canon) return direct_step(c, false);
     cudaGraphExec_t &g = c->graph[c->pcur][c->ccur];
     if (!g) {
         cudaGraph_t graph;
@@ -771,6 +772,7 @@ static int ingest_staging(ss_ctx *c, uint64_t n, bool canon) {
         launch_ingest(c->stream, c->staging, n, c->P, c->px[0], c->pid[0]);
         launch_zero_u32(c->stream, c->counts[0], c->P.nbins);
         launch_bin(c->stream, n, c->P, c->px[0], c->key[0], c->counts[0], c->d_err);
+        c->canon = canon;
     }
     c->launches += 3;
     CKR(check_launch(c, "init"));
@@ -1098,6 +1100,41 @@ int ss_profile_read(ss_ctx *c, double *ms, uint64_t *count) {
 int ss_launch_count(ss_ctx *c, uint64_t *out) {
     if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
     *out = c->launches;
+    return SS_OK;
+}
+
+int ss_fp64_rate(double *fma_per_second) {
+    if (!fma_per_second) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null argument");
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return fail(nullptr, SS_ERR_CUDA, "no CUDA device");
+    const unsigned blocks = (unsigned)sms * 8u;  // 2048 threads per SM
+    const int iters = 4096;
+    double *d_out = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaStream_t s = nullptr;
+    float best = 0.0f;
+    cudaError_t st = cudaMalloc(&d_out, sizeof(double) * blocks * 256);
+    if (st == cudaSuccess) st = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (st == cudaSuccess) st = cudaEventCreate(&e0);
+    if (st == cudaSuccess) st = cudaEventCreate(&e1);
+    for (int rep = 0; rep < 4 && st == cudaSuccess; ++rep) {  // the first launch warms up
+        cudaEventRecord(e0, s);
+        ss::launch_fp64_rate(s, blocks, iters, d_out);
+        cudaEventRecord(e1, s);
+        st = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (st == cudaSuccess) st = cudaEventElapsedTime(&ms, e0, e1);
+        if (st == cudaSuccess && rep > 0 && (best == 0.0f || ms < best)) best = ms;
+    }
+    if (st == cudaSuccess) st = cudaGetLastError();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+    if (d_out) cudaFree(d_out);
+    if (st != cudaSuccess || best <= 0.0f) return fail(nullptr, SS_ERR_CUDA, "fp64 rate probe: %s", cudaGetErrorString(st));
+    *fma_per_second = (double)blocks * 256.0 * 8.0 * iters / (best * 1e-3);
     return SS_OK;
 }
 
