@@ -122,6 +122,17 @@ int ss_run(ss_ctx *ctx, uint64_t steps, uint64_t *timestep_out);
  * their atan2 in [0, 2 pi), whose sine and cosine give them back to FP64
  * rounding. */
 int ss_noise(ss_ctx *ctx, uint64_t timestep, double *out);
+/* One do_timestep on host-resident particles: the rows of `in` ([n][5] host
+ * doubles) replace the state as in ss_resume at the current step (the same
+ * checks), the step runs with on-device noise, and the new state is written
+ * to `out` ([n][5]) -- ss_resume + ss_do_timestep + ss_get_particles in one
+ * call, with the read-back of each chunk of updated particles overlapping
+ * the update of the next (a second stream).  The particles stay in the
+ * caller's order (no sort this step).  `in` and `out` may be the same
+ * buffer; pinned host memory gives the full copy bandwidth.  The drop-in
+ * form of Simulation::do_timestep (src/bin/simulation/mod.rs:251-374) for a
+ * caller that keeps the particles in host memory. */
+int ss_step_host(ss_ctx *ctx, const double *in, double *out, uint64_t n, uint64_t *timestep_out);
 /* Wait for the context's stream. */
 int ss_synchronize(ss_ctx *ctx);
 

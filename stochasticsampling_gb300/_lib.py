@@ -11,7 +11,8 @@ LIB_PATH = os.path.join(HERE, "libssgpu.so")
 
 # every symbol that include/ssgpu.h declares
 EXPORTS = [
-    "ss_create", "ss_destroy", "ss_init", "ss_init_distribution", "ss_resume", "ss_do_timestep", "ss_run", "ss_noise", "ss_synchronize",
+    "ss_create", "ss_destroy", "ss_init", "ss_init_distribution", "ss_resume", "ss_do_timestep", "ss_run", "ss_noise", "ss_step_host",
+    "ss_synchronize",
     "ss_get_particles", "ss_get_distribution", "ss_get_counts", "ss_get_flow_field", "ss_get_magnetic_field",
     "ss_get_flow_complex", "ss_get_magnetic_complex", "ss_get_timestep", "ss_mean_flow_field",
     "ss_mean_magnetic_field", "ss_langevin", "ss_profile_enable", "ss_profile_read", "ss_launch_count",
@@ -109,6 +110,7 @@ def load(build_if_missing=True):
         "ss_do_timestep": [vp, dp, u64p],
         "ss_run": [vp, u64, u64p],
         "ss_noise": [vp, u64, dp],
+        "ss_step_host": [vp, dp, dp, u64, u64p],
         "ss_synchronize": [vp],
         "ss_get_particles": [vp, dp, u64],
         "ss_get_distribution": [vp, dp],

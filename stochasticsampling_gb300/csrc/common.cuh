@@ -98,11 +98,11 @@ __device__ __forceinline__ double ref_modulo(double f, double m) {
     // m > 0 finite (box sizes, 2 pi); a NaN f fails both range tests and
     // goes through fmod as in the IEEE form of these compares
     const long long kf = dkey(f), km = dkey(m);
+    if (kf >= 0 && kf < km) return f;  // [+-0, m): f itself, without an FP64 operation
     if (kf > -km && kf < km + (1ll << 52)) {  // key(2 m): the exponent of m plus one
-        // f - m, f + m or f, as one addition (f + -0.0 == f for every f,
-        // signed zeros included); the choice is made on the integer pipe
-        const long long mb = __double_as_longlong(m), sign = (long long)0x8000000000000000ull;
-        return f + __longlong_as_double((kf >= km) ? (mb ^ sign) : ((kf < 0) ? mb : sign));
+        // f - m or f + m; the sign of m is chosen on the integer pipe
+        const long long mb = __double_as_longlong(m);
+        return f + __longlong_as_double((kf >= km) ? (mb ^ (long long)0x8000000000000000ull) : mb);
     }
     double r = fmod(f, m);
     return (r < 0.0) ? r + fabs(m) : r;
@@ -111,7 +111,9 @@ __device__ __forceinline__ double ref_modulo(double f, double m) {
 // ang_pbc, src/particle.rs:37-44
 __device__ __forceinline__ void ref_ang_pbc(double &phi, double &theta) {
     double t = ref_modulo(theta, kTwoPi);
-    if (t > kPi) {
+    // t > pi on the integer pipe (a NaN t compares false, as in FP64)
+    const long long bt = __double_as_longlong(t);
+    if (dkey(t) > dkey(kPi) && (bt & 0x7FFFFFFFFFFFFFFFll) <= 0x7FF0000000000000ll) {
         phi = ref_modulo(phi + kPi, kTwoPi);
         theta = kTwoPi - t;
     } else {

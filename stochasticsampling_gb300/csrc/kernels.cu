@@ -121,6 +121,35 @@ __global__ void k_bin(unsigned long long n, DevParams P, const double *__restric
     if (err) atomicOr(errflag, err);
 }
 
+// Particle::new of k_ingest fused with the first histogram of k_bin
+// (Simulation::init, src/bin/simulation/mod.rs:163-196): one pass over the
+// rows.  CANON: every row in the canonical quasi-2-D state.
+template <bool CANON>
+__global__ void k_ingest_bin(const double *__restrict__ aos, unsigned long long n, DevParams P,
+                             double *__restrict__ x, double *__restrict__ y, double *__restrict__ z,
+                             double *__restrict__ phi, double *__restrict__ theta, uint32_t *__restrict__ id,
+                             uint32_t *__restrict__ key, uint32_t *__restrict__ counts,
+                             uint32_t *__restrict__ errflag) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *p = aos + 5 * i;
+    double px = ref_modulo(p[0], P.bx), py = ref_modulo(p[1], P.by), pz = ref_modulo(p[2], P.bz);
+    double ph = p[3], th = p[4];
+    ref_ang_pbc(ph, th);
+    px = ref_modulo(px, P.bx);
+    py = ref_modulo(py, P.by);
+    pz = ref_modulo(pz, P.bz);
+    ref_ang_pbc(ph, th);
+    x[i] = px; y[i] = py; z[i] = pz; phi[i] = ph; theta[i] = th;
+    id[i] = (uint32_t)i;
+    uint32_t err = 0, cell;
+    unsigned long long bin;
+    bin_particle<CANON>(P, px, py, pz, ph, th, cell, bin, err);
+    atomicAdd(counts + bin, 1u);
+    key[i] = cell;
+    if (err) atomicOr(errflag, err);
+}
+
 // counts -> normalised distribution, (c / D) * V exactly as
 // sample_from + the box-volume rescale (distribution/mod.rs:183,
 // simulation/mod.rs:255-257)
@@ -555,6 +584,17 @@ void launch_ingest(cudaStream_t s, const double *aos, unsigned long long n, cons
 void launch_egest(cudaStream_t s, unsigned long long n, double *const xs[5], const uint32_t *id, double *aos) {
     if (!n) return;
     k_egest<<<nblocks(n, 256), 256, 0, s>>>(n, xs[0], xs[1], xs[2], xs[3], xs[4], id, aos);
+}
+
+void launch_ingest_bin(cudaStream_t s, bool canon, const double *aos, unsigned long long n, const DevParams &P,
+                       double *const xs[5], uint32_t *id, uint32_t *key, uint32_t *counts, uint32_t *err) {
+    if (!n) return;
+    if (canon)
+        k_ingest_bin<true><<<nblocks(n, 256), 256, 0, s>>>(aos, n, P, xs[0], xs[1], xs[2], xs[3], xs[4], id, key,
+                                                           counts, err);
+    else
+        k_ingest_bin<false><<<nblocks(n, 256), 256, 0, s>>>(aos, n, P, xs[0], xs[1], xs[2], xs[3], xs[4], id, key,
+                                                            counts, err);
 }
 
 void launch_bin(cudaStream_t s, unsigned long long n, const DevParams &P, double *const xs[5], uint32_t *key,

@@ -11,6 +11,9 @@ void launch_scan_rows(cudaStream_t s, const double *aos, unsigned long long n, u
 void launch_ingest(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P, double *const xs[5],
                    uint32_t *id);
 void launch_egest(cudaStream_t s, unsigned long long n, double *const xs[5], const uint32_t *id, double *aos);
+// k_ingest and k_bin in one pass (canon: every row in the canonical quasi-2-D state)
+void launch_ingest_bin(cudaStream_t s, bool canon, const double *aos, unsigned long long n, const DevParams &P,
+                       double *const xs[5], uint32_t *id, uint32_t *key, uint32_t *counts, uint32_t *err);
 void launch_bin(cudaStream_t s, unsigned long long n, const DevParams &P, double *const xs[5], uint32_t *key,
                 uint32_t *counts, uint32_t *err);
 void launch_counts_to_dist(cudaStream_t s, const uint32_t *counts, const DevParams &P, double *dist);

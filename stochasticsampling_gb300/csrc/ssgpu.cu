@@ -43,6 +43,9 @@ namespace ss {
 void record_error(const char *msg) { g_last_error = msg; }
 }  // namespace ss
 
+// ss_step_host splits the update and the read-back into this many chunks
+constexpr int kHostChunks = 8;
+
 struct ss_ctx {
     ss_grid grid{};
     ss_box box{};
@@ -93,6 +96,10 @@ struct ss_ctx {
     int fft_n[3] = {1, 1, 1};
 
     cudaGraphExec_t graph[2][2] = {};
+    // ss_step_host: a copy stream and one event per chunk of the read-back
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t chunk_ev[kHostChunks + 1] = {};
+    uint64_t h_step = 0;  // host source of the step counter copy
     uint64_t launches = 0;
     uint64_t launches_per_step = 0;
     Timing timing;
@@ -370,11 +377,11 @@ static int enqueue_step(ss_ctx *c, int pcur, int ccur, bool host_noise, uint64_t
     return SS_OK;
 }
 
-static void advance(ss_ctx *c) {
+static void advance(ss_ctx *c, bool sorted) {
     // a replayed graph does not run the host side of enqueue_solve_m: the
     // widened FP64 copy of the mixed fields is stale after every step
     c->wide_valid = false;
-    if (c->sort) c->pcur ^= 1;
+    if (sorted) c->pcur ^= 1;
     c->dist_idx = c->ccur;
     c->ccur ^= 1;
     c->timestep += 1;
@@ -405,7 +412,7 @@ static int direct_step(ss_ctx *c, bool host_noise) {
     c->launches += nl;
     c->launches_per_step = nl;
     accumulate_timing(c);
-    advance(c);
+    advance(c, c->sort);
     return SS_OK;
 }
 
@@ -428,7 +435,7 @@ static int graph_step(ss_ctx *c) {
     }
     CK(cudaGraphLaunch(g, c->stream));
     c->launches += c->launches_per_step;
-    advance(c);
+    advance(c, c->sort);
     return SS_OK;
 }
 
@@ -486,6 +493,9 @@ static void destroy_impl(ss_ctx *c) {
     cudaFree(c->sums);
     for (auto &e : c->timing.ev)
         if (e) cudaEventDestroy(e);
+    for (auto &e : c->chunk_ev)
+        if (e) cudaEventDestroy(e);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -768,13 +778,14 @@ static int ingest_staging(ss_ctx *c, uint64_t n, bool canon) {
         launch_bin_m(c->stream, c->fixed, n, c->M, c->px[0], c->pa[0], c->key[0], c->counts[0]);
         // quasi2d: the canonical state (z = 0, theta = pi/2) lets the update skip z and theta
         c->canon = canon;
+        c->launches += 3;
     } else {
-        launch_ingest(c->stream, c->staging, n, c->P, c->px[0], c->pid[0]);
         launch_zero_u32(c->stream, c->counts[0], c->P.nbins);
-        launch_bin(c->stream, n, c->P, c->px[0], c->key[0], c->counts[0], c->d_err);
+        launch_ingest_bin(c->stream, canon, c->staging, n, c->P, c->px[0], c->pid[0], c->key[0], c->counts[0],
+                          c->d_err);
         c->canon = canon;
+        c->launches += 2;
     }
-    c->launches += 3;
     CKR(check_launch(c, "init"));
     c->dist_idx = 0;
     c->fields_mag_valid = false;
@@ -927,6 +938,69 @@ int ss_get_particles(ss_ctx *c, double *out, uint64_t n) {
     CK(cudaMemcpyAsync(out, c->staging, 5 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return read_device_error(c);
+}
+
+// One step of host-resident particles: the rows of `in` replace the state
+// (ss_resume at the current step), one do_timestep, the new state into
+// `out`.  The update runs in chunks; each chunk is laid out as rows and
+// copied back on a second stream while the next chunk updates, so the
+// read-back hides behind the update.  The step does not sort (sorting
+// changes no result): the particles stay in the caller's order.
+static int step_host_fp64(ss_ctx *c, double *out) {
+    if (!c->copy_stream) CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (auto &e : c->chunk_ev)
+        if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    uint64_t nl = 0;
+    const int p = c->pcur, cc = c->ccur;
+    CKR(enqueue_solve(c, true, c->mag_step, c->counts[cc], nullptr, c->prm.hydro_screening, p, false, &nl));
+    launch_zero_u32(c->stream, c->counts[1 - cc], c->P.nbins);
+    ++nl;
+    const unsigned long long n = c->P.n;
+    const unsigned long long chunk = ((n + kHostChunks - 1) / kHostChunks + 255) / 256 * 256;
+    for (int k = 0; k < kHostChunks; ++k) {
+        const unsigned long long off = (unsigned long long)k * chunk;
+        if (off >= n) break;
+        const unsigned long long cnt = (n - off < chunk) ? n - off : chunk;
+        DevParams Pk = c->P;
+        Pk.n = cnt;
+        double *xs[5];
+        for (int d = 0; d < 5; ++d) xs[d] = c->px[p][d] + off;
+        launch_update(c->stream, c->q2d, c->canon, c->mag_step, false, Pk, xs, c->key[p] + off, c->pid[p] + off,
+                      c->table, c->noise_dev, c->d_step, c->counts[1 - cc], c->d_err);
+        // the ids are the identity after the ingest: chunk k fills rows off .. off + cnt
+        launch_egest(c->stream, cnt, xs, c->pid[p] + off, c->staging);
+        nl += 2;
+        CKR(check_launch(c, "update (host step)"));
+        CK(cudaEventRecord(c->chunk_ev[k], c->stream));
+        CK(cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[k], 0));
+        CK(cudaMemcpyAsync(out + 5 * off, c->staging + 5 * off, 5 * cnt * sizeof(double), cudaMemcpyDeviceToHost,
+                           c->copy_stream));
+    }
+    launch_step_inc(c->stream, c->d_step);
+    ++nl;
+    CK(cudaEventRecord(c->chunk_ev[kHostChunks], c->copy_stream));
+    CK(cudaStreamWaitEvent(c->stream, c->chunk_ev[kHostChunks], 0));
+    CK(cudaStreamSynchronize(c->stream));
+    c->launches += nl;
+    advance(c, false);
+    return read_device_error(c);
+}
+
+int ss_step_host(ss_ctx *c, const double *in, double *out, uint64_t n, uint64_t *timestep_out) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    if (!out) return fail(c, SS_ERR_INVALID_ARGUMENT, "out is NULL");
+    CKR(load_particles(c, in, n));
+    CK(cudaSetDevice(c->device));
+    c->h_step = c->timestep;
+    CK(cudaMemcpyAsync(c->d_step, &c->h_step, sizeof c->h_step, cudaMemcpyHostToDevice, c->stream));
+    if (c->mixed) {
+        CKR(direct_step(c, false));
+        CKR(ss_get_particles(c, out, n));
+    } else {
+        CKR(step_host_fp64(c, out));
+    }
+    if (timestep_out) *timestep_out = c->timestep;
+    return SS_OK;
 }
 
 int ss_get_counts(ss_ctx *c, uint32_t *out) {

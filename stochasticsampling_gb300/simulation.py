@@ -144,6 +144,24 @@ class Simulation:
             self._check(self.lib.ss_do_timestep(self._h, _ptr(z), ctypes.byref(t)))
         return t.value
 
+    def step_host(self, particles, out=None):
+        """One step of host-resident particles (ss_step_host): `particles`
+        replace the state at the current step, the step runs, and the new
+        state comes back in `out` ((n, 5) float64, C-contiguous; may be
+        `particles` itself).  Returns `out`."""
+        p = _f64(particles, (-1, 5))
+        out = np.empty((p.shape[0], 5)) if out is None else self._out_rows(out, p.shape[0])
+        t = ctypes.c_uint64()
+        self._check(self.lib.ss_step_host(self._h, _ptr(p), _ptr(out), p.shape[0], ctypes.byref(t)))
+        return out
+
+    @staticmethod
+    def _out_rows(out, n):
+        if not (isinstance(out, np.ndarray) and out.dtype == np.float64 and out.flags.c_contiguous
+                and out.shape == (n, 5) and out.flags.writeable):
+            raise ValueError(f"out must be a writeable C-contiguous float64 array of shape ({n}, 5)")
+        return out
+
     def run(self, steps):
         t = ctypes.c_uint64()
         self._check(self.lib.ss_run(self._h, int(steps), ctypes.byref(t)))
@@ -159,7 +177,7 @@ class Simulation:
         self._check(self.lib.ss_synchronize(self._h))
 
     def get_particles(self, out=None):
-        out = np.empty((self.n, 5)) if out is None else out
+        out = np.empty((self.n, 5)) if out is None else self._out_rows(out, self.n)
         self._check(self.lib.ss_get_particles(self._h, _ptr(out), self.n))
         return out
 
