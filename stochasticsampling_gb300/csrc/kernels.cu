@@ -150,6 +150,47 @@ __global__ void k_ingest_bin(const double *__restrict__ aos, unsigned long long 
     if (err) atomicOr(errflag, err);
 }
 
+// k_ingest_bin with the row checks of k_scan_rows, for rows off .. off + n
+// of a larger array (aos, the arrays and id point at row off): scan[0] gets
+// the first row with a non-finite coordinate, scan[1] a non-zero value when
+// some row is off the canonical quasi-2-D state.  Rows with a non-finite
+// coordinate are binned like any other (their bins clamp, nothing is
+// flagged); the caller discards the whole result when scan[0] is set.
+__global__ void k_ingest_bin_check(const double *__restrict__ aos, unsigned long long n, unsigned long long off,
+                                   DevParams P, double *__restrict__ x, double *__restrict__ y,
+                                   double *__restrict__ z, double *__restrict__ phi, double *__restrict__ theta,
+                                   uint32_t *__restrict__ id, uint32_t *__restrict__ key,
+                                   uint32_t *__restrict__ counts, unsigned long long *__restrict__ scan,
+                                   uint32_t *__restrict__ errflag) {
+    const unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    bool noncanon = false;
+    if (i < n) {
+        const double *p = aos + 5 * i;
+        const unsigned long long *b = reinterpret_cast<const unsigned long long *>(p);
+        bool bad = false;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) bad |= ((b[k] >> 52) & 0x7FFull) == 0x7FFull;
+        noncanon = b[2] != 0ull || b[4] != (unsigned long long)__double_as_longlong(kPiHalf);
+        if (bad) atomicMin(&scan[0], off + i);
+        double px = ref_modulo(p[0], P.bx), py = ref_modulo(p[1], P.by), pz = ref_modulo(p[2], P.bz);
+        double ph = p[3], th = p[4];
+        ref_ang_pbc(ph, th);
+        px = ref_modulo(px, P.bx);
+        py = ref_modulo(py, P.by);
+        pz = ref_modulo(pz, P.bz);
+        ref_ang_pbc(ph, th);
+        x[i] = px; y[i] = py; z[i] = pz; phi[i] = ph; theta[i] = th;
+        id[i] = (uint32_t)(off + i);
+        uint32_t err = 0, cell;
+        unsigned long long bin;
+        bin_particle<false>(P, px, py, pz, ph, th, cell, bin, err);
+        atomicAdd(counts + bin, 1u);
+        key[i] = cell;
+        if (err && !bad) atomicOr(errflag, err);
+    }
+    if (__any_sync(0xffffffffu, noncanon) && (threadIdx.x & 31) == 0) atomicOr(&scan[1], 1ull);
+}
+
 // counts -> normalised distribution, (c / D) * V exactly as
 // sample_from + the box-volume rescale (distribution/mod.rs:183,
 // simulation/mod.rs:255-257)
@@ -595,6 +636,14 @@ void launch_ingest_bin(cudaStream_t s, bool canon, const double *aos, unsigned l
     else
         k_ingest_bin<false><<<nblocks(n, 256), 256, 0, s>>>(aos, n, P, xs[0], xs[1], xs[2], xs[3], xs[4], id, key,
                                                             counts, err);
+}
+
+void launch_ingest_bin_check(cudaStream_t s, const double *aos, unsigned long long n, unsigned long long off,
+                             const DevParams &P, double *const xs[5], uint32_t *id, uint32_t *key,
+                             uint32_t *counts, unsigned long long *scan, uint32_t *err) {
+    if (!n) return;
+    k_ingest_bin_check<<<nblocks(n, 256), 256, 0, s>>>(aos, n, off, P, xs[0], xs[1], xs[2], xs[3], xs[4], id, key,
+                                                       counts, scan, err);
 }
 
 void launch_bin(cudaStream_t s, unsigned long long n, const DevParams &P, double *const xs[5], uint32_t *key,

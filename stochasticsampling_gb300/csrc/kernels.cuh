@@ -11,6 +11,11 @@ void launch_scan_rows(cudaStream_t s, const double *aos, unsigned long long n, u
 void launch_ingest(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P, double *const xs[5],
                    uint32_t *id);
 void launch_egest(cudaStream_t s, unsigned long long n, double *const xs[5], const uint32_t *id, double *aos);
+// k_ingest_bin plus the row checks of k_scan_rows on rows off .. off + n
+// (aos, xs, id, key point at row off)
+void launch_ingest_bin_check(cudaStream_t s, const double *aos, unsigned long long n, unsigned long long off,
+                             const DevParams &P, double *const xs[5], uint32_t *id, uint32_t *key,
+                             uint32_t *counts, unsigned long long *scan, uint32_t *err);
 // k_ingest and k_bin in one pass (canon: every row in the canonical quasi-2-D state)
 void launch_ingest_bin(cudaStream_t s, bool canon, const double *aos, unsigned long long n, const DevParams &P,
                        double *const xs[5], uint32_t *id, uint32_t *key, uint32_t *counts, uint32_t *err);

@@ -44,7 +44,7 @@ void record_error(const char *msg) { g_last_error = msg; }
 }  // namespace ss
 
 // ss_step_host splits the update and the read-back into this many chunks
-constexpr int kHostChunks = 8;
+constexpr int kHostChunks = 16;
 
 struct ss_ctx {
     ss_grid grid{};
@@ -100,6 +100,7 @@ struct ss_ctx {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t chunk_ev[kHostChunks + 1] = {};
     uint64_t h_step = 0;  // host source of the step counter copy
+    uint32_t *counts_in = nullptr;  // histogram of rows being loaded, until they are accepted
     uint64_t launches = 0;
     uint64_t launches_per_step = 0;
     Timing timing;
@@ -496,6 +497,7 @@ static void destroy_impl(ss_ctx *c) {
     for (auto &e : c->chunk_ev)
         if (e) cudaEventDestroy(e);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    cudaFree(c->counts_in);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -940,6 +942,8 @@ int ss_get_particles(ss_ctx *c, double *out, uint64_t n) {
     return read_device_error(c);
 }
 
+static int ensure_host_pipeline(ss_ctx *c);
+
 // One step of host-resident particles: the rows of `in` replace the state
 // (ss_resume at the current step), one do_timestep, the new state into
 // `out`.  The update runs in chunks; each chunk is laid out as rows and
@@ -947,9 +951,7 @@ int ss_get_particles(ss_ctx *c, double *out, uint64_t n) {
 // read-back hides behind the update.  The step does not sort (sorting
 // changes no result): the particles stay in the caller's order.
 static int step_host_fp64(ss_ctx *c, double *out) {
-    if (!c->copy_stream) CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-    for (auto &e : c->chunk_ev)
-        if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CKR(ensure_host_pipeline(c));
     uint64_t nl = 0;
     const int p = c->pcur, cc = c->ccur;
     CKR(enqueue_solve(c, true, c->mag_step, c->counts[cc], nullptr, c->prm.hydro_screening, p, false, &nl));
@@ -986,11 +988,82 @@ static int step_host_fp64(ss_ctx *c, double *out) {
     return read_device_error(c);
 }
 
+static int ensure_host_pipeline(ss_ctx *c) {
+    if (!c->copy_stream) CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (auto &e : c->chunk_ev)
+        if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return SS_OK;
+}
+
+// ss_resume's load for ss_step_host (FP64 path): the upload runs in chunks
+// on the copy stream and each chunk is checked, sanitised and binned as soon
+// as it lands, into the particle buffer the state does not use and a
+// separate histogram.  Only when every row is finite do they become the
+// state, so rejected rows leave it untouched, as in ss_resume.
+static int load_host_fp64(ss_ctx *c, const double *in, uint64_t n) {
+    if (!in) return fail(c, SS_ERR_INVALID_ARGUMENT, "particles is NULL");
+    if (n != c->P.n)
+        return fail(c, SS_ERR_PARTICLE_COUNT,
+                    "Given initial condition has not the same number of particles (%llu) as given in the "
+                    "parameter file (%llu).",
+                    (unsigned long long)n, (unsigned long long)c->P.n);
+    CKR(ensure_host_pipeline(c));
+    const int alt = 1 - c->pcur;
+    const size_t N = (size_t)n;
+    if (!c->px[alt][0]) {
+        for (int k = 0; k < 5; ++k) CK(cudaMalloc((void **)&c->px[alt][k], N * sizeof(double)));
+        CK(cudaMalloc((void **)&c->key[alt], N * sizeof(uint32_t)));
+        CK(cudaMalloc((void **)&c->pid[alt], N * sizeof(uint32_t)));
+    }
+    if (!c->counts_in) CK(cudaMalloc((void **)&c->counts_in, (size_t)c->P.nbins * sizeof(uint32_t)));
+    static const unsigned long long scan_init[2] = {~0ull, 0ull};
+    unsigned long long scan[2];
+    CK(cudaMemcpyAsync(c->d_scan, scan_init, sizeof scan_init, cudaMemcpyHostToDevice, c->stream));
+    launch_zero_u32(c->stream, c->counts_in, c->P.nbins);
+    // the upload must not overwrite the staging rows before earlier work on the stream is done
+    CK(cudaEventRecord(c->chunk_ev[kHostChunks], c->stream));
+    CK(cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[kHostChunks], 0));
+    const unsigned long long chunk = ((N + kHostChunks - 1) / kHostChunks + 255) / 256 * 256;
+    uint64_t nl = 1;
+    for (int k = 0; k < kHostChunks; ++k) {
+        const unsigned long long off = (unsigned long long)k * chunk;
+        if (off >= N) break;
+        const unsigned long long cnt = (N - off < chunk) ? N - off : chunk;
+        CK(cudaMemcpyAsync(c->staging + 5 * off, in + 5 * off, 5 * cnt * sizeof(double), cudaMemcpyHostToDevice,
+                           c->copy_stream));
+        CK(cudaEventRecord(c->chunk_ev[k], c->copy_stream));
+        CK(cudaStreamWaitEvent(c->stream, c->chunk_ev[k], 0));
+        double *xs[5];
+        for (int d = 0; d < 5; ++d) xs[d] = c->px[alt][d] + off;
+        launch_ingest_bin_check(c->stream, c->staging + 5 * off, cnt, off, c->P, xs, c->pid[alt] + off,
+                                c->key[alt] + off, c->counts_in, c->d_scan, c->d_err);
+        ++nl;
+        CKR(check_launch(c, "ingest (host step)"));
+    }
+    CK(cudaMemcpyAsync(scan, c->d_scan, sizeof scan, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->launches += nl;
+    if (scan[0] != ~0ull)
+        return fail(c, SS_ERR_INVALID_ARGUMENT, "particle %llu has a non-finite coordinate", scan[0]);
+    // accept: the loaded rows are the state, their histogram the first one (Simulation::init)
+    CK(cudaMemcpyAsync(c->counts[0], c->counts_in, (size_t)c->P.nbins * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                       c->stream));
+    c->pcur = alt;
+    c->ccur = 0;
+    c->dist_idx = 0;
+    c->canon = c->q2d && scan[1] == 0ull;
+    c->fields_mag_valid = false;
+    c->solved = false;
+    c->initialized = true;
+    return SS_OK;
+}
+
 int ss_step_host(ss_ctx *c, const double *in, double *out, uint64_t n, uint64_t *timestep_out) {
     if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
     if (!out) return fail(c, SS_ERR_INVALID_ARGUMENT, "out is NULL");
-    CKR(load_particles(c, in, n));
     CK(cudaSetDevice(c->device));
+    if (c->mixed) CKR(load_particles(c, in, n));
+    else CKR(load_host_fp64(c, in, n));
     c->h_step = c->timestep;
     CK(cudaMemcpyAsync(c->d_step, &c->h_step, sizeof c->h_step, cudaMemcpyHostToDevice, c->stream));
     if (c->mixed) {

@@ -49,6 +49,12 @@ def test_step_host_equals_resume_step_get(n, flags):
         assert np.array_equal(a.get_counts(), b.get_counts()), t
         assert np.array_equal(a.get_flow_field(), b.get_flow_field()), t
         cur = ref
+    # graph-replayed steps after the host steps (the state now lives in the
+    # other particle buffer of b)
+    a.run(2)
+    b.run(2)
+    assert np.array_equal(a.get_particles(), b.get_particles())
+    assert np.array_equal(a.get_counts(), b.get_counts())
     a.close()
     b.close()
 
