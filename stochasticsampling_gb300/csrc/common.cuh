@@ -74,6 +74,9 @@ struct DevParams {
     double dthph;      // gwtheta*gwphi  (simulation/mod.rs:315)
     double sigma_rot;  // sqrt(2 Dr dt)  (simulation/mod.rs:267-270)
     double cos_half_pi, sin_half_pi;  // cos/sin of kPiHalf as evaluated on this device
+    double shape_dt, reorient_dt;     // shape * dt, magnetic_reorientation * dt (canonical table)
+    float igwf[5];     // 1 / gw in FP32 (first estimate of the bin index)
+    float bintol[5];   // half-width of the band around an integer where the FP32 estimate defers to FP64
     unsigned long long seed;
     int quasi2d;
     int bin_theta_half;  // the theta bin of pi/2 (every particle after a quasi2d step)
@@ -236,6 +239,30 @@ __device__ __forceinline__ int ref_bin(double v, double w, double iw, int n, uin
     return i;
 }
 
+// ref_bin with a first estimate in FP32: q = float(v) * float(1/w) lies
+// within 3 * 2^-24 * q (+ one ulp of 2^-126) of v / w.  When it is farther
+// than tol = 8 * 2^-24 * (n + 1) from every integer (set on the host), the
+// exact v / w and its FP64 rounding lie strictly between the same two
+// integers, so floor(q) is the reference's index; otherwise (and for v
+// outside [2^-126, 2^30), NaN included) ref_bin decides in FP64.
+__device__ __forceinline__ int ref_bin_f(double v, double w, double iw, float iwf, float tol, int n,
+                                         uint32_t &err) {
+    const long long kv = __double_as_longlong(v);
+    if (kv >= 0x3810000000000000ll && kv < 0x41D0000000000000ll) {  // [2^-126, 2^30)
+        const float q = d2f_pos(v) * iwf;
+        const float fl = floorf(q), fr = q - fl;
+        if (fr > tol && fr < 1.0f - tol) {
+            const int i = (int)fl;
+            if (i >= n) {
+                if (i > n) err |= ERR_BIN_RANGE;
+                return n - 1;
+            }
+            return i;
+        }
+    }
+    return ref_bin(v, w, iw, n, err);
+}
+
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -----------------
 __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
     constexpr uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
@@ -351,11 +378,14 @@ __device__ __forceinline__ double trig_angle(int j) {
 }
 
 // sin b and cos b - 1 for |b| <= 2^-8 (+ a few FP32 ulps): Taylor to b^5 and
-// b^6 (the first omitted terms are below 4e-18 and 2e-19 relative)
+// b^4.  The first omitted terms are below 4e-18 relative (sin) and 1.2e-17
+// absolute (cos b - 1, relative 7e-13): every caller adds cos b - 1 times a
+// factor of at most 1 to a value of order 1, where 1.2e-17 is a tenth of an
+// ulp.
 __device__ __forceinline__ void trig_small(double b, double &sb, double &cb) {
     const double z = b * b;
     sb = fma(b * z, fma(z, 1.0 / 120.0, -1.0 / 6.0), b);
-    cb = z * fma(z, fma(z, -1.0 / 720.0, 1.0 / 24.0), -0.5);
+    cb = z * fma(z, 1.0 / 24.0, -0.5);
 }
 
 // sin a and cos a (sincos for a outside [0, 6.3))
@@ -374,6 +404,7 @@ __device__ __forceinline__ void tab_sincos(double a, double &s, double &c) {
 }
 
 // sin r and cos r - 1, the latter without the cancellation of cos r - 1
+// (to 1.2e-17 absolute, see trig_small)
 __device__ __forceinline__ void sin_cosm1(double r, double &s, double &cm1) {
     const int j = trig_round(r);
     if (j < 0) {
@@ -642,65 +673,80 @@ __device__ __forceinline__ void langevin(double &x, double &y, double &z, double
     }
 }
 
+// Row of the canonical table (k_table, for quasi2d steps without the
+// dipolar solver): the fields the canonical chain reads, pre-multiplied by
+// dt: u0 dt, u1 dt, W01 dt, shape dt E00, shape dt E01, shape dt E11, the
+// diffusion length, 0.
+constexpr int CT_U0 = 0, CT_U1 = 1, CT_W01 = 2, CT_E00 = 3, CT_E01 = 4, CT_E11 = 5, CT_DIFF = 6;
+constexpr int CTAB_STRIDE = 8;
+
 // The chain of `langevin` for a quasi-2-D particle in the canonical state
 // (theta = pi/2 and z = 0, which every particle holds after a quasi2d step)
 // and no magnetic modifiers: n = (cos phi, sin phi, cos(pi/2)) with
 // cos(pi/2) (6.1e-17 in FP64) taken as 0 and sin(pi/2) == 1 exactly, so the
 // products with n_z and every z component drop out; the rotation axis then
-// enters only through k x n = (sa sin phi, -sa cos phi).  Each dropped term
-// is below half an ulp of the sum it joins, so the results can differ from
-// the full chain's in the last bit, like the rounding of sin / cos / atan2.
-// z and theta are not produced (the quasi2d step overwrites them with 0 and
-// pi/2, which the canonical state already holds).
-template <class F>
-__device__ __forceinline__ void langevin_canon(double &x, double &y, double &phi, const F &fld, const double xi[3],
-                                               double sa, double rot, uint32_t mask, double dt, double reorient,
-                                               double shape, double bx, double by) {
+// enters only through k x n = (sa sin phi, -sa cos phi).  The step's factor
+// dt is applied to the fields once per cell (the canonical table) instead
+// of to every particle's sums: dp = n dt + u dt, dn = -(W dt) n + (f - n
+// (f . n)) with f = (shape dt E) n -- the same terms, each dropped or
+// regrouped product below half an ulp of the sum it joins, so the results
+// can differ from the full chain's in the last bits, like the rounding of
+// sin / cos / atan2.  z and theta are not produced (the quasi2d step
+// overwrites them with 0 and pi/2, which the canonical state already holds).
+__device__ __forceinline__ void langevin_canon(double &x, double &y, double &phi, const double *__restrict__ ct,
+                                               const double xi[3], double sa, double rot, uint32_t mask, double dt,
+                                               double reorient_dt, double bx, double by) {
     double sp, cp;
     tab_sincos(phi, sp, cp);
-    double dp0 = 0.0, dp1 = 0.0, dn0 = 0.0, dn1 = 0.0;
-    if (mask & M_SELF_PROPULSION) {
-        dp0 = cp;
-        dp1 = sp;
+    const double2 c01 = __ldg(reinterpret_cast<const double2 *>(ct));       // u0 dt, u1 dt
+    const double2 c23 = __ldg(reinterpret_cast<const double2 *>(ct) + 1);   // W01 dt, s E00
+    const double2 c45 = __ldg(reinterpret_cast<const double2 *>(ct) + 2);   // s E01, s E11
+    const double2 c67 = __ldg(reinterpret_cast<const double2 *>(ct) + 3);   // diffusion length, 0
+    double dp0, dp1;
+    if ((mask & M_SELF_PROPULSION) && (mask & M_CONVECTION)) {
+        dp0 = fma(cp, dt, c01.x);
+        dp1 = fma(sp, dt, c01.y);
+    } else if (mask & M_SELF_PROPULSION) {
+        dp0 = cp * dt;
+        dp1 = sp * dt;
+    } else if (mask & M_CONVECTION) {
+        dp0 = c01.x;
+        dp1 = c01.y;
+    } else {
+        dp0 = 0.0;
+        dp1 = 0.0;
     }
-    if (mask & M_CONVECTION) {
-        dp0 = dp0 + fld.flow(0);
-        dp1 = dp1 + fld.flow(1);
+    double dn0 = 0.0, dn1 = 0.0;
+    if (mask & M_EXTERNAL_FIELD) {  // b = (0, reorient dt, 0): b - n (n . b)
+        const double d = sp * reorient_dt;
+        dn0 = -(cp * d);
+        dn1 = reorient_dt - sp * d;
     }
-    if (mask & M_EXTERNAL_FIELD) {  // b = (0, reorient, 0): b - n (n . b)
-        const double d = sp * reorient;
-        dn0 = dn0 + (0.0 - cp * d);
-        dn1 = dn1 + (reorient - sp * d);
+    if (mask & M_JEFFREY_VORTICITY) {  // -(W n) dt, W n = (w01 n1, -w01 n0)
+        if (mask & M_EXTERNAL_FIELD) {
+            dn0 = fma(-c23.x, sp, dn0);
+            dn1 = fma(c23.x, cp, dn1);
+        } else {
+            dn0 = -(c23.x * sp);
+            dn1 = c23.x * cp;
+        }
     }
-    if (mask & M_JEFFREY_VORTICITY) {  // -(W n), W n = (w01 n1, -w01 n0)
-        const double w01 = fld.r[T_W01];
-        dn0 = dn0 + (-(w01 * sp));
-        dn1 = dn1 + (-((-w01) * cp));
-    }
-    if (mask & M_JEFFREY_STRAIN) {  // f = shape E n, f - n (f . n)
-        const double e00 = fld.r[T_E00], e01 = fld.r[T_E01], e11 = fld.r[T_E11];
-        const double f0 = (e00 * cp + e01 * sp) * shape, f1 = (e01 * cp + e11 * sp) * shape;
-        const double fn = f0 * cp + f1 * sp;
-        dn0 = dn0 + (f0 - cp * fn);
-        dn1 = dn1 + (f1 - sp * fn);
-    }
-    if (mask & M_STEP) {
-        dp0 = dp0 * dt;
-        dp1 = dp1 * dt;
-        dn0 = dn0 * dt;
-        dn1 = dn1 * dt;
+    if (mask & M_JEFFREY_STRAIN) {  // f = shape dt E n, f - n (f . n)
+        const double f0 = fma(c23.y, cp, c45.x * sp), f1 = fma(c45.x, cp, c45.y * sp);
+        const double fn = fma(f0, cp, f1 * sp);
+        dn0 = dn0 + fma(-cp, fn, f0);
+        dn1 = dn1 + fma(-sp, fn, f1);
     }
     if (mask & M_TRANS_DIFFUSION) {
-        const double diff = fld.diff();
-        dp0 = dp0 + xi[0] * diff;
-        dp1 = dp1 + xi[1] * diff;
+        dp0 = fma(xi[0], c67.x, dp0);
+        dp1 = fma(xi[1], c67.x, dp1);
     }
-    if (mask & M_ROT_DIFFUSION) {  // n (cos rot - 1) + (k x n) sin rot
+    if (mask & M_ROT_DIFFUSION) {  // n (cos rot - 1) + (k x n) sin rot, k x n = sa (sin phi, -cos phi)
         double sr, cm1;
         sin_cosm1(rot, sr, cm1);
-        const double k0 = sa * sp, k1 = (-sa) * cp;
-        dn0 = dn0 + (cp * cm1 + k0 * sr);
-        dn1 = dn1 + (sp * cm1 + k1 * sr);
+        const double q = sa * sr;
+        dn0 = dn0 + fma(cp, cm1, sp * q);
+        dn1 = dn1 + fma(sp, cm1, -(cp * q));
     }
     const double px = x + dp0, py = y + dp1;
     const double v0 = cp + dn0, v1 = sp + dn1;

@@ -96,11 +96,11 @@ template <bool CANON = false>
 __device__ __forceinline__ void bin_particle(const DevParams &P, double x, double y, double z, double phi,
                                              double theta, uint32_t &cell, unsigned long long &bin,
                                              uint32_t &err) {
-    int ix = ref_bin(x, P.gw[0], P.igw[0], P.gx, err);
-    int iy = ref_bin(y, P.gw[1], P.igw[1], P.gy, err);
-    int iz = CANON ? 0 : ref_bin(z, P.gw[2], P.igw[2], P.gz, err);
-    int ip = ref_bin(phi, P.gw[3], P.igw[3], P.gphi, err);
-    int it = CANON ? P.bin_theta_half : ref_bin(theta, P.gw[4], P.igw[4], P.gtheta, err);
+    int ix = ref_bin_f(x, P.gw[0], P.igw[0], P.igwf[0], P.bintol[0], P.gx, err);
+    int iy = ref_bin_f(y, P.gw[1], P.igw[1], P.igwf[1], P.bintol[1], P.gy, err);
+    int iz = CANON ? 0 : ref_bin_f(z, P.gw[2], P.igw[2], P.igwf[2], P.bintol[2], P.gz, err);
+    int ip = ref_bin_f(phi, P.gw[3], P.igw[3], P.igwf[3], P.bintol[3], P.gphi, err);
+    int it = CANON ? P.bin_theta_half : ref_bin_f(theta, P.gw[4], P.igw[4], P.igwf[4], P.bintol[4], P.gtheta, err);
     cell = (uint32_t)((ix * P.gy + iy) * P.gz + iz);
     bin = (unsigned long long)cell * (unsigned long long)P.nang + (unsigned long long)(ip * P.gtheta + it);
 }
@@ -345,7 +345,8 @@ __global__ void k_kspace(const double2 *__restrict__ fwd, double2 *__restrict__ 
 // (simulation/mod.rs:302-308), Re u, Re B * mdd, Re grad B (:323-339)
 // ------------------------------------------------------------------------
 template <bool FLOW, bool MAG>
-__global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__restrict__ table, int tstride) {
+__global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__restrict__ table, int tstride,
+                        double *__restrict__ ctab) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     const int nc = P.ncell;
     if (c >= nc) return;
@@ -365,6 +366,17 @@ __global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__
         row[T_E11] = (g[4] + g[4]) * 0.5;
         row[T_E12] = (g[5] + g[7]) * 0.5;
         row[T_E22] = (g[8] + g[8]) * 0.5;
+        if (ctab) {  // the canonical quasi-2-D chain's row (CT_*), pre-multiplied by dt
+            double *cr = ctab + (long long)c * CTAB_STRIDE;
+            cr[CT_U0] = row[T_U] * P.dt;
+            cr[CT_U1] = row[T_U + 1] * P.dt;
+            cr[CT_W01] = row[T_W01] * P.dt;
+            cr[CT_E00] = row[T_E00] * P.shape_dt;
+            cr[CT_E01] = row[T_E01] * P.shape_dt;
+            cr[CT_E11] = row[T_E11] * P.shape_dt;
+            cr[CT_DIFF] = row[T_DIFF];
+            cr[7] = 0.0;
+        }
     }
     if (MAG) {
 #pragma unroll
@@ -393,7 +405,7 @@ __global__ void __launch_bounds__(256) k_update(DevParams P, double *__restrict_
                                                 uint32_t *__restrict__ counts_next, uint32_t *__restrict__ errflag) {
     unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    const int ts = (MAG || TRI) ? TABLE_STRIDE_MAG : TABLE_STRIDE;
+    const int ts = CANON ? CTAB_STRIDE : (MAG || TRI) ? TABLE_STRIDE_MAG : TABLE_STRIDE;
     uint32_t cell = key[i];
     uint32_t pid = id[i];
     double px = x[i], py = y[i], pph = phi[i];
@@ -414,7 +426,7 @@ __global__ void __launch_bounds__(256) k_update(DevParams P, double *__restrict_
         rot = r[4];
     }
     if (CANON) {
-        langevin_canon(px, py, pph, F, xi, sa, rot, P.mask, P.dt, P.reorient, P.shape, P.bx, P.by);
+        langevin_canon(px, py, pph, F.r, xi, sa, rot, P.mask, P.dt, P.reorient_dt, P.bx, P.by);
     } else {
         bool have_theta = Q2D && (__double_as_longlong(pth) == __double_as_longlong(kPiHalf));
         langevin<Q2D>(px, py, pz, pph, pth, F, xi, ca, sa, rot, P.mask, P.dt, P.reorient, P.shape, P.drag, P.bx,
@@ -689,25 +701,25 @@ void launch_kspace(cudaStream_t s, bool flow, bool mag, const double2 *fwd, doub
 }
 
 void launch_table(cudaStream_t s, bool flow, bool mag, const double2 *inv, const DevParams &P, double *table,
-                  int tstride) {
+                  int tstride, double *ctab) {
     unsigned b = nblocks(P.ncell, 128);
-    if (flow && mag) k_table<true, true><<<b, 128, 0, s>>>(inv, P, table, tstride);
-    else if (flow) k_table<true, false><<<b, 128, 0, s>>>(inv, P, table, tstride);
-    else k_table<false, true><<<b, 128, 0, s>>>(inv, P, table, tstride);
+    if (flow && mag) k_table<true, true><<<b, 128, 0, s>>>(inv, P, table, tstride, ctab);
+    else if (flow) k_table<true, false><<<b, 128, 0, s>>>(inv, P, table, tstride, ctab);
+    else k_table<false, true><<<b, 128, 0, s>>>(inv, P, table, tstride, nullptr);
 }
 
 void launch_update(cudaStream_t s, bool q2d, bool canon, bool mag, bool host_noise, const DevParams &P,
-                   double *const xs[5], uint32_t *key, const uint32_t *id, const double *table, const double *noise,
-                   const unsigned long long *d_step, uint32_t *counts_next, uint32_t *err) {
+                   double *const xs[5], uint32_t *key, const uint32_t *id, const double *table, const double *ctab,
+                   const double *noise, const unsigned long long *d_step, uint32_t *counts_next, uint32_t *err) {
     if (!P.n) return;
     unsigned b = nblocks(P.n, 256);
-    if (q2d && canon && !mag && !P.gather && !(P.mask & (M_MDD_FORCE | M_MDD_ROTATION))) {
+    if (q2d && canon && ctab && !mag && !P.gather && !(P.mask & (M_MDD_FORCE | M_MDD_ROTATION))) {
         if (host_noise)
             k_update<true, false, 1, false, true><<<b, 256, 0, s>>>(P, xs[0], xs[1], xs[2], xs[3], xs[4], key, id,
-                                                                    table, noise, d_step, counts_next, err);
+                                                                    ctab, noise, d_step, counts_next, err);
         else
             k_update<true, false, 0, false, true><<<b, 256, 0, s>>>(P, xs[0], xs[1], xs[2], xs[3], xs[4], key, id,
-                                                                    table, noise, d_step, counts_next, err);
+                                                                    ctab, noise, d_step, counts_next, err);
         return;
     }
 #define SS_UPD(Q, M, N, T)                                                                                   \

@@ -28,11 +28,12 @@ void launch_contract(cudaStream_t s, bool stress, bool mag, const uint32_t *coun
 void launch_kspace(cudaStream_t s, bool flow, bool mag, const double2 *fwd, double2 *inv, const DevParams &P,
                    double screening);
 void launch_table(cudaStream_t s, bool flow, bool mag, const double2 *inv, const DevParams &P, double *table,
-                  int tstride);
-// canon: quasi2d with every particle in the canonical state (z = 0, theta = pi/2)
+                  int tstride, double *ctab);
+// canon: quasi2d with every particle in the canonical state (z = 0, theta = pi/2);
+// ctab: the canonical table of the step (k_table), or null
 void launch_update(cudaStream_t s, bool q2d, bool canon, bool mag, bool host_noise, const DevParams &P,
-                   double *const xs[5], uint32_t *key, const uint32_t *id, const double *table, const double *noise,
-                   const unsigned long long *d_step, uint32_t *counts_next, uint32_t *err);
+                   double *const xs[5], uint32_t *key, const uint32_t *id, const double *table, const double *ctab,
+                   const double *noise, const unsigned long long *d_step, uint32_t *counts_next, uint32_t *err);
 void launch_step_inc(cudaStream_t s, unsigned long long *d_step);
 void launch_sample_initial(cudaStream_t s, bool homogeneous, const DevParams &P, double kappa, double *aos,
                            uint32_t *err);

@@ -67,6 +67,7 @@ struct ss_ctx {
     uint32_t *counts[2] = {};
     double2 *fwd = nullptr, *inv = nullptr;
     double *table = nullptr;
+    double *ctab = nullptr;  // canonical quasi-2-D rows (CT_*), FP64 quasi2d contexts
     uint32_t *cellcount = nullptr, *cursor = nullptr;
     double *kern = nullptr, *lut = nullptr;
     double *staging = nullptr, *noise_dev = nullptr, *dist_dev = nullptr, *realbuf = nullptr;
@@ -296,7 +297,8 @@ static int enqueue_solve(ss_ctx *c, bool flow, bool mag, const uint32_t *counts,
     // the table has rows for the dipolar terms only when the step uses them
     const bool table_mag = mag && c->mag_step;
     if (flow || table_mag) {
-        launch_table(c->stream, flow, table_mag, c->inv, c->P, c->table, ts);
+        launch_table(c->stream, flow, table_mag, c->inv, c->P, c->table, ts,
+                     (flow && !table_mag && !c->P.gather) ? c->ctab : nullptr);
         ++*nl;
         CKR(check_launch(c, "table"));
     }
@@ -370,7 +372,7 @@ static int enqueue_step(ss_ctx *c, int pcur, int ccur, bool host_noise, uint64_t
     mark(c, 5);
     launch_zero_u32(c->stream, c->counts[1 - ccur], c->P.nbins);
     launch_update(c->stream, c->q2d, c->canon, c->mag_step, host_noise, c->P, c->px[p], c->key[p], c->pid[p], c->table,
-                  c->noise_dev, c->d_step, c->counts[1 - ccur], c->d_err);
+                  c->ctab, c->noise_dev, c->d_step, c->counts[1 - ccur], c->d_err);
     launch_step_inc(c->stream, c->d_step);
     *nl += 3;
     CKR(check_launch(c, "update"));
@@ -483,7 +485,7 @@ static void destroy_impl(ss_ctx *c) {
         cudaFree(c->pid[b]);
         cudaFree(c->counts[b]);
     }
-    cudaFree(c->fwd); cudaFree(c->inv); cudaFree(c->table); cudaFree(c->cellcount); cudaFree(c->cursor);
+    cudaFree(c->fwd); cudaFree(c->inv); cudaFree(c->table); cudaFree(c->ctab); cudaFree(c->cellcount); cudaFree(c->cursor);
     cudaFree(c->kern); cudaFree(c->lut); cudaFree(c->staging); cudaFree(c->noise_dev); cudaFree(c->dist_dev);
     cudaFree(c->realbuf); cudaFree(c->d_step); cudaFree(c->d_err); cudaFree(c->d_scan); cudaFree(c->d_halfpi);
     for (auto &kv : c->plans_c) cufftDestroy(kv.second);
@@ -591,12 +593,21 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     P.gw[3] = kTwoPi / (double)grid->phi;
     P.gw[4] = kPi / (double)grid->theta;
     for (int k = 0; k < 5; ++k) P.igw[k] = 1.0 / P.gw[k];
+    {  // FP32 first estimate of the bin index: the band where FP64 decides (ref_bin_f)
+        const int nk[5] = {P.gx, P.gy, P.gz, P.gphi, P.gtheta};
+        for (int k = 0; k < 5; ++k) {
+            P.igwf[k] = (float)P.igw[k];
+            P.bintol[k] = (float)(8.0 * 0x1p-24 * ((double)nk[k] + 1.0));
+        }
+    }
     P.dt = params->timestep;
     P.Dt = params->trans_diffusion;
     P.Dr = params->rot_diffusion;
     P.shape = params->shape;
     P.drag = params->magnetic_drag;
     P.reorient = params->magnetic_reorientation;
+    P.shape_dt = params->shape * params->timestep;
+    P.reorient_dt = params->magnetic_reorientation * params->timestep;
     P.mdd = params->magnetic_dipole_dipole;
     P.volex = params->volume_exclusion;
     P.dist_den = P.gw[0] * P.gw[1] * P.gw[2] * P.gw[3] * P.gw[4] * (double)P.n;
@@ -667,6 +678,7 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     if (rc == SS_OK) rc = alloc((void **)&c->fwd, 12 * ncell * sizeof(double2));
     if (rc == SS_OK) rc = alloc((void **)&c->inv, 24 * ncell * sizeof(double2));
     if (rc == SS_OK) rc = alloc((void **)&c->table, ncell * TABLE_STRIDE_MAG * sizeof(double));
+    if (rc == SS_OK && c->q2d && !c->mixed) rc = alloc((void **)&c->ctab, ncell * CTAB_STRIDE * sizeof(double));
     if (rc == SS_OK) rc = alloc((void **)&c->cellcount, ncell * sizeof(uint32_t));
     if (rc == SS_OK) rc = alloc((void **)&c->cursor, ncell * sizeof(uint32_t));
     if (rc == SS_OK) rc = alloc((void **)&c->kern, 12 * nang * sizeof(double));
@@ -968,7 +980,7 @@ static int step_host_fp64(ss_ctx *c, double *out) {
         double *xs[5];
         for (int d = 0; d < 5; ++d) xs[d] = c->px[p][d] + off;
         launch_update(c->stream, c->q2d, c->canon, c->mag_step, false, Pk, xs, c->key[p] + off, c->pid[p] + off,
-                      c->table, c->noise_dev, c->d_step, c->counts[1 - cc], c->d_err);
+                      c->table, c->ctab, c->noise_dev, c->d_step, c->counts[1 - cc], c->d_err);
         // the ids are the identity after the ingest: chunk k fills rows off .. off + cnt
         launch_egest(c->stream, cnt, xs, c->pid[p] + off, c->staging);
         nl += 2;
