@@ -117,10 +117,10 @@ int ss_run(ss_ctx *ctx, uint64_t steps, uint64_t *timestep_out);
 /* The on-device noise of step `timestep` as the RandomVector array the
  * verification mode takes: out[n][5] host doubles (x, y, z, axis_angle,
  * rotate_angle) in the caller's particle order (src/bin/simulation/mod.rs:
- * 272-286).  The step uses the axis as its cosine and sine (rounded from
- * FP32 and renormalised to unit length in FP64); axis_angle is reported as
- * their atan2 in [0, 2 pi), whose sine and cosine give them back to FP64
- * rounding. */
+ * 272-286).  The step uses the axis as its sine and cosine (the sine is the
+ * FP32 sine as an exact double, the cosine sqrt(1 - sine^2) in FP64 with the
+ * FP32 cosine's sign: a unit pair); axis_angle is reported as their atan2 in
+ * [0, 2 pi), whose sine and cosine give them back to FP64 rounding. */
 int ss_noise(ss_ctx *ctx, uint64_t timestep, double *out);
 /* One do_timestep on host-resident particles: the rows of `in` ([n][5] host
  * doubles) replace the state as in ss_resume at the current step (the same

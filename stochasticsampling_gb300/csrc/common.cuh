@@ -308,10 +308,12 @@ __device__ __forceinline__ float neg2log1m(double x) {
 // of that FP32 result, and ss_noise returns the same doubles, so the FP64
 // oracle fed ss_noise sees exactly what the update used.  Radii take 52-bit
 // uniforms through neg2log1m (tails to 8.5 sigma); angles take 24-bit
-// uniforms.  The axis angle is returned as its cosine and sine, rounded to
-// FP32 and renormalised in FP64 to unit length (to 1e-21: the second-order
-// expansion of 1/sqrt(1 + d) with |d| < 2^-22), so that
-// sincos(atan2(sa, ca)) reproduces (ca, sa) to FP64 rounding.
+// uniforms.  The axis angle is returned as its sine and cosine: the sine is
+// the FP32 sine (an exact double), the cosine sqrt(1 - sine^2) in FP64 with
+// the sign of the FP32 cosine, a unit pair to FP64 rounding, so that
+// sincos(atan2(sa, ca)) reproduces (ca, sa) to FP64 rounding.  The
+// canonical quasi-2-D chain reads only the sine, which then costs no FP64
+// operation.
 template <bool Q2D, bool WANT_ALPHA = false>
 __device__ __forceinline__ void philox_noise(unsigned long long seed, uint32_t id, unsigned long long t,
                                              double sigma, double xi[3], double &ca, double &sa,
@@ -334,11 +336,9 @@ __device__ __forceinline__ void philox_noise(unsigned long long seed, uint32_t i
     }
     float saf, caf;
     sincospif(2.0f * (float)(r1.x >> 8) * 0x1p-24f, &saf, &caf);
-    const double c0 = f2d(caf), s0 = f2d(saf);
-    const double d = fma(c0, c0, fma(s0, s0, -1.0));        // |c0, s0|^2 - 1
-    const double inv = fma(d, fma(0.375, d, -0.5), 1.0);     // 1 / sqrt(1 + d)
-    ca = c0 * inv;
-    sa = s0 * inv;
+    sa = f2d(saf);
+    ca = sqrt(fma(-sa, sa, 1.0));  // |saf| <= 1: the argument is >= 0
+    ca = __longlong_as_double(__double_as_longlong(ca) | ((long long)(__float_as_uint(caf) >> 31) << 63));
     rot = sigma * f2d(sqrtf(neg2log1m(u12(r1.z, r1.w))));
     if (WANT_ALPHA) {
         double a = atan2(sa, ca);
@@ -448,6 +448,38 @@ __device__ __forceinline__ double tab_atan2(double y, double x) {
     const double at = fma(eps * z, fma(z, fma(z, -1.0 / 7.0, 1.0 / 5.0), -1.0 / 3.0), eps);
     const double ang = trig_angle(j) + at;
     return __longlong_as_double(__double_as_longlong(ang) ^ (__double_as_longlong(y) & (long long)0x8000000000000000ull));
+}
+
+// modulo(atan2(y, x), 2 pi) (particle.rs:106-121 with :26-35) through the
+// table: for y < 0 the angle is 2 pi - a_j - eps with 2 pi - a_j exact
+// (a_j a multiple of 2^-7 below pi), one rounding where the reference
+// rounds atan2 and then its sum with 2 pi, so no wrap is needed afterwards
+// (the result lies in [0, 2 pi], 2 pi only for y within an ulp below 0, as in
+// the reference).  y = -0.0 counts as y >= 0 (+0.0 where the reference
+// gives -0.0).  Inputs outside tab_atan2's range go through atan2 and
+// ref_modulo.
+__device__ __forceinline__ double tab_angle(double y, double x) {
+    const float af = atan2f(fabsf(d2f(y)), d2f(x));
+    const int j = __float2int_rn(af * 128.0f);
+    const double2 t = __ldg(&kTrig[j]);
+    const double ay = fabs(y);
+    const double d = fma(ay, t.y, x * t.x);
+    const double e = fma(-x, t.y, ay * t.x);
+    const long long db = __double_as_longlong(d);
+    const int ed = (int)(db >> 52), ee = (int)((__double_as_longlong(e) >> 52) & 0x7FF);
+    if (db < 0x3C30000000000000ll || db >= 0x43C0000000000000ll || ee > ed - 8)
+        return ref_modulo(atan2(y, x), kTwoPi);
+    const double r0 = f2d(__frcp_rn(d2f_pos(d)));
+    const double r = fma(r0, fma(-d, r0, 1.0), r0);
+    const double q = e * r;
+    const double eps = fma(r, fma(-d, q, e), q);
+    const double z = eps * eps;
+    const double at = fma(eps * z, fma(z, fma(z, -1.0 / 7.0, 1.0 / 5.0), -1.0 / 3.0), eps);
+    // y < 0: (2 pi - a_j) - eps, else a_j + eps; the choice and the sign on the integer pipe
+    const long long yb = __double_as_longlong(y), sign = (long long)0x8000000000000000ull;
+    const bool neg = yb < 0 && yb != sign;
+    const double base = neg ? __ldg(&kTwoPiMinus[j]) : trig_angle(j);
+    return base + __longlong_as_double(__double_as_longlong(at) ^ (neg ? sign : 0ll));
 }
 
 // ---- the Langevin chain ------------------------------------------------
@@ -741,18 +773,23 @@ __device__ __forceinline__ void langevin_canon(double &x, double &y, double &phi
         dp0 = fma(xi[0], c67.x, dp0);
         dp1 = fma(xi[1], c67.x, dp1);
     }
-    if (mask & M_ROT_DIFFUSION) {  // n (cos rot - 1) + (k x n) sin rot, k x n = sa (sin phi, -cos phi)
+    // v = n + dn; the rotational diffusion (n (cos rot - 1) + (k x n) sin rot,
+    // k x n = sa (sin phi, -cos phi)) joins as n cos rot + sa sin rot (sin phi, -cos phi)
+    double v0, v1;
+    if (mask & M_ROT_DIFFUSION) {
         double sr, cm1;
         sin_cosm1(rot, sr, cm1);
         const double q = sa * sr;
-        dn0 = dn0 + fma(cp, cm1, sp * q);
-        dn1 = dn1 + fma(sp, cm1, -(cp * q));
+        v0 = fma(cp, cm1, cp) + fma(sp, q, dn0);
+        v1 = fma(sp, cm1, sp) + fma(-cp, q, dn1);
+    } else {
+        v0 = cp + dn0;
+        v1 = sp + dn1;
     }
     const double px = x + dp0, py = y + dp1;
-    const double v0 = cp + dn0, v1 = sp + dn1;
     x = ref_modulo(px, bx);
     y = ref_modulo(py, by);
-    phi = ref_modulo(tab_atan2(v1, v0), kTwoPi);
+    phi = tab_angle(v1, v0);
 }
 
 }  // namespace ss
