@@ -375,57 +375,139 @@ __global__ void k_dn_transpose(const float *__restrict__ src, float *__restrict_
     }
 }
 
+// ---- tiled input and output layers -------------------------------------
+// A CTA of 128 threads takes the tile x = x0, phi = p0, p0 + 1, y = y0 ..
+// y0 + 127 (256 voxels, 2 per thread: the same y, both phi rows) and stages
+// its periodic halo (x0 +- 1, p0 - 1 .. p0 + 2, y0 - 1 .. y0 + 128) in
+// shared memory once; the 27 taps then read shared memory, and each staged
+// row serves both voxels of its thread.  Activation rows (32 channels, 64 B)
+// are stored with their four 16-byte chunks permuted by (row >> 1) & 3, so
+// that 8 consecutive rows read by one phase of a 128-bit load fall in 8
+// distinct bank groups.
+constexpr int kTileY = 128, kTileP = 2, kHaloY = kTileY + 2, kHaloP = kTileP + 2;
+constexpr int kOutSmem = 3 * kHaloP * kHaloY * 64;  // bf16 rows of the output layer's input
+
+__device__ __forceinline__ int wrap_idx(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+__device__ __forceinline__ int tile_chunk(int row, int k) { return k ^ ((row >> 1) & 3); }
+
+// tile coordinates of the CTA: blockIdx.x over (x, phi pairs, y chunks)
+__device__ __forceinline__ void tile_origin(Dims d, int &x0, int &p0, int &y0) {
+    const int ny_t = d.ny / kTileY, np_t = (d.np + kTileP - 1) / kTileP;
+    int b = blockIdx.x;
+    y0 = (b % ny_t) * kTileY;
+    b /= ny_t;
+    p0 = (b % np_t) * kTileP;
+    x0 = b / np_t;
+}
+
 // input layer 1 -> 32 channels, ReLU: A1[v] = ReLU(b_in + sum_tap w_in[tap] x[nbr(v, tap)])
 // (x in the activation layout)
-__global__ void __launch_bounds__(128) k_dn_in(const float *__restrict__ x, const float *__restrict__ P,
-                                               __nv_bfloat16 *__restrict__ A1, Dims d, int nvox) {
-    __shared__ float sw[kTaps * kC + kC];
+__global__ void __launch_bounds__(128) k_dn_in_tiled(const float *__restrict__ x, const float *__restrict__ P,
+                                                     __nv_bfloat16 *__restrict__ A1, Dims d) {
+    __shared__ __align__(16) float sw[kTaps * kC + kC];
+    __shared__ float sx[3][kHaloP][kHaloY];
+    int x0, p0, y0;
+    tile_origin(d, x0, p0, y0);
     for (int i = threadIdx.x; i < kTaps * kC + kC; i += blockDim.x) sw[i] = P[kOffWin + i];
+    for (int i = threadIdx.x; i < 3 * kHaloP * kHaloY; i += blockDim.x) {
+        const int ys = i % kHaloY, ip = (i / kHaloY) % kHaloP, ix = i / (kHaloY * kHaloP);
+        const int gx = wrap_idx(x0 + ix - 1, d.nx), gp = wrap_idx(p0 + ip - 1, d.np), gy = wrap_idx(y0 + ys - 1, d.ny);
+        sx[ix][ip][ys] = x[((size_t)gx * d.np + gp) * d.ny + gy];
+    }
     __syncthreads();
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;  // activation index
-    if (v >= nvox) return;
-    const Vox vx = Vox::from_act(v, d);
-    float a[32];
+    const int ty = threadIdx.x;
+    float a0[32], a1[32];
 #pragma unroll
-    for (int c = 0; c < kC; ++c) a[c] = sw[kTaps * kC + c];
+    for (int c = 0; c < kC; ++c) a0[c] = a1[c] = sw[kTaps * kC + c];
     for (int t = 0; t < kTaps; ++t) {
-        const float xv = x[vx.moved(t, d).act(d)];
+        const int dx = t / 9, dy = (t / 3) % 3, dp = t % 3;  // tap = (dx+1) 9 + (dy+1) 3 + (dp+1)
+        const float x0v = sx[dx][dp][ty + dy], x1v = sx[dx][dp + 1][ty + dy];
+        const float4 *w4 = reinterpret_cast<const float4 *>(sw + t * kC);
 #pragma unroll
-        for (int c = 0; c < kC; ++c) a[c] = fmaf(sw[t * kC + c], xv, a[c]);
+        for (int c4 = 0; c4 < kC / 4; ++c4) {
+            const float4 w = w4[c4];
+            a0[4 * c4] = fmaf(w.x, x0v, a0[4 * c4]);
+            a0[4 * c4 + 1] = fmaf(w.y, x0v, a0[4 * c4 + 1]);
+            a0[4 * c4 + 2] = fmaf(w.z, x0v, a0[4 * c4 + 2]);
+            a0[4 * c4 + 3] = fmaf(w.w, x0v, a0[4 * c4 + 3]);
+            a1[4 * c4] = fmaf(w.x, x1v, a1[4 * c4]);
+            a1[4 * c4 + 1] = fmaf(w.y, x1v, a1[4 * c4 + 1]);
+            a1[4 * c4 + 2] = fmaf(w.z, x1v, a1[4 * c4 + 2]);
+            a1[4 * c4 + 3] = fmaf(w.w, x1v, a1[4 * c4 + 3]);
+        }
     }
 #pragma unroll
-    for (int c = 0; c < kC; ++c) a[c] = fmaxf(a[c], 0.f);
-    store_bf16x32(A1 + (size_t)v * kC, a);
+    for (int c = 0; c < kC; ++c) {
+        a0[c] = fmaxf(a0[c], 0.f);
+        a1[c] = fmaxf(a1[c], 0.f);
+    }
+    const int y = y0 + ty;
+    store_bf16x32(A1 + (((size_t)x0 * d.np + p0) * d.ny + y) * kC, a0);
+    if (p0 + 1 < d.np) store_bf16x32(A1 + (((size_t)x0 * d.np + p0 + 1) * d.ny + y) * kC, a1);
 }
 
 // output layer 32 -> 1 with the residual: y[v] = x[v] + b_out + sum_tap w_out[tap] . A3[nbr(v, tap)]
-// (x and y in the activation layout).  Four threads per voxel, 8 channels
-// each (one 16-byte load per tap), summed with two shuffles.
-__global__ void __launch_bounds__(128) k_dn_out(const __nv_bfloat16 *__restrict__ A3, const float *__restrict__ x,
-                                                const float *__restrict__ P, float *__restrict__ y, Dims d, int nvox) {
-    __shared__ float sw[kTaps * kC + 1];
+// (x and y in the activation layout)
+__global__ void __launch_bounds__(128) k_dn_out_tiled(const __nv_bfloat16 *__restrict__ A3,
+                                                      const float *__restrict__ x, const float *__restrict__ P,
+                                                      float *__restrict__ y, Dims d) {
+    extern __shared__ __align__(16) unsigned char dn_out_smem[];
+    float *sw = reinterpret_cast<float *>(dn_out_smem + kOutSmem);
+    int x0, p0, y0;
+    tile_origin(d, x0, p0, y0);
+    const uint32_t base = smem_u32(dn_out_smem);
+    for (int i = threadIdx.x; i < 3 * kHaloP * kHaloY * 4; i += blockDim.x) {
+        const int k = i & 3, r = i >> 2;  // 16-byte chunk k of staged row r
+        const int ys = r % kHaloY, ip = (r / kHaloY) % kHaloP, ix = r / (kHaloY * kHaloP);
+        const int gx = wrap_idx(x0 + ix - 1, d.nx), gp = wrap_idx(p0 + ip - 1, d.np), gy = wrap_idx(y0 + ys - 1, d.ny);
+        cp_async16(base + (uint32_t)(r * 64 + tile_chunk(ys, k) * 16),
+                   A3 + (((size_t)gx * d.np + gp) * d.ny + gy) * kC + 8 * k);
+    }
+    cp_async_commit();
     for (int i = threadIdx.x; i < kTaps * kC + 1; i += blockDim.x) sw[i] = P[kOffWout + i];
+    cp_async_wait<0>();
     __syncthreads();
-    const int g = blockIdx.x * blockDim.x + threadIdx.x, v = g >> 2, q = g & 3;
-    const bool live = v < nvox;
-    float acc = 0.f;
-    if (live) {
-        const Vox vx = Vox::from_act(v, d);
-        for (int t = 0; t < kTaps; ++t) {
-            const uint4 u = *reinterpret_cast<const uint4 *>(A3 + (size_t)vx.moved(t, d).act(d) * kC + 8 * q);
-            const uint32_t w[4] = {u.x, u.y, u.z, u.w};
-            const float *wt = sw + t * kC + 8 * q;
+    const int ty = threadIdx.x;
+    // one partial sum per 8-channel chunk and voxel: 8 independent FMA chains per thread
+    float acc0[4] = {0.f, 0.f, 0.f, 0.f}, acc1[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int dx = 0; dx < 3; ++dx) {
+        for (int dy = 0; dy < 3; ++dy) {
+            const int ys = ty + dy;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162 *>(&w[j]);
-                acc = fmaf(wt[2 * j], __low2float(h), acc);
-                acc = fmaf(wt[2 * j + 1], __high2float(h), acc);
+            for (int ip = 0; ip < kHaloP; ++ip) {
+                // staged row (dx, ip, ys) is tap (dx, dy, ip) of voxel p0 and tap (dx, dy, ip - 1) of voxel p0 + 1
+                const int r = (dx * kHaloP + ip) * kHaloY + ys;
+                const float4 *w0 = reinterpret_cast<const float4 *>(sw + (dx * 9 + dy * 3 + ip) * kC);
+                const float4 *w1 = reinterpret_cast<const float4 *>(sw + (dx * 9 + dy * 3 + ip - 1) * kC);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const uint4 u = *reinterpret_cast<const uint4 *>(dn_out_smem + r * 64 + tile_chunk(ys, k) * 16);
+                    const float v[8] = {__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xFFFF0000u),
+                                        __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xFFFF0000u),
+                                        __uint_as_float(u.z << 16), __uint_as_float(u.z & 0xFFFF0000u),
+                                        __uint_as_float(u.w << 16), __uint_as_float(u.w & 0xFFFF0000u)};
+                    if (ip < 3) {
+                        const float4 a = w0[2 * k], b = w0[2 * k + 1];
+                        float t = acc0[k];
+                        t = fmaf(a.x, v[0], t); t = fmaf(a.y, v[1], t); t = fmaf(a.z, v[2], t); t = fmaf(a.w, v[3], t);
+                        t = fmaf(b.x, v[4], t); t = fmaf(b.y, v[5], t); t = fmaf(b.z, v[6], t); t = fmaf(b.w, v[7], t);
+                        acc0[k] = t;
+                    }
+                    if (ip > 0) {
+                        const float4 a = w1[2 * k], b = w1[2 * k + 1];
+                        float t = acc1[k];
+                        t = fmaf(a.x, v[0], t); t = fmaf(a.y, v[1], t); t = fmaf(a.z, v[2], t); t = fmaf(a.w, v[3], t);
+                        t = fmaf(b.x, v[4], t); t = fmaf(b.y, v[5], t); t = fmaf(b.z, v[6], t); t = fmaf(b.w, v[7], t);
+                        acc1[k] = t;
+                    }
+                }
             }
         }
     }
-    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-    if (live && q == 0) y[v] = x[v] + acc + sw[kTaps * kC];
+    const float bo = sw[kTaps * kC];
+    const size_t v0 = ((size_t)x0 * d.np + p0) * d.ny + y0 + ty;
+    y[v0] = x[v0] + ((acc0[0] + acc0[1]) + (acc0[2] + acc0[3])) + bo;
+    if (p0 + 1 < d.np) y[v0 + d.ny] = x[v0 + d.ny] + ((acc1[0] + acc1[1]) + (acc1[2] + acc1[3])) + bo;
 }
 
 // mean-square loss against the target and its gradient dy = 2 (y - t) / V;
@@ -763,6 +845,8 @@ void conv_attrs() {
     cudaFuncSetAttribute(k_conv32<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
     cudaFuncSetAttribute(k_conv32<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
     cudaFuncSetAttribute(k_conv32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
+    cudaFuncSetAttribute(k_dn_out_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kOutSmem + (kTaps * kC + 4) * (int)sizeof(float));
     done = true;
 }
 
@@ -792,10 +876,11 @@ void transpose(ss_dn *n, const float *src, float *dst, cudaStream_t s) {
 void enqueue_forward_act(ss_dn *n, const float *x, float *ya, cudaStream_t s) {
     const unsigned b = (unsigned)((n->nvox + 127) / 128);
     transpose<true>(n, x, n->xa, s);
-    k_dn_in<<<b, 128, 0, s>>>(n->xa, n->P, n->A1, n->d, n->nvox);
+    const unsigned tiles = (unsigned)(n->d.nx * ((n->d.np + kTileP - 1) / kTileP) * (n->d.ny / kTileY));
+    k_dn_in_tiled<<<tiles, 128, 0, s>>>(n->xa, n->P, n->A1, n->d);
     launch_conv<0>(n, n->A1, n->Wp2, n->P + kOffB2, nullptr, n->A2, s);
     launch_conv<0>(n, n->A2, n->Wp3, n->P + kOffB3, nullptr, n->A3, s);
-    k_dn_out<<<4 * b, 128, 0, s>>>(n->A3, n->xa, n->P, ya, n->d, n->nvox);
+    k_dn_out_tiled<<<tiles, 128, kOutSmem + (kTaps * kC + 4) * sizeof(float), s>>>(n->A3, n->xa, n->P, ya, n->d);
     n->launches += 5;
 }
 
