@@ -85,8 +85,9 @@ def evaluate(dn, steps=2000, every=200, n_low=1_000_000, n_ref=64_000_000, plain
     runs = {}
 
     def make(n, s, mixed=False):
+        # without the per-step counting sort: the plain FP64 runs' fastest form
         p = dict(PARAMS, number_of_particles=n, seed=s)
-        sim = ss.Simulation(grid=GRID, box=BOX, params=p, quasi2d=True, mixed=mixed)
+        sim = ss.Simulation(grid=GRID, box=BOX, params=p, quasi2d=True, mixed=mixed, sort=False)
         sim.init(initial_rows(n, seed=s))
         return sim
 
