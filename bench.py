@@ -3,10 +3,11 @@ workload (N = 1e7 particles, grid 128x128x1x32x1, box 40x40, Dt 0.1, Dr 1.0,
 active stress -2, dt 0.005, 1 % sinusoidal density perturbation along x),
 plain FP64 path (the headline `value`), with sections for the FP32 mixed
 path (FP64 and fixed-point positions), the batched ensemble of 64 parameter
-sets and the learned denoiser in the loop.
+sets, the learned denoiser in the loop and the 3-D magnetic workload (2e7
+particles, grid 64^3 x 16 x 8; FP64 and FP32 mixed).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--no-mixed] [--no-ensemble] [--no-denoise] [--only SECTION]
+                    [--no-mixed] [--no-ensemble] [--no-denoise] [--no-c2] [--only SECTION]
 
 One JSON line on stdout (rank 0).  --impl reference times the CPU path of the
 same workload instead: the FP64 C restatement of the reference timestep
@@ -321,6 +322,88 @@ def measure_mixed(args, stream, p0, rank, world, dist, barrier, mode=True):
             "errors_vs_fp64_one_step": errors}
 
 
+# 3-D workload with the dipolar solver: box 20^3, grid 64x64x64x16x8,
+# 2e7 particles (uniform positions, orientations uniform on the sphere),
+# dipolar coupling 0.5, external field 1 (along the reference's field axis),
+# active stress -1, Dt 0.1, Dr 1.0, dt 0.002
+C2_GRID = (64, 64, 64, 16, 8)
+C2_BOX = (20.0, 20.0, 20.0)
+C2_N = 20_000_000
+C2_PARAMS = dict(timestep=0.002, trans_diffusion=0.1, rot_diffusion=1.0, stress_active=-1.0,
+                 magnetic_reorientation=1.0, magnetic_dipole_dipole=0.5)
+
+
+def c2_particles(n, seed=3):
+    rng = np.random.default_rng(seed)
+    return np.column_stack([C2_BOX[0] * rng.random(n), C2_BOX[1] * rng.random(n), C2_BOX[2] * rng.random(n),
+                            TWOPI * rng.random(n), np.arccos(1 - 2 * rng.random(n))])
+
+
+def measure_c2(args, stream, rank, world, dist, barrier):
+    """The 3-D magnetic workload: the plain FP64 path and the FP32 mixed path
+    (FP64 positions), each over graph-replayed steps, and the mixed path's
+    errors per field against the FP64 path after one step from identical
+    state and noise."""
+    import torch
+
+    import stochasticsampling_gb300 as ss
+    n = C2_N if not args.particles else max(1, args.particles * 2)
+    steps = max(1, min(args.steps, 20))
+    params = dict(C2_PARAMS, number_of_particles=n, seed=5 + rank)
+    p0 = c2_particles(n, seed=3 + rank)
+    out = {"workload": "3-D with the dipolar solver: box 20^3, grid 64x64x64x16x8, uniform positions and "
+                       "orientations on the sphere, dipolar coupling 0.5, external field 1, active stress -1, "
+                       "Dt 0.1, Dr 1.0, dt 0.002", "particles": n, "steps": steps}
+    for name, mode in (("fp64", False), ("mixed", True)):
+        sim = ss.Simulation(grid=C2_GRID, box=C2_BOX, params=params, mixed=mode, stream=stream.cuda_stream)
+        sim.init(p0)
+        with torch.cuda.stream(stream):
+            sim.run(args.warmup)
+            torch.cuda.synchronize()
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sim.run(steps)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            barrier()
+            ms = e0.elapsed_time(e1)
+        sim.profile(True)
+        sim.run(min(steps, 5))
+        stage_ms, nprof = sim.profile_read()
+        sim.profile(False)
+        sim.close()
+        value, ms_max = aggregate(ms, n, steps, world, dist)
+        out[name] = {"value": value, "unit": UNIT, "ms_per_step": ms_max / steps,
+                     "dtype": "f32 + f64 positions" if mode else "f64",
+                     "stage_ms": {k: v / max(1, nprof) for k, v in stage_ms.items()}}
+    m = ss.Simulation(grid=C2_GRID, box=C2_BOX, params=params, mixed=True)
+    d = ss.Simulation(grid=C2_GRID, box=C2_BOX, params=params)
+    m.init(p0)
+    d.init(p0)
+    cm, cd = m.get_counts().astype(np.float64), d.get_counts().astype(np.float64)
+    noise = m.noise(0)
+    m.do_timestep()
+    d.do_timestep(noise)
+    um, ud = m.get_flow_field(), d.get_flow_field()
+    bm, bd = m.get_magnetic_field(), d.get_magnetic_field()
+    pm, pd = m.get_particles(), d.get_particles()
+    disp = np.linalg.norm(pd[:, :3] - p0[:, :3])
+    ang = np.abs(pm[:, 3] - pd[:, 3])
+    ang = np.minimum(ang, 2 * np.pi - ang)
+    out["mixed"]["errors_vs_fp64_one_step"] = {
+        "histogram_l1_rel": float(np.abs(cm - cd).sum() / cd.sum()),
+        "flow_l2_rel": float(np.linalg.norm(um - ud) / np.linalg.norm(ud)),
+        "magnetic_l2_rel": float(np.linalg.norm(bm - bd) / np.linalg.norm(bd)),
+        "position_l2_rel_to_displacement": float(np.linalg.norm((pm - pd)[:, :3]) / disp),
+        "phi_rms_rad": float(np.sqrt(np.mean(ang ** 2))),
+        "theta_rms_rad": float(np.sqrt(np.mean((pm[:, 4] - pd[:, 4]) ** 2))),
+    }
+    m.close()
+    d.close()
+    return out
+
+
 def measure_ensemble(args, stream, rank, world, dist, barrier):
     """The batched ensemble: 64 independent 2-D simulations (particle counts
     log-uniform in [50k, 2M], grid edges {32, 64, 128}, 16 or 32 phi bins,
@@ -445,6 +528,8 @@ def run_gpu(args, rank, world, dist):
     if args.only:
         if args.only == "ensemble":
             res = measure_ensemble(args, stream, rank, world, dist, barrier)
+        elif args.only == "c2":
+            res = measure_c2(args, stream, rank, world, dist, barrier)
         elif args.only == "denoised":
             res = measure_denoised(args, rank)
         else:
@@ -521,6 +606,7 @@ def run_gpu(args, rank, world, dist):
     mixed = None if args.no_mixed else measure_mixed(args, stream, p0, rank, world, dist, barrier)
     mixed_fixed = None if args.no_mixed else measure_mixed(args, stream, p0, rank, world, dist, barrier, "fixed64")
     ensemble = None if args.no_ensemble else measure_ensemble(args, stream, rank, world, dist, barrier)
+    c2 = None if args.no_c2 else measure_c2(args, stream, rank, world, dist, barrier)
     denoised = None if args.no_denoise else measure_denoised(args, rank)
 
     if rank != 0:
@@ -587,6 +673,7 @@ def run_gpu(args, rank, world, dist):
         "mixed": mixed,
         "mixed_fixed64": mixed_fixed,
         "ensemble": ensemble,
+        "c2_3d_magnetic": c2,
         "denoised": denoised,
     }
     print(json.dumps(line), flush=True)
@@ -602,10 +689,11 @@ def main():
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32 mixed-precision measurement")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-denoise", action="store_true", help="skip the learned-denoiser measurement")
+    ap.add_argument("--no-c2", action="store_true", help="skip the 3-D magnetic measurement")
     ap.add_argument("--denoise-pairs", type=int, default=1000)
     ap.add_argument("--denoise-epochs", type=int, default=1)
     ap.add_argument("--denoise-steps", type=int, default=400)
-    ap.add_argument("--only", choices=["mixed", "fixed64", "ensemble", "denoised"], default=None,
+    ap.add_argument("--only", choices=["mixed", "fixed64", "ensemble", "denoised", "c2"], default=None,
                     help="run one section alone (a smaller command for profiling); prints its JSON")
     ap.add_argument("--ensemble-members", type=int, default=64)
     ap.add_argument("--ensemble-config", default=None,
