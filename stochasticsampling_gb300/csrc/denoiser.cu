@@ -56,7 +56,8 @@ constexpr int kBAll = kTaps * kBTap;         // 54 KB
 constexpr int kLineRows = kTileM + 2;        // y = -1 .. 128 of a segment
 constexpr int kChunkBytes = kLineRows * 16;  // one 16-byte K chunk of every row of a line
 constexpr int kLineBytes = 4 * kChunkBytes;  // 8320 B
-constexpr int kSlots = 12;                   // 3 x-planes x 4 positions along phi
+constexpr int kRing = 6;                     // positions along phi per x-plane: 3 in use, 1 freeing, 2 landing
+constexpr int kSlots = 3 * kRing;            // line buffers
 constexpr int kPChunk = 4;                   // tiles along phi per work item
 constexpr int kSmemConv = kBAll + kSlots * kLineBytes + 128;  // + the mbarrier, tensor-memory slot, failure flag
 static_assert(kSmemConv <= 227 * 1024, "the convolution's shared memory exceeds a CTA's limit");
@@ -173,6 +174,11 @@ __host__ __device__ __forceinline__ int core_offset(int row, int k) {
 
 // MODE 0: bias + ReLU -> BF16; MODE 1: bias -> FP32; MODE 2: times ReLU'(ref) -> BF16.
 // Work item = (x, y segment, kPChunk consecutive phi); ny a multiple of 128.
+// Two accumulators in tensor memory (columns 0-31 and 32-63) pipeline the
+// tiles of a work item: the MMAs of tile k run while the CTA's warps take
+// tile k - 1's accumulator out (epilogue) and start the copies of the line
+// tile k + 2 adds, two tiles ahead, into the ring slot of a line whose last
+// MMAs completed before.
 template <int MODE>
 __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__restrict__ X,
                                                       const uint8_t *__restrict__ Wpacked,
@@ -182,8 +188,8 @@ __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__res
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *sB = smem;
     uint8_t *sL = smem + kBAll;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(sL + kSlots * kLineBytes);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 1);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(sL + kSlots * kLineBytes);  // one per accumulator
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
     volatile int *sfail = reinterpret_cast<volatile int *>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -191,10 +197,11 @@ __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__res
         reinterpret_cast<uint4 *>(sB)[i] = reinterpret_cast<const uint4 *>(Wpacked)[i];
     if (tid == 0) {
         mbar_init(smem_u32(mbar), 1);
+        mbar_init(smem_u32(mbar + 1), 1);
         *sfail = 0;
         fence_mbar_init();
     }
-    if (warp == 0) tmem_alloc(smem_u32(tslot), 32);
+    if (warp == 0) tmem_alloc(smem_u32(tslot), 64);
     fence_proxy_async();
     tc_before_sync();
     __syncthreads();
@@ -202,18 +209,18 @@ __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__res
     const uint32_t tmem = *tslot;
     const uint32_t sL0 = smem_u32(sL), sB0 = smem_u32(sB);
     const int nseg = d.ny / kTileM, npc = (d.np + kPChunk - 1) / kPChunk;
-    uint32_t phase = 0;
+    uint32_t phase0 = 0, phase1 = 0;
 
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         const int pc = item % npc, ys = (item / npc) % nseg, x = item / (npc * nseg);
         const int p0 = pc * kPChunk, pcount = min(kPChunk, d.np - p0), y0 = ys * kTileM;
-        // line (x + dx, p0 + q - 1) of this segment, rows y0 - 1 .. y0 + 128, into slot (dx + 1) 4 + q % 4
+        // line (x + dx, p0 + q - 1) of this segment, rows y0 - 1 .. y0 + 128, into slot (dx + 1) kRing + q % kRing
         auto load_line = [&](int dx, int q) {
             int xl = x + dx, pl = p0 + q - 1;
             xl = xl < 0 ? xl + d.nx : (xl >= d.nx ? xl - d.nx : xl);
             pl = ((pl % d.np) + d.np) % d.np;
             const __nv_bfloat16 *line = X + (size_t)(xl * d.np + pl) * d.ny * kC;
-            const uint32_t dst0 = sL0 + (uint32_t)(((dx + 1) * 4 + (q & 3)) * kLineBytes);
+            const uint32_t dst0 = sL0 + (uint32_t)(((dx + 1) * kRing + q % kRing) * kLineBytes);
             for (int e = tid; e < kLineRows * 4; e += kTileM) {
                 const int r = e >> 2, j = e & 3;
                 int yl = y0 + r - 1;
@@ -221,47 +228,16 @@ __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__res
                 cp_async16(dst0 + j * kChunkBytes + r * 16, line + (size_t)yl * kC + j * 8);
             }
         };
-        for (int q = 0; q < 3; ++q)
-            for (int dx = -1; dx <= 1; ++dx) load_line(dx, q);
-        cp_async_commit();
-        for (int k = 0; k < pcount; ++k) {
-            // the line the next tile adds goes where the line of tile k - 1's
-            // first phi row was (its MMAs completed before this iteration)
-            if (k + 3 <= pcount + 1)
-                for (int dx = -1; dx <= 1; ++dx) load_line(dx, k + 3);
-            cp_async_commit();
-            cp_async_wait<1>();  // the lines of tile k have landed
-            fence_proxy_async();
-            __syncthreads();
-            if (*sfail) break;
-            if (tid == 0) {
-                tc_after_sync();
-                uint32_t acc = 0;
-                for (int dx = -1; dx <= 1; ++dx)
-                    for (int dp = -1; dp <= 1; ++dp) {
-                        const uint32_t line = sL0 + (uint32_t)(((dx + 1) * 4 + ((k + 1 + dp) & 3)) * kLineBytes);
-#pragma unroll
-                        for (int dy = -1; dy <= 1; ++dy) {
-                            const int tap = (dx + 1) * 9 + (dy + 1) * 3 + (dp + 1);
-#pragma unroll
-                            for (int kk = 0; kk < 2; ++kk) {
-                                const uint64_t ad = smem_desc(line + kk * 2 * kChunkBytes + (1 + dy) * 16, kChunkBytes, 128);
-                                const uint64_t bd = smem_desc(sB0 + tap * kBTap + kk * 256, 128, 512);
-                                mma_bf16(tmem, ad, bd, kIdesc, acc);
-                                acc = 1;
-                            }
-                        }
-                    }
-                mma_commit(smem_u32(mbar));
-            }
-            if (!mbar_wait(smem_u32(mbar), phase)) *sfail = 1;
-            phase ^= 1u;
-            __syncthreads();
-            if (*sfail) break;
+        // accumulator of tile kt -> bias / ReLU -> Y (every thread one row)
+        auto epilogue = [&](int kt) -> bool {
+            const int a = kt & 1;
+            if (!mbar_wait(smem_u32(mbar + a), a ? phase1 : phase0)) return false;
+            if (a) phase1 ^= 1u;
+            else phase0 ^= 1u;
             tc_after_sync();
             uint32_t r[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), r);
-            const size_t vo = (size_t)((x * d.np + p0 + k) * d.ny + y0 + warp * 32 + lane);  // this thread's row
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(32 * a), r);
+            const size_t vo = (size_t)((x * d.np + p0 + kt) * d.ny + y0 + warp * 32 + lane);  // this thread's row
             if (MODE == 1) {
                 float4 *out = reinterpret_cast<float4 *>(reinterpret_cast<float *>(Y) + vo * kC);
 #pragma unroll
@@ -274,16 +250,16 @@ __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__res
                 uint32_t packed[16];
 #pragma unroll
                 for (int q = 0; q < 16; ++q) {
-                    float a = __uint_as_float(r[2 * q]), b = __uint_as_float(r[2 * q + 1]);
+                    float a0 = __uint_as_float(r[2 * q]), b0 = __uint_as_float(r[2 * q + 1]);
                     if (MODE == 0) {
-                        a = fmaxf(a + bias[2 * q], 0.f);
-                        b = fmaxf(b + bias[2 * q + 1], 0.f);
+                        a0 = fmaxf(a0 + bias[2 * q], 0.f);
+                        b0 = fmaxf(b0 + bias[2 * q + 1], 0.f);
                     } else {
                         const __nv_bfloat16 *rr = ref + vo * kC;
-                        a = __bfloat162float(rr[2 * q]) > 0.f ? a : 0.f;
-                        b = __bfloat162float(rr[2 * q + 1]) > 0.f ? b : 0.f;
+                        a0 = __bfloat162float(rr[2 * q]) > 0.f ? a0 : 0.f;
+                        b0 = __bfloat162float(rr[2 * q + 1]) > 0.f ? b0 : 0.f;
                     }
-                    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+                    __nv_bfloat162 h = __floats2bfloat162_rn(a0, b0);
                     packed[q] = *reinterpret_cast<uint32_t *>(&h);
                 }
                 uint4 *out = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(Y) + vo * kC);
@@ -291,18 +267,66 @@ __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__res
                 for (int q = 0; q < 4; ++q)
                     out[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
             }
-            // every thread's tensor-memory reads finish before the next tile's MMAs overwrite it
+            return true;
+        };
+        for (int q = 0; q < 3; ++q)
+            for (int dx = -1; dx <= 1; ++dx) load_line(dx, q);
+        cp_async_commit();
+        if (3 <= pcount + 1)
+            for (int dx = -1; dx <= 1; ++dx) load_line(dx, 3);
+        cp_async_commit();
+        int k = 0;
+        for (; k < pcount; ++k) {
+            // the line tile k + 2 adds goes into the slot of line k - 2, whose
+            // last MMAs (tile k - 2) completed before tile k - 2's epilogue
+            if (k + 4 <= pcount + 1)
+                for (int dx = -1; dx <= 1; ++dx) load_line(dx, k + 4);
+            cp_async_commit();
+            cp_async_wait<2>();  // the lines of tile k have landed
+            fence_proxy_async();
+            __syncthreads();
+            if (*sfail) break;
+            if (tid == 0) {
+                tc_after_sync();
+                const uint32_t dacc = tmem + (uint32_t)(32 * (k & 1));
+                uint32_t acc = 0;
+                for (int dx = -1; dx <= 1; ++dx)
+                    for (int dp = -1; dp <= 1; ++dp) {
+                        const uint32_t line = sL0 + (uint32_t)(((dx + 1) * kRing + (k + 1 + dp) % kRing) * kLineBytes);
+#pragma unroll
+                        for (int dy = -1; dy <= 1; ++dy) {
+                            const int tap = (dx + 1) * 9 + (dy + 1) * 3 + (dp + 1);
+#pragma unroll
+                            for (int kk = 0; kk < 2; ++kk) {
+                                const uint64_t ad = smem_desc(line + kk * 2 * kChunkBytes + (1 + dy) * 16, kChunkBytes, 128);
+                                const uint64_t bd = smem_desc(sB0 + tap * kBTap + kk * 256, 128, 512);
+                                mma_bf16(dacc, ad, bd, kIdesc, acc);
+                                acc = 1;
+                            }
+                        }
+                    }
+                mma_commit(smem_u32(mbar + (k & 1)));
+            }
+            // tile k - 1 leaves its accumulator while tile k's MMAs run
+            if (k > 0 && !epilogue(k - 1)) *sfail = 1;
+            // every thread's tensor-memory reads finish before tile k + 1's MMAs overwrite that accumulator
             tc_before_sync();
             __syncthreads();
         }
         if (*sfail) break;
+        if (pcount > 0) {
+            if (!epilogue(pcount - 1)) *sfail = 1;
+            tc_before_sync();
+            __syncthreads();
+            if (*sfail) break;
+        }
     }
     if (*sfail && tid == 0) atomicOr(err, kErrTimeout);
     cp_async_wait<0>();
     tc_before_sync();
     __syncthreads();
     tc_after_sync();
-    if (warp == 0) tmem_dealloc(tmem, 32);
+    if (warp == 0) tmem_dealloc(tmem, 64);
 }
 
 // FP32 weights W[tap][n][k] -> BF16 in the K-major core-matrix layout of the
