@@ -309,8 +309,8 @@ __global__ void __launch_bounds__(512, MINB) k_ens_update(const WorkUnit *__rest
             philox_noise_f<true>(M.seed, (uint32_t)(i - E.part_off), t, M.sigma_rot, xi, ca, sa, rot);
             float st[3];
             langevin_mixed<true>(pph, pth, st, F, xi, ca, sa, rot, M);
-            px = advance64(px, st[0], cx, M.gx, M.gwf[0], M.bx, M.bx2);
-            py = advance64(py, st[1], cy, M.gy, M.gwf[1], M.by, M.by2);
+            px = advance64(px, st[0], M.bx);
+            py = advance64(py, st[1], M.by);
             int cell, bin;
             bin2d(M, px, py, pph, cell, bin);
             atomicAdd(counts_next + E.bin_off + bin, 1u);

@@ -333,12 +333,10 @@ __global__ void __launch_bounds__(256) k_update_m(MixedParams M, double *__restr
         Y[i] = py;
         if (!CANON) Z[i] = pz;
     } else {
-        const int gyz = M.gy * M.gz;
-        const int cx = (int)cell / gyz, cy = ((int)cell / M.gz) % M.gy, cz = (int)cell % M.gz;
-        double px = advance64(x[i], st[0], cx, M.gx, M.gwf[0], M.bx, M.bx2);
-        double py = advance64(y[i], st[1], cy, M.gy, M.gwf[1], M.by, M.by2);
+        double px = advance64(x[i], st[0], M.bx);
+        double py = advance64(y[i], st[1], M.by);
         double pz = 0.0;
-        if (!Q2D) pz = advance64(z[i], st[2], cz, M.gz, M.gwf[2], M.bz, M.bz2);
+        if (!Q2D) pz = advance64(z[i], st[2], M.bz);
         bin_mixed(M, px, py, pz, pph, pth, ncell, bin);
         x[i] = px;
         y[i] = py;

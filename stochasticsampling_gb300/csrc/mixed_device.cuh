@@ -222,24 +222,9 @@ __device__ __forceinline__ void langevin_mixed(float &phi, float &theta, float s
 }
 
 // FP64 position advance: x + dx wrapped into [0, L) (modulo of
-// src/particle.rs:26-35 with 2L precomputed).  From an interior cell a step
-// shorter than one cell cannot leave the box, so only particles in the first
-// or last cell of the axis, or with long steps, pay for the wrap tests.
-// The wrap is a called function so that the compiler does not evaluate its
-// FP64 compares (predicated) for the interior particles too.
-static __device__ __noinline__ double wrap64(double xn, double L, double L2) {
-    if (xn > -L && xn < L2) {
-        if (xn >= L) return xn - L;
-        if (xn < 0.0) return xn + L;
-        return xn;
-    }
-    double r = fmod(xn, L);
-    return r < 0.0 ? r + L : r;
-}
-__device__ __forceinline__ double advance64(double x, float dx, int cell, int n, float w, double L, double L2) {
-    const double xn = x + f2d(dx);
-    if (cell > 0 && cell < n - 1 && fabsf(dx) < w) return xn;
-    return wrap64(xn, L, L2);
-}
+// src/particle.rs:26-35), with ref_modulo's range tests on the integer pipe:
+// an FP64 compare would occupy GB300's FP64 pipe for a whole warp whenever
+// one of its particles sits in an edge cell.
+__device__ __forceinline__ double advance64(double x, float dx, double L) { return ref_modulo(x + f2d(dx), L); }
 
 }  // namespace ss
