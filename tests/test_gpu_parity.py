@@ -208,6 +208,17 @@ def test_quasi2d_off_canonical_rows(oracle):
     g.close()
 
 
+def test_fp64_rate_probe():
+    """ss_fp64_rate: the FP64 FMA rate of the device, a positive finite rate
+    below the nominal peak of any current GPU."""
+    import ctypes
+    ss = _gpu()
+    from stochasticsampling_gb300 import _lib
+    r = ctypes.c_double()
+    _lib.check(_lib.load().ss_fp64_rate(ctypes.byref(r)))
+    assert 1e9 < r.value < 1e14, r.value
+
+
 def test_philox_noise_statistics():
     ss = _gpu()
     n = 1_000_000
