@@ -585,17 +585,24 @@ def run_gpu(args, rank, world, dist):
 
     def e2e_loop(fused):
         nonlocal host_in, host_out
+
+        def one(k0):
+            if fused:
+                sim.step_host(host_in, out=host_out)
+            else:
+                sim.resume(host_in, k0)
+                sim.do_timestep()
+                sim.get_particles(out=host_out)
+
+        # untimed warm-up steps: the first launch of each kernel loads it
+        for _ in range(2):
+            one(sim.get_timestep())
         ts = sim.get_timestep()
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
         for k in range(e2e_steps):
-            if fused:
-                sim.step_host(host_in, out=host_out)
-            else:
-                sim.resume(host_in, ts + k)
-                sim.do_timestep()
-                sim.get_particles(out=host_out)
+            one(ts + k)
             host_in, host_out = host_out, host_in
         torch.cuda.synchronize()
         return aggregate(1e3 * (time.perf_counter() - t0), N, e2e_steps, world, dist)[0]
