@@ -450,38 +450,6 @@ __device__ __forceinline__ double tab_atan2(double y, double x) {
     return __longlong_as_double(__double_as_longlong(ang) ^ (__double_as_longlong(y) & (long long)0x8000000000000000ull));
 }
 
-// modulo(atan2(y, x), 2 pi) (particle.rs:106-121 with :26-35) through the
-// table: for y < 0 the angle is 2 pi - a_j - eps with 2 pi - a_j exact
-// (a_j a multiple of 2^-7 below pi), one rounding where the reference
-// rounds atan2 and then its sum with 2 pi, so no wrap is needed afterwards
-// (the result lies in [0, 2 pi], 2 pi only for y within an ulp below 0, as in
-// the reference).  y = -0.0 counts as y >= 0 (+0.0 where the reference
-// gives -0.0).  Inputs outside tab_atan2's range go through atan2 and
-// ref_modulo.
-__device__ __forceinline__ double tab_angle(double y, double x) {
-    const float af = atan2f(fabsf(d2f(y)), d2f(x));
-    const int j = __float2int_rn(af * 128.0f);
-    const double2 t = __ldg(&kTrig[j]);
-    const double ay = fabs(y);
-    const double d = fma(ay, t.y, x * t.x);
-    const double e = fma(-x, t.y, ay * t.x);
-    const long long db = __double_as_longlong(d);
-    const int ed = (int)(db >> 52), ee = (int)((__double_as_longlong(e) >> 52) & 0x7FF);
-    if (db < 0x3C30000000000000ll || db >= 0x43C0000000000000ll || ee > ed - 8)
-        return ref_modulo(atan2(y, x), kTwoPi);
-    const double r0 = f2d(__frcp_rn(d2f_pos(d)));
-    const double r = fma(r0, fma(-d, r0, 1.0), r0);
-    const double q = e * r;
-    const double eps = fma(r, fma(-d, q, e), q);
-    const double z = eps * eps;
-    const double at = fma(eps * z, fma(z, fma(z, -1.0 / 7.0, 1.0 / 5.0), -1.0 / 3.0), eps);
-    // y < 0: (2 pi - a_j) - eps, else a_j + eps; the choice and the sign on the integer pipe
-    const long long yb = __double_as_longlong(y), sign = (long long)0x8000000000000000ull;
-    const bool neg = yb < 0 && yb != sign;
-    const double base = neg ? __ldg(&kTwoPiMinus[j]) : trig_angle(j);
-    return base + __longlong_as_double(__double_as_longlong(at) ^ (neg ? sign : 0ll));
-}
-
 // ---- the Langevin chain ------------------------------------------------
 // Field access for the chain.  TableFields reads one row of the per-cell
 // table; MatrixFields carries full 3x3 matrices (used by ss_langevin).
@@ -716,12 +684,16 @@ constexpr int CTAB_STRIDE = 8;
 // (theta = pi/2 and z = 0, which every particle holds after a quasi2d step)
 // and no magnetic modifiers: n = (cos phi, sin phi, cos(pi/2)) with
 // cos(pi/2) (6.1e-17 in FP64) taken as 0 and sin(pi/2) == 1 exactly, so the
-// products with n_z and every z component drop out; the rotation axis then
-// enters only through k x n = (sa sin phi, -sa cos phi).  The step's factor
-// dt is applied to the fields once per cell (the canonical table) instead
-// of to every particle's sums: dp = n dt + u dt, dn = -(W dt) n + (f - n
-// (f . n)) with f = (shape dt E) n -- the same terms, each dropped or
-// regrouped product below half an ulp of the sum it joins, so the results
+// products with n_z and every z component drop out.  The step's factor dt is
+// applied to the fields once per cell (the canonical table) instead of to
+// every particle's sums.  In the plane every deterministic orientation
+// term is a multiple of n_perp = (-sin phi, cos phi): the external field
+// (0, r, 0) gives (r cos phi) n_perp, the vorticity W01 n_perp, the strain
+// (n_perp . f) n_perp, and the rotational diffusion turns n into
+// n cos rot - sa sin rot n_perp.  So v = n + dn = C n + G n_perp with
+// C = cos rot and G the sum of those coefficients, and the new angle
+// atan2(v) is phi + atan2(G, C), formed without v.  Each regrouped or
+// dropped product is below half an ulp of the sum it joins, so the results
 // can differ from the full chain's in the last bits, like the rounding of
 // sin / cos / atan2.  z and theta are not produced (the quasi2d step
 // overwrites them with 0 and pi/2, which the canonical state already holds).
@@ -748,48 +720,28 @@ __device__ __forceinline__ void langevin_canon(double &x, double &y, double &phi
         dp0 = 0.0;
         dp1 = 0.0;
     }
-    double dn0 = 0.0, dn1 = 0.0;
-    if (mask & M_EXTERNAL_FIELD) {  // b = (0, reorient dt, 0): b - n (n . b)
-        const double d = sp * reorient_dt;
-        dn0 = -(cp * d);
-        dn1 = reorient_dt - sp * d;
-    }
-    if (mask & M_JEFFREY_VORTICITY) {  // -(W n) dt, W n = (w01 n1, -w01 n0)
-        if (mask & M_EXTERNAL_FIELD) {
-            dn0 = fma(-c23.x, sp, dn0);
-            dn1 = fma(c23.x, cp, dn1);
-        } else {
-            dn0 = -(c23.x * sp);
-            dn1 = c23.x * cp;
-        }
-    }
-    if (mask & M_JEFFREY_STRAIN) {  // f = shape dt E n, f - n (f . n)
-        const double f0 = fma(c23.y, cp, c45.x * sp), f1 = fma(c45.x, cp, c45.y * sp);
-        const double fn = fma(f0, cp, f1 * sp);
-        dn0 = dn0 + fma(-cp, fn, f0);
-        dn1 = dn1 + fma(-sp, fn, f1);
-    }
     if (mask & M_TRANS_DIFFUSION) {
         dp0 = fma(xi[0], c67.x, dp0);
         dp1 = fma(xi[1], c67.x, dp1);
     }
-    // v = n + dn; the rotational diffusion (n (cos rot - 1) + (k x n) sin rot,
-    // k x n = sa (sin phi, -cos phi)) joins as n cos rot + sa sin rot (sin phi, -cos phi)
-    double v0, v1;
-    if (mask & M_ROT_DIFFUSION) {
-        double sr, cm1;
-        sin_cosm1(rot, sr, cm1);
-        const double q = sa * sr;
-        v0 = fma(cp, cm1, cp) + fma(sp, q, dn0);
-        v1 = fma(sp, cm1, sp) + fma(-cp, q, dn1);
-    } else {
-        v0 = cp + dn0;
-        v1 = sp + dn1;
+    // the coefficient of n_perp, term by term in the reference's order
+    double G = 0.0;
+    if (mask & M_EXTERNAL_FIELD) G = reorient_dt * cp;  // b - n (n . b), b = (0, r dt, 0)
+    if (mask & M_JEFFREY_VORTICITY) G = (mask & M_EXTERNAL_FIELD) ? G + c23.x : c23.x;  // -(W n) dt
+    if (mask & M_JEFFREY_STRAIN) {  // f - n (f . n), f = shape dt E n
+        const double f0 = fma(c23.y, cp, c45.x * sp), f1 = fma(c45.x, cp, c45.y * sp);
+        G = G + fma(cp, f1, -(sp * f0));
+    }
+    double C = 1.0;
+    if (mask & M_ROT_DIFFUSION) {  // n cos rot + (k x n) sin rot, k x n = -sa n_perp
+        double sr;
+        tab_sincos(rot, sr, C);
+        G = fma(-sa, sr, G);
     }
     const double px = x + dp0, py = y + dp1;
     x = ref_modulo(px, bx);
     y = ref_modulo(py, by);
-    phi = tab_angle(v1, v0);
+    phi = ref_modulo(phi + tab_atan2(G, C), kTwoPi);
 }
 
 }  // namespace ss

@@ -1,7 +1,6 @@
 """Writes trig_table.inc: cos, sin and cos - 1 of a_j = j / 128 for
 j = 0 .. TRIG_N - 1, each correctly rounded to double (mpmath at 80 digits),
-and 2 pi - a_j (exact for a_j <= pi, the range it is used on), as C
-hex-float literals.  The table feeds the table-based sin / cos / atan2
+as C hex-float literals.  The table feeds the table-based sin / cos / atan2
 of common.cuh.
 
     python stochasticsampling_gb300/csrc/gen_trig_table.py
@@ -37,13 +36,6 @@ def main(path=None):
     out += [f"    {r}," for r in rows]
     out += ["};", "static __device__ double kTrigCm1[kTrigN] = {"]
     out += [f"    {c}," for c in cm1]
-    out += ["};", "// 2 pi - j / 128 (exact: j / 128 is a multiple of 2^-7, the difference lies in [pi, 2 pi])",
-            "static __device__ double kTwoPiMinus[kTrigN] = {"]
-    two_pi = 2.0 * 3.141592653589793
-    for j in range(TRIG_N):
-        v = two_pi - j / 128.0
-        assert mpmath.mpf(v) == mpmath.mpf(two_pi) - mpmath.mpf(j) / 128 or v < 2.0  # exact where it is used
-        out.append(f"    {v.hex()},")
     out += ["};", ""]
     path = path or os.path.join(os.path.dirname(os.path.abspath(__file__)), "trig_table.inc")
     with open(path, "w") as f:
