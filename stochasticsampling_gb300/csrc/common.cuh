@@ -404,7 +404,7 @@ __device__ __forceinline__ void tab_sincos(double a, double &s, double &c) {
 }
 
 // sin r and cos r - 1, the latter without the cancellation of cos r - 1
-// (to 1.2e-17 absolute, see trig_small)
+// (from cos a_j - 1; within about an ulp of its own size)
 __device__ __forceinline__ void sin_cosm1(double r, double &s, double &cm1) {
     const int j = trig_round(r);
     if (j < 0) {
