@@ -350,7 +350,7 @@ __device__ __forceinline__ void philox_noise(unsigned long long seed, uint32_t i
 // kTrig[j] = (cos a_j, sin a_j) and kTrigCm1[j] = cos a_j - 1 at a_j = j / 128,
 // correctly rounded (gen_trig_table.py).  An angle a_j + b with |b| <= 2^-8
 // needs only short Taylor polynomials in b and the addition theorem: about
-// 12 FP64 operations for sin and cos and 15 for atan2, where the general
+// 12 FP64 operations for sin and cos and 16 for atan2, where the general
 // routines spend an argument reduction and long polynomials on the FP64
 // pipe (the bound of the update).  Results agree with the correctly rounded
 // values to about an ulp, like the library routines'.
