@@ -71,6 +71,7 @@ struct ss_ctx {
     uint32_t *cellcount = nullptr, *cursor = nullptr;
     double *kern = nullptr, *lut = nullptr;
     double *staging = nullptr, *noise_dev = nullptr, *dist_dev = nullptr, *realbuf = nullptr;
+    double *staging_sorted = nullptr;  // mixed: the rows in cell order before the ingest
     unsigned long long *d_step = nullptr;
     uint32_t *d_err = nullptr;
     unsigned long long *d_scan = nullptr;  // row validation: first non-finite particle, non-canonical flag
@@ -487,7 +488,7 @@ static void destroy_impl(ss_ctx *c) {
     }
     cudaFree(c->fwd); cudaFree(c->inv); cudaFree(c->table); cudaFree(c->ctab); cudaFree(c->cellcount); cudaFree(c->cursor);
     cudaFree(c->kern); cudaFree(c->lut); cudaFree(c->staging); cudaFree(c->noise_dev); cudaFree(c->dist_dev);
-    cudaFree(c->realbuf); cudaFree(c->d_step); cudaFree(c->d_err); cudaFree(c->d_scan); cudaFree(c->d_halfpi);
+    cudaFree(c->realbuf); cudaFree(c->staging_sorted); cudaFree(c->d_step); cudaFree(c->d_err); cudaFree(c->d_scan); cudaFree(c->d_halfpi);
     for (auto &kv : c->plans_c) cufftDestroy(kv.second);
     for (int b = 0; b < 2; ++b)
         for (int k = 0; k < 2; ++k) cudaFree(c->pa[b][k]);
@@ -787,12 +788,16 @@ static int ingest_staging(ss_ctx *c, uint64_t n, bool canon) {
     c->pcur = 0;
     c->ccur = 0;
     if (c->mixed) {
-        launch_ingest_m(c->stream, c->fixed, c->staging, n, c->P, c->M, c->px[0], c->pa[0], c->pid[0]);
+        // rows in cell order (locality of the update's gathers and atomics); pid gets their caller indices
+        if (!c->staging_sorted) CK(cudaMalloc((void **)&c->staging_sorted, 5 * (size_t)n * sizeof(double)));
+        launch_sort_rows_m(c->stream, c->staging, n, c->P, c->M, c->key[0], c->cellcount, c->cursor,
+                           c->staging_sorted, c->pid[0]);
+        launch_ingest_m(c->stream, c->fixed, c->staging_sorted, n, c->P, c->M, c->px[0], c->pa[0], nullptr);
         launch_zero_u32(c->stream, c->counts[0], c->P.nbins);
         launch_bin_m(c->stream, c->fixed, n, c->M, c->px[0], c->pa[0], c->key[0], c->counts[0]);
         // quasi2d: the canonical state (z = 0, theta = pi/2) lets the update skip z and theta
         c->canon = canon;
-        c->launches += 3;
+        c->launches += 7;
     } else {
         launch_zero_u32(c->stream, c->counts[0], c->P.nbins);
         launch_ingest_bin(c->stream, canon, c->staging, n, c->P, c->px[0], c->pid[0], c->key[0], c->counts[0],
