@@ -79,6 +79,42 @@ __global__ void k_ingest(const double *__restrict__ aos, unsigned long long n, D
     id[i] = (uint32_t)i;
 }
 
+// Rows reordered by spatial cell before the ingest (a counting sort), so
+// that the particles of a cell sit together in memory: the update's field
+// gathers and histogram atomics then hit the same rows one after another
+// (the 3-D histogram of 2^25 bins does not fit L2).  Particles move a
+// fraction of a cell per step, so the order keeps its locality; the noise
+// stays keyed by the caller's index (id).  The key is the cell of the
+// wrapped position from an FP32 estimate; the exact bins come later.
+__global__ void k_row_cells(const double *__restrict__ aos, unsigned long long n, DevParams P,
+                            uint32_t *__restrict__ cellkey, uint32_t *__restrict__ cellcount) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *p = aos + 5 * i;
+    const int nk[3] = {P.gx, P.gy, P.gz};
+    const double L[3] = {P.bx, P.by, P.bz};
+    int c[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int f = (int)floorf(d2f_pos(ref_modulo(p[k], L[k])) * P.igwf[k]);
+        c[k] = f < 0 ? 0 : (f >= nk[k] ? nk[k] - 1 : f);
+    }
+    const uint32_t cell = (uint32_t)((c[0] * P.gy + c[1]) * P.gz + c[2]);
+    cellkey[i] = cell;
+    atomicAdd(cellcount + cell, 1u);
+}
+__global__ void k_sort_rows(const double *__restrict__ aos, unsigned long long n, const uint32_t *__restrict__ cellkey,
+                            uint32_t *__restrict__ cursor, double *__restrict__ sorted, uint32_t *__restrict__ orig) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long pos = atomicAdd(cursor + cellkey[i], 1u);
+    const double *src = aos + 5 * i;
+    double *dst = sorted + 5 * pos;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) dst[k] = src[k];
+    orig[pos] = (uint32_t)i;
+}
+
 // SoA slot i -> AoS row id[i] (the caller's order)
 __global__ void k_egest(unsigned long long n, const double *__restrict__ x, const double *__restrict__ y,
                         const double *__restrict__ z, const double *__restrict__ phi,
@@ -141,7 +177,7 @@ __global__ void k_ingest_bin(const double *__restrict__ aos, unsigned long long 
     pz = ref_modulo(pz, P.bz);
     ref_ang_pbc(ph, th);
     x[i] = px; y[i] = py; z[i] = pz; phi[i] = ph; theta[i] = th;
-    id[i] = (uint32_t)i;
+    if (id) id[i] = (uint32_t)i;
     uint32_t err = 0, cell;
     unsigned long long bin;
     bin_particle<CANON>(P, px, py, pz, ph, th, cell, bin, err);
@@ -637,6 +673,15 @@ void launch_ingest(cudaStream_t s, const double *aos, unsigned long long n, cons
 void launch_egest(cudaStream_t s, unsigned long long n, double *const xs[5], const uint32_t *id, double *aos) {
     if (!n) return;
     k_egest<<<nblocks(n, 256), 256, 0, s>>>(n, xs[0], xs[1], xs[2], xs[3], xs[4], id, aos);
+}
+
+void launch_sort_rows(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P,
+                      uint32_t *cellkey, uint32_t *cellcount, uint32_t *cursor, double *sorted, uint32_t *orig) {
+    if (!n) return;
+    launch_zero_u32(s, cellcount, P.ncell);
+    k_row_cells<<<nblocks(n, 256), 256, 0, s>>>(aos, n, P, cellkey, cellcount);
+    launch_scan(s, cellcount, P.ncell, cursor);
+    k_sort_rows<<<nblocks(n, 256), 256, 0, s>>>(aos, n, cellkey, cursor, sorted, orig);
 }
 
 void launch_ingest_bin(cudaStream_t s, bool canon, const double *aos, unsigned long long n, const DevParams &P,

@@ -16,7 +16,12 @@ void launch_egest(cudaStream_t s, unsigned long long n, double *const xs[5], con
 void launch_ingest_bin_check(cudaStream_t s, const double *aos, unsigned long long n, unsigned long long off,
                              const DevParams &P, double *const xs[5], uint32_t *id, uint32_t *key,
                              uint32_t *counts, unsigned long long *scan, uint32_t *err);
-// k_ingest and k_bin in one pass (canon: every row in the canonical quasi-2-D state)
+// counting sort of host-layout rows by spatial cell: sorted[pos] = aos[i],
+// orig[pos] = i (cellkey, cellcount, cursor: scratch of n, ncell, ncell)
+void launch_sort_rows(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P,
+                      uint32_t *cellkey, uint32_t *cellcount, uint32_t *cursor, double *sorted, uint32_t *orig);
+// k_ingest and k_bin in one pass (canon: every row in the canonical quasi-2-D state);
+// id == nullptr leaves id as it is
 void launch_ingest_bin(cudaStream_t s, bool canon, const double *aos, unsigned long long n, const DevParams &P,
                        double *const xs[5], uint32_t *id, uint32_t *key, uint32_t *counts, uint32_t *err);
 void launch_bin(cudaStream_t s, unsigned long long n, const DevParams &P, double *const xs[5], uint32_t *key,

@@ -13,40 +13,8 @@
 // FP64 path); spectra float2; table rows of 16 (32 with dipolar terms) floats.
 #include "mixed.cuh"
 #include "mixed_device.cuh"
-#include "kernels.cuh"
 
 namespace ss {
-
-// Rows reordered by spatial cell before the ingest (a counting sort), so
-// that the particles of a cell sit together in memory: the update's field
-// gathers and histogram atomics then hit the same rows one after another
-// (the 3-D histogram of 2^25 bins does not fit L2).  Particles move a
-// fraction of a cell per step, so the order keeps its locality; the noise
-// stays keyed by the caller's index (id).
-__global__ void k_row_cells_m(const double *__restrict__ aos, unsigned long long n, DevParams P, MixedParams M,
-                              uint32_t *__restrict__ cellkey, uint32_t *__restrict__ cellcount) {
-    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double *p = aos + 5 * i;
-    const int ix = bin_f(d2f_pos(ref_modulo(p[0], P.bx)), M.igwf[0], M.gx);
-    const int iy = bin_f(d2f_pos(ref_modulo(p[1], P.by)), M.igwf[1], M.gy);
-    const int iz = bin_f(d2f_pos(ref_modulo(p[2], P.bz)), M.igwf[2], M.gz);
-    const uint32_t cell = (uint32_t)((ix * M.gy + iy) * M.gz + iz);
-    cellkey[i] = cell;
-    atomicAdd(cellcount + cell, 1u);
-}
-__global__ void k_sort_rows_m(const double *__restrict__ aos, unsigned long long n,
-                              const uint32_t *__restrict__ cellkey, uint32_t *__restrict__ cursor,
-                              double *__restrict__ sorted, uint32_t *__restrict__ orig) {
-    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const unsigned long long pos = atomicAdd(cursor + cellkey[i], 1u);
-    const double *src = aos + 5 * i;
-    double *dst = sorted + 5 * pos;
-#pragma unroll
-    for (int k = 0; k < 5; ++k) dst[k] = src[k];
-    orig[pos] = (uint32_t)i;
-}
 
 // Particle::new in FP64, then the angles rounded to FP32 (and the position
 // converted to fixed point when FIX); id (when given) gets the identity
@@ -395,15 +363,6 @@ __global__ void k_noise_m(MixedParams M, unsigned long long t, double *__restric
 // ========================================================================
 static inline unsigned nb(unsigned long long n, unsigned bs) { return (unsigned)((n + bs - 1) / bs); }
 
-void launch_sort_rows_m(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P,
-                        const MixedParams &M, uint32_t *cellkey, uint32_t *cellcount, uint32_t *cursor,
-                        double *sorted, uint32_t *orig) {
-    if (!n) return;
-    launch_zero_u32(s, cellcount, M.ncell);
-    k_row_cells_m<<<nb(n, 256), 256, 0, s>>>(aos, n, P, M, cellkey, cellcount);
-    launch_scan(s, cellcount, M.ncell, cursor);
-    k_sort_rows_m<<<nb(n, 256), 256, 0, s>>>(aos, n, cellkey, cursor, sorted, orig);
-}
 void launch_ingest_m(cudaStream_t s, bool fixed, const double *aos, unsigned long long n, const DevParams &P,
                      const MixedParams &M, double *const xs[3], float *const as[2], uint32_t *id) {
     (void)M;

@@ -28,11 +28,6 @@ struct MixedParams {
     uint32_t mask;
 };
 
-// counting sort of host-layout rows by spatial cell: sorted[pos] = aos[i],
-// orig[pos] = i (cellkey, cellcount, cursor: scratch of n, ncell, ncell)
-void launch_sort_rows_m(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P,
-                        const MixedParams &M, uint32_t *cellkey, uint32_t *cellcount, uint32_t *cursor,
-                        double *sorted, uint32_t *orig);
 // id == nullptr: leave id as it is (rows already sorted, id holds their caller indices)
 void launch_ingest_m(cudaStream_t s, bool fixed, const double *aos, unsigned long long n, const DevParams &P,
                      const MixedParams &M, double *const xs[3], float *const as[2], uint32_t *id);

@@ -71,7 +71,7 @@ struct ss_ctx {
     uint32_t *cellcount = nullptr, *cursor = nullptr;
     double *kern = nullptr, *lut = nullptr;
     double *staging = nullptr, *noise_dev = nullptr, *dist_dev = nullptr, *realbuf = nullptr;
-    double *staging_sorted = nullptr;  // mixed: the rows in cell order before the ingest
+    double *staging_sorted = nullptr;  // the rows in cell order before the ingest
     unsigned long long *d_step = nullptr;
     uint32_t *d_err = nullptr;
     unsigned long long *d_scan = nullptr;  // row validation: first non-finite particle, non-canonical flag
@@ -788,10 +788,11 @@ static int ingest_staging(ss_ctx *c, uint64_t n, bool canon) {
     c->pcur = 0;
     c->ccur = 0;
     if (c->mixed) {
-        // rows in cell order (locality of the update's gathers and atomics); pid gets their caller indices
+        // rows in cell order (locality of the update's gathers and atomics); pid gets their caller
+        // indices.  (The FP64 update is bound by the FP64 pipe, not by those accesses: no sort there.)
         if (!c->staging_sorted) CK(cudaMalloc((void **)&c->staging_sorted, 5 * (size_t)n * sizeof(double)));
-        launch_sort_rows_m(c->stream, c->staging, n, c->P, c->M, c->key[0], c->cellcount, c->cursor,
-                           c->staging_sorted, c->pid[0]);
+        launch_sort_rows(c->stream, c->staging, n, c->P, c->key[0], c->cellcount, c->cursor, c->staging_sorted,
+                         c->pid[0]);
         launch_ingest_m(c->stream, c->fixed, c->staging_sorted, n, c->P, c->M, c->px[0], c->pa[0], nullptr);
         launch_zero_u32(c->stream, c->counts[0], c->P.nbins);
         launch_bin_m(c->stream, c->fixed, n, c->M, c->px[0], c->pa[0], c->key[0], c->counts[0]);
