@@ -34,6 +34,7 @@
 #include <vector>
 
 #include "../../include/ssgpu.h"
+#include "kernels.cuh"
 #include "mixed_device.cuh"
 
 using namespace ss;
@@ -287,7 +288,8 @@ __global__ void __launch_bounds__(512, MINB) k_ens_update(const WorkUnit *__rest
                                                           double *__restrict__ x, double *__restrict__ y,
                                                           float *__restrict__ phi, const float *__restrict__ table,
                                                           const unsigned long long *__restrict__ d_step,
-                                                          uint32_t *__restrict__ counts_next) {
+                                                          uint32_t *__restrict__ counts_next,
+                                                          const uint32_t *__restrict__ pid) {
     __shared__ EnsMember E;
     const unsigned long long t = *d_step;
     for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
@@ -306,7 +308,7 @@ __global__ void __launch_bounds__(512, MINB) k_ens_update(const WorkUnit *__rest
             const int cx = bin_f(d2f_pos(px), M.igwf[0], M.gx), cy = bin_f(d2f_pos(py), M.igwf[1], M.gy);
             TableFieldsF F(table + (long long)(E.cell_off + cx * M.gy + cy) * kEnsRow);
             float xi[3], ca, sa, rot;
-            philox_noise_f<true>(M.seed, (uint32_t)(i - E.part_off), t, M.sigma_rot, xi, ca, sa, rot);
+            philox_noise_f<true>(M.seed, pid[i], t, M.sigma_rot, xi, ca, sa, rot);  // the caller's index in the member
             float st[3];
             langevin_mixed<true>(pph, pth, st, F, xi, ca, sa, rot, M);
             px = advance64(px, st[0], M.bx);
@@ -322,18 +324,20 @@ __global__ void __launch_bounds__(512, MINB) k_ens_update(const WorkUnit *__rest
 }
 
 using UpdateKernel = void (*)(const WorkUnit *, int, const EnsMember *, double *, double *, float *, const float *,
-                              const unsigned long long *, uint32_t *);
+                              const unsigned long long *, uint32_t *, const uint32_t *);
 constexpr int kUpdateVariants = 3;
 const UpdateKernel kUpdate[kUpdateVariants] = {k_ens_update<1>, k_ens_update<2>, k_ens_update<3>};
 
 __global__ void k_ens_step_inc(unsigned long long *d_step) { *d_step += 1ull; }
 
+// member rows back in the caller's order (pid: the caller's index in the member)
 __global__ void k_ens_egest(unsigned long long start, unsigned long long n, const double *__restrict__ x,
-                            const double *__restrict__ y, const float *__restrict__ phi, double *__restrict__ aos) {
+                            const double *__restrict__ y, const float *__restrict__ phi,
+                            const uint32_t *__restrict__ pid, double *__restrict__ aos) {
     unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
     if (k >= n) return;
     unsigned long long i = start + k;
-    double *p = aos + 5 * k;
+    double *p = aos + 5 * (unsigned long long)pid[i];
     p[0] = x[i]; p[1] = y[i]; p[2] = 0.0; p[3] = (double)phi[i]; p[4] = 1.5707963267948966;
 }
 
@@ -376,6 +380,10 @@ struct ss_ens {
     int nchunks = 0;
     size_t chunk_smem = 0;  // dynamic shared memory of k_ens_contract
     double *x = nullptr, *y = nullptr, *staging = nullptr, *realbuf = nullptr;
+    // a member's rows in cell order at init (locality of the update), with each
+    // particle's index in the member's caller order
+    double *staging_sorted = nullptr;
+    uint32_t *pid = nullptr, *cellkey = nullptr, *cellcount = nullptr, *cursor = nullptr;
     float *phi = nullptr;
     uint32_t *counts[2] = {};
     float2 *fwd = nullptr, *inv = nullptr;
@@ -461,7 +469,7 @@ int enqueue_solve(ss_ens *e, int ccur, uint64_t *nl) {
 void launch_update(ss_ens *e, int variant, int threads, int bps, double *x, double *y, float *phi,
                    uint32_t *counts_next) {
     kUpdate[variant]<<<(unsigned)(e->sms * bps), threads, 0, e->stream>>>(e->d_units, e->nunits, e->d_mem, x, y, phi,
-                                                                         e->table, e->d_step, counts_next);
+                                                                         e->table, e->d_step, counts_next, e->pid);
 }
 
 // one do_timestep of every member: solve from counts[ccur], move the
@@ -572,7 +580,8 @@ void destroy(ss_ens *e) {
     for (auto &g : e->graph)
         if (g) cudaGraphExecDestroy(g);
     cudaFree(e->d_mem); cudaFree(e->d_units); cudaFree(e->d_chunks); cudaFree(e->x); cudaFree(e->y);
-    cudaFree(e->staging); cudaFree(e->realbuf); cudaFree(e->phi); cudaFree(e->diff); cudaFree(e->means);
+    cudaFree(e->staging); cudaFree(e->staging_sorted); cudaFree(e->pid); cudaFree(e->cellkey);
+    cudaFree(e->cellcount); cudaFree(e->cursor); cudaFree(e->realbuf); cudaFree(e->phi); cudaFree(e->diff); cudaFree(e->means);
     cudaFree(e->counts[0]);
     cudaFree(e->counts[1]); cudaFree(e->fwd); cudaFree(e->inv); cudaFree(e->table); cudaFree(e->kern); cudaFree(e->lut);
     cudaFree(e->sums); cudaFree(e->d_step);
@@ -759,6 +768,11 @@ int ss_ensemble_create(const ss_grid *grids, const ss_box *boxes, const ss_param
     A((void **)&e->d_step, sizeof(unsigned long long));
     A((void **)&e->realbuf, 3ull * max_cell * sizeof(double));
     A((void **)&e->staging, 5ull * max_n * sizeof(double));
+    A((void **)&e->staging_sorted, 5ull * max_n * sizeof(double));
+    A((void **)&e->pid, N * sizeof(uint32_t));
+    A((void **)&e->cellkey, max_n * sizeof(uint32_t));
+    A((void **)&e->cellcount, (size_t)max_cell * sizeof(uint32_t));
+    A((void **)&e->cursor, (size_t)max_cell * sizeof(uint32_t));
     // every copy on the ensemble's stream (a non-blocking stream does not
     // order itself after the legacy stream of a plain cudaMemcpy)
     const cudaStream_t st = e->stream;
@@ -827,15 +841,22 @@ int ss_ensemble_init(ss_ens *e, const double *particles, uint64_t total) {
         const EnsMember &E = e->mem[m];
         ECK(cudaMemcpyAsync(e->staging, particles + 5 * E.part_off, 5 * E.M.n * sizeof(double),
                             cudaMemcpyHostToDevice, e->stream));
-        k_ens_ingest<<<nb((long long)E.M.n, 256), 256, 0, e->stream>>>(e->staging, E.part_off, E.M.n, E.M.bx, E.M.by,
-                                                                        e->x, e->y, e->phi);
+        // the member's rows in cell order, their caller indices into pid
+        DevParams P{};
+        P.gx = E.M.gx; P.gy = E.M.gy; P.gz = 1; P.ncell = E.M.gx * E.M.gy;
+        P.bx = E.M.bx; P.by = E.M.by; P.bz = 1.0;
+        P.igwf[0] = E.M.igwf[0]; P.igwf[1] = E.M.igwf[1]; P.igwf[2] = 1.0f;
+        launch_sort_rows(e->stream, e->staging, E.M.n, P, e->cellkey, e->cellcount, e->cursor, e->staging_sorted,
+                         e->pid + E.part_off);
+        k_ens_ingest<<<nb((long long)E.M.n, 256), 256, 0, e->stream>>>(e->staging_sorted, E.part_off, E.M.n, E.M.bx,
+                                                                        E.M.by, e->x, e->y, e->phi);
         ECK(cudaGetLastError());
     }
     ECK(cudaMemsetAsync(e->counts[0], 0, (size_t)e->total_bins * sizeof(uint32_t), e->stream));
     k_ens_bin<<<(unsigned)(e->sms * 4), 256, 0, e->stream>>>(e->d_units, e->nunits, e->d_mem, e->x, e->y, e->phi,
                                                               e->counts[0]);
     ECK(cudaGetLastError());
-    e->launches += e->nm + 1;
+    e->launches += 5 * e->nm + 1;
     ECK(cudaMemsetAsync(e->d_step, 0, sizeof(unsigned long long), e->stream));
     ECK(cudaStreamSynchronize(e->stream));
     e->ccur = 0;
@@ -922,7 +943,8 @@ int ss_ensemble_get_particles(ss_ens *e, uint32_t member, double *out) {
     if (!e || !out || member >= e->nm) return efail(e, SS_ERR_INVALID_ARGUMENT, "bad member or null argument");
     ECK(cudaSetDevice(e->device));
     const EnsMember &E = e->mem[member];
-    k_ens_egest<<<nb((long long)E.M.n, 256), 256, 0, e->stream>>>(E.part_off, E.M.n, e->x, e->y, e->phi, e->staging);
+    k_ens_egest<<<nb((long long)E.M.n, 256), 256, 0, e->stream>>>(E.part_off, E.M.n, e->x, e->y, e->phi, e->pid,
+                                                                    e->staging);
     ECK(cudaGetLastError());
     ECK(cudaMemcpyAsync(out, e->staging, 5 * E.M.n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
     ECK(cudaStreamSynchronize(e->stream));
