@@ -355,7 +355,9 @@ def measure_c2(args, stream, rank, world, dist, barrier):
                        "orientations on the sphere, dipolar coupling 0.5, external field 1, active stress -1, "
                        "Dt 0.1, Dr 1.0, dt 0.002", "particles": n, "steps": steps}
     for name, mode in (("fp64", False), ("mixed", True)):
-        sim = ss.Simulation(grid=C2_GRID, box=C2_BOX, params=params, mixed=mode, stream=stream.cuda_stream)
+        # rows counting-sorted by cell at init keep their locality over these steps: no per-step sort
+        sim = ss.Simulation(grid=C2_GRID, box=C2_BOX, params=params, mixed=mode, sort=False,
+                            stream=stream.cuda_stream)
         sim.init(p0)
         with torch.cuda.stream(stream):
             sim.run(args.warmup)

@@ -787,22 +787,29 @@ static int load_particles(ss_ctx *c, const double *particles, uint64_t n) {
 static int ingest_staging(ss_ctx *c, uint64_t n, bool canon) {
     c->pcur = 0;
     c->ccur = 0;
-    if (c->mixed) {
-        // rows in cell order (locality of the update's gathers and atomics); pid gets their caller
-        // indices.  (The FP64 update is bound by the FP64 pipe, not by those accesses: no sort there.)
+    // Rows in cell order (locality of the update's gathers and atomics); pid gets their caller
+    // indices.  Every mixed context sorts; an FP64 context sorts only on a 3-D grid, whose
+    // histogram outgrows L2 (the 2-D FP64 update is bound by the FP64 pipe, not by those
+    // accesses, and the sort would only slow ss_resume).
+    const bool sort_rows = c->mixed || c->P.gz > 1;
+    if (sort_rows) {
         if (!c->staging_sorted) CK(cudaMalloc((void **)&c->staging_sorted, 5 * (size_t)n * sizeof(double)));
         launch_sort_rows(c->stream, c->staging, n, c->P, c->key[0], c->cellcount, c->cursor, c->staging_sorted,
                          c->pid[0]);
-        launch_ingest_m(c->stream, c->fixed, c->staging_sorted, n, c->P, c->M, c->px[0], c->pa[0], nullptr);
+        c->launches += 4;
+    }
+    const double *rows = sort_rows ? c->staging_sorted : c->staging;
+    if (c->mixed) {
+        launch_ingest_m(c->stream, c->fixed, rows, n, c->P, c->M, c->px[0], c->pa[0], nullptr);
         launch_zero_u32(c->stream, c->counts[0], c->P.nbins);
         launch_bin_m(c->stream, c->fixed, n, c->M, c->px[0], c->pa[0], c->key[0], c->counts[0]);
         // quasi2d: the canonical state (z = 0, theta = pi/2) lets the update skip z and theta
         c->canon = canon;
-        c->launches += 7;
+        c->launches += 3;
     } else {
         launch_zero_u32(c->stream, c->counts[0], c->P.nbins);
-        launch_ingest_bin(c->stream, canon, c->staging, n, c->P, c->px[0], c->pid[0], c->key[0], c->counts[0],
-                          c->d_err);
+        launch_ingest_bin(c->stream, canon, rows, n, c->P, c->px[0], sort_rows ? nullptr : c->pid[0], c->key[0],
+                          c->counts[0], c->d_err);
         c->canon = canon;
         c->launches += 2;
     }
