@@ -352,8 +352,9 @@ __device__ __forceinline__ void philox_noise(unsigned long long seed, uint32_t i
 // needs only short Taylor polynomials in b and the addition theorem: about
 // 12 FP64 operations for sin and cos and 16 for atan2, where the general
 // routines spend an argument reduction and long polynomials on the FP64
-// pipe (the bound of the update).  Results agree with the correctly rounded
-// values to about an ulp, like the library routines'.
+// pipe (the bound of the update).  sin and cos are within 1.7e-16 of the
+// correctly rounded values (an ulp of 1; relative to a value near a zero
+// of sin or cos that is more than an ulp), atan2 within 2 ulp.
 #include "trig_table.inc"
 
 // j = round(128 a) for +0 <= a < 6.3, from a's bits on the integer pipe;
