@@ -1035,11 +1035,11 @@ static int load_host_fp64(ss_ctx *c, const double *in, uint64_t n) {
     CKR(ensure_host_pipeline(c));
     const int alt = 1 - c->pcur;
     const size_t N = (size_t)n;
-    if (!c->px[alt][0]) {
-        for (int k = 0; k < 5; ++k) CK(cudaMalloc((void **)&c->px[alt][k], N * sizeof(double)));
-        CK(cudaMalloc((void **)&c->key[alt], N * sizeof(uint32_t)));
-        CK(cudaMalloc((void **)&c->pid[alt], N * sizeof(uint32_t)));
-    }
+    // each missing buffer on its own, so that a failed call leaves nothing half-made for the next
+    for (int k = 0; k < 5; ++k)
+        if (!c->px[alt][k]) CK(cudaMalloc((void **)&c->px[alt][k], N * sizeof(double)));
+    if (!c->key[alt]) CK(cudaMalloc((void **)&c->key[alt], N * sizeof(uint32_t)));
+    if (!c->pid[alt]) CK(cudaMalloc((void **)&c->pid[alt], N * sizeof(uint32_t)));
     if (!c->counts_in) CK(cudaMalloc((void **)&c->counts_in, (size_t)c->P.nbins * sizeof(uint32_t)));
     static const unsigned long long scan_init[2] = {~0ull, 0ull};
     unsigned long long scan[2];
