@@ -1087,11 +1087,14 @@ int ss_step_host(ss_ctx *c, const double *in, double *out, uint64_t n, uint64_t 
     if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
     if (!out) return fail(c, SS_ERR_INVALID_ARGUMENT, "out is NULL");
     CK(cudaSetDevice(c->device));
-    if (c->mixed) CKR(load_particles(c, in, n));
-    else CKR(load_host_fp64(c, in, n));
+    // the pipelined form for the FP64 path; the mixed path, and a context recording per-stage
+    // times (whose stage events the chunked step does not set), run the three calls in sequence
+    const bool fused = !c->mixed && !c->timing.on;
+    if (fused) CKR(load_host_fp64(c, in, n));
+    else CKR(load_particles(c, in, n));
     c->h_step = c->timestep;
     CK(cudaMemcpyAsync(c->d_step, &c->h_step, sizeof c->h_step, cudaMemcpyHostToDevice, c->stream));
-    if (c->mixed) {
+    if (!fused) {
         CKR(direct_step(c, false));
         CKR(ss_get_particles(c, out, n));
     } else {
