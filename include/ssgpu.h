@@ -128,7 +128,8 @@ int ss_noise(ss_ctx *ctx, uint64_t timestep, double *out);
  * to `out` ([n][5]) -- ss_resume + ss_do_timestep + ss_get_particles in one
  * call, with the read-back of each chunk of updated particles overlapping
  * the update of the next (a second stream).  The particles stay in the
- * caller's order (no sort this step).  `in` and `out` may be the same
+ * caller's order (no sort this step).  Mixed-precision contexts, and
+ * contexts recording per-stage times, run it as those three calls.  `in` and `out` may be the same
  * buffer; pinned host memory gives the full copy bandwidth.  The drop-in
  * form of Simulation::do_timestep (src/bin/simulation/mod.rs:251-374) for a
  * caller that keeps the particles in host memory. */
