@@ -104,3 +104,25 @@ def test_step_host_rejects_bad_rows_and_keeps_state():
     with pytest.raises(ValueError):
         g.get_particles(out=np.empty((n, 4)))
     g.close()
+
+
+def test_step_host_with_stage_timing():
+    """With per-stage timing on, ss_step_host runs as resume + step + read-back."""
+    ss = _gpu()
+    n = 50_000
+    rng = np.random.default_rng(8)
+    p = _rows(rng, n)
+    mk = lambda: ss.Simulation(grid=GRID, box=BOX, params=dict(PARAMS, number_of_particles=n, seed=14),
+                               quasi2d=True, sort=False)
+    a, b = mk(), mk()
+    a.init(p)
+    b.init(p)
+    b.profile(True)
+    a.resume(p, 0)
+    a.do_timestep()
+    assert np.array_equal(b.step_host(p), a.get_particles())
+    ms, steps = b.profile_read()
+    assert steps == 1 and ms["update"] > 0
+    b.profile(False)
+    a.close()
+    b.close()
