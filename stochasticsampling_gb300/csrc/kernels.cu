@@ -60,23 +60,20 @@ __global__ void k_scan_rows(const double *__restrict__ aos, unsigned long long n
     if (__any_sync(0xffffffffu, noncanon) && (threadIdx.x & 31) == 0) atomicOr(&scan[1], 1ull);
 }
 
-// Particle::new (src/particle.rs:186-201): modulo on positions and ang_pbc on
-// angles, then pbc once more; AoS [n][5] -> SoA.
-__global__ void k_ingest(const double *__restrict__ aos, unsigned long long n, DevParams P, double *__restrict__ x,
-                         double *__restrict__ y, double *__restrict__ z, double *__restrict__ phi,
-                         double *__restrict__ theta, uint32_t *__restrict__ id) {
-    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double *p = aos + 5 * i;
-    double px = ref_modulo(p[0], P.bx), py = ref_modulo(p[1], P.by), pz = ref_modulo(p[2], P.bz);
-    double ph = p[3], th = p[4];
+// Particle::new (src/particle.rs:186-201) on one caller row: modulo on the
+// positions and ang_pbc on the angles, then both once more.
+__device__ __forceinline__ void ingest_row(const double *__restrict__ p, const DevParams &P, double &px, double &py,
+                                           double &pz, double &ph, double &th) {
+    px = ref_modulo(p[0], P.bx);
+    py = ref_modulo(p[1], P.by);
+    pz = ref_modulo(p[2], P.bz);
+    ph = p[3];
+    th = p[4];
     ref_ang_pbc(ph, th);
     px = ref_modulo(px, P.bx);
     py = ref_modulo(py, P.by);
     pz = ref_modulo(pz, P.bz);
     ref_ang_pbc(ph, th);
-    x[i] = px; y[i] = py; z[i] = pz; phi[i] = ph; theta[i] = th;
-    id[i] = (uint32_t)i;
 }
 
 // Rows reordered by spatial cell before the ingest (a counting sort), so
@@ -141,25 +138,11 @@ __device__ __forceinline__ void bin_particle(const DevParams &P, double x, doubl
     bin = (unsigned long long)cell * (unsigned long long)P.nang + (unsigned long long)(ip * P.gtheta + it);
 }
 
-// Distribution::histogram_from (src/distribution/mod.rs:146-160) with
-// integer counts; also records each particle's spatial cell.
-__global__ void k_bin(unsigned long long n, DevParams P, const double *__restrict__ x,
-                      const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ phi,
-                      const double *__restrict__ theta, uint32_t *__restrict__ key, uint32_t *__restrict__ counts,
-                      uint32_t *__restrict__ errflag) {
-    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint32_t err = 0, cell;
-    unsigned long long bin;
-    bin_particle(P, x[i], y[i], z[i], phi[i], theta[i], cell, bin, err);
-    atomicAdd(counts + bin, 1u);
-    key[i] = cell;
-    if (err) atomicOr(errflag, err);
-}
-
-// Particle::new of k_ingest fused with the first histogram of k_bin
-// (Simulation::init, src/bin/simulation/mod.rs:163-196): one pass over the
-// rows.  CANON: every row in the canonical quasi-2-D state.
+// Particle::new (ingest_row, AoS [n][5] -> SoA) fused with the first
+// histogram, Distribution::histogram_from (src/distribution/mod.rs:146-160)
+// with integer counts, and each particle's spatial cell (Simulation::init,
+// src/bin/simulation/mod.rs:163-196): one pass over the rows.  CANON: every
+// row in the canonical quasi-2-D state.
 template <bool CANON>
 __global__ void k_ingest_bin(const double *__restrict__ aos, unsigned long long n, DevParams P,
                              double *__restrict__ x, double *__restrict__ y, double *__restrict__ z,
@@ -168,14 +151,8 @@ __global__ void k_ingest_bin(const double *__restrict__ aos, unsigned long long 
                              uint32_t *__restrict__ errflag) {
     unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double *p = aos + 5 * i;
-    double px = ref_modulo(p[0], P.bx), py = ref_modulo(p[1], P.by), pz = ref_modulo(p[2], P.bz);
-    double ph = p[3], th = p[4];
-    ref_ang_pbc(ph, th);
-    px = ref_modulo(px, P.bx);
-    py = ref_modulo(py, P.by);
-    pz = ref_modulo(pz, P.bz);
-    ref_ang_pbc(ph, th);
+    double px, py, pz, ph, th;
+    ingest_row(aos + 5 * i, P, px, py, pz, ph, th);
     x[i] = px; y[i] = py; z[i] = pz; phi[i] = ph; theta[i] = th;
     if (id) id[i] = (uint32_t)i;
     uint32_t err = 0, cell;
@@ -208,13 +185,8 @@ __global__ void k_ingest_bin_check(const double *__restrict__ aos, unsigned long
         for (int k = 0; k < 5; ++k) bad |= ((b[k] >> 52) & 0x7FFull) == 0x7FFull;
         noncanon = b[2] != 0ull || b[4] != (unsigned long long)__double_as_longlong(kPiHalf);
         if (bad) atomicMin(&scan[0], off + i);
-        double px = ref_modulo(p[0], P.bx), py = ref_modulo(p[1], P.by), pz = ref_modulo(p[2], P.bz);
-        double ph = p[3], th = p[4];
-        ref_ang_pbc(ph, th);
-        px = ref_modulo(px, P.bx);
-        py = ref_modulo(py, P.by);
-        pz = ref_modulo(pz, P.bz);
-        ref_ang_pbc(ph, th);
+        double px, py, pz, ph, th;
+        ingest_row(p, P, px, py, pz, ph, th);
         x[i] = px; y[i] = py; z[i] = pz; phi[i] = ph; theta[i] = th;
         id[i] = (uint32_t)(off + i);
         uint32_t err = 0, cell;
@@ -664,12 +636,6 @@ void launch_scan_rows(cudaStream_t s, const double *aos, unsigned long long n, u
     if (n) k_scan_rows<<<nblocks(n, 256), 256, 0, s>>>(aos, n, scan);
 }
 
-void launch_ingest(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P, double *const xs[5],
-                   uint32_t *id) {
-    if (!n) return;
-    k_ingest<<<nblocks(n, 256), 256, 0, s>>>(aos, n, P, xs[0], xs[1], xs[2], xs[3], xs[4], id);
-}
-
 void launch_egest(cudaStream_t s, unsigned long long n, double *const xs[5], const uint32_t *id, double *aos) {
     if (!n) return;
     k_egest<<<nblocks(n, 256), 256, 0, s>>>(n, xs[0], xs[1], xs[2], xs[3], xs[4], id, aos);
@@ -701,12 +667,6 @@ void launch_ingest_bin_check(cudaStream_t s, const double *aos, unsigned long lo
     if (!n) return;
     k_ingest_bin_check<<<nblocks(n, 256), 256, 0, s>>>(aos, n, off, P, xs[0], xs[1], xs[2], xs[3], xs[4], id, key,
                                                        counts, scan, err);
-}
-
-void launch_bin(cudaStream_t s, unsigned long long n, const DevParams &P, double *const xs[5], uint32_t *key,
-                uint32_t *counts, uint32_t *err) {
-    if (!n) return;
-    k_bin<<<nblocks(n, 256), 256, 0, s>>>(n, P, xs[0], xs[1], xs[2], xs[3], xs[4], key, counts, err);
 }
 
 void launch_counts_to_dist(cudaStream_t s, const uint32_t *counts, const DevParams &P, double *dist) {

@@ -8,8 +8,6 @@
 namespace ss {
 
 void launch_scan_rows(cudaStream_t s, const double *aos, unsigned long long n, unsigned long long *scan);
-void launch_ingest(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P, double *const xs[5],
-                   uint32_t *id);
 void launch_egest(cudaStream_t s, unsigned long long n, double *const xs[5], const uint32_t *id, double *aos);
 // k_ingest_bin plus the row checks of k_scan_rows on rows off .. off + n
 // (aos, xs, id, key point at row off)
@@ -20,12 +18,10 @@ void launch_ingest_bin_check(cudaStream_t s, const double *aos, unsigned long lo
 // orig[pos] = i (cellkey, cellcount, cursor: scratch of n, ncell, ncell)
 void launch_sort_rows(cudaStream_t s, const double *aos, unsigned long long n, const DevParams &P,
                       uint32_t *cellkey, uint32_t *cellcount, uint32_t *cursor, double *sorted, uint32_t *orig);
-// k_ingest and k_bin in one pass (canon: every row in the canonical quasi-2-D state);
+// Particle::new and the first histogram in one pass (canon: every row in the canonical quasi-2-D state);
 // id == nullptr leaves id as it is
 void launch_ingest_bin(cudaStream_t s, bool canon, const double *aos, unsigned long long n, const DevParams &P,
                        double *const xs[5], uint32_t *id, uint32_t *key, uint32_t *counts, uint32_t *err);
-void launch_bin(cudaStream_t s, unsigned long long n, const DevParams &P, double *const xs[5], uint32_t *key,
-                uint32_t *counts, uint32_t *err);
 void launch_counts_to_dist(cudaStream_t s, const uint32_t *counts, const DevParams &P, double *dist);
 void launch_contract(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const double *dist,
                      const double *lut, int lut_n, const double *kern, const DevParams &P, double2 *fwd,
