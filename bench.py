@@ -1,8 +1,9 @@
 """Benchmark of the GB300 timestep: particle-steps/s on the 2-D production
 workload (N = 1e7 particles, grid 128x128x1x32x1, box 40x40, Dt 0.1, Dr 1.0,
 active stress -2, dt 0.005, 1 % sinusoidal density perturbation along x),
-plain FP64 path (the headline `value`), with sections for the FP32 mixed
-path (FP64 and fixed-point positions), the batched ensemble of 64 parameter
+plain FP64 path (the headline `value`), with sections for the same FP64
+mode with the update's increments in two-float arithmetic (f32x2), the FP32
+mixed path (FP64 and fixed-point positions), the batched ensemble of 64 parameter
 sets, the learned denoiser in the loop and the 3-D magnetic workload (2e7
 particles, grid 64^3 x 16 x 8; FP64 and FP32 mixed).
 
@@ -251,6 +252,84 @@ def measure_sorted(args, stream, p0, params, world, dist, barrier):
     sim.close()
     value, ms_max = aggregate(ms, N, args.steps, world, dist)
     return {"value": value, "unit": UNIT, "ms_per_step": ms_max / args.steps}
+
+
+def measure_f32x2(args, stream, p0, params, world, dist, barrier):
+    """The same workload in the FP64 mode with SS_FLAG_F32X2 (the canonical
+    update's increments in two-float arithmetic, the state in FP64):
+    throughput over K graph-replayed steps, the update kernel's time from
+    per-stage events and its HBM roofline, end to end through ss_step_host,
+    and the largest deviation of x, y, phi from the FP64 mode after one step
+    from identical state and noise."""
+    import torch
+
+    import stochasticsampling_gb300 as ss
+    sim = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True, sort=False, f32x2=True,
+                        stream=stream.cuda_stream)
+    sim.init(p0)
+    with torch.cuda.stream(stream):
+        sim.run(args.warmup)
+        torch.cuda.synchronize()
+        barrier()
+        l0 = sim.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.run(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        launches = sim.launch_count() - l0
+    value, ms_max = aggregate(ms, N, args.steps, world, dist)
+    sim.profile(True)
+    sim.run(args.steps)
+    stage_ms, nprof = sim.profile_read()
+    sim.profile(False)
+    stage_avg = {k: v / max(1, nprof) for k, v in stage_ms.items()}
+    # end to end: ss_step_host with pinned host rows, as the FP64 headline
+    host_in = torch.empty((N, 5), dtype=torch.float64, pin_memory=True).numpy()
+    host_out = torch.empty((N, 5), dtype=torch.float64, pin_memory=True).numpy()
+    host_in[:] = sim.get_particles()
+    for _ in range(2):
+        sim.step_host(host_in, out=host_out)
+    e2e_steps = max(1, min(args.steps, 10))
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.step_host(host_in, out=host_out)
+        host_in, host_out = host_out, host_in
+    torch.cuda.synchronize()
+    e2e = aggregate(1e3 * (time.perf_counter() - t0), N, e2e_steps, world, dist)[0]
+    # one step from identical state and noise in both modes
+    state = sim.get_particles()
+    ts = sim.get_timestep()
+    ref = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True, sort=False, stream=stream.cuda_stream)
+    dev = []
+    for g in (sim, ref):
+        g.resume(state, ts)
+        g.do_timestep()
+        dev.append(g.get_particles())
+    ref.close()
+    sim.close()
+    d = np.abs(dev[0] - dev[1])
+    d = np.minimum(d, np.array([BOX[0], BOX[1], BOX[2], 2 * np.pi, np.pi]) - d)
+    gx, gy, gz, gp, gt = GRID
+    ncell, nbins = gx * gy * gz, gx * gy * gz * gp * gt
+    upd_bytes = N * (24 + 24 + 4 + 4 + 4) + ncell * 16 * 8 + nbins * 4
+    upd_ms = stage_avg["update"]
+    peak, peak_kind = peaks()
+    achieved = upd_bytes / (upd_ms / 1e3) / 1e9
+    return {"value": value, "unit": UNIT, "ms_per_step": ms_max / args.steps, "gpu_launches": launches,
+            "dtype": "f64 state and sums, f32x2 increments",
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "kernel": "k_update (two-float canonical chain)",
+                         "peak_source": peak_kind, "bytes_per_launch": upd_bytes, "avg_launch_ms": upd_ms},
+            "stage_ms": stage_avg,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": N * 5 * 8, "d2h_bytes_per_step": N * 5 * 8,
+                    "steps": e2e_steps, "api": "ss_step_host, pinned"},
+            "max_abs_dev_vs_fp64_one_step": {"x": float(d[:, 0].max()), "y": float(d[:, 1].max()),
+                                             "phi": float(d[:, 3].max())}}
 
 
 def measure_mixed(args, stream, p0, rank, world, dist, barrier, mode=True):
@@ -534,6 +613,8 @@ def run_gpu(args, rank, world, dist):
             res = measure_c2(args, stream, rank, world, dist, barrier)
         elif args.only == "denoised":
             res = measure_denoised(args, rank)
+        elif args.only == "f32x2":
+            res = measure_f32x2(args, stream, p0, params, world, dist, barrier)
         else:
             res = measure_mixed(args, stream, p0, rank, world, dist, barrier,
                                 "fixed64" if args.only == "fixed64" else True)
@@ -612,6 +693,7 @@ def run_gpu(args, rank, world, dist):
     e2e_sep = e2e_loop(False)
     e2e_value = e2e_loop(True)
     sim.close()
+    f32x2 = measure_f32x2(args, stream, p0, params, world, dist, barrier)
     mixed = None if args.no_mixed else measure_mixed(args, stream, p0, rank, world, dist, barrier)
     mixed_fixed = None if args.no_mixed else measure_mixed(args, stream, p0, rank, world, dist, barrier, "fixed64")
     ensemble = None if args.no_ensemble else measure_ensemble(args, stream, rank, world, dist, barrier)
@@ -673,6 +755,7 @@ def run_gpu(args, rank, world, dist):
                           "achieved_gbs": step_bytes / (ms_max / args.steps / 1e3) / 1e9},
         "stage_ms": stage_avg,
         "sorted": sorted_line,
+        "f32x2": f32x2,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N * 5 * 8, "d2h_bytes_per_step": N * 5 * 8,
                 "steps": e2e_steps, "api": "ss_step_host(host rows in, host rows out), pinned",
                 "separate_calls": {"value": e2e_sep, "api": "ss_resume(host) + ss_do_timestep + ss_get_particles(host)"}},
@@ -702,7 +785,7 @@ def main():
     ap.add_argument("--denoise-pairs", type=int, default=1000)
     ap.add_argument("--denoise-epochs", type=int, default=1)
     ap.add_argument("--denoise-steps", type=int, default=400)
-    ap.add_argument("--only", choices=["mixed", "fixed64", "ensemble", "denoised", "c2"], default=None,
+    ap.add_argument("--only", choices=["mixed", "fixed64", "ensemble", "denoised", "c2", "f32x2"], default=None,
                     help="run one section alone (a smaller command for profiling); prints its JSON")
     ap.add_argument("--ensemble-members", type=int, default=64)
     ap.add_argument("--ensemble-config", default=None,

@@ -39,6 +39,7 @@ FLAG_MIXED = 16
 FLAG_TRILINEAR = 32
 FLAG_TRILINEAR_ZFROMY = 64
 FLAG_FIXED64 = 128
+FLAG_F32X2 = 256
 
 NUM_STAGES = 8
 STAGES = ["contract", "fft_forward", "kspace", "fft_inverse", "table", "update", "sort", "other"]

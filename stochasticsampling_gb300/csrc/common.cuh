@@ -75,6 +75,8 @@ struct DevParams {
     double sigma_rot;  // sqrt(2 Dr dt)  (simulation/mod.rs:267-270)
     double cos_half_pi, sin_half_pi;  // cos/sin of kPiHalf as evaluated on this device
     double shape_dt, reorient_dt;     // shape * dt, magnetic_reorientation * dt (canonical table)
+    float dt2[2], reorient2[2], sigma2[2];  // dt, reorient_dt, sigma_rot as float pairs (hi, lo)
+    int f32x2;         // the canonical quasi-2-D chain in two-float arithmetic (f32x2.cuh)
     float igwf[5];     // 1 / gw in FP32 (first estimate of the bin index)
     float bintol[5];   // half-width of the band around an integer where the FP32 estimate defers to FP64
     unsigned long long seed;
@@ -314,32 +316,48 @@ __device__ __forceinline__ float neg2log1m(double x) {
 // sincos(atan2(sa, ca)) reproduces (ca, sa) to FP64 rounding.  The
 // canonical quasi-2-D chain reads only the sine, which then costs no FP64
 // operation.
+// The FP32 draws of the first two Philox blocks: the normals xi0, xi1, the
+// sine and cosine of the axis angle and the Rayleigh radius of the rotation
+// angle before sigma (philox_noise turns them into exact doubles; the
+// two-float update uses them as they are).
+struct NoiseF {
+    float xi0, xi1, sa, ca, rad;
+};
+__device__ __forceinline__ NoiseF philox_noise_f(unsigned long long seed, uint32_t id, unsigned long long t) {
+    const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+    const uint32_t tl = (uint32_t)t, th = (uint32_t)(t >> 32);
+    const uint4 r0 = philox4x32_10(make_uint4(id, tl, th, 0u), key);
+    const uint4 r1 = philox4x32_10(make_uint4(id, tl, th, 1u), key);
+    NoiseF f;
+    const float rad = sqrtf(neg2log1m(u12(r0.x, r0.y)));
+    float s, c;
+    sincospif(2.0f * (float)(r0.z >> 8) * 0x1p-24f, &s, &c);
+    f.xi0 = rad * c;
+    f.xi1 = rad * s;
+    sincospif(2.0f * (float)(r1.x >> 8) * 0x1p-24f, &f.sa, &f.ca);
+    f.rad = sqrtf(neg2log1m(u12(r1.z, r1.w)));
+    return f;
+}
+
 template <bool Q2D, bool WANT_ALPHA = false>
 __device__ __forceinline__ void philox_noise(unsigned long long seed, uint32_t id, unsigned long long t,
                                              double sigma, double xi[3], double &ca, double &sa,
                                              double &rot, double *alpha = nullptr) {
-    uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
-    uint32_t tl = (uint32_t)t, th = (uint32_t)(t >> 32);
-    uint4 r0 = philox4x32_10(make_uint4(id, tl, th, 0u), key);
-    uint4 r1 = philox4x32_10(make_uint4(id, tl, th, 1u), key);
-    const float rad = sqrtf(neg2log1m(u12(r0.x, r0.y)));
-    float s, c;
-    sincospif(2.0f * (float)(r0.z >> 8) * 0x1p-24f, &s, &c);
-    xi[0] = f2d(rad * c);
-    xi[1] = f2d(rad * s);
+    const NoiseF f = philox_noise_f(seed, id, t);
+    xi[0] = f2d(f.xi0);
+    xi[1] = f2d(f.xi1);
     if (Q2D) {
         xi[2] = 0.0;  // overwritten position z: never read
     } else {
-        uint4 r2 = philox4x32_10(make_uint4(id, tl, th, 2u), key);
+        const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+        const uint4 r2 = philox4x32_10(make_uint4(id, (uint32_t)t, (uint32_t)(t >> 32), 2u), key);
         const float rad2 = sqrtf(neg2log1m(u12(r2.x, r2.y)));
         xi[2] = f2d(rad2 * cospif(2.0f * (float)(r2.z >> 8) * 0x1p-24f));
     }
-    float saf, caf;
-    sincospif(2.0f * (float)(r1.x >> 8) * 0x1p-24f, &saf, &caf);
-    sa = f2d(saf);
-    ca = sqrt(fma(-sa, sa, 1.0));  // |saf| <= 1: the argument is >= 0
-    ca = __longlong_as_double(__double_as_longlong(ca) | ((long long)(__float_as_uint(caf) >> 31) << 63));
-    rot = sigma * f2d(sqrtf(neg2log1m(u12(r1.z, r1.w))));
+    sa = f2d(f.sa);
+    ca = sqrt(fma(-sa, sa, 1.0));  // |sa| <= 1: the argument is >= 0
+    ca = __longlong_as_double(__double_as_longlong(ca) | ((long long)(__float_as_uint(f.ca) >> 31) << 63));
+    rot = sigma * f2d(f.rad);
     if (WANT_ALPHA) {
         double a = atan2(sa, ca);
         *alpha = a < 0.0 ? a + kTwoPi : a;

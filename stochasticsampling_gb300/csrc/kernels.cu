@@ -9,6 +9,7 @@
 //   cuFFT     inverse Z2Z of 12 (+12) components
 //   table     per-cell row: Re u, W, E, B*mdd, grad B
 //   update    gather row by cell, Langevin step, wrap, bin into next histogram
+#include "f32x2.cuh"
 #include "kernels.cuh"
 
 #include <cstdio>
@@ -375,15 +376,22 @@ __global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__
         row[T_E12] = (g[5] + g[7]) * 0.5;
         row[T_E22] = (g[8] + g[8]) * 0.5;
         if (ctab) {  // the canonical quasi-2-D chain's row (CT_*), pre-multiplied by dt
+            const double v[CTAB_STRIDE] = {row[T_U] * P.dt, row[T_U + 1] * P.dt, row[T_W01] * P.dt,
+                                           row[T_E00] * P.shape_dt, row[T_E01] * P.shape_dt,
+                                           row[T_E11] * P.shape_dt, row[T_DIFF], 0.0};
             double *cr = ctab + (long long)c * CTAB_STRIDE;
-            cr[CT_U0] = row[T_U] * P.dt;
-            cr[CT_U1] = row[T_U + 1] * P.dt;
-            cr[CT_W01] = row[T_W01] * P.dt;
-            cr[CT_E00] = row[T_E00] * P.shape_dt;
-            cr[CT_E01] = row[T_E01] * P.shape_dt;
-            cr[CT_E11] = row[T_E11] * P.shape_dt;
-            cr[CT_DIFF] = row[T_DIFF];
-            cr[7] = 0.0;
+            if (P.f32x2) {  // the same row as float pairs (hi, lo) in the same 64 bytes
+                float *cf = reinterpret_cast<float *>(cr);
+#pragma unroll
+                for (int k = 0; k < CTAB_STRIDE; ++k) {
+                    const float h = __double2float_rn(v[k]);
+                    cf[2 * k] = h;
+                    cf[2 * k + 1] = __double2float_rn(v[k] - (double)h);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < CTAB_STRIDE; ++k) cr[k] = v[k];
+            }
         }
     }
     if (MAG) {
@@ -394,6 +402,41 @@ __global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__
     }
 }
 
+// The canonical quasi-2-D step with its increments in two-float arithmetic
+// (f32x2.cuh): the noise as floats (Philox) or as pairs of the host noise,
+// the cell's float-pair table row ct, and the sums with the FP64 state in
+// FP64 (h first, then l) before the periodic wrap.  Its kernel variant is
+// compiled for 5 blocks of 256 per SM (48 registers, no spills): the chain
+// is bound by instruction issue, and 62.5 % occupancy issues 5 % more per
+// clock than the 50 % that 58 registers allow.
+template <int NOISE>
+__device__ __forceinline__ void langevin_canon_f2(const DevParams &P, double &px, double &py, double &pph,
+                                                  const float4 *__restrict__ ct, uint32_t pid,
+                                                  const double *__restrict__ noise,
+                                                  const unsigned long long *__restrict__ d_step) {
+    const xf::CanonTerms T = {(P.mask & M_SELF_PROPULSION) != 0u, (P.mask & M_CONVECTION) != 0u,
+                              (P.mask & M_TRANS_DIFFUSION) != 0u, (P.mask & M_ROT_DIFFUSION) != 0u,
+                              (P.mask & M_EXTERNAL_FIELD) != 0u, (P.mask & M_JEFFREY_VORTICITY) != 0u,
+                              (P.mask & M_JEFFREY_STRAIN) != 0u};
+    const xf::f2 dt2 = {P.dt2[0], P.dt2[1]}, re2 = {P.reorient2[0], P.reorient2[1]};
+    xf::f2 dx, dy, dph;
+    if (NOISE == 0) {
+        const NoiseF f = philox_noise_f(P.seed, pid, *d_step);
+        // unnormalised: sincos_f2 adds the low part to the reduced angle exactly
+        const xf::f2 rot = xf::mul_u(xf::f2{P.sigma2[0], P.sigma2[1]}, f.rad);
+        xf::canon_increments(pph, ct, f.xi0, f.xi1, f.sa, rot, T, dt2, re2, dx, dy, dph);
+    } else {
+        const double *r = noise + 5ull * pid;
+        double sa, ca;
+        sincos(r[3], &sa, &ca);
+        xf::canon_increments(pph, ct, xf::split(r[0]), xf::split(r[1]), xf::split(sa), xf::split(r[4]), T, dt2,
+                             re2, dx, dy, dph);
+    }
+    px = ref_modulo((px + f2d(dx.h)) + f2d(dx.l), P.bx);
+    py = ref_modulo((py + f2d(dy.h)) + f2d(dy.l), P.by);
+    pph = ref_modulo((pph + f2d(dph.h)) + f2d(dph.l), kTwoPi);
+}
+
 // ------------------------------------------------------------------------
 // particle update: the loop of src/bin/simulation/mod.rs:318-369 fused with
 // the next step's binning (histogram_from) so each step reads and writes the
@@ -401,10 +444,12 @@ __global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__
 // indexed by the caller's particle order.  CANON (quasi2d, every particle in
 // the canonical state z = 0, theta = pi/2, no magnetic step, nearest-cell
 // gather): the chain of langevin_canon, and z and theta are neither read nor
-// written.
+// written.  F2 (with CANON): the same chain's increments in two-float
+// arithmetic (f32x2.cuh) from the float-pair table row, added to the FP64
+// state in FP64.
 // ------------------------------------------------------------------------
-template <bool Q2D, bool MAG, int NOISE, bool TRI, bool CANON = false>
-__global__ void __launch_bounds__(256) k_update(DevParams P, double *__restrict__ x, double *__restrict__ y,
+template <bool Q2D, bool MAG, int NOISE, bool TRI, bool CANON = false, bool F2 = false>
+__global__ void __launch_bounds__(256, (CANON && F2) ? 5 : 1) k_update(DevParams P, double *__restrict__ x, double *__restrict__ y,
                                                 double *__restrict__ z, double *__restrict__ phi,
                                                 double *__restrict__ theta, uint32_t *__restrict__ key,
                                                 const uint32_t *__restrict__ id, const double *__restrict__ table,
@@ -424,21 +469,25 @@ __global__ void __launch_bounds__(256) k_update(DevParams P, double *__restrict_
         trilinear_row<MAG>(table, P, px, py, pz, trow);
         F.r = trow;
     }
-    double xi[3], ca, sa, rot;
-    if (NOISE == 0) {
-        philox_noise<Q2D>(P.seed, pid, *d_step, P.sigma_rot, xi, ca, sa, rot);
+    if (CANON && F2) {
+        langevin_canon_f2<NOISE>(P, px, py, pph, reinterpret_cast<const float4 *>(F.r), pid, noise, d_step);
     } else {
-        const double *r = noise + 5ull * pid;
-        xi[0] = r[0]; xi[1] = r[1]; xi[2] = r[2];
-        sincos(r[3], &sa, &ca);
-        rot = r[4];
-    }
-    if (CANON) {
-        langevin_canon(px, py, pph, F.r, xi, sa, rot, P.mask, P.dt, P.reorient_dt, P.bx, P.by);
-    } else {
-        bool have_theta = Q2D && (__double_as_longlong(pth) == __double_as_longlong(kPiHalf));
-        langevin<Q2D>(px, py, pz, pph, pth, F, xi, ca, sa, rot, P.mask, P.dt, P.reorient, P.shape, P.drag, P.bx,
-                      P.by, P.bz, have_theta, P.cos_half_pi, P.sin_half_pi);
+        double xi[3], ca, sa, rot;
+        if (NOISE == 0) {
+            philox_noise<Q2D>(P.seed, pid, *d_step, P.sigma_rot, xi, ca, sa, rot);
+        } else {
+            const double *r = noise + 5ull * pid;
+            xi[0] = r[0]; xi[1] = r[1]; xi[2] = r[2];
+            sincos(r[3], &sa, &ca);
+            rot = r[4];
+        }
+        if (CANON) {
+            langevin_canon(px, py, pph, F.r, xi, sa, rot, P.mask, P.dt, P.reorient_dt, P.bx, P.by);
+        } else {
+            bool have_theta = Q2D && (__double_as_longlong(pth) == __double_as_longlong(kPiHalf));
+            langevin<Q2D>(px, py, pz, pph, pth, F, xi, ca, sa, rot, P.mask, P.dt, P.reorient, P.shape, P.drag,
+                          P.bx, P.by, P.bz, have_theta, P.cos_half_pi, P.sin_half_pi);
+        }
     }
     uint32_t err = 0, ncell;
     unsigned long long bin;
@@ -719,12 +768,12 @@ void launch_update(cudaStream_t s, bool q2d, bool canon, bool mag, bool host_noi
     if (!P.n) return;
     unsigned b = nblocks(P.n, 256);
     if (q2d && canon && ctab && !mag && !P.gather && !(P.mask & (M_MDD_FORCE | M_MDD_ROTATION))) {
-        if (host_noise)
-            k_update<true, false, 1, false, true><<<b, 256, 0, s>>>(P, xs[0], xs[1], xs[2], xs[3], xs[4], key, id,
-                                                                    ctab, noise, d_step, counts_next, err);
-        else
-            k_update<true, false, 0, false, true><<<b, 256, 0, s>>>(P, xs[0], xs[1], xs[2], xs[3], xs[4], key, id,
-                                                                    ctab, noise, d_step, counts_next, err);
+#define SS_CANON(N, F)                                                                                      \
+    k_update<true, false, N, false, true, F><<<b, 256, 0, s>>>(P, xs[0], xs[1], xs[2], xs[3], xs[4], key, id, \
+                                                               ctab, noise, d_step, counts_next, err)
+        if (P.f32x2) { if (host_noise) SS_CANON(1, true); else SS_CANON(0, true); }
+        else { if (host_noise) SS_CANON(1, false); else SS_CANON(0, false); }
+#undef SS_CANON
         return;
     }
 #define SS_UPD(Q, M, N, T)                                                                                   \

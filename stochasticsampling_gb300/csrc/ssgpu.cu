@@ -560,6 +560,10 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
         destroy_impl(c);
         return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "the mixed-precision mode supports at most 1024 angle bins");
     }
+    if (c->mixed && (flags & SS_FLAG_F32X2)) {
+        destroy_impl(c);
+        return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "SS_FLAG_F32X2 applies to the FP64 mode only");
+    }
     if (c->mixed) c->sort = false;
     c->mag_step = (flags & SS_FLAG_ALWAYS_MAGNETIC) || params->magnetic_dipole_dipole != 0.0 ||
                   params->magnetic_drag != 0.0;
@@ -616,6 +620,15 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     P.measure = P.gw[3] * P.gw[4];
     P.dthph = P.gw[4] * P.gw[3];
     P.sigma_rot = std::sqrt(2. * params->rot_diffusion * params->timestep);
+    {  // float pairs (hi, lo) of the constants of the two-float chain
+        const double v[3] = {P.dt, P.reorient_dt, P.sigma_rot};
+        float *out[3] = {P.dt2, P.reorient2, P.sigma2};
+        for (int k = 0; k < 3; ++k) {
+            out[k][0] = (float)v[k];
+            out[k][1] = (float)(v[k] - (double)out[k][0]);
+        }
+    }
+    P.f32x2 = (flags & SS_FLAG_F32X2) ? 1 : 0;
     P.seed = params->seed;
     P.quasi2d = c->q2d ? 1 : 0;
     {  // floor((pi/2) / gw_theta) with the n -> n-1 clamp: the bin ref_bin gives pi/2

@@ -52,7 +52,7 @@ class Simulation:
     """One simulation on the current CUDA device."""
 
     def __init__(self, settings=None, *, grid=None, box=None, params=None, quasi2d=False, sort=True, graph=True,
-                 always_magnetic=False, mixed=False, gather="nearest", stream=None):
+                 always_magnetic=False, mixed=False, gather="nearest", f32x2=False, stream=None):
         if settings is not None:
             grid, box, params = geometry_from_settings(settings)
         if grid is None or box is None or params is None:
@@ -76,6 +76,8 @@ class Simulation:
             flags |= _lib.FLAG_NO_GRAPH
         if always_magnetic:
             flags |= _lib.FLAG_ALWAYS_MAGNETIC
+        if f32x2:
+            flags |= _lib.FLAG_F32X2
         if mixed == "fixed64":
             flags |= _lib.FLAG_FIXED64
         elif mixed:

@@ -1,0 +1,208 @@
+"""The two-float arithmetic of the FP64 update (csrc/f32x2.cuh), compiled for
+the CPU from the same header (tests/f32x2_host.cpp) and checked against
+x86 extended precision (64-bit significand): the double -> pair split,
+sin / cos of a double angle and of a pair angle, atan2 of pairs, and the
+increments dx, dy, dphi of the canonical quasi-2-D chain.  The GPU parity
+tests pin the compiled device code against the oracle."""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "..", "stochasticsampling_gb300", "csrc")
+LD = np.longdouble
+
+pytestmark = pytest.mark.skipif(np.finfo(np.longdouble).nmant < 63 or shutil.which("g++") is None,
+                                reason="needs g++ and a long double with a 64-bit significand")
+
+TERMS = dict(sp=1, conv=2, trans=4, rot=8, ext=16, vort=32, strain=64, float_noise=128)
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    out = tmp_path_factory.mktemp("xf") / "libxf.so"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", "-I", CSRC,
+                    os.path.join(HERE, "f32x2_host.cpp"), "-o", str(out)], check=True)
+    L = ctypes.CDLL(str(out))
+    for name in ("xf_split", "xf_sincos_d", "xf_sincos_f2", "xf_atan2", "xf_canon"):
+        getattr(L, name).restype = None
+    return L
+
+
+def _p(a):
+    return np.ascontiguousarray(a).ctypes.data_as(ctypes.c_void_p)
+
+
+def split(lib, d):
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    out = np.empty(2 * d.size, np.float32)
+    lib.xf_split(len(d), _p(d), _p(out))
+    return out.reshape(-1, 2)
+
+
+def val(pairs):
+    """exact value of float pairs (rows h, l) in extended precision"""
+    pairs = np.asarray(pairs)
+    return pairs[..., 0].astype(LD) + pairs[..., 1].astype(LD)
+
+
+def rand_pairs(rng, x):
+    """pairs (h, l) of arbitrary low parts around x: h = float(x), l a float below ulp(h) / 2"""
+    h = np.float32(x)
+    l = (rng.random(h.shape) - 0.5) * np.spacing(np.abs(h)).astype(np.float64)
+    return np.stack([h, l.astype(np.float32)], axis=-1)
+
+
+def test_split_is_nearest_pair(lib):
+    rng = np.random.default_rng(0)
+    d = np.concatenate([rng.normal(size=2000) * 10.0 ** rng.integers(-30, 30, 2000),
+                        [0.0, -0.0, 1.0, -1.5, 2.0 ** -126, 3.0 * 2.0 ** -127, 1e-300, np.pi]])
+    p = split(lib, d)
+    assert np.array_equal(p[:, 0], d.astype(np.float32))
+    rest = d - p[:, 0].astype(np.float64)  # exact: h is within half an ulp of float of d
+    big = np.abs(d) >= 2.0 ** -90
+    assert np.array_equal(p[big, 1], rest[big].astype(np.float32))
+    assert np.all(np.abs(p[~big, 1].astype(np.float64) - rest[~big]) <= 2.0 ** -126)
+    for bad in (np.inf, -np.inf):
+        h, l = split(lib, [bad])[0]
+        assert h == bad and l == 0.0
+    assert np.isnan(split(lib, [np.nan])[0, 0])
+
+
+def test_sincos_of_double_angles(lib):
+    rng = np.random.default_rng(1)
+    a = np.concatenate([rng.random(20000) * 2 * np.pi, np.arange(0, 6.3, 1 / 512.0),
+                        np.arange(0, 6.3, 1 / 512.0) + 1 / 1024.0, [0.0, 1e-300, 2.0 ** -20, np.pi / 2, np.pi,
+                                                                   6.2999999, 6.3, 7.0, 100.0, -0.5]])
+    out = np.empty(4 * a.size)
+    lib.xf_sincos_d(len(a), _p(a), _p(out))
+    out = out.reshape(-1, 4)
+    al = a.astype(LD)
+    es = np.abs(val(out[:, 0:2]) - np.sin(al))
+    ec = np.abs(val(out[:, 2:4]) - np.cos(al))
+    # measured: 7.6e-15 (2^-47.1) at most, 6e-16 on average (the pair's own resolution)
+    assert es.max() < 2.0 ** -46 and ec.max() < 2.0 ** -46, (float(es.max()), float(ec.max()))
+
+
+def test_sincos_of_pair_angles(lib):
+    rng = np.random.default_rng(2)
+    r = rand_pairs(rng, np.concatenate([np.abs(rng.normal(size=20000)) * 0.4, rng.random(2000) * 6.25,
+                                        [0.0, 1e-9, 1 / 512.0, 6.2499]]))
+    out = np.empty(4 * len(r))
+    lib.xf_sincos_f2(len(r), _p(r), _p(out))
+    out = out.reshape(-1, 4)
+    rl = val(r)
+    es = np.abs(val(out[:, 0:2]) - np.sin(rl))
+    ec = np.abs(val(out[:, 2:4]) - np.cos(rl))
+    assert es.max() < 2.0 ** -46 and ec.max() < 2.0 ** -46, (float(es.max()), float(ec.max()))
+    # angles beyond the table go through FP64 sincos
+    far = rand_pairs(rng, np.array([6.25, 7.0, 30.0]))
+    o2 = np.empty(12)
+    lib.xf_sincos_f2(3, _p(far), _p(o2))
+    assert np.all(np.abs(val(o2.reshape(-1, 4)[:, 0:2]) - np.sin(val(far))) < 1e-15)
+
+
+def test_atan2_of_pairs(lib):
+    rng = np.random.default_rng(3)
+    n = 20000
+    ang = np.concatenate([rng.normal(size=n) * 0.2, rng.random(n) * 2 * np.pi - np.pi])
+    rad = 0.2 + rng.random(2 * n) * 2
+    y, x = rand_pairs(rng, rad * np.sin(ang)), rand_pairs(rng, rad * np.cos(ang))
+    out = np.empty(2 * len(y))
+    lib.xf_atan2(len(y), _p(y), _p(x), _p(out))
+    exact = np.arctan2(val(y), val(x))
+    err = np.abs(val(out.reshape(-1, 2)) - exact)
+    # about 2^-47 of the table angle a_j and of the result: an angle near 1e-3
+    # reached as a_1 - eps (2^-9 - 1e-3) carries ~4e-17 absolute
+    assert np.all(err <= 2.0 ** -46 * (np.abs(exact) + 2.0 ** -8)), float(err.max())
+    # zero, signed zero, axes, tiny and huge vectors
+    cases = [(0.0, 1.0), (-0.0, 1.0), (0.0, -1.0), (-0.0, -1.0), (1.0, 0.0), (-1.0, 0.0), (1e-30, 1.0),
+             (1e30, 1e30), (3.0, -4.0), (-3.0, -4.0)]
+    yy = np.array([[c[0], 0.0] for c in cases], np.float32)
+    xx = np.array([[c[1], 0.0] for c in cases], np.float32)
+    o = np.empty(2 * len(cases))
+    lib.xf_atan2(len(cases), _p(yy), _p(xx), _p(o))
+    o = o.reshape(-1, 2)
+    for k, (cy, cx) in enumerate(cases):
+        ref = np.arctan2(LD(np.float32(cy)), LD(np.float32(cx)))
+        assert abs(val(o[k]) - ref) <= 2.0 ** -46 * abs(ref) + 1e-300, (cy, cx)
+        assert np.signbit(o[k, 0]) == np.signbit(ref), (cy, cx)
+
+
+def _canon_inputs(rng, n, scale_flow=1.0):
+    phi = rng.random(n) * 2 * np.pi
+    dt, shape_dt, reorient_dt = 0.005, 0.4 * 0.005, 0.8 * 0.005
+    u0, u1 = (rng.normal(size=n) * 0.5 * scale_flow * dt for _ in range(2))
+    w01 = rng.normal(size=n) * 0.3 * scale_flow * dt
+    e00, e01, e11 = (rng.normal(size=n) * 0.3 * scale_flow * shape_dt for _ in range(3))
+    diff = np.full(n, np.sqrt(2 * 0.1 * dt))
+    ct = np.zeros((n, 8, 2), np.float32)
+    for k, v in enumerate([u0, u1, w01, e00, e01, e11, diff]):
+        ct[:, k] = rand_pairs(rng, v)
+    xi = np.concatenate([rand_pairs(rng, rng.normal(size=n)), rand_pairs(rng, rng.normal(size=n))], axis=1)
+    sa = rand_pairs(rng, np.sin(rng.random(n) * 2 * np.pi))
+    rot = rand_pairs(rng, 0.1 * np.sqrt(-2 * np.log(1 - rng.random(n))))
+    dtp = rand_pairs(rng, np.array([dt]))[0]
+    rep = rand_pairs(rng, np.array([reorient_dt]))[0]
+    return phi, ct, xi, sa, rot, dtp, rep
+
+
+def _canon_exact(phi, ct, xi, sa, rot, dtp, rep, terms, float_noise):
+    """the chain's increments in extended precision from the same inputs"""
+    cp, sp = np.cos(phi.astype(LD)), np.sin(phi.astype(LD))
+    u0, u1, w01, e00, e01, e11, diff = (val(ct[:, k]) for k in range(7))
+    x0, x1, s_a = (xi[:, 0].astype(LD), xi[:, 2].astype(LD), sa[:, 0].astype(LD)) if float_noise else \
+        (val(xi[:, 0:2]), val(xi[:, 2:4]), val(sa))
+    dt, re, r = val(dtp), val(rep), val(rot)
+    d0 = np.zeros_like(cp)
+    d1 = np.zeros_like(cp)
+    if terms & TERMS["sp"]:
+        d0, d1 = d0 + cp * dt, d1 + sp * dt
+    if terms & TERMS["conv"]:
+        d0, d1 = d0 + u0, d1 + u1
+    if terms & TERMS["trans"]:
+        d0, d1 = d0 + x0 * diff, d1 + x1 * diff
+    G = np.zeros_like(cp)
+    if terms & TERMS["ext"]:
+        G = G + re * cp
+    if terms & TERMS["vort"]:
+        G = G + w01
+    if terms & TERMS["strain"]:
+        f0, f1 = e00 * cp + e01 * sp, e01 * cp + e11 * sp
+        G = G + (cp * f1 - sp * f0)
+    C = np.ones_like(cp)
+    if terms & TERMS["rot"]:
+        G = G - s_a * np.sin(r)
+        C = np.cos(r)
+    return d0, d1, np.arctan2(G, C)
+
+
+@pytest.mark.parametrize("terms", [
+    TERMS["sp"] | TERMS["conv"] | TERMS["trans"] | TERMS["rot"] | TERMS["vort"],
+    TERMS["sp"] | TERMS["conv"] | TERMS["trans"] | TERMS["rot"] | TERMS["vort"] | TERMS["strain"] | TERMS["ext"],
+    TERMS["sp"] | TERMS["trans"] | TERMS["rot"] | TERMS["float_noise"],
+    TERMS["conv"] | TERMS["vort"] | TERMS["strain"],
+    TERMS["sp"] | TERMS["ext"],
+    0,
+], ids=["c1_terms", "all_terms", "device_noise", "flow_only", "no_noise", "none"])
+def test_canonical_increments(lib, terms):
+    rng = np.random.default_rng(terms)
+    n = 20000
+    phi, ct, xi, sa, rot, dtp, rep = _canon_inputs(rng, n)
+    out = np.empty(6 * n)
+    lib.xf_canon(n, _p(phi), _p(ct), _p(xi), _p(sa), _p(rot), ctypes.c_uint(terms), _p(dtp), _p(rep), _p(out))
+    out = out.reshape(n, 3, 2)
+    got = [val(out[:, k]) for k in range(3)]
+    exact = _canon_exact(phi, ct, xi, sa, rot, dtp, rep, terms, bool(terms & TERMS["float_noise"]))
+    for k, (g, e) in enumerate(zip(got, exact)):
+        err = np.abs(g - e)
+        # a few 2^-48 of the increment's terms: measured at most 7e-16 on dx, dy
+        # (terms up to ~0.15) and 4.1e-15 on dphi (up to ~0.5, mostly from
+        # sin rot), against ulps of 4.4e-16 (phi near pi) to 7.1e-15 (x near 40)
+        # and the 1e-12 bar of the step
+        assert np.all(err <= 2.0 ** -45 * np.maximum(np.abs(e), 0.01)), (k, float(err.max()))
+        assert float(err.max()) < (1.5e-15, 1.5e-15, 8e-15)[k], (k, float(err.max()))

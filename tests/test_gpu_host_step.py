@@ -27,8 +27,9 @@ def _rows(rng, n, canonical=True):
 
 
 @pytest.mark.parametrize("n", [100_003, 1_000_000], ids=["ragged", "1e6"])
-@pytest.mark.parametrize("flags", [dict(), dict(sort=False), dict(mixed=True), dict(mixed="fixed64")],
-                         ids=["fp64_sort", "fp64", "mixed", "fixed64"])
+@pytest.mark.parametrize("flags", [dict(), dict(sort=False), dict(sort=False, f32x2=True), dict(mixed=True),
+                                   dict(mixed="fixed64")],
+                         ids=["fp64_sort", "fp64", "f32x2", "mixed", "fixed64"])
 def test_step_host_equals_resume_step_get(n, flags):
     ss = _gpu()
     rng = np.random.default_rng(5)
