@@ -22,6 +22,10 @@ void xf_split(int n, const double *d, float *out) {
     }
 }
 
+void xf_to_double(int n, const float *f, double *out) {
+    for (int i = 0; i < n; ++i) out[i] = to_double(f[i]);
+}
+
 void xf_sincos_d(int n, const double *a, double *out) {
     for (int i = 0; i < n; ++i) {
         f2 s, c;

@@ -28,7 +28,7 @@ def lib(tmp_path_factory):
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", "-I", CSRC,
                     os.path.join(HERE, "f32x2_host.cpp"), "-o", str(out)], check=True)
     L = ctypes.CDLL(str(out))
-    for name in ("xf_split", "xf_sincos_d", "xf_sincos_f2", "xf_atan2", "xf_canon"):
+    for name in ("xf_split", "xf_to_double", "xf_sincos_d", "xf_sincos_f2", "xf_atan2", "xf_canon"):
         getattr(L, name).restype = None
     return L
 
@@ -71,6 +71,23 @@ def test_split_is_nearest_pair(lib):
         h, l = split(lib, [bad])[0]
         assert h == bad and l == 0.0
     assert np.isnan(split(lib, [np.nan])[0, 0])
+
+
+def test_to_double_is_exact(lib):
+    """float -> double from the bits: every class of float (zero, subnormal,
+    normal, inf, NaN) as the exact conversion gives it"""
+    rng = np.random.default_rng(4)
+    bits = np.concatenate([rng.integers(0, 2 ** 32, 200000, dtype=np.uint64).astype(np.uint32),
+                           np.array([0, 0x80000000, 1, 0x807FFFFF, 0x00800000, 0x7F7FFFFF, 0x7F800000,
+                                     0xFF800000, 0x7FC00001], np.uint32)])
+    f = bits.view(np.float32)
+    out = np.empty(f.size)
+    lib.xf_to_double(len(f), _p(f), _p(out))
+    with np.errstate(invalid="ignore"):  # signalling NaNs among the random bits
+        ref = f.astype(np.float64)
+    nan = np.isnan(ref)
+    assert np.array_equal(out[~nan].view(np.uint64), ref[~nan].view(np.uint64))
+    assert np.all(np.isnan(out[nan]))
 
 
 def test_sincos_of_double_angles(lib):
