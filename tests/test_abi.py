@@ -19,6 +19,15 @@ def test_header_and_loader_agree():
     assert _declared() == sorted(_lib.EXPORTS)
 
 
+def test_flag_values_agree_with_the_header():
+    from stochasticsampling_gb300 import _lib
+    text = open(os.path.join(ROOT, "include", "ssgpu.h")).read()
+    flags = dict(re.findall(r"^#define SS_(FLAG_\w+)\s+(\d+)u", text, flags=re.M))
+    assert "FLAG_F32X2" in flags and len(flags) >= 9
+    for name, value in flags.items():
+        assert getattr(_lib, name) == int(value), name
+
+
 def test_library_exports_every_declared_symbol():
     from stochasticsampling_gb300 import _lib
     L = _lib.load()
