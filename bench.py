@@ -419,10 +419,11 @@ def c2_particles(n, seed=3):
 
 
 def measure_c2(args, stream, rank, world, dist, barrier):
-    """The 3-D magnetic workload: the plain FP64 path and the FP32 mixed path
-    (FP64 positions), each over graph-replayed steps, and the mixed path's
-    errors per field against the FP64 path after one step from identical
-    state and noise."""
+    """The 3-D magnetic workload: the plain FP64 path, the FP64 mode with
+    two-float increments (SS_FLAG_F32X2) and the FP32 mixed path (FP64
+    positions), each over graph-replayed steps; the mixed path's errors per
+    field and the two-float mode's largest deviations against the FP64 path
+    after one step from identical state and noise."""
     import torch
 
     import stochasticsampling_gb300 as ss
@@ -433,9 +434,9 @@ def measure_c2(args, stream, rank, world, dist, barrier):
     out = {"workload": "3-D with the dipolar solver: box 20^3, grid 64x64x64x16x8, uniform positions and "
                        "orientations on the sphere, dipolar coupling 0.5, external field 1, active stress -1, "
                        "Dt 0.1, Dr 1.0, dt 0.002", "particles": n, "steps": steps}
-    for name, mode in (("fp64", False), ("mixed", True)):
+    for name, mode, f32x2 in (("fp64", False, False), ("f32x2", False, True), ("mixed", True, False)):
         # rows counting-sorted by cell at init keep their locality over these steps: no per-step sort
-        sim = ss.Simulation(grid=C2_GRID, box=C2_BOX, params=params, mixed=mode, sort=False,
+        sim = ss.Simulation(grid=C2_GRID, box=C2_BOX, params=params, mixed=mode, sort=False, f32x2=f32x2,
                             stream=stream.cuda_stream)
         sim.init(p0)
         with torch.cuda.stream(stream):
@@ -456,16 +457,27 @@ def measure_c2(args, stream, rank, world, dist, barrier):
         sim.close()
         value, ms_max = aggregate(ms, n, steps, world, dist)
         out[name] = {"value": value, "unit": UNIT, "ms_per_step": ms_max / steps,
-                     "dtype": "f32 + f64 positions" if mode else "f64",
+                     "dtype": "f32 + f64 positions" if mode else
+                     ("f64 state and sums, f32x2 increments" if f32x2 else "f64"),
                      "stage_ms": {k: v / max(1, nprof) for k, v in stage_ms.items()}}
     m = ss.Simulation(grid=C2_GRID, box=C2_BOX, params=params, mixed=True)
     d = ss.Simulation(grid=C2_GRID, box=C2_BOX, params=params)
+    f = ss.Simulation(grid=C2_GRID, box=C2_BOX, params=params, f32x2=True)
     m.init(p0)
     d.init(p0)
+    f.init(p0)
     cm, cd = m.get_counts().astype(np.float64), d.get_counts().astype(np.float64)
     noise = m.noise(0)
     m.do_timestep()
     d.do_timestep(noise)
+    f.do_timestep(noise)
+    pf, pd0 = f.get_particles(), d.get_particles()
+    df = np.abs(pf - pd0)
+    df[:, 3] = np.minimum(df[:, 3], 2 * np.pi - df[:, 3]) * np.sin(pd0[:, 4])
+    out["f32x2"]["max_abs_dev_vs_fp64_one_step"] = {
+        "position": float(df[:, :3].max()), "theta": float(df[:, 4].max()),
+        "phi_times_sin_theta": float(df[:, 3].max())}
+    f.close()
     um, ud = m.get_flow_field(), d.get_flow_field()
     bm, bd = m.get_magnetic_field(), d.get_magnetic_field()
     pm, pd = m.get_particles(), d.get_particles()

@@ -72,12 +72,12 @@ typedef struct {
 #define SS_FLAG_FIXED64 128u       /* as SS_FLAG_MIXED, with positions accumulated in 64-bit fixed point
                                       (units of L / 2^64: periodic wrap by integer overflow, exact binning by
                                       a 64-bit high multiply, no FP64 instruction in the step) */
-#define SS_FLAG_F32X2 256u         /* FP64 mode: the quasi-2-D update of particles in the canonical state
-                                      (z = 0, theta = pi/2, nearest-cell gather, no dipolar terms) computes
-                                      the step's increments dx, dy, dphi in two-float (FP32 pair)
-                                      arithmetic, about 2^-46 relative, and adds them to the FP64 state in
-                                      FP64; every other part of the step, and every other update, as in
-                                      the FP64 mode (not with SS_FLAG_MIXED or SS_FLAG_FIXED64) */
+#define SS_FLAG_F32X2 256u         /* FP64 mode: the update computes each step's increments (position,
+                                      and the angle changes) in two-float (FP32 pair) arithmetic, about
+                                      2^-46 relative, and adds them to the FP64 state in FP64; the field
+                                      table is then kept as float pairs.  Needs the nearest-cell gather
+                                      (no effect with SS_FLAG_TRILINEAR*); not with SS_FLAG_MIXED or
+                                      SS_FLAG_FIXED64 */
 #define SS_FLAG_TRILINEAR 32u      /* gather every field by trilinear interpolation at the particle position
                                       (src/mesh/interpolate.rs:11-119) instead of the nearest cell that
                                       do_timestep uses (FP64 mode) */

@@ -76,7 +76,8 @@ struct DevParams {
     double cos_half_pi, sin_half_pi;  // cos/sin of kPiHalf as evaluated on this device
     double shape_dt, reorient_dt;     // shape * dt, magnetic_reorientation * dt (canonical table)
     float dt2[2], reorient2[2], sigma2[2];  // dt, reorient_dt, sigma_rot as float pairs (hi, lo)
-    int f32x2;         // the canonical quasi-2-D chain in two-float arithmetic (f32x2.cuh)
+    float reorient_f2[2], shape2[2], drag2[2];  // magnetic_reorientation, shape, magnetic_drag as pairs
+    int f32x2;         // the update's increments in two-float arithmetic (f32x2.cuh), nearest-cell gather
     float igwf[5];     // 1 / gw in FP32 (first estimate of the bin index)
     float bintol[5];   // half-width of the band around an integer where the FP32 estimate defers to FP64
     unsigned long long seed;
@@ -339,6 +340,15 @@ __device__ __forceinline__ NoiseF philox_noise_f(unsigned long long seed, uint32
     return f;
 }
 
+// The third normal (the z component of the translational noise, 3-D steps)
+// as its FP32 value, from the third Philox block.
+__device__ __forceinline__ float philox_xi2_f(unsigned long long seed, uint32_t id, unsigned long long t) {
+    const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+    const uint4 r2 = philox4x32_10(make_uint4(id, (uint32_t)t, (uint32_t)(t >> 32), 2u), key);
+    const float rad2 = sqrtf(neg2log1m(u12(r2.x, r2.y)));
+    return rad2 * cospif(2.0f * (float)(r2.z >> 8) * 0x1p-24f);
+}
+
 template <bool Q2D, bool WANT_ALPHA = false>
 __device__ __forceinline__ void philox_noise(unsigned long long seed, uint32_t id, unsigned long long t,
                                              double sigma, double xi[3], double &ca, double &sa,
@@ -346,14 +356,7 @@ __device__ __forceinline__ void philox_noise(unsigned long long seed, uint32_t i
     const NoiseF f = philox_noise_f(seed, id, t);
     xi[0] = f2d(f.xi0);
     xi[1] = f2d(f.xi1);
-    if (Q2D) {
-        xi[2] = 0.0;  // overwritten position z: never read
-    } else {
-        const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
-        const uint4 r2 = philox4x32_10(make_uint4(id, (uint32_t)t, (uint32_t)(t >> 32), 2u), key);
-        const float rad2 = sqrtf(neg2log1m(u12(r2.x, r2.y)));
-        xi[2] = f2d(rad2 * cospif(2.0f * (float)(r2.z >> 8) * 0x1p-24f));
-    }
+    xi[2] = Q2D ? 0.0 : f2d(philox_xi2_f(seed, id, t));  // quasi2d: z is overwritten, never read
     sa = f2d(f.sa);
     ca = sqrt(fma(-sa, sa, 1.0));  // |sa| <= 1: the argument is >= 0
     ca = __longlong_as_double(__double_as_longlong(ca) | ((long long)(__float_as_uint(f.ca) >> 31) << 63));

@@ -1,16 +1,18 @@
 // f32x2.cuh -- two-float arithmetic (a value held as the unevaluated sum
 // h + l of two floats, about 48 significant bits) and the increments of the
-// canonical quasi-2-D Langevin step (src/integrators/langevin.rs via
-// src/bin/simulation/mod.rs:318-369, the chain of langevin_canon in
-// common.cuh) computed in it.
+// Langevin step (src/bin/simulation/mod.rs:318-369) computed in it: the
+// canonical quasi-2-D chain (langevin_canon in common.cuh) and the full
+// chain (langevin<> in common.cuh, 3-D and quasi-2-D rows off the canonical
+// state).
 //
 // GB300 issues FP32 at 128 operations per clock per SM and FP64 at 2, so a
 // two-float operation of 3 to 11 FP32 instructions costs a fraction of one
 // FP64 instruction.  The particle state stays FP64.  A step's increments
-// (dx, dy of order |v| dt + sqrt(2 Dt dt) |xi|, dphi of order |rot|) are
-// small beside the coordinates they are added to, so their relative error
-// of about 2^-47 lies near or below an ulp of the new coordinate; those
-// additions (two per coordinate, h then l) are the only FP64 arithmetic.
+// (dx, dy of order |v| dt + sqrt(2 Dt dt) |xi|, the angle changes of order
+// |rot|) are small beside the coordinates they are added to, so their
+// relative error of about 2^-47 lies near or below an ulp of the new
+// coordinate; those additions (two per coordinate, h then l) are the only
+// FP64 arithmetic.
 //
 // Error-free transformations (Dekker 1971; Knuth, TAOCP vol. 2, 4.2.2;
 // Muller et al., Handbook of Floating-Point Arithmetic, ch. 4): two_sum,
@@ -32,6 +34,9 @@
 #define SS_TRIGF_ATTR static const
 struct float4 {
     float x, y, z, w;
+};
+struct float2 {
+    float x, y;
 };
 #endif
 
@@ -59,6 +64,7 @@ SS_XF uint32_t fbits(float f) { return __float_as_uint(f); }
 SS_XF float bitsf(uint32_t u) { return __uint_as_float(u); }
 SS_XF int clz32(uint32_t v) { return __clz((int)v); }
 SS_XF float4 trigf(int j) { return __ldg(&kTrigF[j]); }
+SS_XF float2 ldg2(const float2 *p) { return __ldg(p); }
 SS_XF double atan2_(double y, double x) { return atan2(y, x); }
 SS_XF void sincos_(double a, double *s, double *c) { sincos(a, s, c); }
 #else
@@ -75,6 +81,7 @@ SS_XF uint32_t fbits(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
 SS_XF float bitsf(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
 SS_XF int clz32(uint32_t v) { return v ? __builtin_clz(v) : 32; }
 SS_XF float4 trigf(int j) { return kTrigF[j]; }
+SS_XF float2 ldg2(const float2 *p) { return *p; }
 SS_XF double atan2_(double y, double x) { return atan2(y, x); }
 SS_XF void sincos_(double a, double *s, double *c) { *s = sin(a); *c = cos(a); }
 #endif
@@ -263,6 +270,64 @@ SS_XF void sincos_f2(f2 r, f2 &s, f2 &c) {
     sincos_red(j, two_sum(sub_(r.h, aj), r.l), s, c);
 }
 
+// sin r and cos r - 1 of a pair angle r >= 0, the latter without the
+// cancellation of cos r - 1: (C_j - 1) + C cb - S sb from the table pair
+// of C_j (C_j - 1 formed exactly by two_sum).  Absolute error about 2^-48
+// on both (the table pair's own rounding of C_j); r.h >= 6.25 or NaN takes
+// FP64 sincos.
+SS_XF void sin_cosm1_f2(f2 r, f2 &s, f2 &cm1) {
+    if (!(r.h >= 0.0f && r.h < 6.25f)) {
+        double sd, cd;
+        sincos_(to_double(r.h) + to_double(r.l), &sd, &cd);
+        s = split(sd);
+        cm1 = split(cd - 1.0);
+        return;
+    }
+    float aj;
+    const int j = round512f(r.h, aj);
+    const f2 b = two_sum(sub_(r.h, aj), r.l);
+    const float4 t = trigf(j);
+    f2 z = two_prod(b.h, b.h);
+    z.l = fma_(add_(b.h, b.h), b.l, z.l);
+    const f2 sb = {b.h, add_(b.l, mul_(mul_(b.h, z.h), fma_(z.h, 1.0f / 120.0f, -1.0f / 6.0f)))};
+    const f2 cb = {mul_(z.h, -0.5f), fma_(mul_(z.h, z.h), 1.0f / 24.0f, mul_(z.l, -0.5f))};
+    {
+        const f2 p = prod(t.x, t.y, sb), q = prod(t.z, t.w, cb);
+        const f2 u = two_sum(t.z, p.h), v = two_sum(u.h, q.h);
+        s = fast_two_sum(v.h, add_(add_(add_(p.l, q.l), add_(u.l, v.l)), t.w));
+    }
+    {
+        const f2 c0 = two_sum(t.x, -1.0f);  // C_j - 1 (with the table's low part below)
+        const f2 p = prod(t.x, t.y, cb), q = prod(-t.z, -t.w, sb);
+        const f2 u = two_sum(c0.h, q.h), v = two_sum(u.h, p.h);
+        cm1 = fast_two_sum(v.h, add_(add_(add_(p.l, q.l), add_(u.l, v.l)), add_(c0.l, t.y)));
+    }
+}
+
+// sqrt of a pair x >= 0: the FP32 root y of x.h and one correction with the
+// exact remainder x - y^2, relative error about 2^-46; (0, 0) for x.h <= 0
+SS_XF f2 sqrt_f2(f2 x) {
+    if (!(x.h > 0.0f)) return {0.0f, 0.0f};
+#ifdef __CUDA_ARCH__
+    const float y = __fsqrt_rn(x.h);
+#else
+    const float y = sqrtf(x.h);
+#endif
+    const f2 yy = two_prod(y, y);
+    const float r = add_(sub_(sub_(x.h, yy.h), yy.l), x.l);  // x.h - yy.h is exact (Sterbenz)
+    return fast_two_sum(y, mul_(r, mul_(0.5f, rcp_(y))));
+}
+
+// a / b for pairs with b.h > 0 normal: an FP32 quotient and one correction
+// with the exact remainder, relative error about 2^-46
+SS_XF f2 div_f2(f2 a, f2 b) {
+    const float r = rcp_(b.h);
+    const float q1 = mul_(a.h, r);
+    const f2 p = two_prod(q1, b.h);
+    const float rem = add_(sub_(sub_(a.h, p.h), p.l), sub_(a.l, mul_(q1, b.l)));
+    return fast_two_sum(q1, mul_(rem, r));
+}
+
 // An estimate of atan2(y, x) for y >= 0 (+0 included) within 1.1e-5: the
 // ratio of the smaller to the larger of y and |x| in [0, 1], atan of it by
 // the odd polynomial of Abramowitz & Stegun 4.4.47 (|error| <= 1e-5), then
@@ -375,6 +440,157 @@ SS_XF void canon_increments(double phi, const float4 *ct, XI xi0, XI xi1, SA sa,
     dx = d0;
     dy = d1;
     dphi = atan2_f2(G, C);
+}
+
+// ---- the full chain (3-D, and quasi-2-D rows off the canonical state) ----
+// Entries of a per-cell field row written as float pairs (the double table
+// row's layout, one pair in each 8 bytes): u[3], W01 W02 W12, E00 E01 E02
+// E11 E12 E22, the diffusion length, B[3] (times the dipolar coupling),
+// grad B[3][3].
+constexpr int R_U = 0, R_W01 = 3, R_W02 = 4, R_W12 = 5, R_E00 = 6, R_E01 = 7, R_E02 = 8, R_E11 = 9,
+              R_E12 = 10, R_E22 = 11, R_DIFF = 12, R_B = 13, R_GB = 16;
+
+SS_XF f2 row_f2(const float2 *row, int k) {
+    const float2 v = ldg2(row + k);
+    return {v.x, v.y};
+}
+
+struct FullTerms {
+    bool self_propulsion, convection, mdd_force, external_field, mdd_rotation, vorticity, strain, step,
+        trans_diffusion, rot_diffusion;
+};
+
+// The cosine of the rotation axis angle as the on-device noise defines it:
+// sqrt(1 - sa^2) with the sign of the FP32 cosine, sa the FP32 sine.
+SS_XF f2 axis_cos(float sa, float ca_f32) {
+    const f2 s2 = two_prod(sa, sa);
+    const f2 om = two_sum(1.0f, -s2.h);
+    const f2 c = sqrt_f2(fast_two_sum(om.h, sub_(om.l, s2.l)));
+    return (fbits(ca_f32) >> 31) ? neg(c) : c;
+}
+
+// Results of the full chain: the position increments and either the angle
+// increments (a = dphi, b = dtheta) or, within 2^-10 of a pole, the direct
+// angles (a = phi in (-pi, pi], b = pi/2 - theta).
+struct FullOut {
+    f2 dp[3], a, b;
+    bool direct;
+};
+
+// The chain of langevin<> (common.cuh; LangevinBuilder and its modifiers,
+// src/integrators/langevin_builder/mod.rs:25-125, modifiers.rs:39-231) in
+// pairs, term by term in the same order, for a particle at (phi, theta) in
+// a cell whose row is `row` (float pairs), with the noise xi (normals), sa,
+// ca (the rotation axis angle) and rot (the rotation angle).
+//
+// The new orientation v = n + dn is turned into angle increments without
+// the cancellation of atan2(v) - (phi, theta): with n the unit vector at
+// (phi, theta), |n_xy| = sin theta = st,
+//   dphi   = atan2(n0 dn1 - n1 dn0, st^2 + n0 dn0 + n1 dn1)
+//   dtheta = atan2(delta ct - dn2 st, |v_xy| st + v2 ct),
+//   delta  = |v_xy| - st = (2 (n0 dn0 + n1 dn1) + dn0^2 + dn1^2) / (|v_xy| + st),
+// the angle between the horizontal projections and the difference of the
+// polar angles (|v_xy| itself from the components of v = n + dn).  Each is about 2^-46 of its own size, where the direct
+// angles carry 2^-46 of pi.  Near a pole (st < 2^-10) the direct angles
+// atan2(v1, v0) and pi/2 - atan2(v2, |v_xy|) of the reference are used.
+template <typename XI, typename SA>
+SS_XF void full_increments(double phi, double theta, const float2 *row, XI xi0, XI xi1, XI xi2, SA sa, f2 ca,
+                           f2 rot, const FullTerms &T, f2 dt, f2 reorient, f2 shape, f2 drag, FullOut &o) {
+    f2 sp, cp, st, ct;
+    sincos_d(phi, sp, cp);
+    sincos_d(theta, st, ct);
+    const f2 n[3] = {mul(st, cp), mul(st, sp), ct};
+    const f2 zero = {0.0f, 0.0f};
+    f2 dp[3] = {zero, zero, zero}, dn[3] = {zero, zero, zero};
+    if (T.self_propulsion) {  // modifiers.rs:39-46
+        dp[0] = n[0];
+        dp[1] = n[1];
+        dp[2] = n[2];
+    }
+    if (T.convection)  // modifiers.rs:49-56
+        for (int k = 0; k < 3; ++k) dp[k] = add(dp[k], row_f2(row, R_U + k));
+    if (T.mdd_force) {  // modifiers.rs:59-70: grad B . n * drag
+        for (int a = 0; a < 3; ++a) {
+            const f2 f = add(add(mul_u(row_f2(row, R_GB + 3 * a), n[0]), mul_u(row_f2(row, R_GB + 3 * a + 1), n[1])),
+                             mul_u(row_f2(row, R_GB + 3 * a + 2), n[2]));
+            dp[a] = add(dp[a], mul_u(f, drag));
+        }
+    }
+    if (T.external_field) {  // modifiers.rs:103-119: b = (0, r, 0), b - n (n . b)
+        const f2 d = mul(n[1], reorient);
+        dn[0] = add(dn[0], neg(mul_u(n[0], d)));
+        dn[1] = add(dn[1], add(reorient, neg(mul_u(n[1], d))));
+        dn[2] = add(dn[2], neg(mul_u(n[2], d)));
+    }
+    if (T.mdd_rotation) {  // modifiers.rs:172-187: b - n (n . b), b the dipolar field
+        const f2 b[3] = {row_f2(row, R_B), row_f2(row, R_B + 1), row_f2(row, R_B + 2)};
+        const f2 d = add(add(mul_u(n[0], b[0]), mul_u(n[1], b[1])), mul_u(n[2], b[2]));
+        for (int k = 0; k < 3; ++k) dn[k] = add(dn[k], add(b[k], neg(mul_u(n[k], d))));
+    }
+    if (T.vorticity) {  // modifiers.rs:123-143: -(W n), W antisymmetric
+        const f2 w01 = row_f2(row, R_W01), w02 = row_f2(row, R_W02), w12 = row_f2(row, R_W12);
+        const f2 f0 = add(mul_u(w01, n[1]), mul_u(w02, n[2]));
+        const f2 f1 = add(neg(mul_u(w01, n[0])), mul_u(w12, n[2]));
+        const f2 f2v = add(neg(mul_u(w02, n[0])), neg(mul_u(w12, n[1])));
+        dn[0] = add(dn[0], neg(f0));
+        dn[1] = add(dn[1], neg(f1));
+        dn[2] = add(dn[2], neg(f2v));
+    }
+    if (T.strain) {  // modifiers.rs:147-170: f - n (f . n), f = shape E n
+        const f2 e00 = row_f2(row, R_E00), e01 = row_f2(row, R_E01), e02 = row_f2(row, R_E02);
+        const f2 e11 = row_f2(row, R_E11), e12 = row_f2(row, R_E12), e22 = row_f2(row, R_E22);
+        f2 f[3] = {add(add(mul_u(e00, n[0]), mul_u(e01, n[1])), mul_u(e02, n[2])),
+                   add(add(mul_u(e01, n[0]), mul_u(e11, n[1])), mul_u(e12, n[2])),
+                   add(add(mul_u(e02, n[0]), mul_u(e12, n[1])), mul_u(e22, n[2]))};
+        for (int k = 0; k < 3; ++k) f[k] = mul(f[k], shape);
+        const f2 fn = add(add(mul_u(f[0], n[0]), mul_u(f[1], n[1])), mul_u(f[2], n[2]));
+        for (int k = 0; k < 3; ++k) dn[k] = add(dn[k], add(f[k], neg(mul_u(n[k], fn))));
+    }
+    if (T.step) {  // mod.rs:114-119
+        for (int k = 0; k < 3; ++k) {
+            dp[k] = mul(dp[k], dt);
+            dn[k] = mul(dn[k], dt);
+        }
+    }
+    if (T.trans_diffusion) {  // modifiers.rs:86-99
+        const f2 diff = row_f2(row, R_DIFF);
+        dp[0] = add(dp[0], mul_noise(diff, xi0));
+        dp[1] = add(dp[1], mul_noise(diff, xi1));
+        dp[2] = add(dp[2], mul_noise(diff, xi2));
+    }
+    if (T.rot_diffusion) {  // modifiers.rs:199-231, as Rodrigues: n (cos r - 1) + (k x n) sin r
+        const f2 ax0 = add(mul_noise(mul(cp, ct), sa), neg(mul_u(ca, sp)));
+        const f2 ax1 = add(mul_u(ca, cp), mul_u(mul_noise(ct, sa), sp));
+        const f2 ax2 = neg(mul_noise(st, sa));
+        f2 sr, cm1;
+        sin_cosm1_f2(rot, sr, cm1);
+        const f2 k0 = add(mul_u(ax1, n[2]), neg(mul_u(ax2, n[1])));
+        const f2 k1 = add(mul_u(ax2, n[0]), neg(mul_u(ax0, n[2])));
+        const f2 k2 = add(mul_u(ax0, n[1]), neg(mul_u(ax1, n[0])));
+        dn[0] = add(dn[0], add(mul_u(n[0], cm1), mul_u(k0, sr)));
+        dn[1] = add(dn[1], add(mul_u(n[1], cm1), mul_u(k1, sr)));
+        dn[2] = add(dn[2], add(mul_u(n[2], cm1), mul_u(k2, sr)));
+    }
+    for (int k = 0; k < 3; ++k) o.dp[k] = dp[k];
+    if (st.h >= 0x1p-10f) {
+        const f2 stst = mul(st, st);
+        const f2 nd = add(mul_u(n[0], dn[0]), mul_u(n[1], dn[1]));
+        o.a = atan2_f2(add(mul_u(n[0], dn[1]), neg(mul_u(n[1], dn[0]))), add(stst, nd));
+        // |v_xy| from v's components (st^2 + q cancels when v nears a pole);
+        // its difference from st from q (which does not cancel)
+        const f2 v0 = add(n[0], dn[0]), v1 = add(n[1], dn[1]);
+        const f2 rxy = sqrt_f2(add(mul_u(v0, v0), mul_u(v1, v1)));
+        const f2 q = add(add(nd, nd), add(mul_u(dn[0], dn[0]), mul_u(dn[1], dn[1])));
+        const f2 delta = div_f2(q, add(rxy, st));
+        o.b = atan2_f2(add(mul_u(delta, ct), neg(mul_u(dn[2], st))),
+                       add(mul_u(rxy, st), mul_u(add(ct, dn[2]), ct)));
+        o.direct = false;
+    } else {
+        const f2 v0 = add(n[0], dn[0]), v1 = add(n[1], dn[1]), v2 = add(n[2], dn[2]);
+        o.a = atan2_f2(v1, v0);
+        o.b = atan2_f2(v2, sqrt_f2(add(mul_u(v0, v0), mul_u(v1, v1))));
+        o.direct = true;
+    }
 }
 
 }  // namespace xf

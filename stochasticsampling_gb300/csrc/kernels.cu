@@ -400,6 +400,18 @@ __global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__
 #pragma unroll
         for (int j = 0; j < 9; ++j) row[T_GB + j] = inv[(long long)(12 + j) * nc + c].x;
     }
+    if (FLOW && P.f32x2 && !P.gather) {
+        // the two-float update reads the row as float pairs (hi, lo), one in
+        // each 8 bytes: u, W, E, the diffusion length (k_contract's), and B,
+        // grad B when written here
+        float2 *pr = reinterpret_cast<float2 *>(row);
+        const int last = MAG ? T_GB + 9 : T_DIFF + 1;
+        for (int k = 0; k < last; ++k) {
+            const double v = row[k];
+            const float h = __double2float_rn(v);
+            pr[k] = make_float2(h, __double2float_rn(v - (double)h));
+        }
+    }
 }
 
 // The canonical quasi-2-D step with its increments in two-float arithmetic
@@ -437,6 +449,67 @@ __device__ __forceinline__ void langevin_canon_f2(const DevParams &P, double &px
     pph = ref_modulo((pph + xf::to_double(dph.h)) + xf::to_double(dph.l), kTwoPi);
 }
 
+static_assert(xf::R_U == T_U && xf::R_W01 == T_W01 && xf::R_W02 == T_W02 && xf::R_W12 == T_W12 &&
+                  xf::R_E00 == T_E00 && xf::R_E01 == T_E01 && xf::R_E02 == T_E02 && xf::R_E11 == T_E11 &&
+                  xf::R_E12 == T_E12 && xf::R_E22 == T_E22 && xf::R_DIFF == T_DIFF && xf::R_B == T_B &&
+                  xf::R_GB == T_GB,
+              "the float-pair row has the layout of the double table row");
+
+// The full chain (3-D, and quasi-2-D rows off the canonical state) with its
+// increments in two-float arithmetic (xf::full_increments) from the cell's
+// float-pair row, then the FP64 sums, the periodic wrap and the angle
+// ranges of Particle::pbc / ang_pbc: phi mod 2 pi, theta in [0, pi] (the
+// range atan2 gives the reference's new theta).  Quasi2d: z = 0 and
+// theta = pi/2 afterwards (simulation/mod.rs:365-368).
+template <bool Q2D, int NOISE>
+__device__ __forceinline__ void langevin_full_f2(const DevParams &P, double &px, double &py, double &pz,
+                                                 double &pph, double &pth, const float2 *__restrict__ row,
+                                                 uint32_t pid, const double *__restrict__ noise,
+                                                 const unsigned long long *__restrict__ d_step) {
+    const uint32_t m = P.mask;
+    const xf::FullTerms T = {(m & M_SELF_PROPULSION) != 0u, (m & M_CONVECTION) != 0u, (m & M_MDD_FORCE) != 0u,
+                             (m & M_EXTERNAL_FIELD) != 0u,  (m & M_MDD_ROTATION) != 0u, (m & M_JEFFREY_VORTICITY) != 0u,
+                             (m & M_JEFFREY_STRAIN) != 0u,  (m & M_STEP) != 0u,      (m & M_TRANS_DIFFUSION) != 0u,
+                             (m & M_ROT_DIFFUSION) != 0u};
+    const xf::f2 dt2 = {P.dt2[0], P.dt2[1]}, re2 = {P.reorient_f2[0], P.reorient_f2[1]};
+    const xf::f2 sh2 = {P.shape2[0], P.shape2[1]}, dr2 = {P.drag2[0], P.drag2[1]};
+    xf::FullOut o;
+    if (NOISE == 0) {
+        const NoiseF f = philox_noise_f(P.seed, pid, *d_step);
+        const float xi2 = Q2D ? 0.0f : philox_xi2_f(P.seed, pid, *d_step);
+        const xf::f2 rot = xf::mul_u(xf::f2{P.sigma2[0], P.sigma2[1]}, f.rad);
+        xf::full_increments(pph, pth, row, f.xi0, f.xi1, xi2, f.sa, xf::axis_cos(f.sa, f.ca), rot, T, dt2, re2,
+                            sh2, dr2, o);
+    } else {
+        const double *r = noise + 5ull * pid;
+        double sa, ca;
+        sincos(r[3], &sa, &ca);
+        xf::full_increments(pph, pth, row, xf::split(r[0]), xf::split(r[1]), xf::split(r[2]), xf::split(sa),
+                            xf::split(ca), xf::split(r[4]), T, dt2, re2, sh2, dr2, o);
+    }
+    px = ref_modulo((px + xf::to_double(o.dp[0].h)) + xf::to_double(o.dp[0].l), P.bx);
+    py = ref_modulo((py + xf::to_double(o.dp[1].h)) + xf::to_double(o.dp[1].l), P.by);
+    double nphi, nth;
+    if (!o.direct) {
+        nphi = (pph + xf::to_double(o.a.h)) + xf::to_double(o.a.l);
+        nth = (pth + xf::to_double(o.b.h)) + xf::to_double(o.b.l);
+        // theta in [0, pi], as the reference's pi/2 - atan2(v2, |v_xy|) (compares on the bits)
+        if (dkey(nth) < 0) nth = 0.0;
+        if (dkey(nth) > dkey(kPi)) nth = kPi;
+    } else {
+        nphi = xf::to_double(o.a.h) + xf::to_double(o.a.l);
+        nth = kPiHalf - (xf::to_double(o.b.h) + xf::to_double(o.b.l));
+    }
+    pph = ref_modulo(nphi, kTwoPi);
+    if (Q2D) {
+        pz = 0.0;
+        pth = kPiHalf;
+    } else {
+        pz = ref_modulo((pz + xf::to_double(o.dp[2].h)) + xf::to_double(o.dp[2].l), P.bz);
+        pth = nth;
+    }
+}
+
 // ------------------------------------------------------------------------
 // particle update: the loop of src/bin/simulation/mod.rs:318-369 fused with
 // the next step's binning (histogram_from) so each step reads and writes the
@@ -449,7 +522,7 @@ __device__ __forceinline__ void langevin_canon_f2(const DevParams &P, double &px
 // state in FP64.
 // ------------------------------------------------------------------------
 template <bool Q2D, bool MAG, int NOISE, bool TRI, bool CANON = false, bool F2 = false>
-__global__ void __launch_bounds__(256, (CANON && F2) ? 5 : 1) k_update(DevParams P, double *__restrict__ x, double *__restrict__ y,
+__global__ void __launch_bounds__(256, F2 ? (CANON ? 5 : 3) : 1) k_update(DevParams P, double *__restrict__ x, double *__restrict__ y,
                                                 double *__restrict__ z, double *__restrict__ phi,
                                                 double *__restrict__ theta, uint32_t *__restrict__ key,
                                                 const uint32_t *__restrict__ id, const double *__restrict__ table,
@@ -471,6 +544,9 @@ __global__ void __launch_bounds__(256, (CANON && F2) ? 5 : 1) k_update(DevParams
     }
     if (CANON && F2) {
         langevin_canon_f2<NOISE>(P, px, py, pph, reinterpret_cast<const float4 *>(F.r), pid, noise, d_step);
+    } else if (F2) {
+        langevin_full_f2<Q2D, NOISE>(P, px, py, pz, pph, pth, reinterpret_cast<const float2 *>(F.r), pid, noise,
+                                     d_step);
     } else {
         double xi[3], ca, sa, rot;
         if (NOISE == 0) {
@@ -779,8 +855,17 @@ void launch_update(cudaStream_t s, bool q2d, bool canon, bool mag, bool host_noi
 #define SS_UPD(Q, M, N, T)                                                                                   \
     k_update<Q, M, N, T><<<b, 256, 0, s>>>(P, xs[0], xs[1], xs[2], xs[3], xs[4], key, id, table, noise, d_step, \
                                            counts_next, err)
-#define SS_UPD_T(Q, M, N) \
-    do { if (P.gather) SS_UPD(Q, M, N, true); else SS_UPD(Q, M, N, false); } while (0)
+#define SS_UPD_F2(Q, M, N)                                                                                  \
+    k_update<Q, M, N, false, false, true><<<b, 256, 0, s>>>(P, xs[0], xs[1], xs[2], xs[3], xs[4], key, id, table, \
+                                                            noise, d_step, counts_next, err)
+    // with the two-float mode (nearest-cell gather) every update reads the
+    // float-pair rows k_table wrote
+#define SS_UPD_T(Q, M, N)                   \
+    do {                                    \
+        if (P.gather) SS_UPD(Q, M, N, true); \
+        else if (P.f32x2) SS_UPD_F2(Q, M, N); \
+        else SS_UPD(Q, M, N, false);        \
+    } while (0)
     if (q2d) {
         if (mag) { if (host_noise) SS_UPD_T(true, true, 1); else SS_UPD_T(true, true, 0); }
         else { if (host_noise) SS_UPD_T(true, false, 1); else SS_UPD_T(true, false, 0); }
@@ -789,6 +874,7 @@ void launch_update(cudaStream_t s, bool q2d, bool canon, bool mag, bool host_noi
         else { if (host_noise) SS_UPD_T(false, false, 1); else SS_UPD_T(false, false, 0); }
     }
 #undef SS_UPD_T
+#undef SS_UPD_F2
 #undef SS_UPD
 }
 

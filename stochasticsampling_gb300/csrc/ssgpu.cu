@@ -621,9 +621,9 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     P.dthph = P.gw[4] * P.gw[3];
     P.sigma_rot = std::sqrt(2. * params->rot_diffusion * params->timestep);
     {  // float pairs (hi, lo) of the constants of the two-float chain
-        const double v[3] = {P.dt, P.reorient_dt, P.sigma_rot};
-        float *out[3] = {P.dt2, P.reorient2, P.sigma2};
-        for (int k = 0; k < 3; ++k) {
+        const double v[6] = {P.dt, P.reorient_dt, P.sigma_rot, P.reorient, P.shape, P.drag};
+        float *out[6] = {P.dt2, P.reorient2, P.sigma2, P.reorient_f2, P.shape2, P.drag2};
+        for (int k = 0; k < 6; ++k) {
             out[k][0] = (float)v[k];
             out[k][1] = (float)(v[k] - (double)out[k][0]);
         }

@@ -80,3 +80,43 @@ void xf_canon(int n, const double *phi, const float *ct, const float *xi, const 
     }
 }
 }
+
+// The full chain.  terms: bits 0..9 = self propulsion, convection, dipolar
+// force, external field, dipolar rotation, vorticity, strain, step,
+// translational diffusion, rotational diffusion; bit 10: the noise as
+// floats (xi h, sa h, ca from axis_cos(sa h, ca h)), else as pairs.
+// row: 32 pairs a particle; xi: 3 pairs; sa, ca, rot: pairs; prm: dt,
+// reorient, shape, drag as pairs.  out: dp (3 pairs), a, b (pairs), direct.
+extern "C" void xf_full(int n, const double *phi, const double *theta, const float *row, const float *xi,
+                        const float *sa, const float *ca, const float *rot, unsigned terms, const float *prm,
+                        double *out) {
+    FullTerms T;
+    T.self_propulsion = terms & 1u;
+    T.convection = terms & 2u;
+    T.mdd_force = terms & 4u;
+    T.external_field = terms & 8u;
+    T.mdd_rotation = terms & 16u;
+    T.vorticity = terms & 32u;
+    T.strain = terms & 64u;
+    T.step = terms & 128u;
+    T.trans_diffusion = terms & 256u;
+    T.rot_diffusion = terms & 512u;
+    const f2 dt = {prm[0], prm[1]}, re = {prm[2], prm[3]}, sh = {prm[4], prm[5]}, dr = {prm[6], prm[7]};
+    for (int i = 0; i < n; ++i) {
+        const float2 *r = reinterpret_cast<const float2 *>(row + 64 * i);
+        const float *x = xi + 6 * i;
+        const f2 ro = {rot[2 * i], rot[2 * i + 1]};
+        FullOut o;
+        if (terms & 1024u)
+            full_increments(phi[i], theta[i], r, x[0], x[2], x[4], sa[2 * i], axis_cos(sa[2 * i], ca[2 * i]), ro, T,
+                            dt, re, sh, dr, o);
+        else
+            full_increments(phi[i], theta[i], r, f2{x[0], x[1]}, f2{x[2], x[3]}, f2{x[4], x[5]},
+                            f2{sa[2 * i], sa[2 * i + 1]}, f2{ca[2 * i], ca[2 * i + 1]}, ro, T, dt, re, sh, dr, o);
+        double *d = out + 11 * i;
+        for (int k = 0; k < 3; ++k) put(d + 2 * k, o.dp[k]);
+        put(d + 6, o.a);
+        put(d + 8, o.b);
+        d[10] = o.direct ? 1.0 : 0.0;
+    }
+}

@@ -223,3 +223,145 @@ def test_canonical_increments(lib, terms):
         # and the 1e-12 bar of the step
         assert np.all(err <= 2.0 ** -45 * np.maximum(np.abs(e), 0.01)), (k, float(err.max()))
         assert float(err.max()) < (1.5e-15, 1.5e-15, 8e-15)[k], (k, float(err.max()))
+
+
+# ---------------------------------------------------------------- full chain
+FULL = dict(sp=1, conv=2, mdd_force=4, ext=8, mdd_rot=16, vort=32, strain=64, step=128, trans=256, rot=512,
+            float_noise=1024)
+FULL_ALL = sum(v for k, v in FULL.items() if k != "float_noise")
+
+
+def _full_inputs(rng, n, theta=None):
+    phi = rng.random(n) * 2 * np.pi
+    theta = np.arccos(1 - 2 * rng.random(n)) if theta is None else theta
+    vals = np.zeros((n, 32))
+    vals[:, 0:3] = rng.normal(size=(n, 3)) * 0.5          # u
+    vals[:, 3:6] = rng.normal(size=(n, 3)) * 0.3          # W01 W02 W12
+    vals[:, 6:12] = rng.normal(size=(n, 6)) * 0.3         # E
+    vals[:, 12] = np.sqrt(2 * 0.002 * 0.1)                # diffusion length
+    vals[:, 13:16] = rng.normal(size=(n, 3)) * 0.5        # B
+    vals[:, 16:25] = rng.normal(size=(n, 9)) * 0.5        # grad B
+    row = np.zeros((n, 32, 2), np.float32)
+    for k in range(25):
+        row[:, k] = rand_pairs(rng, vals[:, k])
+    xi = np.concatenate([rand_pairs(rng, rng.normal(size=n)) for _ in range(3)], axis=1)
+    alpha = rng.random(n) * 2 * np.pi
+    sa, ca = rand_pairs(rng, np.sin(alpha)), rand_pairs(rng, np.cos(alpha))
+    rot = rand_pairs(rng, 0.063 * np.sqrt(-2 * np.log(1 - rng.random(n))))  # sigma = sqrt(2 Dr dt), Dr 1, dt 0.002
+    prm = np.concatenate([rand_pairs(rng, np.array([v]))[0] for v in (0.002, 1.0, 0.6, 0.2)])
+    return phi, theta, row, xi, sa, ca, rot, prm
+
+
+def _full_exact(phi, theta, row, xi, sa, ca, rot, prm, terms):
+    """langevin<> (the FP64 chain) in extended precision from the same inputs:
+    the new position increments and angles"""
+    f = val(row.reshape(len(phi), 32, 2))
+    cp, sp, ct, st = np.cos(phi.astype(LD)), np.sin(phi.astype(LD)), np.cos(theta.astype(LD)), np.sin(theta.astype(LD))
+    n = [st * cp, st * sp, ct]
+    if terms & FULL["float_noise"]:
+        x = [xi[:, 2 * k].astype(LD) for k in range(3)]
+        s_a = sa[:, 0].astype(LD)
+        c_a = np.copysign(np.sqrt(1 - s_a * s_a), ca[:, 0].astype(LD))
+    else:
+        x = [val(xi[:, 2 * k:2 * k + 2]) for k in range(3)]
+        s_a, c_a = val(sa), val(ca)
+    dt, re, sh, dr = (val(prm[2 * k:2 * k + 2]) for k in range(4))
+    r = val(rot)
+    z = np.zeros_like(cp)
+    dp, dn = [z.copy(), z.copy(), z.copy()], [z.copy(), z.copy(), z.copy()]
+    if terms & FULL["sp"]:
+        dp = [n[0].copy(), n[1].copy(), n[2].copy()]
+    if terms & FULL["conv"]:
+        dp = [dp[k] + f[:, k] for k in range(3)]
+    if terms & FULL["mdd_force"]:
+        g = f[:, 16:25]
+        dp = [dp[a] + (g[:, 3 * a] * n[0] + g[:, 3 * a + 1] * n[1] + g[:, 3 * a + 2] * n[2]) * dr for a in range(3)]
+    if terms & FULL["ext"]:
+        d = n[1] * re
+        dn = [dn[0] - n[0] * d, dn[1] + (re - n[1] * d), dn[2] - n[2] * d]
+    if terms & FULL["mdd_rot"]:
+        b = [f[:, 13 + k] for k in range(3)]
+        d = n[0] * b[0] + n[1] * b[1] + n[2] * b[2]
+        dn = [dn[k] + (b[k] - n[k] * d) for k in range(3)]
+    if terms & FULL["vort"]:
+        w01, w02, w12 = f[:, 3], f[:, 4], f[:, 5]
+        fv = [w01 * n[1] + w02 * n[2], -w01 * n[0] + w12 * n[2], -w02 * n[0] - w12 * n[1]]
+        dn = [dn[k] - fv[k] for k in range(3)]
+    if terms & FULL["strain"]:
+        e00, e01, e02, e11, e12, e22 = (f[:, 6 + k] for k in range(6))
+        fs = [(e00 * n[0] + e01 * n[1] + e02 * n[2]) * sh, (e01 * n[0] + e11 * n[1] + e12 * n[2]) * sh,
+              (e02 * n[0] + e12 * n[1] + e22 * n[2]) * sh]
+        fn = fs[0] * n[0] + fs[1] * n[1] + fs[2] * n[2]
+        dn = [dn[k] + (fs[k] - n[k] * fn) for k in range(3)]
+    if terms & FULL["step"]:
+        dp = [v * dt for v in dp]
+        dn = [v * dt for v in dn]
+    if terms & FULL["trans"]:
+        dp = [dp[k] + x[k] * f[:, 12] for k in range(3)]
+    if terms & FULL["rot"]:
+        ax = [cp * ct * s_a - c_a * sp, c_a * cp + ct * s_a * sp, -s_a * st]
+        kx = [ax[1] * n[2] - ax[2] * n[1], ax[2] * n[0] - ax[0] * n[2], ax[0] * n[1] - ax[1] * n[0]]
+        dn = [dn[k] + n[k] * (np.cos(r) - 1) + kx[k] * np.sin(r) for k in range(3)]
+    v = [n[k] + dn[k] for k in range(3)]
+    nphi = np.arctan2(v[1], v[0])
+    nth = LD(np.pi) / 2 - np.arctan2(v[2], np.sqrt(v[0] ** 2 + v[1] ** 2))
+    return dp, nphi, nth
+
+
+def _run_full(lib, inputs, terms):
+    phi, theta, row, xi, sa, ca, rot, prm = inputs
+    n = len(phi)
+    out = np.empty(11 * n)
+    lib.xf_full(n, _p(phi), _p(theta), _p(row), _p(xi), _p(sa), _p(ca), _p(rot), ctypes.c_uint(terms), _p(prm),
+                _p(out))
+    return out.reshape(n, 11)
+
+
+def _wrap(a):
+    """angle difference brought to (-pi, pi]"""
+    return (a + LD(np.pi)) % (2 * LD(np.pi)) - LD(np.pi)
+
+
+@pytest.mark.parametrize("terms", [
+    FULL_ALL,
+    FULL_ALL | FULL["float_noise"],
+    FULL["sp"] | FULL["conv"] | FULL["ext"] | FULL["mdd_rot"] | FULL["vort"] | FULL["step"] | FULL["trans"]
+    | FULL["rot"] | FULL["float_noise"],
+    FULL["step"] | FULL["rot"],
+    FULL["sp"] | FULL["step"],
+], ids=["all_terms", "all_terms_device_noise", "c2_terms", "rotation_only", "no_rotation"])
+def test_full_chain(lib, terms):
+    rng = np.random.default_rng(terms)
+    inputs = _full_inputs(rng, 20000)
+    phi, theta = inputs[0], inputs[1]
+    out = _run_full(lib, inputs, terms)
+    dp, nphi, nth = _full_exact(*inputs, terms)
+    for k in range(3):
+        err = np.abs(val(out[:, 2 * k:2 * k + 2]) - dp[k])
+        assert float(err.max()) < 2e-18 + 2.0 ** -45 * float(np.abs(dp[k]).max()), (k, float(err.max()))
+    inc = out[:, 10] == 0
+    gphi = np.where(inc, phi.astype(LD) + val(out[:, 6:8]), val(out[:, 6:8]))
+    gth = np.where(inc, theta.astype(LD) + val(out[:, 8:10]), LD(np.pi) / 2 - val(out[:, 8:10]))
+    # errors on the sphere: phi's times sin theta (phi is ill-conditioned near a
+    # pole in any arithmetic), theta's as they are; the increments carry a few
+    # 2^-48 of the orientation change, the direct angles near a pole 2^-46 of pi
+    ephi, eth = np.abs(_wrap(gphi - nphi)) * np.sin(nth), np.abs(gth - nth)
+    assert float(ephi[inc].max()) < 1e-14 and float(eth[inc].max()) < 1e-14, (float(ephi[inc].max()),
+                                                                              float(eth[inc].max()))
+    if np.any(~inc):
+        assert float(ephi[~inc].max()) < 6e-14 and float(eth[~inc].max()) < 6e-14
+
+
+def test_full_chain_near_and_at_the_poles(lib):
+    rng = np.random.default_rng(7)
+    theta = np.concatenate([np.zeros(50), np.full(50, np.pi), rng.random(400) * 2e-3,
+                            np.pi - rng.random(400) * 2e-3])
+    inputs = _full_inputs(rng, len(theta), theta=theta)
+    out = _run_full(lib, inputs, FULL_ALL)
+    dp, nphi, nth = _full_exact(*inputs, FULL_ALL)
+    inc = out[:, 10] == 0
+    assert np.any(inc) and np.any(~inc)
+    gphi = np.where(inc, inputs[0].astype(LD) + val(out[:, 6:8]), val(out[:, 6:8]))
+    gth = np.where(inc, inputs[1].astype(LD) + val(out[:, 8:10]), LD(np.pi) / 2 - val(out[:, 8:10]))
+    assert float((np.abs(_wrap(gphi - nphi)) * np.sin(nth)).max()) < 6e-14
+    assert float(np.abs(gth - nth).max()) < 6e-14
