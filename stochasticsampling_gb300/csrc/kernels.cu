@@ -353,6 +353,17 @@ __global__ void k_kspace(const double2 *__restrict__ fwd, double2 *__restrict__ 
 // per-cell table: W = (G - G^T) * 0.5, E = (G + G^T) * 0.5 on real parts
 // (simulation/mod.rs:302-308), Re u, Re B * mdd, Re grad B (:323-339)
 // ------------------------------------------------------------------------
+// A table entry: a double, or (with the two-float update) the float pair
+// (hi, lo) of that double in the same 8 bytes.
+__device__ __forceinline__ void put_entry(double *row, int k, double v, bool pairs) {
+    if (pairs) {
+        const float h = __double2float_rn(v);
+        reinterpret_cast<float2 *>(row)[k] = make_float2(h, __double2float_rn(v - (double)h));
+    } else {
+        row[k] = v;
+    }
+}
+
 template <bool FLOW, bool MAG>
 __global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__restrict__ table, int tstride,
                         double *__restrict__ ctab) {
@@ -360,34 +371,39 @@ __global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__
     const int nc = P.ncell;
     if (c >= nc) return;
     double *row = table + (long long)c * tstride;
+    // the two-float update (nearest-cell gather) reads the row as float
+    // pairs: u, W, E, the diffusion length (k_contract's, converted here)
+    // and B, grad B; the flow solve runs every step, so FLOW marks a full row
+    const bool pairs = FLOW && P.f32x2 && !P.gather;
     if (FLOW) {
-        double g[9];
+        double g[9], u[3];
 #pragma unroll
         for (int j = 0; j < 9; ++j) g[j] = inv[(long long)j * nc + c].x;
 #pragma unroll
-        for (int r = 0; r < 3; ++r) row[T_U + r] = inv[(long long)(9 + r) * nc + c].x;
-        row[T_W01] = (g[1] - g[3]) * 0.5;
-        row[T_W02] = (g[2] - g[6]) * 0.5;
-        row[T_W12] = (g[5] - g[7]) * 0.5;
-        row[T_E00] = (g[0] + g[0]) * 0.5;
-        row[T_E01] = (g[1] + g[3]) * 0.5;
-        row[T_E02] = (g[2] + g[6]) * 0.5;
-        row[T_E11] = (g[4] + g[4]) * 0.5;
-        row[T_E12] = (g[5] + g[7]) * 0.5;
-        row[T_E22] = (g[8] + g[8]) * 0.5;
+        for (int r = 0; r < 3; ++r) u[r] = inv[(long long)(9 + r) * nc + c].x;
+        const double w01 = (g[1] - g[3]) * 0.5, w02 = (g[2] - g[6]) * 0.5, w12 = (g[5] - g[7]) * 0.5;
+        const double e00 = (g[0] + g[0]) * 0.5, e01 = (g[1] + g[3]) * 0.5, e02 = (g[2] + g[6]) * 0.5;
+        const double e11 = (g[4] + g[4]) * 0.5, e12 = (g[5] + g[7]) * 0.5, e22 = (g[8] + g[8]) * 0.5;
+        const double diff = row[T_DIFF];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) put_entry(row, T_U + r, u[r], pairs);
+        put_entry(row, T_W01, w01, pairs);
+        put_entry(row, T_W02, w02, pairs);
+        put_entry(row, T_W12, w12, pairs);
+        put_entry(row, T_E00, e00, pairs);
+        put_entry(row, T_E01, e01, pairs);
+        put_entry(row, T_E02, e02, pairs);
+        put_entry(row, T_E11, e11, pairs);
+        put_entry(row, T_E12, e12, pairs);
+        put_entry(row, T_E22, e22, pairs);
+        if (pairs) put_entry(row, T_DIFF, diff, true);
         if (ctab) {  // the canonical quasi-2-D chain's row (CT_*), pre-multiplied by dt
-            const double v[CTAB_STRIDE] = {row[T_U] * P.dt, row[T_U + 1] * P.dt, row[T_W01] * P.dt,
-                                           row[T_E00] * P.shape_dt, row[T_E01] * P.shape_dt,
-                                           row[T_E11] * P.shape_dt, row[T_DIFF], 0.0};
+            const double v[CTAB_STRIDE] = {u[0] * P.dt, u[1] * P.dt, w01 * P.dt, e00 * P.shape_dt,
+                                           e01 * P.shape_dt, e11 * P.shape_dt, diff, 0.0};
             double *cr = ctab + (long long)c * CTAB_STRIDE;
             if (P.f32x2) {  // the same row as float pairs (hi, lo) in the same 64 bytes
-                float *cf = reinterpret_cast<float *>(cr);
 #pragma unroll
-                for (int k = 0; k < CTAB_STRIDE; ++k) {
-                    const float h = __double2float_rn(v[k]);
-                    cf[2 * k] = h;
-                    cf[2 * k + 1] = __double2float_rn(v[k] - (double)h);
-                }
+                for (int k = 0; k < CTAB_STRIDE; ++k) put_entry(cr, k, v[k], true);
             } else {
 #pragma unroll
                 for (int k = 0; k < CTAB_STRIDE; ++k) cr[k] = v[k];
@@ -396,21 +412,9 @@ __global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__
     }
     if (MAG) {
 #pragma unroll
-        for (int r = 0; r < 3; ++r) row[T_B + r] = inv[(long long)(21 + r) * nc + c].x * P.mdd;
+        for (int r = 0; r < 3; ++r) put_entry(row, T_B + r, inv[(long long)(21 + r) * nc + c].x * P.mdd, pairs);
 #pragma unroll
-        for (int j = 0; j < 9; ++j) row[T_GB + j] = inv[(long long)(12 + j) * nc + c].x;
-    }
-    if (FLOW && P.f32x2 && !P.gather) {
-        // the two-float update reads the row as float pairs (hi, lo), one in
-        // each 8 bytes: u, W, E, the diffusion length (k_contract's), and B,
-        // grad B when written here
-        float2 *pr = reinterpret_cast<float2 *>(row);
-        const int last = MAG ? T_GB + 9 : T_DIFF + 1;
-        for (int k = 0; k < last; ++k) {
-            const double v = row[k];
-            const float h = __double2float_rn(v);
-            pr[k] = make_float2(h, __double2float_rn(v - (double)h));
-        }
+        for (int j = 0; j < 9; ++j) put_entry(row, T_GB + j, inv[(long long)(12 + j) * nc + c].x, pairs);
     }
 }
 
