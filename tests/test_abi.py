@@ -62,6 +62,13 @@ def test_invalid_arguments_are_rejected_on_the_host():
     rc = L.ss_create(ctypes.byref(Grid(4, 4, 1, 4, 1)), ctypes.byref(Box(1, 1, 1)), ctypes.byref(bad), 0, None,
                      ctypes.byref(h))
     assert rc == _lib.SS_ERR_INVALID_ARGUMENT
+    # flag combinations the FP64 mode alone supports
+    for fl, what in ((_lib.FLAG_MIXED | _lib.FLAG_F32X2, "F32X2"), (_lib.FLAG_FIXED64 | _lib.FLAG_F32X2, "F32X2"),
+                     (_lib.FLAG_MIXED | _lib.FLAG_TRILINEAR, "trilinear")):
+        h = ctypes.c_void_p()
+        rc = L.ss_create(ctypes.byref(Grid(4, 4, 1, 4, 1)), ctypes.byref(Box(1, 1, 1)), ctypes.byref(p),
+                         _lib.FLAG_QUASI2D | fl, None, ctypes.byref(h))
+        assert rc == _lib.SS_ERR_INVALID_ARGUMENT and what in _lib.last_error() and not h.value
     # null context
     assert L.ss_do_timestep(None, None, None) == _lib.SS_ERR_INVALID_ARGUMENT
 
