@@ -120,3 +120,19 @@ extern "C" void xf_full(int n, const double *phi, const double *theta, const flo
         d[10] = o.direct ? 1.0 : 0.0;
     }
 }
+
+// the pair helpers of the full chain: op 0 sqrt_f2(a), 1 div_f2(a, b),
+// 2 sin_cosm1_f2(a) (two pairs out), 3 axis_cos(a.h, b.h); a, b: pairs,
+// out: 4 doubles a row
+extern "C" void xf_helpers(int n, int op, const float *a, const float *b, double *out) {
+    for (int i = 0; i < n; ++i) {
+        const f2 x = {a[2 * i], a[2 * i + 1]}, y = {b[2 * i], b[2 * i + 1]};
+        f2 r0 = {0.0f, 0.0f}, r1 = {0.0f, 0.0f};
+        if (op == 0) r0 = sqrt_f2(x);
+        else if (op == 1) r0 = div_f2(x, y);
+        else if (op == 2) sin_cosm1_f2(x, r0, r1);
+        else r0 = axis_cos(x.h, y.h);
+        put(out + 4 * i, r0);
+        put(out + 4 * i + 2, r1);
+    }
+}

@@ -28,7 +28,8 @@ def lib(tmp_path_factory):
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", "-I", CSRC,
                     os.path.join(HERE, "f32x2_host.cpp"), "-o", str(out)], check=True)
     L = ctypes.CDLL(str(out))
-    for name in ("xf_split", "xf_to_double", "xf_sincos_d", "xf_sincos_f2", "xf_atan2", "xf_canon"):
+    for name in ("xf_split", "xf_to_double", "xf_sincos_d", "xf_sincos_f2", "xf_atan2", "xf_canon", "xf_full",
+                 "xf_helpers"):
         getattr(L, name).restype = None
     return L
 
@@ -365,3 +366,52 @@ def test_full_chain_near_and_at_the_poles(lib):
     gth = np.where(inc, inputs[1].astype(LD) + val(out[:, 8:10]), LD(np.pi) / 2 - val(out[:, 8:10]))
     assert float((np.abs(_wrap(gphi - nphi)) * np.sin(nth)).max()) < 6e-14
     assert float(np.abs(gth - nth).max()) < 6e-14
+
+
+def _helpers(lib, op, a, b=None):
+    b = a if b is None else b
+    out = np.empty(4 * len(a))
+    lib.xf_helpers(len(a), op, _p(a), _p(b), _p(out))
+    return out.reshape(-1, 4)
+
+
+def test_pair_sqrt_and_quotient(lib):
+    rng = np.random.default_rng(8)
+    x = rand_pairs(rng, np.concatenate([rng.random(20000) * 4, 10.0 ** rng.uniform(-20, 20, 2000)]))
+    r = val(_helpers(lib, 0, x)[:, 0:2])
+    assert np.all(np.abs(r - np.sqrt(val(x))) <= 2.0 ** -45 * np.sqrt(val(x)))
+    assert np.all(_helpers(lib, 0, np.zeros((3, 2), np.float32))[:, 0:2] == 0)
+    y = rand_pairs(rng, 0.1 + rng.random(len(x)) * 3)
+    q = val(_helpers(lib, 1, x, y)[:, 0:2])
+    exact = val(x) / val(y)
+    assert np.all(np.abs(q - exact) <= 2.0 ** -45 * np.abs(exact))
+
+
+def test_pair_sin_and_cos_minus_one(lib):
+    rng = np.random.default_rng(9)
+    r = rand_pairs(rng, np.concatenate([np.abs(rng.normal(size=20000)) * 0.1, rng.random(2000) * 6.2,
+                                        [0.0, 1e-8, 1 / 512.0]]))
+    o = _helpers(lib, 2, r)
+    rl = val(r)
+    es = np.abs(val(o[:, 0:2]) - np.sin(rl))
+    # cos r - 1 without cancellation: within the table pair's own 2^-49 of C_j plus 2^-47 of the value
+    ec = np.abs(val(o[:, 2:4]) - (np.cos(rl) - 1))
+    assert float(es.max()) < 2.0 ** -46
+    assert np.all(ec <= 2.0 ** -48 + 2.0 ** -46 * np.abs(np.cos(rl) - 1)), float(ec.max())
+    far = rand_pairs(rng, np.array([6.3, 9.0]))
+    of = _helpers(lib, 2, far)
+    assert np.all(np.abs(val(of[:, 2:4]) - (np.cos(val(far)) - 1)) < 1e-15)
+
+
+def test_axis_cosine_is_the_unit_complement_of_the_sine(lib):
+    """sqrt(1 - sa^2) with the sign of the FP32 cosine, as the on-device noise
+    defines the rotation axis"""
+    rng = np.random.default_rng(10)
+    ang = rng.random(20000) * 2 * np.pi
+    sa = np.stack([np.sin(ang).astype(np.float32), np.zeros(len(ang), np.float32)], axis=-1)
+    ca = np.stack([np.cos(ang).astype(np.float32), np.zeros(len(ang), np.float32)], axis=-1)
+    o = val(_helpers(lib, 3, sa, ca)[:, 0:2])
+    s = sa[:, 0].astype(LD)
+    exact = np.copysign(np.sqrt(1 - s * s), ca[:, 0].astype(LD))
+    assert np.all(np.abs(o - exact) <= 2.0 ** -45)
+    assert np.all(np.signbit(o.astype(np.float64)) == np.signbit(ca[:, 0]))
