@@ -49,7 +49,16 @@ def geometry_from_settings(settings):
 
 
 class Simulation:
-    """One simulation on the current CUDA device."""
+    """One simulation on the current CUDA device.
+
+    Keyword flags of ``ss_create``: ``quasi2d`` (the cargo feature),
+    ``sort=False`` (no counting sort by cell), ``graph=False`` (direct
+    launches), ``always_magnetic`` (the dipolar solve every step),
+    ``mixed`` (True: FP32 with FP64 positions, "fixed64": FP32 with 64-bit
+    fixed-point positions), ``gather`` ("nearest", "trilinear",
+    "trilinear_zfromy"), ``f32x2`` (FP64 state with each step's increments in
+    two-float arithmetic, within 1e-14 of the FP64 step; FP64 mode and
+    nearest-cell gather only)."""
 
     def __init__(self, settings=None, *, grid=None, box=None, params=None, quasi2d=False, sort=True, graph=True,
                  always_magnetic=False, mixed=False, gather="nearest", f32x2=False, stream=None):
