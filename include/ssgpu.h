@@ -221,27 +221,35 @@ int ss_fp64_rate(double *fma_per_second);
  * allocation.  This entry point has no counterpart in the reference.
  *
  * It is for callers that cannot call cudaMalloc or cudaFree where they need
- * the histogram: code running while a stream is captured into a CUDA graph,
- * a hook inside another library's loop where the device-wide synchronisation
- * of cudaFree would stall or deadlock it, or an application that reserves a
- * fixed device-memory budget at start-up.  It gives the same result as
- * ss_init + ss_get_distribution on a context, without creating one:
+ * the histogram: a hook inside another library's loop, where the device-wide
+ * synchronisation of cudaFree would stall or deadlock that loop, or an
+ * application that reserves a fixed device-memory budget at start-up and may
+ * not grow it.  It gives the same result as ss_init + ss_get_distribution on
+ * a context, without creating one:
  * dist[b] = (count_b / (gw_x gw_y gw_z gw_phi gw_theta n)) * (L_x L_y L_z),
  * after applying Particle::new (src/particle.rs:186-201) to every row.
  *
- *   particles: DEVICE pointer, [n][5] doubles (x, y, z, phi, theta), finite
+ *   particles: DEVICE pointer, [n][5] doubles (x, y, z, phi, theta),
+ *              1 <= n <= 2^32 - 1 (the limit of ss_create)
  *   dist:      DEVICE pointer, [x][y][z][phi][theta] doubles, written in full
  *   stream:    cudaStream_t to run on (NULL: the legacy default stream)
  *
+ * Rows must be finite.  ss_init refuses a non-finite row on the host; here
+ * the rows are only seen on the device, so such a row is not counted and
+ * every bin of dist is written as NaN instead, which the caller finds in the
+ * result when it reads it.
+ *
  * Scratch: one file-scope device array of SS_NOALLOC_MAX_BINS u32 counts
- * (8 MiB), which every GPU that loads this library holds until the process
- * exits.  Grids with more bins are rejected (SS_ERR_INVALID_ARGUMENT).  Every
- * call shares that array and clears it first, so calls whose kernels overlap
- * on the GPU (two streams, two threads) race and corrupt each other's counts:
- * order them on one stream.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress, with that device current); make that
- * first call before any stream capture.  The call is asynchronous: it only
- * enqueues kernels.  Errors are reported by ss_last_error(NULL, ...). */
+ * plus an error word (8 MiB), which every GPU that loads this library holds
+ * until the process exits.  Grids with more bins are rejected
+ * (SS_ERR_INVALID_ARGUMENT).  Every call shares that array and clears it
+ * first, so calls whose kernels overlap on the GPU (two streams, two threads)
+ * race and corrupt each other's counts: order them on one stream.  The first
+ * call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current) and the device's
+ * multiprocessor count; make that first call before any stream capture.  The
+ * call is asynchronous: it only enqueues kernels.  Errors are reported by
+ * ss_last_error(NULL, ...). */
 #define SS_NOALLOC_MAX_BINS 2097152u
 int ss_sample_distribution_noalloc(const ss_grid *grid, const ss_box *box, const double *particles, uint64_t n,
                                    double *dist, void *stream);

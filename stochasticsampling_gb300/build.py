@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libssgpu.so")
-SOURCES = ["kernels.cu", "ssgpu.cu", "noalloc.cu", "mixed.cu", "ensemble.cu", "denoiser.cu"]
+SOURCES = ["kernels.cu", "contract.cu", "ssgpu.cu", "noalloc.cu", "mixed.cu", "ensemble.cu", "denoiser.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 

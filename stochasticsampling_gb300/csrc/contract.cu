@@ -1,0 +1,447 @@
+// contract.cu -- the angular contraction of the histogram for the FP64 and the
+// FP32 mixed paths: average_stress (src/flowfield/stress.rs:60-96),
+// DirectorField::from_distribution (src/polarization/director.rs:36-61) and
+// the density of src/bin/simulation/mod.rs:312-316.
+//
+// A block takes kCTile consecutive cells, one thread per cell.  Their counts
+// are contiguous in HBM ([cell][phi][theta]); the block stages them, up to
+// kAngChunk angles of every cell at a time, into shared memory with coalesced
+// loads (16 bytes wide where the rows allow it), each row padded to an odd
+// stride so that thread t reading angle a of its own cell hits bank
+// (t * stride + a) mod 32 -- 32 different banks.  Thread t then runs over its
+// cell's angles in order while the angle kernels of the chunk are broadcast
+// from shared memory (every thread reads the same angle at the same time).
+// The histogram is read once, coalesced.
+//
+// FP64 path.  GB300 executes FP64 at 1/64 of the FP32 rate, so the products
+// K_j(a) * f(count) are not formed in FP64.  At set-up every kernel component
+// is split into four signed 12-bit integer slices relative to its largest
+// magnitude (kernel_slices, host side):
+//     K_j(a) = 2^(E_j - 48) * (m_j1(a) 2^36 + m_j2(a) 2^24 + m_j3(a) 2^12 + m_j4(a))
+// up to 2^-49 max_a |K_j(a)|.  While a cell holds at most 2^12 particles,
+// every product m * count and every partial sum over the cell's angles is an
+// integer of magnitude at most 2^24, exact in FP32.  The four slice sums
+// combine exactly in a 64-bit integer; one conversion and one multiplication
+// by 2^(E_j - 48) * measure * V / D give the component in FP64.  A cell with
+// more particles runs the FP64 loop instead.  The result differs from the
+// reference's sum of K_j(a) * ((count / D) * V) by a few ulps.
+//
+// FP32 path.  Products K_j(a) * count in FP32, scaled once by
+// measure * V / D (or by the denoised distribution's scale).  The
+// per-component sums that the mean handling needs are formed in a fixed
+// order -- float-pair warp sums, block sums in FP64 in warp order, and the
+// last block to finish adds the blocks' sums in block order -- so they are
+// the same bit for bit from run to run.
+#include "kernels.cuh"
+#include "mixed.cuh"
+
+#include <cmath>
+
+namespace ss {
+
+namespace {
+
+constexpr int kCTile = 128;     // cells (= threads) per block
+constexpr int kAngChunk = 128;  // angles of every cell staged at a time
+constexpr int kSliceW = 48;     // floats per angle of the FP64 path's slice table: 12 components x 4 slices
+constexpr uint32_t kExactCells = 4096;  // particles per cell below which the FP32 slice sums are exact
+
+struct Staging {
+    int na;      // angles per cell
+    int stride;  // padded row stride of the staged counts (odd)
+    int qshift;  // log2(na / 4) when the rows are read 16 bytes wide and na / 4 is a power of two, else -1
+};
+
+// counts (or FP32 distribution bits) of rows r < tc, angles a0 .. a0 + ach,
+// from src = base of row 0, into tile[r * stride + a - a0]
+__device__ __forceinline__ void stage_rows(const uint32_t *__restrict__ src, const Staging &S, int a0, int ach,
+                                           int tc, uint32_t *__restrict__ tile) {
+    const int tid = threadIdx.x;
+    if (ach == S.na && (S.na & 3) == 0) {
+        // the tile is tc * na contiguous words, 16-byte aligned (cell0 * na * 4 is a multiple of 16)
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+        const int qpr = S.na >> 2, nq = tc * qpr;
+#pragma unroll 8
+        for (int q = tid; q < nq; q += kCTile) {
+            const uint4 v = __ldg(s4 + q);
+            const int r = S.qshift >= 0 ? (q >> S.qshift) : q / qpr;
+            uint32_t *d = tile + r * S.stride + ((q - r * qpr) << 2);
+            d[0] = v.x;
+            d[1] = v.y;
+            d[2] = v.z;
+            d[3] = v.w;
+        }
+    } else {
+        const int nw = tc * ach;
+        for (int i = tid; i < nw; i += kCTile) {
+            const int r = i / ach, a = i - r * ach;
+            tile[r * S.stride + a] = __ldg(src + (long long)r * S.na + a0 + a);
+        }
+    }
+}
+
+// a float pair (hi, lo) summed over the warp by error-free transformations;
+// every lane ends with the same pair, returned as hi + lo in FP64
+__device__ __forceinline__ double warp_pair_sum(float v) {
+    float hi = v, lo = 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_xor_sync(0xffffffffu, hi, o), l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+        const float s = hi + h2, bb = s - hi;
+        const float e = (hi - (s - bb)) + (h2 - bb);  // (hi + h2) - s exactly (Knuth's two-sum)
+        lo = (lo + l2) + e;
+        hi = s;
+    }
+    return (double)hi + (double)lo;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 path
+// ---------------------------------------------------------------------------
+template <bool STRESS, bool MAG>
+__global__ void __launch_bounds__(kCTile) k_contract_x(const uint32_t *__restrict__ counts,
+                                                       const float *__restrict__ kslice,
+                                                       const double *__restrict__ factor,
+                                                       const double *__restrict__ kern,
+                                                       const double *__restrict__ lut, int lut_n, DevParams P,
+                                                       Staging S, double2 *__restrict__ fwd,
+                                                       double *__restrict__ table, int tstride,
+                                                       uint32_t *__restrict__ cellcount) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int na = S.na;
+    float *ks = reinterpret_cast<float *>(smem);  // [chunk angle][48]
+    uint32_t *tile = reinterpret_cast<uint32_t *>(ks + (na < kAngChunk ? na : kAngChunk) * kSliceW);
+    const int tid = threadIdx.x, cell0 = blockIdx.x * kCTile;
+    const int tc = min(kCTile, P.ncell - cell0);
+    const bool live = tid < tc;
+    const int cell = cell0 + tid;
+    float acc[48];
+#pragma unroll
+    for (int j = 0; j < 48; ++j) acc[j] = 0.f;
+    uint32_t csum = 0;
+    const uint32_t *src = counts + (long long)cell0 * na;
+    for (int a0 = 0; a0 < na; a0 += kAngChunk) {
+        const int ach = min(kAngChunk, na - a0);
+        __syncthreads();  // the previous chunk is consumed
+        {
+            const float4 *g = reinterpret_cast<const float4 *>(kslice + (long long)a0 * kSliceW);
+            float4 *d = reinterpret_cast<float4 *>(ks);
+            for (int i = tid; i < ach * (kSliceW / 4); i += kCTile) d[i] = __ldg(g + i);
+        }
+        stage_rows(src, S, a0, ach, tc, tile);
+        __syncthreads();
+        if (live) {
+            const uint32_t *row = tile + tid * S.stride;
+            for (int a = 0; a < ach; ++a) {
+                const uint32_t n = row[a];
+                csum += n;
+                // the exact float of n < 2^23 from its bits; larger counts exceed
+                // the exactness bound and are redone in FP64 below
+                const float c = __uint_as_float((n & 0x7FFFFFu) | 0x4B000000u) - 8388608.f;
+                const float4 *k4 = reinterpret_cast<const float4 *>(ks + a * kSliceW);
+                if (STRESS) {
+#pragma unroll
+                    for (int q = 0; q < 9; ++q) {
+                        const float4 k = k4[q];
+                        acc[4 * q + 0] = fmaf(k.x, c, acc[4 * q + 0]);
+                        acc[4 * q + 1] = fmaf(k.y, c, acc[4 * q + 1]);
+                        acc[4 * q + 2] = fmaf(k.z, c, acc[4 * q + 2]);
+                        acc[4 * q + 3] = fmaf(k.w, c, acc[4 * q + 3]);
+                    }
+                }
+                if (MAG) {
+#pragma unroll
+                    for (int q = 9; q < 12; ++q) {
+                        const float4 k = k4[q];
+                        acc[4 * q + 0] = fmaf(k.x, c, acc[4 * q + 0]);
+                        acc[4 * q + 1] = fmaf(k.y, c, acc[4 * q + 1]);
+                        acc[4 * q + 2] = fmaf(k.z, c, acc[4 * q + 2]);
+                        acc[4 * q + 3] = fmaf(k.w, c, acc[4 * q + 3]);
+                    }
+                }
+            }
+        }
+    }
+    if (!live) return;
+    const int nc = P.ncell;
+    double sig[12];
+    if (csum <= kExactCells) {
+#pragma unroll
+        for (int j = 0; j < 12; ++j) {
+            if ((j < 9 && STRESS) || (j >= 9 && MAG)) {
+                const long long A = (long long)__float2int_rn(acc[4 * j + 0]) * (1ll << 36) +
+                                    (long long)__float2int_rn(acc[4 * j + 1]) * (1ll << 24) +
+                                    (long long)__float2int_rn(acc[4 * j + 2]) * (1ll << 12) +
+                                    (long long)__float2int_rn(acc[4 * j + 3]);
+                sig[j] = (double)A * factor[j];
+            }
+        }
+    } else {
+        // a crowded cell: the reference's FP64 sum of K_j(a) * ((count / D) * V), times measure
+        double s[12];
+#pragma unroll
+        for (int j = 0; j < 12; ++j) s[j] = 0.0;
+        const long long row = (long long)cell * na;
+        for (int a = 0; a < na; ++a) {
+            const uint32_t n = counts[row + a];
+            const double f = ((int)n < lut_n && (int)n >= 0) ? __ldg(lut + n) : ((double)n / P.dist_den) * P.volume;
+            if (STRESS) {
+#pragma unroll
+                for (int j = 0; j < 9; ++j) s[j] = fma(kern[j * na + a], f, s[j]);
+            }
+            if (MAG) {
+#pragma unroll
+                for (int j = 9; j < 12; ++j) s[j] = fma(kern[j * na + a], f, s[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 12; ++j) sig[j] = s[j] * P.measure;
+    }
+    if (STRESS) {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = make_double2(sig[j], 0.0);
+    }
+    if (MAG) {
+#pragma unroll
+        for (int j = 9; j < 12; ++j) fwd[(long long)j * nc + cell] = make_double2(sig[j], 0.0);
+    }
+    const double dens = (((double)csum / P.dist_den) * P.volume) * P.dthph;
+    table[(long long)cell * tstride + T_DIFF] = sqrt(2.0 * P.dt * (P.Dt + P.volex * dens));
+    if (tstride == TABLE_STRIDE_MAG) table[(long long)cell * tstride + T_DENS] = dens;
+    cellcount[cell] = csum;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 mixed path.  DIST: the tile holds the bits of an FP32 distribution
+// (the denoised histogram) instead of counts.
+// ---------------------------------------------------------------------------
+template <bool STRESS, bool MAG, bool DIST>
+__global__ void __launch_bounds__(kCTile) k_contract_f(const uint32_t *__restrict__ src_bins,
+                                                       const float *__restrict__ kern, MixedParams M, Staging S,
+                                                       float scale, float dscale, float2 *__restrict__ fwd,
+                                                       float *__restrict__ table, int tstride,
+                                                       double *__restrict__ partials, unsigned *__restrict__ done,
+                                                       double *__restrict__ sums) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double red[kCTile / 32][12];
+    __shared__ bool s_last;
+    const int na = S.na;
+    float *kf = reinterpret_cast<float *>(smem);  // [chunk angle][12]
+    uint32_t *tile = reinterpret_cast<uint32_t *>(kf + (na < kAngChunk ? na : kAngChunk) * 12);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, cell0 = blockIdx.x * kCTile;
+    const int tc = min(kCTile, M.ncell - cell0);
+    const bool live = tid < tc;
+    const int cell = cell0 + tid;
+    float acc[12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) acc[j] = 0.f;
+    float dsum = 0.f;
+    uint32_t csum = 0;
+    const uint32_t *src = src_bins + (long long)cell0 * na;
+    for (int a0 = 0; a0 < na; a0 += kAngChunk) {
+        const int ach = min(kAngChunk, na - a0);
+        __syncthreads();
+        // the chunk's angle kernels, transposed to [angle][component]
+        for (int i = tid; i < 12 * ach; i += kCTile) {
+            const int j = i / ach, a = i - j * ach;
+            kf[a * 12 + j] = __ldg(kern + (long long)j * na + a0 + a);
+        }
+        stage_rows(src, S, a0, ach, tc, tile);
+        __syncthreads();
+        if (live) {
+            const uint32_t *row = tile + tid * S.stride;
+            for (int a = 0; a < ach; ++a) {
+                const uint32_t w = row[a];
+                float f;
+                if (DIST) {
+                    f = __uint_as_float(w);
+                    dsum += f;
+                } else {
+                    f = __uint2float_rn(w);
+                    csum += w;
+                }
+                const float4 *k4 = reinterpret_cast<const float4 *>(kf + a * 12);
+                if (STRESS) {
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        const float4 k = k4[q];
+                        acc[4 * q + 0] = fmaf(k.x, f, acc[4 * q + 0]);
+                        acc[4 * q + 1] = fmaf(k.y, f, acc[4 * q + 1]);
+                        acc[4 * q + 2] = fmaf(k.z, f, acc[4 * q + 2]);
+                        acc[4 * q + 3] = fmaf(k.w, f, acc[4 * q + 3]);
+                    }
+                }
+                if (STRESS || MAG) {
+                    const float4 k = k4[2];
+                    if (STRESS) acc[8] = fmaf(k.x, f, acc[8]);
+                    if (MAG) {
+                        acc[9] = fmaf(k.y, f, acc[9]);
+                        acc[10] = fmaf(k.z, f, acc[10]);
+                        acc[11] = fmaf(k.w, f, acc[11]);
+                    }
+                }
+            }
+        }
+    }
+    const int nc = M.ncell;
+    float out[12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) out[j] = acc[j] * scale;
+    if (live) {
+        if (STRESS) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = make_float2(out[j], 0.f);
+        }
+        if (MAG) {
+#pragma unroll
+            for (int j = 9; j < 12; ++j) fwd[(long long)j * nc + cell] = make_float2(out[j], 0.f);
+        }
+        const float dens = DIST ? dsum * dscale * M.dthph
+                                : (float)(((double)csum / M.dist_den) * M.volume) * M.dthph;
+        table[(long long)cell * tstride + T_DIFF] = sqrtf(M.two_dt * (M.Dt + M.volex * dens));
+    }
+    // the block's component sums in a fixed order
+#pragma unroll
+    for (int j = 0; j < 12; ++j) {
+        if ((j < 9 && STRESS) || (j >= 9 && MAG)) {
+            const double v = warp_pair_sum(live ? out[j] : 0.f);
+            if (lane == 0) red[warp][j] = v;
+        }
+    }
+    __syncthreads();
+    if (tid < 12 && ((tid < 9 && STRESS) || (tid >= 9 && MAG))) {
+        double v = 0.0;
+#pragma unroll
+        for (int w = 0; w < kCTile / 32; ++w) v += red[w][tid];
+        partials[(long long)blockIdx.x * 12 + tid] = v;
+        __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    // the last block: the blocks' sums in block order
+    __threadfence();
+    for (int j = warp; j < 12; j += kCTile / 32) {
+        if ((j < 9 && STRESS) || (j >= 9 && MAG)) {
+            double v = 0.0;
+            for (int b = lane; b < (int)gridDim.x; b += 32) v += __ldcg(partials + (long long)b * 12 + j);
+            v = warp_sum_d(v);
+            if (lane == 0) sums[j] = v;
+        }
+    }
+    if (tid == 0) *done = 0u;  // ready for the next launch
+}
+
+Staging make_staging(int na) {
+    Staging S;
+    S.na = na;
+    const int ach = na < kAngChunk ? na : kAngChunk;
+    S.stride = ach | 1;
+    S.qshift = -1;
+    if ((na & 3) == 0 && na <= kAngChunk) {
+        const int q = na >> 2;
+        if ((q & (q - 1)) == 0) {
+            int l = 0;
+            while ((1 << l) < q) ++l;
+            S.qshift = l;
+        }
+    }
+    return S;
+}
+
+size_t smem_x(int na) {
+    const int ach = na < kAngChunk ? na : kAngChunk;
+    return (size_t)ach * kSliceW * sizeof(float) + (size_t)kCTile * (ach | 1) * sizeof(uint32_t);
+}
+size_t smem_f(int na) {
+    const int ach = na < kAngChunk ? na : kAngChunk;
+    return (size_t)ach * 12 * sizeof(float) + (size_t)kCTile * (ach | 1) * sizeof(uint32_t);
+}
+
+unsigned tiles(int ncell) { return (unsigned)((ncell + kCTile - 1) / kCTile); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+void kernel_slices(const std::vector<double> &K, int na, double measure_v_over_d, std::vector<float> &slices,
+                   std::vector<double> &factor) {
+    slices.assign((size_t)na * kSliceW, 0.f);
+    factor.assign(12, 0.0);
+    for (int j = 0; j < 12; ++j) {
+        double mx = 0.0;
+        for (int a = 0; a < na; ++a) mx = std::fmax(mx, std::fabs(K[(size_t)j * na + a]));
+        if (!(mx > 0.0) || !std::isfinite(mx)) continue;  // an all-zero component stays zero
+        const int E = std::ilogb(mx) + 1;                 // max |K_j| < 2^E
+        for (int a = 0; a < na; ++a) {
+            // v = K 2^(12 - E), |v| < 2^12; four roundings to integers, each
+            // remainder (exact) scaled by 2^12 for the next slice
+            double v = std::ldexp(K[(size_t)j * na + a], 12 - E);
+            for (int s = 0; s < 4; ++s) {
+                const double m = std::nearbyint(v);
+                slices[(size_t)a * kSliceW + 4 * j + s] = (float)m;
+                v = std::ldexp(v - m, 12);
+            }
+        }
+        factor[j] = std::ldexp(1.0, E - 48) * measure_v_over_d;
+    }
+}
+
+void contract_prepare() {
+    const int big = 227 * 1024;
+    cudaFuncSetAttribute(k_contract_x<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_contract_x<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_contract_x<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_contract_f<true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_contract_f<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_contract_f<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_contract_f<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_contract_f<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_contract_f<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+}
+
+void launch_contract_x(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kslice,
+                       const double *factor, const double *kern, const double *lut, int lut_n, const DevParams &P,
+                       double2 *fwd, double *table, int tstride, uint32_t *cellcount) {
+    const Staging S = make_staging(P.nang);
+    const size_t sm = smem_x(P.nang);
+    const unsigned b = tiles(P.ncell);
+#define SS_CX(ST, MG)                                                                                        \
+    k_contract_x<ST, MG><<<b, kCTile, sm, s>>>(counts, kslice, factor, kern, lut, lut_n, P, S, fwd, table, \
+                                               tstride, cellcount)
+    if (stress && mag) SS_CX(true, true);
+    else if (stress) SS_CX(true, false);
+    else SS_CX(false, true);
+#undef SS_CX
+}
+
+unsigned contract_m_blocks(int ncell) { return tiles(ncell); }
+
+void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kern,
+                       const MixedParams &M, float2 *fwd, float *table, int tstride, double *partials,
+                       unsigned *done, double *sums, const float *dist, float fscale) {
+    const Staging S = make_staging(M.nang);
+    const size_t sm = smem_f(M.nang);
+    const unsigned b = tiles(M.ncell);
+    const bool fd = dist != nullptr;
+    const uint32_t *src = fd ? reinterpret_cast<const uint32_t *>(dist) : counts;
+    // counts: f = count, scaled by measure * V / D; a distribution: f = value, scaled by measure * fscale
+    const float scale = fd ? M.measure * fscale : (float)((double)M.measure * (M.volume / M.dist_den));
+#define SS_CF(ST, MG, D)                                                                                    \
+    k_contract_f<ST, MG, D><<<b, kCTile, sm, s>>>(src, kern, M, S, scale, fscale, fwd, table, tstride,    \
+                                                  partials, done, sums)
+    if (stress && mag) { if (fd) SS_CF(true, true, true); else SS_CF(true, true, false); }
+    else if (stress) { if (fd) SS_CF(true, false, true); else SS_CF(true, false, false); }
+    else { if (fd) SS_CF(false, true, true); else SS_CF(false, true, false); }
+#undef SS_CF
+}
+
+}  // namespace ss

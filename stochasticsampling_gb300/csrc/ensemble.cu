@@ -50,6 +50,7 @@ struct EnsMember {
     int cell_off;
     int kern_off;
     int lut_off;  // kEnsLut FP32 distribution values of the counts 0 .. kEnsLut - 1
+    int chunk0, nchunk;  // the member's cell chunks (consecutive in the chunk list)
     float screening;
     float stepx, stepy;
 };
@@ -123,15 +124,16 @@ __global__ void k_ens_bin(const WorkUnit *__restrict__ units, int nunits, const 
 // counts (contiguous) and the member's 9 x nang stress kernel are staged in
 // shared memory with coalesced loads; thread c then sums its cell's row,
 // visiting the angles from a = c mod nang on so that a warp's shared-memory
-// reads fall in different banks.  The chunk's 9 component sums are added to
-// the member's FP64 sums with one atomic each.
+// reads fall in different banks.  The chunk's 9 component sums go to
+// partials[chunk][9]; k_ens_means adds a member's chunks in chunk order, so
+// the sums are the same bit for bit from run to run.
 __global__ void __launch_bounds__(kChunkCells) k_ens_contract(const CellChunk *__restrict__ chunks,
                                                               const EnsMember *__restrict__ mem,
                                                               const uint32_t *__restrict__ counts,
                                                               const float *__restrict__ kern,
                                                               const float *__restrict__ lut,
                                                               float2 *__restrict__ fwd, float *__restrict__ diff,
-                                                              double *__restrict__ sums) {
+                                                              double *__restrict__ partials) {
     extern __shared__ uint32_t s_counts[];
     __shared__ float s_kern[9 * kEnsMaxPhi];
     __shared__ double s_red[kChunkCells / 32][9];
@@ -177,15 +179,21 @@ __global__ void __launch_bounds__(kChunkCells) k_ens_contract(const CellChunk *_
     if (tid < 9) {
         double v = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += s_red[w][tid];
-        atomicAdd(sums + 9 * ch.member + tid, v);
+        partials[9ll * blockIdx.x + tid] = v;
     }
 }
 
-// per member and component: the FP64 mean rounded to FP32
-__global__ void k_ens_means(const EnsMember *__restrict__ mem, int nm, const double *__restrict__ sums,
+// per member and component: the sum of the member's chunk sums in chunk
+// order (FP64), as the mean rounded to FP32
+__global__ void k_ens_means(const EnsMember *__restrict__ mem, int nm, const double *__restrict__ partials,
                             float *__restrict__ means) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < 9 * nm) means[i] = (float)(sums[i] / (double)mem[i / 9].M.ncell);
+    if (i >= 9 * nm) return;
+    const EnsMember &E = mem[i / 9];
+    const int j = i % 9;
+    double v = 0.0;
+    for (int k = 0; k < E.nchunk; ++k) v += partials[9ll * (E.chunk0 + k) + j];
+    means[i] = (float)(v / (double)E.M.ncell);
 }
 
 // subtract the means before the FP32 transform (the k_center_m of a single context)
@@ -388,7 +396,7 @@ struct ss_ens {
     uint32_t *counts[2] = {};
     float2 *fwd = nullptr, *inv = nullptr;
     float *table = nullptr, *kern = nullptr, *lut = nullptr, *diff = nullptr, *means = nullptr;
-    double *sums = nullptr;
+    double *sums = nullptr;  // per cell chunk, its 9 component sums
     unsigned long long *d_step = nullptr;
     cudaGraphExec_t graph[2] = {};
     uint64_t launches = 0, step_launches = 0;
@@ -447,7 +455,6 @@ unsigned nb(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 int enqueue_solve(ss_ens *e, int ccur, uint64_t *nl) {
     cudaStream_t s = e->stream;
     const unsigned nc = (unsigned)e->nchunks;
-    ECK(cudaMemsetAsync(e->sums, 0, 9ull * e->nm * sizeof(double), s));
     k_ens_contract<<<nc, kChunkCells, e->chunk_smem, s>>>(e->d_chunks, e->d_mem, e->counts[ccur], e->kern, e->lut,
                                                            e->fwd, e->diff, e->sums);
     k_ens_means<<<nb(9ll * e->nm, 128), 128, 0, s>>>(e->d_mem, (int)e->nm, e->sums, e->means);
@@ -731,7 +738,9 @@ int ss_ensemble_create(const ss_grid *grids, const ss_box *boxes, const ss_param
     std::vector<CellChunk> chunks;
     for (uint32_t m = 0; m < count; ++m) {
         const int nc = e->mem[m].M.ncell, per = chunk_cells(e->mem[m].M.nang);
+        e->mem[m].chunk0 = (int)chunks.size();
         for (int c0 = 0; c0 < nc; c0 += per) chunks.push_back({m, c0, std::min(per, nc - c0)});
+        e->mem[m].nchunk = (int)chunks.size() - e->mem[m].chunk0;
         e->chunk_smem = std::max(e->chunk_smem, (size_t)per * e->mem[m].M.nang * sizeof(uint32_t));
     }
     e->nchunks = (int)chunks.size();
@@ -764,7 +773,7 @@ int ss_ensemble_create(const ss_grid *grids, const ss_box *boxes, const ss_param
     A((void **)&e->table, (size_t)e->total_cells * kEnsRow * sizeof(float));
     A((void **)&e->kern, kern.size() * sizeof(float));
     A((void **)&e->lut, lut.size() * sizeof(float));
-    A((void **)&e->sums, 9ull * count * sizeof(double));
+    A((void **)&e->sums, 9ull * chunks.size() * sizeof(double));
     A((void **)&e->d_step, sizeof(unsigned long long));
     A((void **)&e->realbuf, 3ull * max_cell * sizeof(double));
     A((void **)&e->staging, 5ull * max_n * sizeof(double));

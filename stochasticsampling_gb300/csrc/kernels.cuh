@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace ss {
@@ -26,6 +28,19 @@ void launch_counts_to_dist(cudaStream_t s, const uint32_t *counts, const DevPara
 void launch_contract(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const double *dist,
                      const double *lut, int lut_n, const double *kern, const DevParams &P, double2 *fwd,
                      double *table, int tstride, uint32_t *cellcount);
+// the FP64 contraction of a histogram (contract.cu): kslice, factor from
+// kernel_slices; kern and lut serve cells of more than 2^12 particles
+void launch_contract_x(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kslice,
+                       const double *factor, const double *kern, const double *lut, int lut_n, const DevParams &P,
+                       double2 *fwd, double *table, int tstride, uint32_t *cellcount);
+// host: the angle kernels K [12][na] as four 12-bit integer slices per entry,
+// slices [na][48] (component j, slice s at 4 j + s), and per component the
+// factor 2^(E_j - 48) * measure_v_over_d that turns the combined slice sums
+// into the contraction
+void kernel_slices(const std::vector<double> &K, int na, double measure_v_over_d, std::vector<float> &slices,
+                   std::vector<double> &factor);
+// shared-memory limits of the contraction kernels on the current device
+void contract_prepare();
 void launch_kspace(cudaStream_t s, bool flow, bool mag, const double2 *fwd, double2 *inv, const DevParams &P,
                    double screening);
 void launch_table(cudaStream_t s, bool flow, bool mag, const double2 *inv, const DevParams &P, double *table,

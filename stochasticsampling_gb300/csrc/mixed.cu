@@ -90,73 +90,6 @@ __global__ void k_bin_m(unsigned long long n, MixedParams M, const double *__res
     key[i] = cell;
 }
 
-// angular contraction in FP32 (thread per cell, angle kernels in shared
-// memory); per-component sums of the result accumulated in FP64 for the
-// mean handling (one FP64 atomic per component per warp)
-// dist != nullptr: the distribution comes from dist[bin] * fscale (the
-// denoised histogram) instead of the counts
-template <bool STRESS, bool MAG>
-__global__ void __launch_bounds__(64) k_contract_m(const uint32_t *__restrict__ counts,
-                                                   const float *__restrict__ lut, int lut_n,
-                                                   const float *__restrict__ kern, MixedParams M,
-                                                   float2 *__restrict__ fwd, float *__restrict__ table, int tstride,
-                                                   double *__restrict__ sums, const float *__restrict__ dist,
-                                                   float fscale) {
-    extern __shared__ float skf[];
-    const int na = M.nang;
-    for (int i = threadIdx.x; i < 12 * na; i += blockDim.x) skf[i] = kern[i];
-    __syncthreads();
-    int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = cell < M.ncell;
-    float acc[13];
-#pragma unroll
-    for (int j = 0; j < 13; ++j) acc[j] = 0.f;
-    if (live) {
-        const long long row = (long long)cell * na;
-        for (int a = 0; a < na; ++a) {
-            float f;
-            if (dist) {
-                f = dist[row + a] * fscale;
-            } else {
-                const uint32_t c = counts[row + a];
-                f = ((int)c < lut_n) ? __ldg(lut + c) : (float)(((double)c / M.dist_den) * M.volume);
-            }
-            if (STRESS) {
-#pragma unroll
-                for (int j = 0; j < 9; ++j) acc[j] = fmaf(skf[j * na + a], f, acc[j]);
-            }
-            if (MAG) {
-#pragma unroll
-                for (int j = 9; j < 12; ++j) acc[j] = fmaf(skf[j * na + a], f, acc[j]);
-            }
-            acc[12] += f;
-        }
-    }
-    const int nc = M.ncell;
-    if (live) {
-        if (STRESS) {
-#pragma unroll
-            for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = make_float2(acc[j] * M.measure, 0.f);
-        }
-        if (MAG) {
-#pragma unroll
-            for (int j = 9; j < 12; ++j) fwd[(long long)j * nc + cell] = make_float2(acc[j] * M.measure, 0.f);
-        }
-        float dens = acc[12] * M.dthph;
-        table[(long long)cell * tstride + T_DIFF] = sqrtf(M.two_dt * (M.Dt + M.volex * dens));
-    }
-    // FP64 component sums: warp partials in FP64, one atomic per warp
-#pragma unroll
-    for (int j = 0; j < 12; ++j) {
-        if ((j < 9 && STRESS) || (j >= 9 && MAG)) {
-            double v = live ? (double)(acc[j] * M.measure) : 0.0;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if ((threadIdx.x & 31) == 0) atomicAdd(sums + j, v);
-        }
-    }
-}
-
 // subtract the FP64 means before the FP32 transform
 __global__ void k_center_m(float2 *__restrict__ fwd, int c0, int c1, int ncell, const double *__restrict__ sums) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -382,22 +315,6 @@ void launch_bin_m(cudaStream_t s, bool fixed, unsigned long long n, const MixedP
     if (fixed) k_bin_m<true><<<nb(n, 256), 256, 0, s>>>(n, M, xs[0], xs[1], xs[2], as[0], as[1], key, counts);
     else k_bin_m<false><<<nb(n, 256), 256, 0, s>>>(n, M, xs[0], xs[1], xs[2], as[0], as[1], key, counts);
 }
-void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *lut, int lut_n,
-                       const float *kern, const MixedParams &M, float2 *fwd, float *table, int tstride,
-                       double *sums, const float *dist, float fscale) {
-    unsigned blocks = nb((unsigned long long)M.ncell, 64);
-    const size_t sm = 12ull * M.nang * sizeof(float);
-    if (stress && mag)
-        k_contract_m<true, true><<<blocks, 64, sm, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums, dist,
-                                                        fscale);
-    else if (stress)
-        k_contract_m<true, false><<<blocks, 64, sm, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums, dist,
-                                                         fscale);
-    else
-        k_contract_m<false, true><<<blocks, 64, sm, s>>>(counts, lut, lut_n, kern, M, fwd, table, tstride, sums, dist,
-                                                         fscale);
-}
-
 // counts -> the denoiser's input, counts / (N / nbins) (mean 1)
 __global__ void k_counts_to_unit(const uint32_t *__restrict__ counts, long long nbins, float inv_mean,
                                  float *__restrict__ x) {

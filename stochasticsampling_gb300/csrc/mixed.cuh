@@ -35,9 +35,16 @@ void launch_egest_m(cudaStream_t s, bool fixed, unsigned long long n, const Mixe
                     float *const as[2], const uint32_t *id, double *aos);
 void launch_bin_m(cudaStream_t s, bool fixed, unsigned long long n, const MixedParams &M, double *const xs[3],
                   float *const as[2], uint32_t *key, uint32_t *counts);
-void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *lut, int lut_n,
-                       const float *kern, const MixedParams &M, float2 *fwd, float *table, int tstride,
-                       double *sums, const float *dist = nullptr, float fscale = 0.f);
+// the FP32 angular contraction (contract.cu): fwd components, the table's
+// diffusion length and the FP64 component sums (sums[0..9) with stress,
+// sums[9..12) with the polarisation) in a fixed order.  partials:
+// contract_m_blocks(ncell) x 12 doubles; done: a counter that is 0 between
+// launches.  dist != nullptr: an FP32 distribution times fscale replaces the
+// counts (the denoised histogram).
+unsigned contract_m_blocks(int ncell);
+void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kern,
+                       const MixedParams &M, float2 *fwd, float *table, int tstride, double *partials,
+                       unsigned *done, double *sums, const float *dist = nullptr, float fscale = 0.f);
 void launch_counts_to_unit(cudaStream_t s, const uint32_t *counts, long long nbins, float inv_mean, float *x);
 void launch_center_m(cudaStream_t s, float2 *fwd, int c0, int c1, int ncell, const double *sums);
 void launch_kspace_m(cudaStream_t s, bool flow, bool mag, const float2 *fwd, float2 *inv, const MixedParams &M,

@@ -1,13 +1,13 @@
 // noalloc.cu -- the distribution of a particle list without any allocation.
 //
 // Some callers cannot call cudaMalloc or cudaFree at the point where they
-// need a histogram: code that runs while a CUDA stream is being captured into
-// a graph, a hook called from another library's loop where the device-wide
-// synchronisation of cudaFree would stall or deadlock it, or an application
-// that reserves a fixed device-memory budget at start-up and may not grow it.
-// ss_sample_distribution_noalloc serves them: its only scratch is the
-// file-scope device array below, of a fixed size, which every GPU that loads
-// this library holds until the process exits.  It allocates nothing.
+// need a histogram: a hook called from another library's loop, where the
+// device-wide synchronisation of cudaFree would stall or deadlock that loop,
+// or an application that reserves a fixed device-memory budget at start-up
+// and may not grow it afterwards.  ss_sample_distribution_noalloc serves
+// them: its only scratch is the file-scope device array below, of a fixed
+// size, which every GPU that loads this library holds until the process
+// exits.  It allocates nothing.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -27,12 +27,16 @@ void record_error(const char *msg);  // ssgpu.cu: the context-free error of ss_l
 
 namespace {
 
-// scratch: one u32 count per bin, shared by every call on a device
-static __device__ __align__(256) uint32_t g_noalloc_counts[SS_NOALLOC_MAX_BINS];
+// scratch: one u32 count per bin, then the error word (index
+// SS_NOALLOC_MAX_BINS: non-zero when a row had a non-finite coordinate),
+// shared by every call on a device
+constexpr unsigned kErrWord = SS_NOALLOC_MAX_BINS;
+static __device__ __align__(256) uint32_t g_noalloc_counts[SS_NOALLOC_MAX_BINS + 64];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 uint32_t *g_counts_ptr[kMaxDevices] = {};
+int g_sms[kMaxDevices] = {};  // multiprocessors of each device, looked up with the address
 
 // the message is returned by ss_last_error(NULL, ...)
 int noalloc_fail(int code, const char *fmt, ...) {
@@ -45,9 +49,10 @@ int noalloc_fail(int code, const char *fmt, ...) {
     return code;
 }
 
-// device address of the scratch array on the current device, looked up once
-// per device with that device current
-int scratch_on_current_device(uint32_t **out) {
+// device address of the scratch array on the current device and the
+// device's multiprocessor count, looked up once per device with that device
+// current
+int scratch_on_current_device(uint32_t **out, int *sms) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return noalloc_fail(SS_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
@@ -58,25 +63,43 @@ int scratch_on_current_device(uint32_t **out) {
         e = cudaGetSymbolAddress(&p, g_noalloc_counts);
         if (e != cudaSuccess)
             return noalloc_fail(SS_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+        int m = 0;
+        e = cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess)
+            return noalloc_fail(SS_ERR_CUDA, "cudaDeviceGetAttribute(multiprocessors): %s", cudaGetErrorString(e));
+        g_sms[dev] = m > 0 ? m : 1;
         g_counts_ptr[dev] = static_cast<uint32_t *>(p);
     }
     *out = g_counts_ptr[dev];
+    *sms = g_sms[dev];
     return SS_OK;
 }
 
+// the counts of the call's bins and the error word to zero
 __global__ void k_noalloc_zero(uint32_t *__restrict__ counts, long long nbins) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     long long stride = (long long)gridDim.x * blockDim.x;
+    if (i == 0) counts[kErrWord] = 0u;
     for (; i < nbins; i += stride) counts[i] = 0u;
 }
 
 // Particle::new (src/particle.rs:186-201) on each row, then the bin of
-// Distribution::coord_to_grid, counted with an atomic add
+// Distribution::coord_to_grid, counted with an atomic add.  A row with a
+// non-finite coordinate (which ss_init refuses) is not counted; it sets the
+// error word instead.
 __global__ void k_noalloc_bin(const double *__restrict__ aos, unsigned long long n, DevParams P,
                               uint32_t *__restrict__ counts) {
     unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double *p = aos + 5 * i;
+    const unsigned long long *b = reinterpret_cast<const unsigned long long *>(p);
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) bad |= ((b[k] >> 52) & 0x7FFull) == 0x7FFull;  // Inf or NaN
+    if (bad) {
+        atomicOr(counts + kErrWord, 1u);
+        return;
+    }
     double x = ref_modulo(p[0], P.bx), y = ref_modulo(p[1], P.by), z = ref_modulo(p[2], P.bz);
     double ph = p[3], th = p[4];
     ref_ang_pbc(ph, th);
@@ -95,12 +118,12 @@ __global__ void k_noalloc_bin(const double *__restrict__ aos, unsigned long long
 }
 
 // (count / D) * V, the normalisation of sample_from and the box-volume
-// rescale of do_timestep
+// rescale of do_timestep; NaN in every bin when a row was non-finite
 __global__ void k_noalloc_dist(const uint32_t *__restrict__ counts, long long nbins, double den, double vol,
                                double *__restrict__ dist) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= nbins) return;
-    dist[i] = ((double)counts[i] / den) * vol;
+    dist[i] = counts[kErrWord] ? __longlong_as_double(0x7FF8000000000000ll) : ((double)counts[i] / den) * vol;
 }
 
 }  // namespace
@@ -122,10 +145,12 @@ extern "C" int ss_sample_distribution_noalloc(const ss_grid *grid, const ss_box 
         !std::isfinite(box->z))
         return noalloc_fail(SS_ERR_INVALID_ARGUMENT, "Box size is invalid. Must be bigger than 0: (%g, %g, %g)",
                             box->x, box->y, box->z);
-    if (n < 1) return noalloc_fail(SS_ERR_INVALID_ARGUMENT, "n must be at least 1");
+    if (n < 1 || n > 0xffffffffull)
+        return noalloc_fail(SS_ERR_INVALID_ARGUMENT, "number_of_particles must lie in [1, 2^32-1]");
 
     uint32_t *counts = nullptr;
-    int rc = scratch_on_current_device(&counts);
+    int sms = 1;
+    int rc = scratch_on_current_device(&counts, &sms);
     if (rc != SS_OK) return rc;
 
     DevParams P{};
@@ -147,7 +172,7 @@ extern "C" int ss_sample_distribution_noalloc(const ss_grid *grid, const ss_box 
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     long long zb = (P.nbins + 255) / 256;
-    if (zb > 152 * 16) zb = 152 * 16;
+    if (zb > 8ll * sms) zb = 8ll * sms;  // a grid-stride loop: eight blocks per multiprocessor suffice
     k_noalloc_zero<<<(unsigned)zb, 256, 0, s>>>(counts, P.nbins);
     k_noalloc_bin<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(particles, n, P, counts);
     k_noalloc_dist<<<(unsigned)((P.nbins + 255) / 256), 256, 0, s>>>(counts, P.nbins, den, vol, dist);

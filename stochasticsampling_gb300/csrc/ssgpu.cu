@@ -70,6 +70,8 @@ struct ss_ctx {
     double *ctab = nullptr;  // canonical quasi-2-D rows (CT_*), FP64 quasi2d contexts
     uint32_t *cellcount = nullptr, *cursor = nullptr;
     double *kern = nullptr, *lut = nullptr;
+    float *kslice = nullptr;    // the angle kernels as 12-bit integer slices (FP64 contraction)
+    double *kfactor = nullptr;  // per component: 2^(E_j - 48) * measure * V / D
     double *staging = nullptr, *noise_dev = nullptr, *dist_dev = nullptr, *realbuf = nullptr;
     double *staging_sorted = nullptr;  // the rows in cell order before the ingest
     unsigned long long *d_step = nullptr;
@@ -88,8 +90,10 @@ struct ss_ctx {
     MixedParams M{};
     float *pa[2][2] = {};  // phi, theta (FP32)
     float2 *fwd_f = nullptr, *inv_f = nullptr;
-    float *table_f = nullptr, *kern_f = nullptr, *lut_f = nullptr;
+    float *table_f = nullptr, *kern_f = nullptr;
     double *sums = nullptr;  // FP64 per-component sums for the mean handling
+    double *partials = nullptr;  // per-block component sums of the FP32 contraction (+ its counter)
+    unsigned *partials_done = nullptr;
     bool wide_valid = false;  // inv (FP64) holds the widened mixed fields
     std::map<int, cufftHandle> plans_c;
 
@@ -108,6 +112,9 @@ struct ss_ctx {
     Timing timing;
     std::string err;
 };
+
+// the FP32 contraction's per-block component sums and, after them, its counter
+static size_t partials_bytes(uint64_t ncell) { return (12ull * contract_m_blocks((int)ncell) + 1) * sizeof(double); }
 
 // ---------------------------------------------------------------------------
 // error helpers
@@ -270,8 +277,12 @@ static int enqueue_solve(ss_ctx *c, bool flow, bool mag, const uint32_t *counts,
                          int pcur, bool sort_now, uint64_t *nl) {
     const int ts = (c->mag_step || c->P.gather) ? TABLE_STRIDE_MAG : TABLE_STRIDE;
     mark(c, 0);
-    launch_contract(c->stream, flow, mag, counts, dist, c->lut, kLutN, c->kern, c->P, c->fwd, c->table, ts,
-                    c->cellcount);
+    if (dist)
+        launch_contract(c->stream, flow, mag, counts, dist, c->lut, kLutN, c->kern, c->P, c->fwd, c->table, ts,
+                        c->cellcount);
+    else
+        launch_contract_x(c->stream, flow, mag, counts, c->kslice, c->kfactor, c->kern, c->lut, kLutN, c->P, c->fwd,
+                          c->table, ts, c->cellcount);
     ++*nl;
     CKR(check_launch(c, "contract"));
     mark(c, 6);
@@ -312,16 +323,15 @@ static int enqueue_solve_m(ss_ctx *c, bool flow, bool mag, const uint32_t *count
     const int ts = c->mag_step ? TABLE_STRIDE_MAG : TABLE_STRIDE;
     const int nc = c->P.ncell;
     mark(c, 0);
-    CK(cudaMemsetAsync(c->sums, 0, 12 * sizeof(double), c->stream));
     if (c->dn && flow) {
         // the denoised histogram replaces the counts in the contraction
         launch_counts_to_unit(c->stream, counts, c->P.nbins, c->dn_inv_mean, c->dn_x);
         *nl += 1 + dn_enqueue_forward(c->dn, c->dn_x, c->dn_y, c->stream);
-        launch_contract_m(c->stream, flow, mag, counts, c->lut_f, kLutN, c->kern_f, c->M, c->fwd_f, c->table_f, ts,
-                          c->sums, c->dn_y, c->dn_fscale);
+        launch_contract_m(c->stream, flow, mag, counts, c->kern_f, c->M, c->fwd_f, c->table_f, ts, c->partials,
+                          c->partials_done, c->sums, c->dn_y, c->dn_fscale);
     } else {
-        launch_contract_m(c->stream, flow, mag, counts, c->lut_f, kLutN, c->kern_f, c->M, c->fwd_f, c->table_f, ts,
-                          c->sums);
+        launch_contract_m(c->stream, flow, mag, counts, c->kern_f, c->M, c->fwd_f, c->table_f, ts, c->partials,
+                          c->partials_done, c->sums);
     }
     if (flow) launch_center_m(c->stream, c->fwd_f, 0, 9, nc, c->sums);
     if (mag) launch_center_m(c->stream, c->fwd_f, 9, 12, nc, c->sums);
@@ -492,7 +502,8 @@ static void destroy_impl(ss_ctx *c) {
     for (auto &kv : c->plans_c) cufftDestroy(kv.second);
     for (int b = 0; b < 2; ++b)
         for (int k = 0; k < 2; ++k) cudaFree(c->pa[b][k]);
-    cudaFree(c->fwd_f); cudaFree(c->inv_f); cudaFree(c->table_f); cudaFree(c->kern_f); cudaFree(c->lut_f);
+    cudaFree(c->fwd_f); cudaFree(c->inv_f); cudaFree(c->table_f); cudaFree(c->kern_f); cudaFree(c->partials);
+    cudaFree(c->kslice); cudaFree(c->kfactor);
     cudaFree(c->dn_x); cudaFree(c->dn_y);
     cudaFree(c->sums);
     for (auto &e : c->timing.ev)
@@ -697,6 +708,8 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     if (rc == SS_OK) rc = alloc((void **)&c->cursor, ncell * sizeof(uint32_t));
     if (rc == SS_OK) rc = alloc((void **)&c->kern, 12 * nang * sizeof(double));
     if (rc == SS_OK) rc = alloc((void **)&c->lut, kLutN * sizeof(double));
+    if (rc == SS_OK) rc = alloc((void **)&c->kslice, 48 * nang * sizeof(float));
+    if (rc == SS_OK) rc = alloc((void **)&c->kfactor, 12 * sizeof(double));
     if (rc == SS_OK) rc = alloc((void **)&c->staging, 5 * N * sizeof(double));
     if (rc == SS_OK) rc = alloc((void **)&c->d_step, sizeof(unsigned long long));
     if (rc == SS_OK) rc = alloc((void **)&c->d_err, sizeof(uint32_t));
@@ -707,8 +720,8 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
         if (rc == SS_OK) rc = alloc((void **)&c->inv_f, 24 * ncell * sizeof(float2));
         if (rc == SS_OK) rc = alloc((void **)&c->table_f, ncell * TABLE_STRIDE_MAG * sizeof(float));
         if (rc == SS_OK) rc = alloc((void **)&c->kern_f, 12 * nang * sizeof(float));
-        if (rc == SS_OK) rc = alloc((void **)&c->lut_f, kLutN * sizeof(float));
         if (rc == SS_OK) rc = alloc((void **)&c->sums, 12 * sizeof(double));
+        if (rc == SS_OK) rc = alloc((void **)&c->partials, partials_bytes(ncell));
     }
     if (rc != SS_OK) {
         std::string m = c->err;
@@ -738,13 +751,21 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     for (int i = 0; i < kLutN; ++i) lut[i] = ((double)i / P.dist_den) * P.volume;
     CKC(cudaMemcpyAsync(c->kern, K.data(), K.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     CKC(cudaMemcpyAsync(c->lut, lut.data(), lut.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    std::vector<float> Kf(K.begin(), K.end()), lutf(lut.begin(), lut.end());
+    std::vector<float> slices;
+    std::vector<double> factor;
+    kernel_slices(K, (int)nang, P.measure * (P.volume / P.dist_den), slices, factor);
+    CKC(cudaMemcpyAsync(c->kslice, slices.data(), slices.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CKC(cudaMemcpyAsync(c->kfactor, factor.data(), factor.size() * sizeof(double), cudaMemcpyHostToDevice,
+                        c->stream));
+    std::vector<float> Kf(K.begin(), K.end());
     if (c->mixed) {
         CKC(cudaMemsetAsync(c->inv_f, 0, 24 * ncell * sizeof(float2), c->stream));
         CKC(cudaMemsetAsync(c->sums, 0, 12 * sizeof(double), c->stream));
+        CKC(cudaMemsetAsync(c->partials, 0, partials_bytes(ncell), c->stream));
+        c->partials_done = reinterpret_cast<unsigned *>(c->partials + 12ull * contract_m_blocks((int)ncell));
         CKC(cudaMemcpyAsync(c->kern_f, Kf.data(), Kf.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-        CKC(cudaMemcpyAsync(c->lut_f, lutf.data(), lutf.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     }
+    contract_prepare();
     launch_half_pi(c->stream, c->d_halfpi);
     double hp[2];
     CKC(cudaMemcpyAsync(hp, c->d_halfpi, sizeof hp, cudaMemcpyDeviceToHost, c->stream));

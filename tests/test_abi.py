@@ -73,6 +73,21 @@ def test_invalid_arguments_are_rejected_on_the_host():
     assert L.ss_do_timestep(None, None, None) == _lib.SS_ERR_INVALID_ARGUMENT
 
 
+def test_noalloc_refuses_more_rows_than_a_context_on_the_host():
+    """ss_sample_distribution_noalloc takes at most 2^32 - 1 rows, like
+    ss_create; the refusal comes before any device work (the pointers are
+    never dereferenced)."""
+    from stochasticsampling_gb300 import _lib
+    from stochasticsampling_gb300._lib import Box, Grid
+    L = _lib.load()
+    fake = ctypes.c_void_p(256)
+    for n in (0, 1 << 32):
+        rc = L.ss_sample_distribution_noalloc(ctypes.byref(Grid(4, 4, 1, 4, 1)), ctypes.byref(Box(1, 1, 1)),
+                                              fake, n, fake, None)
+        assert rc == _lib.SS_ERR_INVALID_ARGUMENT
+        assert "2^32-1" in _lib.last_error()
+
+
 def test_no_cpu_fallback_without_gpu():
     import torch
     if torch.cuda.is_available():

@@ -38,6 +38,11 @@ MEMBERS = [
 ]
 
 
+# flow after one step against the FP64 oracle: the FP32 binning moves a few
+# particles into a neighbouring bin, and the flow is built from those counts
+ENS_FLOW_TOL = 1e-2
+
+
 def _members(spec=MEMBERS):
     return [dict(grid=g, box=b, params=dict(p, number_of_particles=n, seed=s)) for g, b, p, n, s in spec]
 
@@ -95,6 +100,49 @@ def test_ensemble_matches_single_contexts():
         assert np.abs(ce - cs).sum() <= max(4, 4e-3 * nm), i
     for s in singles:
         s.close()
+    ens.close()
+
+
+def test_ensemble_one_step_against_oracle(oracle):
+    """Three members with uneven particle counts and grids, one ensemble step
+    against oracle.Simulation (the FP64 restatement of the reference step)
+    from the same rows, fed each member's own noise: the Philox stream of a
+    stand-alone mixed context with the member's seed (ss_noise), which the
+    ensemble draws for that member.  The mixed path's per-field bounds hold:
+    the initial histogram differs only for particles within FP32 rounding of
+    a bin edge, and the flow, positions and angles after the step are within
+    the FP32 bounds of tests/test_gpu_mixed.py."""
+    from test_gpu_parity import _pair
+    ss = _gpu()
+    spec = [MEMBERS[0], MEMBERS[2], MEMBERS[3]]
+    members = _members(spec)
+    rows = _rows(np.random.default_rng(17), members)
+    ens = ss.Ensemble(members)
+    ens.init(rows)
+    oracles = []
+    for i, (grid, box, params, n, seed) in enumerate(spec):
+        r = rows[ens.offsets[i]:ens.offsets[i + 1]]
+        g, o, st = _pair(oracle, (f"member{i}", grid, box, params, n, True), seed=seed, mixed=True)
+        g.init(r)
+        noise = g.noise(0)
+        g.close()
+        o.init(r)
+        h = oracle.histogram(st, o.particles()).ravel()
+        c = ens.get_counts(i).astype(np.float64)
+        assert c.sum() == n and np.abs(c - h).sum() <= 2e-3 * n, i
+        o.do_timestep(noise)
+        oracles.append(o)
+    ens.run(1)
+    for i, ((grid, box, params, n, seed), o) in enumerate(zip(spec, oracles)):
+        eu = rel_l2(ens.get_flow_field(i), o.flow().real)
+        ep, op = ens.get_particles(i), o.particles()
+        ex = rel_l2(ep[:, :2], op[:, :2])
+        ephi = float(np.sqrt(np.mean(_wrapdiff(ep[:, 3], op[:, 3], 2 * np.pi) ** 2)))
+        print(f"ensemble member {i} vs oracle: flow {eu:.3e} positions {ex:.3e} phi rms {ephi:.3e}")
+        assert eu < ENS_FLOW_TOL, (i, eu)
+        assert ex < 1e-6, (i, ex)
+        assert ephi < 1e-4, (i, ephi)
+        assert np.all(ep[:, 2] == 0.0) and np.all(ep[:, 4] == np.pi / 2)
     ens.close()
 
 

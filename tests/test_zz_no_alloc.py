@@ -1,7 +1,7 @@
 """ss_sample_distribution_noalloc, the entry point for callers that cannot
-allocate device memory at the point where they need a histogram (inside a
-stream capture, inside another library's loop where cudaFree's device-wide
-synchronisation is not allowed, or under a fixed memory budget).
+allocate device memory at the point where they need a histogram (a hook
+inside another library's loop, where cudaFree's device-wide synchronisation
+would stall that loop, or an application under a fixed memory budget).
 
 It must give the same distribution as the allocating path (ss_init +
 ss_get_distribution on a context) -- bit-exact, like every histogram here --
@@ -92,3 +92,20 @@ def test_noalloc_rejects_grids_beyond_its_scratch():
                                           None)
     assert rc == _lib.SS_ERR_INVALID_ARGUMENT
     assert "at most 2097152" in _lib.last_error()
+
+
+def test_noalloc_marks_a_non_finite_row_and_recovers():
+    """A row with a NaN coordinate (which ss_init refuses) is not counted and
+    turns every bin into NaN; the next call with finite rows is exact again."""
+    torch, ss, _lib, L = _setup()
+    rng = np.random.default_rng(9)
+    grid, box = (16, 12, 1, 8, 1), (8.0, 6.0, 1.0)
+    good = _cloud(rng, 20_000, box, True)
+    bad = good.copy()
+    bad[777, 3] = np.nan
+    assert np.isnan(_noalloc(torch, L, _lib, grid, box, bad)).all()
+    sim = ss.Simulation(grid=grid, box=box, params=dict(number_of_particles=good.shape[0]), quasi2d=True)
+    sim.init(good)
+    want = sim.get_distribution()
+    sim.close()
+    assert np.array_equal(_noalloc(torch, L, _lib, grid, box, good), want)
