@@ -39,6 +39,31 @@ WORKLOAD = "2-D production size, plain FP64: N=1e7, grid 128x128x1x32x1, box 40x
 TWOPI = 2 * np.pi
 
 
+def workload_config(n):
+    """The `config` object of the JSON line, identical in both arms."""
+    return {"workload": WORKLOAD, "particles": n, "grid": list(GRID), "box": list(BOX), **PARAMS,
+            "l2": "inputs larger than L2 (400 MB particle state per step)"}
+
+
+E2E_MIN_STEPS = 20
+
+
+def e2e_median(step, n, steps, world, dist):
+    """End-to-end throughput from `steps` host-timed calls of step(k) (each
+    synchronised), the median step time: returns (particle-steps/s,
+    median ms, steps)."""
+    import torch
+    times = []
+    for k in range(steps):
+        t0 = time.perf_counter()
+        step(k)
+        torch.cuda.synchronize()
+        times.append(1e3 * (time.perf_counter() - t0))
+    med = statistics.median(times)
+    value, ms = aggregate(med, n, 1, world, dist)
+    return value, ms, steps
+
+
 def c1_particles(n, seed=1):
     rng = np.random.default_rng(seed)
     L = BOX[0]
@@ -191,6 +216,7 @@ def run_reference(args, rank, world):
     rate, _ = cpu_step_rate(probe_n, 1, nthreads)
     budget_s = 150.0
     n_sample = int(min(N, max(100_000, rate * budget_s / max(1, args.steps + args.warmup))))
+    # the whole workload per step whenever the budget allows it (the GPU arm's config)
     from oracle import oracle as O2
     s = O2.make_settings(GRID, BOX, timestep=PARAMS["timestep"], trans_diff=PARAMS["trans_diffusion"],
                          rot_diff=PARAMS["rot_diffusion"], active=PARAMS["stress_active"], quasi2d=True)
@@ -210,7 +236,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC_NAME, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "particles_per_step": n_sample, "l2": "inputs larger than L2"},
+        "config": workload_config(n_sample),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -292,15 +318,14 @@ def measure_f32x2(args, stream, p0, params, world, dist, barrier):
     host_in[:] = sim.get_particles()
     for _ in range(2):
         sim.step_host(host_in, out=host_out)
-    e2e_steps = max(1, min(args.steps, 10))
     torch.cuda.synchronize()
     barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        sim.step_host(host_in, out=host_out)
-        host_in, host_out = host_out, host_in
-    torch.cuda.synchronize()
-    e2e = aggregate(1e3 * (time.perf_counter() - t0), N, e2e_steps, world, dist)[0]
+    bufs = [host_in, host_out]
+
+    def one(k):
+        sim.step_host(bufs[k % 2], out=bufs[1 - k % 2])
+
+    e2e, e2e_ms, e2e_steps = e2e_median(one, N, max(E2E_MIN_STEPS, min(args.steps, 50)), world, dist)
     # one step from identical state and noise in both modes
     state = sim.get_particles()
     ts = sim.get_timestep()
@@ -327,7 +352,7 @@ def measure_f32x2(args, stream, p0, params, world, dist, barrier):
                          "peak_source": peak_kind, "bytes_per_launch": upd_bytes, "avg_launch_ms": upd_ms},
             "stage_ms": stage_avg,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": N * 5 * 8, "d2h_bytes_per_step": N * 5 * 8,
-                    "steps": e2e_steps, "api": "ss_step_host, pinned"},
+                    "steps": e2e_steps, "median_ms_per_step": e2e_ms, "api": "ss_step_host, pinned"},
             "max_abs_dev_vs_fp64_one_step": {"x": float(d[:, 0].max()), "y": float(d[:, 1].max()),
                                              "phi": float(d[:, 3].max())}}
 
@@ -399,6 +424,62 @@ def measure_mixed(args, stream, p0, rank, world, dist, barrier, mode=True):
                          "kernel": "k_update_m", "peak_source": peak_kind, "bytes_per_launch": upd_bytes,
                          "avg_launch_ms": stage["update"]},
             "errors_vs_fp64_one_step": errors}
+
+
+# the reference's CPU-runnable 2-D case: box 10x10, grid 32x32x1x16x1,
+# 1e5 particles (uniform positions and phi), Dt 0.1, Dr 0.5, active stress
+# -1, dt 0.01, 100 steps, FP64
+C0_GRID = (32, 32, 1, 16, 1)
+C0_BOX = (10.0, 10.0, 1.0)
+C0_N = 100_000
+C0_STEPS = 100
+C0_PARAMS = dict(timestep=0.01, trans_diffusion=0.1, rot_diffusion=0.5, stress_active=-1.0)
+
+
+def measure_c0(stream, cpu=True):
+    """The small 2-D workload in full (100 steps of 1e5 particles): the FP64
+    GPU path (one CUDA graph per step) and, on the host cores, the oracle
+    (the FP64 C restatement of the reference step, OpenMP like the reference's
+    rayon loops)."""
+    import torch
+
+    import stochasticsampling_gb300 as ss
+    rng = np.random.default_rng(4)
+    p0 = np.column_stack([C0_BOX[0] * rng.random(C0_N), C0_BOX[1] * rng.random(C0_N), np.zeros(C0_N),
+                          TWOPI * rng.random(C0_N), np.full(C0_N, np.pi / 2)])
+    params = dict(C0_PARAMS, number_of_particles=C0_N, seed=1)
+    sim = ss.Simulation(grid=C0_GRID, box=C0_BOX, params=params, quasi2d=True, sort=False, stream=stream.cuda_stream)
+    sim.init(p0)
+    with torch.cuda.stream(stream):
+        sim.run(5)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.run(C0_STEPS)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+    sim.close()
+    out = {"workload": "2-D, box 10x10, grid 32x32x1x16x1, N=1e5, Dt 0.1, Dr 0.5, active -1, dt 0.01, 100 steps, FP64",
+           "gpu": {"value": C0_N * C0_STEPS / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / C0_STEPS,
+                   "note": "launch-bound: a few microseconds of work per kernel"}}
+    if cpu:
+        from oracle import oracle as O
+        nthreads = os.cpu_count() or 1
+        st = O.make_settings(C0_GRID, C0_BOX, timestep=C0_PARAMS["timestep"], trans_diff=C0_PARAMS["trans_diffusion"],
+                             rot_diff=C0_PARAMS["rot_diffusion"], active=C0_PARAMS["stress_active"], quasi2d=True,
+                             seed=1)
+        o = O.Simulation(st, C0_N, nthreads=nthreads)
+        o.init(p0)
+        t0 = time.perf_counter()
+        for _ in range(C0_STEPS):
+            o.do_timestep()
+        secs = time.perf_counter() - t0
+        out["cpu"] = {"value": C0_N * C0_STEPS / secs, "unit": UNIT, "ms_per_step": 1e3 * secs / C0_STEPS,
+                      "cores": nthreads, "kind": "port",
+                      "sample": f"all {C0_STEPS} steps, FP64 C restatement of do_timestep, OpenMP on {nthreads} "
+                                f"threads ({cpu_model()})"}
+    return out
 
 
 # 3-D workload with the dipolar solver: box 20^3, grid 64x64x64x16x8,
@@ -625,6 +706,8 @@ def run_gpu(args, rank, world, dist):
             res = measure_c2(args, stream, rank, world, dist, barrier)
         elif args.only == "denoised":
             res = measure_denoised(args, rank)
+        elif args.only == "c0":
+            res = measure_c0(stream, cpu=rank == 0)
         elif args.only == "f32x2":
             res = measure_f32x2(args, stream, p0, params, world, dist, barrier)
         else:
@@ -676,7 +759,7 @@ def run_gpu(args, rank, world, dist):
     host_in = torch.empty((N, 5), dtype=torch.float64, pin_memory=True).numpy()
     host_out = torch.empty((N, 5), dtype=torch.float64, pin_memory=True).numpy()
     host_in[:] = sim.get_particles()
-    e2e_steps = max(1, min(args.steps, 10))
+    e2e_steps = max(E2E_MIN_STEPS, min(args.steps, 50))
 
     def e2e_loop(fused):
         nonlocal host_in, host_out
@@ -695,15 +778,16 @@ def run_gpu(args, rank, world, dist):
         ts = sim.get_timestep()
         torch.cuda.synchronize()
         barrier()
-        t0 = time.perf_counter()
-        for k in range(e2e_steps):
+
+        def timed(k):
+            nonlocal host_in, host_out
             one(ts + k)
             host_in, host_out = host_out, host_in
-        torch.cuda.synchronize()
-        return aggregate(1e3 * (time.perf_counter() - t0), N, e2e_steps, world, dist)[0]
 
-    e2e_sep = e2e_loop(False)
-    e2e_value = e2e_loop(True)
+        return e2e_median(timed, N, e2e_steps, world, dist)
+
+    e2e_sep, e2e_sep_ms, _ = e2e_loop(False)
+    e2e_value, e2e_ms, _ = e2e_loop(True)
     sim.close()
     f32x2 = measure_f32x2(args, stream, p0, params, world, dist, barrier)
     mixed = None if args.no_mixed else measure_mixed(args, stream, p0, rank, world, dist, barrier)
@@ -711,6 +795,7 @@ def run_gpu(args, rank, world, dist):
     ensemble = None if args.no_ensemble else measure_ensemble(args, stream, rank, world, dist, barrier)
     c2 = None if args.no_c2 else measure_c2(args, stream, rank, world, dist, barrier)
     denoised = None if args.no_denoise else measure_denoised(args, rank)
+    c0 = measure_c0(stream, cpu=(rank == 0 and not args.no_cpu_baseline))
 
     if rank != 0:
         return
@@ -754,10 +839,10 @@ def run_gpu(args, rank, world, dist):
         "metric": METRIC_NAME, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "particles": N, "grid": list(GRID), "box": list(BOX), **PARAMS,
-                   "noise": "on-device Philox4x32-10", "execution": "CUDA graph per step, particles in input order (no counting sort)",
-                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
-                   "l2": "inputs larger than L2 (400 MB particle state per step)"},
+        "config": workload_config(N),
+        "execution": {"noise": "on-device Philox4x32-10",
+                      "graph": "CUDA graph per step, particles in input order (no counting sort)",
+                      "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": "k_update (fused Langevin step + next-step binning)",
                      "peak_source": peak_kind, "bytes_per_launch": upd_bytes, "avg_launch_ms": upd_ms,
@@ -769,8 +854,11 @@ def run_gpu(args, rank, world, dist):
         "sorted": sorted_line,
         "f32x2": f32x2,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N * 5 * 8, "d2h_bytes_per_step": N * 5 * 8,
-                "steps": e2e_steps, "api": "ss_step_host(host rows in, host rows out), pinned",
-                "separate_calls": {"value": e2e_sep, "api": "ss_resume(host) + ss_do_timestep + ss_get_particles(host)"}},
+                "steps": e2e_steps, "median_ms_per_step": e2e_ms,
+                "timing": "each step timed on the host (synchronised), median of the steps",
+                "api": "ss_step_host(host rows in, host rows out), pinned",
+                "separate_calls": {"value": e2e_sep, "median_ms_per_step": e2e_sep_ms,
+                                   "api": "ss_resume(host) + ss_do_timestep + ss_get_particles(host)"}},
         "gpu_launches": launches,
         "clocks": clk,
         "cpu_baseline": cpu,
@@ -778,6 +866,7 @@ def run_gpu(args, rank, world, dist):
         "mixed_fixed64": mixed_fixed,
         "ensemble": ensemble,
         "c2_3d_magnetic": c2,
+        "c0_small_2d": c0,
         "denoised": denoised,
     }
     print(json.dumps(line), flush=True)
@@ -797,7 +886,7 @@ def main():
     ap.add_argument("--denoise-pairs", type=int, default=1000)
     ap.add_argument("--denoise-epochs", type=int, default=1)
     ap.add_argument("--denoise-steps", type=int, default=400)
-    ap.add_argument("--only", choices=["mixed", "fixed64", "ensemble", "denoised", "c2", "f32x2"], default=None,
+    ap.add_argument("--only", choices=["mixed", "fixed64", "ensemble", "denoised", "c2", "f32x2", "c0"], default=None,
                     help="run one section alone (a smaller command for profiling); prints its JSON")
     ap.add_argument("--ensemble-members", type=int, default=64)
     ap.add_argument("--ensemble-config", default=None,

@@ -335,9 +335,19 @@ int ss_dn_set_params(ss_dn *dn, const float *host, uint64_t count);
 /* y = network(x), DEVICE arrays; returns after completion */
 int ss_dn_forward(ss_dn *dn, const float *x, float *y);
 /* batch samples x[batch][V], t[batch][V] (DEVICE): loss = mean over the batch
- * of mean_v (y - t)^2; with lr > 0 one Adam step (beta 0.9 / 0.999) on the
+ * of mean_v (y - t)^2 (plus the moment term of ss_dn_set_loss); with lr > 0 one Adam step (beta 0.9 / 0.999) on the
  * batch-mean gradient, with lr = 0 the loss only */
 int ss_dn_train(ss_dn *dn, const float *x, const float *t, uint32_t batch, float lr, double *loss);
+/* The training loss: w = 0 (the default) is the mean-square error above.
+ * w > 0 adds, per cell (x, y), w times the squared second angular harmonic
+ * of the residual r = y - t over phi, summed over cells and divided by the
+ * voxel count: mean_v r^2 + w sum_cells (c2^2 + s2^2) / V with c2 = sum_k r_k
+ * cos 2 phi_k, s2 = sum_k r_k sin 2 phi_k at the phi bin centres.  In the
+ * plane the flow depends on a cell's orientation distribution only through
+ * that harmonic (the Oseen projection removes the density's part), so the
+ * term weights the error that reaches the flow.  No counterpart in the
+ * reference (the denoiser is an extension). */
+int ss_dn_set_loss(ss_dn *dn, float moment_weight);
 /* the batch-mean gradient of that loss (host float[count]) without an update */
 int ss_dn_gradients(ss_dn *dn, const float *x, const float *t, uint32_t batch, float *grads, uint64_t count,
                     double *loss);

@@ -19,7 +19,7 @@ EXPORTS = [
     "ss_sample_distribution_noalloc", "ss_ensemble_create", "ss_ensemble_destroy", "ss_ensemble_init",
     "ss_ensemble_autotune", "ss_ensemble_set_config", "ss_ensemble_run", "ss_ensemble_synchronize", "ss_ensemble_get_particles",
     "ss_ensemble_get_counts", "ss_ensemble_get_flow_field", "ss_ensemble_info", "ss_dn_conv32", "ss_dn_create",
-    "ss_dn_destroy", "ss_dn_info", "ss_dn_get_params", "ss_dn_set_params", "ss_dn_forward", "ss_dn_train",
+    "ss_dn_destroy", "ss_dn_info", "ss_dn_set_loss", "ss_dn_get_params", "ss_dn_set_params", "ss_dn_forward", "ss_dn_train",
     "ss_dn_gradients", "ss_dn_sample_histogram", "ss_set_denoiser", "ss_fp64_rate", "ss_last_error", "ss_version",
 ]
 
@@ -144,6 +144,7 @@ def load(build_if_missing=True):
         "ss_dn_conv32": [vp, vp, vp, vp, vp, u32, u32, u32, u32, vp],
         "ss_dn_create": [u32, u32, u32, u64, vp, ctypes.POINTER(vp)],
         "ss_dn_destroy": [vp],
+        "ss_dn_set_loss": [vp, ctypes.c_float],
         "ss_dn_info": [vp, u64p, u64p],
         "ss_dn_get_params": [vp, ctypes.POINTER(ctypes.c_float), u64],
         "ss_dn_set_params": [vp, ctypes.POINTER(ctypes.c_float), u64],

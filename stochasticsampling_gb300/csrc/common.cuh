@@ -84,6 +84,8 @@ struct DevParams {
     int quasi2d;
     int bin_theta_half;  // the theta bin of pi/2 (every particle after a quasi2d step)
     int gather;        // 0 nearest cell, 1 trilinear, 2 trilinear with the z fraction from y
+    int hdim[3];       // half-spectrum shape of the real-to-complex transforms: the last axis of size > 1 halved
+    int nhalf;         // hdim[0] * hdim[1] * hdim[2]
     uint32_t mask;     // Langevin modifiers that can change the state
 };
 

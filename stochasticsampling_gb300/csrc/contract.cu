@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(kCTile) k_contract_x(const uint32_t *__restric
                                                        const double *__restrict__ factor,
                                                        const double *__restrict__ kern,
                                                        const double *__restrict__ lut, int lut_n, DevParams P,
-                                                       Staging S, double2 *__restrict__ fwd,
+                                                       Staging S, double *__restrict__ fwd,
                                                        double *__restrict__ table, int tstride,
                                                        uint32_t *__restrict__ cellcount) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -205,11 +205,11 @@ __global__ void __launch_bounds__(kCTile) k_contract_x(const uint32_t *__restric
     }
     if (STRESS) {
 #pragma unroll
-        for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = make_double2(sig[j], 0.0);
+        for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = sig[j];
     }
     if (MAG) {
 #pragma unroll
-        for (int j = 9; j < 12; ++j) fwd[(long long)j * nc + cell] = make_double2(sig[j], 0.0);
+        for (int j = 9; j < 12; ++j) fwd[(long long)j * nc + cell] = sig[j];
     }
     const double dens = (((double)csum / P.dist_den) * P.volume) * P.dthph;
     table[(long long)cell * tstride + T_DIFF] = sqrt(2.0 * P.dt * (P.Dt + P.volex * dens));
@@ -410,7 +410,7 @@ void contract_prepare() {
 
 void launch_contract_x(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kslice,
                        const double *factor, const double *kern, const double *lut, int lut_n, const DevParams &P,
-                       double2 *fwd, double *table, int tstride, uint32_t *cellcount) {
+                       double *fwd, double *table, int tstride, uint32_t *cellcount) {
     const Staging S = make_staging(P.nang);
     const size_t sm = smem_x(P.nang);
     const unsigned b = tiles(P.ncell);

@@ -557,6 +557,63 @@ __global__ void k_dn_loss(const float *__restrict__ y, const float *__restrict__
     }
 }
 
+// the loss with the angular-moment term: per cell (x, y) the residual
+// r = y - t over phi has the second harmonic c2 = sum_k r_k cos 2 phi_k,
+// s2 = sum_k r_k sin 2 phi_k (phi_k the bin centres).  In the plane the active
+// stress of a cell, and with it the flow, depends on the cell's orientation
+// distribution only through its density and this harmonic, and the Oseen
+// projection removes the density's part, so the flow error of a denoised
+// histogram is the error of this harmonic.  The loss is
+//     mean_v r^2 + w * sum_cells (c2^2 + s2^2) / V
+// (for white noise both terms are alike at w = 1), its gradient
+//     dy_k = 2 / V * (r_k + w (c2 cos 2 phi_k + s2 sin 2 phi_k)).
+// One thread per cell; the layout is [x][phi][y], so consecutive threads
+// read consecutive y.
+__global__ void k_dn_loss_moment(const float *__restrict__ y, const float *__restrict__ t, float *__restrict__ dy,
+                                 Dims d, float w, double *__restrict__ sums, float *__restrict__ db_out) {
+    extern __shared__ float cs[];  // cos 2 phi_k, then sin 2 phi_k
+    for (int k = threadIdx.x; k < d.np; k += blockDim.x) {
+        float sn, cn;
+        sincospif((2.f * (float)k + 1.f) * 2.f / (float)d.np, &sn, &cn);  // 2 phi_k / pi
+        cs[k] = cn;
+        cs[d.np + k] = sn;
+    }
+    __syncthreads();
+    const int ncell = d.nx * d.ny;
+    const float inv_v = 1.f / (float)((long long)ncell * d.np);
+    double l = 0.0, g = 0.0;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
+        const int x = c / d.ny, yy = c - x * d.ny;
+        const size_t base = (size_t)x * d.np * d.ny + yy;
+        float c2 = 0.f, s2 = 0.f;
+        for (int k = 0; k < d.np; ++k) {
+            const size_t v = base + (size_t)k * d.ny;
+            const float r = y[v] - t[v];
+            c2 = fmaf(cs[k], r, c2);
+            s2 = fmaf(cs[d.np + k], r, s2);
+        }
+        const float mc = w * c2, ms = w * s2;
+        for (int k = 0; k < d.np; ++k) {
+            const size_t v = base + (size_t)k * d.ny;
+            const float r = y[v] - t[v];
+            const float gv = 2.f * inv_v * (r + fmaf(mc, cs[k], ms * cs[d.np + k]));
+            dy[v] = gv;
+            l += (double)(r * r);
+            g += (double)gv;
+        }
+        l += (double)w * ((double)c2 * c2 + (double)s2 * s2);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        l += __shfl_xor_sync(0xffffffffu, l, o);
+        g += __shfl_xor_sync(0xffffffffu, g, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&sums[0], l * (double)inv_v);
+        if (db_out) atomicAdd(db_out, (float)g);
+    }
+}
+
 // backward of the output layer into its input: dZ3[u][c] = (sum_tap
 // w_out[tap][c] dy[nbr(u, 26 - tap)]) * (A3[u][c] > 0)
 __global__ void __launch_bounds__(128) k_dn_out_bwd(const float *__restrict__ dy, const float *__restrict__ P,
@@ -844,6 +901,7 @@ struct ss_dn {
     unsigned *err = nullptr;
     long long adam_t = 0;
     uint64_t launches = 0;
+    float moment_weight = 0.f;  // w of the angular-moment term of the loss (k_dn_loss_moment); 0: mean-square only
 };
 
 namespace {
@@ -919,7 +977,11 @@ void enqueue_forward(ss_dn *n, const float *x, float *y, cudaStream_t s) {
 void enqueue_backward(ss_dn *n, const float *t, const float *ya, cudaStream_t s, bool grads) {
     const unsigned b = (unsigned)((n->nvox + 127) / 128);
     transpose<true>(n, t, n->ta, s);
-    k_dn_loss<<<2 * n->sms, 256, 0, s>>>(ya, n->ta, n->dy, n->nvox, n->sums, grads ? n->G + kOffBout : nullptr);
+    if (n->moment_weight > 0.f)
+        k_dn_loss_moment<<<2 * n->sms, 128, 2 * n->d.np * sizeof(float), s>>>(
+            ya, n->ta, n->dy, n->d, n->moment_weight, n->sums, grads ? n->G + kOffBout : nullptr);
+    else
+        k_dn_loss<<<2 * n->sms, 256, 0, s>>>(ya, n->ta, n->dy, n->nvox, n->sums, grads ? n->G + kOffBout : nullptr);
     n->launches += 2;
     if (!grads) return;
     const dim3 wg(kTaps, (unsigned)(n->sms > 0 ? (4 * n->sms + kTaps - 1) / kTaps : 8));
@@ -1059,6 +1121,13 @@ int ss_dn_forward(ss_dn *n, const float *x, float *y) {
     enqueue_forward(n, x, y, n->stream);
     DCK(cudaGetLastError());
     return check_err(n);
+}
+
+int ss_dn_set_loss(ss_dn *n, float moment_weight) {
+    if (!n || !(moment_weight >= 0.f) || !std::isfinite(moment_weight))
+        return dnfail(SS_ERR_INVALID_ARGUMENT, "ss_dn_set_loss: null network or moment weight not finite and >= 0");
+    n->moment_weight = moment_weight;
+    return SS_OK;
 }
 
 // batch samples [batch][V] (DEVICE): loss averaged over the batch; with

@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(64) k_contract(const uint32_t *__restrict__ co
                                                  const double *__restrict__ dist,
                                                  const double *__restrict__ lut, int lut_n,
                                                  const double *__restrict__ kern, DevParams P,
-                                                 double2 *__restrict__ fwd, double *__restrict__ table,
+                                                 double *__restrict__ fwd, double *__restrict__ table,
                                                  int tstride, uint32_t *__restrict__ cellcount) {
     extern __shared__ double sk[];
     const int na = P.nang;
@@ -262,11 +262,11 @@ __global__ void __launch_bounds__(64) k_contract(const uint32_t *__restrict__ co
     const int nc = P.ncell;
     if (STRESS) {
 #pragma unroll
-        for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = make_double2(acc[j] * P.measure, 0.0);
+        for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = acc[j] * P.measure;
     }
     if (MAG) {
 #pragma unroll
-        for (int j = 0; j < 3; ++j) fwd[(long long)(9 + j) * nc + cell] = make_double2(acc[9 + j] * P.measure, 0.0);
+        for (int j = 0; j < 3; ++j) fwd[(long long)(9 + j) * nc + cell] = acc[9 + j] * P.measure;
     }
     double dens = acc[12] * P.dthph;
     double volex = P.volex * dens;
@@ -278,75 +278,149 @@ __global__ void __launch_bounds__(64) k_contract(const uint32_t *__restrict__ co
 // ------------------------------------------------------------------------
 // k space: SpectralSolver::fft_mean_flow_field (spectral_solver.rs:133-189),
 // MagneticSolver::fft_mean_magnetic_field (magnetic_solver.rs:71-95) and both
-// update_gradient (spectral_solver.rs:192-229, magnetic_solver.rs:98-135).
-// fwd: [0..9) sigma_k, [9..12) P_k.  inv: [0..9) G_k = i k_a u_b, [9..12) u_k,
-// [12..21) grad B_k, [21..24) B_k.  Complex products with k (imaginary part
-// zero) reduce exactly to real scalings.
+// update_gradient (spectral_solver.rs:192-229, magnetic_solver.rs:98-135), on
+// the half spectrum of the real-to-complex transforms.
+//
+// The reference applies these operators to the full spectrum of a
+// complex-to-complex FFT of each real field and keeps the real part of the
+// complex inverse (simulation/mod.rs:399-414).  With X(k) the operator's
+// output, Re ifft(X) is the complex-to-real inverse of the Hermitian part
+// H(k) = (X(k) + conj X(-k)) / 2, and Im ifft(X) that of
+// (X(k) - conj X(-k)) / 2i.  X(-k) is the operator at the mirrored wave
+// vector with the spectrum conj sigma(k) (the spectrum of a real field); the
+// mirror negates every component of k except a Nyquist one (index n/2 of an
+// even n, whose wave number -n/2 is its own mirror).  With no Nyquist index
+// the operators give conj X(-k) = X(k) exactly (every operation is odd or
+// even in k), so H = X and the anti-Hermitian part is zero: only bins on a
+// Nyquist plane evaluate the operators twice.
+//
+// fwd: [0..9) sigma_k, [9..12) P_k.  out: [0..9) G_k = i k_a u_b, [9..12) u_k,
+// [12..21) grad B_k, [21..24) B_k, all [comp][half bin].  Complex products
+// with k (imaginary part zero) reduce exactly to real scalings.
 // ------------------------------------------------------------------------
-template <bool FLOW, bool MAG>
-__global__ void k_kspace(const double2 *__restrict__ fwd, double2 *__restrict__ inv, DevParams P,
-                         double screening, double stepx, double stepy, double stepz) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nc = P.ncell;
-    if (c >= nc) return;
-    int iz = c % P.gz;
-    int iy = (c / P.gz) % P.gy;
-    int ix = c / (P.gz * P.gy);
-    double k[3] = {kval(ix, P.gx, stepx), kval(iy, P.gy, stepy), kval(iz, P.gz, stepz)};
+__device__ __forceinline__ void flow_ops(const double k[3], const double kn[3], double fac, const double2 *sig,
+                                         double2 *o) {
+    double2 sg[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const double2 a0 = sig[3 * r + 0], a1 = sig[3 * r + 1], a2 = sig[3 * r + 2];
+        sg[r].x = (a0.x * k[0] + a1.x * k[1]) + a2.x * k[2];
+        sg[r].y = (a0.y * k[0] + a1.y * k[1]) + a2.y * k[2];
+    }
+    const double ksr = (kn[0] * sg[0].x + kn[1] * sg[1].x) + kn[2] * sg[2].x;
+    const double ksi = (kn[0] * sg[0].y + kn[1] * sg[1].y) + kn[2] * sg[2].y;
+    double2 u[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const double tr = (sg[r].x - kn[r] * ksr) * fac;
+        const double ti = (sg[r].y - kn[r] * ksi) * fac;
+        u[r] = make_double2(-ti, tr);  // times i
+        o[9 + r] = u[r];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) o[3 * a + b] = make_double2(-(k[a] * u[b].y), k[a] * u[b].x);
+}
+
+__device__ __forceinline__ void mag_ops(const double k[3], const double kn[3], double norm, const double2 *p,
+                                        double2 *o) {
+    const double dr = (kn[0] * p[0].x + kn[1] * p[1].x) + kn[2] * p[2].x;
+    const double di = (kn[0] * p[0].y + kn[1] * p[1].y) + kn[2] * p[2].y;
+    double2 b[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        b[r] = make_double2((p[r].x - kn[r] * dr) / norm, (p[r].y - kn[r] * di) / norm);
+        o[9 + r] = b[r];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb) o[3 * a + bb] = make_double2(-(k[a] * b[bb].y), k[a] * b[bb].x);
+}
+
+// ANTI: the anti-Hermitian part (the imaginary parts of the reference's
+// complex fields) instead of the Hermitian one
+template <bool FLOW, bool MAG, bool ANTI>
+__global__ void k_kspace(const double2 *__restrict__ fwd, double2 *__restrict__ out, DevParams P, double screening,
+                         double stepx, double stepy, double stepz) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nh = P.nhalf;
+    if (h >= nh) return;
+    const int iz = h % P.hdim[2];
+    const int iy = (h / P.hdim[2]) % P.hdim[1];
+    const int ix = h / (P.hdim[2] * P.hdim[1]);
+    const double k[3] = {kval(ix, P.gx, stepx), kval(iy, P.gy, stepy), kval(iz, P.gz, stepz)};
+    const bool nyq[3] = {(P.gx & 1) == 0 && 2 * ix == P.gx, (P.gy & 1) == 0 && 2 * iy == P.gy,
+                         (P.gz & 1) == 0 && 2 * iz == P.gz};
+    const bool mirror = nyq[0] || nyq[1] || nyq[2];
+    const bool kzero = (ix | iy | iz) == 0;
     // |k|^2 = ((0 + kx^2) + ky^2) + kz^2 (fft_helper.rs:80-82)
     double s = (k[0] * k[0] + k[1] * k[1]);
     s = s + k[2] * k[2];
     // 1/|k|^2 via num-complex's real/complex division: s / (s*s); 1/|k| for k-hat;
     // both zero at k = 0 (fft_helper.rs:84-85, 96-97)
-    double ik2 = (c == 0) ? 0.0 : s / (s * s);
-    double inrm = (c == 0) ? 0.0 : 1.0 / sqrt(s);
-    double kn[3] = {k[0] * inrm, k[1] * inrm, k[2] * inrm};
-    const double norm = (double)nc;
+    const double ik2 = kzero ? 0.0 : s / (s * s);
+    const double inrm = kzero ? 0.0 : 1.0 / sqrt(s);
+    const double kn[3] = {k[0] * inrm, k[1] * inrm, k[2] * inrm};
+    const double km[3] = {nyq[0] ? k[0] : -k[0], nyq[1] ? k[1] : -k[1], nyq[2] ? k[2] : -k[2]};
+    const double knm[3] = {km[0] * inrm, km[1] * inrm, km[2] * inrm};
+    const double norm = (double)P.ncell;
+    auto emit = [&](int c0, const double2 *X, const double2 *Xm) {
+#pragma unroll
+        for (int j = 0; j < 12; ++j) {
+            double2 v;
+            if (!mirror) {
+                v = ANTI ? make_double2(0.0, 0.0) : X[j];
+            } else if (ANTI) {  // (X - conj Xm) / 2i
+                v = make_double2((X[j].y + Xm[j].y) * 0.5, -(X[j].x - Xm[j].x) * 0.5);
+            } else {  // (X + conj Xm) / 2
+                v = make_double2((X[j].x + Xm[j].x) * 0.5, (X[j].y - Xm[j].y) * 0.5);
+            }
+            out[(long long)(c0 + j) * nh + h] = v;
+        }
+    };
     if (FLOW) {
-        double2 sg[3];
+        double2 sig[9], X[12], Xm[12];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            double2 a0 = fwd[(long long)(3 * r + 0) * nc + c];
-            double2 a1 = fwd[(long long)(3 * r + 1) * nc + c];
-            double2 a2 = fwd[(long long)(3 * r + 2) * nc + c];
-            sg[r].x = (a0.x * k[0] + a1.x * k[1]) + a2.x * k[2];
-            sg[r].y = (a0.y * k[0] + a1.y * k[1]) + a2.y * k[2];
+        for (int j = 0; j < 9; ++j) sig[j] = fwd[(long long)j * nh + h];
+        const double fac = (ik2 + screening) / norm;
+        flow_ops(k, kn, fac, sig, X);
+        if (mirror) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) sig[j].y = -sig[j].y;
+            flow_ops(km, knm, fac, sig, Xm);
         }
-        double ksr = (kn[0] * sg[0].x + kn[1] * sg[1].x) + kn[2] * sg[2].x;
-        double ksi = (kn[0] * sg[0].y + kn[1] * sg[1].y) + kn[2] * sg[2].y;
-        double fac = (ik2 + screening) / norm;
-        double2 u[3];
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            double tr = (sg[r].x - kn[r] * ksr) * fac;
-            double ti = (sg[r].y - kn[r] * ksi) * fac;
-            u[r] = make_double2(-ti, tr);  // times i
-            inv[(long long)(9 + r) * nc + c] = u[r];
-        }
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = 0; b < 3; ++b)
-                inv[(long long)(3 * a + b) * nc + c] = make_double2(-(k[a] * u[b].y), k[a] * u[b].x);
+        emit(0, X, Xm);
     }
     if (MAG) {
-        double2 p[3];
+        double2 pol[3], X[12], Xm[12];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) p[r] = fwd[(long long)(9 + r) * nc + c];
-        double dr = (kn[0] * p[0].x + kn[1] * p[1].x) + kn[2] * p[2].x;
-        double di = (kn[0] * p[0].y + kn[1] * p[1].y) + kn[2] * p[2].y;
-        double2 b[3];
+        for (int j = 0; j < 3; ++j) pol[j] = fwd[(long long)(9 + j) * nh + h];
+        mag_ops(k, kn, norm, pol, X);
+        if (mirror) {
 #pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            b[r] = make_double2((p[r].x - kn[r] * dr) / norm, (p[r].y - kn[r] * di) / norm);
-            inv[(long long)(21 + r) * nc + c] = b[r];
+            for (int j = 0; j < 3; ++j) pol[j].y = -pol[j].y;
+            mag_ops(km, knm, norm, pol, Xm);
         }
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int bb = 0; bb < 3; ++bb)
-                inv[(long long)(12 + 3 * a + bb) * nc + c] = make_double2(-(k[a] * b[bb].y), k[a] * b[bb].x);
+        emit(12, X, Xm);
     }
+}
+
+// real <-> complex copies of a one-cell grid (no axis to transform)
+__global__ void k_real_to_complex(const double *__restrict__ src, int count, double2 *__restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) dst[i] = make_double2(src[i], 0.0);
+}
+__global__ void k_complex_to_real(const double2 *__restrict__ src, int count, double *__restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) dst[i] = src[i].x;
+}
+// the reference's complex field [comp][cell] from its real and imaginary parts
+__global__ void k_combine_complex(const double *__restrict__ re, const double *__restrict__ im, long long count,
+                                  double2 *__restrict__ dst) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < count) dst[i] = make_double2(re[i], im[i]);
 }
 
 // ------------------------------------------------------------------------
@@ -365,7 +439,7 @@ __device__ __forceinline__ void put_entry(double *row, int k, double v, bool pai
 }
 
 template <bool FLOW, bool MAG>
-__global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__restrict__ table, int tstride,
+__global__ void k_table(const double *__restrict__ inv, DevParams P, double *__restrict__ table, int tstride,
                         double *__restrict__ ctab) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     const int nc = P.ncell;
@@ -378,9 +452,9 @@ __global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__
     if (FLOW) {
         double g[9], u[3];
 #pragma unroll
-        for (int j = 0; j < 9; ++j) g[j] = inv[(long long)j * nc + c].x;
+        for (int j = 0; j < 9; ++j) g[j] = inv[(long long)j * nc + c];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) u[r] = inv[(long long)(9 + r) * nc + c].x;
+        for (int r = 0; r < 3; ++r) u[r] = inv[(long long)(9 + r) * nc + c];
         const double w01 = (g[1] - g[3]) * 0.5, w02 = (g[2] - g[6]) * 0.5, w12 = (g[5] - g[7]) * 0.5;
         const double e00 = (g[0] + g[0]) * 0.5, e01 = (g[1] + g[3]) * 0.5, e02 = (g[2] + g[6]) * 0.5;
         const double e11 = (g[4] + g[4]) * 0.5, e12 = (g[5] + g[7]) * 0.5, e22 = (g[8] + g[8]) * 0.5;
@@ -412,9 +486,9 @@ __global__ void k_table(const double2 *__restrict__ inv, DevParams P, double *__
     }
     if (MAG) {
 #pragma unroll
-        for (int r = 0; r < 3; ++r) put_entry(row, T_B + r, inv[(long long)(21 + r) * nc + c].x * P.mdd, pairs);
+        for (int r = 0; r < 3; ++r) put_entry(row, T_B + r, inv[(long long)(21 + r) * nc + c] * P.mdd, pairs);
 #pragma unroll
-        for (int j = 0; j < 9; ++j) put_entry(row, T_GB + j, inv[(long long)(12 + j) * nc + c].x, pairs);
+        for (int j = 0; j < 9; ++j) put_entry(row, T_GB + j, inv[(long long)(12 + j) * nc + c], pairs);
     }
 }
 
@@ -803,7 +877,7 @@ void launch_counts_to_dist(cudaStream_t s, const uint32_t *counts, const DevPara
 }
 
 void launch_contract(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const double *dist,
-                     const double *lut, int lut_n, const double *kern, const DevParams &P, double2 *fwd,
+                     const double *lut, int lut_n, const double *kern, const DevParams &P, double *fwd,
                      double *table, int tstride, uint32_t *cellcount) {
     unsigned blocks = nblocks((unsigned long long)P.ncell, 64);
     const size_t smem = 12ull * P.nang * sizeof(double);
@@ -825,16 +899,32 @@ void launch_contract(cudaStream_t s, bool stress, bool mag, const uint32_t *coun
 #undef SS_CONTRACT
 }
 
-void launch_kspace(cudaStream_t s, bool flow, bool mag, const double2 *fwd, double2 *inv, const DevParams &P,
-                   double screening) {
+void launch_kspace(cudaStream_t s, bool flow, bool mag, bool anti, const double2 *fwd, double2 *inv,
+                   const DevParams &P, double screening) {
     double sx = kTwoPi / P.bx, sy = kTwoPi / P.by, sz = kTwoPi / P.bz;
-    unsigned b = nblocks(P.ncell, 128);
-    if (flow && mag) k_kspace<true, true><<<b, 128, 0, s>>>(fwd, inv, P, screening, sx, sy, sz);
-    else if (flow) k_kspace<true, false><<<b, 128, 0, s>>>(fwd, inv, P, screening, sx, sy, sz);
-    else k_kspace<false, true><<<b, 128, 0, s>>>(fwd, inv, P, screening, sx, sy, sz);
+    unsigned b = nblocks(P.nhalf, 128);
+#define SS_KS(F, M)                                                                   \
+    do {                                                                              \
+        if (anti) k_kspace<F, M, true><<<b, 128, 0, s>>>(fwd, inv, P, screening, sx, sy, sz); \
+        else k_kspace<F, M, false><<<b, 128, 0, s>>>(fwd, inv, P, screening, sx, sy, sz);     \
+    } while (0)
+    if (flow && mag) SS_KS(true, true);
+    else if (flow) SS_KS(true, false);
+    else SS_KS(false, true);
+#undef SS_KS
 }
 
-void launch_table(cudaStream_t s, bool flow, bool mag, const double2 *inv, const DevParams &P, double *table,
+void launch_real_to_complex(cudaStream_t s, const double *src, int count, double2 *dst) {
+    if (count > 0) k_real_to_complex<<<nblocks(count, 128), 128, 0, s>>>(src, count, dst);
+}
+void launch_complex_to_real(cudaStream_t s, const double2 *src, int count, double *dst) {
+    if (count > 0) k_complex_to_real<<<nblocks(count, 128), 128, 0, s>>>(src, count, dst);
+}
+void launch_combine_complex(cudaStream_t s, const double *re, const double *im, long long count, double2 *dst) {
+    if (count > 0) k_combine_complex<<<nblocks(count, 256), 256, 0, s>>>(re, im, count, dst);
+}
+
+void launch_table(cudaStream_t s, bool flow, bool mag, const double *inv, const DevParams &P, double *table,
                   int tstride, double *ctab) {
     unsigned b = nblocks(P.ncell, 128);
     if (flow && mag) k_table<true, true><<<b, 128, 0, s>>>(inv, P, table, tstride, ctab);

@@ -25,14 +25,15 @@ void launch_sort_rows(cudaStream_t s, const double *aos, unsigned long long n, c
 void launch_ingest_bin(cudaStream_t s, bool canon, const double *aos, unsigned long long n, const DevParams &P,
                        double *const xs[5], uint32_t *id, uint32_t *key, uint32_t *counts, uint32_t *err);
 void launch_counts_to_dist(cudaStream_t s, const uint32_t *counts, const DevParams &P, double *dist);
+// the contraction of a distribution (or of counts): real fields fwd [12][ncell]
 void launch_contract(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const double *dist,
-                     const double *lut, int lut_n, const double *kern, const DevParams &P, double2 *fwd,
+                     const double *lut, int lut_n, const double *kern, const DevParams &P, double *fwd,
                      double *table, int tstride, uint32_t *cellcount);
 // the FP64 contraction of a histogram (contract.cu): kslice, factor from
 // kernel_slices; kern and lut serve cells of more than 2^12 particles
 void launch_contract_x(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kslice,
                        const double *factor, const double *kern, const double *lut, int lut_n, const DevParams &P,
-                       double2 *fwd, double *table, int tstride, uint32_t *cellcount);
+                       double *fwd, double *table, int tstride, uint32_t *cellcount);
 // host: the angle kernels K [12][na] as four 12-bit integer slices per entry,
 // slices [na][48] (component j, slice s at 4 j + s), and per component the
 // factor 2^(E_j - 48) * measure_v_over_d that turns the combined slice sums
@@ -41,9 +42,16 @@ void kernel_slices(const std::vector<double> &K, int na, double measure_v_over_d
                    std::vector<double> &factor);
 // shared-memory limits of the contraction kernels on the current device
 void contract_prepare();
-void launch_kspace(cudaStream_t s, bool flow, bool mag, const double2 *fwd, double2 *inv, const DevParams &P,
-                   double screening);
-void launch_table(cudaStream_t s, bool flow, bool mag, const double2 *inv, const DevParams &P, double *table,
+// the k-space operators on the half spectrum (fwd [12][nhalf] -> inv
+// [24][nhalf]): their Hermitian part, or with anti the anti-Hermitian part
+// (the imaginary parts of the reference's complex fields)
+void launch_kspace(cudaStream_t s, bool flow, bool mag, bool anti, const double2 *fwd, double2 *inv,
+                   const DevParams &P, double screening);
+void launch_real_to_complex(cudaStream_t s, const double *src, int count, double2 *dst);
+void launch_complex_to_real(cudaStream_t s, const double2 *src, int count, double *dst);
+void launch_combine_complex(cudaStream_t s, const double *re, const double *im, long long count, double2 *dst);
+// the per-cell field rows from the real fields inv [24][ncell]
+void launch_table(cudaStream_t s, bool flow, bool mag, const double *inv, const DevParams &P, double *table,
                   int tstride, double *ctab);
 // canon: quasi2d with every particle in the canonical state (z = 0, theta = pi/2);
 // ctab: the canonical table of the step (k_table), or null

@@ -61,11 +61,16 @@ struct ss_ctx {
     int pcur = 0, ccur = 0, dist_idx = 0;
     bool fields_mag_valid = false;  // inverse buffer holds B of the last solve
     bool solved = false;            // a step ran since the last init
+    double screening_last = 0.0;    // the screening of the last flow solve (for the complex getters)
 
     double *px[2][5] = {};
     uint32_t *key[2] = {}, *pid[2] = {};
     uint32_t *counts[2] = {};
-    double2 *fwd = nullptr, *inv = nullptr;
+    // FP64 field solve: real fields -> half spectra -> real fields
+    double *fr = nullptr;                   // contraction output, [12][ncell] real
+    double2 *fwd = nullptr, *invh = nullptr;  // half spectra [12][nhalf], [24][nhalf]
+    double *ir = nullptr;                   // the step's real fields [24][ncell] (the table's input)
+    double2 *inv = nullptr;  // complex fields [24][ncell] for the getters (FP64: on demand; mixed: widened)
     double *table = nullptr;
     double *ctab = nullptr;  // canonical quasi-2-D rows (CT_*), FP64 quasi2d contexts
     uint32_t *cellcount = nullptr, *cursor = nullptr;
@@ -97,7 +102,7 @@ struct ss_ctx {
     bool wide_valid = false;  // inv (FP64) holds the widened mixed fields
     std::map<int, cufftHandle> plans_c;
 
-    std::map<int, cufftHandle> plans;
+    std::map<int, cufftHandle> plans;  // key: batch * 4 + kind (0 Z2Z, 1 D2Z, 2 Z2D)
     int fft_rank = 0;
     int fft_n[3] = {1, 1, 1};
 
@@ -216,27 +221,50 @@ void ss::build_angle_kernels(const ss_grid &grid, const ss_params &prm, std::vec
 // spectral_solver.rs:44-68 and magnetic_solver.rs:38-52).  Axes of length 1
 // are dropped: they do not change the memory layout of [comp][x][y][z].
 // ---------------------------------------------------------------------------
-static int get_plan(ss_ctx *c, int batch, cufftHandle *out) {
-    auto it = c->plans.find(batch);
+// real-to-complex (D2Z) and complex-to-real (Z2D) plans, out of place: the
+// real fields [batch][ncell] and their half spectra [batch][nhalf]
+static int get_plan(ss_ctx *c, int batch, int kind, cufftHandle *out) {
+    const int key = batch * 4 + kind;
+    auto it = c->plans.find(key);
     if (it != c->plans.end()) {
         *out = it->second;
         return SS_OK;
     }
     cufftHandle h;
-    int nc = c->P.ncell;
-    CKF(cufftPlanMany(&h, c->fft_rank, c->fft_n, nullptr, 1, nc, nullptr, 1, nc, CUFFT_Z2Z, batch));
+    const int nc = c->P.ncell, nh = c->P.nhalf;
+    if (kind == 1)
+        CKF(cufftPlanMany(&h, c->fft_rank, c->fft_n, nullptr, 1, nc, nullptr, 1, nh, CUFFT_D2Z, batch));
+    else
+        CKF(cufftPlanMany(&h, c->fft_rank, c->fft_n, nullptr, 1, nh, nullptr, 1, nc, CUFFT_Z2D, batch));
     CKF(cufftSetStream(h, c->stream));
-    c->plans[batch] = h;
+    c->plans[key] = h;
     *out = h;
     return SS_OK;
 }
 
-static int fft(ss_ctx *c, double2 *data, int batch, int dir) {
-    if (c->fft_rank == 0 || batch == 0) return SS_OK;  // 1-cell grid: the DFT is the identity
+// forward: real fields src [batch][ncell] -> half spectra dst [batch][nhalf]
+static int fft_r2c(ss_ctx *c, const double *src, double2 *dst, int batch) {
+    if (batch == 0) return SS_OK;
+    if (c->fft_rank == 0) {  // 1-cell grid: the DFT is the identity
+        launch_real_to_complex(c->stream, src, batch, dst);
+        return check_launch(c, "real_to_complex");
+    }
     cufftHandle h = 0;
-    CKR(get_plan(c, batch, &h));
-    CKF(cufftExecZ2Z(h, reinterpret_cast<cufftDoubleComplex *>(data), reinterpret_cast<cufftDoubleComplex *>(data),
-                     dir));
+    CKR(get_plan(c, batch, 1, &h));
+    CKF(cufftExecD2Z(h, const_cast<cufftDoubleReal *>(src), reinterpret_cast<cufftDoubleComplex *>(dst)));
+    return SS_OK;
+}
+
+// inverse: half spectra src [batch][nhalf] (overwritten) -> real fields dst [batch][ncell]
+static int fft_c2r(ss_ctx *c, double2 *src, double *dst, int batch) {
+    if (batch == 0) return SS_OK;
+    if (c->fft_rank == 0) {
+        launch_complex_to_real(c->stream, src, batch, dst);
+        return check_launch(c, "complex_to_real");
+    }
+    cufftHandle h = 0;
+    CKR(get_plan(c, batch, 2, &h));
+    CKF(cufftExecZ2D(h, reinterpret_cast<cufftDoubleComplex *>(src), dst));
     return SS_OK;
 }
 
@@ -278,10 +306,10 @@ static int enqueue_solve(ss_ctx *c, bool flow, bool mag, const uint32_t *counts,
     const int ts = (c->mag_step || c->P.gather) ? TABLE_STRIDE_MAG : TABLE_STRIDE;
     mark(c, 0);
     if (dist)
-        launch_contract(c->stream, flow, mag, counts, dist, c->lut, kLutN, c->kern, c->P, c->fwd, c->table, ts,
+        launch_contract(c->stream, flow, mag, counts, dist, c->lut, kLutN, c->kern, c->P, c->fr, c->table, ts,
                         c->cellcount);
     else
-        launch_contract_x(c->stream, flow, mag, counts, c->kslice, c->kfactor, c->kern, c->lut, kLutN, c->P, c->fwd,
+        launch_contract_x(c->stream, flow, mag, counts, c->kslice, c->kfactor, c->kern, c->lut, kLutN, c->P, c->fr,
                           c->table, ts, c->cellcount);
     ++*nl;
     CKR(check_launch(c, "contract"));
@@ -294,22 +322,24 @@ static int enqueue_solve(ss_ctx *c, bool flow, bool mag, const uint32_t *counts,
         CKR(check_launch(c, "sort"));
     }
     mark(c, 1);
-    if (flow && mag) CKR(fft(c, c->fwd, 12, CUFFT_FORWARD));
-    else if (flow) CKR(fft(c, c->fwd, 9, CUFFT_FORWARD));
-    else CKR(fft(c, c->fwd + 9ll * c->P.ncell, 3, CUFFT_FORWARD));
+    const long long nc = c->P.ncell, nh = c->P.nhalf;
+    if (flow && mag) CKR(fft_r2c(c, c->fr, c->fwd, 12));
+    else if (flow) CKR(fft_r2c(c, c->fr, c->fwd, 9));
+    else CKR(fft_r2c(c, c->fr + 9 * nc, c->fwd + 9 * nh, 3));
     mark(c, 2);
-    launch_kspace(c->stream, flow, mag, c->fwd, c->inv, c->P, screening);
+    launch_kspace(c->stream, flow, mag, false, c->fwd, c->invh, c->P, screening);
     ++*nl;
     CKR(check_launch(c, "kspace"));
     mark(c, 3);
-    if (flow && mag) CKR(fft(c, c->inv, 24, CUFFT_INVERSE));
-    else if (flow) CKR(fft(c, c->inv, 12, CUFFT_INVERSE));
-    else CKR(fft(c, c->inv + 12ll * c->P.ncell, 12, CUFFT_INVERSE));
+    if (flow && mag) CKR(fft_c2r(c, c->invh, c->ir, 24));
+    else if (flow) CKR(fft_c2r(c, c->invh, c->ir, 12));
+    else CKR(fft_c2r(c, c->invh + 12 * nh, c->ir + 12 * nc, 12));
+    if (flow) c->screening_last = screening;
     mark(c, 4);
     // the table has rows for the dipolar terms only when the step uses them
     const bool table_mag = mag && c->mag_step;
     if (flow || table_mag) {
-        launch_table(c->stream, flow, table_mag, c->inv, c->P, c->table, ts,
+        launch_table(c->stream, flow, table_mag, c->ir, c->P, c->table, ts,
                      (flow && !table_mag && !c->P.gather) ? c->ctab : nullptr);
         ++*nl;
         CKR(check_launch(c, "table"));
@@ -496,7 +526,7 @@ static void destroy_impl(ss_ctx *c) {
         cudaFree(c->pid[b]);
         cudaFree(c->counts[b]);
     }
-    cudaFree(c->fwd); cudaFree(c->inv); cudaFree(c->table); cudaFree(c->ctab); cudaFree(c->cellcount); cudaFree(c->cursor);
+    cudaFree(c->fr); cudaFree(c->fwd); cudaFree(c->invh); cudaFree(c->ir); cudaFree(c->inv); cudaFree(c->table); cudaFree(c->ctab); cudaFree(c->cellcount); cudaFree(c->cursor);
     cudaFree(c->kern); cudaFree(c->lut); cudaFree(c->staging); cudaFree(c->noise_dev); cudaFree(c->dist_dev);
     cudaFree(c->realbuf); cudaFree(c->staging_sorted); cudaFree(c->d_step); cudaFree(c->d_err); cudaFree(c->d_scan); cudaFree(c->d_halfpi);
     for (auto &kv : c->plans_c) cufftDestroy(kv.second);
@@ -675,12 +705,20 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
         M.mask = mask;
     }
 
-    // FFT geometry: drop axes of length 1
+    // FFT geometry: drop axes of length 1; the real-to-complex transforms
+    // halve the last remaining axis
     {
         int dims[3] = {P.gx, P.gy, P.gz}, r = 0;
         for (int k = 0; k < 3; ++k)
             if (dims[k] > 1) c->fft_n[r++] = dims[k];
         c->fft_rank = r;
+        for (int k = 2; k >= 0; --k)
+            if (dims[k] > 1) {
+                dims[k] = dims[k] / 2 + 1;
+                break;
+            }
+        for (int k = 0; k < 3; ++k) P.hdim[k] = dims[k];
+        P.nhalf = dims[0] * dims[1] * dims[2];
     }
 
     auto alloc = [&](void **p, size_t bytes) -> int {
@@ -700,7 +738,13 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
         if (rc == SS_OK) rc = alloc((void **)&c->pid[b], N * sizeof(uint32_t));
     }
     for (int b = 0; b < 2 && rc == SS_OK; ++b) rc = alloc((void **)&c->counts[b], (size_t)P.nbins * sizeof(uint32_t));
-    if (rc == SS_OK) rc = alloc((void **)&c->fwd, 12 * ncell * sizeof(double2));
+    const size_t nhalf = (size_t)P.nhalf;
+    if (!c->mixed) {
+        if (rc == SS_OK) rc = alloc((void **)&c->fr, 12 * ncell * sizeof(double));
+        if (rc == SS_OK) rc = alloc((void **)&c->fwd, 12 * nhalf * sizeof(double2));
+        if (rc == SS_OK) rc = alloc((void **)&c->invh, 24 * nhalf * sizeof(double2));
+        if (rc == SS_OK) rc = alloc((void **)&c->ir, 24 * ncell * sizeof(double));
+    }
     if (rc == SS_OK) rc = alloc((void **)&c->inv, 24 * ncell * sizeof(double2));
     if (rc == SS_OK) rc = alloc((void **)&c->table, ncell * TABLE_STRIDE_MAG * sizeof(double));
     if (rc == SS_OK && c->q2d && !c->mixed) rc = alloc((void **)&c->ctab, ncell * CTAB_STRIDE * sizeof(double));
@@ -737,7 +781,11 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
             return fail(nullptr, SS_ERR_CUDA, "%s", m_.c_str());                                      \
         }                                                                                             \
     } while (0)
-    CKC(cudaMemsetAsync(c->fwd, 0, 12 * ncell * sizeof(double2), c->stream));
+    if (!c->mixed) {
+        CKC(cudaMemsetAsync(c->fr, 0, 12 * ncell * sizeof(double), c->stream));
+        CKC(cudaMemsetAsync(c->fwd, 0, 12 * nhalf * sizeof(double2), c->stream));
+        CKC(cudaMemsetAsync(c->ir, 0, 24 * ncell * sizeof(double), c->stream));
+    }
     CKC(cudaMemsetAsync(c->inv, 0, 24 * ncell * sizeof(double2), c->stream));
     CKC(cudaMemsetAsync(c->table, 0, ncell * TABLE_STRIDE_MAG * sizeof(double), c->stream));
     CKC(cudaMemsetAsync(c->counts[0], 0, (size_t)P.nbins * sizeof(uint32_t), c->stream));
@@ -777,10 +825,13 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     // plans for the step
     {
         cufftHandle h;
-        int r1 = c->mixed ? get_plan_c(c, c->mag_step ? 12 : 9, &h) : get_plan(c, c->mag_step ? 12 : 9, &h);
-        int r2 = (r1 == SS_OK) ? (c->mixed ? get_plan_c(c, c->mag_step ? 24 : 12, &h)
-                                           : get_plan(c, c->mag_step ? 24 : 12, &h))
+        int r1 = SS_OK, r2 = SS_OK;
+        if (c->fft_rank > 0) {
+            r1 = c->mixed ? get_plan_c(c, c->mag_step ? 12 : 9, &h) : get_plan(c, c->mag_step ? 12 : 9, 1, &h);
+            r2 = (r1 == SS_OK) ? (c->mixed ? get_plan_c(c, c->mag_step ? 24 : 12, &h)
+                                           : get_plan(c, c->mag_step ? 24 : 12, 2, &h))
                                : r1;
+        }
         if (r1 != SS_OK || r2 != SS_OK) {
             std::string m = c->err;
             destroy_impl(c);
@@ -1159,15 +1210,41 @@ int ss_get_distribution(ss_ctx *c, double *out) {
     return read_device_error(c);
 }
 
-static int copy_real(ss_ctx *c, const double2 *src, int comps, double *out) {
-    long long cnt = (long long)comps * c->P.ncell;
-    if (!c->realbuf) CK(cudaMalloc((void **)&c->realbuf, 24ull * c->P.ncell * sizeof(double)));
-    launch_real_parts(c->stream, src, cnt, c->realbuf);
-    c->launches += 1;
-    CKR(check_launch(c, "real_parts"));
-    CK(cudaMemcpyAsync(out, c->realbuf, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+// the real fields of the last solve, components comp0 .. comp0 + comps, to
+// host memory (the mixed path's widened fields, or the FP64 solve's own)
+static int widen_fields(ss_ctx *c);
+static int copy_real(ss_ctx *c, int comp0, int comps, double *out) {
+    const long long nc = c->P.ncell, cnt = (long long)comps * nc;
+    if (c->mixed) {
+        CKR(widen_fields(c));
+        if (!c->realbuf) CK(cudaMalloc((void **)&c->realbuf, 24ull * c->P.ncell * sizeof(double)));
+        launch_real_parts(c->stream, c->inv + comp0 * nc, cnt, c->realbuf);
+        c->launches += 1;
+        CKR(check_launch(c, "real_parts"));
+        CK(cudaMemcpyAsync(out, c->realbuf, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    } else {
+        CK(cudaMemcpyAsync(out, c->ir + comp0 * nc, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    }
     CK(cudaStreamSynchronize(c->stream));
     return SS_OK;
+}
+
+// FP64 contexts: the complex fields of the last solve, as the reference's
+// complex inverse gives them, into inv [comp][cell]: the real parts are the
+// solve's own; the imaginary parts are the complex-to-real transform of the
+// operators' anti-Hermitian part (zero away from Nyquist bins), from the
+// half spectra that are still resident.
+static int complex_fields(ss_ctx *c, bool flow) {
+    if (c->mixed) return widen_fields(c);
+    const long long nc = c->P.ncell, nh = c->P.nhalf;
+    const int c0 = flow ? 0 : 12;
+    if (!c->realbuf) CK(cudaMalloc((void **)&c->realbuf, 24ull * c->P.ncell * sizeof(double)));
+    launch_kspace(c->stream, flow, !flow, true, c->fwd, c->invh, c->P, flow ? c->screening_last : 0.0);
+    CKR(check_launch(c, "kspace (imaginary parts)"));
+    CKR(fft_c2r(c, c->invh + c0 * nh, c->realbuf + c0 * nc, 12));
+    launch_combine_complex(c->stream, c->ir + c0 * nc, c->realbuf + c0 * nc, 12 * nc, c->inv + c0 * nc);
+    c->launches += 2;
+    return check_launch(c, "combine_complex");
 }
 
 // The dipolar field of the last solve, computed on demand when the step
@@ -1200,22 +1277,20 @@ static int widen_fields(ss_ctx *c) {
 int ss_get_flow_field(ss_ctx *c, double *out) {
     if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
     CK(cudaSetDevice(c->device));
-    CKR(widen_fields(c));
-    return copy_real(c, c->inv + 9ll * c->P.ncell, 3, out);
+    return copy_real(c, 9, 3, out);
 }
 
 int ss_get_magnetic_field(ss_ctx *c, double *out) {
     if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
     CK(cudaSetDevice(c->device));
     CKR(ensure_magnetic(c));
-    CKR(widen_fields(c));
-    return copy_real(c, c->inv + 21ll * c->P.ncell, 3, out);
+    return copy_real(c, 21, 3, out);
 }
 
 int ss_get_flow_complex(ss_ctx *c, double *u, double *grad) {
     if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
     CK(cudaSetDevice(c->device));
-    CKR(widen_fields(c));
+    CKR(complex_fields(c, true));
     const size_t nc = c->P.ncell;
     if (u) CK(cudaMemcpyAsync(u, c->inv + 9 * nc, 3 * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
     if (grad) CK(cudaMemcpyAsync(grad, c->inv, 9 * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
@@ -1227,7 +1302,7 @@ int ss_get_magnetic_complex(ss_ctx *c, double *b, double *gradb) {
     if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
     CK(cudaSetDevice(c->device));
     CKR(ensure_magnetic(c));
-    CKR(widen_fields(c));
+    CKR(complex_fields(c, false));
     const size_t nc = c->P.ncell;
     if (b) CK(cudaMemcpyAsync(b, c->inv + 21 * nc, 3 * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
     if (gradb) CK(cudaMemcpyAsync(gradb, c->inv + 12 * nc, 9 * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));

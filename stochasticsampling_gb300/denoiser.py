@@ -64,6 +64,12 @@ class Denoiser:
             raise ValueError(f"expected a grid of shape {self.shape}")
         return 1
 
+    def set_loss(self, moment_weight=0.0):
+        """Training loss: the mean-square error plus moment_weight times the
+        squared second angular harmonic of the residual per cell
+        (ss_dn_set_loss), the part of the error that reaches the flow."""
+        check(self.lib.ss_dn_set_loss(self._h, float(moment_weight)))
+
     @property
     def params(self):
         out = np.empty(self.nparams, dtype=np.float32)

@@ -144,12 +144,17 @@ def test_denoiser_forward_matches_torch():
     dn.close()
 
 
-def test_denoiser_gradients_match_torch():
+@pytest.mark.parametrize("shape,w", [((3, 128, 4), 0.0), ((3, 128, 8), 4.0)], ids=["mse", "mse_and_moment"])
+def test_denoiser_gradients_match_torch(shape, w):
+    """Parameter gradients and loss against torch autograd of the same
+    network and loss: the mean-square error, and with the angular-moment term
+    (ss_dn_set_loss) w * sum_cells (c2^2 + s2^2) / V, c2 and s2 the second
+    harmonic of the residual over phi."""
     ss = _gpu()
     torch = _torch()
     from stochasticsampling_gb300.denoiser import split_params
-    shape = (3, 128, 4)
     dn, P = _net(ss, shape, seed=4)
+    dn.set_loss(w)
     g = torch.Generator().manual_seed(2)
     x = 1.0 + 0.3 * torch.randn(2, *shape, generator=g)
     t = 1.0 + 0.1 * torch.randn(2, *shape, generator=g)
@@ -173,7 +178,11 @@ def test_denoiser_gradients_match_torch():
         a2 = bf(torch.relu(conv(a1, bf(P_t["w2"]), P_t["b2"])))
         a3 = bf(torch.relu(conv(a2, bf(P_t["w3"]), P_t["b3"])))
         yb = x[b] + conv(a3, P_t["w_out"][:, None, :], P_t["b_out"])[0]
-        lt = lt + ((yb - t[b]) ** 2).mean() / 2
+        r = yb - t[b]
+        phi2 = 2 * (torch.arange(shape[2], dtype=torch.float64) + 0.5) * 2 * np.pi / shape[2]
+        c2 = (r * torch.cos(phi2).float()).sum(-1)
+        s2 = (r * torch.sin(phi2).float()).sum(-1)
+        lt = lt + ((r ** 2).mean() + w * (c2 ** 2 + s2 ** 2).sum() / r.numel()) / 2
     lt.backward()
     assert abs(loss - lt.item()) <= 1e-3 * lt.item()
     got = split_params(grads)
