@@ -395,17 +395,23 @@ void kernel_slices(const std::vector<double> &K, int na, double measure_v_over_d
     }
 }
 
-void contract_prepare() {
-    const int big = 227 * 1024;
-    cudaFuncSetAttribute(k_contract_x<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_contract_x<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_contract_x<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_contract_f<true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_contract_f<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_contract_f<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_contract_f<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_contract_f<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_contract_f<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+cudaError_t contract_prepare() {
+    // the largest dynamic shared memory any grid needs (angle chunks of kAngChunk)
+    const int bx = (int)smem_x(kAngChunk), bf = (int)smem_f(kAngChunk);
+    cudaError_t e = cudaSuccess;
+    auto set = [&](const void *f, int bytes) {
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    };
+    set((const void *)k_contract_x<true, true>, bx);
+    set((const void *)k_contract_x<true, false>, bx);
+    set((const void *)k_contract_x<false, true>, bx);
+    set((const void *)k_contract_f<true, true, false>, bf);
+    set((const void *)k_contract_f<true, false, false>, bf);
+    set((const void *)k_contract_f<false, true, false>, bf);
+    set((const void *)k_contract_f<true, true, true>, bf);
+    set((const void *)k_contract_f<true, false, true>, bf);
+    set((const void *)k_contract_f<false, true, true>, bf);
+    return e;
 }
 
 void launch_contract_x(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kslice,

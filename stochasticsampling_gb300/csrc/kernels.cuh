@@ -41,7 +41,7 @@ void launch_contract_x(cudaStream_t s, bool stress, bool mag, const uint32_t *co
 void kernel_slices(const std::vector<double> &K, int na, double measure_v_over_d, std::vector<float> &slices,
                    std::vector<double> &factor);
 // shared-memory limits of the contraction kernels on the current device
-void contract_prepare();
+cudaError_t contract_prepare();
 // the k-space operators on the half spectrum (fwd [12][nhalf] -> inv
 // [24][nhalf]): their Hermitian part, or with anti the anti-Hermitian part
 // (the imaginary parts of the reference's complex fields)

@@ -813,7 +813,7 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
         c->partials_done = reinterpret_cast<unsigned *>(c->partials + 12ull * contract_m_blocks((int)ncell));
         CKC(cudaMemcpyAsync(c->kern_f, Kf.data(), Kf.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     }
-    contract_prepare();
+    CKC(contract_prepare());
     launch_half_pi(c->stream, c->d_halfpi);
     double hp[2];
     CKC(cudaMemcpyAsync(hp, c->d_halfpi, sizeof hp, cudaMemcpyDeviceToHost, c->stream));
