@@ -86,6 +86,8 @@ struct DevParams {
     int gather;        // 0 nearest cell, 1 trilinear, 2 trilinear with the z fraction from y
     int hdim[3];       // half-spectrum shape of the real-to-complex transforms: the last axis of size > 1 halved
     int nhalf;         // hdim[0] * hdim[1] * hdim[2]
+    int cstride;       // component stride of the contraction's real fields: ncell rounded up to even, so
+                       // every component starts 16-byte aligned (the real-to-complex transforms need it)
     uint32_t mask;     // Langevin modifiers that can change the state
 };
 

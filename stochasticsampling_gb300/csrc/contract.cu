@@ -4,11 +4,13 @@
 // the density of src/bin/simulation/mod.rs:312-316.
 //
 // A block takes kCTile consecutive cells, one thread per cell.  Their counts
-// are contiguous in HBM ([cell][phi][theta]); the block stages them, up to
-// kAngChunk angles of every cell at a time, into shared memory with coalesced
-// loads (16 bytes wide where the rows allow it), each row padded to an odd
-// stride so that thread t reading angle a of its own cell hits bank
-// (t * stride + a) mod 32 -- 32 different banks.  Thread t then runs over its
+// are contiguous in HBM ([cell][phi][theta]); the block stages them, 32
+// angles of every cell at a time, into shared memory with coalesced loads
+// (16 bytes wide where the rows allow it), each row padded to an odd stride
+// so that thread t reading angle a of its own cell hits bank
+// (t * stride + a) mod 32 -- 32 different banks.  The small tiles (64 cells,
+// 32 angles: 8 KB of counts) let many blocks share an SM, so that one
+// block's loads overlap another's arithmetic.  Thread t then runs over its
 // cell's angles in order while the angle kernels of the chunk are broadcast
 // from shared memory (every thread reads the same angle at the same time).
 // The histogram is read once, coalesced.
@@ -41,31 +43,33 @@ namespace ss {
 
 namespace {
 
-constexpr int kCTile = 128;     // cells (= threads) per block
-constexpr int kAngChunk = 128;  // angles of every cell staged at a time
+constexpr int kCTile = 64;     // cells (= threads) per block
+constexpr int kAngChunk = 32;  // angles of every cell staged at a time
 constexpr int kSliceW = 48;     // floats per angle of the FP64 path's slice table: 12 components x 4 slices
 constexpr uint32_t kExactCells = 4096;  // particles per cell below which the FP32 slice sums are exact
 
 struct Staging {
     int na;      // angles per cell
     int stride;  // padded row stride of the staged counts (odd)
-    int qshift;  // log2(na / 4) when the rows are read 16 bytes wide and na / 4 is a power of two, else -1
+    int vec;     // rows are read 16 bytes wide: na a multiple of 4 (so every staged segment is 16-byte aligned)
 };
 
 // counts (or FP32 distribution bits) of rows r < tc, angles a0 .. a0 + ach,
-// from src = base of row 0, into tile[r * stride + a - a0]
+// from src = base of row 0, into tile[r * stride + a - a0].  With 16-byte
+// loads a row segment of 32 angles is 8 quads: quad q of the tile lands at
+// row q / 8, word 4 (q % 8), and with the stride of 33 words a warp's 32
+// quads (4 rows x 8) store to 32 different banks.
 __device__ __forceinline__ void stage_rows(const uint32_t *__restrict__ src, const Staging &S, int a0, int ach,
                                            int tc, uint32_t *__restrict__ tile) {
     const int tid = threadIdx.x;
-    if (ach == S.na && (S.na & 3) == 0) {
-        // the tile is tc * na contiguous words, 16-byte aligned (cell0 * na * 4 is a multiple of 16)
-        const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
-        const int qpr = S.na >> 2, nq = tc * qpr;
-#pragma unroll 8
+    if (S.vec && (ach & 3) == 0) {
+        const int qpr = ach >> 2, nq = tc * qpr, rq = S.na >> 2;
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(src + a0);
+#pragma unroll 4
         for (int q = tid; q < nq; q += kCTile) {
-            const uint4 v = __ldg(s4 + q);
-            const int r = S.qshift >= 0 ? (q >> S.qshift) : q / qpr;
-            uint32_t *d = tile + r * S.stride + ((q - r * qpr) << 2);
+            const int r = q / qpr, cq = q - r * qpr;
+            const uint4 v = __ldg(s4 + (long long)r * rq + cq);
+            uint32_t *d = tile + r * S.stride + 4 * cq;
             d[0] = v.x;
             d[1] = v.y;
             d[2] = v.z;
@@ -205,11 +209,11 @@ __global__ void __launch_bounds__(kCTile) k_contract_x(const uint32_t *__restric
     }
     if (STRESS) {
 #pragma unroll
-        for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = sig[j];
+        for (int j = 0; j < 9; ++j) fwd[(long long)j * P.cstride + cell] = sig[j];
     }
     if (MAG) {
 #pragma unroll
-        for (int j = 9; j < 12; ++j) fwd[(long long)j * nc + cell] = sig[j];
+        for (int j = 9; j < 12; ++j) fwd[(long long)j * P.cstride + cell] = sig[j];
     }
     const double dens = (((double)csum / P.dist_den) * P.volume) * P.dthph;
     table[(long long)cell * tstride + T_DIFF] = sqrt(2.0 * P.dt * (P.Dt + P.volex * dens));
@@ -224,7 +228,7 @@ __global__ void __launch_bounds__(kCTile) k_contract_x(const uint32_t *__restric
 template <bool STRESS, bool MAG, bool DIST>
 __global__ void __launch_bounds__(kCTile) k_contract_f(const uint32_t *__restrict__ src_bins,
                                                        const float *__restrict__ kern, MixedParams M, Staging S,
-                                                       float scale, float dscale, float2 *__restrict__ fwd,
+                                                       float scale, float dscale, float *__restrict__ fwd,
                                                        float *__restrict__ table, int tstride,
                                                        double *__restrict__ partials, unsigned *__restrict__ done,
                                                        double *__restrict__ sums) {
@@ -296,11 +300,11 @@ __global__ void __launch_bounds__(kCTile) k_contract_f(const uint32_t *__restric
     if (live) {
         if (STRESS) {
 #pragma unroll
-            for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = make_float2(out[j], 0.f);
+            for (int j = 0; j < 9; ++j) fwd[(long long)j * M.cstride + cell] = out[j];
         }
         if (MAG) {
 #pragma unroll
-            for (int j = 9; j < 12; ++j) fwd[(long long)j * nc + cell] = make_float2(out[j], 0.f);
+            for (int j = 9; j < 12; ++j) fwd[(long long)j * M.cstride + cell] = out[j];
         }
         const float dens = DIST ? dsum * dscale * M.dthph
                                 : (float)(((double)csum / M.dist_den) * M.volume) * M.dthph;
@@ -344,15 +348,7 @@ Staging make_staging(int na) {
     S.na = na;
     const int ach = na < kAngChunk ? na : kAngChunk;
     S.stride = ach | 1;
-    S.qshift = -1;
-    if ((na & 3) == 0 && na <= kAngChunk) {
-        const int q = na >> 2;
-        if ((q & (q - 1)) == 0) {
-            int l = 0;
-            while ((1 << l) < q) ++l;
-            S.qshift = l;
-        }
-    }
+    S.vec = (na & 3) == 0;
     return S;
 }
 
@@ -432,7 +428,7 @@ void launch_contract_x(cudaStream_t s, bool stress, bool mag, const uint32_t *co
 unsigned contract_m_blocks(int ncell) { return tiles(ncell); }
 
 void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kern,
-                       const MixedParams &M, float2 *fwd, float *table, int tstride, double *partials,
+                       const MixedParams &M, float *fwd, float *table, int tstride, double *partials,
                        unsigned *done, double *sums, const float *dist, float fscale) {
     const Staging S = make_staging(M.nang);
     const size_t sm = smem_f(M.nang);

@@ -262,11 +262,11 @@ __global__ void __launch_bounds__(64) k_contract(const uint32_t *__restrict__ co
     const int nc = P.ncell;
     if (STRESS) {
 #pragma unroll
-        for (int j = 0; j < 9; ++j) fwd[(long long)j * nc + cell] = acc[j] * P.measure;
+        for (int j = 0; j < 9; ++j) fwd[(long long)j * P.cstride + cell] = acc[j] * P.measure;
     }
     if (MAG) {
 #pragma unroll
-        for (int j = 0; j < 3; ++j) fwd[(long long)(9 + j) * nc + cell] = acc[9 + j] * P.measure;
+        for (int j = 0; j < 3; ++j) fwd[(long long)(9 + j) * P.cstride + cell] = acc[9 + j] * P.measure;
     }
     double dens = acc[12] * P.dthph;
     double volex = P.volex * dens;
@@ -408,9 +408,9 @@ __global__ void k_kspace(const double2 *__restrict__ fwd, double2 *__restrict__ 
 }
 
 // real <-> complex copies of a one-cell grid (no axis to transform)
-__global__ void k_real_to_complex(const double *__restrict__ src, int count, double2 *__restrict__ dst) {
+__global__ void k_real_to_complex(const double *__restrict__ src, int count, int sstride, double2 *__restrict__ dst) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count) dst[i] = make_double2(src[i], 0.0);
+    if (i < count) dst[i] = make_double2(src[(long long)i * sstride], 0.0);
 }
 __global__ void k_complex_to_real(const double2 *__restrict__ src, int count, double *__restrict__ dst) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -914,8 +914,8 @@ void launch_kspace(cudaStream_t s, bool flow, bool mag, bool anti, const double2
 #undef SS_KS
 }
 
-void launch_real_to_complex(cudaStream_t s, const double *src, int count, double2 *dst) {
-    if (count > 0) k_real_to_complex<<<nblocks(count, 128), 128, 0, s>>>(src, count, dst);
+void launch_real_to_complex(cudaStream_t s, const double *src, int count, int sstride, double2 *dst) {
+    if (count > 0) k_real_to_complex<<<nblocks(count, 128), 128, 0, s>>>(src, count, sstride, dst);
 }
 void launch_complex_to_real(cudaStream_t s, const double2 *src, int count, double *dst) {
     if (count > 0) k_complex_to_real<<<nblocks(count, 128), 128, 0, s>>>(src, count, dst);

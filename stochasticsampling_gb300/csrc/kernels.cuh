@@ -47,7 +47,8 @@ cudaError_t contract_prepare();
 // (the imaginary parts of the reference's complex fields)
 void launch_kspace(cudaStream_t s, bool flow, bool mag, bool anti, const double2 *fwd, double2 *inv,
                    const DevParams &P, double screening);
-void launch_real_to_complex(cudaStream_t s, const double *src, int count, double2 *dst);
+// one-cell grids: src values sstride apart -> complex (value, 0)
+void launch_real_to_complex(cudaStream_t s, const double *src, int count, int sstride, double2 *dst);
 void launch_complex_to_real(cudaStream_t s, const double2 *src, int count, double *dst);
 void launch_combine_complex(cudaStream_t s, const double *re, const double *im, long long count, double2 *dst);
 // the per-cell field rows from the real fields inv [24][ncell]

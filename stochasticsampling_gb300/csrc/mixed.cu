@@ -91,82 +91,124 @@ __global__ void k_bin_m(unsigned long long n, MixedParams M, const double *__res
 }
 
 // subtract the FP64 means before the FP32 transform
-__global__ void k_center_m(float2 *__restrict__ fwd, int c0, int c1, int ncell, const double *__restrict__ sums) {
+__global__ void k_center_m(float *__restrict__ fr, int c0, int c1, int ncell, int cstride,
+                           const double *__restrict__ sums) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     long long total = (long long)(c1 - c0) * ncell;
     if (i >= total) return;
     int comp = c0 + (int)(i / ncell);
-    long long idx = (long long)comp * ncell + (i % ncell);
+    long long idx = (long long)comp * cstride + (i % ncell);
     float mean = (float)(sums[comp] / (double)ncell);
-    fwd[idx].x -= mean;
+    fr[idx] -= mean;
 }
 
-template <bool FLOW, bool MAG>
-__global__ void k_kspace_m(const float2 *__restrict__ fwd, float2 *__restrict__ inv, MixedParams M, float screening,
+// the operators of the FP64 path's k_kspace (kernels.cu) in FP32
+__device__ __forceinline__ void flow_ops_f(const float k[3], const float kn[3], float fac, const float2 *sig,
+                                           float2 *o) {
+    float2 sg[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float2 a0 = sig[3 * r + 0], a1 = sig[3 * r + 1], a2 = sig[3 * r + 2];
+        sg[r].x = a0.x * k[0] + a1.x * k[1] + a2.x * k[2];
+        sg[r].y = a0.y * k[0] + a1.y * k[1] + a2.y * k[2];
+    }
+    const float ksr = kn[0] * sg[0].x + kn[1] * sg[1].x + kn[2] * sg[2].x;
+    const float ksi = kn[0] * sg[0].y + kn[1] * sg[1].y + kn[2] * sg[2].y;
+    float2 u[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float tr = (sg[r].x - kn[r] * ksr) * fac;
+        const float ti = (sg[r].y - kn[r] * ksi) * fac;
+        u[r] = make_float2(-ti, tr);
+        o[9 + r] = u[r];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) o[3 * a + b] = make_float2(-(k[a] * u[b].y), k[a] * u[b].x);
+}
+
+__device__ __forceinline__ void mag_ops_f(const float k[3], const float kn[3], float norm, bool kzero,
+                                          const float2 *p, float2 *o) {
+    const float dr = kn[0] * p[0].x + kn[1] * p[1].x + kn[2] * p[2].x;
+    const float di = kn[0] * p[0].y + kn[1] * p[1].y + kn[2] * p[2].y;
+    float2 b[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        // the k = 0 mode (the mean) was removed and is added back in FP64
+        b[r] = kzero ? make_float2(0.f, 0.f)
+                     : make_float2((p[r].x - kn[r] * dr) / norm, (p[r].y - kn[r] * di) / norm);
+        o[9 + r] = b[r];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb) o[3 * a + bb] = make_float2(-(k[a] * b[bb].y), k[a] * b[bb].x);
+}
+
+// the half-spectrum k space of the FP64 path (kernels.cu, k_kspace) in FP32:
+// the operators' Hermitian part (ANTI: the anti-Hermitian part), evaluated
+// twice only on Nyquist planes
+template <bool FLOW, bool MAG, bool ANTI>
+__global__ void k_kspace_m(const float2 *__restrict__ fwd, float2 *__restrict__ out, MixedParams M, float screening,
                            float stepx, float stepy, float stepz) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nc = M.ncell;
-    if (c >= nc) return;
-    int iz = c % M.gz;
-    int iy = (c / M.gz) % M.gy;
-    int ix = c / (M.gz * M.gy);
-    float k[3] = {kval_f(ix, M.gx, stepx), kval_f(iy, M.gy, stepy), kval_f(iz, M.gz, stepz)};
-    float s = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
-    float ik2 = (c == 0) ? 0.f : 1.f / s;
-    float inrm = (c == 0) ? 0.f : rsqrtf(s);
-    float kn[3] = {k[0] * inrm, k[1] * inrm, k[2] * inrm};
-    const float norm = (float)nc;
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nh = M.nhalf;
+    if (h >= nh) return;
+    const int iz = h % M.hdim[2];
+    const int iy = (h / M.hdim[2]) % M.hdim[1];
+    const int ix = h / (M.hdim[2] * M.hdim[1]);
+    const float k[3] = {kval_f(ix, M.gx, stepx), kval_f(iy, M.gy, stepy), kval_f(iz, M.gz, stepz)};
+    const bool nyq[3] = {(M.gx & 1) == 0 && 2 * ix == M.gx, (M.gy & 1) == 0 && 2 * iy == M.gy,
+                         (M.gz & 1) == 0 && 2 * iz == M.gz};
+    const bool mirror = nyq[0] || nyq[1] || nyq[2];
+    const bool kzero = (ix | iy | iz) == 0;
+    const float s = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+    const float ik2 = kzero ? 0.f : 1.f / s;
+    const float inrm = kzero ? 0.f : rsqrtf(s);
+    const float kn[3] = {k[0] * inrm, k[1] * inrm, k[2] * inrm};
+    const float km[3] = {nyq[0] ? k[0] : -k[0], nyq[1] ? k[1] : -k[1], nyq[2] ? k[2] : -k[2]};
+    const float knm[3] = {km[0] * inrm, km[1] * inrm, km[2] * inrm};
+    const float norm = (float)M.ncell;
+    auto emit = [&](int c0, const float2 *X, const float2 *Xm) {
+#pragma unroll
+        for (int j = 0; j < 12; ++j) {
+            float2 v;
+            if (!mirror) v = ANTI ? make_float2(0.f, 0.f) : X[j];
+            else if (ANTI) v = make_float2((X[j].y + Xm[j].y) * 0.5f, -(X[j].x - Xm[j].x) * 0.5f);
+            else v = make_float2((X[j].x + Xm[j].x) * 0.5f, (X[j].y - Xm[j].y) * 0.5f);
+            out[(long long)(c0 + j) * nh + h] = v;
+        }
+    };
     if (FLOW) {
-        float2 sg[3];
+        float2 sig[9], X[12], Xm[12];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            float2 a0 = fwd[(long long)(3 * r + 0) * nc + c];
-            float2 a1 = fwd[(long long)(3 * r + 1) * nc + c];
-            float2 a2 = fwd[(long long)(3 * r + 2) * nc + c];
-            sg[r].x = a0.x * k[0] + a1.x * k[1] + a2.x * k[2];
-            sg[r].y = a0.y * k[0] + a1.y * k[1] + a2.y * k[2];
+        for (int j = 0; j < 9; ++j) sig[j] = fwd[(long long)j * nh + h];
+        const float fac = (ik2 + screening) / norm;
+        flow_ops_f(k, kn, fac, sig, X);
+        if (mirror) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) sig[j].y = -sig[j].y;
+            flow_ops_f(km, knm, fac, sig, Xm);
         }
-        float ksr = kn[0] * sg[0].x + kn[1] * sg[1].x + kn[2] * sg[2].x;
-        float ksi = kn[0] * sg[0].y + kn[1] * sg[1].y + kn[2] * sg[2].y;
-        float fac = (ik2 + screening) / norm;
-        float2 u[3];
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            float tr = (sg[r].x - kn[r] * ksr) * fac;
-            float ti = (sg[r].y - kn[r] * ksi) * fac;
-            u[r] = make_float2(-ti, tr);
-            inv[(long long)(9 + r) * nc + c] = u[r];
-        }
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = 0; b < 3; ++b)
-                inv[(long long)(3 * a + b) * nc + c] = make_float2(-(k[a] * u[b].y), k[a] * u[b].x);
+        emit(0, X, Xm);
     }
     if (MAG) {
-        float2 p[3];
+        float2 pol[3], X[12], Xm[12];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) p[r] = fwd[(long long)(9 + r) * nc + c];
-        float dr = kn[0] * p[0].x + kn[1] * p[1].x + kn[2] * p[2].x;
-        float di = kn[0] * p[0].y + kn[1] * p[1].y + kn[2] * p[2].y;
-        float2 b[3];
+        for (int j = 0; j < 3; ++j) pol[j] = fwd[(long long)(9 + j) * nh + h];
+        mag_ops_f(k, kn, norm, kzero, pol, X);
+        if (mirror) {
 #pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            // the k = 0 mode (the mean) was removed and is added back in FP64
-            b[r] = (c == 0) ? make_float2(0.f, 0.f)
-                            : make_float2((p[r].x - kn[r] * dr) / norm, (p[r].y - kn[r] * di) / norm);
-            inv[(long long)(21 + r) * nc + c] = b[r];
+            for (int j = 0; j < 3; ++j) pol[j].y = -pol[j].y;
+            mag_ops_f(km, knm, norm, kzero, pol, Xm);
         }
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int bb = 0; bb < 3; ++bb)
-                inv[(long long)(12 + 3 * a + bb) * nc + c] = make_float2(-(k[a] * b[bb].y), k[a] * b[bb].x);
+        emit(12, X, Xm);
     }
 }
 
 template <bool FLOW, bool MAG>
-__global__ void k_table_m(const float2 *__restrict__ inv, MixedParams M, float *__restrict__ table, int tstride,
+__global__ void k_table_m(const float *__restrict__ inv, MixedParams M, float *__restrict__ table, int tstride,
                           const double *__restrict__ sums) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     const int nc = M.ncell;
@@ -175,9 +217,9 @@ __global__ void k_table_m(const float2 *__restrict__ inv, MixedParams M, float *
     if (FLOW) {
         float g[9];
 #pragma unroll
-        for (int j = 0; j < 9; ++j) g[j] = inv[(long long)j * nc + c].x;
+        for (int j = 0; j < 9; ++j) g[j] = inv[(long long)j * nc + c];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) row[T_U + r] = inv[(long long)(9 + r) * nc + c].x;
+        for (int r = 0; r < 3; ++r) row[T_U + r] = inv[(long long)(9 + r) * nc + c];
         row[T_W01] = (g[1] - g[3]) * 0.5f;
         row[T_W02] = (g[2] - g[6]) * 0.5f;
         row[T_W12] = (g[5] - g[7]) * 0.5f;
@@ -191,25 +233,33 @@ __global__ void k_table_m(const float2 *__restrict__ inv, MixedParams M, float *
     if (MAG) {
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-            double b = (double)inv[(long long)(21 + r) * nc + c].x + sums[9 + r] / (double)nc;
+            double b = (double)inv[(long long)(21 + r) * nc + c] + sums[9 + r] / (double)nc;
             row[T_B + r] = (float)(b * M.mdd);
         }
 #pragma unroll
-        for (int j = 0; j < 9; ++j) row[T_GB + j] = inv[(long long)(12 + j) * nc + c].x;
+        for (int j = 0; j < 9; ++j) row[T_GB + j] = inv[(long long)(12 + j) * nc + c];
     }
 }
 
-// complex float field -> complex double (for the FP64 getters); adds the FP64
-// mean back to the components listed in [m0, m1)
-__global__ void k_widen_m(const float2 *__restrict__ src, long long count, int ncell, int comp0, int m0, int m1,
-                          const double *__restrict__ sums, double2 *__restrict__ dst) {
+// complex double fields for the FP64 getters from FP32 real and imaginary
+// parts; adds the FP64 mean back to the components listed in [m0, m1)
+__global__ void k_widen_m(const float *__restrict__ re, const float *__restrict__ im, long long count, int ncell,
+                          int comp0, int m0, int m1, const double *__restrict__ sums, double2 *__restrict__ dst) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= count) return;
-    float2 v = src[i];
     int comp = comp0 + (int)(i / ncell);
-    double re = (double)v.x;
-    if (comp >= m0 && comp < m1) re += sums[comp - 12] / (double)ncell;
-    dst[i] = make_double2(re, (double)v.y);
+    double r = (double)re[i];
+    if (comp >= m0 && comp < m1) r += sums[comp - 12] / (double)ncell;
+    dst[i] = make_double2(r, im ? (double)im[i] : 0.0);
+}
+
+__global__ void k_real_to_complex_f(const float *__restrict__ src, int count, int sstride, float2 *__restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) dst[i] = make_float2(src[(long long)i * sstride], 0.f);
+}
+__global__ void k_complex_to_real_f(const float2 *__restrict__ src, int count, float *__restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) dst[i] = src[i].x;
 }
 
 // NOISE: 0 Philox, 1 host array.  CANON (quasi2d only): z == 0 and
@@ -324,28 +374,40 @@ __global__ void k_counts_to_unit(const uint32_t *__restrict__ counts, long long 
 void launch_counts_to_unit(cudaStream_t s, const uint32_t *counts, long long nbins, float inv_mean, float *x) {
     if (nbins > 0) k_counts_to_unit<<<nb((unsigned long long)nbins, 256), 256, 0, s>>>(counts, nbins, inv_mean, x);
 }
-void launch_center_m(cudaStream_t s, float2 *fwd, int c0, int c1, int ncell, const double *sums) {
+void launch_center_m(cudaStream_t s, float *fr, int c0, int c1, int ncell, int cstride, const double *sums) {
     long long total = (long long)(c1 - c0) * ncell;
-    if (total > 0) k_center_m<<<nb(total, 256), 256, 0, s>>>(fwd, c0, c1, ncell, sums);
+    if (total > 0) k_center_m<<<nb(total, 256), 256, 0, s>>>(fr, c0, c1, ncell, cstride, sums);
 }
-void launch_kspace_m(cudaStream_t s, bool flow, bool mag, const float2 *fwd, float2 *inv, const MixedParams &M,
-                     float screening) {
+void launch_kspace_m(cudaStream_t s, bool flow, bool mag, bool anti, const float2 *fwd, float2 *inv,
+                     const MixedParams &M, float screening) {
     float sx = (float)(kTwoPi / M.bx), sy = (float)(kTwoPi / M.by), sz = (float)(kTwoPi / M.bz);
-    unsigned b = nb(M.ncell, 128);
-    if (flow && mag) k_kspace_m<true, true><<<b, 128, 0, s>>>(fwd, inv, M, screening, sx, sy, sz);
-    else if (flow) k_kspace_m<true, false><<<b, 128, 0, s>>>(fwd, inv, M, screening, sx, sy, sz);
-    else k_kspace_m<false, true><<<b, 128, 0, s>>>(fwd, inv, M, screening, sx, sy, sz);
+    unsigned b = nb(M.nhalf, 128);
+#define SS_KSM(F, G)                                                                                     \
+    do {                                                                                                 \
+        if (anti) k_kspace_m<F, G, true><<<b, 128, 0, s>>>(fwd, inv, M, screening, sx, sy, sz);      \
+        else k_kspace_m<F, G, false><<<b, 128, 0, s>>>(fwd, inv, M, screening, sx, sy, sz);          \
+    } while (0)
+    if (flow && mag) SS_KSM(true, true);
+    else if (flow) SS_KSM(true, false);
+    else SS_KSM(false, true);
+#undef SS_KSM
 }
-void launch_table_m(cudaStream_t s, bool flow, bool mag, const float2 *inv, const MixedParams &M, float *table,
+void launch_table_m(cudaStream_t s, bool flow, bool mag, const float *inv, const MixedParams &M, float *table,
                     int tstride, const double *sums) {
     unsigned b = nb(M.ncell, 128);
     if (flow && mag) k_table_m<true, true><<<b, 128, 0, s>>>(inv, M, table, tstride, sums);
     else if (flow) k_table_m<true, false><<<b, 128, 0, s>>>(inv, M, table, tstride, sums);
     else k_table_m<false, true><<<b, 128, 0, s>>>(inv, M, table, tstride, sums);
 }
-void launch_widen_m(cudaStream_t s, const float2 *src, long long count, int ncell, int comp0, int m0, int m1,
-                    const double *sums, double2 *dst) {
-    if (count > 0) k_widen_m<<<nb(count, 256), 256, 0, s>>>(src, count, ncell, comp0, m0, m1, sums, dst);
+void launch_widen_m(cudaStream_t s, const float *re, const float *im, long long count, int ncell, int comp0, int m0,
+                    int m1, const double *sums, double2 *dst) {
+    if (count > 0) k_widen_m<<<nb(count, 256), 256, 0, s>>>(re, im, count, ncell, comp0, m0, m1, sums, dst);
+}
+void launch_real_to_complex_f(cudaStream_t s, const float *src, int count, int sstride, float2 *dst) {
+    if (count > 0) k_real_to_complex_f<<<nb(count, 128), 128, 0, s>>>(src, count, sstride, dst);
+}
+void launch_complex_to_real_f(cudaStream_t s, const float2 *src, int count, float *dst) {
+    if (count > 0) k_complex_to_real_f<<<nb(count, 128), 128, 0, s>>>(src, count, dst);
 }
 void launch_update_m(cudaStream_t s, bool fixed, bool q2d, bool canon, bool mag, bool host_noise, const MixedParams &M,
                      double *const xs[3], float *const as[2], uint32_t *key, const uint32_t *id, const float *table,

@@ -26,6 +26,9 @@ struct MixedParams {
     float drag, reorient, shape, mdd, sigma_rot;
     unsigned long long seed;
     uint32_t mask;
+    int hdim[3];  // half-spectrum shape of the real-to-complex transforms (as DevParams)
+    int nhalf;
+    int cstride;  // component stride of the contraction's real fields (as DevParams)
 };
 
 // id == nullptr: leave id as it is (rows already sorted, id holds their caller indices)
@@ -35,7 +38,7 @@ void launch_egest_m(cudaStream_t s, bool fixed, unsigned long long n, const Mixe
                     float *const as[2], const uint32_t *id, double *aos);
 void launch_bin_m(cudaStream_t s, bool fixed, unsigned long long n, const MixedParams &M, double *const xs[3],
                   float *const as[2], uint32_t *key, uint32_t *counts);
-// the FP32 angular contraction (contract.cu): fwd components, the table's
+// the FP32 angular contraction (contract.cu): real fwd [12][ncell], the table's
 // diffusion length and the FP64 component sums (sums[0..9) with stress,
 // sums[9..12) with the polarisation) in a fixed order.  partials:
 // contract_m_blocks(ncell) x 12 doubles; done: a counter that is 0 between
@@ -43,16 +46,23 @@ void launch_bin_m(cudaStream_t s, bool fixed, unsigned long long n, const MixedP
 // counts (the denoised histogram).
 unsigned contract_m_blocks(int ncell);
 void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kern,
-                       const MixedParams &M, float2 *fwd, float *table, int tstride, double *partials,
+                       const MixedParams &M, float *fwd, float *table, int tstride, double *partials,
                        unsigned *done, double *sums, const float *dist = nullptr, float fscale = 0.f);
 void launch_counts_to_unit(cudaStream_t s, const uint32_t *counts, long long nbins, float inv_mean, float *x);
-void launch_center_m(cudaStream_t s, float2 *fwd, int c0, int c1, int ncell, const double *sums);
-void launch_kspace_m(cudaStream_t s, bool flow, bool mag, const float2 *fwd, float2 *inv, const MixedParams &M,
-                     float screening);
-void launch_table_m(cudaStream_t s, bool flow, bool mag, const float2 *inv, const MixedParams &M, float *table,
+// the FP64 means removed from the real fields fr [comp][cstride], components c0 .. c1
+void launch_center_m(cudaStream_t s, float *fr, int c0, int c1, int ncell, int cstride, const double *sums);
+// the k-space operators on the half spectrum, Hermitian part (or with anti the
+// anti-Hermitian part); as launch_kspace of the FP64 path
+void launch_kspace_m(cudaStream_t s, bool flow, bool mag, bool anti, const float2 *fwd, float2 *inv,
+                     const MixedParams &M, float screening);
+void launch_table_m(cudaStream_t s, bool flow, bool mag, const float *inv, const MixedParams &M, float *table,
                     int tstride, const double *sums);
-void launch_widen_m(cudaStream_t s, const float2 *src, long long count, int ncell, int comp0, int m0, int m1,
-                    const double *sums, double2 *dst);
+// complex FP64 fields dst [comp][cell] from FP32 real parts re and imaginary
+// parts im (null: zero), the FP64 mean added to components m0 .. m1
+void launch_widen_m(cudaStream_t s, const float *re, const float *im, long long count, int ncell, int comp0, int m0,
+                    int m1, const double *sums, double2 *dst);
+void launch_real_to_complex_f(cudaStream_t s, const float *src, int count, int sstride, float2 *dst);
+void launch_complex_to_real_f(cudaStream_t s, const float2 *src, int count, float *dst);
 void launch_update_m(cudaStream_t s, bool fixed, bool q2d, bool canon, bool mag, bool host_noise, const MixedParams &M,
                      double *const xs[3], float *const as[2], uint32_t *key, const uint32_t *id, const float *table,
                      const double *noise, const unsigned long long *d_step, uint32_t *counts_next);

@@ -94,13 +94,14 @@ struct ss_ctx {
     bool canon = false;  // quasi2d: z == 0 and theta == pi/2 hold for every particle
     MixedParams M{};
     float *pa[2][2] = {};  // phi, theta (FP32)
-    float2 *fwd_f = nullptr, *inv_f = nullptr;
+    float *fr_f = nullptr, *ir_f = nullptr, *ii_f = nullptr;  // real fields [12][ncell], [24][ncell], imaginary parts
+    float2 *fwd_f = nullptr, *inv_f = nullptr;               // half spectra [12][nhalf], [24][nhalf]
     float *table_f = nullptr, *kern_f = nullptr;
     double *sums = nullptr;  // FP64 per-component sums for the mean handling
     double *partials = nullptr;  // per-block component sums of the FP32 contraction (+ its counter)
     unsigned *partials_done = nullptr;
     bool wide_valid = false;  // inv (FP64) holds the widened mixed fields
-    std::map<int, cufftHandle> plans_c;
+    std::map<int, cufftHandle> plans_c;  // key: batch * 4 + kind (1 R2C, 2 C2R)
 
     std::map<int, cufftHandle> plans;  // key: batch * 4 + kind (0 Z2Z, 1 D2Z, 2 Z2D)
     int fft_rank = 0;
@@ -231,11 +232,14 @@ static int get_plan(ss_ctx *c, int batch, int kind, cufftHandle *out) {
         return SS_OK;
     }
     cufftHandle h;
-    const int nc = c->P.ncell, nh = c->P.nhalf;
-    if (kind == 1)
-        CKF(cufftPlanMany(&h, c->fft_rank, c->fft_n, nullptr, 1, nc, nullptr, 1, nh, CUFFT_D2Z, batch));
+    const int nc = c->P.ncell, nh = c->P.nhalf, cs = c->P.cstride;
+    int rn[3], hn[3];  // the real and the half-spectrum shapes
+    for (int k = 0; k < c->fft_rank; ++k) rn[k] = hn[k] = c->fft_n[k];
+    hn[c->fft_rank - 1] = c->fft_n[c->fft_rank - 1] / 2 + 1;
+    if (kind == 1)  // input components cstride apart (16-byte aligned starts)
+        CKF(cufftPlanMany(&h, c->fft_rank, c->fft_n, rn, 1, cs, hn, 1, nh, CUFFT_D2Z, batch));
     else
-        CKF(cufftPlanMany(&h, c->fft_rank, c->fft_n, nullptr, 1, nh, nullptr, 1, nc, CUFFT_Z2D, batch));
+        CKF(cufftPlanMany(&h, c->fft_rank, c->fft_n, hn, 1, nh, rn, 1, nc, CUFFT_Z2D, batch));
     CKF(cufftSetStream(h, c->stream));
     c->plans[key] = h;
     *out = h;
@@ -246,7 +250,7 @@ static int get_plan(ss_ctx *c, int batch, int kind, cufftHandle *out) {
 static int fft_r2c(ss_ctx *c, const double *src, double2 *dst, int batch) {
     if (batch == 0) return SS_OK;
     if (c->fft_rank == 0) {  // 1-cell grid: the DFT is the identity
-        launch_real_to_complex(c->stream, src, batch, dst);
+        launch_real_to_complex(c->stream, src, batch, c->P.cstride, dst);
         return check_launch(c, "real_to_complex");
     }
     cufftHandle h = 0;
@@ -268,26 +272,50 @@ static int fft_c2r(ss_ctx *c, double2 *src, double *dst, int batch) {
     return SS_OK;
 }
 
-static int get_plan_c(ss_ctx *c, int batch, cufftHandle *out) {
-    auto it = c->plans_c.find(batch);
+// the FP32 real-to-complex (R2C) and complex-to-real (C2R) plans of the mixed path
+static int get_plan_c(ss_ctx *c, int batch, int kind, cufftHandle *out) {
+    const int key = batch * 4 + kind;
+    auto it = c->plans_c.find(key);
     if (it != c->plans_c.end()) {
         *out = it->second;
         return SS_OK;
     }
     cufftHandle h;
-    int nc = c->P.ncell;
-    CKF(cufftPlanMany(&h, c->fft_rank, c->fft_n, nullptr, 1, nc, nullptr, 1, nc, CUFFT_C2C, batch));
+    const int nc = c->P.ncell, nh = c->P.nhalf, cs = c->P.cstride;
+    int rn[3], hn[3];
+    for (int k = 0; k < c->fft_rank; ++k) rn[k] = hn[k] = c->fft_n[k];
+    hn[c->fft_rank - 1] = c->fft_n[c->fft_rank - 1] / 2 + 1;
+    if (kind == 1)
+        CKF(cufftPlanMany(&h, c->fft_rank, c->fft_n, rn, 1, cs, hn, 1, nh, CUFFT_R2C, batch));
+    else
+        CKF(cufftPlanMany(&h, c->fft_rank, c->fft_n, hn, 1, nh, rn, 1, nc, CUFFT_C2R, batch));
     CKF(cufftSetStream(h, c->stream));
-    c->plans_c[batch] = h;
+    c->plans_c[key] = h;
     *out = h;
     return SS_OK;
 }
 
-static int fft_c(ss_ctx *c, float2 *data, int batch, int dir) {
-    if (c->fft_rank == 0 || batch == 0) return SS_OK;
+static int fft_r2c_f(ss_ctx *c, const float *src, float2 *dst, int batch) {
+    if (batch == 0) return SS_OK;
+    if (c->fft_rank == 0) {
+        launch_real_to_complex_f(c->stream, src, batch, c->P.cstride, dst);
+        return check_launch(c, "real_to_complex (mixed)");
+    }
     cufftHandle h = 0;
-    CKR(get_plan_c(c, batch, &h));
-    CKF(cufftExecC2C(h, reinterpret_cast<cufftComplex *>(data), reinterpret_cast<cufftComplex *>(data), dir));
+    CKR(get_plan_c(c, batch, 1, &h));
+    CKF(cufftExecR2C(h, const_cast<cufftReal *>(src), reinterpret_cast<cufftComplex *>(dst)));
+    return SS_OK;
+}
+
+static int fft_c2r_f(ss_ctx *c, float2 *src, float *dst, int batch) {
+    if (batch == 0) return SS_OK;
+    if (c->fft_rank == 0) {
+        launch_complex_to_real_f(c->stream, src, batch, dst);
+        return check_launch(c, "complex_to_real (mixed)");
+    }
+    cufftHandle h = 0;
+    CKR(get_plan_c(c, batch, 2, &h));
+    CKF(cufftExecC2R(h, reinterpret_cast<cufftComplex *>(src), dst));
     return SS_OK;
 }
 
@@ -325,7 +353,7 @@ static int enqueue_solve(ss_ctx *c, bool flow, bool mag, const uint32_t *counts,
     const long long nc = c->P.ncell, nh = c->P.nhalf;
     if (flow && mag) CKR(fft_r2c(c, c->fr, c->fwd, 12));
     else if (flow) CKR(fft_r2c(c, c->fr, c->fwd, 9));
-    else CKR(fft_r2c(c, c->fr + 9 * nc, c->fwd + 9 * nh, 3));
+    else CKR(fft_r2c(c, c->fr + 9ll * c->P.cstride, c->fwd + 9 * nh, 3));
     mark(c, 2);
     launch_kspace(c->stream, flow, mag, false, c->fwd, c->invh, c->P, screening);
     ++*nl;
@@ -357,33 +385,35 @@ static int enqueue_solve_m(ss_ctx *c, bool flow, bool mag, const uint32_t *count
         // the denoised histogram replaces the counts in the contraction
         launch_counts_to_unit(c->stream, counts, c->P.nbins, c->dn_inv_mean, c->dn_x);
         *nl += 1 + dn_enqueue_forward(c->dn, c->dn_x, c->dn_y, c->stream);
-        launch_contract_m(c->stream, flow, mag, counts, c->kern_f, c->M, c->fwd_f, c->table_f, ts, c->partials,
+        launch_contract_m(c->stream, flow, mag, counts, c->kern_f, c->M, c->fr_f, c->table_f, ts, c->partials,
                           c->partials_done, c->sums, c->dn_y, c->dn_fscale);
     } else {
-        launch_contract_m(c->stream, flow, mag, counts, c->kern_f, c->M, c->fwd_f, c->table_f, ts, c->partials,
+        launch_contract_m(c->stream, flow, mag, counts, c->kern_f, c->M, c->fr_f, c->table_f, ts, c->partials,
                           c->partials_done, c->sums);
     }
-    if (flow) launch_center_m(c->stream, c->fwd_f, 0, 9, nc, c->sums);
-    if (mag) launch_center_m(c->stream, c->fwd_f, 9, 12, nc, c->sums);
+    if (flow) launch_center_m(c->stream, c->fr_f, 0, 9, nc, c->P.cstride, c->sums);
+    if (mag) launch_center_m(c->stream, c->fr_f, 9, 12, nc, c->P.cstride, c->sums);
     *nl += 1 + (flow ? 1 : 0) + (mag ? 1 : 0);
     CKR(check_launch(c, "contract (mixed)"));
     mark(c, 6);
     mark(c, 1);
-    if (flow && mag) CKR(fft_c(c, c->fwd_f, 12, CUFFT_FORWARD));
-    else if (flow) CKR(fft_c(c, c->fwd_f, 9, CUFFT_FORWARD));
-    else CKR(fft_c(c, c->fwd_f + 9ll * nc, 3, CUFFT_FORWARD));
+    const long long nh = c->P.nhalf;
+    if (flow && mag) CKR(fft_r2c_f(c, c->fr_f, c->fwd_f, 12));
+    else if (flow) CKR(fft_r2c_f(c, c->fr_f, c->fwd_f, 9));
+    else CKR(fft_r2c_f(c, c->fr_f + 9ll * c->P.cstride, c->fwd_f + 9 * nh, 3));
     mark(c, 2);
-    launch_kspace_m(c->stream, flow, mag, c->fwd_f, c->inv_f, c->M, (float)screening);
+    launch_kspace_m(c->stream, flow, mag, false, c->fwd_f, c->inv_f, c->M, (float)screening);
     ++*nl;
     CKR(check_launch(c, "kspace (mixed)"));
     mark(c, 3);
-    if (flow && mag) CKR(fft_c(c, c->inv_f, 24, CUFFT_INVERSE));
-    else if (flow) CKR(fft_c(c, c->inv_f, 12, CUFFT_INVERSE));
-    else CKR(fft_c(c, c->inv_f + 12ll * nc, 12, CUFFT_INVERSE));
+    if (flow && mag) CKR(fft_c2r_f(c, c->inv_f, c->ir_f, 24));
+    else if (flow) CKR(fft_c2r_f(c, c->inv_f, c->ir_f, 12));
+    else CKR(fft_c2r_f(c, c->inv_f + 12 * nh, c->ir_f + 12ll * nc, 12));
+    if (flow) c->screening_last = screening;
     mark(c, 4);
     const bool table_mag = mag && c->mag_step;
     if (flow || table_mag) {
-        launch_table_m(c->stream, flow, table_mag, c->inv_f, c->M, c->table_f, ts, c->sums);
+        launch_table_m(c->stream, flow, table_mag, c->ir_f, c->M, c->table_f, ts, c->sums);
         ++*nl;
         CKR(check_launch(c, "table (mixed)"));
     }
@@ -532,7 +562,7 @@ static void destroy_impl(ss_ctx *c) {
     for (auto &kv : c->plans_c) cufftDestroy(kv.second);
     for (int b = 0; b < 2; ++b)
         for (int k = 0; k < 2; ++k) cudaFree(c->pa[b][k]);
-    cudaFree(c->fwd_f); cudaFree(c->inv_f); cudaFree(c->table_f); cudaFree(c->kern_f); cudaFree(c->partials);
+    cudaFree(c->fr_f); cudaFree(c->ir_f); cudaFree(c->ii_f); cudaFree(c->fwd_f); cudaFree(c->inv_f); cudaFree(c->table_f); cudaFree(c->kern_f); cudaFree(c->partials);
     cudaFree(c->kslice); cudaFree(c->kfactor);
     cudaFree(c->dn_x); cudaFree(c->dn_y);
     cudaFree(c->sums);
@@ -717,8 +747,9 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
                 dims[k] = dims[k] / 2 + 1;
                 break;
             }
-        for (int k = 0; k < 3; ++k) P.hdim[k] = dims[k];
-        P.nhalf = dims[0] * dims[1] * dims[2];
+        for (int k = 0; k < 3; ++k) P.hdim[k] = c->M.hdim[k] = dims[k];
+        P.nhalf = c->M.nhalf = dims[0] * dims[1] * dims[2];
+        P.cstride = c->M.cstride = P.ncell + (P.ncell & 1);
     }
 
     auto alloc = [&](void **p, size_t bytes) -> int {
@@ -740,7 +771,7 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     for (int b = 0; b < 2 && rc == SS_OK; ++b) rc = alloc((void **)&c->counts[b], (size_t)P.nbins * sizeof(uint32_t));
     const size_t nhalf = (size_t)P.nhalf;
     if (!c->mixed) {
-        if (rc == SS_OK) rc = alloc((void **)&c->fr, 12 * ncell * sizeof(double));
+        if (rc == SS_OK) rc = alloc((void **)&c->fr, 12 * (size_t)P.cstride * sizeof(double));
         if (rc == SS_OK) rc = alloc((void **)&c->fwd, 12 * nhalf * sizeof(double2));
         if (rc == SS_OK) rc = alloc((void **)&c->invh, 24 * nhalf * sizeof(double2));
         if (rc == SS_OK) rc = alloc((void **)&c->ir, 24 * ncell * sizeof(double));
@@ -760,8 +791,10 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     if (rc == SS_OK) rc = alloc((void **)&c->d_scan, 2 * sizeof(unsigned long long));
     if (rc == SS_OK) rc = alloc((void **)&c->d_halfpi, 2 * sizeof(double));
     if (c->mixed) {
-        if (rc == SS_OK) rc = alloc((void **)&c->fwd_f, 12 * ncell * sizeof(float2));
-        if (rc == SS_OK) rc = alloc((void **)&c->inv_f, 24 * ncell * sizeof(float2));
+        if (rc == SS_OK) rc = alloc((void **)&c->fr_f, 12 * (size_t)P.cstride * sizeof(float));
+        if (rc == SS_OK) rc = alloc((void **)&c->ir_f, 24 * ncell * sizeof(float));
+        if (rc == SS_OK) rc = alloc((void **)&c->fwd_f, 12 * nhalf * sizeof(float2));
+        if (rc == SS_OK) rc = alloc((void **)&c->inv_f, 24 * nhalf * sizeof(float2));
         if (rc == SS_OK) rc = alloc((void **)&c->table_f, ncell * TABLE_STRIDE_MAG * sizeof(float));
         if (rc == SS_OK) rc = alloc((void **)&c->kern_f, 12 * nang * sizeof(float));
         if (rc == SS_OK) rc = alloc((void **)&c->sums, 12 * sizeof(double));
@@ -782,7 +815,7 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
         }                                                                                             \
     } while (0)
     if (!c->mixed) {
-        CKC(cudaMemsetAsync(c->fr, 0, 12 * ncell * sizeof(double), c->stream));
+        CKC(cudaMemsetAsync(c->fr, 0, 12 * (size_t)P.cstride * sizeof(double), c->stream));
         CKC(cudaMemsetAsync(c->fwd, 0, 12 * nhalf * sizeof(double2), c->stream));
         CKC(cudaMemsetAsync(c->ir, 0, 24 * ncell * sizeof(double), c->stream));
     }
@@ -807,7 +840,7 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
                         c->stream));
     std::vector<float> Kf(K.begin(), K.end());
     if (c->mixed) {
-        CKC(cudaMemsetAsync(c->inv_f, 0, 24 * ncell * sizeof(float2), c->stream));
+        CKC(cudaMemsetAsync(c->ir_f, 0, 24 * ncell * sizeof(float), c->stream));
         CKC(cudaMemsetAsync(c->sums, 0, 12 * sizeof(double), c->stream));
         CKC(cudaMemsetAsync(c->partials, 0, partials_bytes(ncell), c->stream));
         c->partials_done = reinterpret_cast<unsigned *>(c->partials + 12ull * contract_m_blocks((int)ncell));
@@ -827,8 +860,8 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
         cufftHandle h;
         int r1 = SS_OK, r2 = SS_OK;
         if (c->fft_rank > 0) {
-            r1 = c->mixed ? get_plan_c(c, c->mag_step ? 12 : 9, &h) : get_plan(c, c->mag_step ? 12 : 9, 1, &h);
-            r2 = (r1 == SS_OK) ? (c->mixed ? get_plan_c(c, c->mag_step ? 24 : 12, &h)
+            r1 = c->mixed ? get_plan_c(c, c->mag_step ? 12 : 9, 1, &h) : get_plan(c, c->mag_step ? 12 : 9, 1, &h);
+            r2 = (r1 == SS_OK) ? (c->mixed ? get_plan_c(c, c->mag_step ? 24 : 12, 2, &h)
                                            : get_plan(c, c->mag_step ? 24 : 12, 2, &h))
                                : r1;
         }
@@ -1263,12 +1296,25 @@ static int ensure_magnetic(ss_ctx *c) {
 }
 
 // mixed mode: the FP32 fields widened into the FP64 buffer the getters read,
-// with the FP64 mean dipolar field added back
+// with the FP64 mean dipolar field added back; the imaginary parts (the
+// reference's complex inverse) from the anti-Hermitian part of the operators,
+// as for the FP64 path
 static int widen_fields(ss_ctx *c) {
     if (!c->mixed || c->wide_valid) return SS_OK;
-    const int nc = c->P.ncell;
-    launch_widen_m(c->stream, c->inv_f, 24ll * nc, nc, 0, 21, 24, c->sums, c->inv);
-    c->launches += 1;
+    const long long nc = c->P.ncell, nh = c->P.nhalf;
+    if (!c->ii_f) CK(cudaMalloc((void **)&c->ii_f, 24ull * c->P.ncell * sizeof(float)));
+    launch_kspace_m(c->stream, true, false, true, c->fwd_f, c->inv_f, c->M, (float)c->screening_last);
+    CKR(check_launch(c, "kspace (mixed, imaginary parts)"));
+    CKR(fft_c2r_f(c, c->inv_f, c->ii_f, 12));
+    if (c->mag_step || c->fields_mag_valid) {
+        launch_kspace_m(c->stream, false, true, true, c->fwd_f, c->inv_f, c->M, 0.f);
+        CKR(check_launch(c, "kspace (mixed, imaginary parts)"));
+        CKR(fft_c2r_f(c, c->inv_f + 12 * nh, c->ii_f + 12 * nc, 12));
+    } else {
+        CK(cudaMemsetAsync(c->ii_f + 12 * nc, 0, 12 * nc * sizeof(float), c->stream));
+    }
+    launch_widen_m(c->stream, c->ir_f, c->ii_f, 24ll * nc, (int)nc, 0, 21, 24, c->sums, c->inv);
+    c->launches += 3;
     CKR(check_launch(c, "widen"));
     c->wide_valid = true;
     return SS_OK;

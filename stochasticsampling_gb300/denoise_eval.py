@@ -38,24 +38,41 @@ PARAMS = dict(timestep=0.005, trans_diffusion=0.1, rot_diffusion=1.0, stress_act
 SHAPE = (GRID[0], GRID[1], GRID[3])
 
 
-def initial_rows(n, amp=0.01, seed=1, phase=0.0, axis=0):
+def initial_rows(n, amp=0.01, seed=1, phase=0.0, axis=0, out=None):
     """n particles of the workload's initial-condition family: density
     1 + amp sin(2 pi s / L + phase) along `axis` (0: x, 1: y; inverse CDF by
-    Newton), uniform along the other axis and in phi."""
-    rng = np.random.default_rng(seed)
+    Newton), uniform along the other axis and in phi.  Large n is drawn in
+    chunks of 2^22 rows on a thread pool (numpy releases the interpreter lock
+    inside its array loops), chunk k from its own stream (seed, k)."""
+    from concurrent.futures import ThreadPoolExecutor
+    rows = np.empty((n, 5)) if out is None else out
     L = BOX[axis]
-    u = rng.random(n)
-    s = u * L
     w = 2 * np.pi / L
-    for _ in range(8):
-        f = s / L + amp * (np.cos(phase) - np.cos(w * s + phase)) / (2 * np.pi) - u
-        s -= f / ((1 + amp * np.sin(w * s + phase)) / L)
-    rows = np.empty((n, 5))
-    rows[:, axis] = np.mod(s, L)
-    rows[:, 1 - axis] = BOX[1 - axis] * rng.random(n)
-    rows[:, 2] = 0.0
-    rows[:, 3] = 2 * np.pi * rng.random(n)
-    rows[:, 4] = np.pi / 2
+    chunk = 1 << 22
+
+    def fill(k):
+        lo, hi = k * chunk, min(n, (k + 1) * chunk)
+        rng = np.random.default_rng([seed, k]) if n > chunk else np.random.default_rng(seed)
+        m = hi - lo
+        u = rng.random(m)
+        s = u * L
+        for _ in range(8):
+            f = s / L + amp * (np.cos(phase) - np.cos(w * s + phase)) / (2 * np.pi) - u
+            s -= f / ((1 + amp * np.sin(w * s + phase)) / L)
+        r = rows[lo:hi]
+        r[:, axis] = np.mod(s, L)
+        r[:, 1 - axis] = BOX[1 - axis] * rng.random(m)
+        r[:, 2] = 0.0
+        r[:, 3] = 2 * np.pi * rng.random(m)
+        r[:, 4] = np.pi / 2
+
+    nchunks = -(-n // chunk)
+    if nchunks == 1:
+        fill(0)
+    else:
+        import os
+        with ThreadPoolExecutor(max_workers=min(nchunks, os.cpu_count() or 1)) as ex:
+            list(ex.map(fill, range(nchunks)))
     return rows
 
 
@@ -105,9 +122,13 @@ def method_pairs(npairs, n_in=1_000_000, n_target=64_000_000, amp_max=0.05, step
     every = max(1, steps // snapshots)
     k = 0
     t_sim = 0.0
+    # one pinned host buffer and one device buffer for every snapshot's rows
+    host = torch.empty((n_target, 5), dtype=torch.float64, pin_memory=True)
+    dev = torch.empty((n_target, 5), dtype=torch.float64, device="cuda")
     for run in range(nruns):
         amp, phase, axis = rng.uniform(0.0, amp_max), rng.uniform(0.0, 2 * np.pi), int(rng.integers(2))
-        rows = initial_rows(n_target, amp=amp, seed=int(rng.integers(1 << 31)), phase=phase, axis=axis)
+        rows = initial_rows(n_target, amp=amp, seed=int(rng.integers(1 << 31)), phase=phase, axis=axis,
+                            out=host.numpy())
         p = dict(PARAMS, number_of_particles=n_target, seed=int(rng.integers(1 << 31)))
         sim = ss.Simulation(grid=GRID, box=BOX, params=p, quasi2d=True, sort=False)
         sim.init(rows)
@@ -119,7 +140,8 @@ def method_pairs(npairs, n_in=1_000_000, n_target=64_000_000, amp_max=0.05, step
                 sim.run(every)
                 sim.synchronize()
                 t_sim += time.perf_counter() - t0
-            dev = torch.from_numpy(sim.get_particles()).cuda()
+            sim.get_particles(out=host.numpy())
+            dev.copy_(host)
             full = _subset_counts(lib, dev, 0, n_target, den_over_vol, dist)
             for j in range(per_snap):
                 if k >= npairs:
@@ -128,8 +150,8 @@ def method_pairs(npairs, n_in=1_000_000, n_target=64_000_000, amp_max=0.05, step
                 X[k] = (c * (nbins / n_in)).float().reshape(SHAPE)
                 T[k] = ((full - c) * (nbins / (n_target - n_in))).float().reshape(SHAPE)
                 k += 1
-            del dev
         sim.close()
+    del host, dev
     torch.cuda.synchronize()
     info = {"runs": nruns, "snapshots_per_run": snapshots, "steps_between_snapshots": every,
             "pairs_per_snapshot": per_snap, "simulation_seconds": t_sim}

@@ -128,7 +128,7 @@ def test_ensemble_one_step_against_oracle(oracle):
         g.close()
         o.init(r)
         h = oracle.histogram(st, o.particles()).ravel()
-        c = ens.get_counts(i).astype(np.float64)
+        c = ens.get_counts(i).astype(np.float64).ravel()
         assert c.sum() == n and np.abs(c - h).sum() <= 2e-3 * n, i
         o.do_timestep(noise)
         oracles.append(o)
