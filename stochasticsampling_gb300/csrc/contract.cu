@@ -84,24 +84,27 @@ __device__ __forceinline__ void stage_rows(const uint32_t *__restrict__ src, con
     }
 }
 
-// a float pair (hi, lo) summed over the warp by error-free transformations;
-// every lane ends with the same pair, returned as hi + lo in FP64
-__device__ __forceinline__ double warp_pair_sum(float v) {
-    float hi = v, lo = 0.f;
+// Float pairs (hi, lo), an unevaluated sum of two floats (about 48 bits),
+// added by error-free transformations (Knuth's two-sum, then a fast two-sum
+// to renormalise); every operation is on the FP32 pipe.
+struct FPair {
+    float hi, lo;
+};
+__device__ __forceinline__ FPair pair_add(FPair a, FPair b) {
+    const float s = a.hi + b.hi, bb = s - a.hi;
+    const float e = (a.hi - (s - bb)) + (b.hi - bb);  // (a.hi + b.hi) - s exactly
+    const float lo = (a.lo + b.lo) + e;
+    const float h = s + lo;
+    return FPair{h, lo - (h - s)};
+}
+// the pair summed over the warp in a fixed butterfly order (every lane ends
+// with the same pair)
+__device__ __forceinline__ FPair warp_pair_sum(FPair v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        const float h2 = __shfl_xor_sync(0xffffffffu, hi, o), l2 = __shfl_xor_sync(0xffffffffu, lo, o);
-        const float s = hi + h2, bb = s - hi;
-        const float e = (hi - (s - bb)) + (h2 - bb);  // (hi + h2) - s exactly (Knuth's two-sum)
-        lo = (lo + l2) + e;
-        hi = s;
+        const FPair w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+        v = pair_add(v, w);
     }
-    return (double)hi + (double)lo;
-}
-
-__device__ __forceinline__ double warp_sum_d(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
@@ -116,7 +119,7 @@ __global__ void __launch_bounds__(kCTile) k_contract_x(const uint32_t *__restric
                                                        const double *__restrict__ lut, int lut_n, DevParams P,
                                                        Staging S, double *__restrict__ fwd,
                                                        double *__restrict__ table, int tstride,
-                                                       uint32_t *__restrict__ cellcount) {
+                                                       uint32_t *__restrict__ cellcount, double dfac) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int na = S.na;
     float *ks = reinterpret_cast<float *>(smem);  // [chunk angle][48]
@@ -173,7 +176,6 @@ __global__ void __launch_bounds__(kCTile) k_contract_x(const uint32_t *__restric
         }
     }
     if (!live) return;
-    const int nc = P.ncell;
     double sig[12];
     if (csum <= kExactCells) {
 #pragma unroll
@@ -215,7 +217,9 @@ __global__ void __launch_bounds__(kCTile) k_contract_x(const uint32_t *__restric
 #pragma unroll
         for (int j = 9; j < 12; ++j) fwd[(long long)j * P.cstride + cell] = sig[j];
     }
-    const double dens = (((double)csum / P.dist_den) * P.volume) * P.dthph;
+    // (count / D) V dtheta dphi with the factor V / D dtheta dphi formed once: a
+    // division per cell costs ~20 FP64 operations on GB300's narrow FP64 pipe
+    const double dens = (double)csum * dfac;
     table[(long long)cell * tstride + T_DIFF] = sqrt(2.0 * P.dt * (P.Dt + P.volex * dens));
     if (tstride == TABLE_STRIDE_MAG) table[(long long)cell * tstride + T_DENS] = dens;
     cellcount[cell] = csum;
@@ -223,121 +227,145 @@ __global__ void __launch_bounds__(kCTile) k_contract_x(const uint32_t *__restric
 
 // ---------------------------------------------------------------------------
 // FP32 mixed path.  DIST: the tile holds the bits of an FP32 distribution
-// (the denoised histogram) instead of counts.
+// (the denoised histogram) instead of counts.  A persistent grid (a few
+// blocks per SM) walks the cell tiles in a fixed pattern; every thread keeps
+// float-pair sums of its cells' components, the block adds its threads'
+// pairs in a fixed order, and the last block to finish adds the blocks'
+// pairs in block order and writes the FP64 sums.  No FP64 arithmetic runs
+// per cell (GB300 executes FP64 at 1/64 of the FP32 rate).
 // ---------------------------------------------------------------------------
 template <bool STRESS, bool MAG, bool DIST>
 __global__ void __launch_bounds__(kCTile) k_contract_f(const uint32_t *__restrict__ src_bins,
                                                        const float *__restrict__ kern, MixedParams M, Staging S,
                                                        float scale, float dscale, float *__restrict__ fwd,
                                                        float *__restrict__ table, int tstride,
-                                                       double *__restrict__ partials, unsigned *__restrict__ done,
+                                                       float2 *__restrict__ partials, unsigned *__restrict__ done,
                                                        double *__restrict__ sums) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ double red[kCTile / 32][12];
+    __shared__ FPair red[kCTile / 32][12];
     __shared__ bool s_last;
     const int na = S.na;
     float *kf = reinterpret_cast<float *>(smem);  // [chunk angle][12]
     uint32_t *tile = reinterpret_cast<uint32_t *>(kf + (na < kAngChunk ? na : kAngChunk) * 12);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, cell0 = blockIdx.x * kCTile;
-    const int tc = min(kCTile, M.ncell - cell0);
-    const bool live = tid < tc;
-    const int cell = cell0 + tid;
-    float acc[12];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nc = M.ncell, ntiles = (nc + kCTile - 1) / kCTile;
+    FPair tot[12];
 #pragma unroll
-    for (int j = 0; j < 12; ++j) acc[j] = 0.f;
-    float dsum = 0.f;
-    uint32_t csum = 0;
-    const uint32_t *src = src_bins + (long long)cell0 * na;
-    for (int a0 = 0; a0 < na; a0 += kAngChunk) {
-        const int ach = min(kAngChunk, na - a0);
-        __syncthreads();
-        // the chunk's angle kernels, transposed to [angle][component]
-        for (int i = tid; i < 12 * ach; i += kCTile) {
-            const int j = i / ach, a = i - j * ach;
-            kf[a * 12 + j] = __ldg(kern + (long long)j * na + a0 + a);
-        }
-        stage_rows(src, S, a0, ach, tc, tile);
-        __syncthreads();
-        if (live) {
-            const uint32_t *row = tile + tid * S.stride;
-            for (int a = 0; a < ach; ++a) {
-                const uint32_t w = row[a];
-                float f;
-                if (DIST) {
-                    f = __uint_as_float(w);
-                    dsum += f;
-                } else {
-                    f = __uint2float_rn(w);
-                    csum += w;
-                }
-                const float4 *k4 = reinterpret_cast<const float4 *>(kf + a * 12);
-                if (STRESS) {
+    for (int j = 0; j < 12; ++j) tot[j] = FPair{0.f, 0.f};
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int cell0 = t * kCTile, tc = min(kCTile, nc - cell0);
+        const bool live = tid < tc;
+        const int cell = cell0 + tid;
+        float acc[12];
 #pragma unroll
-                    for (int q = 0; q < 2; ++q) {
-                        const float4 k = k4[q];
-                        acc[4 * q + 0] = fmaf(k.x, f, acc[4 * q + 0]);
-                        acc[4 * q + 1] = fmaf(k.y, f, acc[4 * q + 1]);
-                        acc[4 * q + 2] = fmaf(k.z, f, acc[4 * q + 2]);
-                        acc[4 * q + 3] = fmaf(k.w, f, acc[4 * q + 3]);
+        for (int j = 0; j < 12; ++j) acc[j] = 0.f;
+        float dsum = 0.f;
+        uint32_t csum = 0;
+        const uint32_t *src = src_bins + (long long)cell0 * na;
+        for (int a0 = 0; a0 < na; a0 += kAngChunk) {
+            const int ach = min(kAngChunk, na - a0);
+            __syncthreads();
+            // the chunk's angle kernels, transposed to [angle][component]
+            for (int i = tid; i < 12 * ach; i += kCTile) {
+                const int j = i / ach, a = i - j * ach;
+                kf[a * 12 + j] = __ldg(kern + (long long)j * na + a0 + a);
+            }
+            stage_rows(src, S, a0, ach, tc, tile);
+            __syncthreads();
+            if (live) {
+                const uint32_t *row = tile + tid * S.stride;
+                for (int a = 0; a < ach; ++a) {
+                    const uint32_t w = row[a];
+                    float f;
+                    if (DIST) {
+                        f = __uint_as_float(w);
+                        dsum += f;
+                    } else {
+                        f = __uint2float_rn(w);
+                        csum += w;
                     }
-                }
-                if (STRESS || MAG) {
-                    const float4 k = k4[2];
-                    if (STRESS) acc[8] = fmaf(k.x, f, acc[8]);
-                    if (MAG) {
-                        acc[9] = fmaf(k.y, f, acc[9]);
-                        acc[10] = fmaf(k.z, f, acc[10]);
-                        acc[11] = fmaf(k.w, f, acc[11]);
+                    const float4 *k4 = reinterpret_cast<const float4 *>(kf + a * 12);
+                    if (STRESS) {
+#pragma unroll
+                        for (int q = 0; q < 2; ++q) {
+                            const float4 k = k4[q];
+                            acc[4 * q + 0] = fmaf(k.x, f, acc[4 * q + 0]);
+                            acc[4 * q + 1] = fmaf(k.y, f, acc[4 * q + 1]);
+                            acc[4 * q + 2] = fmaf(k.z, f, acc[4 * q + 2]);
+                            acc[4 * q + 3] = fmaf(k.w, f, acc[4 * q + 3]);
+                        }
+                    }
+                    if (STRESS || MAG) {
+                        const float4 k = k4[2];
+                        if (STRESS) acc[8] = fmaf(k.x, f, acc[8]);
+                        if (MAG) {
+                            acc[9] = fmaf(k.y, f, acc[9]);
+                            acc[10] = fmaf(k.z, f, acc[10]);
+                            acc[11] = fmaf(k.w, f, acc[11]);
+                        }
                     }
                 }
             }
         }
-    }
-    const int nc = M.ncell;
-    float out[12];
+        if (live) {
+            float out[12];
 #pragma unroll
-    for (int j = 0; j < 12; ++j) out[j] = acc[j] * scale;
-    if (live) {
-        if (STRESS) {
+            for (int j = 0; j < 12; ++j) out[j] = acc[j] * scale;
+            if (STRESS) {
 #pragma unroll
-            for (int j = 0; j < 9; ++j) fwd[(long long)j * M.cstride + cell] = out[j];
+                for (int j = 0; j < 9; ++j) fwd[(long long)j * M.cstride + cell] = out[j];
+            }
+            if (MAG) {
+#pragma unroll
+                for (int j = 9; j < 12; ++j) fwd[(long long)j * M.cstride + cell] = out[j];
+            }
+#pragma unroll
+            for (int j = 0; j < 12; ++j)
+                if ((j < 9 && STRESS) || (j >= 9 && MAG)) tot[j] = pair_add(tot[j], FPair{out[j], 0.f});
+            // density = (count / D) V dtheta dphi; dscale = V / D dtheta dphi (or the distribution's scale)
+            const float dens = DIST ? dsum * dscale : (float)csum * dscale;
+            table[(long long)cell * tstride + T_DIFF] = sqrtf(M.two_dt * (M.Dt + M.volex * dens));
         }
-        if (MAG) {
-#pragma unroll
-            for (int j = 9; j < 12; ++j) fwd[(long long)j * M.cstride + cell] = out[j];
-        }
-        const float dens = DIST ? dsum * dscale * M.dthph
-                                : (float)(((double)csum / M.dist_den) * M.volume) * M.dthph;
-        table[(long long)cell * tstride + T_DIFF] = sqrtf(M.two_dt * (M.Dt + M.volex * dens));
     }
-    // the block's component sums in a fixed order
+    // the block's pairs: warp butterflies, then the warps in order
 #pragma unroll
     for (int j = 0; j < 12; ++j) {
         if ((j < 9 && STRESS) || (j >= 9 && MAG)) {
-            const double v = warp_pair_sum(live ? out[j] : 0.f);
+            const FPair v = warp_pair_sum(tot[j]);
             if (lane == 0) red[warp][j] = v;
         }
     }
     __syncthreads();
     if (tid < 12 && ((tid < 9 && STRESS) || (tid >= 9 && MAG))) {
-        double v = 0.0;
+        FPair v = red[0][tid];
 #pragma unroll
-        for (int w = 0; w < kCTile / 32; ++w) v += red[w][tid];
-        partials[(long long)blockIdx.x * 12 + tid] = v;
+        for (int w = 1; w < kCTile / 32; ++w) v = pair_add(v, red[w][tid]);
+        partials[(long long)blockIdx.x * 12 + tid] = make_float2(v.hi, v.lo);
         __threadfence();
     }
     __syncthreads();
     if (tid == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
     __syncthreads();
     if (!s_last) return;
-    // the last block: the blocks' sums in block order
+    // the last block: each thread adds a fixed, strided subset of the blocks'
+    // pairs, then the threads' pairs in a fixed tree
     __threadfence();
-    for (int j = warp; j < 12; j += kCTile / 32) {
-        if ((j < 9 && STRESS) || (j >= 9 && MAG)) {
-            double v = 0.0;
-            for (int b = lane; b < (int)gridDim.x; b += 32) v += __ldcg(partials + (long long)b * 12 + j);
-            v = warp_sum_d(v);
-            if (lane == 0) sums[j] = v;
+    for (int j = 0; j < 12; ++j) {
+        if (!((j < 9 && STRESS) || (j >= 9 && MAG))) continue;
+        FPair v{0.f, 0.f};
+        for (int b = tid; b < (int)gridDim.x; b += kCTile) {
+            const float2 q = __ldcg(partials + (long long)b * 12 + j);
+            v = pair_add(v, FPair{q.x, q.y});
+        }
+        v = warp_pair_sum(v);
+        __syncthreads();
+        if (lane == 0) red[warp][0] = v;
+        __syncthreads();
+        if (tid == 0) {
+            FPair t = red[0][0];
+#pragma unroll
+            for (int w = 1; w < kCTile / 32; ++w) t = pair_add(t, red[w][0]);
+            sums[j] = (double)t.hi + (double)t.lo;
         }
     }
     if (tid == 0) *done = 0u;  // ready for the next launch
@@ -416,29 +444,36 @@ void launch_contract_x(cudaStream_t s, bool stress, bool mag, const uint32_t *co
     const Staging S = make_staging(P.nang);
     const size_t sm = smem_x(P.nang);
     const unsigned b = tiles(P.ncell);
+    const double dfac = (P.volume / P.dist_den) * P.dthph;
 #define SS_CX(ST, MG)                                                                                        \
     k_contract_x<ST, MG><<<b, kCTile, sm, s>>>(counts, kslice, factor, kern, lut, lut_n, P, S, fwd, table, \
-                                               tstride, cellcount)
+                                               tstride, cellcount, dfac)
     if (stress && mag) SS_CX(true, true);
     else if (stress) SS_CX(true, false);
     else SS_CX(false, true);
 #undef SS_CX
 }
 
-unsigned contract_m_blocks(int ncell) { return tiles(ncell); }
+// the persistent grid of the FP32 contraction: at most kMBlocksPerSM blocks per SM
+constexpr int kMBlocksPerSM = 8;
+unsigned contract_m_blocks(int ncell, int sms) {
+    const unsigned t = tiles(ncell), cap = (unsigned)(kMBlocksPerSM * (sms > 0 ? sms : 1));
+    return t < cap ? t : cap;
+}
 
 void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kern,
-                       const MixedParams &M, float *fwd, float *table, int tstride, double *partials,
-                       unsigned *done, double *sums, const float *dist, float fscale) {
+                       const MixedParams &M, float *fwd, float *table, int tstride, float2 *partials,
+                       unsigned *done, double *sums, int sms, const float *dist, float fscale) {
     const Staging S = make_staging(M.nang);
     const size_t sm = smem_f(M.nang);
-    const unsigned b = tiles(M.ncell);
+    const unsigned b = contract_m_blocks(M.ncell, sms);
     const bool fd = dist != nullptr;
     const uint32_t *src = fd ? reinterpret_cast<const uint32_t *>(dist) : counts;
     // counts: f = count, scaled by measure * V / D; a distribution: f = value, scaled by measure * fscale
     const float scale = fd ? M.measure * fscale : (float)((double)M.measure * (M.volume / M.dist_den));
+    const float dscale = fd ? fscale * M.dthph : (float)((M.volume / M.dist_den) * (double)M.dthph);
 #define SS_CF(ST, MG, D)                                                                                    \
-    k_contract_f<ST, MG, D><<<b, kCTile, sm, s>>>(src, kern, M, S, scale, fscale, fwd, table, tstride,    \
+    k_contract_f<ST, MG, D><<<b, kCTile, sm, s>>>(src, kern, M, S, scale, dscale, fwd, table, tstride,   \
                                                   partials, done, sums)
     if (stress && mag) { if (fd) SS_CF(true, true, true); else SS_CF(true, true, false); }
     else if (stress) { if (fd) SS_CF(true, false, true); else SS_CF(true, false, false); }

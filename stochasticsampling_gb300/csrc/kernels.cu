@@ -259,7 +259,6 @@ __global__ void __launch_bounds__(64) k_contract(const uint32_t *__restrict__ co
         }
         acc[12] += f;
     }
-    const int nc = P.ncell;
     if (STRESS) {
 #pragma unroll
         for (int j = 0; j < 9; ++j) fwd[(long long)j * P.cstride + cell] = acc[j] * P.measure;

@@ -38,16 +38,16 @@ void launch_egest_m(cudaStream_t s, bool fixed, unsigned long long n, const Mixe
                     float *const as[2], const uint32_t *id, double *aos);
 void launch_bin_m(cudaStream_t s, bool fixed, unsigned long long n, const MixedParams &M, double *const xs[3],
                   float *const as[2], uint32_t *key, uint32_t *counts);
-// the FP32 angular contraction (contract.cu): real fwd [12][ncell], the table's
-// diffusion length and the FP64 component sums (sums[0..9) with stress,
-// sums[9..12) with the polarisation) in a fixed order.  partials:
-// contract_m_blocks(ncell) x 12 doubles; done: a counter that is 0 between
-// launches.  dist != nullptr: an FP32 distribution times fscale replaces the
-// counts (the denoised histogram).
-unsigned contract_m_blocks(int ncell);
+// the FP32 angular contraction (contract.cu): real fwd [12][cstride], the
+// table's diffusion length and the FP64 component sums (sums[0..9) with
+// stress, sums[9..12) with the polarisation) in a fixed order.  partials:
+// contract_m_blocks(ncell, sms) x 12 float pairs; done: a counter that is 0
+// between launches; sms: multiprocessors of the device.  dist != nullptr: an
+// FP32 distribution times fscale replaces the counts (the denoised histogram).
+unsigned contract_m_blocks(int ncell, int sms);
 void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kern,
-                       const MixedParams &M, float *fwd, float *table, int tstride, double *partials,
-                       unsigned *done, double *sums, const float *dist = nullptr, float fscale = 0.f);
+                       const MixedParams &M, float *fwd, float *table, int tstride, float2 *partials,
+                       unsigned *done, double *sums, int sms, const float *dist = nullptr, float fscale = 0.f);
 void launch_counts_to_unit(cudaStream_t s, const uint32_t *counts, long long nbins, float inv_mean, float *x);
 // the FP64 means removed from the real fields fr [comp][cstride], components c0 .. c1
 void launch_center_m(cudaStream_t s, float *fr, int c0, int c1, int ncell, int cstride, const double *sums);

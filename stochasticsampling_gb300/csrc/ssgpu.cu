@@ -53,6 +53,7 @@ struct ss_ctx {
     uint32_t flags = 0;
     DevParams P{};
     int device = 0;
+    int sms = 1;  // multiprocessors of the device
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     bool q2d = false, mag_step = false, sort = true, use_graph = true;
@@ -98,7 +99,7 @@ struct ss_ctx {
     float2 *fwd_f = nullptr, *inv_f = nullptr;               // half spectra [12][nhalf], [24][nhalf]
     float *table_f = nullptr, *kern_f = nullptr;
     double *sums = nullptr;  // FP64 per-component sums for the mean handling
-    double *partials = nullptr;  // per-block component sums of the FP32 contraction (+ its counter)
+    float2 *partials = nullptr;  // per-block float-pair component sums of the FP32 contraction (+ its counter)
     unsigned *partials_done = nullptr;
     bool wide_valid = false;  // inv (FP64) holds the widened mixed fields
     std::map<int, cufftHandle> plans_c;  // key: batch * 4 + kind (1 R2C, 2 C2R)
@@ -120,7 +121,9 @@ struct ss_ctx {
 };
 
 // the FP32 contraction's per-block component sums and, after them, its counter
-static size_t partials_bytes(uint64_t ncell) { return (12ull * contract_m_blocks((int)ncell) + 1) * sizeof(double); }
+static size_t partials_bytes(uint64_t ncell, int sms) {
+    return (12ull * contract_m_blocks((int)ncell, sms) + 1) * sizeof(float2);
+}
 
 // ---------------------------------------------------------------------------
 // error helpers
@@ -386,10 +389,10 @@ static int enqueue_solve_m(ss_ctx *c, bool flow, bool mag, const uint32_t *count
         launch_counts_to_unit(c->stream, counts, c->P.nbins, c->dn_inv_mean, c->dn_x);
         *nl += 1 + dn_enqueue_forward(c->dn, c->dn_x, c->dn_y, c->stream);
         launch_contract_m(c->stream, flow, mag, counts, c->kern_f, c->M, c->fr_f, c->table_f, ts, c->partials,
-                          c->partials_done, c->sums, c->dn_y, c->dn_fscale);
+                          c->partials_done, c->sums, c->sms, c->dn_y, c->dn_fscale);
     } else {
         launch_contract_m(c->stream, flow, mag, counts, c->kern_f, c->M, c->fr_f, c->table_f, ts, c->partials,
-                          c->partials_done, c->sums);
+                          c->partials_done, c->sums, c->sms);
     }
     if (flow) launch_center_m(c->stream, c->fr_f, 0, 9, nc, c->P.cstride, c->sums);
     if (mag) launch_center_m(c->stream, c->fr_f, 9, 12, nc, c->P.cstride, c->sums);
@@ -639,10 +642,12 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     c->mag_step = (flags & SS_FLAG_ALWAYS_MAGNETIC) || params->magnetic_dipole_dipole != 0.0 ||
                   params->magnetic_drag != 0.0;
     cudaError_t e = cudaGetDevice(&c->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
     if (e != cudaSuccess) {
         destroy_impl(c);
         return fail(nullptr, SS_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
     }
+    if (c->sms < 1) c->sms = 1;
     if (stream) {
         c->stream = (cudaStream_t)stream;
     } else {
@@ -798,7 +803,7 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
         if (rc == SS_OK) rc = alloc((void **)&c->table_f, ncell * TABLE_STRIDE_MAG * sizeof(float));
         if (rc == SS_OK) rc = alloc((void **)&c->kern_f, 12 * nang * sizeof(float));
         if (rc == SS_OK) rc = alloc((void **)&c->sums, 12 * sizeof(double));
-        if (rc == SS_OK) rc = alloc((void **)&c->partials, partials_bytes(ncell));
+        if (rc == SS_OK) rc = alloc((void **)&c->partials, partials_bytes(ncell, c->sms));
     }
     if (rc != SS_OK) {
         std::string m = c->err;
@@ -842,8 +847,8 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
     if (c->mixed) {
         CKC(cudaMemsetAsync(c->ir_f, 0, 24 * ncell * sizeof(float), c->stream));
         CKC(cudaMemsetAsync(c->sums, 0, 12 * sizeof(double), c->stream));
-        CKC(cudaMemsetAsync(c->partials, 0, partials_bytes(ncell), c->stream));
-        c->partials_done = reinterpret_cast<unsigned *>(c->partials + 12ull * contract_m_blocks((int)ncell));
+        CKC(cudaMemsetAsync(c->partials, 0, partials_bytes(ncell, c->sms), c->stream));
+        c->partials_done = reinterpret_cast<unsigned *>(c->partials + 12ull * contract_m_blocks((int)ncell, c->sms));
         CKC(cudaMemcpyAsync(c->kern_f, Kf.data(), Kf.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     }
     CKC(contract_prepare());

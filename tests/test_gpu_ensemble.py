@@ -38,9 +38,13 @@ MEMBERS = [
 ]
 
 
-# flow after one step against the FP64 oracle: the FP32 binning moves a few
-# particles into a neighbouring bin, and the flow is built from those counts
-ENS_FLOW_TOL = 1e-2
+# flow after one step against the FP64 oracle: 2e-6 when the member's FP32
+# histogram equals the oracle's (measured 3e-7 .. 4.5e-7); when the FP32
+# binning put a few particles at bin edges into the neighbouring bin, the
+# flow (driven by the density fluctuations) moves with them (measured 2.4e-3
+# for 150,000 particles)
+ENS_FLOW_TOL_EXACT = 2e-6
+ENS_FLOW_TOL_EDGE = 1e-2
 
 
 def _members(spec=MEMBERS):
@@ -110,8 +114,9 @@ def test_ensemble_one_step_against_oracle(oracle):
     stand-alone mixed context with the member's seed (ss_noise), which the
     ensemble draws for that member.  The mixed path's per-field bounds hold:
     the initial histogram differs only for particles within FP32 rounding of
-    a bin edge, and the flow, positions and angles after the step are within
-    the FP32 bounds of tests/test_gpu_mixed.py."""
+    a bin edge, and the flow, positions (< 1e-8, measured <= 3.6e-9) and
+    angles (< 1e-6 rad RMS, measured <= 2.7e-7) after the step are within the
+    FP32 bounds of tests/test_gpu_mixed.py."""
     from test_gpu_parity import _pair
     ss = _gpu()
     spec = [MEMBERS[0], MEMBERS[2], MEMBERS[3]]
@@ -119,7 +124,7 @@ def test_ensemble_one_step_against_oracle(oracle):
     rows = _rows(np.random.default_rng(17), members)
     ens = ss.Ensemble(members)
     ens.init(rows)
-    oracles = []
+    oracles, same_hist = [], []
     for i, (grid, box, params, n, seed) in enumerate(spec):
         r = rows[ens.offsets[i]:ens.offsets[i + 1]]
         g, o, st = _pair(oracle, (f"member{i}", grid, box, params, n, True), seed=seed, mixed=True)
@@ -130,6 +135,7 @@ def test_ensemble_one_step_against_oracle(oracle):
         h = oracle.histogram(st, o.particles()).ravel()
         c = ens.get_counts(i).astype(np.float64).ravel()
         assert c.sum() == n and np.abs(c - h).sum() <= 2e-3 * n, i
+        same_hist.append(bool(np.array_equal(c, h)))
         o.do_timestep(noise)
         oracles.append(o)
     ens.run(1)
@@ -139,9 +145,9 @@ def test_ensemble_one_step_against_oracle(oracle):
         ex = rel_l2(ep[:, :2], op[:, :2])
         ephi = float(np.sqrt(np.mean(_wrapdiff(ep[:, 3], op[:, 3], 2 * np.pi) ** 2)))
         print(f"ensemble member {i} vs oracle: flow {eu:.3e} positions {ex:.3e} phi rms {ephi:.3e}")
-        assert eu < ENS_FLOW_TOL, (i, eu)
-        assert ex < 1e-6, (i, ex)
-        assert ephi < 1e-4, (i, ephi)
+        assert eu < (ENS_FLOW_TOL_EXACT if same_hist[i] else ENS_FLOW_TOL_EDGE), (i, eu, same_hist[i])
+        assert ex < 1e-8, (i, ex)
+        assert ephi < 1e-6, (i, ephi)
         assert np.all(ep[:, 2] == 0.0) and np.all(ep[:, 4] == np.pi / 2)
     ens.close()
 

@@ -4,12 +4,14 @@ accumulated in FP64 (SS_FLAG_MIXED) or in 64-bit fixed point (SS_FLAG_FIXED64).
 The mixed path keeps positions and the spectral k = 0 / mean handling in FP64
 and does everything else in FP32, so it is not held to 1e-12; each field's
 error against the FP64 oracle is bounded instead (one step from identical
-state and noise):
-  histogram       differs only for particles within FP32 rounding of a bin edge
-  u, grad u       relative L2 error < 1e-5
+state and noise; measured on GB300 in brackets):
+  histogram       differs only for particles within FP32 rounding of a bin
+                  edge (none for the seeded clouds of the one-step test)
+  u, grad u       relative L2 error < 2e-6 (1.8e-7 .. 3.8e-7)
   B               relative L2 error < 1e-5
-  positions       relative L2 error < 1e-8 (FP64 accumulation of FP32 steps)
-  orientations    relative L2 error < 1e-6
+  positions       relative L2 error < 5e-9 (4.7e-10 .. 1.1e-9; FP64
+                  accumulation of FP32 steps)
+  phi             RMS error < 1e-6 rad (1.8e-7 .. 2.0e-7)
 """
 import numpy as np
 import pytest
@@ -41,22 +43,22 @@ def test_mixed_one_step_errors(oracle, cfg, mode):
     c_g = g.get_counts().astype(np.float64)
     c_o = oracle.histogram(s, o.particles())
     assert c_g.sum() == n
-    assert np.abs(c_g - c_o).sum() <= 2e-3 * n  # FP32 binning at bin edges
+    # FP32 binning differs from the reference's only within FP32 rounding of a
+    # bin edge; none of these seeded particles lies that close
+    assert np.array_equal(c_g, c_o)
     g.do_timestep(noise)
     o.do_timestep(noise)
     u, gu = g.get_flow_complex()
     ou = o.flow()
-    # the reference histogram feeds the oracle; the mixed histogram differs
-    # in a few bins, so compare the fields relative to their norm
     eu, egu = rel_l2(u, ou), rel_l2(gu, o.flow_grad())
     gp, op = g.get_particles(), o.particles()
     ex = rel_l2(gp[:, :3], op[:, :3])
     ephi = float(np.sqrt(np.mean(_wrapdiff(gp[:, 3], op[:, 3], 2 * np.pi) ** 2)))
     print(f"mixed {cfg[0]} {mode}: hist {np.abs(c_g - c_o).sum() / n:.3e} u {eu:.3e} grad u {egu:.3e} "
           f"positions {ex:.3e} phi rms {ephi:.3e}")
-    assert eu < 1e-2 and egu < 1e-2
-    assert ex < 1e-6
-    assert ephi < 1e-4
+    assert eu < 2e-6 and egu < 2e-6
+    assert ex < 5e-9
+    assert ephi < 1e-6
     g.close()
 
 
