@@ -37,6 +37,9 @@
 #include "kernels.cuh"
 #include "mixed.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cmath>
 
 namespace ss {
@@ -371,6 +374,229 @@ __global__ void __launch_bounds__(kCTile) k_contract_f(const uint32_t *__restric
     if (tid == 0) *done = 0u;  // ready for the next launch
 }
 
+// ---------------------------------------------------------------------------
+// FP32 mixed path, TMA-staged (rows of a multiple of 16 bytes).  The
+// histogram, viewed as a 2-D tensor [ncell][nang] of u32, is copied tile by
+// tile -- 64 cells x 32 angles, 8 KB -- by the tensor memory accelerator
+// (cp.async.bulk.tensor.2d) into one of two shared-memory buffers, each
+// completing on its own mbarrier, two tiles ahead of the arithmetic: one
+// elected thread issues the copies, no thread spends instructions on
+// addresses, and the copies overlap the FMAs.  Angles past the row end and
+// cells past the grid arrive as zeros (the copy's out-of-bounds fill),
+// against zero-padded angle kernels.  The buffers keep the tensor's dense
+// layout (rows of 32 words); thread t visits its row's angles from
+// a = t mod 32 on, so a warp's 32 reads hit 32 banks, and the angle kernels
+// ([angle][12] floats, staged once per block) are then read 48 bytes apart,
+// which also maps a warp's 16-byte reads to distinct banks.  Every mbarrier
+// wait is bounded: on a timeout the kernel sets bit kErrTmaTimeout of err,
+// waits (bounded) for its own copies and leaves the sums wrong but the
+// launch protocol intact.
+// ---------------------------------------------------------------------------
+constexpr int kTmaBytes = kCTile * kAngChunk * 4;  // one tile: 8 KB
+constexpr uint32_t kWaitPolls = 1u << 22;
+constexpr unsigned kErrTmaTimeout = 0x100u;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(a), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t a, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t a, uint32_t parity) {
+    for (uint32_t i = 0; i < kWaitPolls; ++i)
+        if (mbar_try_wait(a, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
+            dst),
+        "l"(map), "r"(x), "r"(y), "r"(mbar)
+        : "memory");
+}
+
+template <bool STRESS, bool MAG, bool DIST>
+__global__ void __launch_bounds__(kCTile) k_contract_t(const __grid_constant__ CUtensorMap tmap,
+                                                       const float *__restrict__ kern_t, int na_pad, MixedParams M,
+                                                       float scale, float dscale, float *__restrict__ fwd,
+                                                       float *__restrict__ table, int tstride,
+                                                       float2 *__restrict__ partials, unsigned *__restrict__ done,
+                                                       double *__restrict__ sums, unsigned *__restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem_tma[];  // TMA destinations: 128-byte aligned at least
+    uint32_t *buf = reinterpret_cast<uint32_t *>(smem_tma);           // 2 tiles of [64][32] words
+    float *kf = reinterpret_cast<float *>(smem_tma + 2 * kTmaBytes);  // [na_pad][12]
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ FPair red[kCTile / 32][12];
+    __shared__ bool s_last;
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nc = M.ncell, ntiles = (nc + kCTile - 1) / kCTile, nch = na_pad / kAngChunk;
+    const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int nitems = my_tiles * nch;
+    for (int i = tid; i < na_pad * 3; i += kCTile)
+        reinterpret_cast<float4 *>(kf)[i] = __ldg(reinterpret_cast<const float4 *>(kern_t) + i);
+    const uint32_t mb0 = smem_addr(&mbar[0]), buf0 = smem_addr(buf);
+    if (tid == 0) {
+        mbar_init(mb0, 1);
+        mbar_init(mb0 + 8, 1);
+        s_fail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int k) {
+        const int m = k / nch, c = k - m * nch, t = (int)blockIdx.x + m * (int)gridDim.x;
+        const uint32_t b = (uint32_t)(k & 1);
+        mbar_expect_tx(mb0 + 8 * b, (uint32_t)kTmaBytes);
+        tma_load_2d(buf0 + b * (uint32_t)kTmaBytes, &tmap, c * kAngChunk, t * kCTile, mb0 + 8 * b);
+    };
+    if (tid == 0) {
+        if (nitems > 0) issue(0);
+        if (nitems > 1) issue(1);
+    }
+    FPair tot[12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) tot[j] = FPair{0.f, 0.f};
+    float acc[12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) acc[j] = 0.f;
+    float dsum = 0.f;
+    uint32_t csum = 0;
+    int k = 0;
+    for (; k < nitems; ++k) {
+        const int m = k / nch, c = k - m * nch;
+        if (c == 0) {
+#pragma unroll
+            for (int j = 0; j < 12; ++j) acc[j] = 0.f;
+            dsum = 0.f;
+            csum = 0;
+        }
+        // every thread observes the copy's completion (which makes its bytes visible to it)
+        if (!mbar_wait_bounded(mb0 + 8 * (uint32_t)(k & 1), (uint32_t)((k >> 1) & 1))) s_fail = 1;
+        __syncthreads();
+        if (s_fail) break;
+        const uint32_t *row = buf + (k & 1) * (kTmaBytes / 4) + tid * kAngChunk;
+        const float *kc = kf + c * kAngChunk * 12;
+#pragma unroll 4
+        for (int i = 0; i < kAngChunk; ++i) {
+            const int a = (i + tid) & (kAngChunk - 1);
+            const uint32_t w = row[a];
+            float f;
+            if (DIST) {
+                f = __uint_as_float(w);
+                dsum += f;
+            } else {
+                f = __uint2float_rn(w);
+                csum += w;
+            }
+            const float4 *k4 = reinterpret_cast<const float4 *>(kc + a * 12);
+            if (STRESS) {
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const float4 kv = k4[q];
+                    acc[4 * q + 0] = fmaf(kv.x, f, acc[4 * q + 0]);
+                    acc[4 * q + 1] = fmaf(kv.y, f, acc[4 * q + 1]);
+                    acc[4 * q + 2] = fmaf(kv.z, f, acc[4 * q + 2]);
+                    acc[4 * q + 3] = fmaf(kv.w, f, acc[4 * q + 3]);
+                }
+            }
+            if (STRESS || MAG) {
+                const float4 kv = k4[2];
+                if (STRESS) acc[8] = fmaf(kv.x, f, acc[8]);
+                if (MAG) {
+                    acc[9] = fmaf(kv.y, f, acc[9]);
+                    acc[10] = fmaf(kv.z, f, acc[10]);
+                    acc[11] = fmaf(kv.w, f, acc[11]);
+                }
+            }
+        }
+        __syncthreads();  // the buffer is consumed: the copy two tiles ahead may overwrite it
+        if (tid == 0 && k + 2 < nitems) {
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            issue(k + 2);
+        }
+        if (c == nch - 1) {
+            const int cell = ((int)blockIdx.x + m * (int)gridDim.x) * kCTile + tid;
+            if (cell < nc) {
+                float out[12];
+#pragma unroll
+                for (int j = 0; j < 12; ++j) out[j] = acc[j] * scale;
+                if (STRESS) {
+#pragma unroll
+                    for (int j = 0; j < 9; ++j) fwd[(long long)j * M.cstride + cell] = out[j];
+                }
+                if (MAG) {
+#pragma unroll
+                    for (int j = 9; j < 12; ++j) fwd[(long long)j * M.cstride + cell] = out[j];
+                }
+#pragma unroll
+                for (int j = 0; j < 12; ++j)
+                    if ((j < 9 && STRESS) || (j >= 9 && MAG)) tot[j] = pair_add(tot[j], FPair{out[j], 0.f});
+                const float dens = DIST ? dsum * dscale : (float)csum * dscale;
+                table[(long long)cell * tstride + T_DIFF] = sqrtf(M.two_dt * (M.Dt + M.volex * dens));
+            }
+        }
+    }
+    if (s_fail) {
+        // the copies this block issued and did not see land: wait for them (bounded) before leaving
+        if (tid == 0) {
+            atomicOr(err, kErrTmaTimeout);
+            for (int q = k; q < nitems && q < k + 2; ++q)
+                mbar_wait_bounded(mb0 + 8 * (uint32_t)(q & 1), (uint32_t)((q >> 1) & 1));
+        }
+        __syncthreads();
+    }
+    // the block's pairs: warp butterflies, then the warps in order
+#pragma unroll
+    for (int j = 0; j < 12; ++j) {
+        if ((j < 9 && STRESS) || (j >= 9 && MAG)) {
+            const FPair v = warp_pair_sum(tot[j]);
+            if (lane == 0) red[warp][j] = v;
+        }
+    }
+    __syncthreads();
+    if (tid < 12 && ((tid < 9 && STRESS) || (tid >= 9 && MAG))) {
+        FPair v = red[0][tid];
+#pragma unroll
+        for (int w = 1; w < kCTile / 32; ++w) v = pair_add(v, red[w][tid]);
+        partials[(long long)blockIdx.x * 12 + tid] = make_float2(v.hi, v.lo);
+        __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (int j = 0; j < 12; ++j) {
+        if (!((j < 9 && STRESS) || (j >= 9 && MAG))) continue;
+        FPair v{0.f, 0.f};
+        for (int b = tid; b < (int)gridDim.x; b += kCTile) {
+            const float2 q = __ldcg(partials + (long long)b * 12 + j);
+            v = pair_add(v, FPair{q.x, q.y});
+        }
+        v = warp_pair_sum(v);
+        __syncthreads();
+        if (lane == 0) red[warp][0] = v;
+        __syncthreads();
+        if (tid == 0) {
+            FPair t = red[0][0];
+#pragma unroll
+            for (int w = 1; w < kCTile / 32; ++w) t = pair_add(t, red[w][0]);
+            sums[j] = (double)t.hi + (double)t.lo;
+        }
+    }
+    if (tid == 0) *done = 0u;
+}
+
 Staging make_staging(int na) {
     Staging S;
     S.na = na;
@@ -435,6 +661,13 @@ cudaError_t contract_prepare() {
     set((const void *)k_contract_f<true, true, true>, bf);
     set((const void *)k_contract_f<true, false, true>, bf);
     set((const void *)k_contract_f<false, true, true>, bf);
+    const int bt = 64 * 1024;
+    set((const void *)k_contract_t<true, true, false>, bt);
+    set((const void *)k_contract_t<true, false, false>, bt);
+    set((const void *)k_contract_t<false, true, false>, bt);
+    set((const void *)k_contract_t<true, true, true>, bt);
+    set((const void *)k_contract_t<true, false, true>, bt);
+    set((const void *)k_contract_t<false, true, true>, bt);
     return e;
 }
 
@@ -461,17 +694,71 @@ unsigned contract_m_blocks(int ncell, int sms) {
     return t < cap ? t : cap;
 }
 
+// the angle kernels [12][na] transposed to [angle][12], zero rows up to a
+// multiple of 32 angles (the TMA-staged contraction)
+void kernel_transposed(const std::vector<double> &K, int na, std::vector<float> &out) {
+    const int pad = (na + kAngChunk - 1) / kAngChunk * kAngChunk;
+    out.assign((size_t)pad * 12, 0.f);
+    for (int a = 0; a < na; ++a)
+        for (int j = 0; j < 12; ++j) out[(size_t)a * 12 + j] = (float)K[(size_t)j * na + a];
+}
+
+// the tensor map of a histogram (or an FP32 distribution) [ncell][na] of
+// 4-byte elements, tiles of 64 cells x 32 angles; false when the rows are not
+// a multiple of 16 bytes (na % 4 != 0), the base is not 16-byte aligned, or
+// the driver's encoder is unavailable
+bool make_bins_tmap(CUtensorMap *map, const void *base, int ncell, int na) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return false;
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    if (na % 4 != 0 || na > (1 << 20) || ncell < 1 || ((uintptr_t)base & 15u)) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)na, (cuuint64_t)ncell};
+    const cuuint64_t strides[1] = {(cuuint64_t)na * 4u};
+    const cuuint32_t box[2] = {(cuuint32_t)kAngChunk, (cuuint32_t)kCTile};
+    const cuuint32_t estr[2] = {1u, 1u};
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void *>(base), dims, strides, box,
+                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+static size_t smem_t(int na_pad) { return 2u * kTmaBytes + (size_t)na_pad * 12 * sizeof(float); }
+bool contract_tma_fits(int na) {
+    const int pad = (na + kAngChunk - 1) / kAngChunk * kAngChunk;
+    return smem_t(pad) <= 64 * 1024;
+}
+
 void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kern,
                        const MixedParams &M, float *fwd, float *table, int tstride, float2 *partials,
-                       unsigned *done, double *sums, int sms, const float *dist, float fscale) {
-    const Staging S = make_staging(M.nang);
-    const size_t sm = smem_f(M.nang);
+                       unsigned *done, double *sums, int sms, const float *dist, float fscale,
+                       const CUtensorMap *tmap, const float *kern_t, unsigned *err) {
     const unsigned b = contract_m_blocks(M.ncell, sms);
     const bool fd = dist != nullptr;
     const uint32_t *src = fd ? reinterpret_cast<const uint32_t *>(dist) : counts;
     // counts: f = count, scaled by measure * V / D; a distribution: f = value, scaled by measure * fscale
     const float scale = fd ? M.measure * fscale : (float)((double)M.measure * (M.volume / M.dist_den));
     const float dscale = fd ? fscale * M.dthph : (float)((M.volume / M.dist_den) * (double)M.dthph);
+    if (tmap && kern_t && err) {
+        const int pad = (M.nang + kAngChunk - 1) / kAngChunk * kAngChunk;
+        const size_t sm = smem_t(pad);
+#define SS_CT(ST, MG, D)                                                                                       \
+    k_contract_t<ST, MG, D><<<b, kCTile, sm, s>>>(*tmap, kern_t, pad, M, scale, dscale, fwd, table, tstride, \
+                                                  partials, done, sums, err)
+        if (stress && mag) { if (fd) SS_CT(true, true, true); else SS_CT(true, true, false); }
+        else if (stress) { if (fd) SS_CT(true, false, true); else SS_CT(true, false, false); }
+        else { if (fd) SS_CT(false, true, true); else SS_CT(false, true, false); }
+#undef SS_CT
+        return;
+    }
+    const Staging S = make_staging(M.nang);
+    const size_t sm = smem_f(M.nang);
 #define SS_CF(ST, MG, D)                                                                                    \
     k_contract_f<ST, MG, D><<<b, kCTile, sm, s>>>(src, kern, M, S, scale, dscale, fwd, table, tstride,   \
                                                   partials, done, sums)

@@ -956,7 +956,6 @@ void transpose(ss_dn *n, const float *src, float *dst, cudaStream_t s) {
 
 // the network on x (histogram layout), output ya in the activation layout
 void enqueue_forward_act(ss_dn *n, const float *x, float *ya, cudaStream_t s) {
-    const unsigned b = (unsigned)((n->nvox + 127) / 128);
     transpose<true>(n, x, n->xa, s);
     const unsigned tiles = (unsigned)(n->d.nx * ((n->d.np + kTileP - 1) / kTileP) * (n->d.ny / kTileY));
     k_dn_in_tiled<<<tiles, 128, 0, s>>>(n->xa, n->P, n->A1, n->d);

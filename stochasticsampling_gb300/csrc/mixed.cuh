@@ -2,6 +2,7 @@
 // timestep (mixed.cu).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <vector>
@@ -44,10 +45,17 @@ void launch_bin_m(cudaStream_t s, bool fixed, unsigned long long n, const MixedP
 // contract_m_blocks(ncell, sms) x 12 float pairs; done: a counter that is 0
 // between launches; sms: multiprocessors of the device.  dist != nullptr: an
 // FP32 distribution times fscale replaces the counts (the denoised histogram).
+// With a tensor map of the source (make_bins_tmap), the transposed angle
+// kernels (kernel_transposed) and an error word, the TMA-staged kernel runs;
+// err gets bit 0x100 when one of its copies timed out.
 unsigned contract_m_blocks(int ncell, int sms);
 void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kern,
                        const MixedParams &M, float *fwd, float *table, int tstride, float2 *partials,
-                       unsigned *done, double *sums, int sms, const float *dist = nullptr, float fscale = 0.f);
+                       unsigned *done, double *sums, int sms, const float *dist = nullptr, float fscale = 0.f,
+                       const CUtensorMap *tmap = nullptr, const float *kern_t = nullptr, unsigned *err = nullptr);
+void kernel_transposed(const std::vector<double> &K, int na, std::vector<float> &out);
+bool make_bins_tmap(CUtensorMap *map, const void *base, int ncell, int na);
+bool contract_tma_fits(int na);
 void launch_counts_to_unit(cudaStream_t s, const uint32_t *counts, long long nbins, float inv_mean, float *x);
 // the FP64 means removed from the real fields fr [comp][cstride], components c0 .. c1
 void launch_center_m(cudaStream_t s, float *fr, int c0, int c1, int ncell, int cstride, const double *sums);

@@ -101,6 +101,12 @@ struct ss_ctx {
     double *sums = nullptr;  // FP64 per-component sums for the mean handling
     float2 *partials = nullptr;  // per-block float-pair component sums of the FP32 contraction (+ its counter)
     unsigned *partials_done = nullptr;
+    // the TMA-staged FP32 contraction: tensor maps of both histograms and of
+    // the denoised distribution, and the angle kernels as [angle][12]
+    CUtensorMap tmap_counts[2];
+    CUtensorMap tmap_dist;
+    bool tma = false, tma_dist = false;
+    float *kern_t = nullptr;
     bool wide_valid = false;  // inv (FP64) holds the widened mixed fields
     std::map<int, cufftHandle> plans_c;  // key: batch * 4 + kind (1 R2C, 2 C2R)
 
@@ -389,10 +395,13 @@ static int enqueue_solve_m(ss_ctx *c, bool flow, bool mag, const uint32_t *count
         launch_counts_to_unit(c->stream, counts, c->P.nbins, c->dn_inv_mean, c->dn_x);
         *nl += 1 + dn_enqueue_forward(c->dn, c->dn_x, c->dn_y, c->stream);
         launch_contract_m(c->stream, flow, mag, counts, c->kern_f, c->M, c->fr_f, c->table_f, ts, c->partials,
-                          c->partials_done, c->sums, c->sms, c->dn_y, c->dn_fscale);
+                          c->partials_done, c->sums, c->sms, c->dn_y, c->dn_fscale,
+                          c->tma_dist ? &c->tmap_dist : nullptr, c->kern_t, c->d_err);
     } else {
+        const CUtensorMap *tm = !c->tma ? nullptr : (counts == c->counts[0] ? &c->tmap_counts[0]
+                                                   : counts == c->counts[1] ? &c->tmap_counts[1] : nullptr);
         launch_contract_m(c->stream, flow, mag, counts, c->kern_f, c->M, c->fr_f, c->table_f, ts, c->partials,
-                          c->partials_done, c->sums, c->sms);
+                          c->partials_done, c->sums, c->sms, nullptr, 0.f, tm, c->kern_t, c->d_err);
     }
     if (flow) launch_center_m(c->stream, c->fr_f, 0, 9, nc, c->P.cstride, c->sums);
     if (mag) launch_center_m(c->stream, c->fr_f, 9, 12, nc, c->P.cstride, c->sums);
@@ -520,6 +529,10 @@ static int read_device_error(ss_ctx *c) {
     uint32_t e = 0;
     CK(cudaMemcpyAsync(&e, c->d_err, sizeof e, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    if (e & 0x100u) {
+        CK(cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream));
+        return fail(c, SS_ERR_CUDA, "a tensor-memory-accelerator copy of the contraction did not complete in time");
+    }
     if (e) {
         return fail(c, SS_ERR_RANGE,
                     "device bounds check fired (flags %u): a particle coordinate was non-finite or outside the "
@@ -565,7 +578,7 @@ static void destroy_impl(ss_ctx *c) {
     for (auto &kv : c->plans_c) cufftDestroy(kv.second);
     for (int b = 0; b < 2; ++b)
         for (int k = 0; k < 2; ++k) cudaFree(c->pa[b][k]);
-    cudaFree(c->fr_f); cudaFree(c->ir_f); cudaFree(c->ii_f); cudaFree(c->fwd_f); cudaFree(c->inv_f); cudaFree(c->table_f); cudaFree(c->kern_f); cudaFree(c->partials);
+    cudaFree(c->fr_f); cudaFree(c->ir_f); cudaFree(c->ii_f); cudaFree(c->fwd_f); cudaFree(c->inv_f); cudaFree(c->table_f); cudaFree(c->kern_f); cudaFree(c->partials); cudaFree(c->kern_t);
     cudaFree(c->kslice); cudaFree(c->kfactor);
     cudaFree(c->dn_x); cudaFree(c->dn_y);
     cudaFree(c->sums);
@@ -804,6 +817,7 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
         if (rc == SS_OK) rc = alloc((void **)&c->kern_f, 12 * nang * sizeof(float));
         if (rc == SS_OK) rc = alloc((void **)&c->sums, 12 * sizeof(double));
         if (rc == SS_OK) rc = alloc((void **)&c->partials, partials_bytes(ncell, c->sms));
+        if (rc == SS_OK) rc = alloc((void **)&c->kern_t, ((nang + 31) / 32 * 32) * 12 * sizeof(float));
     }
     if (rc != SS_OK) {
         std::string m = c->err;
@@ -850,6 +864,12 @@ int ss_create(const ss_grid *grid, const ss_box *box, const ss_params *params, u
         CKC(cudaMemsetAsync(c->partials, 0, partials_bytes(ncell, c->sms), c->stream));
         c->partials_done = reinterpret_cast<unsigned *>(c->partials + 12ull * contract_m_blocks((int)ncell, c->sms));
         CKC(cudaMemcpyAsync(c->kern_f, Kf.data(), Kf.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        std::vector<float> Kt;
+        kernel_transposed(K, (int)nang, Kt);
+        CKC(cudaMemcpyAsync(c->kern_t, Kt.data(), Kt.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        c->tma = contract_tma_fits((int)nang) &&
+                 make_bins_tmap(&c->tmap_counts[0], c->counts[0], (int)ncell, (int)nang) &&
+                 make_bins_tmap(&c->tmap_counts[1], c->counts[1], (int)ncell, (int)nang);
     }
     CKC(contract_prepare());
     launch_half_pi(c->stream, c->d_halfpi);
@@ -1058,6 +1078,7 @@ int ss_set_denoiser(ss_ctx *c, ss_dn *dn) {
         if (!c->dn_x) {
             CK(cudaMalloc((void **)&c->dn_x, (size_t)c->P.nbins * sizeof(float)));
             CK(cudaMalloc((void **)&c->dn_y, (size_t)c->P.nbins * sizeof(float)));
+            c->tma_dist = c->tma && make_bins_tmap(&c->tmap_dist, c->dn_y, c->P.ncell, c->P.nang);
         }
         const double mean = (double)c->P.n / (double)c->P.nbins;  // counts per bin
         c->dn_inv_mean = (float)(1.0 / mean);
