@@ -377,22 +377,26 @@ __global__ void __launch_bounds__(kCTile) k_contract_f(const uint32_t *__restric
 // ---------------------------------------------------------------------------
 // FP32 mixed path, TMA-staged (rows of a multiple of 16 bytes).  The
 // histogram, viewed as a 2-D tensor [ncell][nang] of u32, is copied tile by
-// tile -- 64 cells x 32 angles, 8 KB -- by the tensor memory accelerator
+// tile -- 128 cells x 32 angles, 16 KB -- by the tensor memory accelerator
 // (cp.async.bulk.tensor.2d) into one of two shared-memory buffers, each
 // completing on its own mbarrier, two tiles ahead of the arithmetic: one
 // elected thread issues the copies, no thread spends instructions on
 // addresses, and the copies overlap the FMAs.  Angles past the row end and
 // cells past the grid arrive as zeros (the copy's out-of-bounds fill),
 // against zero-padded angle kernels.  The buffers keep the tensor's dense
-// layout (rows of 32 words); thread t visits its row's angles from
-// a = t mod 32 on, so a warp's 32 reads hit 32 banks, and the angle kernels
-// ([angle][12] floats, staged once per block) are then read 48 bytes apart,
-// which also maps a warp's 16-byte reads to distinct banks.  Every mbarrier
+// layout (rows of 32 words); thread t takes rows t and t + 64 and visits
+// their angles from a = t mod 32 on, so a warp's 32 reads hit 32 banks, and
+// the angle kernels ([angle][12] floats, staged once per block) are then read
+// 48 bytes apart, which also maps a warp's 16-byte reads to distinct banks;
+// each such read serves both of the thread's cells, halving the shared-memory
+// traffic that bounds the kernel.  Every mbarrier
 // wait is bounded: on a timeout the kernel sets bit kErrTmaTimeout of err,
 // waits (bounded) for its own copies and leaves the sums wrong but the
 // launch protocol intact.
 // ---------------------------------------------------------------------------
-constexpr int kTmaBytes = kCTile * kAngChunk * 4;  // one tile: 8 KB
+constexpr int kTmaCells = 2 * kCTile;                // cells per tile: two per thread
+constexpr int kTmaBytes = kTmaCells * kAngChunk * 4;  // one tile: 16 KB
+constexpr int kTmaBlocksPerSM = 4;                    // 2 x 16 KB + the angle kernels per block
 constexpr uint32_t kWaitPolls = 1u << 22;
 constexpr unsigned kErrTmaTimeout = 0x100u;
 
@@ -440,7 +444,7 @@ __global__ void __launch_bounds__(kCTile) k_contract_t(const __grid_constant__ C
     __shared__ bool s_last;
     __shared__ int s_fail;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nc = M.ncell, ntiles = (nc + kCTile - 1) / kCTile, nch = na_pad / kAngChunk;
+    const int nc = M.ncell, ntiles = (nc + kTmaCells - 1) / kTmaCells, nch = na_pad / kAngChunk;
     const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     const int nitems = my_tiles * nch;
     for (int i = tid; i < na_pad * 3; i += kCTile)
@@ -457,7 +461,7 @@ __global__ void __launch_bounds__(kCTile) k_contract_t(const __grid_constant__ C
         const int m = k / nch, c = k - m * nch, t = (int)blockIdx.x + m * (int)gridDim.x;
         const uint32_t b = (uint32_t)(k & 1);
         mbar_expect_tx(mb0 + 8 * b, (uint32_t)kTmaBytes);
-        tma_load_2d(buf0 + b * (uint32_t)kTmaBytes, &tmap, c * kAngChunk, t * kCTile, mb0 + 8 * b);
+        tma_load_2d(buf0 + b * (uint32_t)kTmaBytes, &tmap, c * kAngChunk, t * kTmaCells, mb0 + 8 * b);
     };
     if (tid == 0) {
         if (nitems > 0) issue(0);
@@ -466,56 +470,79 @@ __global__ void __launch_bounds__(kCTile) k_contract_t(const __grid_constant__ C
     FPair tot[12];
 #pragma unroll
     for (int j = 0; j < 12; ++j) tot[j] = FPair{0.f, 0.f};
-    float acc[12];
+    float acc[2][12];
+    float dsum[2];
+    uint32_t csum[2];
 #pragma unroll
-    for (int j = 0; j < 12; ++j) acc[j] = 0.f;
-    float dsum = 0.f;
-    uint32_t csum = 0;
+    for (int h = 0; h < 2; ++h) {
+#pragma unroll
+        for (int j = 0; j < 12; ++j) acc[h][j] = 0.f;
+        dsum[h] = 0.f;
+        csum[h] = 0;
+    }
     int k = 0;
     for (; k < nitems; ++k) {
         const int m = k / nch, c = k - m * nch;
         if (c == 0) {
 #pragma unroll
-            for (int j = 0; j < 12; ++j) acc[j] = 0.f;
-            dsum = 0.f;
-            csum = 0;
+            for (int h = 0; h < 2; ++h) {
+#pragma unroll
+                for (int j = 0; j < 12; ++j) acc[h][j] = 0.f;
+                dsum[h] = 0.f;
+                csum[h] = 0;
+            }
         }
         // every thread observes the copy's completion (which makes its bytes visible to it)
         if (!mbar_wait_bounded(mb0 + 8 * (uint32_t)(k & 1), (uint32_t)((k >> 1) & 1))) s_fail = 1;
         __syncthreads();
         if (s_fail) break;
-        const uint32_t *row = buf + (k & 1) * (kTmaBytes / 4) + tid * kAngChunk;
+        const uint32_t *row0 = buf + (k & 1) * (kTmaBytes / 4) + tid * kAngChunk;
+        const uint32_t *row1 = row0 + kCTile * kAngChunk;
         const float *kc = kf + c * kAngChunk * 12;
-#pragma unroll 4
+#pragma unroll 2
         for (int i = 0; i < kAngChunk; ++i) {
             const int a = (i + tid) & (kAngChunk - 1);
-            const uint32_t w = row[a];
-            float f;
+            const uint32_t w0 = row0[a], w1 = row1[a];
+            float f0, f1;
             if (DIST) {
-                f = __uint_as_float(w);
-                dsum += f;
+                f0 = __uint_as_float(w0);
+                f1 = __uint_as_float(w1);
+                dsum[0] += f0;
+                dsum[1] += f1;
             } else {
-                f = __uint2float_rn(w);
-                csum += w;
+                f0 = __uint2float_rn(w0);
+                f1 = __uint2float_rn(w1);
+                csum[0] += w0;
+                csum[1] += w1;
             }
             const float4 *k4 = reinterpret_cast<const float4 *>(kc + a * 12);
             if (STRESS) {
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {
                     const float4 kv = k4[q];
-                    acc[4 * q + 0] = fmaf(kv.x, f, acc[4 * q + 0]);
-                    acc[4 * q + 1] = fmaf(kv.y, f, acc[4 * q + 1]);
-                    acc[4 * q + 2] = fmaf(kv.z, f, acc[4 * q + 2]);
-                    acc[4 * q + 3] = fmaf(kv.w, f, acc[4 * q + 3]);
+                    acc[0][4 * q + 0] = fmaf(kv.x, f0, acc[0][4 * q + 0]);
+                    acc[0][4 * q + 1] = fmaf(kv.y, f0, acc[0][4 * q + 1]);
+                    acc[0][4 * q + 2] = fmaf(kv.z, f0, acc[0][4 * q + 2]);
+                    acc[0][4 * q + 3] = fmaf(kv.w, f0, acc[0][4 * q + 3]);
+                    acc[1][4 * q + 0] = fmaf(kv.x, f1, acc[1][4 * q + 0]);
+                    acc[1][4 * q + 1] = fmaf(kv.y, f1, acc[1][4 * q + 1]);
+                    acc[1][4 * q + 2] = fmaf(kv.z, f1, acc[1][4 * q + 2]);
+                    acc[1][4 * q + 3] = fmaf(kv.w, f1, acc[1][4 * q + 3]);
                 }
             }
             if (STRESS || MAG) {
                 const float4 kv = k4[2];
-                if (STRESS) acc[8] = fmaf(kv.x, f, acc[8]);
+                if (STRESS) {
+                    acc[0][8] = fmaf(kv.x, f0, acc[0][8]);
+                    acc[1][8] = fmaf(kv.x, f1, acc[1][8]);
+                }
                 if (MAG) {
-                    acc[9] = fmaf(kv.y, f, acc[9]);
-                    acc[10] = fmaf(kv.z, f, acc[10]);
-                    acc[11] = fmaf(kv.w, f, acc[11]);
+                    acc[0][9] = fmaf(kv.y, f0, acc[0][9]);
+                    acc[0][10] = fmaf(kv.z, f0, acc[0][10]);
+                    acc[0][11] = fmaf(kv.w, f0, acc[0][11]);
+                    acc[1][9] = fmaf(kv.y, f1, acc[1][9]);
+                    acc[1][10] = fmaf(kv.z, f1, acc[1][10]);
+                    acc[1][11] = fmaf(kv.w, f1, acc[1][11]);
                 }
             }
         }
@@ -525,24 +552,27 @@ __global__ void __launch_bounds__(kCTile) k_contract_t(const __grid_constant__ C
             issue(k + 2);
         }
         if (c == nch - 1) {
-            const int cell = ((int)blockIdx.x + m * (int)gridDim.x) * kCTile + tid;
-            if (cell < nc) {
-                float out[12];
 #pragma unroll
-                for (int j = 0; j < 12; ++j) out[j] = acc[j] * scale;
-                if (STRESS) {
+            for (int h = 0; h < 2; ++h) {
+                const int cell = ((int)blockIdx.x + m * (int)gridDim.x) * kTmaCells + h * kCTile + tid;
+                if (cell < nc) {
+                    float out[12];
 #pragma unroll
-                    for (int j = 0; j < 9; ++j) fwd[(long long)j * M.cstride + cell] = out[j];
+                    for (int j = 0; j < 12; ++j) out[j] = acc[h][j] * scale;
+                    if (STRESS) {
+#pragma unroll
+                        for (int j = 0; j < 9; ++j) fwd[(long long)j * M.cstride + cell] = out[j];
+                    }
+                    if (MAG) {
+#pragma unroll
+                        for (int j = 9; j < 12; ++j) fwd[(long long)j * M.cstride + cell] = out[j];
+                    }
+#pragma unroll
+                    for (int j = 0; j < 12; ++j)
+                        if ((j < 9 && STRESS) || (j >= 9 && MAG)) tot[j] = pair_add(tot[j], FPair{out[j], 0.f});
+                    const float dens = DIST ? dsum[h] * dscale : (float)csum[h] * dscale;
+                    table[(long long)cell * tstride + T_DIFF] = sqrtf(M.two_dt * (M.Dt + M.volex * dens));
                 }
-                if (MAG) {
-#pragma unroll
-                    for (int j = 9; j < 12; ++j) fwd[(long long)j * M.cstride + cell] = out[j];
-                }
-#pragma unroll
-                for (int j = 0; j < 12; ++j)
-                    if ((j < 9 && STRESS) || (j >= 9 && MAG)) tot[j] = pair_add(tot[j], FPair{out[j], 0.f});
-                const float dens = DIST ? dsum * dscale : (float)csum * dscale;
-                table[(long long)cell * tstride + T_DIFF] = sqrtf(M.two_dt * (M.Dt + M.volex * dens));
             }
         }
     }
@@ -661,7 +691,7 @@ cudaError_t contract_prepare() {
     set((const void *)k_contract_f<true, true, true>, bf);
     set((const void *)k_contract_f<true, false, true>, bf);
     set((const void *)k_contract_f<false, true, true>, bf);
-    const int bt = 64 * 1024;
+    const int bt = 80 * 1024;
     set((const void *)k_contract_t<true, true, false>, bt);
     set((const void *)k_contract_t<true, false, false>, bt);
     set((const void *)k_contract_t<false, true, false>, bt);
@@ -708,6 +738,7 @@ void kernel_transposed(const std::vector<double> &K, int na, std::vector<float> 
 // a multiple of 16 bytes (na % 4 != 0), the base is not 16-byte aligned, or
 // the driver's encoder is unavailable
 bool make_bins_tmap(CUtensorMap *map, const void *base, int ncell, int na) {
+    // tiles of kTmaCells cells x kAngChunk angles
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
         void *fn = nullptr;
@@ -721,7 +752,7 @@ bool make_bins_tmap(CUtensorMap *map, const void *base, int ncell, int na) {
     if (na % 4 != 0 || na > (1 << 20) || ncell < 1 || ((uintptr_t)base & 15u)) return false;
     const cuuint64_t dims[2] = {(cuuint64_t)na, (cuuint64_t)ncell};
     const cuuint64_t strides[1] = {(cuuint64_t)na * 4u};
-    const cuuint32_t box[2] = {(cuuint32_t)kAngChunk, (cuuint32_t)kCTile};
+    const cuuint32_t box[2] = {(cuuint32_t)kAngChunk, (cuuint32_t)kTmaCells};
     const cuuint32_t estr[2] = {1u, 1u};
     const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void *>(base), dims, strides, box,
                               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -732,7 +763,7 @@ bool make_bins_tmap(CUtensorMap *map, const void *base, int ncell, int na) {
 static size_t smem_t(int na_pad) { return 2u * kTmaBytes + (size_t)na_pad * 12 * sizeof(float); }
 bool contract_tma_fits(int na) {
     const int pad = (na + kAngChunk - 1) / kAngChunk * kAngChunk;
-    return smem_t(pad) <= 64 * 1024;
+    return smem_t(pad) <= 80 * 1024;
 }
 
 void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *counts, const float *kern,
@@ -748,6 +779,9 @@ void launch_contract_m(cudaStream_t s, bool stress, bool mag, const uint32_t *co
     if (tmap && kern_t && err) {
         const int pad = (M.nang + kAngChunk - 1) / kAngChunk * kAngChunk;
         const size_t sm = smem_t(pad);
+        const unsigned tt = (unsigned)((M.ncell + kTmaCells - 1) / kTmaCells);
+        const unsigned cap = (unsigned)(kTmaBlocksPerSM * (sms > 0 ? sms : 1));
+        const unsigned b = tt < cap ? tt : cap;  // every block resident: tiles are split evenly
 #define SS_CT(ST, MG, D)                                                                                       \
     k_contract_t<ST, MG, D><<<b, kCTile, sm, s>>>(*tmap, kern_t, pad, M, scale, dscale, fwd, table, tstride, \
                                                   partials, done, sums, err)

@@ -209,14 +209,20 @@ __device__ __forceinline__ void langevin_mixed(float &phi, float &theta, float s
         phi = nphi < 0.0f ? nphi + 6.28318530717958647692f : nphi;
         theta = 1.57079632679489661923f;
     } else {
-        float nth = 1.57079632679489661923f - atan2f(v2, sqrtf(v0 * v0 + v1 * v1));
-        float t = modulo_f(nth, 6.28318530717958647692f);
-        if (t > 3.14159265358979323846f) {
-            phi = modulo_f(nphi + 3.14159265358979323846f, 6.28318530717958647692f);
-            theta = 6.28318530717958647692f - t;
+        // ang_pbc (src/particle.rs:37-44) of (nphi, nth): atan2f gives
+        // nphi in [-pi, pi] and nth = pi/2 - atan2f(v2, |v_xy| >= 0) in
+        // [0, pi], so modulo 2 pi is nphi + 2 pi for a negative nphi and the
+        // identity otherwise, and the fold above pi cannot occur (fmodf, which
+        // the general form would call, is far costlier on GB300).  A
+        // non-finite angle stays non-finite, as through fmodf.
+        const float nth = 1.57079632679489661923f - atan2f(v2, sqrtf(v0 * v0 + v1 * v1));
+        if (nth > 3.14159265358979323846f) {
+            float p = nphi + 3.14159265358979323846f;
+            phi = p < 0.0f ? p + 6.28318530717958647692f : (p >= 6.28318530717958647692f ? p - 6.28318530717958647692f : p);
+            theta = 6.28318530717958647692f - nth;
         } else {
-            phi = modulo_f(nphi, 6.28318530717958647692f);
-            theta = t;
+            phi = nphi < 0.0f ? nphi + 6.28318530717958647692f : nphi;
+            theta = nth;
         }
     }
 }
