@@ -521,8 +521,8 @@ __device__ __forceinline__ void langevin_canon_f2(const DevParams &P, double &px
         xf::canon_increments(pph, ct, xf::split(r[0]), xf::split(r[1]), xf::split(sa), xf::split(r[4]), T, dt2,
                              re2, dx, dy, dph);
     }
-    px = ref_modulo((px + xf::to_double(dx.h)) + xf::to_double(dx.l), P.bx);
-    py = ref_modulo((py + xf::to_double(dy.h)) + xf::to_double(dy.l), P.by);
+    px = modulo_rare((px + xf::to_double(dx.h)) + xf::to_double(dx.l), P.bx);
+    py = modulo_rare((py + xf::to_double(dy.h)) + xf::to_double(dy.l), P.by);
     pph = ref_modulo((pph + xf::to_double(dph.h)) + xf::to_double(dph.l), kTwoPi);
 }
 

@@ -231,16 +231,8 @@ __device__ __forceinline__ void langevin_mixed(float &phi, float &theta, float s
 // src/particle.rs:26-35), with ref_modulo's range tests on the integer pipe:
 // an FP64 compare would occupy GB300's FP64 pipe for a whole warp whenever
 // one of its particles sits in an edge cell.
-// x + dx in FP64, then modulo (src/particle.rs:26-35).  On GB300 a warp-wide
-// FP64 instruction occupies a sub-partition's FP64 unit for 64 cycles, so
-// the wrap (rare: a particle leaving the box) is skipped for the whole warp
-// when no active lane needs it: one FP64 addition per coordinate.
-__device__ __forceinline__ double advance64(double x, float dx, double L) {
-    const double p = x + f2d(dx);
-    const long long kp = dkey(p);
-    const bool inside = kp >= 0 && kp < dkey(L);  // [+-0, L): modulo returns p itself
-    if (__all_sync(__activemask(), inside)) return p;
-    return inside ? p : ref_modulo(p, L);
-}
+// x + dx in FP64, then modulo (src/particle.rs:26-35): one FP64 addition per
+// coordinate, the wrap out of line (modulo_rare).
+__device__ __forceinline__ double advance64(double x, float dx, double L) { return modulo_rare(x + f2d(dx), L); }
 
 }  // namespace ss
