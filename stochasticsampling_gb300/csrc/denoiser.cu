@@ -59,10 +59,7 @@ constexpr int kLineBytes = 4 * kChunkBytes;  // 8320 B
 constexpr int kRing = 6;                     // positions along phi per x-plane: 3 in use, 1 freeing, 2 landing
 constexpr int kSlots = 3 * kRing;            // line buffers
 constexpr int kPChunk = 4;                   // tiles along phi per work item
-constexpr int kBGroup = 3 * kBTap;           // 6 KB: the three dy taps of one (dx, dphi) as one N = 96 operand
-constexpr int kXchBytes = 2 * 4 * kC * 4;    // the wide epilogue's row exchange across warps (1 KB)
-constexpr int kSmemConv = kBAll + kSlots * kLineBytes + 128 + kXchBytes;  // + the mbarriers, tensor-memory slot,
-                                                                          // failure flag, row exchange
+constexpr int kSmemConv = kBAll + kSlots * kLineBytes + 128;  // + the mbarrier, tensor-memory slot, failure flag
 static_assert(kSmemConv <= 227 * 1024, "the convolution's shared memory exceeds a CTA's limit");
 constexpr uint32_t kWaitLimit = 1u << 22;    // mbarrier polls before giving up
 constexpr unsigned kErrTimeout = 1u;
@@ -169,9 +166,6 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
 // instruction descriptor: D FP32, A and B BF16, both K-major, N = 32, M = 128
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kC >> 3) << 17) |
                             ((uint32_t)(kTileM >> 4) << 24);
-// the same with N = 96 (the wide form: three dy taps side by side)
-constexpr uint32_t kIdescWide = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)((3 * kC) >> 3) << 17) |
-                                ((uint32_t)(kTileM >> 4) << 24);
 
 // byte offset of element (row, k) of a K-major operand block in the core-matrix layout
 __host__ __device__ __forceinline__ int core_offset(int row, int k) {
@@ -185,18 +179,7 @@ __host__ __device__ __forceinline__ int core_offset(int row, int k) {
 // tile k - 1's accumulator out (epilogue) and start the copies of the line
 // tile k + 2 adds, two tiles ahead, into the ring slot of a line whose last
 // MMAs completed before.
-//
-// WIDE (ny = 128: one segment holds the whole periodic y range): for every
-// (dx, dphi) one MMA of N = 96 multiplies the unshifted line (rows y = 0..127)
-// by the weights of its three dy taps side by side, giving
-// P_dy[r] = sum_(dx, dphi) line(y = r) W(dx, dy, dphi) in columns 32 (dy + 1)
-// of the accumulator (two accumulators at columns 0 and 128); the epilogue
-// forms out[t] = P_-1[t - 1] + P_0[t] + P_+1[t + 1], indices mod 128, from
-// the neighbouring tensor-memory lanes: warp shuffles within a warp, a
-// shared-memory exchange of one row across the warp boundaries.  18 MMAs
-// per tile instead of 54, and every line is read by the tensor core once
-// per (dx, dphi) instead of three times.
-template <int MODE, bool WIDE>
+template <int MODE>
 __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__restrict__ X,
                                                       const uint8_t *__restrict__ Wpacked,
                                                       const float *__restrict__ bias,
@@ -208,10 +191,7 @@ __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__res
     uint64_t *mbar = reinterpret_cast<uint64_t *>(sL + kSlots * kLineBytes);  // one per accumulator
     uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
     volatile int *sfail = reinterpret_cast<volatile int *>(tslot + 1);
-    float *xch = reinterpret_cast<float *>(smem + kBAll + kSlots * kLineBytes + 128);  // [2][4 warps][32]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    constexpr uint32_t kTmemCols = WIDE ? 256u : 64u;
-    constexpr uint32_t kAccCols = WIDE ? 128u : 32u;  // column offset of the second accumulator
 
     for (int i = tid; i < kBAll / 16; i += kTileM)
         reinterpret_cast<uint4 *>(sB)[i] = reinterpret_cast<const uint4 *>(Wpacked)[i];
@@ -221,7 +201,7 @@ __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__res
         *sfail = 0;
         fence_mbar_init();
     }
-    if (warp == 0) tmem_alloc(smem_u32(tslot), kTmemCols);
+    if (warp == 0) tmem_alloc(smem_u32(tslot), 64);
     fence_proxy_async();
     tc_before_sync();
     __syncthreads();
@@ -248,52 +228,15 @@ __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__res
                 cp_async16(dst0 + j * kChunkBytes + r * 16, line + (size_t)yl * kC + j * 8);
             }
         };
-        // accumulator of tile kt -> bias / ReLU -> Y (every thread one row).
-        // Every thread reaches the wide form's barrier, also after a failed wait.
+        // accumulator of tile kt -> bias / ReLU -> Y (every thread one row)
         auto epilogue = [&](int kt) -> bool {
             const int a = kt & 1;
-            const bool ok = mbar_wait(smem_u32(mbar + a), a ? phase1 : phase0);
-            if (ok) {
-                if (a) phase1 ^= 1u;
-                else phase0 ^= 1u;
-            }
+            if (!mbar_wait(smem_u32(mbar + a), a ? phase1 : phase0)) return false;
+            if (a) phase1 ^= 1u;
+            else phase0 ^= 1u;
             tc_after_sync();
             uint32_t r[32];
-            if (WIDE) {
-                uint32_t rm[32], rp[32];
-                const uint32_t base = tmem + ((uint32_t)(warp * 32) << 16) + kAccCols * (uint32_t)a;
-                if (ok) {
-                    tmem_ld32(base, rm);
-                    tmem_ld32(base + 32u, r);
-                    tmem_ld32(base + 64u, rp);
-                } else {
-#pragma unroll
-                    for (int q = 0; q < 32; ++q) rm[q] = r[q] = rp[q] = 0u;
-                }
-                // rows across the warp boundaries: P_-1 of each warp's last row, P_+1 of its first
-                if (lane == 31) {
-#pragma unroll
-                    for (int q = 0; q < 32; ++q) xch[warp * 32 + q] = __uint_as_float(rm[q]);
-                }
-                if (lane == 0) {
-#pragma unroll
-                    for (int q = 0; q < 32; ++q) xch[128 + warp * 32 + q] = __uint_as_float(rp[q]);
-                }
-                __syncthreads();
-                const int wprev = (warp + 3) & 3, wnext = (warp + 1) & 3;
-#pragma unroll
-                for (int q = 0; q < 32; ++q) {
-                    float lo = __shfl_up_sync(0xffffffffu, __uint_as_float(rm[q]), 1);
-                    float hi = __shfl_down_sync(0xffffffffu, __uint_as_float(rp[q]), 1);
-                    if (lane == 0) lo = xch[wprev * 32 + q];
-                    if (lane == 31) hi = xch[128 + wnext * 32 + q];
-                    r[q] = __float_as_uint((lo + __uint_as_float(r[q])) + hi);
-                }
-            } else {
-                if (!ok) return false;
-                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(32 * a), r);
-            }
-            if (!ok) return false;
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(32 * a), r);
             const size_t vo = (size_t)((x * d.np + p0 + kt) * d.ny + y0 + warp * 32 + lane);  // this thread's row
             if (MODE == 1) {
                 float4 *out = reinterpret_cast<float4 *>(reinterpret_cast<float *>(Y) + vo * kC);
@@ -345,33 +288,20 @@ __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__res
             if (*sfail) break;
             if (tid == 0) {
                 tc_after_sync();
-                const uint32_t dacc = tmem + kAccCols * (uint32_t)(k & 1);
+                const uint32_t dacc = tmem + (uint32_t)(32 * (k & 1));
                 uint32_t acc = 0;
                 for (int dx = -1; dx <= 1; ++dx)
                     for (int dp = -1; dp <= 1; ++dp) {
                         const uint32_t line = sL0 + (uint32_t)(((dx + 1) * kRing + (k + 1 + dp) % kRing) * kLineBytes);
-                        if (WIDE) {
-                            const int g = (dx + 1) * 3 + (dp + 1);
+#pragma unroll
+                        for (int dy = -1; dy <= 1; ++dy) {
+                            const int tap = (dx + 1) * 9 + (dy + 1) * 3 + (dp + 1);
 #pragma unroll
                             for (int kk = 0; kk < 2; ++kk) {
-                                // rows 1 .. 128 of the line: y = 0 .. 127
-                                const uint64_t ad = smem_desc(line + kk * 2 * kChunkBytes + 16, kChunkBytes, 128);
-                                const uint64_t bd = smem_desc(sB0 + g * kBGroup + kk * 256, 128, 512);
-                                mma_bf16(dacc, ad, bd, kIdescWide, acc);
+                                const uint64_t ad = smem_desc(line + kk * 2 * kChunkBytes + (1 + dy) * 16, kChunkBytes, 128);
+                                const uint64_t bd = smem_desc(sB0 + tap * kBTap + kk * 256, 128, 512);
+                                mma_bf16(dacc, ad, bd, kIdesc, acc);
                                 acc = 1;
-                            }
-                        } else {
-#pragma unroll
-                            for (int dy = -1; dy <= 1; ++dy) {
-                                const int tap = (dx + 1) * 9 + (dy + 1) * 3 + (dp + 1);
-#pragma unroll
-                                for (int kk = 0; kk < 2; ++kk) {
-                                    const uint64_t ad =
-                                        smem_desc(line + kk * 2 * kChunkBytes + (1 + dy) * 16, kChunkBytes, 128);
-                                    const uint64_t bd = smem_desc(sB0 + tap * kBTap + kk * 256, 128, 512);
-                                    mma_bf16(dacc, ad, bd, kIdesc, acc);
-                                    acc = 1;
-                                }
                             }
                         }
                     }
@@ -396,35 +326,22 @@ __global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__res
     tc_before_sync();
     __syncthreads();
     tc_after_sync();
-    if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+    if (warp == 0) tmem_dealloc(tmem, 64);
 }
 
 // FP32 weights W[tap][n][k] -> BF16 in the K-major core-matrix layout of the
 // B operand, one 2 KB block per tap.  MIRROR: block t holds W[26 - t][k][n]
 // (the weights of the backward-data convolution).
-// WIDE: the taps grouped by (dx, dphi), the three dy taps of a group as rows
-// 32 (dy + 1) .. 32 (dy + 1) + 31 of one N = 96 operand (6 KB per group).
-template <bool MIRROR, bool WIDE>
+template <bool MIRROR>
 __global__ void k_pack_weights(const float *__restrict__ W, uint8_t *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kTaps * kC * kC) return;
     const int t = i / (kC * kC), n = (i / kC) % kC, k = i % kC;
     const float w = MIRROR ? W[((kTaps - 1 - t) * kC + k) * kC + n] : W[(t * kC + n) * kC + k];
-    const int g = (t / 9) * 3 + t % 3, dyi = (t / 3) % 3;  // tap t = 9 (dx + 1) + 3 (dy + 1) + (dphi + 1)
-    const int off = WIDE ? g * kBGroup + core_offset(dyi * kC + n, k) : t * kBTap + core_offset(n, k);
-    *reinterpret_cast<__nv_bfloat16 *>(out + off) = __float2bfloat16_rn(w);
+    *reinterpret_cast<__nv_bfloat16 *>(out + t * kBTap + core_offset(n, k)) = __float2bfloat16_rn(w);
 }
 
 int g_sms = 0;
-
-void set_conv_attrs() {
-    cudaFuncSetAttribute(k_conv32<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
-    cudaFuncSetAttribute(k_conv32<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
-    cudaFuncSetAttribute(k_conv32<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
-    cudaFuncSetAttribute(k_conv32<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
-    cudaFuncSetAttribute(k_conv32<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
-    cudaFuncSetAttribute(k_conv32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
-}
 
 // work items of the convolution: (x, y segment of 128, kPChunk positions along phi)
 int conv_items(Dims d) { return d.nx * (d.ny / kTileM) * ((d.np + kPChunk - 1) / kPChunk); }
@@ -893,7 +810,9 @@ extern "C" int ss_dn_conv32(const void *x, const float *w, const float *bias, co
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
         if (g_sms <= 0) g_sms = 1;
-        set_conv_attrs();
+        cudaFuncSetAttribute(k_conv32<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
+        cudaFuncSetAttribute(k_conv32<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
+        cudaFuncSetAttribute(k_conv32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
     }
     uint8_t *packed = nullptr;
     unsigned *derr = nullptr;
@@ -902,23 +821,15 @@ extern "C" int ss_dn_conv32(const void *x, const float *w, const float *bias, co
     if (e == cudaSuccess) e = cudaMemsetAsync(derr, 0, sizeof(unsigned), s);
     if (e == cudaSuccess) {
         const int nw = kTaps * kC * kC;
-        const bool wide = ny == (uint32_t)kTileM;
-        if (mode == 2) {
-            if (wide) k_pack_weights<true, true><<<(nw + 255) / 256, 256, 0, s>>>(w, packed);
-            else k_pack_weights<true, false><<<(nw + 255) / 256, 256, 0, s>>>(w, packed);
-        } else {
-            if (wide) k_pack_weights<false, true><<<(nw + 255) / 256, 256, 0, s>>>(w, packed);
-            else k_pack_weights<false, false><<<(nw + 255) / 256, 256, 0, s>>>(w, packed);
-        }
+        if (mode == 2) k_pack_weights<true><<<(nw + 255) / 256, 256, 0, s>>>(w, packed);
+        else k_pack_weights<false><<<(nw + 255) / 256, 256, 0, s>>>(w, packed);
         Dims d{(int)nx, (int)ny, (int)np};
         const int items = conv_items(d), grid = items < g_sms ? items : g_sms;
         const __nv_bfloat16 *X = reinterpret_cast<const __nv_bfloat16 *>(x);
         const __nv_bfloat16 *R = reinterpret_cast<const __nv_bfloat16 *>(ref);
-#define SS_CONV(M, W) k_conv32<M, W><<<grid, kTileM, kSmemConv, s>>>(X, packed, bias, R, y, d, items, derr)
-        if (mode == 0) { if (wide) SS_CONV(0, true); else SS_CONV(0, false); }
-        else if (mode == 1) { if (wide) SS_CONV(1, true); else SS_CONV(1, false); }
-        else { if (wide) SS_CONV(2, true); else SS_CONV(2, false); }
-#undef SS_CONV
+        if (mode == 0) k_conv32<0><<<grid, kTileM, kSmemConv, s>>>(X, packed, bias, R, y, d, items, derr);
+        else if (mode == 1) k_conv32<1><<<grid, kTileM, kSmemConv, s>>>(X, packed, bias, R, y, d, items, derr);
+        else k_conv32<2><<<grid, kTileM, kSmemConv, s>>>(X, packed, bias, R, y, d, items, derr);
         e = cudaGetLastError();
     }
     unsigned herr = 0;
@@ -1013,34 +924,27 @@ int dnfail(int code, const char *fmt, ...) {
 void conv_attrs() {
     static bool done = false;
     if (done) return;
-    set_conv_attrs();
+    cudaFuncSetAttribute(k_conv32<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
+    cudaFuncSetAttribute(k_conv32<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
+    cudaFuncSetAttribute(k_conv32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
     cudaFuncSetAttribute(k_dn_out_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          kOutSmem + (kTaps * kC + 4) * (int)sizeof(float));
     done = true;
 }
 
-// the wide form (N = 96 MMAs) serves grids whose y extent is one tile
 template <int MODE>
 void launch_conv(ss_dn *n, const __nv_bfloat16 *X, const uint8_t *W, const float *bias, const __nv_bfloat16 *ref,
                  void *Y, cudaStream_t s) {
     const int items = conv_items(n->d), grid = items < n->sms ? items : n->sms;
-    if (n->d.ny == kTileM) k_conv32<MODE, true><<<grid, kTileM, kSmemConv, s>>>(X, W, bias, ref, Y, n->d, items, n->err);
-    else k_conv32<MODE, false><<<grid, kTileM, kSmemConv, s>>>(X, W, bias, ref, Y, n->d, items, n->err);
+    k_conv32<MODE><<<grid, kTileM, kSmemConv, s>>>(X, W, bias, ref, Y, n->d, items, n->err);
 }
 
 void pack_all(ss_dn *n, cudaStream_t s) {
     const int nw = kTaps * kC * kC, b = (nw + 255) / 256;
-    if (n->d.ny == kTileM) {
-        k_pack_weights<false, true><<<b, 256, 0, s>>>(n->P + kOffW2, n->Wp2);
-        k_pack_weights<false, true><<<b, 256, 0, s>>>(n->P + kOffW3, n->Wp3);
-        k_pack_weights<true, true><<<b, 256, 0, s>>>(n->P + kOffW2, n->Wm2);
-        k_pack_weights<true, true><<<b, 256, 0, s>>>(n->P + kOffW3, n->Wm3);
-    } else {
-        k_pack_weights<false, false><<<b, 256, 0, s>>>(n->P + kOffW2, n->Wp2);
-        k_pack_weights<false, false><<<b, 256, 0, s>>>(n->P + kOffW3, n->Wp3);
-        k_pack_weights<true, false><<<b, 256, 0, s>>>(n->P + kOffW2, n->Wm2);
-        k_pack_weights<true, false><<<b, 256, 0, s>>>(n->P + kOffW3, n->Wm3);
-    }
+    k_pack_weights<false><<<b, 256, 0, s>>>(n->P + kOffW2, n->Wp2);
+    k_pack_weights<false><<<b, 256, 0, s>>>(n->P + kOffW3, n->Wp3);
+    k_pack_weights<true><<<b, 256, 0, s>>>(n->P + kOffW2, n->Wm2);
+    k_pack_weights<true><<<b, 256, 0, s>>>(n->P + kOffW3, n->Wm3);
     n->launches += 4;
 }
 
