@@ -303,13 +303,16 @@ int ss_ensemble_info(ss_ens *ens, uint64_t *particles, uint32_t *groups, uint64_
 /* ---- learned histogram denoiser ------------------------------------------
  * One 3x3x3 periodic convolution of 32 -> 32 channels on the tensor cores
  * (tcgen05, BF16 operands, FP32 accumulation): the building block of the
- * denoiser, exposed for tests.  x: DEVICE bf16 [nx][np][ny][32] (the
- * activation layout: channels last, y fastest); w: DEVICE float [27][32
+ * denoiser, exposed for tests.  x: DEVICE bf16 in the activation layout
+ * [nx][np][4][ny][8] (channel c of voxel (x, y, p) in chunk c / 8, lane
+ * c % 8: each line's 128-row segment of one 8-channel chunk is one
+ * contiguous 2 KB block), 16-byte aligned; w: DEVICE float [27][32
  * out][32 in], tap = 9 (dx+1) + 3 (dy+1) + (dp+1) (the torch conv3d weight
  * [out][in][dx+1][dy+1][dp+1] reordered);
  * bias: DEVICE float[32].  mode 0: y = bf16 ReLU(conv(x) + bias); mode 1:
  * y = float conv(x) + bias; mode 2: y = bf16 conv^T(x) * (ref > 0), the
- * backward-data step through a ReLU (ref: DEVICE bf16, bias unused).
+ * backward-data step through a ReLU (ref: DEVICE bf16, bias unused); y and
+ * ref in the same layout as x (float for mode 1), 16-byte aligned.
  * ny must be a positive multiple of 128.  Returns after completion. */
 int ss_dn_conv32(const void *x, const float *w, const float *bias, const void *ref, void *y, uint32_t nx,
                  uint32_t ny, uint32_t np, uint32_t mode, void *stream);

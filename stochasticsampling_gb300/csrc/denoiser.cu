@@ -3,31 +3,33 @@
 // low-particle-count histogram on the (x, y, phi) grid to an estimate of the
 // high-count distribution before the stress / Stokes solve.
 //
-// Activations are BF16, channels last, in the layout [x][phi][y][32], so
-// that a line along y (the 128 voxels of one tile) is contiguous.  The
+// Activations are BF16 in the layout [x][phi][4 chunks][y][8 channels]:
+// along a line (x, phi) each 8-channel chunk is a contiguous plane of ny
+// rows of 16 B, so the 128 voxels of one tile are four 2 KB blocks.  The
 // 32 -> 32 convolutions are implicit GEMMs on the 5th-generation tensor
 // cores: per tile (x, phi, 128 consecutive y), D[128 x 32] = sum over the 27
 // taps of A_tap[128 x 32] W_tap[32 x 32]^T, BF16 operands in shared memory,
-// FP32 accumulator in tensor memory, one elected thread issuing tcgen05.mma
-// (M = 128, N = 32, K = 16).  A CTA walks along phi: it keeps the lines
-// (x + dx, phi + dphi) of the current tile in a ring of 12 line buffers (3
-// x-planes x 4 positions along phi), each line with one halo row at either
-// end (130 rows), and loads only the 3 lines the next tile adds; the 27 taps
-// are descriptor offsets into those lines (the y shift is a 16-byte row
-// offset), so every activation row is read from global memory about 3 times
-// instead of 27.  Lines are copied with cp.async; a tile's 54 MMAs are issued
-// back to back and committed to an mbarrier.  The epilogue reads the
-// accumulator with tcgen05.ld (one voxel's 32 channels per thread), adds the
-// bias and applies ReLU (or the ReLU derivative of a reference tensor, for
-// the backward pass).
+// FP32 accumulator in tensor memory, one elected thread issuing tcgen05.mma.
+// A CTA walks along phi through its runs of tiles and loads each input line
+// (x + dx, phi) once per run (with one halo row at either end, periodic in
+// y) into a ring of 18 line buffers; the 27 taps are descriptor offsets into
+// those lines (the y shift is a 16-byte row offset).  The 3 lines of one
+// input position feed the output tiles phi - 1, phi and phi + 1, so each
+// (dx, dy, K half) is one MMA of M = 128, N = 96 (K = 16) with the three
+// dphi taps' weights stacked along N.  The kernel is warp-specialised: one
+// thread streams the lines with bulk copies, one thread issues the MMAs into
+// a ring of 8 accumulators in tensor memory, and four warps drain finished
+// accumulators with tcgen05.ld (one voxel's 32 channels per thread), add the
+// bias and apply ReLU (or the ReLU derivative of a reference tensor, for the
+// backward pass) while the next positions' MMAs run.
 //
 // Shared-memory operand layouts (K-major, no swizzle).  A line: for each of
-// its 4 K chunks (8 channels, 16 bytes) the 130 rows at a 16-byte stride, so
-// row groups are 128 B apart (stride offset) and K chunks 2080 B (leading
+// its 4 K chunks (8 channels, 16 bytes) the rows at a 16-byte stride, so row
+// groups are 128 B apart (stride offset) and K chunks 2176 B (leading
 // offset).  Weights: per tap 32 rows x 4 chunks in 8 x 16 B core matrices,
 // leading offset 128 B, stride offset 512 B.  Every wait is bounded: on a
-// timeout the kernel records an error, waits for its own copies, frees its
-// tensor memory and returns.
+// timeout the kernel records an error, waits for its own copies and MMAs,
+// frees its tensor memory and returns.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -53,14 +55,24 @@ constexpr int kTaps = 27;                    // 3 x 3 x 3
 constexpr int kTileM = 128;                  // voxels per tile (MMA M): one line segment along y
 constexpr int kBTap = kC * kC * 2;           // 2 KB of weights per tap
 constexpr int kBAll = kTaps * kBTap;         // 54 KB
-constexpr int kLineRows = kTileM + 2;        // y = -1 .. 128 of a segment
-constexpr int kChunkBytes = kLineRows * 16;  // one 16-byte K chunk of every row of a line
-constexpr int kLineBytes = 4 * kChunkBytes;  // 8320 B
-constexpr int kRing = 6;                     // positions along phi per x-plane: 3 in use, 1 freeing, 2 landing
-constexpr int kSlots = 3 * kRing;            // line buffers
-constexpr int kPChunk = 4;                   // tiles along phi per work item
-constexpr int kSmemConv = kBAll + kSlots * kLineBytes + 128;  // + the mbarrier, tensor-memory slot, failure flag
+// A line buffer: 4 K chunks (8 channels, 16 B per row) of 136 rows each.
+// Rows 8 .. 135 of a chunk hold y0 .. y0 + 127 (one 2 KB bulk copy), row 7
+// the halo y0 - 1; the halo y0 + 128 sits in row 136, which is row 0 of the
+// next chunk (rows 0 .. 6 of a chunk are never read), and for the last
+// chunk in the 128 bytes past it.
+constexpr int kChunkRows = 136;
+constexpr int kChunkBytes = kChunkRows * 16;       // 2176 B: the A operand's leading offset
+constexpr int kBodyOff = 8 * 16;                   // byte offset of row y0 in a chunk
+constexpr int kLineBytes = 4 * kChunkBytes + 128;  // 8832 B
+constexpr int kBodyBytes = kTileM * 16;            // one chunk of 128 rows
+constexpr int kSlots = 18;                         // line buffers (a ring)
+constexpr int kAccStages = 8;                      // accumulators of 32 columns in tensor memory (a ring)
+constexpr int kConvThreads = 192;                  // warp 0 loads, warp 1 issues MMAs, warps 2-5 drain
+constexpr int kBarBytes = 512;
+constexpr int kSmemConv = 1024 + kBAll + kSlots * kLineBytes + kBarBytes + 16;  // + alignment slack
 static_assert(kSmemConv <= 227 * 1024, "the convolution's shared memory exceeds a CTA's limit");
+static_assert(8 * (2 * kSlots + 2 * kAccStages + 1) <= kBarBytes, "mbarriers do not fit");
+static_assert(kBAll % 16 == 0 && kLineBytes % 16 == 0 && kChunkBytes % 16 == 0, "bulk copies need 16-B alignment");
 constexpr uint32_t kWaitLimit = 1u << 22;    // mbarrier polls before giving up
 constexpr unsigned kErrTimeout = 1u;
 
@@ -120,6 +132,41 @@ __device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
         if (mbar_try_wait(addr, parity)) return true;
     return false;
 }
+// the same, giving up early once another role of the CTA has failed
+__device__ __forceinline__ bool mbar_wait_or_fail(uint32_t addr, uint32_t parity, const volatile int *fail) {
+    for (uint32_t i = 0; i < kWaitLimit; ++i) {
+        if (mbar_try_wait(addr, parity)) return true;
+        if ((i & 255u) == 255u && *fail) return false;
+    }
+    return false;
+}
+// a long wait (the whole kernel): polls with a 256 ns pause, giving up after ~1 s or
+// once another role of the CTA has failed
+__device__ __forceinline__ bool mbar_wait_long(uint32_t addr, uint32_t parity, const volatile int *fail) {
+    for (uint32_t i = 0; i < kWaitLimit; ++i) {
+        if (mbar_try_wait(addr, parity)) return true;
+        if (*fail) return false;
+        __nanosleep(256);
+    }
+    return false;
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t addr) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(addr) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t addr, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(addr), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void st_shared16(uint32_t addr, uint4 v) {
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+                 : "memory");
+}
+// bytes (a multiple of 16) from global src to shared dst, both 16-byte aligned,
+// completing as transactions on mbar
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
 __device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void tmem_alloc(uint32_t slot, uint32_t ncols) {
@@ -130,18 +177,36 @@ __device__ __forceinline__ void tmem_alloc(uint32_t slot, uint32_t ncols) {
 __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(ncols) : "memory");
 }
-// D[tmem] (+)= A[smem] * B[smem]^T, kind::f16 (BF16 operands, FP32 accumulator)
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate) {
+// D[tmem] (+)= A[smem] * B[smem]^T, kind::f16 (BF16 operands, FP32 accumulator),
+// issued by one elected lane of a converged warp; descriptors as (low, high)
+// 32-bit words
+__device__ __forceinline__ void mma_bf16_elect(uint32_t d_tmem, uint32_t alo, uint32_t ahi, uint32_t blo,
+                                               uint32_t bhi, uint32_t idesc, uint32_t accumulate) {
     asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        "{\n .reg .pred p, e;\n .reg .b64 ad, bd;\n mov.b64 ad, {%1, %2};\n mov.b64 bd, {%3, %4};\n"
+        " setp.ne.b32 p, %6, 0;\n elect.sync _|e, 0xffffffff;\n"
+        " @e tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %5, p;\n}\n" ::"r"(d_tmem),
+        "r"(alo), "r"(ahi), "r"(blo), "r"(bhi), "r"(idesc), "r"(accumulate)
         : "memory");
 }
-__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+// the same issued by the one calling thread
+__device__ __forceinline__ void mma_bf16_one(uint32_t d_tmem, uint32_t alo, uint32_t ahi, uint32_t blo, uint32_t bhi,
+                                             uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n .reg .b64 ad, bd;\n mov.b64 ad, {%1, %2};\n mov.b64 bd, {%3, %4};\n"
+        " setp.ne.b32 p, %6, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %5, p;\n}\n" ::"r"(d_tmem),
+        "r"(alo), "r"(ahi), "r"(blo), "r"(bhi), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit_one(uint32_t mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
                  : "memory");
+}
+__device__ __forceinline__ void mma_commit_elect(uint32_t mbar) {
+    asm volatile(
+        "{\n .reg .pred e;\n elect.sync _|e, 0xffffffff;\n"
+        " @e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}\n" ::"r"(mbar)
+        : "memory");
 }
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile(
@@ -157,15 +222,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 }
 
-// shared-memory matrix descriptor: K-major, no swizzle; lbo = byte offset
-// between K-adjacent core matrices, sbo = between 8-row groups
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
-}
-// instruction descriptor: D FP32, A and B BF16, both K-major, N = 32, M = 128
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kC >> 3) << 17) |
-                            ((uint32_t)(kTileM >> 4) << 24);
+// instruction descriptor: D FP32, A and B BF16, both K-major, M = 128 (N in bits 17-22, in units of 8)
+constexpr uint32_t kIdescM128 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTileM >> 4) << 24);
+// Shared-memory matrix descriptors (K-major, no swizzle), as two 32-bit words:
+// low = start address >> 4 (bits 0-13) | leading (K chunk) offset >> 4 << 16;
+// high = stride (8-row group) offset >> 4 | version 1 at bit 46 (bit 14 of the high word).
+constexpr uint32_t kADescHiWord = (uint32_t)(128 >> 4) | (1u << 14);  // lines: 8-row groups 128 B apart
+constexpr uint32_t kBDescHiWord = (uint32_t)(512 >> 4) | (1u << 14);  // weights: 8-row groups 512 B apart
 
 // byte offset of element (row, k) of a K-major operand block in the core-matrix layout
 __host__ __device__ __forceinline__ int core_offset(int row, int k) {
@@ -173,178 +236,513 @@ __host__ __device__ __forceinline__ int core_offset(int row, int k) {
 }
 
 // MODE 0: bias + ReLU -> BF16; MODE 1: bias -> FP32; MODE 2: times ReLU'(ref) -> BF16.
-// Work item = (x, y segment, kPChunk consecutive phi); ny a multiple of 128.
-// Two accumulators in tensor memory (columns 0-31 and 32-63) pipeline the
-// tiles of a work item: the MMAs of tile k run while the CTA's warps take
-// tile k - 1's accumulator out (epilogue) and start the copies of the line
-// tile k + 2 adds, two tiles ahead, into the ring slot of a line whose last
-// MMAs completed before.
+// ny a multiple of 128.  Output tiles (x, y segment, phi) in the order phi
+// fastest; CTA b takes the contiguous range [b T / grid, (b + 1) T / grid)
+// of the T tiles and walks it in runs of consecutive phi at one (x, y
+// segment).  A run of L tiles streams its L + 2 input positions along phi;
+// the 3 lines (dx = -1, 0, 1) of input position p feed the output tiles
+// p + 1, p and p - 1 (dphi = -1, 0, +1), so one MMA of N = 96 covers all
+// three with the weights of the three dphi taps stacked along N (the packed
+// weights keep each (dx, dy) triple in the order dphi = +1, 0, -1): 18 MMAs
+// per input position instead of 54 of N = 32, and less than half the
+// shared-memory operand bytes.  The accumulators of consecutive tiles are
+// consecutive 32-column stages of a ring in tensor memory; an MMA is split
+// where the ring wraps, and where a tile takes its first product
+// (accumulate off).  Roles, synchronised through mbarriers with bounded
+// waits:
+//  - warp 0 (one thread) streams lines into a ring of kSlots buffers with
+//    bulk copies (cp.async.bulk): per line its 4 chunk bodies (2 KB each,
+//    contiguous in the activation layout) and its 8 halo pieces (16 B,
+//    periodic in y) straight into rows 7 and 136; full[slot] completes when
+//    the 8,320 bytes are in;
+//  - warp 1 (one thread) waits for a position's 3 lines and, when a tile
+//    starts, for its accumulator stage to be free; issues the MMAs; returns
+//    the lines to the producer (empty[slot]) and commits the tile that the
+//    position completed to acc_full[stage];
+//  - warps 2-5 wait for acc_full, read the accumulator (warp w the tensor-
+//    memory lanes 32 (w mod 4) ..), release it to acc_empty and write the
+//    outputs, while the tensor core already runs the next positions.
 template <int MODE>
-__global__ void __launch_bounds__(kTileM, 1) k_conv32(const __nv_bfloat16 *__restrict__ X,
-                                                      const uint8_t *__restrict__ Wpacked,
-                                                      const float *__restrict__ bias,
-                                                      const __nv_bfloat16 *__restrict__ ref, void *__restrict__ Y,
-                                                      Dims d, int nitems, unsigned *__restrict__ err) {
-    extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *sB = smem;
-    uint8_t *sL = smem + kBAll;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(sL + kSlots * kLineBytes);  // one per accumulator
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
+__global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 *__restrict__ X,
+                                                            const uint8_t *__restrict__ Wpacked,
+                                                            const float *__restrict__ bias,
+                                                            const __nv_bfloat16 *__restrict__ ref,
+                                                            void *__restrict__ Y, Dims d, unsigned *__restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t sB0 = (raw + 1023u) & ~1023u;
+    uint8_t *const sB = smem_raw + (sB0 - raw);
+    const uint32_t sL0 = sB0 + kBAll;
+    const uint32_t bar0 = sL0 + kSlots * kLineBytes;
+    auto full_bar = [&](uint32_t s) { return bar0 + 8u * s; };
+    auto empty_bar = [&](uint32_t s) { return bar0 + 8u * (kSlots + s); };
+    auto accf_bar = [&](uint32_t a) { return bar0 + 8u * (2 * kSlots + a); };
+    auto acce_bar = [&](uint32_t a) { return bar0 + 8u * (2 * kSlots + kAccStages + a); };
+    const uint32_t fin_bar = bar0 + 8u * (2 * kSlots + 2 * kAccStages);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(sB + kBAll + kSlots * kLineBytes + kBarBytes);
     volatile int *sfail = reinterpret_cast<volatile int *>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    for (int i = tid; i < kBAll / 16; i += kTileM)
+    for (int i = tid; i < kBAll / 16; i += kConvThreads)
         reinterpret_cast<uint4 *>(sB)[i] = reinterpret_cast<const uint4 *>(Wpacked)[i];
     if (tid == 0) {
-        mbar_init(smem_u32(mbar), 1);
-        mbar_init(smem_u32(mbar + 1), 1);
+        for (int s = 0; s < kSlots; ++s) {
+            mbar_init(full_bar(s), 1);  // the expect_tx arrival (+ the transactions)
+            mbar_init(empty_bar(s), 1);
+        }
+        for (int a = 0; a < kAccStages; ++a) {
+            mbar_init(accf_bar(a), 1);
+            mbar_init(acce_bar(a), 4);  // one arrival per epilogue warp
+        }
+        mbar_init(fin_bar, 1);
         *sfail = 0;
         fence_mbar_init();
     }
-    if (warp == 0) tmem_alloc(smem_u32(tslot), 64);
+    if (warp == 1) tmem_alloc(smem_u32(tslot), 32 * kAccStages);
     fence_proxy_async();
     tc_before_sync();
     __syncthreads();
     tc_after_sync();
     const uint32_t tmem = *tslot;
-    const uint32_t sL0 = smem_u32(sL), sB0 = smem_u32(sB);
-    const int nseg = d.ny / kTileM, npc = (d.np + kPChunk - 1) / kPChunk;
-    uint32_t phase0 = 0, phase1 = 0;
 
-    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int pc = item % npc, ys = (item / npc) % nseg, x = item / (npc * nseg);
-        const int p0 = pc * kPChunk, pcount = min(kPChunk, d.np - p0), y0 = ys * kTileM;
-        // line (x + dx, p0 + q - 1) of this segment, rows y0 - 1 .. y0 + 128, into slot (dx + 1) kRing + q % kRing
-        auto load_line = [&](int dx, int q) {
-            int xl = x + dx, pl = p0 + q - 1;
-            xl = xl < 0 ? xl + d.nx : (xl >= d.nx ? xl - d.nx : xl);
-            pl = ((pl % d.np) + d.np) % d.np;
-            const __nv_bfloat16 *line = X + (size_t)(xl * d.np + pl) * d.ny * kC;
-            const uint32_t dst0 = sL0 + (uint32_t)(((dx + 1) * kRing + q % kRing) * kLineBytes);
-            for (int e = tid; e < kLineRows * 4; e += kTileM) {
-                const int r = e >> 2, j = e & 3;
-                int yl = y0 + r - 1;
-                yl = yl < 0 ? yl + d.ny : (yl >= d.ny ? yl - d.ny : yl);
-                cp_async16(dst0 + j * kChunkBytes + r * 16, line + (size_t)yl * kC + j * 8);
-            }
-        };
-        // accumulator of tile kt -> bias / ReLU -> Y (every thread one row)
-        auto epilogue = [&](int kt) -> bool {
-            const int a = kt & 1;
-            if (!mbar_wait(smem_u32(mbar + a), a ? phase1 : phase0)) return false;
-            if (a) phase1 ^= 1u;
-            else phase0 ^= 1u;
-            tc_after_sync();
-            uint32_t r[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(32 * a), r);
-            const size_t vo = (size_t)((x * d.np + p0 + kt) * d.ny + y0 + warp * 32 + lane);  // this thread's row
-            if (MODE == 1) {
-                float4 *out = reinterpret_cast<float4 *>(reinterpret_cast<float *>(Y) + vo * kC);
+    const int nseg = d.ny / kTileM;
+    const int T = d.nx * nseg * d.np;
+    const int t0 = (int)((long long)blockIdx.x * T / gridDim.x);
+    const int t1 = (int)((long long)(blockIdx.x + 1) * T / gridDim.x);
+    // tile t -> (x, y0, p)
+    auto decode = [&](int t, int &x, int &y0, int &p) {
+        p = t % d.np;
+        y0 = ((t / d.np) % nseg) * kTileM;
+        x = t / (d.np * nseg);
+    };
+    auto wrapi = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
+
+    if (warp == 0) {
+        // ---- producer: the 3 lines of every input position of every run ----
+        if (lane == 0) {
+            uint32_t seq = 0;
+            bool ok = true;
+            for (int r0 = t0; r0 < t1 && ok;) {
+                int x, y0, pa;
+                decode(r0, x, y0, pa);
+                const int L = min(t1 - r0, d.np - pa);
+                const int ytop = wrapi(y0 - 1, d.ny), ybot = wrapi(y0 + kTileM, d.ny);
+                for (int j = 0; j < L + 2 && ok; ++j) {
+                    const int pin = wrapi(pa - 1 + j, d.np);
+                    for (int dx = -1; dx <= 1; ++dx, ++seq) {
+                        const uint32_t slot = seq % kSlots;
+                        if (seq >= (uint32_t)kSlots &&
+                            !mbar_wait_or_fail(empty_bar(slot), ((seq / kSlots) - 1u) & 1u, sfail)) {
+                            ok = false;
+                            break;
+                        }
+                        // chunk plane c of the line: ny rows of 16 B from X + (line 4 + c) ny 8
+                        const __nv_bfloat16 *plane = X + (size_t)(wrapi(x + dx, d.nx) * d.np + pin) * 4 * d.ny * 8;
+                        const uint32_t dst = sL0 + slot * (uint32_t)kLineBytes;
+                        mbar_expect_tx(full_bar(slot), 4u * (kBodyBytes + 32u));
 #pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    out[q] = make_float4(__uint_as_float(r[4 * q]) + bias[4 * q],
-                                         __uint_as_float(r[4 * q + 1]) + bias[4 * q + 1],
-                                         __uint_as_float(r[4 * q + 2]) + bias[4 * q + 2],
-                                         __uint_as_float(r[4 * q + 3]) + bias[4 * q + 3]);
-            } else {
-                uint32_t packed[16];
-#pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    float a0 = __uint_as_float(r[2 * q]), b0 = __uint_as_float(r[2 * q + 1]);
-                    if (MODE == 0) {
-                        a0 = fmaxf(a0 + bias[2 * q], 0.f);
-                        b0 = fmaxf(b0 + bias[2 * q + 1], 0.f);
-                    } else {
-                        const __nv_bfloat16 *rr = ref + vo * kC;
-                        a0 = __bfloat162float(rr[2 * q]) > 0.f ? a0 : 0.f;
-                        b0 = __bfloat162float(rr[2 * q + 1]) > 0.f ? b0 : 0.f;
-                    }
-                    __nv_bfloat162 h = __floats2bfloat162_rn(a0, b0);
-                    packed[q] = *reinterpret_cast<uint32_t *>(&h);
-                }
-                uint4 *out = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(Y) + vo * kC);
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    out[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
-            }
-            return true;
-        };
-        for (int q = 0; q < 3; ++q)
-            for (int dx = -1; dx <= 1; ++dx) load_line(dx, q);
-        cp_async_commit();
-        if (3 <= pcount + 1)
-            for (int dx = -1; dx <= 1; ++dx) load_line(dx, 3);
-        cp_async_commit();
-        int k = 0;
-        for (; k < pcount; ++k) {
-            // the line tile k + 2 adds goes into the slot of line k - 2, whose
-            // last MMAs (tile k - 2) completed before tile k - 2's epilogue
-            if (k + 4 <= pcount + 1)
-                for (int dx = -1; dx <= 1; ++dx) load_line(dx, k + 4);
-            cp_async_commit();
-            cp_async_wait<2>();  // the lines of tile k have landed
-            fence_proxy_async();
-            __syncthreads();
-            if (*sfail) break;
-            if (tid == 0) {
-                tc_after_sync();
-                const uint32_t dacc = tmem + (uint32_t)(32 * (k & 1));
-                uint32_t acc = 0;
-                for (int dx = -1; dx <= 1; ++dx)
-                    for (int dp = -1; dp <= 1; ++dp) {
-                        const uint32_t line = sL0 + (uint32_t)(((dx + 1) * kRing + (k + 1 + dp) % kRing) * kLineBytes);
-#pragma unroll
-                        for (int dy = -1; dy <= 1; ++dy) {
-                            const int tap = (dx + 1) * 9 + (dy + 1) * 3 + (dp + 1);
-#pragma unroll
-                            for (int kk = 0; kk < 2; ++kk) {
-                                const uint64_t ad = smem_desc(line + kk * 2 * kChunkBytes + (1 + dy) * 16, kChunkBytes, 128);
-                                const uint64_t bd = smem_desc(sB0 + tap * kBTap + kk * 256, 128, 512);
-                                mma_bf16(dacc, ad, bd, kIdesc, acc);
-                                acc = 1;
-                            }
+                        for (int c = 0; c < 4; ++c) {
+                            const __nv_bfloat16 *pc = plane + (size_t)c * d.ny * 8;
+                            const uint32_t dc = dst + c * kChunkBytes + kBodyOff;
+                            bulk_load(dc, pc + (size_t)y0 * 8, kBodyBytes, full_bar(slot));
+                            bulk_load(dc - 16, pc + (size_t)ytop * 8, 16, full_bar(slot));
+                            bulk_load(dc + kBodyBytes, pc + (size_t)ybot * 8, 16, full_bar(slot));
                         }
                     }
-                mma_commit(smem_u32(mbar + (k & 1)));
+                }
+                r0 += L;
             }
-            // tile k - 1 leaves its accumulator while tile k's MMAs run
-            if (k > 0 && !epilogue(k - 1)) *sfail = 1;
-            // every thread's tensor-memory reads finish before tile k + 1's MMAs overwrite that accumulator
-            tc_before_sync();
-            __syncthreads();
+            if (!ok) *sfail = 1;
+            // every load issued lands before the CTA may exit
+            for (uint32_t s = seq > (uint32_t)kSlots ? seq - kSlots : 0u; s < seq; ++s)
+                if (!mbar_wait(full_bar(s % kSlots), (s / kSlots) & 1u)) *sfail = 1;
         }
-        if (*sfail) break;
-        if (pcount > 0) {
-            if (!epilogue(pcount - 1)) *sfail = 1;
+    } else if (warp == 1) {
+        // ---- MMA issuer: the whole warp walks the schedule, one elected lane issues ----
+        // Per input position the MMAs go to at most three pieces of the accumulator ring: a
+        // piece is (tensor-memory column, N, weight block offset, accumulate flag).  The
+        // plan is made once per position; the 18 (dx, dy, K half) products then cost one
+        // add per descriptor each, so the issue keeps pace with the tensor core.
+        uint32_t seq = 0;
+        int ibase = 0;  // the CTA's count of tiles before this run (accumulator stage = count mod kAccStages)
+        bool ok = true;
+        for (int r0 = t0; r0 < t1 && ok;) {
+            int x, y0, pa;
+            decode(r0, x, y0, pa);
+            const int L = min(t1 - r0, d.np - pa);
+            for (int j = 0; j < L + 2; ++j, seq += 3) {
+                // the position's lines
+#pragma unroll
+                for (int dx = 0; dx < 3; ++dx) {
+                    const uint32_t q = seq + dx;
+                    if (ok) ok = mbar_wait_or_fail(full_bar(q % kSlots), (q / kSlots) & 1u, sfail);
+                }
+                // tile j starts at this position: its stage's previous tile has left it
+                const int inew = ibase + j;
+                if (ok && j < L && inew >= kAccStages)
+                    ok = mbar_wait_or_fail(acce_bar(inew % kAccStages), ((inew / kAccStages) - 1) & 1, sfail);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) break;
+                tc_after_sync();
+                // plan: tiles lo..hi take this position's products; tile k's block in the weight
+                // triple is k - j + 2 (dphi = +1, 0, -1); pieces split where the stage ring wraps
+                const int lo = j - 2 > 0 ? j - 2 : 0, hi = j < L - 1 ? j : L - 1;
+                uint32_t pc[3], pn[3], pb[3];  // pieces of the plain plan: column, idesc, B offset >> 4
+                uint32_t qc[3], qn[3], qb[3], qa[3];  // the first product's plan (the new tile separate)
+                int np_ = 0, nq = 0;
+                auto split = [&](int klo, int khi, uint32_t *c, uint32_t *n, uint32_t *b, int &cnt) {
+                    if (klo > khi) return;
+                    const int s0 = (ibase + klo) & (kAccStages - 1), tot = khi - klo + 1;
+                    const int n1 = tot < kAccStages - s0 ? tot : kAccStages - s0;
+                    c[cnt] = tmem + (uint32_t)(32 * s0);
+                    n[cnt] = kIdescM128 | ((uint32_t)(4 * n1) << 17);
+                    b[cnt] = (uint32_t)((klo - j + 2) * (kBTap >> 4));
+                    ++cnt;
+                    if (n1 < tot) {
+                        c[cnt] = tmem;
+                        n[cnt] = kIdescM128 | ((uint32_t)(4 * (tot - n1)) << 17);
+                        b[cnt] = (uint32_t)((klo + n1 - j + 2) * (kBTap >> 4));
+                        ++cnt;
+                    }
+                };
+                split(lo, hi, pc, pn, pb, np_);
+                if (j < L) {
+                    qc[0] = tmem + (uint32_t)(32 * ((ibase + j) & (kAccStages - 1)));
+                    qn[0] = kIdescM128 | (4u << 17);
+                    qb[0] = (uint32_t)(2 * (kBTap >> 4));
+                    qa[0] = 0u;  // tile j's first product
+                    nq = 1;
+                    split(lo, j - 1, qc, qn, qb, nq);
+                    for (int k = 1; k < 3; ++k) qa[k] = 1u;
+                } else {
+                    for (int k = 0; k < 3; ++k) {
+                        qc[k] = pc[k];
+                        qn[k] = pn[k];
+                        qb[k] = pb[k];
+                        qa[k] = 1u;
+                    }
+                    nq = np_;
+                }
+                const uint32_t bdesc0 = ((sB0 >> 4) & 0x3FFFu) | ((uint32_t)(128 >> 4) << 16);
+#pragma unroll
+                for (int dx = 0; dx < 3; ++dx) {
+                    const uint32_t lb = sL0 + ((seq + dx) % kSlots) * (uint32_t)kLineBytes;
+                    const uint32_t adesc0 = (lb >> 4) | ((uint32_t)(kChunkBytes >> 4) << 16);
+#pragma unroll
+                    for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+                        for (int kk = 0; kk < 2; ++kk) {
+                            const uint32_t a = adesc0 + (uint32_t)((kk * 2 * kChunkBytes + kBodyOff + (dy - 1) * 16) >> 4);
+                            const uint32_t b = bdesc0 + (uint32_t)(((dx * 9 + dy * 3) * kBTap + kk * 256) >> 4);
+                            if (dx == 0 && dy == 0 && kk == 0) {
+#pragma unroll
+                                for (int k = 0; k < 3; ++k)
+                                    if (k < nq) mma_bf16_elect(qc[k], a, kADescHiWord, b + qb[k], kBDescHiWord, qn[k], qa[k]);
+                            } else {
+#pragma unroll
+                                for (int k = 0; k < 3; ++k)
+                                    if (k < np_) mma_bf16_elect(pc[k], a, kADescHiWord, b + pb[k], kBDescHiWord, pn[k], 1u);
+                            }
+                        }
+                }
+#pragma unroll
+                for (int dx = 0; dx < 3; ++dx) mma_commit_elect(empty_bar((seq + dx) % kSlots));
+                if (j >= 2) mma_commit_elect(accf_bar((ibase + j - 2) % kAccStages));  // tile j - 2 is complete
+            }
+            ibase += L;
+            r0 += L;
+        }
+        if (!ok && lane == 0) *sfail = 1;
+        // the MMAs issued complete before the tensor memory is freed
+        mma_commit_elect(fin_bar);
+        if (!mbar_wait(fin_bar, 0) && lane == 0) *sfail = 1;
+        __syncwarp();
+    } else if (warp >= 2) {
+        // ---- epilogue ----
+        const int q = warp & 3;  // tensor-memory lanes 32 q .. 32 q + 31
+        int i = 0;
+        for (int t = t0; t < t1; ++t, ++i) {
+            const int a = i % kAccStages;
+            if (!mbar_wait_or_fail(accf_bar(a), (i / kAccStages) & 1, sfail)) {
+                *sfail = 1;
+                break;
+            }
+            tc_after_sync();
+            uint32_t r[32];
+            tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(32 * a), r);
             tc_before_sync();
-            __syncthreads();
-            if (*sfail) break;
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acce_bar(a));
+            int x, y0, p;
+            decode(t, x, y0, p);
+            // this thread's voxel: row y of line x np + p; chunk plane c at (line 4 + c) ny
+            const size_t line = (size_t)x * d.np + p, y = (size_t)(y0 + q * 32 + lane);
+            auto at = [&](int c) { return ((line * 4 + c) * d.ny + y) * 8; };
+            if (MODE == 1) {
+                float *out = reinterpret_cast<float *>(Y);
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    float4 *o = reinterpret_cast<float4 *>(out + at(c));
+                    o[0] = make_float4(__uint_as_float(r[8 * c]) + bias[8 * c], __uint_as_float(r[8 * c + 1]) + bias[8 * c + 1],
+                                       __uint_as_float(r[8 * c + 2]) + bias[8 * c + 2],
+                                       __uint_as_float(r[8 * c + 3]) + bias[8 * c + 3]);
+                    o[1] = make_float4(__uint_as_float(r[8 * c + 4]) + bias[8 * c + 4],
+                                       __uint_as_float(r[8 * c + 5]) + bias[8 * c + 5],
+                                       __uint_as_float(r[8 * c + 6]) + bias[8 * c + 6],
+                                       __uint_as_float(r[8 * c + 7]) + bias[8 * c + 7]);
+                }
+            } else {
+                uint32_t packed[16];
+                uint32_t mask[16];
+                if (MODE == 2) {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const uint4 u = *reinterpret_cast<const uint4 *>(ref + at(c));
+                        mask[4 * c] = u.x;
+                        mask[4 * c + 1] = u.y;
+                        mask[4 * c + 2] = u.z;
+                        mask[4 * c + 3] = u.w;
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    float a0 = __uint_as_float(r[2 * c]), b0 = __uint_as_float(r[2 * c + 1]);
+                    if (MODE == 0) {
+                        a0 = fmaxf(a0 + bias[2 * c], 0.f);
+                        b0 = fmaxf(b0 + bias[2 * c + 1], 0.f);
+                    } else {
+                        const __nv_bfloat162 m = *reinterpret_cast<const __nv_bfloat162 *>(&mask[c]);
+                        a0 = __low2float(m) > 0.f ? a0 : 0.f;
+                        b0 = __high2float(m) > 0.f ? b0 : 0.f;
+                    }
+                    __nv_bfloat162 h = __floats2bfloat162_rn(a0, b0);
+                    packed[c] = *reinterpret_cast<uint32_t *>(&h);
+                }
+                __nv_bfloat16 *out = reinterpret_cast<__nv_bfloat16 *>(Y);
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    *reinterpret_cast<uint4 *>(out + at(c)) =
+                        make_uint4(packed[4 * c], packed[4 * c + 1], packed[4 * c + 2], packed[4 * c + 3]);
+            }
         }
     }
+    __syncthreads();
     if (*sfail && tid == 0) atomicOr(err, kErrTimeout);
-    cp_async_wait<0>();
+    tc_after_sync();
+    if (warp == 1) tmem_dealloc(tmem, 32 * kAccStages);
+}
+
+// Weight gradient of a 32 -> 32 layer on the tensor cores:
+//   dW[tap][co][ci] = sum_v dZ[v][co] A[nbr(v, tap)][ci],   db[co] = sum_v dZ[v][co].
+// A GEMM over voxels: D[(4 lines x 32 ci) = 128][32 co] += X_rows[128][16 voxels]
+// dZ[32][16 voxels]^T, both operands MN-major in shared memory (no swizzle):
+// a core matrix is 8 voxels x 8 channels, one 16-byte row per voxel, which is
+// how a line buffer already holds its chunks, so the dy shift is again a
+// 16-byte row offset and the 4 lines of one MMA are 4 consecutive line slots
+// (M-group stride = the chunk stride, 2176 B, with line slots exactly 4
+// chunks long).  Per tile (x, y segment, phi) the 9 lines (dx, dphi) and the
+// tile's dZ are bulk-copied into one of two buffers; the 27 taps are 3 MMAs
+// of M = 128 per (dy, 16-voxel step): lines 0-3, 4-7 and 8 plus a line of
+// ones (its rows give db) and two slots whose rows are discarded.  9
+// accumulators of 32 columns persist in tensor memory over the CTA's tiles;
+// at the end the CTA writes its partial sums, and k_dn_wgrad_reduce adds
+// the CTAs' partials in a fixed order.
+constexpr int kWgSlotBytes = 4 * kChunkBytes;        // 8704 B: lines back to back at the M-group stride
+constexpr int kWgBufSlots = 10;                      // 9 lines + the ones line
+constexpr int kWgSlots = 2 * kWgBufSlots + 2;        // two buffers + 2 slots the last group's discarded rows read
+constexpr int kWgDzBytes = 4 * kBodyBytes;           // a tile's dZ: 4 chunks of 128 rows
+constexpr int kWgPartial = kTaps * kC * kC + kC;     // floats per CTA: dW then db
+constexpr int kSmemWg = 1024 + 2 * kWgDzBytes + kWgSlots * kWgSlotBytes + 128 + 64;
+static_assert(kSmemWg <= 227 * 1024, "the weight gradient's shared memory exceeds a CTA's limit");
+// M = 128, N = 32, A and B MN-major (bits 15, 16)
+constexpr uint32_t kIdescWg = kIdescM128 | (4u << 17) | (1u << 15) | (1u << 16);
+
+__global__ void __launch_bounds__(kConvThreads, 1) k_dn_wgrad_tc(const __nv_bfloat16 *__restrict__ dZ,
+                                                                 const __nv_bfloat16 *__restrict__ X,
+                                                                 float *__restrict__ partial, Dims d,
+                                                                 unsigned *__restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t sZ0 = (raw + 1023u) & ~1023u;  // dZ buffers
+    uint8_t *const sZ = smem_raw + (sZ0 - raw);
+    const uint32_t sS0 = sZ0 + 2 * kWgDzBytes;    // line slots
+    const uint32_t bar0 = sS0 + kWgSlots * kWgSlotBytes + 128;
+    auto full_bar = [&](uint32_t b) { return bar0 + 8u * b; };
+    auto empty_bar = [&](uint32_t b) { return bar0 + 16u + 8u * b; };
+    const uint32_t fin_bar = bar0 + 32u;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(sZ + (bar0 + 40u - sZ0));
+    volatile int *sfail = reinterpret_cast<volatile int *>(tslot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // the ones lines (rows y0 .. y0 + 127 of every chunk of slot 9 of each buffer)
+    for (int i = tid; i < 2 * 4 * kTileM; i += kConvThreads) {
+        const int b = i / (4 * kTileM), c = (i / kTileM) % 4, r = i % kTileM;
+        const uint32_t one2 = 0x3F803F80u;  // two BF16 1.0
+        st_shared16(sS0 + (uint32_t)((b * kWgBufSlots + 9) * kWgSlotBytes + c * kChunkBytes + kBodyOff + r * 16),
+                    make_uint4(one2, one2, one2, one2));
+    }
+    if (tid == 0) {
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(full_bar(b), 1);
+            mbar_init(empty_bar(b), 1);
+        }
+        mbar_init(fin_bar, 1);
+        *sfail = 0;
+        fence_mbar_init();
+    }
+    if (warp == 1) tmem_alloc(smem_u32(tslot), 512);
+    fence_proxy_async();
     tc_before_sync();
     __syncthreads();
     tc_after_sync();
-    if (warp == 0) tmem_dealloc(tmem, 64);
+    const uint32_t tmem = *tslot;
+
+    const int nseg = d.ny / kTileM;
+    const int T = d.nx * nseg * d.np;
+    const int t0 = (int)((long long)blockIdx.x * T / gridDim.x);
+    const int t1 = (int)((long long)(blockIdx.x + 1) * T / gridDim.x);
+    auto wrapi = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
+
+    if (warp == 0) {
+        // ---- producer: per tile 9 lines (12 bulk copies each) and the tile's dZ (4) ----
+        if (lane == 0) {
+            bool ok = true;
+            int i = 0;
+            for (int t = t0; t < t1; ++t, ++i) {
+                const int b = i & 1;
+                if (i >= 2 && !mbar_wait_or_fail(empty_bar(b), ((i >> 1) - 1) & 1, sfail)) {
+                    ok = false;
+                    break;
+                }
+                const int p = t % d.np, y0 = ((t / d.np) % nseg) * kTileM, x = t / (d.np * nseg);
+                const int ytop = wrapi(y0 - 1, d.ny), ybot = wrapi(y0 + kTileM, d.ny);
+                mbar_expect_tx(full_bar(b), 9u * 4u * (kBodyBytes + 32u) + (uint32_t)kWgDzBytes);
+                for (int l = 0; l < 9; ++l) {
+                    const int dx = l / 3 - 1, dp = l % 3 - 1;
+                    const __nv_bfloat16 *plane =
+                        X + (size_t)(wrapi(x + dx, d.nx) * d.np + wrapi(p + dp, d.np)) * 4 * d.ny * 8;
+                    const uint32_t dst = sS0 + (uint32_t)((b * kWgBufSlots + l) * kWgSlotBytes);
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const __nv_bfloat16 *pc = plane + (size_t)c * d.ny * 8;
+                        const uint32_t dc = dst + c * kChunkBytes + kBodyOff;
+                        bulk_load(dc, pc + (size_t)y0 * 8, kBodyBytes, full_bar(b));
+                        bulk_load(dc - 16, pc + (size_t)ytop * 8, 16, full_bar(b));
+                        bulk_load(dc + kBodyBytes, pc + (size_t)ybot * 8, 16, full_bar(b));
+                    }
+                }
+                const __nv_bfloat16 *zp = dZ + (size_t)(x * d.np + p) * 4 * d.ny * 8;
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    bulk_load(sZ0 + (uint32_t)(b * kWgDzBytes + c * kBodyBytes), zp + ((size_t)c * d.ny + y0) * 8,
+                              kBodyBytes, full_bar(b));
+            }
+            if (!ok) *sfail = 1;
+            // the loads issued land before the CTA may exit
+            for (int k = i > 2 ? i - 2 : 0; k < i; ++k)
+                if (!mbar_wait(full_bar(k & 1), (k >> 1) & 1)) *sfail = 1;
+        }
+    } else if (warp == 1) {
+        // ---- MMA issuer ----
+        if (lane == 0) {
+            constexpr uint32_t kAHi = (uint32_t)(kChunkBytes >> 4) | (1u << 14);  // M groups: the chunk stride
+            constexpr uint32_t kBHi = (uint32_t)(kBodyBytes >> 4) | (1u << 14);   // N groups: the dZ chunk stride
+            constexpr uint32_t kLbo = (uint32_t)(128 >> 4) << 16;                 // K groups: 8 voxels, 128 B
+            bool ok = true;
+            int i = 0;
+            for (int t = t0; t < t1; ++t, ++i) {
+                const int b = i & 1;
+                if (!mbar_wait_or_fail(full_bar(b), (i >> 1) & 1, sfail)) {
+                    ok = false;
+                    break;
+                }
+                tc_after_sync();
+                const uint32_t s0 = sS0 + (uint32_t)(b * kWgBufSlots * kWgSlotBytes), z0 = sZ0 + (uint32_t)(b * kWgDzBytes);
+#pragma unroll
+                for (int kk = 0; kk < kTileM / 16; ++kk) {
+                    const uint32_t bl = ((z0 + kk * 256) >> 4) | kLbo;
+                    const uint32_t acc = (i > 0 || kk > 0) ? 1u : 0u;
+#pragma unroll
+                    for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+                        for (int g = 0; g < 3; ++g) {
+                            const uint32_t al = ((s0 + g * 4 * kWgSlotBytes + kBodyOff + (16 * kk + dy - 1) * 16) >> 4) | kLbo;
+                            mma_bf16_one(tmem + (uint32_t)(32 * (dy * 3 + g)), al, kAHi, bl, kBHi, kIdescWg, acc);
+                        }
+                }
+                mma_commit_one(empty_bar(b));
+            }
+            if (!ok) *sfail = 1;
+            mma_commit_one(fin_bar);
+        }
+        __syncwarp();
+    }
+    // ---- every thread: the accumulators leave once the MMAs are done ----
+    bool done = warp == 1 ? mbar_wait(fin_bar, 0) : mbar_wait_long(fin_bar, 0, sfail);
+    if (warp >= 2 && done && t1 > t0) {
+        const int q = warp & 3;  // tensor-memory lanes 32 q ..: rows (line 4 g + q, ci = lane)
+        tc_after_sync();
+        float *out = partial + (size_t)blockIdx.x * kWgPartial;
+#pragma unroll 1
+        for (int a = 0; a < 9; ++a) {
+            const int dy = a / 3, g = a % 3, l = 4 * g + q;
+            uint32_t r[32];
+            tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(32 * a), r);
+            if (l < 9) {
+                const int tap = (l / 3) * 9 + dy * 3 + (l % 3);
+#pragma unroll
+                for (int co = 0; co < kC; ++co) out[(tap * kC + co) * kC + lane] = __uint_as_float(r[co]);
+            } else if (l == 9 && dy == 1 && lane == 0) {
+#pragma unroll
+                for (int co = 0; co < kC; ++co) out[kTaps * kC * kC + co] = __uint_as_float(r[co]);
+            }
+        }
+    } else if (warp >= 2 && t1 <= t0) {
+        float *out = partial + (size_t)blockIdx.x * kWgPartial;
+        for (int e = tid - 64; e < kWgPartial; e += kConvThreads - 64) out[e] = 0.f;
+    }
+    if (!done) *sfail = 1;
+    tc_before_sync();
+    __syncthreads();
+    if (*sfail && tid == 0) atomicOr(err, kErrTimeout);
+    tc_after_sync();
+    if (warp == 1) tmem_dealloc(tmem, 512);
+}
+
+// dW[e] += sum over the CTAs c of partial[c][e], in the order c = 0, 1, ...
+// (e < 27 x 32 x 32: the weights, then the 32 biases)
+__global__ void k_dn_wgrad_reduce(const float *__restrict__ partial, int ncta, float *__restrict__ dW,
+                                  float *__restrict__ db) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= kWgPartial) return;
+    float s = 0.f;
+    for (int c = 0; c < ncta; ++c) s += partial[(size_t)c * kWgPartial + e];
+    if (e < kTaps * kC * kC) dW[e] += s;
+    else db[e - kTaps * kC * kC] += s;
 }
 
 // FP32 weights W[tap][n][k] -> BF16 in the K-major core-matrix layout of the
-// B operand, one 2 KB block per tap.  MIRROR: block t holds W[26 - t][k][n]
-// (the weights of the backward-data convolution).
+// B operand, one 2 KB block per tap, tap = 9 (dx + 1) + 3 (dy + 1) + (dphi + 1);
+// within each (dx, dy) triple the blocks run dphi = +1, 0, -1, so that the
+// triple is the B operand of N = 96 whose column blocks feed the output
+// tiles phi - 1, phi, phi + 1 of one input position.  MIRROR: tap t holds
+// W[26 - t][k][n] (the weights of the backward-data convolution).
 template <bool MIRROR>
 __global__ void k_pack_weights(const float *__restrict__ W, uint8_t *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kTaps * kC * kC) return;
     const int t = i / (kC * kC), n = (i / kC) % kC, k = i % kC;
     const float w = MIRROR ? W[((kTaps - 1 - t) * kC + k) * kC + n] : W[(t * kC + n) * kC + k];
-    *reinterpret_cast<__nv_bfloat16 *>(out + t * kBTap + core_offset(n, k)) = __float2bfloat16_rn(w);
+    const int block = t - t % 3 + (2 - t % 3);
+    *reinterpret_cast<__nv_bfloat16 *>(out + block * kBTap + core_offset(n, k)) = __float2bfloat16_rn(w);
 }
 
 int g_sms = 0;
 
-// work items of the convolution: (x, y segment of 128, kPChunk positions along phi)
-int conv_items(Dims d) { return d.nx * (d.ny / kTileM) * ((d.np + kPChunk - 1) / kPChunk); }
+// tiles of the convolution: (x, y segment of 128, phi)
+int conv_tiles(Dims d) { return d.nx * (d.ny / kTileM) * d.np; }
+
+
 
 // ---- the network's CUDA-core layers -----------------------------------
 // Parameters (FP32, one array): w_in[27][32], b_in[32], w2[27][32][32],
@@ -353,28 +751,43 @@ constexpr int kOffWin = 0, kOffBin = kOffWin + kTaps * kC, kOffW2 = kOffBin + kC
               kOffW3 = kOffB2 + kC, kOffB3 = kOffW3 + kTaps * kC * kC, kOffWout = kOffB3 + kC,
               kOffBout = kOffWout + kTaps * kC, kParams = kOffBout + 1;
 
-__device__ __forceinline__ void store_bf16x32(__nv_bfloat16 *dst, const float (&a)[32]) {
-    uint32_t q[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-        __nv_bfloat162 h = __floats2bfloat162_rn(a[2 * i], a[2 * i + 1]);
-        q[i] = *reinterpret_cast<uint32_t *>(&h);
-    }
-    uint4 *o = reinterpret_cast<uint4 *>(dst);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) o[i] = make_uint4(q[4 * i], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]);
+// The activation layout: line = x np + phi, channel chunk c = channel / 8
+// (16 B of BF16); element (line, y, channel) at ((line 4 + c) ny + y) 8 +
+// channel % 8.  Each line's chunk plane (ny rows of 16 B) is contiguous, so
+// a tile's 128 rows of one chunk are one 2 KB block.  act_at(v, c, ny) is
+// the element offset of chunk c of voxel v = line ny + y.
+__device__ __forceinline__ size_t act_at_line(uint32_t line, uint32_t y, int c, int ny) {
+    return (((size_t)line * 4 + (size_t)c) * (size_t)ny + y) * 8;
 }
-__device__ __forceinline__ void load_bf16x32(const __nv_bfloat16 *src, float (&a)[32]) {
-    const uint4 *s = reinterpret_cast<const uint4 *>(src);
+__device__ __forceinline__ size_t act_at(size_t v, int c, int ny) {
+    const uint32_t line = (uint32_t)v / (uint32_t)ny, y = (uint32_t)v - line * (uint32_t)ny;  // v < 2^27
+    return act_at_line(line, y, c, ny);
+}
+// the 32 channels of voxel v, rounded to BF16
+__device__ __forceinline__ void store_act32(__nv_bfloat16 *A, size_t v, int ny, const float (&a)[32]) {
+    const size_t at0 = act_at(v, 0, ny), plane = (size_t)ny * 8;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const uint4 u = s[i];
+    for (int c = 0; c < 4; ++c) {
+        uint32_t q[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            __nv_bfloat162 h = __floats2bfloat162_rn(a[8 * c + 2 * i], a[8 * c + 2 * i + 1]);
+            q[i] = *reinterpret_cast<uint32_t *>(&h);
+        }
+        *reinterpret_cast<uint4 *>(A + at0 + c * plane) = make_uint4(q[0], q[1], q[2], q[3]);
+    }
+}
+__device__ __forceinline__ void load_act32(const __nv_bfloat16 *A, size_t v, int ny, float (&a)[32]) {
+    const size_t at0 = act_at(v, 0, ny), plane = (size_t)ny * 8;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const uint4 u = *reinterpret_cast<const uint4 *>(A + at0 + c * plane);
         const uint32_t w[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162 *>(&w[j]);
-            a[8 * i + 2 * j] = __low2float(h);
-            a[8 * i + 2 * j + 1] = __high2float(h);
+            a[8 * c + 2 * j] = __low2float(h);
+            a[8 * c + 2 * j + 1] = __high2float(h);
         }
     }
 }
@@ -404,15 +817,15 @@ __global__ void k_dn_transpose(const float *__restrict__ src, float *__restrict_
 // y0 + 127 (256 voxels, 2 per thread: the same y, both phi rows) and stages
 // its periodic halo (x0 +- 1, p0 - 1 .. p0 + 2, y0 - 1 .. y0 + 128) in
 // shared memory once; the 27 taps then read shared memory, and each staged
-// row serves both voxels of its thread.  Activation rows (32 channels, 64 B)
-// are stored with their four 16-byte chunks permuted by (row >> 1) & 3, so
-// that 8 consecutive rows read by one phase of a 128-bit load fall in 8
-// distinct bank groups.
+// row serves both voxels of its thread.  The output layer stages its input
+// as 4 chunk planes of 16-byte rows, as the activation layout holds them, so
+// the copies are contiguous on both sides and a warp's 128-bit reads of one
+// plane (32 consecutive rows) are free of bank conflicts.
 constexpr int kTileY = 128, kTileP = 2, kHaloY = kTileY + 2, kHaloP = kTileP + 2;
-constexpr int kOutSmem = 3 * kHaloP * kHaloY * 64;  // bf16 rows of the output layer's input
+constexpr int kOutRows = 3 * kHaloP * kHaloY;       // staged rows of the output layer's input
+constexpr int kOutSmem = kOutRows * 64;              // their 4 chunk planes of 16-byte rows
 
 __device__ __forceinline__ int wrap_idx(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
-__device__ __forceinline__ int tile_chunk(int row, int k) { return k ^ ((row >> 1) & 3); }
 
 // tile coordinates of the CTA: blockIdx.x over (x, phi pairs, y chunks)
 __device__ __forceinline__ void tile_origin(Dims d, int &x0, int &p0, int &y0) {
@@ -466,8 +879,8 @@ __global__ void __launch_bounds__(128) k_dn_in_tiled(const float *__restrict__ x
         a1[c] = fmaxf(a1[c], 0.f);
     }
     const int y = y0 + ty;
-    store_bf16x32(A1 + (((size_t)x0 * d.np + p0) * d.ny + y) * kC, a0);
-    if (p0 + 1 < d.np) store_bf16x32(A1 + (((size_t)x0 * d.np + p0 + 1) * d.ny + y) * kC, a1);
+    store_act32(A1, ((size_t)x0 * d.np + p0) * d.ny + y, d.ny, a0);
+    if (p0 + 1 < d.np) store_act32(A1, ((size_t)x0 * d.np + p0 + 1) * d.ny + y, d.ny, a1);
 }
 
 // output layer 32 -> 1 with the residual: y[v] = x[v] + b_out + sum_tap w_out[tap] . A3[nbr(v, tap)]
@@ -480,12 +893,13 @@ __global__ void __launch_bounds__(128) k_dn_out_tiled(const __nv_bfloat16 *__res
     int x0, p0, y0;
     tile_origin(d, x0, p0, y0);
     const uint32_t base = smem_u32(dn_out_smem);
-    for (int i = threadIdx.x; i < 3 * kHaloP * kHaloY * 4; i += blockDim.x) {
-        const int k = i & 3, r = i >> 2;  // 16-byte chunk k of staged row r
+    for (int i = threadIdx.x; i < kOutRows * 4; i += blockDim.x) {
+        // 16-byte chunk k of staged row r, staged as planes [k][r] like the activation layout:
+        // consecutive threads copy consecutive rows of one plane, contiguous on both sides
+        const int k = i / kOutRows, r = i - k * kOutRows;
         const int ys = r % kHaloY, ip = (r / kHaloY) % kHaloP, ix = r / (kHaloY * kHaloP);
         const int gx = wrap_idx(x0 + ix - 1, d.nx), gp = wrap_idx(p0 + ip - 1, d.np), gy = wrap_idx(y0 + ys - 1, d.ny);
-        cp_async16(base + (uint32_t)(r * 64 + tile_chunk(ys, k) * 16),
-                   A3 + (((size_t)gx * d.np + gp) * d.ny + gy) * kC + 8 * k);
+        cp_async16(base + (uint32_t)(i * 16), A3 + act_at_line((uint32_t)(gx * d.np + gp), (uint32_t)gy, k, d.ny));
     }
     cp_async_commit();
     for (int i = threadIdx.x; i < kTaps * kC + 1; i += blockDim.x) sw[i] = P[kOffWout + i];
@@ -505,7 +919,7 @@ __global__ void __launch_bounds__(128) k_dn_out_tiled(const __nv_bfloat16 *__res
                 const float4 *w1 = reinterpret_cast<const float4 *>(sw + (dx * 9 + dy * 3 + ip - 1) * kC);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const uint4 u = *reinterpret_cast<const uint4 *>(dn_out_smem + r * 64 + tile_chunk(ys, k) * 16);
+                    const uint4 u = *reinterpret_cast<const uint4 *>(dn_out_smem + (k * kOutRows + r) * 16);
                     const float v[8] = {__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xFFFF0000u),
                                         __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xFFFF0000u),
                                         __uint_as_float(u.z << 16), __uint_as_float(u.z & 0xFFFF0000u),
@@ -634,10 +1048,10 @@ __global__ void __launch_bounds__(128) k_dn_out_bwd(const float *__restrict__ dy
         for (int c = 0; c < kC; ++c) g[c] = fmaf(sw[t * kC + c], dv, g[c]);
     }
     float a[32];
-    load_bf16x32(A3 + (size_t)u * kC, a);
+    load_act32(A3, (size_t)u, d.ny, a);
 #pragma unroll
     for (int c = 0; c < kC; ++c) g[c] = a[c] > 0.f ? g[c] : 0.f;
-    store_bf16x32(dZ3 + (size_t)u * kC, g);
+    store_act32(dZ3, (size_t)u, d.ny, g);
 }
 
 // Reduce-scatter across a warp: each lane holds v[0..31]; afterwards lane l
@@ -680,7 +1094,7 @@ __global__ void __launch_bounds__(128) k_dn_wgrad_c1(const __nv_bfloat16 *__rest
         if (OUT) {
             s_own = sv[v];
         } else {
-            load_bf16x32(S + (size_t)v * kC, own);
+            load_act32(S, (size_t)v, d.ny, own);
             float t[32];
 #pragma unroll
             for (int c = 0; c < kC; ++c) t[c] = own[c];
@@ -690,7 +1104,7 @@ __global__ void __launch_bounds__(128) k_dn_wgrad_c1(const __nv_bfloat16 *__rest
             const Vox u = vx.moved(tap, d);
             float p[32];
             if (OUT) {
-                load_bf16x32(S + (size_t)u.act(d) * kC, p);
+                load_act32(S, (size_t)u.act(d), d.ny, p);
 #pragma unroll
                 for (int c = 0; c < kC; ++c) p[c] *= s_own;
             } else {
@@ -704,80 +1118,6 @@ __global__ void __launch_bounds__(128) k_dn_wgrad_c1(const __nv_bfloat16 *__rest
     __syncthreads();
     for (int i = tid; i < kTaps * kC; i += blockDim.x) atomicAdd(&dW[i], acc[i]);
     if (!OUT && tid < kC) atomicAdd(&db[tid], acc[kTaps * kC + tid]);
-}
-
-// weight gradient of a 32 -> 32 layer: dW[tap][co][ci] = sum_v dZ[v][co] A[nbr(v, tap)][ci].
-// Grid (27 taps, blocks over voxel tiles of 128).  A tile of dZ and the
-// tap-shifted tile of A are staged in shared memory as FP32; each thread
-// accumulates a 4 x 4 block of (co, ci) over a quarter of the tile's voxels.
-__global__ void __launch_bounds__(256) k_dn_wgrad32(const __nv_bfloat16 *__restrict__ dZ,
-                                                    const __nv_bfloat16 *__restrict__ A, float *__restrict__ dW,
-                                                    float *__restrict__ db, Dims d, int ntiles) {
-    __shared__ __align__(16) float sZ[kTileM][kC + 4];
-    __shared__ __align__(16) float sA[kTileM][kC + 4];
-    const int tap = blockIdx.x, tid = threadIdx.x;
-    const int g = tid >> 6, lt = tid & 63, cb = lt >> 3, ib = lt & 7;
-    float acc[4][4], bacc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
-    const int r = tid >> 1, h = tid & 1;
-    const bool centre = tap == kTaps / 2 && ib == 0;  // these threads also sum dZ (the bias gradient)
-    for (int tile = blockIdx.y; tile < ntiles; tile += gridDim.y) {
-        const int v = tile * kTileM + r;  // activation indices
-        const int u = Vox::from_act(v, d).moved(tap, d).act(d);
-        const uint4 *zs = reinterpret_cast<const uint4 *>(dZ + (size_t)v * kC + 16 * h);
-        const uint4 *as = reinterpret_cast<const uint4 *>(A + (size_t)u * kC + 16 * h);
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            const uint4 zu = zs[q], au = as[q];
-            const uint32_t zw[4] = {zu.x, zu.y, zu.z, zu.w}, aw[4] = {au.x, au.y, au.z, au.w};
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const __nv_bfloat162 zh = *reinterpret_cast<const __nv_bfloat162 *>(&zw[j]);
-                const __nv_bfloat162 ah = *reinterpret_cast<const __nv_bfloat162 *>(&aw[j]);
-                sZ[r][16 * h + 8 * q + 2 * j] = __low2float(zh);
-                sZ[r][16 * h + 8 * q + 2 * j + 1] = __high2float(zh);
-                sA[r][16 * h + 8 * q + 2 * j] = __low2float(ah);
-                sA[r][16 * h + 8 * q + 2 * j + 1] = __high2float(ah);
-            }
-        }
-        __syncthreads();
-#pragma unroll 4
-        for (int k = g; k < kTileM; k += 4) {
-            const float4 z = *reinterpret_cast<const float4 *>(&sZ[k][4 * cb]);
-            const float4 a = *reinterpret_cast<const float4 *>(&sA[k][4 * ib]);
-            const float zz[4] = {z.x, z.y, z.z, z.w}, aa[4] = {a.x, a.y, a.z, a.w};
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(zz[i], aa[j], acc[i][j]);
-            if (centre) {
-#pragma unroll
-                for (int i = 0; i < 4; ++i) bacc[i] += zz[i];
-            }
-        }
-        __syncthreads();
-    }
-    // the four voxel groups' partial sums, then one atomic per (co, ci)
-    float *red = &sZ[0][0];  // 4 x 64 x 16 floats fit in sZ
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) red[(g * 64 + lt) * 16 + 4 * i + j] = acc[i][j];
-    __syncthreads();
-    for (int o = tid; o < kC * kC; o += blockDim.x) {
-        const int co = o >> 5, ci = o & 31;
-        const int l = (co >> 2) * 8 + (ci >> 2), e = (co & 3) * 4 + (ci & 3);
-        const float s = red[(0 * 64 + l) * 16 + e] + red[(1 * 64 + l) * 16 + e] + red[(2 * 64 + l) * 16 + e] +
-                        red[(3 * 64 + l) * 16 + e];
-        atomicAdd(&dW[(tap * kC + co) * kC + ci], s);
-    }
-    if (centre) {
-#pragma unroll
-        for (int i = 0; i < 4; ++i) atomicAdd(&db[4 * cb + i], bacc[i]);
-    }
 }
 
 // Adam (Kingma and Ba, 2015) on the FP32 parameters
@@ -799,10 +1139,14 @@ extern "C" int ss_dn_conv32(const void *x, const float *w, const float *bias, co
                             uint32_t nx, uint32_t ny, uint32_t np, uint32_t mode, void *stream) {
     char buf[256];
     if (!x || !w || !y || (mode != 2 && !bias) || (mode == 2 && !ref) || mode > 2 || nx < 1 || ny < 1 || np < 1 ||
-        ny % kTileM != 0 || (unsigned long long)nx * ny * np > (1ull << 27)) {
-        ss::record_error("ss_dn_conv32: null pointer, mode > 2, or ny not a positive multiple of 128");
+        ny % kTileM != 0 || (unsigned long long)nx * ny * np > (1ull << 27) ||
+        (((uintptr_t)x | (uintptr_t)y | (uintptr_t)ref) & 15u) != 0) {
+        ss::record_error(
+            "ss_dn_conv32: null pointer, mode > 2, ny not a positive multiple of 128, or x, y, ref not 16-byte "
+            "aligned");
         return SS_ERR_INVALID_ARGUMENT;
     }
+    Dims d{(int)nx, (int)ny, (int)np};
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaSuccess;
     if (!g_sms) {
@@ -823,13 +1167,12 @@ extern "C" int ss_dn_conv32(const void *x, const float *w, const float *bias, co
         const int nw = kTaps * kC * kC;
         if (mode == 2) k_pack_weights<true><<<(nw + 255) / 256, 256, 0, s>>>(w, packed);
         else k_pack_weights<false><<<(nw + 255) / 256, 256, 0, s>>>(w, packed);
-        Dims d{(int)nx, (int)ny, (int)np};
-        const int items = conv_items(d), grid = items < g_sms ? items : g_sms;
+        const int tiles = conv_tiles(d), grid = tiles < g_sms ? tiles : g_sms;
         const __nv_bfloat16 *X = reinterpret_cast<const __nv_bfloat16 *>(x);
         const __nv_bfloat16 *R = reinterpret_cast<const __nv_bfloat16 *>(ref);
-        if (mode == 0) k_conv32<0><<<grid, kTileM, kSmemConv, s>>>(X, packed, bias, R, y, d, items, derr);
-        else if (mode == 1) k_conv32<1><<<grid, kTileM, kSmemConv, s>>>(X, packed, bias, R, y, d, items, derr);
-        else k_conv32<2><<<grid, kTileM, kSmemConv, s>>>(X, packed, bias, R, y, d, items, derr);
+        if (mode == 0) k_conv32<0><<<grid, kConvThreads, kSmemConv, s>>>(X, packed, bias, R, y, d, derr);
+        else if (mode == 1) k_conv32<1><<<grid, kConvThreads, kSmemConv, s>>>(X, packed, bias, R, y, d, derr);
+        else k_conv32<2><<<grid, kConvThreads, kSmemConv, s>>>(X, packed, bias, R, y, d, derr);
         e = cudaGetLastError();
     }
     unsigned herr = 0;
@@ -897,6 +1240,7 @@ struct ss_dn {
           *ta = nullptr;
     uint8_t *Wp2 = nullptr, *Wp3 = nullptr, *Wm2 = nullptr, *Wm3 = nullptr;
     __nv_bfloat16 *A1 = nullptr, *A2 = nullptr, *A3 = nullptr, *D1 = nullptr, *D2 = nullptr;
+    float *wpart = nullptr;  // the weight gradients' per-CTA partial sums
     double *sums = nullptr;
     unsigned *err = nullptr;
     long long adam_t = 0;
@@ -927,6 +1271,7 @@ void conv_attrs() {
     cudaFuncSetAttribute(k_conv32<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
     cudaFuncSetAttribute(k_conv32<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
     cudaFuncSetAttribute(k_conv32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
+    cudaFuncSetAttribute(k_dn_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemWg);
     cudaFuncSetAttribute(k_dn_out_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          kOutSmem + (kTaps * kC + 4) * (int)sizeof(float));
     done = true;
@@ -935,8 +1280,8 @@ void conv_attrs() {
 template <int MODE>
 void launch_conv(ss_dn *n, const __nv_bfloat16 *X, const uint8_t *W, const float *bias, const __nv_bfloat16 *ref,
                  void *Y, cudaStream_t s) {
-    const int items = conv_items(n->d), grid = items < n->sms ? items : n->sms;
-    k_conv32<MODE><<<grid, kTileM, kSmemConv, s>>>(X, W, bias, ref, Y, n->d, items, n->err);
+    const int tiles = conv_tiles(n->d), grid = tiles < n->sms ? tiles : n->sms;
+    k_conv32<MODE><<<grid, kConvThreads, kSmemConv, s>>>(X, W, bias, ref, Y, n->d, n->err);
 }
 
 void pack_all(ss_dn *n, cudaStream_t s) {
@@ -983,16 +1328,20 @@ void enqueue_backward(ss_dn *n, const float *t, const float *ya, cudaStream_t s,
         k_dn_loss<<<2 * n->sms, 256, 0, s>>>(ya, n->ta, n->dy, n->nvox, n->sums, grads ? n->G + kOffBout : nullptr);
     n->launches += 2;
     if (!grads) return;
-    const dim3 wg(kTaps, (unsigned)(n->sms > 0 ? (4 * n->sms + kTaps - 1) / kTaps : 8));
+    const int wgrid = conv_tiles(n->d) < n->sms ? conv_tiles(n->d) : n->sms;
+    auto wgrad = [&](const __nv_bfloat16 *dZ, const __nv_bfloat16 *A, float *dW, float *db) {
+        k_dn_wgrad_tc<<<wgrid, kConvThreads, kSmemWg, s>>>(dZ, A, n->wpart, n->d, n->err);
+        k_dn_wgrad_reduce<<<(kWgPartial + 255) / 256, 256, 0, s>>>(n->wpart, wgrid, dW, db);
+    };
     const unsigned pg = (unsigned)(n->ntiles < 8 * n->sms ? n->ntiles : 8 * n->sms);
     k_dn_out_bwd<<<b, 128, 0, s>>>(n->dy, n->P, n->A3, n->D1, n->d, n->nvox);
     k_dn_wgrad_c1<true><<<pg, 128, 0, s>>>(n->A3, n->dy, n->G + kOffWout, nullptr, n->d, n->ntiles);
-    k_dn_wgrad32<<<wg, 256, 0, s>>>(n->D1, n->A2, n->G + kOffW3, n->G + kOffB3, n->d, n->ntiles);
+    wgrad(n->D1, n->A2, n->G + kOffW3, n->G + kOffB3);
     launch_conv<2>(n, n->D1, n->Wm3, nullptr, n->A2, n->D2, s);
-    k_dn_wgrad32<<<wg, 256, 0, s>>>(n->D2, n->A1, n->G + kOffW2, n->G + kOffB2, n->d, n->ntiles);
+    wgrad(n->D2, n->A1, n->G + kOffW2, n->G + kOffB2);
     launch_conv<2>(n, n->D2, n->Wm2, nullptr, n->A1, n->D1, s);
     k_dn_wgrad_c1<false><<<pg, 128, 0, s>>>(n->D1, n->xa, n->G + kOffWin, n->G + kOffBin, n->d, n->ntiles);
-    n->launches += 8;
+    n->launches += 10;
 }
 
 int check_err(ss_dn *n) {
@@ -1011,7 +1360,7 @@ void destroy_dn(ss_dn *n) {
     cudaFree(n->xa); cudaFree(n->ta);
     cudaFree(n->Wp2); cudaFree(n->Wp3); cudaFree(n->Wm2); cudaFree(n->Wm3);
     cudaFree(n->A1); cudaFree(n->A2); cudaFree(n->A3); cudaFree(n->D1); cudaFree(n->D2);
-    cudaFree(n->sums); cudaFree(n->err);
+    cudaFree(n->sums); cudaFree(n->err); cudaFree(n->wpart);
     if (n->own_stream && n->stream) cudaStreamDestroy(n->stream);
     delete n;
 }
@@ -1052,6 +1401,7 @@ int ss_dn_create(uint32_t nx, uint32_t ny, uint32_t np, uint64_t seed, void *str
     A((void **)&n->A1, ab); A((void **)&n->A2, ab); A((void **)&n->A3, ab); A((void **)&n->D1, ab);
     A((void **)&n->D2, ab);
     A((void **)&n->sums, 2 * sizeof(double)); A((void **)&n->err, sizeof(unsigned));
+    A((void **)&n->wpart, (size_t)(n->sms > 0 ? n->sms : 1) * kWgPartial * sizeof(float));
     // He initialisation of the convolutions; the output layer starts near
     // zero so that the network starts as the identity (residual)
     std::vector<float> h(kParams, 0.f);

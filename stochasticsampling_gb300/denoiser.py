@@ -187,31 +187,37 @@ def train(dn, X, T, epochs=1, batch=8, lr=1e-3, seed=0, val=None):
 
 
 def _main():
-    """python -m stochasticsampling_gb300.denoiser [--forwards K] [--shape NX NY NP]:
+    """python -m stochasticsampling_gb300.denoiser [--forwards K] [--train-steps S] [--shape NX NY NP]:
     K forward passes of a freshly initialised network on a random histogram
-    of the given grid (default the production grid 128 x 128 x 32), timed with
-    CUDA events; the command the convolution's profiles were taken with."""
+    of the given grid (default the production grid 128 x 128 x 32), then S
+    training steps (batch 1, Adam) on a random pair, each timed with CUDA
+    events; the command the convolution's profiles were taken with."""
     import argparse
 
     import torch
     ap = argparse.ArgumentParser()
     ap.add_argument("--forwards", type=int, default=3)
+    ap.add_argument("--train-steps", type=int, default=0)
     ap.add_argument("--shape", type=int, nargs=3, default=(128, 128, 32))
     args = ap.parse_args()
     dn = Denoiser(tuple(args.shape), seed=0)
     g = torch.Generator(device="cuda").manual_seed(0)
     x = 1.0 + 0.5 * torch.rand(tuple(args.shape), device="cuda", generator=g)
     y = torch.empty_like(x)
-    times = []
-    for _ in range(args.forwards):
+
+    def timed(fn):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        dn.forward(x, out=y)
+        fn()
         e1.record()
         torch.cuda.synchronize()
-        times.append(e0.elapsed_time(e1))
+        return e0.elapsed_time(e1)
+
+    fwd = [timed(lambda: dn.forward(x, out=y)) for _ in range(args.forwards)]
+    t = 1.0 + 0.1 * torch.rand(tuple(args.shape), device="cuda", generator=g)
+    train = [timed(lambda: dn.train(x[None], t[None], lr=1e-4)) for _ in range(args.train_steps)]
     dn.close()
-    print({"shape": list(args.shape), "forward_ms": times})
+    print({"shape": list(args.shape), "forward_ms": fwd, "train_step_ms": train})
 
 
 if __name__ == "__main__":

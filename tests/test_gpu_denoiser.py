@@ -1,7 +1,8 @@
 """The denoiser's tensor-core convolution (ss_dn_conv32, tcgen05) against a
 plain PyTorch fp32 reference: conv3d with circular padding on the same
-BF16-rounded inputs and weights.  Activations are [nx][nphi][ny][32]
-(ny a multiple of 128).
+BF16-rounded inputs and weights.  The tests hold activations as
+[nx][nphi][ny][32] and pass them to the library in its layout
+[nx][nphi][4][ny][8] (ny a multiple of 128).
 
 Products of BF16 numbers are exact in FP32, so the kernel differs from the
 reference only by FP32 summation order (864 terms): relative error below
@@ -17,7 +18,10 @@ from test_gpu_parity import _gpu
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(2, 128, 8), (3, 128, 5), (2, 256, 3)]  # (nx, ny, nphi)
+# (nx, ny, nphi); the larger grids give every CTA several tiles, so that the
+# line ring is reused along phi and the CTAs' ranges cross segments and x
+SHAPES = [(2, 128, 8), (3, 128, 5), (2, 256, 3), (24, 256, 12), (128, 128, 32)]
+SHAPE_IDS = ["x".join(map(str, s)) for s in SHAPES]
 
 
 def _torch():
@@ -29,15 +33,33 @@ def _torch():
 
 def _conv_ref(torch, x, w, bias):
     """x (nx, nphi, ny, 32) fp32 (the activation layout); w (27, 32 out, 32 in)
-    -> periodic 3x3x3 conv + bias in the same layout."""
+    -> periodic 3x3x3 conv + bias in the same layout (on the device of x,
+    in full FP32: no TF32)."""
     import torch.nn.functional as F
     wt = w.reshape(3, 3, 3, 32, 32).permute(3, 4, 0, 1, 2).contiguous()  # [out][in][dx][dy][dp]
     xi = x.permute(3, 0, 2, 1)[None]  # (1, C, nx, ny, nphi)
-    y = F.conv3d(F.pad(xi, (1, 1, 1, 1, 1, 1), mode="circular"), wt, bias)
+    tf32 = torch.backends.cudnn.allow_tf32
+    torch.backends.cudnn.allow_tf32 = False
+    try:
+        y = F.conv3d(F.pad(xi, (1, 1, 1, 1, 1, 1), mode="circular"), wt.to(x.device),
+                     None if bias is None else bias.to(x.device))
+    finally:
+        torch.backends.cudnn.allow_tf32 = tf32
     return y[0].permute(1, 3, 2, 0).contiguous()
 
 
-def _call(ss, x, w, b, ref, y, shape, mode):
+def planar(a):
+    """[nx][nphi][ny][32] -> the library's activation layout [nx][nphi][4][ny][8]."""
+    nx, np_, ny, _ = a.shape
+    return a.reshape(nx, np_, ny, 4, 8).permute(0, 1, 3, 2, 4).contiguous()
+
+
+def unplanar(a):
+    nx, np_, _, ny, _ = a.shape
+    return a.permute(0, 1, 3, 2, 4).reshape(nx, np_, ny, 32)
+
+
+def _raw(ss, x, w, b, ref, y, shape, mode):
     lib = ss.load_library()
     p = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
     rc = lib.ss_dn_conv32(p(x), p(w), p(b), p(ref), p(y), *shape, mode, None)
@@ -45,7 +67,14 @@ def _call(ss, x, w, b, ref, y, shape, mode):
         raise ss.SsError(rc, ss._lib.last_error())
 
 
-@pytest.mark.parametrize("shape", SHAPES, ids=["2x128x8", "3x128x5", "2x256x3"])
+def _call(ss, x, w, b, ref, y, shape, mode):
+    """The convolution on x, ref, y given as [nx][nphi][ny][32] (y filled in place)."""
+    yp = planar(y)
+    _raw(ss, planar(x), w, b, None if ref is None else planar(ref), yp, shape, mode)
+    y.copy_(unplanar(yp))
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=SHAPE_IDS)
 def test_conv32_forward_matches_torch(shape):
     ss = _gpu()
     torch = _torch()
@@ -54,7 +83,7 @@ def test_conv32_forward_matches_torch(shape):
     x = torch.randn(nx, np_, ny, 32, generator=g).to(torch.bfloat16)
     w = (0.1 * torch.randn(27, 32, 32, generator=g)).to(torch.bfloat16).float()
     b = 0.1 * torch.randn(32, generator=g)
-    want = _conv_ref(torch, x.float(), w, b)
+    want = _conv_ref(torch, x.float().cuda(), w, b).cpu()
     xd, wd, bd = x.cuda(), w.cuda(), b.cuda()
     y32 = torch.empty(nx, np_, ny, 32, device="cuda")
     _call(ss, xd, wd, bd, None, y32, shape, 1)
@@ -67,11 +96,10 @@ def test_conv32_forward_matches_torch(shape):
     assert (y16.cpu().float() - relu).abs().max().item() <= 2.0 ** -7 * scale
 
 
-def test_conv32_backward_data_matches_autograd():
+@pytest.mark.parametrize("shape", [(3, 128, 4), (24, 256, 12)], ids=["3x128x4", "24x256x12"])
+def test_conv32_backward_data_matches_autograd(shape):
     ss = _gpu()
     torch = _torch()
-    import torch.nn.functional as F
-    shape = (3, 128, 4)
     g = torch.Generator().manual_seed(5)
     nx, ny, np_ = shape
     up = torch.randn(nx, np_, ny, 32, generator=g).to(torch.bfloat16)      # dL/dy
@@ -94,7 +122,12 @@ def test_conv32_rejects_bad_shapes():
     w = torch.zeros(27, 32, 32, device="cuda")
     b = torch.zeros(32, device="cuda")
     with pytest.raises(ss.SsError):
-        _call(ss, x, w, b, None, torch.empty_like(x), (5, 5, 5), 0)
+        _raw(ss, x, w, b, None, torch.empty_like(x), (5, 5, 5), 0)
+    # an input that does not start on a 16-byte boundary (its bulk copies need one)
+    big = torch.zeros(2 * 128 * 2 * 32 + 1, device="cuda", dtype=torch.bfloat16)
+    y = torch.empty(2 * 128 * 2 * 32, device="cuda", dtype=torch.bfloat16)
+    with pytest.raises(ss.SsError):
+        _raw(ss, big[1:], w, b, None, y, (2, 128, 2), 0)
 
 
 # ---------------------------------------------------------------- the network
@@ -144,7 +177,8 @@ def test_denoiser_forward_matches_torch():
     dn.close()
 
 
-@pytest.mark.parametrize("shape,w", [((3, 128, 4), 0.0), ((3, 128, 8), 4.0)], ids=["mse", "mse_and_moment"])
+@pytest.mark.parametrize("shape,w", [((3, 128, 4), 0.0), ((3, 128, 8), 4.0), ((24, 256, 12), 0.0)],
+                         ids=["mse", "mse_and_moment", "mse_24x256x12"])
 def test_denoiser_gradients_match_torch(shape, w):
     """Parameter gradients and loss against torch autograd of the same
     network and loss: the mean-square error, and with the angular-moment term
