@@ -65,13 +65,14 @@ constexpr int kChunkBytes = kChunkRows * 16;       // 2176 B: the A operand's le
 constexpr int kBodyOff = 8 * 16;                   // byte offset of row y0 in a chunk
 constexpr int kLineBytes = 4 * kChunkBytes + 128;  // 8832 B
 constexpr int kBodyBytes = kTileM * 16;            // one chunk of 128 rows
-constexpr int kSlots = 18;                         // line buffers (a ring)
+constexpr int kPosSlots = 6;                       // position buffers of 3 lines (a ring)
+constexpr int kPosBytes = 3 * kLineBytes;
 constexpr int kAccStages = 8;                      // accumulators of 32 columns in tensor memory (a ring)
 constexpr int kConvThreads = 192;                  // warp 0 loads, warp 1 issues MMAs, warps 2-5 drain
 constexpr int kBarBytes = 512;
-constexpr int kSmemConv = 1024 + kBAll + kSlots * kLineBytes + kBarBytes + 16;  // + alignment slack
+constexpr int kSmemConv = 1024 + kBAll + kPosSlots * kPosBytes + kBarBytes + 16;  // + alignment slack
 static_assert(kSmemConv <= 227 * 1024, "the convolution's shared memory exceeds a CTA's limit");
-static_assert(8 * (2 * kSlots + 2 * kAccStages + 1) <= kBarBytes, "mbarriers do not fit");
+static_assert(8 * (2 * kPosSlots + 2 * kAccStages + 1) <= kBarBytes, "mbarriers do not fit");
 static_assert(kBAll % 16 == 0 && kLineBytes % 16 == 0 && kChunkBytes % 16 == 0, "bulk copies need 16-B alignment");
 constexpr uint32_t kWaitLimit = 1u << 22;    // mbarrier polls before giving up
 constexpr unsigned kErrTimeout = 1u;
@@ -178,35 +179,19 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(ncols) : "memory");
 }
 // D[tmem] (+)= A[smem] * B[smem]^T, kind::f16 (BF16 operands, FP32 accumulator),
-// issued by one elected lane of a converged warp; descriptors as (low, high)
-// 32-bit words
-__device__ __forceinline__ void mma_bf16_elect(uint32_t d_tmem, uint32_t alo, uint32_t ahi, uint32_t blo,
-                                               uint32_t bhi, uint32_t idesc, uint32_t accumulate) {
+// issued by the calling thread
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
     asm volatile(
-        "{\n .reg .pred p, e;\n .reg .b64 ad, bd;\n mov.b64 ad, {%1, %2};\n mov.b64 bd, {%3, %4};\n"
-        " setp.ne.b32 p, %6, 0;\n elect.sync _|e, 0xffffffff;\n"
-        " @e tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %5, p;\n}\n" ::"r"(d_tmem),
-        "r"(alo), "r"(ahi), "r"(blo), "r"(bhi), "r"(idesc), "r"(accumulate)
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
-// the same issued by the one calling thread
-__device__ __forceinline__ void mma_bf16_one(uint32_t d_tmem, uint32_t alo, uint32_t ahi, uint32_t blo, uint32_t bhi,
-                                             uint32_t idesc, uint32_t accumulate) {
-    asm volatile(
-        "{\n .reg .pred p;\n .reg .b64 ad, bd;\n mov.b64 ad, {%1, %2};\n mov.b64 bd, {%3, %4};\n"
-        " setp.ne.b32 p, %6, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %5, p;\n}\n" ::"r"(d_tmem),
-        "r"(alo), "r"(ahi), "r"(blo), "r"(bhi), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-__device__ __forceinline__ void mma_commit_one(uint32_t mbar) {
+// mbarrier arrival once the calling thread's MMAs issued so far have completed
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
                  : "memory");
-}
-__device__ __forceinline__ void mma_commit_elect(uint32_t mbar) {
-    asm volatile(
-        "{\n .reg .pred e;\n elect.sync _|e, 0xffffffff;\n"
-        " @e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}\n" ::"r"(mbar)
-        : "memory");
 }
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile(
@@ -224,11 +209,39 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 
 // instruction descriptor: D FP32, A and B BF16, both K-major, M = 128 (N in bits 17-22, in units of 8)
 constexpr uint32_t kIdescM128 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTileM >> 4) << 24);
-// Shared-memory matrix descriptors (K-major, no swizzle), as two 32-bit words:
-// low = start address >> 4 (bits 0-13) | leading (K chunk) offset >> 4 << 16;
-// high = stride (8-row group) offset >> 4 | version 1 at bit 46 (bit 14 of the high word).
-constexpr uint32_t kADescHiWord = (uint32_t)(128 >> 4) | (1u << 14);  // lines: 8-row groups 128 B apart
-constexpr uint32_t kBDescHiWord = (uint32_t)(512 >> 4) | (1u << 14);  // weights: 8-row groups 512 B apart
+// Shared-memory matrix descriptors (no swizzle): start address >> 4 in bits
+// 0-13, leading offset >> 4 in bits 16-29, stride offset >> 4 in bits 32-45,
+// version 1 in bit 46.  The convolution's operands are K-major: a line's K
+// chunks 2176 B apart and its 8-row groups 128 B apart; the weights' K chunks
+// 128 B apart and their 8-row groups 512 B apart.
+constexpr uint64_t kADesc = ((uint64_t)(kChunkBytes >> 4) << 16) | ((uint64_t)(128 >> 4) << 32) | (1ull << 46);
+constexpr uint64_t kBDesc = ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(512 >> 4) << 32) | (1ull << 46);
+// start-address offsets (>> 4) of the (dx, dy, K half) product (indices 0-2, 0-2, 0-1) within a
+// position buffer and within the packed weights
+__host__ __device__ constexpr uint64_t a_off(int dx, int dy, int kk) {
+    return (uint64_t)((dx * kLineBytes + kk * 2 * kChunkBytes + kBodyOff + (dy - 1) * 16) >> 4);
+}
+__host__ __device__ constexpr uint64_t b_off(int dx, int dy, int kk) {
+    return (uint64_t)(((dx * 9 + dy * 3) * kBTap + kk * 256) >> 4);
+}
+// one piece of a position's MMAs: the accumulator columns of consecutive tiles
+struct Piece {
+    uint32_t col;    // tensor-memory address of the first tile's accumulator
+    uint32_t idesc;  // instruction descriptor (N = 32 x tiles)
+    uint64_t boff;   // offset (>> 4) of the first tile's weight block within a triple
+    uint32_t acc;    // accumulate (0: the first product of the piece's tiles)
+};
+// the 17 (dx, dy, K half) products after the first, NP pieces each
+template <int NP>
+__device__ __forceinline__ void issue_rest(uint64_t adesc0, uint64_t bdesc0, const Piece *pp) {
+#pragma unroll
+    for (int t = 1; t < 18; ++t) {
+        const int dx = t / 6, dy = (t / 2) % 3, kk = t % 2;
+        const uint64_t a = adesc0 + a_off(dx, dy, kk), b = bdesc0 + b_off(dx, dy, kk);
+#pragma unroll
+        for (int k = 0; k < NP; ++k) mma_bf16(pp[k].col, a, b + pp[k].boff, pp[k].idesc, 1u);
+    }
+}
 
 // byte offset of element (row, k) of a K-major operand block in the core-matrix layout
 __host__ __device__ __forceinline__ int core_offset(int row, int k) {
@@ -244,21 +257,24 @@ __host__ __device__ __forceinline__ int core_offset(int row, int k) {
 // p + 1, p and p - 1 (dphi = -1, 0, +1), so one MMA of N = 96 covers all
 // three with the weights of the three dphi taps stacked along N (the packed
 // weights keep each (dx, dy) triple in the order dphi = +1, 0, -1): 18 MMAs
-// per input position instead of 54 of N = 32, and less than half the
-// shared-memory operand bytes.  The accumulators of consecutive tiles are
-// consecutive 32-column stages of a ring in tensor memory; an MMA is split
-// where the ring wraps, and where a tile takes its first product
-// (accumulate off).  Roles, synchronised through mbarriers with bounded
-// waits:
-//  - warp 0 (one thread) streams lines into a ring of kSlots buffers with
-//    bulk copies (cp.async.bulk): per line its 4 chunk bodies (2 KB each,
-//    contiguous in the activation layout) and its 8 halo pieces (16 B,
+// per input position instead of 54 of N = 32.  The accumulators of
+// consecutive tiles are consecutive 32-column stages of a ring in tensor
+// memory; an MMA is split where the ring wraps, and where a tile takes its
+// first product (accumulate off).  The tensor core takes an N = 96 MMA every
+// 56 cycles, so the issuing thread's loop is kept to a few instructions per
+// MMA: 64-bit descriptors plus compile-time offsets, and a branch-free path
+// for positions whose tiles lie in one piece of the ring.  Roles,
+// synchronised through mbarriers with bounded waits:
+//  - warp 0 streams positions into a ring of kPosSlots buffers of 3 lines
+//    with bulk copies (cp.async.bulk), 12 lanes at once (one bulk copy costs
+//    its issuing thread some 80 cycles): per line its 4 chunk bodies (2 KB
+//    each, contiguous in the activation layout) and its 8 halo pieces (16 B,
 //    periodic in y) straight into rows 7 and 136; full[slot] completes when
-//    the 8,320 bytes are in;
-//  - warp 1 (one thread) waits for a position's 3 lines and, when a tile
-//    starts, for its accumulator stage to be free; issues the MMAs; returns
-//    the lines to the producer (empty[slot]) and commits the tile that the
-//    position completed to acc_full[stage];
+//    the position's 24,960 bytes are in;
+//  - warp 1 (one thread) waits for the position and, when a tile starts,
+//    for its accumulator stage to be free; issues the MMAs; returns the
+//    position's buffer to the producer (empty[slot]) and commits the tile
+//    that the position completed to acc_full[stage];
 //  - warps 2-5 wait for acc_full, read the accumulator (warp w the tensor-
 //    memory lanes 32 (w mod 4) ..), release it to acc_empty and write the
 //    outputs, while the tensor core already runs the next positions.
@@ -273,20 +289,20 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 
     const uint32_t sB0 = (raw + 1023u) & ~1023u;
     uint8_t *const sB = smem_raw + (sB0 - raw);
     const uint32_t sL0 = sB0 + kBAll;
-    const uint32_t bar0 = sL0 + kSlots * kLineBytes;
+    const uint32_t bar0 = sL0 + kPosSlots * kPosBytes;
     auto full_bar = [&](uint32_t s) { return bar0 + 8u * s; };
-    auto empty_bar = [&](uint32_t s) { return bar0 + 8u * (kSlots + s); };
-    auto accf_bar = [&](uint32_t a) { return bar0 + 8u * (2 * kSlots + a); };
-    auto acce_bar = [&](uint32_t a) { return bar0 + 8u * (2 * kSlots + kAccStages + a); };
-    const uint32_t fin_bar = bar0 + 8u * (2 * kSlots + 2 * kAccStages);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(sB + kBAll + kSlots * kLineBytes + kBarBytes);
+    auto empty_bar = [&](uint32_t s) { return bar0 + 8u * (kPosSlots + s); };
+    auto accf_bar = [&](uint32_t a) { return bar0 + 8u * (2 * kPosSlots + a); };
+    auto acce_bar = [&](uint32_t a) { return bar0 + 8u * (2 * kPosSlots + kAccStages + a); };
+    const uint32_t fin_bar = bar0 + 8u * (2 * kPosSlots + 2 * kAccStages);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(sB + kBAll + kPosSlots * kPosBytes + kBarBytes);
     volatile int *sfail = reinterpret_cast<volatile int *>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     for (int i = tid; i < kBAll / 16; i += kConvThreads)
         reinterpret_cast<uint4 *>(sB)[i] = reinterpret_cast<const uint4 *>(Wpacked)[i];
     if (tid == 0) {
-        for (int s = 0; s < kSlots; ++s) {
+        for (int s = 0; s < kPosSlots; ++s) {
             mbar_init(full_bar(s), 1);  // the expect_tx arrival (+ the transactions)
             mbar_init(empty_bar(s), 1);
         }
@@ -318,144 +334,107 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 
     auto wrapi = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
 
     if (warp == 0) {
-        // ---- producer: the 3 lines of every input position of every run ----
-        if (lane == 0) {
-            uint32_t seq = 0;
-            bool ok = true;
-            for (int r0 = t0; r0 < t1 && ok;) {
-                int x, y0, pa;
-                decode(r0, x, y0, pa);
-                const int L = min(t1 - r0, d.np - pa);
-                const int ytop = wrapi(y0 - 1, d.ny), ybot = wrapi(y0 + kTileM, d.ny);
-                for (int j = 0; j < L + 2 && ok; ++j) {
-                    const int pin = wrapi(pa - 1 + j, d.np);
-                    for (int dx = -1; dx <= 1; ++dx, ++seq) {
-                        const uint32_t slot = seq % kSlots;
-                        if (seq >= (uint32_t)kSlots &&
-                            !mbar_wait_or_fail(empty_bar(slot), ((seq / kSlots) - 1u) & 1u, sfail)) {
-                            ok = false;
-                            break;
-                        }
-                        // chunk plane c of the line: ny rows of 16 B from X + (line 4 + c) ny 8
-                        const __nv_bfloat16 *plane = X + (size_t)(wrapi(x + dx, d.nx) * d.np + pin) * 4 * d.ny * 8;
-                        const uint32_t dst = sL0 + slot * (uint32_t)kLineBytes;
-                        mbar_expect_tx(full_bar(slot), 4u * (kBodyBytes + 32u));
-#pragma unroll
-                        for (int c = 0; c < 4; ++c) {
-                            const __nv_bfloat16 *pc = plane + (size_t)c * d.ny * 8;
-                            const uint32_t dc = dst + c * kChunkBytes + kBodyOff;
-                            bulk_load(dc, pc + (size_t)y0 * 8, kBodyBytes, full_bar(slot));
-                            bulk_load(dc - 16, pc + (size_t)ytop * 8, 16, full_bar(slot));
-                            bulk_load(dc + kBodyBytes, pc + (size_t)ybot * 8, 16, full_bar(slot));
-                        }
-                    }
-                }
-                r0 += L;
-            }
-            if (!ok) *sfail = 1;
-            // every load issued lands before the CTA may exit
-            for (uint32_t s = seq > (uint32_t)kSlots ? seq - kSlots : 0u; s < seq; ++s)
-                if (!mbar_wait(full_bar(s % kSlots), (s / kSlots) & 1u)) *sfail = 1;
-        }
-    } else if (warp == 1) {
-        // ---- MMA issuer: the whole warp walks the schedule, one elected lane issues ----
-        // Per input position the MMAs go to at most three pieces of the accumulator ring: a
-        // piece is (tensor-memory column, N, weight block offset, accumulate flag).  The
-        // plan is made once per position; the 18 (dx, dy, K half) products then cost one
-        // add per descriptor each, so the issue keeps pace with the tensor core.
-        uint32_t seq = 0;
-        int ibase = 0;  // the CTA's count of tiles before this run (accumulator stage = count mod kAccStages)
+        // ---- producer: the 3 lines of every input position of every run; lane 4 dx + c
+        // (12 lanes) copies chunk c of line dx: its body and its two halo rows ----
+        uint32_t pos = 0;  // the CTA's count of input positions
         bool ok = true;
         for (int r0 = t0; r0 < t1 && ok;) {
             int x, y0, pa;
             decode(r0, x, y0, pa);
             const int L = min(t1 - r0, d.np - pa);
-            for (int j = 0; j < L + 2; ++j, seq += 3) {
-                // the position's lines
-#pragma unroll
-                for (int dx = 0; dx < 3; ++dx) {
-                    const uint32_t q = seq + dx;
-                    if (ok) ok = mbar_wait_or_fail(full_bar(q % kSlots), (q / kSlots) & 1u, sfail);
-                }
-                // tile j starts at this position: its stage's previous tile has left it
-                const int inew = ibase + j;
-                if (ok && j < L && inew >= kAccStages)
-                    ok = mbar_wait_or_fail(acce_bar(inew % kAccStages), ((inew / kAccStages) - 1) & 1, sfail);
+            const int ytop = wrapi(y0 - 1, d.ny), ybot = wrapi(y0 + kTileM, d.ny);
+            for (int j = 0; j < L + 2; ++j, ++pos) {
+                const uint32_t slot = pos % kPosSlots;
+                if (pos >= (uint32_t)kPosSlots)
+                    ok = mbar_wait_or_fail(empty_bar(slot), ((pos / kPosSlots) - 1u) & 1u, sfail);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok) break;
-                tc_after_sync();
-                // plan: tiles lo..hi take this position's products; tile k's block in the weight
-                // triple is k - j + 2 (dphi = +1, 0, -1); pieces split where the stage ring wraps
-                const int lo = j - 2 > 0 ? j - 2 : 0, hi = j < L - 1 ? j : L - 1;
-                uint32_t pc[3], pn[3], pb[3];  // pieces of the plain plan: column, idesc, B offset >> 4
-                uint32_t qc[3], qn[3], qb[3], qa[3];  // the first product's plan (the new tile separate)
-                int np_ = 0, nq = 0;
-                auto split = [&](int klo, int khi, uint32_t *c, uint32_t *n, uint32_t *b, int &cnt) {
-                    if (klo > khi) return;
-                    const int s0 = (ibase + klo) & (kAccStages - 1), tot = khi - klo + 1;
-                    const int n1 = tot < kAccStages - s0 ? tot : kAccStages - s0;
-                    c[cnt] = tmem + (uint32_t)(32 * s0);
-                    n[cnt] = kIdescM128 | ((uint32_t)(4 * n1) << 17);
-                    b[cnt] = (uint32_t)((klo - j + 2) * (kBTap >> 4));
-                    ++cnt;
-                    if (n1 < tot) {
-                        c[cnt] = tmem;
-                        n[cnt] = kIdescM128 | ((uint32_t)(4 * (tot - n1)) << 17);
-                        b[cnt] = (uint32_t)((klo + n1 - j + 2) * (kBTap >> 4));
-                        ++cnt;
-                    }
-                };
-                split(lo, hi, pc, pn, pb, np_);
-                if (j < L) {
-                    qc[0] = tmem + (uint32_t)(32 * ((ibase + j) & (kAccStages - 1)));
-                    qn[0] = kIdescM128 | (4u << 17);
-                    qb[0] = (uint32_t)(2 * (kBTap >> 4));
-                    qa[0] = 0u;  // tile j's first product
-                    nq = 1;
-                    split(lo, j - 1, qc, qn, qb, nq);
-                    for (int k = 1; k < 3; ++k) qa[k] = 1u;
-                } else {
-                    for (int k = 0; k < 3; ++k) {
-                        qc[k] = pc[k];
-                        qn[k] = pn[k];
-                        qb[k] = pb[k];
-                        qa[k] = 1u;
-                    }
-                    nq = np_;
+                const int pin = wrapi(pa - 1 + j, d.np);
+                if (lane == 0) mbar_expect_tx(full_bar(slot), 3u * 4u * (kBodyBytes + 32u));
+                __syncwarp();
+                if (lane < 12) {
+                    const int dx = lane >> 2, c = lane & 3;
+                    // chunk plane c of the line: ny rows of 16 B from X + (line 4 + c) ny 8
+                    const __nv_bfloat16 *pc =
+                        X + ((size_t)(wrapi(x + dx - 1, d.nx) * d.np + pin) * 4 + c) * d.ny * 8;
+                    const uint32_t dc = sL0 + slot * (uint32_t)kPosBytes + (uint32_t)(dx * kLineBytes + c * kChunkBytes + kBodyOff);
+                    bulk_load(dc, pc + (size_t)y0 * 8, kBodyBytes, full_bar(slot));
+                    bulk_load(dc - 16, pc + (size_t)ytop * 8, 16, full_bar(slot));
+                    bulk_load(dc + kBodyBytes, pc + (size_t)ybot * 8, 16, full_bar(slot));
                 }
-                const uint32_t bdesc0 = ((sB0 >> 4) & 0x3FFFu) | ((uint32_t)(128 >> 4) << 16);
-#pragma unroll
-                for (int dx = 0; dx < 3; ++dx) {
-                    const uint32_t lb = sL0 + ((seq + dx) % kSlots) * (uint32_t)kLineBytes;
-                    const uint32_t adesc0 = (lb >> 4) | ((uint32_t)(kChunkBytes >> 4) << 16);
-#pragma unroll
-                    for (int dy = 0; dy < 3; ++dy)
-#pragma unroll
-                        for (int kk = 0; kk < 2; ++kk) {
-                            const uint32_t a = adesc0 + (uint32_t)((kk * 2 * kChunkBytes + kBodyOff + (dy - 1) * 16) >> 4);
-                            const uint32_t b = bdesc0 + (uint32_t)(((dx * 9 + dy * 3) * kBTap + kk * 256) >> 4);
-                            if (dx == 0 && dy == 0 && kk == 0) {
-#pragma unroll
-                                for (int k = 0; k < 3; ++k)
-                                    if (k < nq) mma_bf16_elect(qc[k], a, kADescHiWord, b + qb[k], kBDescHiWord, qn[k], qa[k]);
-                            } else {
-#pragma unroll
-                                for (int k = 0; k < 3; ++k)
-                                    if (k < np_) mma_bf16_elect(pc[k], a, kADescHiWord, b + pb[k], kBDescHiWord, pn[k], 1u);
-                            }
-                        }
-                }
-#pragma unroll
-                for (int dx = 0; dx < 3; ++dx) mma_commit_elect(empty_bar((seq + dx) % kSlots));
-                if (j >= 2) mma_commit_elect(accf_bar((ibase + j - 2) % kAccStages));  // tile j - 2 is complete
+                __syncwarp();
             }
-            ibase += L;
             r0 += L;
         }
         if (!ok && lane == 0) *sfail = 1;
-        // the MMAs issued complete before the tensor memory is freed
-        mma_commit_elect(fin_bar);
-        if (!mbar_wait(fin_bar, 0) && lane == 0) *sfail = 1;
+        // every load issued lands before the CTA may exit
+        if (lane == 0)
+            for (uint32_t q = pos > (uint32_t)kPosSlots ? pos - kPosSlots : 0u; q < pos; ++q)
+                if (!mbar_wait(full_bar(q % kPosSlots), (q / kPosSlots) & 1u)) *sfail = 1;
+    } else if (warp == 1) {
+        // ---- MMA issuer ----
+        if (lane == 0) {
+            uint32_t pos = 0;
+            int ibase = 0;  // the CTA's count of tiles before this run (accumulator stage = count mod kAccStages)
+            bool ok = true;
+            const uint64_t bdesc0 = kBDesc | (uint64_t)((sB0 >> 4) & 0x3FFFu);
+            for (int r0 = t0; r0 < t1 && ok;) {
+                int x, y0, pa;
+                decode(r0, x, y0, pa);
+                const int L = min(t1 - r0, d.np - pa);
+                for (int j = 0; j < L + 2; ++j, ++pos) {
+                    const uint32_t slot = pos % kPosSlots;
+                    ok = mbar_wait_or_fail(full_bar(slot), (pos / kPosSlots) & 1u, sfail);
+                    // tile j starts at this position: its stage's previous tile has left it
+                    const int inew = ibase + j;
+                    if (ok && j < L && inew >= kAccStages)
+                        ok = mbar_wait_or_fail(acce_bar(inew % kAccStages), ((inew / kAccStages) - 1) & 1, sfail);
+                    if (!ok) break;
+                    tc_after_sync();
+                    // plan: tiles lo..hi take this position's products; tile k's block in the weight
+                    // triple is k - j + 2 (dphi = +1, 0, -1); pieces split where the stage ring wraps
+                    const int lo = j - 2 > 0 ? j - 2 : 0, hi = j < L - 1 ? j : L - 1;
+                    Piece pp[2], pq[3];
+                    int np_ = 0, nq = 0;
+                    auto split = [&](int klo, int khi, Piece *pc, int &cnt) {
+                        if (klo > khi) return;
+                        const int s0 = (ibase + klo) & (kAccStages - 1), tot = khi - klo + 1;
+                        const int n1 = tot < kAccStages - s0 ? tot : kAccStages - s0;
+                        pc[cnt++] = Piece{tmem + (uint32_t)(32 * s0), kIdescM128 | ((uint32_t)(4 * n1) << 17),
+                                          (uint64_t)((klo - j + 2) * (kBTap >> 4)), 1u};
+                        if (n1 < tot)
+                            pc[cnt++] = Piece{tmem, kIdescM128 | ((uint32_t)(4 * (tot - n1)) << 17),
+                                              (uint64_t)((klo + n1 - j + 2) * (kBTap >> 4)), 1u};
+                    };
+                    split(lo, hi, pp, np_);
+                    if (j < L) {
+                        pq[0] = Piece{tmem + (uint32_t)(32 * ((ibase + j) & (kAccStages - 1))), kIdescM128 | (4u << 17),
+                                      (uint64_t)(2 * (kBTap >> 4)), 0u};  // tile j's first product
+                        nq = 1;
+                        split(lo, j - 1, pq, nq);
+                    } else {
+                        pq[0] = pp[0];
+                        pq[1] = pp[1];
+                        nq = np_;
+                    }
+                    const uint64_t adesc0 = kADesc | (uint64_t)(((sL0 + slot * (uint32_t)kPosBytes) >> 4) & 0x3FFFu);
+                    // the first (dx, dy, K half) product with the first-product plan, then the 17 others
+                    for (int k = 0; k < nq; ++k)
+                        mma_bf16(pq[k].col, adesc0 + a_off(0, 0, 0), bdesc0 + b_off(0, 0, 0) + pq[k].boff, pq[k].idesc,
+                                 pq[k].acc);
+                    if (np_ == 1) issue_rest<1>(adesc0, bdesc0, pp);
+                    else issue_rest<2>(adesc0, bdesc0, pp);
+                    mma_commit(empty_bar(slot));
+                    if (j >= 2) mma_commit(accf_bar((ibase + j - 2) % kAccStages));  // tile j - 2 is complete
+                }
+                ibase += L;
+                r0 += L;
+            }
+            if (!ok) *sfail = 1;
+            // the MMAs issued complete before the tensor memory is freed
+            mma_commit(fin_bar);
+            if (!mbar_wait(fin_bar, 0)) *sfail = 1;
+        }
         __syncwarp();
     } else if (warp >= 2) {
         // ---- epilogue ----
@@ -463,7 +442,8 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 
         int i = 0;
         for (int t = t0; t < t1; ++t, ++i) {
             const int a = i % kAccStages;
-            if (!mbar_wait_or_fail(accf_bar(a), (i / kAccStages) & 1, sfail)) {
+            // tcgen05.ld wants the whole warp: the lanes leave together
+            if (!__all_sync(0xffffffffu, mbar_wait_or_fail(accf_bar(a), (i / kAccStages) & 1, sfail))) {
                 *sfail = 1;
                 break;
             }
@@ -584,9 +564,9 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_dn_wgrad_tc(const __nv_bflo
     if (tid == 0) {
         for (int b = 0; b < 2; ++b) {
             mbar_init(full_bar(b), 1);
-            mbar_init(empty_bar(b), 1);
+            mbar_init(empty_bar(b), 2);  // both issuers' commits
         }
-        mbar_init(fin_bar, 1);
+        mbar_init(fin_bar, 2);
         *sfail = 0;
         fence_mbar_init();
     }
@@ -604,81 +584,88 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_dn_wgrad_tc(const __nv_bflo
     auto wrapi = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
 
     if (warp == 0) {
-        // ---- producer: per tile 9 lines (12 bulk copies each) and the tile's dZ (4) ----
-        if (lane == 0) {
-            bool ok = true;
-            int i = 0;
-            for (int t = t0; t < t1; ++t, ++i) {
-                const int b = i & 1;
-                if (i >= 2 && !mbar_wait_or_fail(empty_bar(b), ((i >> 1) - 1) & 1, sfail)) {
-                    ok = false;
-                    break;
-                }
-                const int p = t % d.np, y0 = ((t / d.np) % nseg) * kTileM, x = t / (d.np * nseg);
-                const int ytop = wrapi(y0 - 1, d.ny), ybot = wrapi(y0 + kTileM, d.ny);
-                mbar_expect_tx(full_bar(b), 9u * 4u * (kBodyBytes + 32u) + (uint32_t)kWgDzBytes);
-                for (int l = 0; l < 9; ++l) {
-                    const int dx = l / 3 - 1, dp = l % 3 - 1;
-                    const __nv_bfloat16 *plane =
-                        X + (size_t)(wrapi(x + dx, d.nx) * d.np + wrapi(p + dp, d.np)) * 4 * d.ny * 8;
-                    const uint32_t dst = sS0 + (uint32_t)((b * kWgBufSlots + l) * kWgSlotBytes);
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        const __nv_bfloat16 *pc = plane + (size_t)c * d.ny * 8;
-                        const uint32_t dc = dst + c * kChunkBytes + kBodyOff;
-                        bulk_load(dc, pc + (size_t)y0 * 8, kBodyBytes, full_bar(b));
-                        bulk_load(dc - 16, pc + (size_t)ytop * 8, 16, full_bar(b));
-                        bulk_load(dc + kBodyBytes, pc + (size_t)ybot * 8, 16, full_bar(b));
-                    }
-                }
-                const __nv_bfloat16 *zp = dZ + (size_t)(x * d.np + p) * 4 * d.ny * 8;
-#pragma unroll
-                for (int c = 0; c < 4; ++c)
-                    bulk_load(sZ0 + (uint32_t)(b * kWgDzBytes + c * kBodyBytes), zp + ((size_t)c * d.ny + y0) * 8,
-                              kBodyBytes, full_bar(b));
+        // ---- producer: per tile 9 lines (4 chunks: body + 2 halo rows each) and the tile's dZ;
+        // the 36 (line, chunk) pairs go to the 32 lanes in two passes ----
+        bool ok = true;
+        int i = 0;
+        for (int t = t0; t < t1; ++t, ++i) {
+            const int b = i & 1;
+            if (i >= 2) ok = mbar_wait_or_fail(empty_bar(b), ((i >> 1) - 1) & 1, sfail);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) break;
+            const int p = t % d.np, y0 = ((t / d.np) % nseg) * kTileM, x = t / (d.np * nseg);
+            const int ytop = wrapi(y0 - 1, d.ny), ybot = wrapi(y0 + kTileM, d.ny);
+            if (lane == 0) mbar_expect_tx(full_bar(b), 9u * 4u * (kBodyBytes + 32u) + (uint32_t)kWgDzBytes);
+            __syncwarp();
+            for (int e = lane; e < 36; e += 32) {
+                const int l = e >> 2, c = e & 3, dx = l / 3 - 1, dp = l % 3 - 1;
+                const __nv_bfloat16 *pc =
+                    X + ((size_t)(wrapi(x + dx, d.nx) * d.np + wrapi(p + dp, d.np)) * 4 + c) * d.ny * 8;
+                const uint32_t dc = sS0 + (uint32_t)((b * kWgBufSlots + l) * kWgSlotBytes + c * kChunkBytes + kBodyOff);
+                bulk_load(dc, pc + (size_t)y0 * 8, kBodyBytes, full_bar(b));
+                bulk_load(dc - 16, pc + (size_t)ytop * 8, 16, full_bar(b));
+                bulk_load(dc + kBodyBytes, pc + (size_t)ybot * 8, 16, full_bar(b));
             }
-            if (!ok) *sfail = 1;
-            // the loads issued land before the CTA may exit
+            if (lane >= 4 && lane < 8) {
+                const int c = lane - 4;
+                bulk_load(sZ0 + (uint32_t)(b * kWgDzBytes + c * kBodyBytes),
+                          dZ + (((size_t)(x * d.np + p) * 4 + c) * d.ny + y0) * 8, kBodyBytes, full_bar(b));
+            }
+            __syncwarp();
+        }
+        if (!ok && lane == 0) *sfail = 1;
+        // the loads issued land before the CTA may exit
+        if (lane == 0)
             for (int k = i > 2 ? i - 2 : 0; k < i; ++k)
                 if (!mbar_wait(full_bar(k & 1), (k >> 1) & 1)) *sfail = 1;
-        }
-    } else if (warp == 1) {
-        // ---- MMA issuer ----
-        if (lane == 0) {
-            constexpr uint32_t kAHi = (uint32_t)(kChunkBytes >> 4) | (1u << 14);  // M groups: the chunk stride
-            constexpr uint32_t kBHi = (uint32_t)(kBodyBytes >> 4) | (1u << 14);   // N groups: the dZ chunk stride
-            constexpr uint32_t kLbo = (uint32_t)(128 >> 4) << 16;                 // K groups: 8 voxels, 128 B
-            bool ok = true;
-            int i = 0;
-            for (int t = t0; t < t1; ++t, ++i) {
-                const int b = i & 1;
-                if (!mbar_wait_or_fail(full_bar(b), (i >> 1) & 1, sfail)) {
-                    ok = false;
-                    break;
-                }
-                tc_after_sync();
-                const uint32_t s0 = sS0 + (uint32_t)(b * kWgBufSlots * kWgSlotBytes), z0 = sZ0 + (uint32_t)(b * kWgDzBytes);
-#pragma unroll
-                for (int kk = 0; kk < kTileM / 16; ++kk) {
-                    const uint32_t bl = ((z0 + kk * 256) >> 4) | kLbo;
-                    const uint32_t acc = (i > 0 || kk > 0) ? 1u : 0u;
-#pragma unroll
-                    for (int dy = 0; dy < 3; ++dy)
-#pragma unroll
-                        for (int g = 0; g < 3; ++g) {
-                            const uint32_t al = ((s0 + g * 4 * kWgSlotBytes + kBodyOff + (16 * kk + dy - 1) * 16) >> 4) | kLbo;
-                            mma_bf16_one(tmem + (uint32_t)(32 * (dy * 3 + g)), al, kAHi, bl, kBHi, kIdescWg, acc);
-                        }
-                }
-                mma_commit_one(empty_bar(b));
+    } else if ((warp == 1 || warp == 2) && lane == 0) {
+        // ---- two MMA issuers: warp 1 the accumulators (dy, group) 0-4, warp 2 the accumulators 5-8;
+        // disjoint, so each accumulator's products keep one order ----
+        constexpr uint64_t kAWg = ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(kChunkBytes >> 4) << 32) | (1ull << 46);
+        constexpr uint64_t kBWg = ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(kBodyBytes >> 4) << 32) | (1ull << 46);
+        bool ok = true;
+        int i = 0;
+        for (int t = t0; t < t1; ++t, ++i) {
+            const int b = i & 1;
+            if (!mbar_wait_or_fail(full_bar(b), (i >> 1) & 1, sfail)) {
+                ok = false;
+                break;
             }
-            if (!ok) *sfail = 1;
-            mma_commit_one(fin_bar);
+            tc_after_sync();
+            const uint64_t a0 = kAWg | (uint64_t)(((sS0 + (uint32_t)(b * kWgBufSlots * kWgSlotBytes)) >> 4) & 0x3FFFu);
+            const uint64_t z0 = kBWg | (uint64_t)(((sZ0 + (uint32_t)(b * kWgDzBytes)) >> 4) & 0x3FFFu);
+            const uint32_t acc0 = i > 0 ? 1u : 0u;
+#pragma unroll
+            for (int kk = 0; kk < kTileM / 16; ++kk) {
+                const uint32_t acc = kk > 0 ? 1u : acc0;
+                const uint64_t bd = z0 + (uint64_t)(kk * 256 >> 4);
+                if (warp == 1) {
+#pragma unroll
+                    for (int a = 0; a < 5; ++a) {
+                        const int dy = a / 3, g = a % 3;
+                        mma_bf16(tmem + (uint32_t)(32 * a),
+                                 a0 + (uint64_t)((g * 4 * kWgSlotBytes + kBodyOff + (16 * kk + dy - 1) * 16) >> 4), bd,
+                                 kIdescWg, acc);
+                    }
+                } else {
+#pragma unroll
+                    for (int a = 5; a < 9; ++a) {
+                        const int dy = a / 3, g = a % 3;
+                        mma_bf16(tmem + (uint32_t)(32 * a),
+                                 a0 + (uint64_t)((g * 4 * kWgSlotBytes + kBodyOff + (16 * kk + dy - 1) * 16) >> 4), bd,
+                                 kIdescWg, acc);
+                    }
+                }
+            }
+            mma_commit(empty_bar(b));
         }
-        __syncwarp();
+        if (!ok) *sfail = 1;
+        mma_commit(fin_bar);
     }
     // ---- every thread: the accumulators leave once the MMAs are done ----
-    bool done = warp == 1 ? mbar_wait(fin_bar, 0) : mbar_wait_long(fin_bar, 0, sfail);
+    // (the issuers wait without the failure shortcut: their MMAs finish before the dealloc)
+    bool done = (warp == 1 || warp == 2) && lane == 0 ? mbar_wait(fin_bar, 0) : mbar_wait_long(fin_bar, 0, sfail);
+    done = __all_sync(0xffffffffu, done);  // tcgen05.ld wants the whole warp
     if (warp >= 2 && done && t1 > t0) {
         const int q = warp & 3;  // tensor-memory lanes 32 q ..: rows (line 4 g + q, ci = lane)
         tc_after_sync();
