@@ -168,10 +168,14 @@ def make_pairs(npairs, shape=(128, 128, 32), n_in=1_000_000, n_target=64_000_000
 
 def train(dn, X, T, epochs=1, batch=8, lr=1e-3, seed=0, val=None):
     """Adam over shuffled minibatches of (X, T); returns the per-epoch mean
-    training loss and, when val = (Xv, Tv) is given, the validation loss."""
+    training loss and, when val = (Xv, Tv) is given, the validation loss.
+    With a validation set the network ends with the parameters of the epoch
+    of lowest validation loss (marked "kept" in its record): the last epoch
+    of a short run at a fixed rate can land on a worse point."""
     import torch
     rng = np.random.default_rng(seed)
     hist = []
+    best = None
     n = X.shape[0]
     for _ in range(epochs):
         order = rng.permutation(n)
@@ -182,7 +186,12 @@ def train(dn, X, T, epochs=1, batch=8, lr=1e-3, seed=0, val=None):
         rec = {"train": float(np.mean(losses))}
         if val is not None:
             rec["val"] = dn.loss(val[0], val[1])
+            if best is None or rec["val"] < best[0]:
+                best = (rec["val"], len(hist), dn.params)
         hist.append(rec)
+    if best is not None:
+        dn.params = best[2]
+        hist[best[1]]["kept"] = True
     return hist
 
 
