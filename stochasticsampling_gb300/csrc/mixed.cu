@@ -264,15 +264,19 @@ __global__ void k_complex_to_real_f(const float2 *__restrict__ src, int count, f
 
 // NOISE: 0 Philox, 1 host array.  CANON (quasi2d only): z == 0 and
 // theta == pi/2 already hold, so they are neither read nor written.  FIX:
-// positions in 64-bit fixed point.
+// positions in 64-bit fixed point.  Two entry points: k_update_m (quasi-2-D)
+// and k_update_m3 (3-D), the latter held to 48 registers (5 blocks of 256
+// per SM, no spills): latency bound, it gains from the extra warps (update
+// 0.69 -> 0.61 ms on the 3-D workload), where the quasi-2-D forms lose 12 %
+// under any explicit minimum of blocks.
 template <bool Q2D, bool CANON, bool MAG, int NOISE, bool FIX>
-__global__ void __launch_bounds__(256) k_update_m(MixedParams M, double *__restrict__ x, double *__restrict__ y,
-                                                  double *__restrict__ z, float *__restrict__ phi,
-                                                  float *__restrict__ theta, uint32_t *__restrict__ key,
-                                                  const uint32_t *__restrict__ id, const float *__restrict__ table,
-                                                  const double *__restrict__ noise,
-                                                  const unsigned long long *__restrict__ d_step,
-                                                  uint32_t *__restrict__ counts_next) {
+__device__ __forceinline__ void update_m_body(const MixedParams &M, double *__restrict__ x, double *__restrict__ y,
+                                              double *__restrict__ z, float *__restrict__ phi,
+                                              float *__restrict__ theta, uint32_t *__restrict__ key,
+                                              const uint32_t *__restrict__ id, const float *__restrict__ table,
+                                              const double *__restrict__ noise,
+                                              const unsigned long long *__restrict__ d_step,
+                                              uint32_t *__restrict__ counts_next) {
     unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
     if (i >= M.n) return;
     const int ts = MAG ? TABLE_STRIDE_MAG : TABLE_STRIDE;
@@ -331,6 +335,20 @@ __global__ void __launch_bounds__(256) k_update_m(MixedParams M, double *__restr
     phi[i] = pph;
     if (!CANON) theta[i] = pth;
 }
+#define SS_UPDATE_M_ARGS                                                                                           \
+    MixedParams M, double *__restrict__ x, double *__restrict__ y, double *__restrict__ z, float *__restrict__ phi, \
+        float *__restrict__ theta, uint32_t *__restrict__ key, const uint32_t *__restrict__ id,                   \
+        const float *__restrict__ table, const double *__restrict__ noise,                                         \
+        const unsigned long long *__restrict__ d_step, uint32_t *__restrict__ counts_next
+template <bool CANON, bool MAG, int NOISE, bool FIX>
+__global__ void __launch_bounds__(256) k_update_m(SS_UPDATE_M_ARGS) {
+    update_m_body<true, CANON, MAG, NOISE, FIX>(M, x, y, z, phi, theta, key, id, table, noise, d_step, counts_next);
+}
+template <bool MAG, int NOISE, bool FIX>
+__global__ void __launch_bounds__(256, 5) k_update_m3(SS_UPDATE_M_ARGS) {
+    update_m_body<false, false, MAG, NOISE, FIX>(M, x, y, z, phi, theta, key, id, table, noise, d_step, counts_next);
+}
+#undef SS_UPDATE_M_ARGS
 
 template <bool Q2D>
 __global__ void k_noise_m(MixedParams M, unsigned long long t, double *__restrict__ out) {
@@ -414,24 +432,27 @@ void launch_update_m(cudaStream_t s, bool fixed, bool q2d, bool canon, bool mag,
                      const double *noise, const unsigned long long *d_step, uint32_t *counts_next) {
     if (!M.n) return;
     unsigned b = nb(M.n, 256);
-#define SS_UPDM(Q, C, G, N)                                                                                 \
+#define SS_UPDM(K, ...)                                                                                     \
     do {                                                                                                    \
         if (fixed)                                                                                          \
-            k_update_m<Q, C, G, N, true><<<b, 256, 0, s>>>(M, xs[0], xs[1], xs[2], as[0], as[1], key, id,   \
-                                                           table, noise, d_step, counts_next);              \
+            K<__VA_ARGS__, true><<<b, 256, 0, s>>>(M, xs[0], xs[1], xs[2], as[0], as[1], key, id, table,   \
+                                                   noise, d_step, counts_next);                             \
         else                                                                                                \
-            k_update_m<Q, C, G, N, false><<<b, 256, 0, s>>>(M, xs[0], xs[1], xs[2], as[0], as[1], key, id,  \
-                                                            table, noise, d_step, counts_next);             \
+            K<__VA_ARGS__, false><<<b, 256, 0, s>>>(M, xs[0], xs[1], xs[2], as[0], as[1], key, id, table,  \
+                                                    noise, d_step, counts_next);                            \
     } while (0)
-#define SS_UPDM_N(Q, C, G) \
-    do { if (host_noise) SS_UPDM(Q, C, G, 1); else SS_UPDM(Q, C, G, 0); } while (0)
+#define SS_UPDM2(C, G) \
+    do { if (host_noise) SS_UPDM(k_update_m, C, G, 1); else SS_UPDM(k_update_m, C, G, 0); } while (0)
+#define SS_UPDM3(G) \
+    do { if (host_noise) SS_UPDM(k_update_m3, G, 1); else SS_UPDM(k_update_m3, G, 0); } while (0)
     if (q2d) {
-        if (canon) { if (mag) SS_UPDM_N(true, true, true); else SS_UPDM_N(true, true, false); }
-        else { if (mag) SS_UPDM_N(true, false, true); else SS_UPDM_N(true, false, false); }
+        if (canon) { if (mag) SS_UPDM2(true, true); else SS_UPDM2(true, false); }
+        else { if (mag) SS_UPDM2(false, true); else SS_UPDM2(false, false); }
     } else {
-        if (mag) SS_UPDM_N(false, false, true); else SS_UPDM_N(false, false, false);
+        if (mag) SS_UPDM3(true); else SS_UPDM3(false);
     }
-#undef SS_UPDM_N
+#undef SS_UPDM3
+#undef SS_UPDM2
 #undef SS_UPDM
 }
 void launch_noise_m(cudaStream_t s, bool q2d, const MixedParams &M, unsigned long long t, double *out) {
