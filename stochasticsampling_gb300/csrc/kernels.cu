@@ -596,10 +596,13 @@ __device__ __forceinline__ void langevin_full_f2(const DevParams &P, double &px,
 // gather): the chain of langevin_canon, and z and theta are neither read nor
 // written.  F2 (with CANON): the same chain's increments in two-float
 // arithmetic (f32x2.cuh) from the float-pair table row, added to the FP64
-// state in FP64.
+// state in FP64.  Register budgets of the F2 forms (launch bounds): 5 blocks
+// of 256 per SM for the canonical chain, 4 for the 3-D chain (64 registers,
+// a few words spilled; 2.02 -> 1.94 ms on the 3-D workload against 3
+// blocks), 3 for the quasi-2-D general chain.
 // ------------------------------------------------------------------------
 template <bool Q2D, bool MAG, int NOISE, bool TRI, bool CANON = false, bool F2 = false>
-__global__ void __launch_bounds__(256, F2 ? (CANON ? 5 : 3) : 1) k_update(DevParams P, double *__restrict__ x, double *__restrict__ y,
+__global__ void __launch_bounds__(256, F2 ? (CANON ? 5 : (Q2D ? 3 : 4)) : 1) k_update(DevParams P, double *__restrict__ x, double *__restrict__ y,
                                                 double *__restrict__ z, double *__restrict__ phi,
                                                 double *__restrict__ theta, uint32_t *__restrict__ key,
                                                 const uint32_t *__restrict__ id, const double *__restrict__ table,
