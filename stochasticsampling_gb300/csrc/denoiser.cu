@@ -141,6 +141,16 @@ __device__ __forceinline__ bool mbar_wait_or_fail(uint32_t addr, uint32_t parity
     }
     return false;
 }
+// a wait of a role off the MMA thread's critical path: polls with a short pause so
+// that it takes few issue slots from the warps it shares a scheduler with
+__device__ __forceinline__ bool mbar_wait_polite(uint32_t addr, uint32_t parity, const volatile int *fail) {
+    for (uint32_t i = 0; i < kWaitLimit; ++i) {
+        if (mbar_try_wait(addr, parity)) return true;
+        if ((i & 15u) == 15u && *fail) return false;
+        __nanosleep(64);
+    }
+    return false;
+}
 // a long wait (the whole kernel): polls with a 256 ns pause, giving up after ~1 s or
 // once another role of the CTA has failed
 __device__ __forceinline__ bool mbar_wait_long(uint32_t addr, uint32_t parity, const volatile int *fail) {
@@ -346,7 +356,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 
             for (int j = 0; j < L + 2; ++j, ++pos) {
                 const uint32_t slot = pos % kPosSlots;
                 if (pos >= (uint32_t)kPosSlots)
-                    ok = mbar_wait_or_fail(empty_bar(slot), ((pos / kPosSlots) - 1u) & 1u, sfail);
+                    ok = mbar_wait_polite(empty_bar(slot), ((pos / kPosSlots) - 1u) & 1u, sfail);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok) break;
                 const int pin = wrapi(pa - 1 + j, d.np);
@@ -443,7 +453,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 
         for (int t = t0; t < t1; ++t, ++i) {
             const int a = i % kAccStages;
             // tcgen05.ld wants the whole warp: the lanes leave together
-            if (!__all_sync(0xffffffffu, mbar_wait_or_fail(accf_bar(a), (i / kAccStages) & 1, sfail))) {
+            if (!__all_sync(0xffffffffu, mbar_wait_polite(accf_bar(a), (i / kAccStages) & 1, sfail))) {
                 *sfail = 1;
                 break;
             }
