@@ -125,7 +125,10 @@ def peaks():
 
 
 class Clocks:
-    """nvidia-smi clock sampling during the timed region."""
+    """nvidia-smi clock sampling (every 20 ms) during the timed region: start()
+    before the warm-up, mark() just before the timed region begins; stop()
+    summarises the samples taken from the mark on (the last one before it
+    when the region is shorter than one sampling interval)."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -137,18 +140,27 @@ class Clocks:
         self.gpu = gpu_index
 
     def start(self):
+        """Starts the sampler and returns once its first sample has arrived (at
+        most 3 s), so that nvidia-smi's own start-up stays out of the timed
+        region that follows."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3.0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
 
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    def mark(self):
+        self.first = len(self.lines)
 
     def stop(self):
         if self.proc is None:
@@ -160,7 +172,9 @@ class Clocks:
             self.proc.kill()
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        first = getattr(self, "first", 0)
+        lines = self.lines[first:] if len(self.lines) > first else self.lines[max(0, first - 1):]
+        for line in lines:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -723,13 +737,14 @@ def run_gpu(args, rank, world, dist):
     sim.init(p0)
 
     with torch.cuda.stream(stream):
+        clocks = Clocks(local)
+        clocks.start()  # (its start-up stays ahead of the warm-up)
         sim.run(args.warmup)
         torch.cuda.synchronize()
         barrier()
         torch.cuda.synchronize()
         l0 = sim.launch_count()
-        clocks = Clocks(local)
-        clocks.start()
+        clocks.mark()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         sim.run(args.steps)
