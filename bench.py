@@ -899,7 +899,7 @@ def main():
     ap.add_argument("--no-denoise", action="store_true", help="skip the learned-denoiser measurement")
     ap.add_argument("--no-c2", action="store_true", help="skip the 3-D magnetic measurement")
     ap.add_argument("--denoise-pairs", type=int, default=1000)
-    ap.add_argument("--denoise-epochs", type=int, default=3)
+    ap.add_argument("--denoise-epochs", type=int, default=6)
     ap.add_argument("--denoise-steps", type=int, default=400)
     ap.add_argument("--only", choices=["mixed", "fixed64", "ensemble", "denoised", "c2", "f32x2", "c0"], default=None,
                     help="run one section alone (a smaller command for profiling); prints its JSON")
