@@ -200,6 +200,17 @@ typedef struct {
 int ss_langevin(const double *particles, uint64_t n, uint32_t mask, const ss_langevin_args *args,
                 double *out);
 
+/* Counting-sort the particles by cell before the update of every
+ * every_steps-th step (0: never, the default).  The FP32 paths and 3-D FP64
+ * contexts sort their rows by cell once, at ingest; particles drift away from
+ * that order over long runs (on the 3-D workload the FP32 update is 10 %
+ * slower after 3,000 steps), which a re-sort every few hundred steps undoes.
+ * A context made without SS_FLAG_NO_SORT already sorts every step.  No
+ * result changes: the particles keep their caller order on every read-back.
+ * Allocates the second particle buffer set on first use.  The stage is timed
+ * as stage 6 (sort). */
+int ss_set_resort(ss_ctx *ctx, uint32_t every_steps);
+
 /* Per-stage timing (CUDA events on the context stream).  enable != 0 starts
  * recording; ss_profile_read fills ms[SS_NUM_STAGES] with the summed time of
  * each stage since enabling and count with the number of steps. */

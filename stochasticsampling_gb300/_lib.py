@@ -15,7 +15,7 @@ EXPORTS = [
     "ss_synchronize",
     "ss_get_particles", "ss_get_distribution", "ss_get_counts", "ss_get_flow_field", "ss_get_magnetic_field",
     "ss_get_flow_complex", "ss_get_magnetic_complex", "ss_get_timestep", "ss_mean_flow_field",
-    "ss_mean_magnetic_field", "ss_langevin", "ss_profile_enable", "ss_profile_read", "ss_launch_count",
+    "ss_mean_magnetic_field", "ss_langevin", "ss_set_resort", "ss_profile_enable", "ss_profile_read", "ss_launch_count",
     "ss_sample_distribution_noalloc", "ss_ensemble_create", "ss_ensemble_destroy", "ss_ensemble_init",
     "ss_ensemble_autotune", "ss_ensemble_set_config", "ss_ensemble_run", "ss_ensemble_synchronize", "ss_ensemble_get_particles",
     "ss_ensemble_get_counts", "ss_ensemble_get_flow_field", "ss_ensemble_info", "ss_dn_conv32", "ss_dn_create",
@@ -124,6 +124,7 @@ def load(build_if_missing=True):
         "ss_mean_flow_field": [vp, ctypes.c_double, dp, dp, dp],
         "ss_mean_magnetic_field": [vp, dp, dp, dp],
         "ss_langevin": [dp, u64, u32, ctypes.POINTER(LangevinArgs), dp],
+        "ss_set_resort": [vp, u32],
         "ss_profile_enable": [vp, ci],
         "ss_profile_read": [vp, dp, u64p],
         "ss_launch_count": [vp, u64p],

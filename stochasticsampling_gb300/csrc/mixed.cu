@@ -11,6 +11,7 @@
 //
 // Layout: particles x, y, z f64 SoA + phi, theta f32 SoA (+ key, id as in the
 // FP64 path); spectra float2; table rows of 16 (32 with dipolar terms) floats.
+#include "kernels.cuh"
 #include "mixed.cuh"
 #include "mixed_device.cuh"
 
@@ -361,6 +362,51 @@ __global__ void k_noise_m(MixedParams M, unsigned long long t, double *__restric
     if (r[3] < 0.0) r[3] += kTwoPi;
 }
 
+// ---- periodic re-sort of the resident particles by cell ------------------
+// Rows sorted by cell at ingest keep the particles of a cell together for
+// many steps, but they drift (on the 3-D workload the update is 10 % slower
+// after 3,000 steps).  A counting sort on the cell keys the update wrote:
+// the particles per cell (warp-aggregated atomics), an exclusive scan, and a
+// scatter of every row into the other buffer set at cursor[key] + its rank.
+// The order within a cell follows the atomics, which changes no result: the
+// noise is keyed by the particle's caller index, the histogram is integer
+// counts, and the rows go back to the caller by that index.
+__global__ void k_count_keys(const uint32_t *__restrict__ key, unsigned long long n, uint32_t *__restrict__ cellcount) {
+    const unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = key[i];
+    const unsigned same = __match_any_sync(__activemask(), k);
+    if ((int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(cellcount + k, (uint32_t)__popc(same));
+}
+// positions as 64-bit words (FP64 or fixed point alike), angles FP32
+__global__ void __launch_bounds__(256) k_scatter_m(unsigned long long n, const unsigned long long *__restrict__ x,
+                                                   const unsigned long long *__restrict__ y,
+                                                   const unsigned long long *__restrict__ z,
+                                                   const float *__restrict__ phi, const float *__restrict__ theta,
+                                                   const uint32_t *__restrict__ key, const uint32_t *__restrict__ id,
+                                                   unsigned long long *__restrict__ x2, unsigned long long *__restrict__ y2,
+                                                   unsigned long long *__restrict__ z2, float *__restrict__ phi2,
+                                                   float *__restrict__ theta2, uint32_t *__restrict__ key2,
+                                                   uint32_t *__restrict__ id2, uint32_t *__restrict__ cursor) {
+    const unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int lane = threadIdx.x & 31;
+    const uint32_t k = key[i];
+    const unsigned same = __match_any_sync(__activemask(), k);
+    const int leader = __ffs(same) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(cursor + k, (uint32_t)__popc(same));
+    base = __shfl_sync(same, base, leader);
+    const uint32_t dst = base + (uint32_t)__popc(same & ((1u << lane) - 1u));
+    x2[dst] = x[i];
+    y2[dst] = y[i];
+    z2[dst] = z[i];
+    phi2[dst] = phi[i];
+    theta2[dst] = theta[i];
+    key2[dst] = k;
+    id2[dst] = id[i];
+}
+
 // ========================================================================
 static inline unsigned nb(unsigned long long n, unsigned bs) { return (unsigned)((n + bs - 1) / bs); }
 
@@ -454,6 +500,17 @@ void launch_update_m(cudaStream_t s, bool fixed, bool q2d, bool canon, bool mag,
 #undef SS_UPDM3
 #undef SS_UPDM2
 #undef SS_UPDM
+}
+void launch_resort_m(cudaStream_t s, const MixedParams &M, double *const xs[3], float *const as[2], const uint32_t *key,
+                     const uint32_t *id, double *const xd[3], float *const ad[2], uint32_t *keyd, uint32_t *idd,
+                     uint32_t *cellcount, uint32_t *cursor) {
+    if (!M.n) return;
+    launch_zero_u32(s, cellcount, M.ncell);
+    k_count_keys<<<nb(M.n, 256), 256, 0, s>>>(key, M.n, cellcount);
+    launch_scan(s, cellcount, M.ncell, cursor);
+    auto w = [](double *p) { return reinterpret_cast<unsigned long long *>(p); };
+    k_scatter_m<<<nb(M.n, 256), 256, 0, s>>>(M.n, w(xs[0]), w(xs[1]), w(xs[2]), as[0], as[1], key, id, w(xd[0]),
+                                              w(xd[1]), w(xd[2]), ad[0], ad[1], keyd, idd, cursor);
 }
 void launch_noise_m(cudaStream_t s, bool q2d, const MixedParams &M, unsigned long long t, double *out) {
     if (!M.n) return;

@@ -71,6 +71,10 @@ void launch_widen_m(cudaStream_t s, const float *re, const float *im, long long 
                     int m1, const double *sums, double2 *dst);
 void launch_real_to_complex_f(cudaStream_t s, const float *src, int count, int sstride, float2 *dst);
 void launch_complex_to_real_f(cudaStream_t s, const float2 *src, int count, float *dst);
+// counting sort of the resident particles by their cell keys into the other buffer set (4 launches)
+void launch_resort_m(cudaStream_t s, const MixedParams &M, double *const xs[3], float *const as[2], const uint32_t *key,
+                     const uint32_t *id, double *const xd[3], float *const ad[2], uint32_t *keyd, uint32_t *idd,
+                     uint32_t *cellcount, uint32_t *cursor);
 void launch_update_m(cudaStream_t s, bool fixed, bool q2d, bool canon, bool mag, bool host_noise, const MixedParams &M,
                      double *const xs[3], float *const as[2], uint32_t *key, const uint32_t *id, const float *table,
                      const double *noise, const unsigned long long *d_step, uint32_t *counts_next);

@@ -57,6 +57,8 @@ struct ss_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     bool q2d = false, mag_step = false, sort = true, use_graph = true;
+    uint32_t resort_every = 0;  // re-sort by cell every this many steps (0: never; ss_set_resort)
+    uint64_t launches_graph[2] = {};  // kernel launches of a captured step without / with the re-sort
     bool initialized = false;
     uint64_t timestep = 0;
     int pcur = 0, ccur = 0, dist_idx = 0;
@@ -114,7 +116,7 @@ struct ss_ctx {
     int fft_rank = 0;
     int fft_n[3] = {1, 1, 1};
 
-    cudaGraphExec_t graph[2][2] = {};
+    cudaGraphExec_t graph[2][2][2] = {};  // [particle buffer][histogram][the step re-sorts]
     // ss_step_host: a copy stream and one event per chunk of the read-back
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t chunk_ev[kHostChunks + 1] = {};
@@ -386,7 +388,11 @@ static int enqueue_solve(ss_ctx *c, bool flow, bool mag, const uint32_t *counts,
 
 // The mixed-precision field solve (mixed.cu): FP32 contraction with FP64
 // component sums, means removed in FP64, C2C FP32 transforms, FP32 k space.
-static int enqueue_solve_m(ss_ctx *c, bool flow, bool mag, const uint32_t *counts, double screening, uint64_t *nl) {
+// sort_pcur >= 0: the step also re-sorts the particles of buffer set
+// sort_pcur into the other set (between the contraction and the transforms,
+// where the per-stage timing puts the FP64 path's sort)
+static int enqueue_solve_m(ss_ctx *c, bool flow, bool mag, const uint32_t *counts, double screening, uint64_t *nl,
+                           int sort_pcur = -1) {
     const int ts = c->mag_step ? TABLE_STRIDE_MAG : TABLE_STRIDE;
     const int nc = c->P.ncell;
     mark(c, 0);
@@ -408,6 +414,13 @@ static int enqueue_solve_m(ss_ctx *c, bool flow, bool mag, const uint32_t *count
     *nl += 1 + (flow ? 1 : 0) + (mag ? 1 : 0);
     CKR(check_launch(c, "contract (mixed)"));
     mark(c, 6);
+    if (sort_pcur >= 0) {
+        const int a = sort_pcur, b = 1 - sort_pcur;
+        launch_resort_m(c->stream, c->M, c->px[a], c->pa[a], c->key[a], c->pid[a], c->px[b], c->pa[b], c->key[b],
+                        c->pid[b], c->cellcount, c->cursor);
+        *nl += 4;
+        CKR(check_launch(c, "re-sort (mixed)"));
+    }
     mark(c, 1);
     const long long nh = c->P.nhalf;
     if (flow && mag) CKR(fft_r2c_f(c, c->fr_f, c->fwd_f, 12));
@@ -433,12 +446,13 @@ static int enqueue_solve_m(ss_ctx *c, bool flow, bool mag, const uint32_t *count
     return SS_OK;
 }
 
-static int enqueue_step_m(ss_ctx *c, int pcur, int ccur, bool host_noise, uint64_t *nl) {
-    CKR(enqueue_solve_m(c, true, c->mag_step, c->counts[ccur], c->prm.hydro_screening, nl));
+static int enqueue_step_m(ss_ctx *c, int pcur, int ccur, bool host_noise, bool sort_now, uint64_t *nl) {
+    CKR(enqueue_solve_m(c, true, c->mag_step, c->counts[ccur], c->prm.hydro_screening, nl, sort_now ? pcur : -1));
+    const int p = sort_now ? 1 - pcur : pcur;
     mark(c, 5);
     launch_zero_u32(c->stream, c->counts[1 - ccur], c->P.nbins);
-    launch_update_m(c->stream, c->fixed, c->q2d, c->canon, c->mag_step, host_noise, c->M, c->px[pcur], c->pa[pcur],
-                    c->key[pcur], c->pid[pcur], c->table_f, c->noise_dev, c->d_step, c->counts[1 - ccur]);
+    launch_update_m(c->stream, c->fixed, c->q2d, c->canon, c->mag_step, host_noise, c->M, c->px[p], c->pa[p],
+                    c->key[p], c->pid[p], c->table_f, c->noise_dev, c->d_step, c->counts[1 - ccur]);
     launch_step_inc(c->stream, c->d_step);
     *nl += 3;
     CKR(check_launch(c, "update (mixed)"));
@@ -447,9 +461,8 @@ static int enqueue_step_m(ss_ctx *c, int pcur, int ccur, bool host_noise, uint64
 }
 
 // One do_timestep for the state (pcur, ccur); does not touch host-side state.
-static int enqueue_step(ss_ctx *c, int pcur, int ccur, bool host_noise, uint64_t *nl) {
-    if (c->mixed) return enqueue_step_m(c, pcur, ccur, host_noise, nl);
-    const bool sort_now = c->sort;
+static int enqueue_step(ss_ctx *c, int pcur, int ccur, bool host_noise, bool sort_now, uint64_t *nl) {
+    if (c->mixed) return enqueue_step_m(c, pcur, ccur, host_noise, sort_now, nl);
     CKR(enqueue_solve(c, true, c->mag_step, c->counts[ccur], nullptr, c->prm.hydro_screening, pcur, sort_now, nl));
     const int p = sort_now ? 1 - pcur : pcur;
     mark(c, 5);
@@ -492,36 +505,47 @@ static void accumulate_timing(ss_ctx *c) {
     c->timing.steps += 1;
 }
 
+// whether this step counting-sorts the particles by cell before its update:
+// every step for an FP64 context made with sorting, and every resort_every-th
+// step (ss_set_resort) for the others
+static bool sorts_now(const ss_ctx *c) {
+    if (c->sort) return true;
+    return c->resort_every > 0 && (c->timestep + 1) % c->resort_every == 0;
+}
+
 static int direct_step(ss_ctx *c, bool host_noise) {
     uint64_t nl = 0;
-    CKR(enqueue_step(c, c->pcur, c->ccur, host_noise, &nl));
+    const bool sort_now = sorts_now(c);
+    CKR(enqueue_step(c, c->pcur, c->ccur, host_noise, sort_now, &nl));
     c->launches += nl;
     c->launches_per_step = nl;
     accumulate_timing(c);
-    advance(c, c->sort);
+    advance(c, sort_now);
     return SS_OK;
 }
 
 static int graph_step(ss_ctx *c) {
     // the step after non-canonical quasi2d rows runs directly (graphs hold the canonical update)
     if (c->q2d && !c->canon) return direct_step(c, false);
-    cudaGraphExec_t &g = c->graph[c->pcur][c->ccur];
+    const bool sort_now = sorts_now(c);
+    cudaGraphExec_t &g = c->graph[c->pcur][c->ccur][sort_now];
     if (!g) {
         cudaGraph_t graph;
         uint64_t nl = 0;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = enqueue_step(c, c->pcur, c->ccur, false, &nl);
+        int rc = enqueue_step(c, c->pcur, c->ccur, false, sort_now, &nl);
         cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
         if (rc != SS_OK) return rc;
         if (e != cudaSuccess) return fail(c, SS_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
         e = cudaGraphInstantiate(&g, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) return fail(c, SS_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
-        c->launches_per_step = nl;
+        c->launches_graph[sort_now] = nl;
     }
     CK(cudaGraphLaunch(g, c->stream));
+    c->launches_per_step = c->launches_graph[sort_now];
     c->launches += c->launches_per_step;
-    advance(c, c->sort);
+    advance(c, sort_now);
     return SS_OK;
 }
 
@@ -563,9 +587,10 @@ static void destroy_impl(ss_ctx *c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto &kv : c->plans) cufftDestroy(kv.second);
-    for (int a = 0; a < 2; ++a)
-        for (int b = 0; b < 2; ++b)
-            if (c->graph[a][b]) cudaGraphExecDestroy(c->graph[a][b]);
+    for (auto &ga : c->graph)
+        for (auto &gb : ga)
+            for (auto &g : gb)
+                if (g) cudaGraphExecDestroy(g);
     for (int b = 0; b < 2; ++b) {
         for (int k = 0; k < 5; ++k) cudaFree(c->px[b][k]);
         cudaFree(c->key[b]);
@@ -1086,12 +1111,13 @@ int ss_set_denoiser(ss_ctx *c, ss_dn *dn) {
     }
     c->dn = dn;
     // the captured steps change: recapture on the next step
-    for (int a = 0; a < 2; ++a)
-        for (int b = 0; b < 2; ++b)
-            if (c->graph[a][b]) {
-                cudaGraphExecDestroy(c->graph[a][b]);
-                c->graph[a][b] = nullptr;
-            }
+    for (auto &ga : c->graph)
+        for (auto &gb : ga)
+            for (auto &g : gb)
+                if (g) {
+                    cudaGraphExecDestroy(g);
+                    g = nullptr;
+                }
     return SS_OK;
 }
 
@@ -1434,6 +1460,28 @@ int ss_langevin(const double *particles, uint64_t n, uint32_t mask, const ss_lan
     cudaFree(d_out);
     cudaFree(d_args);
     if (e != cudaSuccess) return fail(nullptr, SS_ERR_CUDA, "ss_langevin: %s", cudaGetErrorString(e));
+    return SS_OK;
+}
+
+int ss_set_resort(ss_ctx *c, uint32_t every_steps) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    CK(cudaSetDevice(c->device));
+    if (every_steps > 0) {
+        // the re-sort writes into the second particle buffer set, which a context made without
+        // the per-step sort has not allocated; each missing buffer on its own
+        const size_t N = (size_t)c->P.n;
+        const int nd = c->mixed ? 3 : 5;
+        for (int b = 0; b < 2; ++b) {
+            for (int k = 0; k < nd; ++k)
+                if (!c->px[b][k]) CK(cudaMalloc((void **)&c->px[b][k], (N ? N : 1) * sizeof(double)));
+            for (int k = 0; c->mixed && k < 2; ++k)
+                if (!c->pa[b][k]) CK(cudaMalloc((void **)&c->pa[b][k], (N ? N : 1) * sizeof(float)));
+            if (!c->key[b]) CK(cudaMalloc((void **)&c->key[b], (N ? N : 1) * sizeof(uint32_t)));
+            if (!c->pid[b]) CK(cudaMalloc((void **)&c->pid[b], (N ? N : 1) * sizeof(uint32_t)));
+        }
+        if (!c->cursor) CK(cudaMalloc((void **)&c->cursor, (size_t)c->P.ncell * sizeof(uint32_t)));
+    }
+    c->resort_every = every_steps;
     return SS_OK;
 }
 

@@ -260,6 +260,11 @@ class Simulation:
         return b, g
 
     # --- instrumentation --------------------------------------------------
+    def set_resort(self, every_steps):
+        """Counting-sort the particles by cell every every_steps steps (0: never);
+        no result changes (ss_set_resort)."""
+        self._check(self.lib.ss_set_resort(self._h, int(every_steps)))
+
     def profile(self, enable=True):
         self._check(self.lib.ss_profile_enable(self._h, 1 if enable else 0))
 
