@@ -96,47 +96,46 @@ struct DevParams {
 // modulo, src/particle.rs:26-35.  fmod(x, m) is exact; for x in (-m, 2m) it
 // equals x, x - m (exact by Sterbenz) or x (then + m), so the fast path gives
 // the identical double without the fmod loop.
-// Doubles as ordered 64-bit integers: sign-magnitude mapped to two's
-// complement, so key(a) < key(b) <=> a < b for non-NaN a, b, and
-// key(-0.0) == key(+0.0).  (Compares on the integer pipe; see d2f_pos.)
-__device__ __forceinline__ long long dkey(double d) {
-    const long long b = __double_as_longlong(d);
-    return b < 0 ? -(b & 0x7FFFFFFFFFFFFFFFll) : b;
-}
+// Range tests on the bits.  For doubles with the sign bit clear the order of
+// the bit patterns, as unsigned 64-bit integers, is the order of the values,
+// so a test of a double against a positive bound is one unsigned compare on
+// the integer pipe.  (A sign-magnitude key built with a select -- b < 0 ?
+// -(b & mask) : b -- is recognised by the compiler as a double comparison
+// and turned back into FP64 instructions: measured, 2 extra FP64 operations
+// per range test.)
+constexpr unsigned long long kSignBit = 0x8000000000000000ull;
+__device__ __forceinline__ unsigned long long dbits(double d) { return (unsigned long long)__double_as_longlong(d); }
 
 __device__ __forceinline__ double ref_modulo(double f, double m) {
     // m > 0 finite (box sizes, 2 pi); a NaN f fails both range tests and
     // goes through fmod as in the IEEE form of these compares
-    const long long kf = dkey(f), km = dkey(m);
-    if (kf >= 0 && kf < km) return f;  // [+-0, m): f itself, without an FP64 operation
-    if (kf > -km && kf < km + (1ll << 52)) {  // key(2 m): the exponent of m plus one
-        // f - m or f + m; the sign of m is chosen on the integer pipe
-        const long long mb = __double_as_longlong(m);
-        return f + __longlong_as_double((kf >= km) ? (mb ^ (long long)0x8000000000000000ull) : mb);
+    const unsigned long long bf = dbits(f), bm = dbits(m);
+    if (bf < bm || bf == kSignBit) return f;  // [+0, m) and -0.0: f itself, without an FP64 operation
+    const bool neg = (bf & kSignBit) != 0;
+    // (-m, 0): |f| < m; [m, 2m): bits below those of 2 m (the exponent of m plus one)
+    if (neg ? (bf & ~kSignBit) < bm : bf < bm + (1ull << 52)) {
+        // f + m or f - m; the sign of m is chosen on the integer pipe
+        return f + __longlong_as_double((long long)(neg ? bm : (bm | kSignBit)));
     }
     double r = fmod(f, m);
     return (r < 0.0) ? r + fabs(m) : r;
 }
 
 // modulo for a position, which leaves the box rarely: the range test inline,
-// the wrap in an out-of-line call.  Inlined, the compiler executes the
-// wrap's FP64 additions speculatively for every particle (measured: 2 to 3
-// DADD per coordinate instead of 1), and on GB300 each warp-wide FP64
-// instruction occupies a sub-partition's FP64 unit for 64 cycles.  The
-// result is ref_modulo's, bit for bit.
+// the wrap in an out-of-line call.  The result is ref_modulo's, bit for bit.
 static __device__ __noinline__ double modulo_wrap(double f, double m) { return ref_modulo(f, m); }
 __device__ __forceinline__ double modulo_rare(double f, double m) {
-    const long long kf = dkey(f);
-    if (kf >= 0 && kf < dkey(m)) return f;
+    const unsigned long long bf = dbits(f);
+    if (bf < dbits(m) || bf == kSignBit) return f;
     return modulo_wrap(f, m);
 }
 
 // ang_pbc, src/particle.rs:37-44
 __device__ __forceinline__ void ref_ang_pbc(double &phi, double &theta) {
     double t = ref_modulo(theta, kTwoPi);
-    // t > pi on the integer pipe (a NaN t compares false, as in FP64)
-    const long long bt = __double_as_longlong(t);
-    if (dkey(t) > dkey(kPi) && (bt & 0x7FFFFFFFFFFFFFFFll) <= 0x7FF0000000000000ll) {
+    // t > pi on the integer pipe (-0.0 and a NaN t compare false, as in FP64)
+    const unsigned long long bt = dbits(t);
+    if ((bt & kSignBit) == 0 && bt > dbits(kPi) && bt <= 0x7FF0000000000000ull) {
         phi = ref_modulo(phi + kPi, kTwoPi);
         theta = kTwoPi - t;
     } else {

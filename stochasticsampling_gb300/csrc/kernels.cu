@@ -570,9 +570,11 @@ __device__ __forceinline__ void langevin_full_f2(const DevParams &P, double &px,
     if (!o.direct) {
         nphi = (pph + xf::to_double(o.a.h)) + xf::to_double(o.a.l);
         nth = (pth + xf::to_double(o.b.h)) + xf::to_double(o.b.l);
-        // theta in [0, pi], as the reference's pi/2 - atan2(v2, |v_xy|) (compares on the bits)
-        if (dkey(nth) < 0) nth = 0.0;
-        if (dkey(nth) > dkey(kPi)) nth = kPi;
+        // theta in [0, pi], as the reference's pi/2 - atan2(v2, |v_xy|) (compares on the bits:
+        // a negative value other than -0.0 -> 0, a positive one above pi (or a NaN) -> pi)
+        const unsigned long long bn = dbits(nth);
+        if ((bn & kSignBit) && bn != kSignBit) nth = 0.0;
+        else if (!(bn & kSignBit) && bn > dbits(kPi)) nth = kPi;
     } else {
         nphi = xf::to_double(o.a.h) + xf::to_double(o.a.l);
         nth = kPiHalf - (xf::to_double(o.b.h) + xf::to_double(o.b.l));
