@@ -759,12 +759,18 @@ def run_gpu(args, rank, world, dist):
     value, ms_max = aggregate(ms, N, args.steps, world, dist)
     sorted_line = measure_sorted(args, stream, p0, params, world, dist, barrier)
 
-    # per-stage CUDA events over K direct-launch steps (same stream, same workload)
-    sim.profile(True)
-    sim.run(args.steps)
-    stage_ms, nprof = sim.profile_read()
+    # per-stage CUDA events over K direct-launch steps (same stream, same
+    # workload), each step on its own: the median per stage, so that a step
+    # delayed on the shared host cores (direct launches are enqueued one by
+    # one) does not move the figures
+    per_step = []
+    for _ in range(args.steps):
+        sim.profile(True)
+        sim.run(1)
+        st, k = sim.profile_read()
+        per_step.append({name: v / max(1, k) for name, v in st.items()})
     sim.profile(False)
-    stage_avg = {k: v / max(1, nprof) for k, v in stage_ms.items()}
+    stage_avg = {name: statistics.median(r[name] for r in per_step) for name in per_step[0]}
 
     # end to end through the C ABI with pinned host buffers: per step the host
     # particle array goes in, the step runs, the particles come out.  The
