@@ -440,6 +440,71 @@ def measure_mixed(args, stream, p0, rank, world, dist, barrier, mode=True):
             "errors_vs_fp64_one_step": errors}
 
 
+# the driver's loop with due outputs on the production workload: the
+# distribution (4.2 MB) and the flow field (0.4 MB) every 10 steps, all
+# particles (400 MB) every 100 steps, over 300 steps
+OUT_STEPS = 300
+OUT_EVERY = dict(distribution=10, flowfield=10, particles=100)
+
+
+def measure_outputs(args, stream, p0, params):
+    """run_simulation (src/bin/main.rs:139-289) on the production workload
+    with an IO sink that drops the entries (the IO worker's compression runs
+    on its own thread and is not timed): the overlapped hand-off
+    (ss_output_begin into page-locked buffers, two outputs in flight)
+    against the blocking getters into fresh arrays.  Wall time of the whole
+    loop on the host, synchronised at both ends; each arm runs once untimed
+    first over 30 steps with the particles every 10 (the overlapped arm's
+    page-locked buffers, 2 x 405 MB, are allocated there and reused, as for
+    a long run)."""
+    import types
+
+    import torch
+
+    import stochasticsampling_gb300 as ss
+    from stochasticsampling_gb300 import driver
+
+    class Sink:
+        def __init__(self):
+            self.entries = 0
+
+        def append(self, e):
+            self.entries += 1
+
+        def write_snapshot(self, snap):
+            self.entries += 1
+
+    def settings(steps, every):
+        o = types.SimpleNamespace(initial_condition=False, final_snapshot=False, magneticfield=None,
+                                  particles_head=None, snapshot=None, **every)
+        return types.SimpleNamespace(simulation=types.SimpleNamespace(output_at_timestep=o,
+                                                                      number_of_timesteps=steps - 1))
+
+    res = {}
+    for overlap in (False, True):
+        sim = ss.Simulation(grid=GRID, box=BOX, params=params, quasi2d=True, sort=False, stream=stream.cuda_stream)
+        sim.init(p0)
+        with torch.cuda.stream(stream):
+            sim.run(args.warmup)
+            # untimed: every output kind in both slots (the buffers of the first use)
+            driver.run_simulation(settings(30, dict(OUT_EVERY, particles=10)), sim, Sink(), overlap=overlap)
+            sim.synchronize()
+            sink = Sink()
+            t0 = time.perf_counter()
+            driver.run_simulation(settings(OUT_STEPS, OUT_EVERY), sim, sink, overlap=overlap)
+            sim.synchronize()
+            secs = time.perf_counter() - t0
+        sim.close()
+        res["overlapped" if overlap else "blocking"] = {
+            "ms_per_step": secs * 1e3 / OUT_STEPS, "value": N * OUT_STEPS / secs, "unit": UNIT,
+            "entries": sink.entries}
+    res["steps"] = OUT_STEPS
+    res["outputs"] = {k: f"every {v} steps" for k, v in OUT_EVERY.items()}
+    res["d2h_bytes_per_100_steps"] = 10 * (GRID[0] * GRID[1] * GRID[3] + 3 * GRID[0] * GRID[1]) * 8 + N * 40
+    res["timing"] = "host wall clock of the loop, synchronised at both ends"
+    return res
+
+
 # the reference's CPU-runnable 2-D case: box 10x10, grid 32x32x1x16x1,
 # 1e5 particles (uniform positions and phi), Dt 0.1, Dr 0.5, active stress
 # -1, dt 0.01, 100 steps, FP64
@@ -724,6 +789,8 @@ def run_gpu(args, rank, world, dist):
             res = measure_c0(stream, cpu=rank == 0)
         elif args.only == "f32x2":
             res = measure_f32x2(args, stream, p0, params, world, dist, barrier)
+        elif args.only == "outputs":
+            res = measure_outputs(args, stream, p0, params)
         else:
             res = measure_mixed(args, stream, p0, rank, world, dist, barrier,
                                 "fixed64" if args.only == "fixed64" else True)
@@ -817,6 +884,7 @@ def run_gpu(args, rank, world, dist):
     c2 = None if args.no_c2 else measure_c2(args, stream, rank, world, dist, barrier)
     denoised = None if args.no_denoise else measure_denoised(args, rank)
     c0 = measure_c0(stream, cpu=(rank == 0 and not args.no_cpu_baseline))
+    outputs = measure_outputs(args, stream, p0, params)
 
     if rank != 0:
         return
@@ -888,6 +956,7 @@ def run_gpu(args, rank, world, dist):
         "ensemble": ensemble,
         "c2_3d_magnetic": c2,
         "c0_small_2d": c0,
+        "driver_outputs": outputs,
         "denoised": denoised,
     }
     print(json.dumps(line), flush=True)
@@ -907,7 +976,7 @@ def main():
     ap.add_argument("--denoise-pairs", type=int, default=1000)
     ap.add_argument("--denoise-epochs", type=int, default=6)
     ap.add_argument("--denoise-steps", type=int, default=400)
-    ap.add_argument("--only", choices=["mixed", "fixed64", "ensemble", "denoised", "c2", "f32x2", "c0"], default=None,
+    ap.add_argument("--only", choices=["mixed", "fixed64", "ensemble", "denoised", "c2", "f32x2", "c0", "outputs"], default=None,
                     help="run one section alone (a smaller command for profiling); prints its JSON")
     ap.add_argument("--ensemble-members", type=int, default=64)
     ap.add_argument("--ensemble-config", default=None,

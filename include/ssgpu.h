@@ -166,6 +166,39 @@ int ss_get_magnetic_complex(ss_ctx *ctx, double *b, double *gradb);
 /* Simulation::get_timestep (:246-248) */
 int ss_get_timestep(ss_ctx *ctx, uint64_t *out);
 
+/* Output that overlaps the steps.  The reference's main loop hands each due
+ * output to its IO worker thread, which serialises and compresses it while
+ * the simulation steps on (src/bin/main.rs:182-262, src/bin/output/
+ * worker.rs:130-248).  ss_output_begin is the device half of that hand-off:
+ * on the context's stream it copies the requested outputs of the current
+ * state into device slot `slot` (0 or 1) -- in HBM, so the next step may
+ * overwrite the state at once -- and then starts their transfer into the
+ * caller's host buffers on the context's output stream.  It returns without
+ * waiting for either, so further ss_do_timestep / ss_run calls queue behind
+ * it and the transfer runs while they execute.  Any buffer may be NULL:
+ *   dist       [nbins] doubles, as ss_get_distribution
+ *   flow       [3][cells] doubles, as ss_get_flow_field
+ *   mag        [3][cells] doubles, as ss_get_magnetic_field
+ *   particles  the first n rows, [n][5], as ss_get_particles
+ * The transfer is asynchronous from page-locked memory (ss_host_alloc, or
+ * cudaHostRegister'ed); from pageable memory the CUDA runtime stages it and
+ * the call may wait for it.  The host buffers hold the outputs once
+ * ss_output_wait(ctx, slot) has returned SS_OK and must not be touched
+ * before.  A slot still in flight cannot begin again (SS_ERR_STATE). */
+int ss_output_begin(ss_ctx *ctx, int slot, double *dist, double *flow, double *mag, double *particles,
+                    uint64_t n);
+/* Block until slot's transfer has landed (SS_OK at once when none is in
+ * flight).  Reports the device's bounds-check flags as they stood when the
+ * outputs were taken (SS_ERR_RANGE), as the synchronous getters do. */
+int ss_output_wait(ss_ctx *ctx, int slot);
+/* *ready = 1 when slot has no transfer in flight (ss_output_wait would not
+ * block), else 0. */
+int ss_output_query(ss_ctx *ctx, int slot, int *ready);
+/* Page-locked host memory (cudaHostAlloc) for the output buffers, and its
+ * release. */
+int ss_host_alloc(uint64_t bytes, void **out);
+int ss_host_free(void *p);
+
 /* Library seams on an explicit distribution dist[x][y][z][phi][theta] (host):
  * SpectralSolver::mean_flow_field(screening, &Distribution) and
  * MagneticSolver::mean_magnetic_field(&Distribution).  Outputs as

@@ -14,7 +14,8 @@ EXPORTS = [
     "ss_create", "ss_destroy", "ss_init", "ss_init_distribution", "ss_resume", "ss_do_timestep", "ss_run", "ss_noise", "ss_step_host",
     "ss_synchronize",
     "ss_get_particles", "ss_get_distribution", "ss_get_counts", "ss_get_flow_field", "ss_get_magnetic_field",
-    "ss_get_flow_complex", "ss_get_magnetic_complex", "ss_get_timestep", "ss_mean_flow_field",
+    "ss_get_flow_complex", "ss_get_magnetic_complex", "ss_get_timestep", "ss_output_begin", "ss_output_wait",
+    "ss_output_query", "ss_host_alloc", "ss_host_free", "ss_mean_flow_field",
     "ss_mean_magnetic_field", "ss_langevin", "ss_set_resort", "ss_profile_enable", "ss_profile_read", "ss_launch_count",
     "ss_sample_distribution_noalloc", "ss_ensemble_create", "ss_ensemble_destroy", "ss_ensemble_init",
     "ss_ensemble_autotune", "ss_ensemble_set_config", "ss_ensemble_run", "ss_ensemble_synchronize", "ss_ensemble_get_particles",
@@ -121,6 +122,11 @@ def load(build_if_missing=True):
         "ss_get_flow_complex": [vp, dp, dp],
         "ss_get_magnetic_complex": [vp, dp, dp],
         "ss_get_timestep": [vp, u64p],
+        "ss_output_begin": [vp, ci, dp, dp, dp, dp, u64],
+        "ss_output_wait": [vp, ci],
+        "ss_output_query": [vp, ci, ctypes.POINTER(ci)],
+        "ss_host_alloc": [u64, ctypes.POINTER(vp)],
+        "ss_host_free": [vp],
         "ss_mean_flow_field": [vp, ctypes.c_double, dp, dp, dp],
         "ss_mean_magnetic_field": [vp, dp, dp, dp],
         "ss_langevin": [dp, u64, u32, ctypes.POINTER(LangevinArgs), dp],

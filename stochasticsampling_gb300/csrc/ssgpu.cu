@@ -122,6 +122,15 @@ struct ss_ctx {
     cudaEvent_t chunk_ev[kHostChunks + 1] = {};
     uint64_t h_step = 0;  // host source of the step counter copy
     uint32_t *counts_in = nullptr;  // histogram of rows being loaded, until they are accepted
+    // ss_output_begin / ss_output_wait: two device slots, each a copy of one
+    // step's outputs, drained into host buffers on the output stream
+    struct OutSlot {
+        double *dist = nullptr, *fields = nullptr, *rows = nullptr;  // [nbins], [6][ncell] (flow, B), [n][5]
+        cudaEvent_t ready = nullptr, done = nullptr;  // taken on the step stream, landed on the output stream
+        uint32_t *h_err = nullptr;  // page-locked copy of the device error word at the snapshot
+        bool pending = false;
+    } out[2];
+    cudaStream_t out_stream = nullptr;
     uint64_t launches = 0;
     uint64_t launches_per_step = 0;
     Timing timing;
@@ -613,6 +622,14 @@ static void destroy_impl(ss_ctx *c) {
         if (e) cudaEventDestroy(e);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     cudaFree(c->counts_in);
+    if (c->out_stream) cudaStreamSynchronize(c->out_stream);
+    for (auto &o : c->out) {
+        cudaFree(o.dist); cudaFree(o.fields); cudaFree(o.rows);
+        if (o.ready) cudaEventDestroy(o.ready);
+        if (o.done) cudaEventDestroy(o.done);
+        if (o.h_err) cudaFreeHost(o.h_err);
+    }
+    if (c->out_stream) cudaStreamDestroy(c->out_stream);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -1411,6 +1428,132 @@ int ss_get_magnetic_complex(ss_ctx *c, double *b, double *gradb) {
 int ss_get_timestep(ss_ctx *c, uint64_t *out) {
     if (!c || !out) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
     *out = c->timestep;
+    return SS_OK;
+}
+
+// the device error word as read_device_error reports it, from a copy taken
+// without waiting for the step stream
+static int report_error_word(ss_ctx *c, uint32_t e) {
+    if (e & 0x100u)
+        return fail(c, SS_ERR_CUDA, "a tensor-memory-accelerator copy of the contraction did not complete in time");
+    if (e)
+        return fail(c, SS_ERR_RANGE,
+                    "device bounds check fired (flags %u): a particle coordinate was non-finite or outside the "
+                    "box after wrapping",
+                    e);
+    return SS_OK;
+}
+
+int ss_output_begin(ss_ctx *c, int slot, double *dist, double *flow, double *mag, double *particles, uint64_t n) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    if (slot < 0 || slot > 1) return fail(c, SS_ERR_INVALID_ARGUMENT, "output slot %d is not 0 or 1", slot);
+    if (!c->initialized) return fail(c, SS_ERR_STATE, "no outputs before ss_init");
+    if (particles && n > c->P.n)
+        return fail(c, SS_ERR_INVALID_ARGUMENT, "asked for %llu of %llu particles", (unsigned long long)n,
+                    (unsigned long long)c->P.n);
+    ss_ctx::OutSlot &o = c->out[slot];
+    if (o.pending) return fail(c, SS_ERR_STATE, "output slot %d is still in flight: ss_output_wait first", slot);
+    CK(cudaSetDevice(c->device));
+    if (!c->out_stream) CK(cudaStreamCreateWithFlags(&c->out_stream, cudaStreamNonBlocking));
+    if (!o.ready) CK(cudaEventCreateWithFlags(&o.ready, cudaEventDisableTiming));
+    if (!o.done) CK(cudaEventCreateWithFlags(&o.done, cudaEventDisableTiming));
+    if (!o.h_err) CK(cudaHostAlloc((void **)&o.h_err, sizeof(uint32_t), cudaHostAllocDefault));
+    const size_t nc = c->P.ncell;
+    // the snapshot, on the step stream: after the steps queued so far, before any queued later
+    if (dist) {
+        if (!o.dist) CK(cudaMalloc((void **)&o.dist, (size_t)c->P.nbins * sizeof(double)));
+        launch_counts_to_dist(c->stream, c->counts[c->dist_idx], c->P, o.dist);
+        c->launches += 1;
+        CKR(check_launch(c, "counts_to_dist"));
+    }
+    if (flow || mag) {
+        if (!o.fields) CK(cudaMalloc((void **)&o.fields, 6 * nc * sizeof(double)));
+        if (mag) CKR(ensure_magnetic(c));
+        if (c->mixed) CKR(widen_fields(c));
+        for (int f = 0; f < 2; ++f) {
+            if (!(f == 0 ? flow : mag)) continue;
+            const size_t comp0 = f == 0 ? 9 : 21;
+            if (c->mixed) {
+                launch_real_parts(c->stream, c->inv + comp0 * nc, 3ll * (long long)nc, o.fields + 3 * f * nc);
+                c->launches += 1;
+                CKR(check_launch(c, "real_parts"));
+            } else {
+                CK(cudaMemcpyAsync(o.fields + 3 * f * nc, c->ir + comp0 * nc, 3 * nc * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, c->stream));
+            }
+        }
+    }
+    if (particles && n) {
+        if (!o.rows) CK(cudaMalloc((void **)&o.rows, 5 * (size_t)c->P.n * sizeof(double)));
+        if (c->mixed)
+            launch_egest_m(c->stream, c->fixed, c->P.n, c->M, c->px[c->pcur], c->pa[c->pcur], c->pid[c->pcur],
+                           o.rows);
+        else launch_egest(c->stream, c->P.n, c->px[c->pcur], c->pid[c->pcur], o.rows);
+        c->launches += 1;
+        CKR(check_launch(c, "egest"));
+    }
+    CK(cudaEventRecord(o.ready, c->stream));
+    // the transfer, on the output stream
+    CK(cudaStreamWaitEvent(c->out_stream, o.ready, 0));
+    if (dist)
+        CK(cudaMemcpyAsync(dist, o.dist, (size_t)c->P.nbins * sizeof(double), cudaMemcpyDeviceToHost,
+                           c->out_stream));
+    if (flow)
+        CK(cudaMemcpyAsync(flow, o.fields, 3 * nc * sizeof(double), cudaMemcpyDeviceToHost, c->out_stream));
+    if (mag)
+        CK(cudaMemcpyAsync(mag, o.fields + 3 * nc, 3 * nc * sizeof(double), cudaMemcpyDeviceToHost,
+                           c->out_stream));
+    if (particles && n)
+        CK(cudaMemcpyAsync(particles, o.rows, 5 * n * sizeof(double), cudaMemcpyDeviceToHost, c->out_stream));
+    CK(cudaMemcpyAsync(o.h_err, c->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->out_stream));
+    CK(cudaEventRecord(o.done, c->out_stream));
+    o.pending = true;
+    return SS_OK;
+}
+
+int ss_output_wait(ss_ctx *c, int slot) {
+    if (!c) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null context");
+    if (slot < 0 || slot > 1) return fail(c, SS_ERR_INVALID_ARGUMENT, "output slot %d is not 0 or 1", slot);
+    ss_ctx::OutSlot &o = c->out[slot];
+    if (!o.pending) return SS_OK;
+    CK(cudaSetDevice(c->device));
+    CK(cudaEventSynchronize(o.done));
+    o.pending = false;
+    return report_error_word(c, *o.h_err);
+}
+
+int ss_output_query(ss_ctx *c, int slot, int *ready) {
+    if (!c || !ready) return fail(c, SS_ERR_INVALID_ARGUMENT, "null argument");
+    if (slot < 0 || slot > 1) return fail(c, SS_ERR_INVALID_ARGUMENT, "output slot %d is not 0 or 1", slot);
+    ss_ctx::OutSlot &o = c->out[slot];
+    if (!o.pending) {
+        *ready = 1;
+        return SS_OK;
+    }
+    CK(cudaSetDevice(c->device));
+    const cudaError_t e = cudaEventQuery(o.done);
+    if (e == cudaErrorNotReady) {
+        *ready = 0;
+        return SS_OK;
+    }
+    CK(e);
+    *ready = 1;
+    return SS_OK;
+}
+
+int ss_host_alloc(uint64_t bytes, void **out) {
+    ss_ctx *c = nullptr;
+    if (!out) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    if (bytes == 0) return fail(nullptr, SS_ERR_INVALID_ARGUMENT, "ss_host_alloc of 0 bytes");
+    CK(cudaHostAlloc(out, (size_t)bytes, cudaHostAllocDefault));
+    return SS_OK;
+}
+
+int ss_host_free(void *p) {
+    ss_ctx *c = nullptr;
+    if (!p) return SS_OK;
+    CK(cudaFreeHost(p));
     return SS_OK;
 }
 

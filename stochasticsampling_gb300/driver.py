@@ -12,8 +12,18 @@ schedule.  Schedule quirks kept from main.rs:
     particles; a magnetic field alone does not trigger it (:245-251);
   - the initial condition entry holds the distribution and, if particles are
     output at all, the (head of the) particles (:145-161).
+
+The reference's loop sends each due output to its IO worker thread and steps
+on while the worker serialises and compresses it (:182-262).  Here the
+device half overlaps too: a due step's outputs are taken into one of two
+device slots and copied into page-locked host buffers while the next steps
+run (ss_output_begin); the host turns them into records for the IO worker
+when the slot is needed again, in step order.
 """
 import os
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
 
 from . import output as io
 from .settings import to_toml
@@ -49,8 +59,102 @@ def _particles_out(settings, sim):
     return sim.get_particles()
 
 
-def run_simulation(settings, sim, out, progress=None):
-    """run_simulation, src/bin/main.rs:139-289."""
+def _copy(a, pool):
+    """A copy of the C-contiguous host array a; one of more than 16 MB is
+    copied in row blocks on the pool's threads (numpy releases the GIL while
+    it copies), so that the particle rows of an output do not hold up the
+    loop for long."""
+    out = np.empty_like(a)
+    if pool is None or a.nbytes < (16 << 20) or a.shape[0] < 2:
+        np.copyto(out, a)
+        return out
+    rows = a.shape[0]
+    step = -(-rows // pool._max_workers)
+    list(pool.map(lambda i: np.copyto(out[i:i + step], a[i:i + step]), range(0, rows, step)))
+    return out
+
+
+class _OverlappedOutputs:
+    """The due outputs of the loop, two steps' worth in flight at a time.
+
+    begin() takes a step's outputs on the device and starts their transfer
+    (Simulation.output_begin into slot k % 2); complete() waits for a slot,
+    copies its host buffers into records and hands them to the IO worker.
+    Slots alternate, so the slot reused next always holds the oldest output
+    and the worker receives entries in step order.  The page-locked host
+    buffers belong to the simulation (sim.output_buffers, released by its
+    close()), so later runs on it reuse them."""
+
+    def __init__(self, sim, out):
+        self.sim, self.out = sim, out
+        self.bufs = sim.output_buffers
+        self.pending = [None, None]
+        self.k = 0
+        self.pool = ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
+
+    def _array(self, slot, name, shape):
+        """The slot's host buffer `name`: the first shape[0] rows of a
+        page-locked array that grows to the largest request."""
+        b = self.bufs[slot].get(name)
+        if b is None or b.array.shape[0] < shape[0] or b.array.shape[1:] != shape[1:]:
+            if b is not None:
+                b.close()
+            b = self.bufs[slot][name] = self.sim.host_array(shape)
+        return b.array[:shape[0]]
+
+    def begin(self, timestep, dist, flow, mag, parts_n, snapshot):
+        """Outputs of the current state: dist/flow/mag flags, the number of
+        particle rows of the entry (None: none), and whether a snapshot is due."""
+        slot = self.k % 2
+        self.k += 1
+        if self.pending[slot] is not None:
+            self.complete(slot)
+        sim = self.sim
+        fshape = (3,) + tuple(sim.grid[:3])
+        rows = sim.n if snapshot else parts_n
+        self.sim.output_begin(
+            slot,
+            dist=self._array(slot, "dist", tuple(sim.dist_shape)) if dist else None,
+            flow=self._array(slot, "flow", fshape) if flow else None,
+            mag=self._array(slot, "mag", fshape) if mag else None,
+            particles=self._array(slot, "rows", (rows, 5)) if rows is not None else None)
+        self.pending[slot] = (timestep, dist, flow, mag, parts_n, snapshot)
+
+    def complete(self, slot):
+        timestep, dist, flow, mag, parts_n, snapshot = self.pending[slot]
+        self.pending[slot] = None
+        self.sim.output_wait(slot)
+        b = self.bufs[slot]
+        d = io.distribution_record(_copy(b["dist"].array, self.pool), self.sim.grid, self.sim.box) if dist else None
+        f = _copy(b["flow"].array, self.pool) if flow else None
+        m = _copy(b["mag"].array, self.pool) if mag else None
+        p = _copy(b["rows"].array[:parts_n], self.pool) if parts_n is not None else None
+        if d is not None or f is not None or p is not None:
+            self.out.append(io.output_entry(timestep, d, f, m, p))
+        if snapshot:
+            self.out.write_snapshot(io.snapshot_record(_copy(b["rows"].array[:self.sim.n], self.pool), timestep))
+
+    def finish(self):
+        for _, slot in sorted((p[0], s) for s, p in enumerate(self.pending) if p is not None):
+            self.complete(slot)
+
+    def close(self):
+        """Wait for transfers still in flight (after an error in the loop)."""
+        for slot in range(2):
+            if self.pending[slot] is not None:
+                self.pending[slot] = None
+                try:
+                    self.sim.output_wait(slot)
+                except Exception:
+                    pass
+        self.pool.shutdown()
+
+
+def run_simulation(settings, sim, out, progress=None, overlap=True):
+    """run_simulation, src/bin/main.rs:139-289.  overlap=True takes the due
+    outputs without stalling the steps (ss_output_begin, two in flight);
+    overlap=False reads each one back with the blocking getters.  Both give
+    the same entries and snapshots."""
     o = settings.simulation.output_at_timestep
     grid = sim.grid
     box = sim.box
@@ -60,6 +164,26 @@ def run_simulation(settings, sim, out, progress=None):
             particles=_particles_out(settings, sim) if o.particles is not None else None))
     timestep_start = sim.get_timestep() + 1
     n = settings.simulation.number_of_timesteps + timestep_start
+    if overlap:
+        outs = _OverlappedOutputs(sim, out)
+        try:
+            for timestep in range(timestep_start, n + 1):
+                sim.do_timestep()
+                due = lambda every: every is not None and timestep % every == 0
+                dist, flow, parts = due(o.distribution), due(o.flowfield), due(o.particles)
+                entry = dist or flow or parts
+                snap = due(o.snapshot)
+                if entry or snap:
+                    parts_n = (sim.n if o.particles_head is None else int(o.particles_head)) if parts else None
+                    outs.begin(timestep, dist, flow, entry and due(o.magneticfield), parts_n, snap)
+                if progress is not None:
+                    progress(timestep)
+            outs.finish()
+        finally:
+            outs.close()
+        if o.final_snapshot:
+            out.write_snapshot(io.snapshot_record(sim.get_particles(), sim.get_timestep()))
+        return
     for timestep in range(timestep_start, n + 1):
         sim.do_timestep()
         due = lambda every: every is not None and timestep % every == 0
@@ -77,10 +201,10 @@ def run_simulation(settings, sim, out, progress=None):
         out.write_snapshot(io.snapshot_record(sim.get_particles(), sim.get_timestep()))
 
 
-def run(settings, output_root, init=None, resume=None, **sim_kwargs):
+def run(settings, output_root, init=None, resume=None, overlap=True, **sim_kwargs):
     """run, src/bin/main.rs:68-135: output directory <root>/<id>/ holding
     <id>.toml, <id>.msgpack-lzma, <id>.index and the snapshots.  Returns the
-    output file path."""
+    output file path.  overlap as for run_simulation."""
     output_id = io.create_output_id(settings.environment.prefix)
     directory = os.path.join(output_root, output_id)
     os.makedirs(directory, exist_ok=False)
@@ -90,7 +214,7 @@ def run(settings, output_root, init=None, resume=None, **sim_kwargs):
     out = io.Worker(directory, output_id, settings.environment.output_format, settings.environment.io_queue_size)
     try:
         out.write_metadata(settings)
-        run_simulation(settings, sim, out)
+        run_simulation(settings, sim, out, overlap=overlap)
     finally:
         out.quit()
         sim.close()

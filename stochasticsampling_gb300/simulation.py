@@ -32,6 +32,36 @@ def _f64(a, shape=None):
     return a
 
 
+class PinnedArray:
+    """Page-locked host memory (ss_host_alloc) viewed as a float64 numpy
+    array, for the transfers of Simulation.output_begin.  close() releases
+    it; the array must not be used afterwards."""
+
+    def __init__(self, shape):
+        self.lib = _lib.load()
+        shape = tuple(int(v) for v in shape)
+        count = int(np.prod(shape))
+        if count < 1:
+            raise ValueError("a pinned array holds at least one element")
+        p = ctypes.c_void_p()
+        check(self.lib.ss_host_alloc(8 * count, ctypes.byref(p)))
+        self._p = p
+        self.array = np.ctypeslib.as_array((ctypes.c_double * count).from_address(p.value)).reshape(shape)
+
+    def close(self):
+        p = getattr(self, "_p", None)
+        if p is not None and p.value:
+            self.array = None
+            self.lib.ss_host_free(p)
+        self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def geometry_from_settings(settings):
     """(grid, box, params) of a Settings object, the ss_grid / ss_box /
     ss_params triple of the C ABI."""
@@ -99,6 +129,8 @@ class Simulation:
                                 ctypes.c_void_p(stream) if stream else None, ctypes.byref(h))
         check(rc)
         self._h = h
+        self._inflight = {}
+        self.output_buffers = [{}, {}]  # the driver's page-locked output buffers per slot
         gx, gy, gz, gp, gt = self.grid
         self.ncell = gx * gy * gz
         self.dist_shape = (gx, gy, gz, gp, gt)
@@ -106,8 +138,12 @@ class Simulation:
     def close(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:
-            self.lib.ss_destroy(h)
+            self.lib.ss_destroy(h)  # waits for transfers in flight
         self._h = None
+        for slot in getattr(self, "output_buffers", []):
+            for b in slot.values():
+                b.close()
+            slot.clear()
 
     def __del__(self):
         try:
@@ -234,6 +270,48 @@ class Simulation:
         t = ctypes.c_uint64()
         self._check(self.lib.ss_get_timestep(self._h, ctypes.byref(t)))
         return t.value
+
+    # --- output overlapped with the steps ---------------------------------
+    def host_array(self, shape):
+        """A page-locked host array for output_begin (a PinnedArray)."""
+        return PinnedArray(shape)
+
+    def output_begin(self, slot, dist=None, flow=None, mag=None, particles=None):
+        """ss_output_begin: take the current state's outputs into device slot
+        `slot` (0 or 1) and start their transfer into the given host arrays
+        (float64, C-contiguous, the shapes of get_distribution,
+        get_flow_field, get_magnetic_field and get_particles_head(n)); the
+        call does not wait, and steps may be queued at once.  The arrays hold
+        the outputs once output_wait(slot) has returned; page-locked arrays
+        (host_array) keep the transfer asynchronous."""
+        def arg(a, shape):
+            if a is None:
+                return None
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.shape != shape:
+                raise ValueError(f"output array must be C-contiguous float64 of shape {shape}")
+            return _ptr(a)
+        n = 0
+        if particles is not None:
+            n = particles.shape[0] if particles.ndim == 2 else -1
+            if not 0 <= n <= self.n:
+                raise ValueError(f"particles must be (n, 5) with n <= {self.n}")
+        fshape = (3,) + self.grid[:3]
+        ptrs = (arg(dist, self.dist_shape), arg(flow, fshape), arg(mag, fshape), arg(particles, (n, 5)))
+        self._check(self.lib.ss_output_begin(self._h, int(slot), *ptrs, n))
+        self._inflight[int(slot)] = (dist, flow, mag, particles)  # alive until the transfer has landed
+
+    def output_wait(self, slot):
+        """ss_output_wait: block until slot's transfer has landed."""
+        try:
+            self._check(self.lib.ss_output_wait(self._h, int(slot)))
+        finally:
+            self._inflight.pop(int(slot), None)
+
+    def output_ready(self, slot):
+        """ss_output_query: True when output_wait(slot) would not block."""
+        r = ctypes.c_int()
+        self._check(self.lib.ss_output_query(self._h, int(slot), ctypes.byref(r)))
+        return bool(r.value)
 
     def get_snapshot(self):
         """Snapshot (src/bin/simulation/mod.rs:80-86,210-217): the particles and

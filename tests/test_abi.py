@@ -71,6 +71,12 @@ def test_invalid_arguments_are_rejected_on_the_host():
         assert rc == _lib.SS_ERR_INVALID_ARGUMENT and what in _lib.last_error() and not h.value
     # null context
     assert L.ss_do_timestep(None, None, None) == _lib.SS_ERR_INVALID_ARGUMENT
+    # the overlapped outputs: null context, null result pointer, nothing to free
+    assert L.ss_output_begin(None, 0, None, None, None, None, 0) == _lib.SS_ERR_INVALID_ARGUMENT
+    assert L.ss_output_wait(None, 0) == _lib.SS_ERR_INVALID_ARGUMENT
+    assert L.ss_output_query(None, 0, None) == _lib.SS_ERR_INVALID_ARGUMENT
+    assert L.ss_host_alloc(16, None) == _lib.SS_ERR_INVALID_ARGUMENT
+    assert L.ss_host_free(None) == _lib.SS_OK
 
 
 def test_noalloc_refuses_more_rows_than_a_context_on_the_host():
