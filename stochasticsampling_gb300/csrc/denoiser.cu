@@ -65,14 +65,29 @@ constexpr int kChunkBytes = kChunkRows * 16;       // 2176 B: the A operand's le
 constexpr int kBodyOff = 8 * 16;                   // byte offset of row y0 in a chunk
 constexpr int kLineBytes = 4 * kChunkBytes + 128;  // 8832 B
 constexpr int kBodyBytes = kTileM * 16;            // one chunk of 128 rows
-constexpr int kPosSlots = 6;                       // position buffers of 3 lines (a ring)
-constexpr int kPosBytes = 3 * kLineBytes;
 constexpr int kAccStages = 8;                      // accumulators of 32 columns in tensor memory (a ring)
-constexpr int kConvThreads = 192;                  // warp 0 loads, warp 1 issues MMAs, warps 2-5 drain
+constexpr int kWgThreads = 192;  // the weight gradient: warp 0 loads, warps 1-2 issue MMAs, warps 2-5 write the sums
 constexpr int kBarBytes = 512;
-constexpr int kSmemConv = 1024 + kBAll + kPosSlots * kPosBytes + kBarBytes + 16;  // + alignment slack
-static_assert(kSmemConv <= 227 * 1024, "the convolution's shared memory exceeds a CTA's limit");
-static_assert(8 * (2 * kPosSlots + 2 * kAccStages + 1) <= kBarBytes, "mbarriers do not fit");
+// The convolution's shape by the number of output rows (along x) a tile
+// covers: ROWS rows take ROWS + 2 input lines per position (a position
+// buffer), ROWS rings of kAccStages accumulators in tensor memory and 4
+// epilogue warps per row; as many position buffers as fit beside the
+// weights (at most 6).  Two rows per tile read 2 lines per output row
+// instead of 3.
+template <int ROWS>
+struct ConvShape {
+    static constexpr int kLines = ROWS + 2;
+    static constexpr int kPosBytes = kLines * kLineBytes;
+    static constexpr int kFree = 227 * 1024 - 1024 - kBAll - kBarBytes - 16;  // + alignment slack
+    static constexpr int kSlots = kFree / kPosBytes < 6 ? kFree / kPosBytes : 6;
+    static constexpr int kThreads = 64 + 128 * ROWS;
+    static constexpr int kTmemCols = 32 * kAccStages * ROWS;
+    static constexpr int kSmem = 1024 + kBAll + kSlots * kPosBytes + kBarBytes + 16;
+    static_assert(kSlots >= 3, "fewer than 3 position buffers fit in shared memory");
+    static_assert(kTmemCols <= 512, "the accumulator rings exceed the tensor memory");
+};
+constexpr int kConvRows = 2;  // output rows per tile of the 32 -> 32 convolution
+static_assert(8 * (2 * 6 + 2 * kAccStages + 2) <= kBarBytes, "mbarriers do not fit");
 static_assert(kBAll % 16 == 0 && kLineBytes % 16 == 0 && kChunkBytes % 16 == 0, "bulk copies need 16-B alignment");
 constexpr uint32_t kWaitLimit = 1u << 22;    // mbarrier polls before giving up
 constexpr unsigned kErrTimeout = 1u;
@@ -241,15 +256,21 @@ struct Piece {
     uint64_t boff;   // offset (>> 4) of the first tile's weight block within a triple
     uint32_t acc;    // accumulate (0: the first product of the piece's tiles)
 };
-// the 17 (dx, dy, K half) products after the first, NP pieces each
-template <int NP>
+// the 17 (dx, dy, K half) products after the first, NP pieces each, for
+// each of ROWS output rows (row r reads the position's lines r .. r + 2 and
+// accumulates into ring r, kAccStages * 32 columns further on)
+template <int NP, int ROWS>
 __device__ __forceinline__ void issue_rest(uint64_t adesc0, uint64_t bdesc0, const Piece *pp) {
 #pragma unroll
     for (int t = 1; t < 18; ++t) {
         const int dx = t / 6, dy = (t / 2) % 3, kk = t % 2;
         const uint64_t a = adesc0 + a_off(dx, dy, kk), b = bdesc0 + b_off(dx, dy, kk);
 #pragma unroll
-        for (int k = 0; k < NP; ++k) mma_bf16(pp[k].col, a, b + pp[k].boff, pp[k].idesc, 1u);
+        for (int k = 0; k < NP; ++k)
+#pragma unroll
+            for (int r = 0; r < ROWS; ++r)
+                mma_bf16(pp[k].col + (uint32_t)(32 * kAccStages * r), a + (uint64_t)r * (kLineBytes >> 4),
+                         b + pp[k].boff, pp[k].idesc, 1u);
     }
 }
 
@@ -259,15 +280,17 @@ __host__ __device__ __forceinline__ int core_offset(int row, int k) {
 }
 
 // MODE 0: bias + ReLU -> BF16; MODE 1: bias -> FP32; MODE 2: times ReLU'(ref) -> BF16.
-// ny a multiple of 128.  Output tiles (x, y segment, phi) in the order phi
-// fastest; CTA b takes the contiguous range [b T / grid, (b + 1) T / grid)
-// of the T tiles and walks it in runs of consecutive phi at one (x, y
-// segment).  A run of L tiles streams its L + 2 input positions along phi;
-// the 3 lines (dx = -1, 0, 1) of input position p feed the output tiles
-// p + 1, p and p - 1 (dphi = -1, 0, +1), so one MMA of N = 96 covers all
-// three with the weights of the three dphi taps stacked along N (the packed
-// weights keep each (dx, dy) triple in the order dphi = +1, 0, -1): 18 MMAs
-// per input position instead of 54 of N = 32.  The accumulators of
+// ny a multiple of 128.  Output tiles (ROWS rows x .. x + ROWS - 1, y
+// segment, phi) in the order phi fastest; CTA b takes the contiguous range
+// [b T / grid, (b + 1) T / grid) of the T tiles and walks it in runs of
+// consecutive phi at one (x, y segment).  A run of L tiles streams its L + 2
+// input positions along phi; a position holds the ROWS + 2 lines x - 1 ..
+// x + ROWS (periodic), and for each output row r the 3 lines r .. r + 2
+// (dx = -1, 0, 1) of input position p feed the output tiles p + 1, p and
+// p - 1 (dphi = -1, 0, +1), so one MMA of N = 96 covers all three with the
+// weights of the three dphi taps stacked along N (the packed weights keep
+// each (dx, dy) triple in the order dphi = +1, 0, -1): 18 MMAs per row and
+// input position instead of 54 of N = 32.  The accumulators of
 // consecutive tiles are consecutive 32-column stages of a ring in tensor
 // memory; an MMA is split where the ring wraps, and where a tile takes its
 // first product (accumulate off).  The tensor core takes an N = 96 MMA every
@@ -275,56 +298,61 @@ __host__ __device__ __forceinline__ int core_offset(int row, int k) {
 // MMA: 64-bit descriptors plus compile-time offsets, and a branch-free path
 // for positions whose tiles lie in one piece of the ring.  Roles,
 // synchronised through mbarriers with bounded waits:
-//  - warp 0 streams positions into a ring of kPosSlots buffers of 3 lines
-//    with bulk copies (cp.async.bulk), 12 lanes at once (one bulk copy costs
-//    its issuing thread some 80 cycles): per line its 4 chunk bodies (2 KB
-//    each, contiguous in the activation layout) and its 8 halo pieces (16 B,
-//    periodic in y) straight into rows 7 and 136; full[slot] completes when
-//    the position's 24,960 bytes are in;
+//  - warp 0 streams positions into a ring of position buffers with bulk
+//    copies (cp.async.bulk), 4 (ROWS + 2) lanes at once (one bulk copy
+//    costs its issuing thread some 80 cycles): per line its 4 chunk bodies
+//    (2 KB each, contiguous in the activation layout) and its 8 halo pieces
+//    (16 B, periodic in y) straight into rows 7 and 136; full[slot]
+//    completes when the position's (ROWS + 2) x 8,320 bytes are in;
 //  - warp 1 (one thread) waits for the position and, when a tile starts,
-//    for its accumulator stage to be free; issues the MMAs; returns the
-//    position's buffer to the producer (empty[slot]) and commits the tile
-//    that the position completed to acc_full[stage];
-//  - warps 2-5 wait for acc_full, read the accumulator (warp w the tensor-
-//    memory lanes 32 (w mod 4) ..), release it to acc_empty and write the
-//    outputs, while the tensor core already runs the next positions.
-template <int MODE>
-__global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 *__restrict__ X,
-                                                            const uint8_t *__restrict__ Wpacked,
-                                                            const float *__restrict__ bias,
-                                                            const __nv_bfloat16 *__restrict__ ref,
-                                                            void *__restrict__ Y, Dims d, unsigned *__restrict__ err) {
+//    for its accumulator stage to be free; issues the MMAs of every row
+//    (row r into its own ring); returns the position's buffer to the
+//    producer (empty[slot]) and commits the tile that the position
+//    completed to acc_full[stage];
+//  - warps 2 + 4 r .. 5 + 4 r wait for acc_full, read row r's accumulator
+//    (warp w the tensor-memory lanes 32 (w mod 4) ..), release it to
+//    acc_empty and write the outputs, while the tensor core already runs
+//    the next positions.
+template <int MODE, int ROWS>
+__global__ void __launch_bounds__(ConvShape<ROWS>::kThreads, 1) k_conv32(const __nv_bfloat16 *__restrict__ X,
+                                                                         const uint8_t *__restrict__ Wpacked,
+                                                                         const float *__restrict__ bias,
+                                                                         const __nv_bfloat16 *__restrict__ ref,
+                                                                         void *__restrict__ Y, Dims d,
+                                                                         unsigned *__restrict__ err) {
+    using CS = ConvShape<ROWS>;
+    constexpr int kSlots = CS::kSlots;
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t sB0 = (raw + 1023u) & ~1023u;
     uint8_t *const sB = smem_raw + (sB0 - raw);
     const uint32_t sL0 = sB0 + kBAll;
-    const uint32_t bar0 = sL0 + kPosSlots * kPosBytes;
+    const uint32_t bar0 = sL0 + kSlots * CS::kPosBytes;
     auto full_bar = [&](uint32_t s) { return bar0 + 8u * s; };
-    auto empty_bar = [&](uint32_t s) { return bar0 + 8u * (kPosSlots + s); };
-    auto accf_bar = [&](uint32_t a) { return bar0 + 8u * (2 * kPosSlots + a); };
-    auto acce_bar = [&](uint32_t a) { return bar0 + 8u * (2 * kPosSlots + kAccStages + a); };
-    const uint32_t fin_bar = bar0 + 8u * (2 * kPosSlots + 2 * kAccStages);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(sB + kBAll + kPosSlots * kPosBytes + kBarBytes);
+    auto empty_bar = [&](uint32_t s) { return bar0 + 8u * (kSlots + s); };
+    auto accf_bar = [&](uint32_t a) { return bar0 + 8u * (2 * kSlots + a); };
+    auto acce_bar = [&](uint32_t a) { return bar0 + 8u * (2 * kSlots + kAccStages + a); };
+    const uint32_t fin_bar = bar0 + 8u * (2 * kSlots + 2 * kAccStages);
+    const uint32_t w_bar = fin_bar + 8u;  // the weights have landed
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(sB + kBAll + kSlots * CS::kPosBytes + kBarBytes);
     volatile int *sfail = reinterpret_cast<volatile int *>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    for (int i = tid; i < kBAll / 16; i += kConvThreads)
-        reinterpret_cast<uint4 *>(sB)[i] = reinterpret_cast<const uint4 *>(Wpacked)[i];
     if (tid == 0) {
-        for (int s = 0; s < kPosSlots; ++s) {
+        for (int s = 0; s < kSlots; ++s) {
             mbar_init(full_bar(s), 1);  // the expect_tx arrival (+ the transactions)
             mbar_init(empty_bar(s), 1);
         }
         for (int a = 0; a < kAccStages; ++a) {
             mbar_init(accf_bar(a), 1);
-            mbar_init(acce_bar(a), 4);  // one arrival per epilogue warp
+            mbar_init(acce_bar(a), 4 * ROWS);  // one arrival per epilogue warp
         }
         mbar_init(fin_bar, 1);
+        mbar_init(w_bar, 1);
         *sfail = 0;
         fence_mbar_init();
     }
-    if (warp == 1) tmem_alloc(smem_u32(tslot), 32 * kAccStages);
+    if (warp == 1) tmem_alloc(smem_u32(tslot), CS::kTmemCols);
     fence_proxy_async();
     tc_before_sync();
     __syncthreads();
@@ -332,42 +360,49 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 
     const uint32_t tmem = *tslot;
 
     const int nseg = d.ny / kTileM;
-    const int T = d.nx * nseg * d.np;
+    const int T = ((d.nx + ROWS - 1) / ROWS) * nseg * d.np;
     const int t0 = (int)((long long)blockIdx.x * T / gridDim.x);
     const int t1 = (int)((long long)(blockIdx.x + 1) * T / gridDim.x);
-    // tile t -> (x, y0, p)
+    // tile t -> (first row x, y0, p)
     auto decode = [&](int t, int &x, int &y0, int &p) {
         p = t % d.np;
         y0 = ((t / d.np) % nseg) * kTileM;
-        x = t / (d.np * nseg);
+        x = (t / (d.np * nseg)) * ROWS;
     };
     auto wrapi = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
 
     if (warp == 0) {
-        // ---- producer: the 3 lines of every input position of every run; lane 4 dx + c
-        // (12 lanes) copies chunk c of line dx: its body and its two halo rows ----
+        // ---- producer: the ROWS + 2 lines of every input position of every run; lane 4 l + c
+        // copies chunk c of line l (x - 1 + l, periodic): its body and its two halo rows ----
         uint32_t pos = 0;  // the CTA's count of input positions
         bool ok = true;
+        // the packed weights (54 KB, one bulk copy), landing while the first positions stream in
+        if (lane == 0) {
+            mbar_expect_tx(w_bar, (uint32_t)kBAll);
+            bulk_load(sB0, Wpacked, (uint32_t)kBAll, w_bar);
+        }
+        __syncwarp();
         for (int r0 = t0; r0 < t1 && ok;) {
             int x, y0, pa;
             decode(r0, x, y0, pa);
             const int L = min(t1 - r0, d.np - pa);
             const int ytop = wrapi(y0 - 1, d.ny), ybot = wrapi(y0 + kTileM, d.ny);
             for (int j = 0; j < L + 2; ++j, ++pos) {
-                const uint32_t slot = pos % kPosSlots;
-                if (pos >= (uint32_t)kPosSlots)
-                    ok = mbar_wait_polite(empty_bar(slot), ((pos / kPosSlots) - 1u) & 1u, sfail);
+                const uint32_t slot = pos % kSlots;
+                if (pos >= (uint32_t)kSlots)
+                    ok = mbar_wait_polite(empty_bar(slot), ((pos / kSlots) - 1u) & 1u, sfail);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok) break;
                 const int pin = wrapi(pa - 1 + j, d.np);
-                if (lane == 0) mbar_expect_tx(full_bar(slot), 3u * 4u * (kBodyBytes + 32u));
+                if (lane == 0) mbar_expect_tx(full_bar(slot), (uint32_t)CS::kLines * 4u * (kBodyBytes + 32u));
                 __syncwarp();
-                if (lane < 12) {
+                if (lane < 4 * CS::kLines) {
                     const int dx = lane >> 2, c = lane & 3;
+                    // line x - 1 + dx, periodic (x - 1 + dx lies in [-1, nx + ROWS])
+                    const int xl = (x + dx - 1 + 2 * d.nx) % d.nx;
                     // chunk plane c of the line: ny rows of 16 B from X + (line 4 + c) ny 8
-                    const __nv_bfloat16 *pc =
-                        X + ((size_t)(wrapi(x + dx - 1, d.nx) * d.np + pin) * 4 + c) * d.ny * 8;
-                    const uint32_t dc = sL0 + slot * (uint32_t)kPosBytes + (uint32_t)(dx * kLineBytes + c * kChunkBytes + kBodyOff);
+                    const __nv_bfloat16 *pc = X + ((size_t)(xl * d.np + pin) * 4 + c) * d.ny * 8;
+                    const uint32_t dc = sL0 + slot * (uint32_t)CS::kPosBytes + (uint32_t)(dx * kLineBytes + c * kChunkBytes + kBodyOff);
                     bulk_load(dc, pc + (size_t)y0 * 8, kBodyBytes, full_bar(slot));
                     bulk_load(dc - 16, pc + (size_t)ytop * 8, 16, full_bar(slot));
                     bulk_load(dc + kBodyBytes, pc + (size_t)ybot * 8, 16, full_bar(slot));
@@ -378,9 +413,11 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 
         }
         if (!ok && lane == 0) *sfail = 1;
         // every load issued lands before the CTA may exit
-        if (lane == 0)
-            for (uint32_t q = pos > (uint32_t)kPosSlots ? pos - kPosSlots : 0u; q < pos; ++q)
-                if (!mbar_wait(full_bar(q % kPosSlots), (q / kPosSlots) & 1u)) *sfail = 1;
+        if (lane == 0) {
+            for (uint32_t q = pos > (uint32_t)kSlots ? pos - kSlots : 0u; q < pos; ++q)
+                if (!mbar_wait(full_bar(q % kSlots), (q / kSlots) & 1u)) *sfail = 1;
+            if (!mbar_wait(w_bar, 0)) *sfail = 1;
+        }
     } else if (warp == 1) {
         // ---- MMA issuer ----
         if (lane == 0) {
@@ -388,13 +425,14 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 
             int ibase = 0;  // the CTA's count of tiles before this run (accumulator stage = count mod kAccStages)
             bool ok = true;
             const uint64_t bdesc0 = kBDesc | (uint64_t)((sB0 >> 4) & 0x3FFFu);
+            ok = mbar_wait_or_fail(w_bar, 0, sfail);
             for (int r0 = t0; r0 < t1 && ok;) {
                 int x, y0, pa;
                 decode(r0, x, y0, pa);
                 const int L = min(t1 - r0, d.np - pa);
                 for (int j = 0; j < L + 2; ++j, ++pos) {
-                    const uint32_t slot = pos % kPosSlots;
-                    ok = mbar_wait_or_fail(full_bar(slot), (pos / kPosSlots) & 1u, sfail);
+                    const uint32_t slot = pos % kSlots;
+                    ok = mbar_wait_or_fail(full_bar(slot), (pos / kSlots) & 1u, sfail);
                     // tile j starts at this position: its stage's previous tile has left it
                     const int inew = ibase + j;
                     if (ok && j < L && inew >= kAccStages)
@@ -427,13 +465,17 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 
                         pq[1] = pp[1];
                         nq = np_;
                     }
-                    const uint64_t adesc0 = kADesc | (uint64_t)(((sL0 + slot * (uint32_t)kPosBytes) >> 4) & 0x3FFFu);
+                    const uint64_t adesc0 =
+                        kADesc | (uint64_t)(((sL0 + slot * (uint32_t)CS::kPosBytes) >> 4) & 0x3FFFu);
                     // the first (dx, dy, K half) product with the first-product plan, then the 17 others
                     for (int k = 0; k < nq; ++k)
-                        mma_bf16(pq[k].col, adesc0 + a_off(0, 0, 0), bdesc0 + b_off(0, 0, 0) + pq[k].boff, pq[k].idesc,
-                                 pq[k].acc);
-                    if (np_ == 1) issue_rest<1>(adesc0, bdesc0, pp);
-                    else issue_rest<2>(adesc0, bdesc0, pp);
+#pragma unroll
+                        for (int r = 0; r < ROWS; ++r)
+                            mma_bf16(pq[k].col + (uint32_t)(32 * kAccStages * r),
+                                     adesc0 + a_off(0, 0, 0) + (uint64_t)r * (kLineBytes >> 4),
+                                     bdesc0 + b_off(0, 0, 0) + pq[k].boff, pq[k].idesc, pq[k].acc);
+                    if (np_ == 1) issue_rest<1, ROWS>(adesc0, bdesc0, pp);
+                    else issue_rest<2, ROWS>(adesc0, bdesc0, pp);
                     mma_commit(empty_bar(slot));
                     if (j >= 2) mma_commit(accf_bar((ibase + j - 2) % kAccStages));  // tile j - 2 is complete
                 }
@@ -447,8 +489,9 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 
         }
         __syncwarp();
     } else if (warp >= 2) {
-        // ---- epilogue ----
+        // ---- epilogue: warps 2 + 4 g .. 5 + 4 g drain row g ----
         const int q = warp & 3;  // tensor-memory lanes 32 q .. 32 q + 31
+        const int g = (warp - 2) >> 2;
         int i = 0;
         for (int t = t0; t < t1; ++t, ++i) {
             const int a = i % kAccStages;
@@ -459,12 +502,14 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 
             }
             tc_after_sync();
             uint32_t r[32];
-            tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(32 * a), r);
+            tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(32 * kAccStages * g + 32 * a), r);
             tc_before_sync();
             __syncwarp();
             if (lane == 0) mbar_arrive(acce_bar(a));
             int x, y0, p;
             decode(t, x, y0, p);
+            x += g;
+            if (x >= d.nx) continue;  // the second row of the last tile of an odd nx
             // this thread's voxel: row y of line x np + p; chunk plane c at (line 4 + c) ny
             const size_t line = (size_t)x * d.np + p, y = (size_t)(y0 + q * 32 + lane);
             auto at = [&](int c) { return ((line * 4 + c) * d.ny + y) * 8; };
@@ -519,7 +564,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv32(const __nv_bfloat16 
     __syncthreads();
     if (*sfail && tid == 0) atomicOr(err, kErrTimeout);
     tc_after_sync();
-    if (warp == 1) tmem_dealloc(tmem, 32 * kAccStages);
+    if (warp == 1) tmem_dealloc(tmem, CS::kTmemCols);
 }
 
 // Weight gradient of a 32 -> 32 layer on the tensor cores:
@@ -547,7 +592,7 @@ static_assert(kSmemWg <= 227 * 1024, "the weight gradient's shared memory exceed
 // M = 128, N = 32, A and B MN-major (bits 15, 16)
 constexpr uint32_t kIdescWg = kIdescM128 | (4u << 17) | (1u << 15) | (1u << 16);
 
-__global__ void __launch_bounds__(kConvThreads, 1) k_dn_wgrad_tc(const __nv_bfloat16 *__restrict__ dZ,
+__global__ void __launch_bounds__(kWgThreads, 1) k_dn_wgrad_tc(const __nv_bfloat16 *__restrict__ dZ,
                                                                  const __nv_bfloat16 *__restrict__ X,
                                                                  float *__restrict__ partial, Dims d,
                                                                  unsigned *__restrict__ err) {
@@ -565,7 +610,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_dn_wgrad_tc(const __nv_bflo
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     // the ones lines (rows y0 .. y0 + 127 of every chunk of slot 9 of each buffer)
-    for (int i = tid; i < 2 * 4 * kTileM; i += kConvThreads) {
+    for (int i = tid; i < 2 * 4 * kTileM; i += kWgThreads) {
         const int b = i / (4 * kTileM), c = (i / kTileM) % 4, r = i % kTileM;
         const uint32_t one2 = 0x3F803F80u;  // two BF16 1.0
         st_shared16(sS0 + (uint32_t)((b * kWgBufSlots + 9) * kWgSlotBytes + c * kChunkBytes + kBodyOff + r * 16),
@@ -696,7 +741,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_dn_wgrad_tc(const __nv_bflo
         }
     } else if (warp >= 2 && t1 <= t0) {
         float *out = partial + (size_t)blockIdx.x * kWgPartial;
-        for (int e = tid - 64; e < kWgPartial; e += kConvThreads - 64) out[e] = 0.f;
+        for (int e = tid - 64; e < kWgPartial; e += kWgThreads - 64) out[e] = 0.f;
     }
     if (!done) *sfail = 1;
     tc_before_sync();
@@ -738,6 +783,20 @@ int g_sms = 0;
 
 // tiles of the convolution: (x, y segment of 128, phi)
 int conv_tiles(Dims d) { return d.nx * (d.ny / kTileM) * d.np; }
+template <int MODE>
+static void conv_dispatch(int sms, const __nv_bfloat16 *X, const uint8_t *W, const float *bias,
+                          const __nv_bfloat16 *ref, void *Y, Dims d, unsigned *err, cudaStream_t s) {
+    using CS = ConvShape<kConvRows>;
+    const int tiles = ((d.nx + kConvRows - 1) / kConvRows) * (d.ny / kTileM) * d.np;
+    const int grid = tiles < sms ? tiles : sms;
+    k_conv32<MODE, kConvRows><<<grid, CS::kThreads, CS::kSmem, s>>>(X, W, bias, ref, Y, d, err);
+}
+static void conv_set_attrs() {
+    const int smem = ConvShape<kConvRows>::kSmem;
+    cudaFuncSetAttribute(k_conv32<0, kConvRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_conv32<1, kConvRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_conv32<2, kConvRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
 
 
 
@@ -1151,9 +1210,7 @@ extern "C" int ss_dn_conv32(const void *x, const float *w, const float *bias, co
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
         if (g_sms <= 0) g_sms = 1;
-        cudaFuncSetAttribute(k_conv32<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
-        cudaFuncSetAttribute(k_conv32<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
-        cudaFuncSetAttribute(k_conv32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
+        conv_set_attrs();
     }
     uint8_t *packed = nullptr;
     unsigned *derr = nullptr;
@@ -1164,12 +1221,11 @@ extern "C" int ss_dn_conv32(const void *x, const float *w, const float *bias, co
         const int nw = kTaps * kC * kC;
         if (mode == 2) k_pack_weights<true><<<(nw + 255) / 256, 256, 0, s>>>(w, packed);
         else k_pack_weights<false><<<(nw + 255) / 256, 256, 0, s>>>(w, packed);
-        const int tiles = conv_tiles(d), grid = tiles < g_sms ? tiles : g_sms;
         const __nv_bfloat16 *X = reinterpret_cast<const __nv_bfloat16 *>(x);
         const __nv_bfloat16 *R = reinterpret_cast<const __nv_bfloat16 *>(ref);
-        if (mode == 0) k_conv32<0><<<grid, kConvThreads, kSmemConv, s>>>(X, packed, bias, R, y, d, derr);
-        else if (mode == 1) k_conv32<1><<<grid, kConvThreads, kSmemConv, s>>>(X, packed, bias, R, y, d, derr);
-        else k_conv32<2><<<grid, kConvThreads, kSmemConv, s>>>(X, packed, bias, R, y, d, derr);
+        if (mode == 0) conv_dispatch<0>(g_sms, X, packed, bias, R, y, d, derr, s);
+        else if (mode == 1) conv_dispatch<1>(g_sms, X, packed, bias, R, y, d, derr, s);
+        else conv_dispatch<2>(g_sms, X, packed, bias, R, y, d, derr, s);
         e = cudaGetLastError();
     }
     unsigned herr = 0;
@@ -1265,9 +1321,7 @@ int dnfail(int code, const char *fmt, ...) {
 void conv_attrs() {
     static bool done = false;
     if (done) return;
-    cudaFuncSetAttribute(k_conv32<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
-    cudaFuncSetAttribute(k_conv32<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
-    cudaFuncSetAttribute(k_conv32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
+    conv_set_attrs();
     cudaFuncSetAttribute(k_dn_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemWg);
     cudaFuncSetAttribute(k_dn_out_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          kOutSmem + (kTaps * kC + 4) * (int)sizeof(float));
@@ -1277,8 +1331,7 @@ void conv_attrs() {
 template <int MODE>
 void launch_conv(ss_dn *n, const __nv_bfloat16 *X, const uint8_t *W, const float *bias, const __nv_bfloat16 *ref,
                  void *Y, cudaStream_t s) {
-    const int tiles = conv_tiles(n->d), grid = tiles < n->sms ? tiles : n->sms;
-    k_conv32<MODE><<<grid, kConvThreads, kSmemConv, s>>>(X, W, bias, ref, Y, n->d, n->err);
+    conv_dispatch<MODE>(n->sms, X, W, bias, ref, Y, n->d, n->err, s);
 }
 
 void pack_all(ss_dn *n, cudaStream_t s) {
@@ -1327,7 +1380,7 @@ void enqueue_backward(ss_dn *n, const float *t, const float *ya, cudaStream_t s,
     if (!grads) return;
     const int wgrid = conv_tiles(n->d) < n->sms ? conv_tiles(n->d) : n->sms;
     auto wgrad = [&](const __nv_bfloat16 *dZ, const __nv_bfloat16 *A, float *dW, float *db) {
-        k_dn_wgrad_tc<<<wgrid, kConvThreads, kSmemWg, s>>>(dZ, A, n->wpart, n->d, n->err);
+        k_dn_wgrad_tc<<<wgrid, kWgThreads, kSmemWg, s>>>(dZ, A, n->wpart, n->d, n->err);
         k_dn_wgrad_reduce<<<(kWgPartial + 255) / 256, 256, 0, s>>>(n->wpart, wgrid, dW, db);
     };
     const unsigned pg = (unsigned)(n->ntiles < 8 * n->sms ? n->ntiles : 8 * n->sms);

@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 
 # (nx, ny, nphi); the larger grids give every CTA several tiles, so that the
 # line ring is reused along phi and the CTAs' ranges cross segments and x
-SHAPES = [(2, 128, 8), (3, 128, 5), (2, 256, 3), (24, 256, 12), (128, 128, 32)]
+SHAPES = [(1, 128, 4), (2, 128, 8), (3, 128, 5), (2, 256, 3), (24, 256, 12), (128, 128, 32)]
 SHAPE_IDS = ["x".join(map(str, s)) for s in SHAPES]
 
 
