@@ -218,6 +218,23 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
                  : "memory");
 }
+// the same two from a whole converged warp: one elected lane (the same one
+// every time, so that its commits cover its MMAs) issues, and the warp's
+// descriptor arithmetic stays warp-uniform
+__device__ __forceinline__ void mma_bf16_warp(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                              uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred e, p;\n .reg .b32 l;\n elect.sync l|e, 0xffffffff;\n setp.ne.b32 p, %4, 0;\n"
+        " @e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit_warp(uint32_t mbar) {
+    asm volatile(
+        "{\n .reg .pred e;\n .reg .b32 l;\n elect.sync l|e, 0xffffffff;\n"
+        " @e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}\n" ::"r"(mbar)
+        : "memory");
+}
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
@@ -269,8 +286,8 @@ __device__ __forceinline__ void issue_rest(uint64_t adesc0, uint64_t bdesc0, con
         for (int k = 0; k < NP; ++k)
 #pragma unroll
             for (int r = 0; r < ROWS; ++r)
-                mma_bf16(pp[k].col + (uint32_t)(32 * kAccStages * r), a + (uint64_t)r * (kLineBytes >> 4),
-                         b + pp[k].boff, pp[k].idesc, 1u);
+                mma_bf16_warp(pp[k].col + (uint32_t)(32 * kAccStages * r), a + (uint64_t)r * (kLineBytes >> 4),
+                              b + pp[k].boff, pp[k].idesc, 1u);
     }
 }
 
@@ -419,24 +436,25 @@ __global__ void __launch_bounds__(ConvShape<ROWS>::kThreads, 1) k_conv32(const _
             if (!mbar_wait(w_bar, 0)) *sfail = 1;
         }
     } else if (warp == 1) {
-        // ---- MMA issuer ----
-        if (lane == 0) {
+        // ---- MMA issuer: the whole warp runs the loop (warp-uniform), one elected lane issues ----
+        {
             uint32_t pos = 0;
             int ibase = 0;  // the CTA's count of tiles before this run (accumulator stage = count mod kAccStages)
             bool ok = true;
             const uint64_t bdesc0 = kBDesc | (uint64_t)((sB0 >> 4) & 0x3FFFu);
-            ok = mbar_wait_or_fail(w_bar, 0, sfail);
+            ok = __all_sync(0xffffffffu, mbar_wait_or_fail(w_bar, 0, sfail));
             for (int r0 = t0; r0 < t1 && ok;) {
                 int x, y0, pa;
                 decode(r0, x, y0, pa);
                 const int L = min(t1 - r0, d.np - pa);
                 for (int j = 0; j < L + 2; ++j, ++pos) {
                     const uint32_t slot = pos % kSlots;
-                    ok = mbar_wait_or_fail(full_bar(slot), (pos / kSlots) & 1u, sfail);
+                    ok = __all_sync(0xffffffffu, mbar_wait_or_fail(full_bar(slot), (pos / kSlots) & 1u, sfail));
                     // tile j starts at this position: its stage's previous tile has left it
                     const int inew = ibase + j;
                     if (ok && j < L && inew >= kAccStages)
-                        ok = mbar_wait_or_fail(acce_bar(inew % kAccStages), ((inew / kAccStages) - 1) & 1, sfail);
+                        ok = __all_sync(0xffffffffu, mbar_wait_or_fail(acce_bar(inew % kAccStages),
+                                                                       ((inew / kAccStages) - 1) & 1, sfail));
                     if (!ok) break;
                     tc_after_sync();
                     // plan: tiles lo..hi take this position's products; tile k's block in the weight
@@ -471,20 +489,20 @@ __global__ void __launch_bounds__(ConvShape<ROWS>::kThreads, 1) k_conv32(const _
                     for (int k = 0; k < nq; ++k)
 #pragma unroll
                         for (int r = 0; r < ROWS; ++r)
-                            mma_bf16(pq[k].col + (uint32_t)(32 * kAccStages * r),
-                                     adesc0 + a_off(0, 0, 0) + (uint64_t)r * (kLineBytes >> 4),
-                                     bdesc0 + b_off(0, 0, 0) + pq[k].boff, pq[k].idesc, pq[k].acc);
+                            mma_bf16_warp(pq[k].col + (uint32_t)(32 * kAccStages * r),
+                                          adesc0 + a_off(0, 0, 0) + (uint64_t)r * (kLineBytes >> 4),
+                                          bdesc0 + b_off(0, 0, 0) + pq[k].boff, pq[k].idesc, pq[k].acc);
                     if (np_ == 1) issue_rest<1, ROWS>(adesc0, bdesc0, pp);
                     else issue_rest<2, ROWS>(adesc0, bdesc0, pp);
-                    mma_commit(empty_bar(slot));
-                    if (j >= 2) mma_commit(accf_bar((ibase + j - 2) % kAccStages));  // tile j - 2 is complete
+                    mma_commit_warp(empty_bar(slot));
+                    if (j >= 2) mma_commit_warp(accf_bar((ibase + j - 2) % kAccStages));  // tile j - 2 is complete
                 }
                 ibase += L;
                 r0 += L;
             }
             if (!ok) *sfail = 1;
             // the MMAs issued complete before the tensor memory is freed
-            mma_commit(fin_bar);
+            mma_commit_warp(fin_bar);
             if (!mbar_wait(fin_bar, 0)) *sfail = 1;
         }
         __syncwarp();
