@@ -120,14 +120,6 @@ struct Vox {
 };
 
 // ---- PTX wrappers ------------------------------------------------------
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 __device__ __forceinline__ void mbar_init(uint32_t addr, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(addr), "r"(count) : "memory");
@@ -296,7 +288,9 @@ __host__ __device__ __forceinline__ int core_offset(int row, int k) {
     return (row >> 3) * 512 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
 }
 
-// MODE 0: bias + ReLU -> BF16; MODE 1: bias -> FP32; MODE 2: times ReLU'(ref) -> BF16.
+// MODE 0: bias + ReLU -> BF16; MODE 1: bias -> FP32; MODE 2: times ReLU'(ref) -> BF16;
+// MODE 3: the 32 -> 1 output layer (weights of output channel 0, the other 31
+// zero): res + channel 0 + bias -> FP32 in the layout [x][phi][y].
 // ny a multiple of 128.  Output tiles (ROWS rows x .. x + ROWS - 1, y
 // segment, phi) in the order phi fastest; CTA b takes the contiguous range
 // [b T / grid, (b + 1) T / grid) of the T tiles and walks it in runs of
@@ -335,6 +329,7 @@ __global__ void __launch_bounds__(ConvShape<ROWS>::kThreads, 1) k_conv32(const _
                                                                          const uint8_t *__restrict__ Wpacked,
                                                                          const float *__restrict__ bias,
                                                                          const __nv_bfloat16 *__restrict__ ref,
+                                                                         const float *__restrict__ res,
                                                                          void *__restrict__ Y, Dims d,
                                                                          unsigned *__restrict__ err) {
     using CS = ConvShape<ROWS>;
@@ -531,7 +526,10 @@ __global__ void __launch_bounds__(ConvShape<ROWS>::kThreads, 1) k_conv32(const _
             // this thread's voxel: row y of line x np + p; chunk plane c at (line 4 + c) ny
             const size_t line = (size_t)x * d.np + p, y = (size_t)(y0 + q * 32 + lane);
             auto at = [&](int c) { return ((line * 4 + c) * d.ny + y) * 8; };
-            if (MODE == 1) {
+            if (MODE == 3) {
+                const size_t v = line * d.ny + y;
+                reinterpret_cast<float *>(Y)[v] = res[v] + __uint_as_float(r[0]) + bias[0];
+            } else if (MODE == 1) {
                 float *out = reinterpret_cast<float *>(Y);
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
@@ -797,23 +795,36 @@ __global__ void k_pack_weights(const float *__restrict__ W, uint8_t *__restrict_
     *reinterpret_cast<__nv_bfloat16 *>(out + block * kBTap + core_offset(n, k)) = __float2bfloat16_rn(w);
 }
 
+// the 32 -> 1 output layer's weights w[tap][ci] as the operand of output
+// channel 0 of a 32 -> 32 layer (channels 1-31 zero)
+__global__ void k_pack_out_weights(const float *__restrict__ W, uint8_t *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kTaps * kC * kC) return;
+    const int t = i / (kC * kC), n = (i / kC) % kC, k = i % kC;
+    const float w = n == 0 ? W[t * kC + k] : 0.f;
+    const int block = t - t % 3 + (2 - t % 3);
+    *reinterpret_cast<__nv_bfloat16 *>(out + block * kBTap + core_offset(n, k)) = __float2bfloat16_rn(w);
+}
+
 int g_sms = 0;
 
 // tiles of the convolution: (x, y segment of 128, phi)
 int conv_tiles(Dims d) { return d.nx * (d.ny / kTileM) * d.np; }
 template <int MODE>
 static void conv_dispatch(int sms, const __nv_bfloat16 *X, const uint8_t *W, const float *bias,
-                          const __nv_bfloat16 *ref, void *Y, Dims d, unsigned *err, cudaStream_t s) {
+                          const __nv_bfloat16 *ref, const float *res, void *Y, Dims d, unsigned *err,
+                          cudaStream_t s) {
     using CS = ConvShape<kConvRows>;
     const int tiles = ((d.nx + kConvRows - 1) / kConvRows) * (d.ny / kTileM) * d.np;
     const int grid = tiles < sms ? tiles : sms;
-    k_conv32<MODE, kConvRows><<<grid, CS::kThreads, CS::kSmem, s>>>(X, W, bias, ref, Y, d, err);
+    k_conv32<MODE, kConvRows><<<grid, CS::kThreads, CS::kSmem, s>>>(X, W, bias, ref, res, Y, d, err);
 }
 static void conv_set_attrs() {
     const int smem = ConvShape<kConvRows>::kSmem;
     cudaFuncSetAttribute(k_conv32<0, kConvRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_conv32<1, kConvRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_conv32<2, kConvRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_conv32<3, kConvRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
 
@@ -896,8 +907,6 @@ __global__ void k_dn_transpose(const float *__restrict__ src, float *__restrict_
 // the copies are contiguous on both sides and a warp's 128-bit reads of one
 // plane (32 consecutive rows) are free of bank conflicts.
 constexpr int kTileY = 128, kTileP = 2, kHaloY = kTileY + 2, kHaloP = kTileP + 2;
-constexpr int kOutRows = 3 * kHaloP * kHaloY;       // staged rows of the output layer's input
-constexpr int kOutSmem = kOutRows * 64;              // their 4 chunk planes of 16-byte rows
 
 __device__ __forceinline__ int wrap_idx(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
@@ -955,71 +964,6 @@ __global__ void __launch_bounds__(128) k_dn_in_tiled(const float *__restrict__ x
     const int y = y0 + ty;
     store_act32(A1, ((size_t)x0 * d.np + p0) * d.ny + y, d.ny, a0);
     if (p0 + 1 < d.np) store_act32(A1, ((size_t)x0 * d.np + p0 + 1) * d.ny + y, d.ny, a1);
-}
-
-// output layer 32 -> 1 with the residual: y[v] = x[v] + b_out + sum_tap w_out[tap] . A3[nbr(v, tap)]
-// (x and y in the activation layout)
-__global__ void __launch_bounds__(128) k_dn_out_tiled(const __nv_bfloat16 *__restrict__ A3,
-                                                      const float *__restrict__ x, const float *__restrict__ P,
-                                                      float *__restrict__ y, Dims d) {
-    extern __shared__ __align__(16) unsigned char dn_out_smem[];
-    float *sw = reinterpret_cast<float *>(dn_out_smem + kOutSmem);
-    int x0, p0, y0;
-    tile_origin(d, x0, p0, y0);
-    const uint32_t base = smem_u32(dn_out_smem);
-    for (int i = threadIdx.x; i < kOutRows * 4; i += blockDim.x) {
-        // 16-byte chunk k of staged row r, staged as planes [k][r] like the activation layout:
-        // consecutive threads copy consecutive rows of one plane, contiguous on both sides
-        const int k = i / kOutRows, r = i - k * kOutRows;
-        const int ys = r % kHaloY, ip = (r / kHaloY) % kHaloP, ix = r / (kHaloY * kHaloP);
-        const int gx = wrap_idx(x0 + ix - 1, d.nx), gp = wrap_idx(p0 + ip - 1, d.np), gy = wrap_idx(y0 + ys - 1, d.ny);
-        cp_async16(base + (uint32_t)(i * 16), A3 + act_at_line((uint32_t)(gx * d.np + gp), (uint32_t)gy, k, d.ny));
-    }
-    cp_async_commit();
-    for (int i = threadIdx.x; i < kTaps * kC + 1; i += blockDim.x) sw[i] = P[kOffWout + i];
-    cp_async_wait<0>();
-    __syncthreads();
-    const int ty = threadIdx.x;
-    // one partial sum per 8-channel chunk and voxel: 8 independent FMA chains per thread
-    float acc0[4] = {0.f, 0.f, 0.f, 0.f}, acc1[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int dx = 0; dx < 3; ++dx) {
-        for (int dy = 0; dy < 3; ++dy) {
-            const int ys = ty + dy;
-#pragma unroll
-            for (int ip = 0; ip < kHaloP; ++ip) {
-                // staged row (dx, ip, ys) is tap (dx, dy, ip) of voxel p0 and tap (dx, dy, ip - 1) of voxel p0 + 1
-                const int r = (dx * kHaloP + ip) * kHaloY + ys;
-                const float4 *w0 = reinterpret_cast<const float4 *>(sw + (dx * 9 + dy * 3 + ip) * kC);
-                const float4 *w1 = reinterpret_cast<const float4 *>(sw + (dx * 9 + dy * 3 + ip - 1) * kC);
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const uint4 u = *reinterpret_cast<const uint4 *>(dn_out_smem + (k * kOutRows + r) * 16);
-                    const float v[8] = {__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xFFFF0000u),
-                                        __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xFFFF0000u),
-                                        __uint_as_float(u.z << 16), __uint_as_float(u.z & 0xFFFF0000u),
-                                        __uint_as_float(u.w << 16), __uint_as_float(u.w & 0xFFFF0000u)};
-                    if (ip < 3) {
-                        const float4 a = w0[2 * k], b = w0[2 * k + 1];
-                        float t = acc0[k];
-                        t = fmaf(a.x, v[0], t); t = fmaf(a.y, v[1], t); t = fmaf(a.z, v[2], t); t = fmaf(a.w, v[3], t);
-                        t = fmaf(b.x, v[4], t); t = fmaf(b.y, v[5], t); t = fmaf(b.z, v[6], t); t = fmaf(b.w, v[7], t);
-                        acc0[k] = t;
-                    }
-                    if (ip > 0) {
-                        const float4 a = w1[2 * k], b = w1[2 * k + 1];
-                        float t = acc1[k];
-                        t = fmaf(a.x, v[0], t); t = fmaf(a.y, v[1], t); t = fmaf(a.z, v[2], t); t = fmaf(a.w, v[3], t);
-                        t = fmaf(b.x, v[4], t); t = fmaf(b.y, v[5], t); t = fmaf(b.z, v[6], t); t = fmaf(b.w, v[7], t);
-                        acc1[k] = t;
-                    }
-                }
-            }
-        }
-    }
-    const float bo = sw[kTaps * kC];
-    const size_t v0 = ((size_t)x0 * d.np + p0) * d.ny + y0 + ty;
-    y[v0] = x[v0] + ((acc0[0] + acc0[1]) + (acc0[2] + acc0[3])) + bo;
-    if (p0 + 1 < d.np) y[v0 + d.ny] = x[v0 + d.ny] + ((acc1[0] + acc1[1]) + (acc1[2] + acc1[3])) + bo;
 }
 
 // mean-square loss against the target and its gradient dy = 2 (y - t) / V;
@@ -1108,7 +1052,8 @@ __global__ void __launch_bounds__(128) k_dn_out_bwd(const float *__restrict__ dy
                                                     const __nv_bfloat16 *__restrict__ A3,
                                                     __nv_bfloat16 *__restrict__ dZ3, Dims d, int nvox) {
     __shared__ float sw[kTaps * kC];
-    for (int i = threadIdx.x; i < kTaps * kC; i += blockDim.x) sw[i] = P[kOffWout + i];
+    // the weights the forward used (BF16, on the tensor cores)
+    for (int i = threadIdx.x; i < kTaps * kC; i += blockDim.x) sw[i] = __bfloat162float(__float2bfloat16_rn(P[kOffWout + i]));
     __syncthreads();
     const int u = blockIdx.x * blockDim.x + threadIdx.x;  // activation index
     if (u >= nvox) return;
@@ -1241,9 +1186,9 @@ extern "C" int ss_dn_conv32(const void *x, const float *w, const float *bias, co
         else k_pack_weights<false><<<(nw + 255) / 256, 256, 0, s>>>(w, packed);
         const __nv_bfloat16 *X = reinterpret_cast<const __nv_bfloat16 *>(x);
         const __nv_bfloat16 *R = reinterpret_cast<const __nv_bfloat16 *>(ref);
-        if (mode == 0) conv_dispatch<0>(g_sms, X, packed, bias, R, y, d, derr, s);
-        else if (mode == 1) conv_dispatch<1>(g_sms, X, packed, bias, R, y, d, derr, s);
-        else conv_dispatch<2>(g_sms, X, packed, bias, R, y, d, derr, s);
+        if (mode == 0) conv_dispatch<0>(g_sms, X, packed, bias, R, nullptr, y, d, derr, s);
+        else if (mode == 1) conv_dispatch<1>(g_sms, X, packed, bias, R, nullptr, y, d, derr, s);
+        else conv_dispatch<2>(g_sms, X, packed, bias, R, nullptr, y, d, derr, s);
         e = cudaGetLastError();
     }
     unsigned herr = 0;
@@ -1309,7 +1254,7 @@ struct ss_dn {
     // dy, yb, xa, ta: FP32 grids in the activation layout
     float *P = nullptr, *G = nullptr, *M = nullptr, *S = nullptr, *dy = nullptr, *yb = nullptr, *xa = nullptr,
           *ta = nullptr;
-    uint8_t *Wp2 = nullptr, *Wp3 = nullptr, *Wm2 = nullptr, *Wm3 = nullptr;
+    uint8_t *Wp2 = nullptr, *Wp3 = nullptr, *Wm2 = nullptr, *Wm3 = nullptr, *Wpo = nullptr;
     __nv_bfloat16 *A1 = nullptr, *A2 = nullptr, *A3 = nullptr, *D1 = nullptr, *D2 = nullptr;
     float *wpart = nullptr;  // the weight gradients' per-CTA partial sums
     double *sums = nullptr;
@@ -1341,15 +1286,13 @@ void conv_attrs() {
     if (done) return;
     conv_set_attrs();
     cudaFuncSetAttribute(k_dn_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemWg);
-    cudaFuncSetAttribute(k_dn_out_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kOutSmem + (kTaps * kC + 4) * (int)sizeof(float));
     done = true;
 }
 
 template <int MODE>
 void launch_conv(ss_dn *n, const __nv_bfloat16 *X, const uint8_t *W, const float *bias, const __nv_bfloat16 *ref,
-                 void *Y, cudaStream_t s) {
-    conv_dispatch<MODE>(n->sms, X, W, bias, ref, Y, n->d, n->err, s);
+                 void *Y, cudaStream_t s, const float *res = nullptr) {
+    conv_dispatch<MODE>(n->sms, X, W, bias, ref, res, Y, n->d, n->err, s);
 }
 
 void pack_all(ss_dn *n, cudaStream_t s) {
@@ -1358,7 +1301,8 @@ void pack_all(ss_dn *n, cudaStream_t s) {
     k_pack_weights<false><<<b, 256, 0, s>>>(n->P + kOffW3, n->Wp3);
     k_pack_weights<true><<<b, 256, 0, s>>>(n->P + kOffW2, n->Wm2);
     k_pack_weights<true><<<b, 256, 0, s>>>(n->P + kOffW3, n->Wm3);
-    n->launches += 4;
+    k_pack_out_weights<<<b, 256, 0, s>>>(n->P + kOffWout, n->Wpo);
+    n->launches += 5;
 }
 
 template <bool TO_ACT>
@@ -1374,7 +1318,8 @@ void enqueue_forward_act(ss_dn *n, const float *x, float *ya, cudaStream_t s) {
     k_dn_in_tiled<<<tiles, 128, 0, s>>>(n->xa, n->P, n->A1, n->d);
     launch_conv<0>(n, n->A1, n->Wp2, n->P + kOffB2, nullptr, n->A2, s);
     launch_conv<0>(n, n->A2, n->Wp3, n->P + kOffB3, nullptr, n->A3, s);
-    k_dn_out_tiled<<<tiles, 128, kOutSmem + (kTaps * kC + 4) * sizeof(float), s>>>(n->A3, n->xa, n->P, ya, n->d);
+    // the 32 -> 1 output layer on the tensor cores (BF16 weights), + the residual
+    launch_conv<3>(n, n->A3, n->Wpo, n->P + kOffBout, nullptr, ya, s, n->xa);
     n->launches += 5;
 }
 
@@ -1426,7 +1371,7 @@ void destroy_dn(ss_dn *n) {
     if (n->stream) cudaStreamSynchronize(n->stream);
     cudaFree(n->P); cudaFree(n->G); cudaFree(n->M); cudaFree(n->S); cudaFree(n->dy); cudaFree(n->yb);
     cudaFree(n->xa); cudaFree(n->ta);
-    cudaFree(n->Wp2); cudaFree(n->Wp3); cudaFree(n->Wm2); cudaFree(n->Wm3);
+    cudaFree(n->Wp2); cudaFree(n->Wp3); cudaFree(n->Wm2); cudaFree(n->Wm3); cudaFree(n->Wpo);
     cudaFree(n->A1); cudaFree(n->A2); cudaFree(n->A3); cudaFree(n->D1); cudaFree(n->D2);
     cudaFree(n->sums); cudaFree(n->err); cudaFree(n->wpart);
     if (n->own_stream && n->stream) cudaStreamDestroy(n->stream);
@@ -1466,6 +1411,7 @@ int ss_dn_create(uint32_t nx, uint32_t ny, uint32_t np, uint64_t seed, void *str
     A((void **)&n->dy, V * sizeof(float)); A((void **)&n->yb, V * sizeof(float));
     A((void **)&n->xa, V * sizeof(float)); A((void **)&n->ta, V * sizeof(float));
     A((void **)&n->Wp2, kBAll); A((void **)&n->Wp3, kBAll); A((void **)&n->Wm2, kBAll); A((void **)&n->Wm3, kBAll);
+    A((void **)&n->Wpo, kBAll);
     A((void **)&n->A1, ab); A((void **)&n->A2, ab); A((void **)&n->A3, ab); A((void **)&n->D1, ab);
     A((void **)&n->D2, ab);
     A((void **)&n->sums, 2 * sizeof(double)); A((void **)&n->err, sizeof(unsigned));

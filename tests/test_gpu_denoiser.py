@@ -133,7 +133,7 @@ def test_conv32_rejects_bad_shapes():
 # ---------------------------------------------------------------- the network
 def _ref_net(torch, x, P, ste=False):
     """The denoiser in torch fp32 with the kernel's BF16 roundings (weights
-    of the 32->32 layers, the three activations)."""
+    of the 32->32 layers and of the output layer, the three activations)."""
     import torch.nn.functional as F
     from stochasticsampling_gb300.denoiser import split_params
     p = {k: torch.as_tensor(v.copy()) for k, v in split_params(P).items()}
@@ -149,7 +149,7 @@ def _ref_net(torch, x, P, ste=False):
     a1 = bf(torch.relu(conv(x[None], p["w_in"][:, :, None], p["b_in"])))
     a2 = bf(torch.relu(conv(a1, bf(p["w2"]), p["b2"])))
     a3 = bf(torch.relu(conv(a2, bf(p["w3"]), p["b3"])))
-    return x + conv(a3, p["w_out"][:, None, :], p["b_out"])[0], p
+    return x + conv(a3, bf(p["w_out"])[:, None, :], p["b_out"])[0], p
 
 
 def _net(ss, shape, seed=3, out_scale=0.05):
@@ -211,7 +211,7 @@ def test_denoiser_gradients_match_torch(shape, w):
         a1 = bf(torch.relu(conv(x[b][None], P_t["w_in"][:, :, None], P_t["b_in"])))
         a2 = bf(torch.relu(conv(a1, bf(P_t["w2"]), P_t["b2"])))
         a3 = bf(torch.relu(conv(a2, bf(P_t["w3"]), P_t["b3"])))
-        yb = x[b] + conv(a3, P_t["w_out"][:, None, :], P_t["b_out"])[0]
+        yb = x[b] + conv(a3, bf(P_t["w_out"])[:, None, :], P_t["b_out"])[0]
         r = yb - t[b]
         phi2 = 2 * (torch.arange(shape[2], dtype=torch.float64) + 0.5) * 2 * np.pi / shape[2]
         c2 = (r * torch.cos(phi2).float()).sum(-1)
