@@ -228,11 +228,9 @@ __device__ __forceinline__ void langevin_mixed(float &phi, float &theta, float s
 }
 
 // FP64 position advance: x + dx wrapped into [0, L) (modulo of
-// src/particle.rs:26-35), with ref_modulo's range tests on the integer pipe:
-// an FP64 compare would occupy GB300's FP64 pipe for a whole warp whenever
-// one of its particles sits in an edge cell.
-// x + dx in FP64, then modulo (src/particle.rs:26-35): one FP64 addition per
-// coordinate, the wrap out of line (modulo_rare).
+// src/particle.rs:26-35): one FP64 addition per coordinate; the wrap's range
+// tests compare raw bits on the integer pipe and the rare wrap itself runs
+// out of line (modulo_rare).
 __device__ __forceinline__ double advance64(double x, float dx, double L) { return modulo_rare(x + f2d(dx), L); }
 
 }  // namespace ss
