@@ -795,6 +795,16 @@ __global__ void k_pack_weights(const float *__restrict__ W, uint8_t *__restrict_
     *reinterpret_cast<__nv_bfloat16 *>(out + block * kBTap + core_offset(n, k)) = __float2bfloat16_rn(w);
 }
 
+// the 1 -> 32 input layer's weights w[tap][co] as the B operand [32 co][32 taps]
+// of its GEMM (taps 27-31 zero)
+__global__ void k_pack_in_weights(const float *__restrict__ W, uint8_t *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kC * kC) return;
+    const int n = i / kC, k = i % kC;
+    const float w = k < kTaps ? W[k * kC + n] : 0.f;
+    *reinterpret_cast<__nv_bfloat16 *>(out + core_offset(n, k)) = __float2bfloat16_rn(w);
+}
+
 // the 32 -> 1 output layer's weights w[tap][ci] as the operand of output
 // channel 0 of a 32 -> 32 layer (channels 1-31 zero)
 __global__ void k_pack_out_weights(const float *__restrict__ W, uint8_t *__restrict__ out) {
@@ -897,73 +907,111 @@ __global__ void k_dn_transpose(const float *__restrict__ src, float *__restrict_
     }
 }
 
-// ---- tiled input and output layers -------------------------------------
-// A CTA of 128 threads takes the tile x = x0, phi = p0, p0 + 1, y = y0 ..
-// y0 + 127 (256 voxels, 2 per thread: the same y, both phi rows) and stages
-// its periodic halo (x0 +- 1, p0 - 1 .. p0 + 2, y0 - 1 .. y0 + 128) in
-// shared memory once; the 27 taps then read shared memory, and each staged
-// row serves both voxels of its thread.  The output layer stages its input
-// as 4 chunk planes of 16-byte rows, as the activation layout holds them, so
-// the copies are contiguous on both sides and a warp's 128-bit reads of one
-// plane (32 consecutive rows) are free of bank conflicts.
-constexpr int kTileY = 128, kTileP = 2, kHaloY = kTileY + 2, kHaloP = kTileP + 2;
+// ---- the input layer on the tensor cores --------------------------------
+// Input layer 1 -> 32 channels with ReLU, A1[v] = ReLU(b_in + sum_tap
+// w_in[tap] bf16(x[nbr(v, tap)])), as one GEMM per tile of 128 voxels (x,
+// phi, y0 .. y0 + 127): A[128 voxels][32] holds the input at the voxel's 27
+// taps (tap = 9 (dx+1) + 3 (dy+1) + (dphi+1)) in BF16, columns 27-31 zero;
+// B = w_in as [32 out][32 taps]; D[128][32] in tensor memory (2 MMAs of
+// K = 16).  A CTA of 128 threads stages the tile's 9 input lines with their
+// periodic y halo in shared memory, each thread builds its voxel's row of A
+// there (K-major core matrices), one thread issues the MMAs, and every warp
+// reads its 32 rows of D back for the bias, the ReLU and the BF16 store.
+// Several CTAs per SM overlap one another's staging, MMAs and stores.
+constexpr int kInThreads = 128;
+constexpr int kInCtasPerSm = 8;  // 8 x 32 tensor-memory columns per SM
 
 __device__ __forceinline__ int wrap_idx(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
-// tile coordinates of the CTA: blockIdx.x over (x, phi pairs, y chunks)
-__device__ __forceinline__ void tile_origin(Dims d, int &x0, int &p0, int &y0) {
-    const int ny_t = d.ny / kTileY, np_t = (d.np + kTileP - 1) / kTileP;
-    int b = blockIdx.x;
-    y0 = (b % ny_t) * kTileY;
-    b /= ny_t;
-    p0 = (b % np_t) * kTileP;
-    x0 = b / np_t;
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&h);
 }
 
-// input layer 1 -> 32 channels, ReLU: A1[v] = ReLU(b_in + sum_tap w_in[tap] x[nbr(v, tap)])
-// (x in the activation layout)
-__global__ void __launch_bounds__(128) k_dn_in_tiled(const float *__restrict__ x, const float *__restrict__ P,
-                                                     __nv_bfloat16 *__restrict__ A1, Dims d) {
-    __shared__ __align__(16) float sw[kTaps * kC + kC];
-    __shared__ float sx[3][kHaloP][kHaloY];
-    int x0, p0, y0;
-    tile_origin(d, x0, p0, y0);
-    for (int i = threadIdx.x; i < kTaps * kC + kC; i += blockDim.x) sw[i] = P[kOffWin + i];
-    for (int i = threadIdx.x; i < 3 * kHaloP * kHaloY; i += blockDim.x) {
-        const int ys = i % kHaloY, ip = (i / kHaloY) % kHaloP, ix = i / (kHaloY * kHaloP);
-        const int gx = wrap_idx(x0 + ix - 1, d.nx), gp = wrap_idx(p0 + ip - 1, d.np), gy = wrap_idx(y0 + ys - 1, d.ny);
-        sx[ix][ip][ys] = x[((size_t)gx * d.np + gp) * d.ny + gy];
+__global__ void __launch_bounds__(kInThreads) k_dn_in_tc(const float *__restrict__ x,
+                                                         const uint8_t *__restrict__ Wpi,
+                                                         const float *__restrict__ bias,
+                                                         __nv_bfloat16 *__restrict__ A1, Dims d,
+                                                         unsigned *__restrict__ err) {
+    __shared__ __align__(1024) uint8_t sA[kTileM * kC * 2];  // [128][32] BF16, core matrices
+    __shared__ __align__(1024) uint8_t sW[kC * kC * 2];      // [32][32] BF16, core matrices
+    __shared__ float sx[9][kTileM + 2];                      // line (dx, dphi), rows y0 - 1 .. y0 + 128
+    __shared__ float sb[kC];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tslot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < kC * kC * 2 / 16; i += kInThreads)
+        reinterpret_cast<uint4 *>(sW)[i] = reinterpret_cast<const uint4 *>(Wpi)[i];
+    if (tid < kC) sb[tid] = bias[tid];
+    const uint32_t mb = smem_u32(&mbar);
+    if (tid == 0) {
+        mbar_init(mb, 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) tmem_alloc(smem_u32(&tslot), 32);
+    fence_proxy_async();  // the weights, written by the threads, are read by the tensor core
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    const uint32_t tmem = tslot;
+    const uint64_t adesc = kBDesc | (uint64_t)((smem_u32(sA) >> 4) & 0x3FFFu);
+    const uint64_t bdesc = kBDesc | (uint64_t)((smem_u32(sW) >> 4) & 0x3FFFu);
+    constexpr uint32_t kIdesc = kIdescM128 | (4u << 17);  // N = 32
+    const int nseg = d.ny / kTileM, T = d.nx * d.np * nseg;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < T && ok; t += gridDim.x) {
+        const int p = t % d.np, y0 = ((t / d.np) % nseg) * kTileM, xx = t / (d.np * nseg);
+        for (int i = tid; i < 9 * (kTileM + 2); i += kInThreads) {
+            const int ys = i % (kTileM + 2), l = i / (kTileM + 2);
+            const int gx = wrap_idx(xx + l / 3 - 1, d.nx), gp = wrap_idx(p + l % 3 - 1, d.np);
+            sx[l][ys] = x[((size_t)gx * d.np + gp) * d.ny + wrap_idx(y0 + ys - 1, d.ny)];
+        }
+        __syncthreads();
+        // row tid of A: tap k = 9 dx + 3 dy + dphi reads line (dx, dphi) at row tid + dy
+        uint32_t w[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            float v[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int k = 2 * j + h;
+                v[h] = k < kTaps ? sx[(k / 9) * 3 + k % 3][tid + (k / 3) % 3] : 0.f;
+            }
+            w[j] = pack_bf16x2(v[0], v[1]);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            st_shared16(smem_u32(sA) + (uint32_t)core_offset(tid, 8 * c),
+                        make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]));
+        fence_proxy_async();  // the rows of A, written by the threads, are read by the tensor core
+        __syncthreads();
+        if (tid == 0) {
+            tc_after_sync();
+            mma_bf16(tmem, adesc, bdesc, kIdesc, 0u);
+            mma_bf16(tmem, adesc + (256 >> 4), bdesc + (256 >> 4), kIdesc, 1u);  // taps 16 .. 31
+            mma_commit(mb);
+        }
+        ok = __syncthreads_and(mbar_wait(mb, phase));
+        phase ^= 1u;
+        if (!ok) break;
+        tc_after_sync();
+        uint32_t r[32];
+        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), r);  // warp w: rows (voxels) 32 w ..
+        tc_before_sync();
+        float a[32];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) a[c] = fmaxf(__uint_as_float(r[c]) + sb[c], 0.f);
+        store_act32(A1, ((size_t)xx * d.np + p) * d.ny + y0 + tid, d.ny, a);
+    }
+    if (!ok && tid == 0) {
+        atomicOr(err, kErrTimeout);
+        // an MMA still in flight completes before the tensor memory is freed
+        mbar_wait(mb, phase ^ 1u);
     }
     __syncthreads();
-    const int ty = threadIdx.x;
-    float a0[32], a1[32];
-#pragma unroll
-    for (int c = 0; c < kC; ++c) a0[c] = a1[c] = sw[kTaps * kC + c];
-    for (int t = 0; t < kTaps; ++t) {
-        const int dx = t / 9, dy = (t / 3) % 3, dp = t % 3;  // tap = (dx+1) 9 + (dy+1) 3 + (dp+1)
-        const float x0v = sx[dx][dp][ty + dy], x1v = sx[dx][dp + 1][ty + dy];
-        const float4 *w4 = reinterpret_cast<const float4 *>(sw + t * kC);
-#pragma unroll
-        for (int c4 = 0; c4 < kC / 4; ++c4) {
-            const float4 w = w4[c4];
-            a0[4 * c4] = fmaf(w.x, x0v, a0[4 * c4]);
-            a0[4 * c4 + 1] = fmaf(w.y, x0v, a0[4 * c4 + 1]);
-            a0[4 * c4 + 2] = fmaf(w.z, x0v, a0[4 * c4 + 2]);
-            a0[4 * c4 + 3] = fmaf(w.w, x0v, a0[4 * c4 + 3]);
-            a1[4 * c4] = fmaf(w.x, x1v, a1[4 * c4]);
-            a1[4 * c4 + 1] = fmaf(w.y, x1v, a1[4 * c4 + 1]);
-            a1[4 * c4 + 2] = fmaf(w.z, x1v, a1[4 * c4 + 2]);
-            a1[4 * c4 + 3] = fmaf(w.w, x1v, a1[4 * c4 + 3]);
-        }
-    }
-#pragma unroll
-    for (int c = 0; c < kC; ++c) {
-        a0[c] = fmaxf(a0[c], 0.f);
-        a1[c] = fmaxf(a1[c], 0.f);
-    }
-    const int y = y0 + ty;
-    store_act32(A1, ((size_t)x0 * d.np + p0) * d.ny + y, d.ny, a0);
-    if (p0 + 1 < d.np) store_act32(A1, ((size_t)x0 * d.np + p0 + 1) * d.ny + y, d.ny, a1);
+    tc_after_sync();
+    if (warp == 0) tmem_dealloc(tmem, 32);
 }
 
 // mean-square loss against the target and its gradient dy = 2 (y - t) / V;
@@ -1093,7 +1141,7 @@ __device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
 // Weight gradients of the 1-channel layers, one tile of 128 voxels per
 // block iteration (persistent grid):
 //   OUT: dW[tap][c] += sum_v dy[v] A3[nbr(v, tap)][c]   (S = A3, sv = dy)
-//   IN:  dW[tap][c] += sum_v dZ1[v][c] x[nbr(v, tap)]   (S = dZ1, sv = x),
+//   IN:  dW[tap][c] += sum_v dZ1[v][c] bf16(x[nbr(v, tap)])   (S = dZ1, sv = x),
 //        and db[c] += sum_v dZ1[v][c]
 // Per tap the warp's 32 x 32 products are reduce-scattered to one channel
 // per lane and added into the block's shared accumulator.
@@ -1127,7 +1175,7 @@ __global__ void __launch_bounds__(128) k_dn_wgrad_c1(const __nv_bfloat16 *__rest
 #pragma unroll
                 for (int c = 0; c < kC; ++c) p[c] *= s_own;
             } else {
-                const float xs = sv[u.act(d)];
+                const float xs = __bfloat162float(__float2bfloat16_rn(sv[u.act(d)]));  // the forward's BF16 input
 #pragma unroll
                 for (int c = 0; c < kC; ++c) p[c] = own[c] * xs;
             }
@@ -1254,7 +1302,7 @@ struct ss_dn {
     // dy, yb, xa, ta: FP32 grids in the activation layout
     float *P = nullptr, *G = nullptr, *M = nullptr, *S = nullptr, *dy = nullptr, *yb = nullptr, *xa = nullptr,
           *ta = nullptr;
-    uint8_t *Wp2 = nullptr, *Wp3 = nullptr, *Wm2 = nullptr, *Wm3 = nullptr, *Wpo = nullptr;
+    uint8_t *Wp2 = nullptr, *Wp3 = nullptr, *Wm2 = nullptr, *Wm3 = nullptr, *Wpo = nullptr, *Wpi = nullptr;
     __nv_bfloat16 *A1 = nullptr, *A2 = nullptr, *A3 = nullptr, *D1 = nullptr, *D2 = nullptr;
     float *wpart = nullptr;  // the weight gradients' per-CTA partial sums
     double *sums = nullptr;
@@ -1302,7 +1350,8 @@ void pack_all(ss_dn *n, cudaStream_t s) {
     k_pack_weights<true><<<b, 256, 0, s>>>(n->P + kOffW2, n->Wm2);
     k_pack_weights<true><<<b, 256, 0, s>>>(n->P + kOffW3, n->Wm3);
     k_pack_out_weights<<<b, 256, 0, s>>>(n->P + kOffWout, n->Wpo);
-    n->launches += 5;
+    k_pack_in_weights<<<(kC * kC + 255) / 256, 256, 0, s>>>(n->P + kOffWin, n->Wpi);
+    n->launches += 6;
 }
 
 template <bool TO_ACT>
@@ -1314,8 +1363,8 @@ void transpose(ss_dn *n, const float *src, float *dst, cudaStream_t s) {
 // the network on x (histogram layout), output ya in the activation layout
 void enqueue_forward_act(ss_dn *n, const float *x, float *ya, cudaStream_t s) {
     transpose<true>(n, x, n->xa, s);
-    const unsigned tiles = (unsigned)(n->d.nx * ((n->d.np + kTileP - 1) / kTileP) * (n->d.ny / kTileY));
-    k_dn_in_tiled<<<tiles, 128, 0, s>>>(n->xa, n->P, n->A1, n->d);
+    const int tiles = n->d.nx * n->d.np * (n->d.ny / kTileM), in_grid = tiles < kInCtasPerSm * n->sms ? tiles : kInCtasPerSm * n->sms;
+    k_dn_in_tc<<<in_grid, kInThreads, 0, s>>>(n->xa, n->Wpi, n->P + kOffBin, n->A1, n->d, n->err);
     launch_conv<0>(n, n->A1, n->Wp2, n->P + kOffB2, nullptr, n->A2, s);
     launch_conv<0>(n, n->A2, n->Wp3, n->P + kOffB3, nullptr, n->A3, s);
     // the 32 -> 1 output layer on the tensor cores (BF16 weights), + the residual
@@ -1371,7 +1420,7 @@ void destroy_dn(ss_dn *n) {
     if (n->stream) cudaStreamSynchronize(n->stream);
     cudaFree(n->P); cudaFree(n->G); cudaFree(n->M); cudaFree(n->S); cudaFree(n->dy); cudaFree(n->yb);
     cudaFree(n->xa); cudaFree(n->ta);
-    cudaFree(n->Wp2); cudaFree(n->Wp3); cudaFree(n->Wm2); cudaFree(n->Wm3); cudaFree(n->Wpo);
+    cudaFree(n->Wp2); cudaFree(n->Wp3); cudaFree(n->Wm2); cudaFree(n->Wm3); cudaFree(n->Wpo); cudaFree(n->Wpi);
     cudaFree(n->A1); cudaFree(n->A2); cudaFree(n->A3); cudaFree(n->D1); cudaFree(n->D2);
     cudaFree(n->sums); cudaFree(n->err); cudaFree(n->wpart);
     if (n->own_stream && n->stream) cudaStreamDestroy(n->stream);
@@ -1412,6 +1461,7 @@ int ss_dn_create(uint32_t nx, uint32_t ny, uint32_t np, uint64_t seed, void *str
     A((void **)&n->xa, V * sizeof(float)); A((void **)&n->ta, V * sizeof(float));
     A((void **)&n->Wp2, kBAll); A((void **)&n->Wp3, kBAll); A((void **)&n->Wm2, kBAll); A((void **)&n->Wm3, kBAll);
     A((void **)&n->Wpo, kBAll);
+    A((void **)&n->Wpi, kC * kC * 2);
     A((void **)&n->A1, ab); A((void **)&n->A2, ab); A((void **)&n->A3, ab); A((void **)&n->D1, ab);
     A((void **)&n->D2, ab);
     A((void **)&n->sums, 2 * sizeof(double)); A((void **)&n->err, sizeof(unsigned));

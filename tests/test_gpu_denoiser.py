@@ -132,8 +132,8 @@ def test_conv32_rejects_bad_shapes():
 
 # ---------------------------------------------------------------- the network
 def _ref_net(torch, x, P, ste=False):
-    """The denoiser in torch fp32 with the kernel's BF16 roundings (weights
-    of the 32->32 layers and of the output layer, the three activations)."""
+    """The denoiser in torch fp32 with the kernel's BF16 roundings (the input
+    of the first layer, the weights of every layer, the three activations)."""
     import torch.nn.functional as F
     from stochasticsampling_gb300.denoiser import split_params
     p = {k: torch.as_tensor(v.copy()) for k, v in split_params(P).items()}
@@ -146,7 +146,7 @@ def _ref_net(torch, x, P, ste=False):
         wt = w.reshape(3, 3, 3, w.shape[1], w.shape[2]).permute(3, 4, 0, 1, 2)
         return F.conv3d(F.pad(a[None], (1, 1, 1, 1, 1, 1), mode="circular"), wt, b)[0]
 
-    a1 = bf(torch.relu(conv(x[None], p["w_in"][:, :, None], p["b_in"])))
+    a1 = bf(torch.relu(conv(bf(x)[None], bf(p["w_in"])[:, :, None], p["b_in"])))
     a2 = bf(torch.relu(conv(a1, bf(p["w2"]), p["b2"])))
     a3 = bf(torch.relu(conv(a2, bf(p["w3"]), p["b3"])))
     return x + conv(a3, bf(p["w_out"])[:, None, :], p["b_out"])[0], p
@@ -208,7 +208,7 @@ def test_denoiser_gradients_match_torch(shape, w):
 
     lt = 0.0
     for b in range(2):
-        a1 = bf(torch.relu(conv(x[b][None], P_t["w_in"][:, :, None], P_t["b_in"])))
+        a1 = bf(torch.relu(conv(bf(x[b])[None], bf(P_t["w_in"])[:, :, None], P_t["b_in"])))
         a2 = bf(torch.relu(conv(a1, bf(P_t["w2"]), P_t["b2"])))
         a3 = bf(torch.relu(conv(a2, bf(P_t["w3"]), P_t["b3"])))
         yb = x[b] + conv(a3, bf(P_t["w_out"])[:, None, :], P_t["b_out"])[0]
