@@ -364,9 +364,9 @@ int ss_dn_conv32(const void *x, const float *w, const float *bias, const void *r
 /* The denoiser network: input x (the histogram divided by its mean count,
  * DEVICE float [nx][ny][np]) -> conv 1->32 + ReLU -> conv 32->32 + ReLU ->
  * conv 32->32 + ReLU -> conv 32->1 -> y = x + that (DEVICE float).  All
- * convolutions 3x3x3 with periodic padding; the 32->32 ones on the tensor
- * cores (BF16 weights and activations, FP32 accumulation), the others on the
- * CUDA cores in FP32.  57,121 FP32 parameters: w_in[27][32], b_in[32],
+ * convolutions 3x3x3 with periodic padding, all on the tensor cores with
+ * BF16 weights, BF16 inputs and activations and FP32 accumulation (the
+ * residual x and the biases stay FP32).  57,121 FP32 parameters: w_in[27][32], b_in[32],
  * w2[27][32][32], b2[32], w3[27][32][32], b3[32], w_out[27][32], b_out
  * (w[tap][out][in], tap as for ss_dn_conv32).  Trained with Adam on the
  * mean-square error against a target distribution. */
