@@ -59,17 +59,17 @@ def _particles_out(settings, sim):
     return sim.get_particles()
 
 
-def _copy(a, pool):
+def _copy(a, pool, nthreads):
     """A copy of the C-contiguous host array a; one of more than 16 MB is
-    copied in row blocks on the pool's threads (numpy releases the GIL while
-    it copies), so that the particle rows of an output do not hold up the
-    loop for long."""
+    copied in nthreads row blocks on the pool's threads (numpy releases the
+    GIL while it copies), so that the particle rows of an output do not hold
+    up the loop for long."""
     out = np.empty_like(a)
-    if pool is None or a.nbytes < (16 << 20) or a.shape[0] < 2:
+    if pool is None or nthreads < 2 or a.nbytes < (16 << 20) or a.shape[0] < 2:
         np.copyto(out, a)
         return out
     rows = a.shape[0]
-    step = -(-rows // pool._max_workers)
+    step = -(-rows // nthreads)
     list(pool.map(lambda i: np.copyto(out[i:i + step], a[i:i + step]), range(0, rows, step)))
     return out
 
@@ -90,7 +90,8 @@ class _OverlappedOutputs:
         self.bufs = sim.output_buffers
         self.pending = [None, None]
         self.k = 0
-        self.pool = ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
+        self.nthreads = max(1, min(16, os.cpu_count() or 1))
+        self.pool = ThreadPoolExecutor(max_workers=self.nthreads)
 
     def _array(self, slot, name, shape):
         """The slot's host buffer `name`: the first shape[0] rows of a
@@ -125,14 +126,16 @@ class _OverlappedOutputs:
         self.pending[slot] = None
         self.sim.output_wait(slot)
         b = self.bufs[slot]
-        d = io.distribution_record(_copy(b["dist"].array, self.pool), self.sim.grid, self.sim.box) if dist else None
-        f = _copy(b["flow"].array, self.pool) if flow else None
-        m = _copy(b["mag"].array, self.pool) if mag else None
-        p = _copy(b["rows"].array[:parts_n], self.pool) if parts_n is not None else None
+        def cp(a):
+            return _copy(a, self.pool, self.nthreads)
+        d = io.distribution_record(cp(b["dist"].array), self.sim.grid, self.sim.box) if dist else None
+        f = cp(b["flow"].array) if flow else None
+        m = cp(b["mag"].array) if mag else None
+        p = cp(b["rows"].array[:parts_n]) if parts_n is not None else None
         if d is not None or f is not None or p is not None:
             self.out.append(io.output_entry(timestep, d, f, m, p))
         if snapshot:
-            self.out.write_snapshot(io.snapshot_record(_copy(b["rows"].array[:self.sim.n], self.pool), timestep))
+            self.out.write_snapshot(io.snapshot_record(cp(b["rows"].array[:self.sim.n]), timestep))
 
     def finish(self):
         for _, slot in sorted((p[0], s) for s, p in enumerate(self.pending) if p is not None):
