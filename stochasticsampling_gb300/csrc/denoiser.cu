@@ -119,6 +119,9 @@ struct Vox {
     __device__ __forceinline__ int act(Dims d) const { return (x * d.np + p) * d.ny + y; }
 };
 
+// i in [-n, 2n) wrapped into [0, n)
+__device__ __forceinline__ int wrap_idx(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
 // ---- PTX wrappers ------------------------------------------------------
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 __device__ __forceinline__ void mbar_init(uint32_t addr, uint32_t count) {
@@ -767,6 +770,146 @@ __global__ void __launch_bounds__(kWgThreads, 1) k_dn_wgrad_tc(const __nv_bfloat
     if (warp == 1) tmem_dealloc(tmem, 512);
 }
 
+// Weight gradients of the 1-channel layers on the tensor cores.  Per tile of
+// 128 voxels (x, phi, y0 .. y0 + 127) one GEMM over the voxels,
+//   D[r][c] += sum_v A[r][v] B[c][v],
+// A[tap][v] the 1-channel operand at the voxel's tap (BF16, K-major; row 27
+// all ones, rows 28-127 zero), B the 32-channel operand at the tile's voxels
+// (its 4 chunk planes, MN-major as the activation layout holds them):
+//   input layer (MIRROR false): A = bf16(x) at v + s_tap, B = dZ1: dW_in, and
+//     the ones row gives db_in;
+//   output layer (MIRROR true): A = bf16(dy) at v - s_tap, B = A3: dW_out
+//     (sum_v dy[v] A3[v + s_tap] = sum_u dy[u - s_tap] A3[u]).
+// The accumulator stays in tensor memory over the CTA's tiles; each CTA
+// writes its 28 x 32 partial sums (element-major: partial[e][cta]) and
+// k_dn_wgrad1_reduce adds the CTAs' partials in a fixed order.
+constexpr int kW1Threads = 128;
+constexpr int kW1CtasPerSm = 4;
+constexpr int kW1Rows = kTaps + 1;                    // 27 taps + the ones row
+constexpr int kW1Partial = kW1Rows * kC;
+constexpr int kW1ABytes = kTileM * kTileM * 2;       // A: 128 x 128 BF16
+constexpr int kW1BBytes = 4 * kBodyBytes;            // B: 4 chunk planes of 128 voxels
+constexpr int kW1Smem = 1024 + kW1ABytes + kW1BBytes + 9 * (kTileM + 2) * 4 + 64;
+// A K-major (8-row groups 2048 B apart, K core matrices 128 B apart); B MN-major as in k_dn_wgrad_tc
+constexpr uint64_t kAW1 = ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(2048 >> 4) << 32) | (1ull << 46);
+constexpr uint64_t kBW1 = ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(kBodyBytes >> 4) << 32) | (1ull << 46);
+constexpr uint32_t kIdescW1 = kIdescM128 | (4u << 17) | (1u << 16);  // N = 32, B MN-major
+
+__device__ __forceinline__ uint32_t w1_a_offset(int row, int v) {
+    return (uint32_t)((row >> 3) * 2048 + (v >> 3) * 128 + (row & 7) * 16 + (v & 7) * 2);
+}
+
+template <bool MIRROR>
+__global__ void __launch_bounds__(kW1Threads) k_dn_wgrad1_tc(const float *__restrict__ s1,
+                                                             const __nv_bfloat16 *__restrict__ S32,
+                                                             float *__restrict__ partial, Dims d,
+                                                             unsigned *__restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t sA0 = (raw + 1023u) & ~1023u;
+    uint8_t *const sA = smem_raw + (sA0 - raw);
+    const uint32_t sB0 = sA0 + kW1ABytes;
+    float *const sx = reinterpret_cast<float *>(sA + kW1ABytes + kW1BBytes);  // 9 lines x (128 + 2)
+    const uint32_t mb = sB0 + kW1BBytes + 9 * (kTileM + 2) * 4;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(sA + (mb - sA0) + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // rows 27 .. 127 of A once: the ones row, then zeros
+    for (int i = tid; i < (kTileM - kTaps) * kTileM; i += kW1Threads) {
+        const int row = kTaps + i / kTileM, v = i % kTileM;
+        *reinterpret_cast<__nv_bfloat16 *>(sA + w1_a_offset(row, v)) =
+            __float2bfloat16_rn(row == kTaps ? 1.f : 0.f);
+    }
+    if (tid == 0) {
+        mbar_init(mb, 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) tmem_alloc(smem_u32(tslot), 32);
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint64_t adesc = kAW1 | (uint64_t)((sA0 >> 4) & 0x3FFFu);
+    const uint64_t bdesc = kBW1 | (uint64_t)((sB0 >> 4) & 0x3FFFu);
+    const int nseg = d.ny / kTileM, T = d.nx * d.np * nseg;
+    uint32_t phase = 0, acc = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < T && ok; t += gridDim.x) {
+        const int p = t % d.np, y0 = ((t / d.np) % nseg) * kTileM, xx = t / (d.np * nseg);
+        // the 1-channel operand's 9 lines (dx, dphi) over y0 - 1 .. y0 + 128
+        for (int i = tid; i < 9 * (kTileM + 2); i += kW1Threads) {
+            const int ys = i % (kTileM + 2), l = i / (kTileM + 2);
+            const int gx = wrap_idx(xx + l / 3 - 1, d.nx), gp = wrap_idx(p + l % 3 - 1, d.np);
+            sx[l * (kTileM + 2) + ys] = s1[((size_t)gx * d.np + gp) * d.ny + wrap_idx(y0 + ys - 1, d.ny)];
+        }
+        // B: the 32-channel operand's 4 chunk planes at the tile's voxels
+        const size_t line = (size_t)xx * d.np + p;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const uint4 u = *reinterpret_cast<const uint4 *>(S32 + ((line * 4 + c) * d.ny + y0 + tid) * 8);
+            st_shared16(sB0 + (uint32_t)(c * kBodyBytes + tid * 16), u);
+        }
+        __syncthreads();
+        // A rows 0 .. 26, column tid: tap k = 9 dx + 3 dy + dphi
+#pragma unroll
+        for (int k = 0; k < kTaps; ++k) {
+            const int dx = k / 9, dy = (k / 3) % 3, dp = k % 3;
+            const float v = MIRROR ? sx[((2 - dx) * 3 + (2 - dp)) * (kTileM + 2) + tid + 2 - dy]
+                                   : sx[(dx * 3 + dp) * (kTileM + 2) + tid + dy];
+            *reinterpret_cast<__nv_bfloat16 *>(sA + w1_a_offset(k, tid)) = __float2bfloat16_rn(v);
+        }
+        fence_proxy_async();  // A and B, written by the threads, are read by the tensor core
+        __syncthreads();
+        if (tid == 0) {
+            tc_after_sync();
+#pragma unroll
+            for (int kk = 0; kk < kTileM / 16; ++kk) {
+                mma_bf16(tmem, adesc + (uint64_t)(kk * 256 >> 4), bdesc + (uint64_t)(kk * 256 >> 4), kIdescW1, acc);
+                acc = 1u;
+            }
+            mma_commit(mb);
+        }
+        acc = 1u;
+        ok = __syncthreads_and(mbar_wait(mb, phase));
+        phase ^= 1u;
+    }
+    if (!ok && tid == 0) {
+        atomicOr(err, kErrTimeout);
+        mbar_wait(mb, phase ^ 1u);  // an MMA still in flight completes before the tensor memory is freed
+    }
+    tc_after_sync();
+    if (warp == 0) {  // rows 0 .. 27 lie in tensor-memory lanes 0 .. 27
+        uint32_t r[32];
+        tmem_ld32(tmem, r);
+        if (lane < kW1Rows) {
+            const bool any = (int)blockIdx.x < T;  // a CTA without tiles leaves its accumulator unwritten
+#pragma unroll
+            for (int c = 0; c < kC; ++c)
+                partial[(size_t)(lane * kC + c) * gridDim.x + blockIdx.x] = any ? __uint_as_float(r[c]) : 0.f;
+        }
+    }
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    if (warp == 0) tmem_dealloc(tmem, 32);
+}
+
+// dW[e] (e < 27 x 32) and db[e - 864] (the ones row) += the sum over the CTAs
+// of partial[e][cta]: one warp per element, lane l adding the CTAs l, l + 32,
+// ... in order, then a fixed shuffle tree (the same order every run)
+__global__ void k_dn_wgrad1_reduce(const float *__restrict__ partial, int ncta, float *__restrict__ dW,
+                                   float *__restrict__ db) {
+    const int e = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (e >= kW1Partial) return;
+    float s = 0.f;
+    for (int c = lane; c < ncta; c += 32) s += partial[(size_t)e * ncta + c];
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        if (e < kTaps * kC) dW[e] += s;
+        else if (db) db[e - kTaps * kC] += s;
+    }
+}
+
 // dW[e] += sum over the CTAs c of partial[c][e], in the order c = 0, 1, ...
 // (e < 27 x 32 x 32: the weights, then the 32 biases)
 __global__ void k_dn_wgrad_reduce(const float *__restrict__ partial, int ncta, float *__restrict__ dW,
@@ -920,8 +1063,6 @@ __global__ void k_dn_transpose(const float *__restrict__ src, float *__restrict_
 // Several CTAs per SM overlap one another's staging, MMAs and stores.
 constexpr int kInThreads = 128;
 constexpr int kInCtasPerSm = 8;  // 8 x 32 tensor-memory columns per SM
-
-__device__ __forceinline__ int wrap_idx(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
     __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
@@ -1119,72 +1260,6 @@ __global__ void __launch_bounds__(128) k_dn_out_bwd(const float *__restrict__ dy
 #pragma unroll
     for (int c = 0; c < kC; ++c) g[c] = a[c] > 0.f ? g[c] : 0.f;
     store_act32(dZ3, (size_t)u, d.ny, g);
-}
-
-// Reduce-scatter across a warp: each lane holds v[0..31]; afterwards lane l
-// holds the sum over the warp of v[l] (31 shuffles instead of 32 x 5).
-__device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int half = 16; half >= 1; half >>= 1) {
-        const bool up = (lane & half) != 0;
-#pragma unroll
-        for (int j = 0; j < half; ++j) {
-            const float send = up ? v[j] : v[j + half];
-            const float keep = up ? v[j + half] : v[j];
-            v[j] = keep + __shfl_xor_sync(0xffffffffu, send, half);
-        }
-    }
-    return v[0];
-}
-
-// Weight gradients of the 1-channel layers, one tile of 128 voxels per
-// block iteration (persistent grid):
-//   OUT: dW[tap][c] += sum_v dy[v] A3[nbr(v, tap)][c]   (S = A3, sv = dy)
-//   IN:  dW[tap][c] += sum_v dZ1[v][c] bf16(x[nbr(v, tap)])   (S = dZ1, sv = x),
-//        and db[c] += sum_v dZ1[v][c]
-// Per tap the warp's 32 x 32 products are reduce-scattered to one channel
-// per lane and added into the block's shared accumulator.
-template <bool OUT>
-__global__ void __launch_bounds__(128) k_dn_wgrad_c1(const __nv_bfloat16 *__restrict__ S, const float *__restrict__ sv,
-                                                     float *__restrict__ dW, float *__restrict__ db, Dims d,
-                                                     int ntiles) {
-    __shared__ float acc[kTaps * kC + kC];
-    const int tid = threadIdx.x, lane = tid & 31;
-    for (int i = tid; i < kTaps * kC + kC; i += blockDim.x) acc[i] = 0.f;
-    __syncthreads();
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int v = tile * kTileM + tid;  // activation index
-        const Vox vx = Vox::from_act(v, d);
-        float own[32];
-        float s_own = 0.f;
-        if (OUT) {
-            s_own = sv[v];
-        } else {
-            load_act32(S, (size_t)v, d.ny, own);
-            float t[32];
-#pragma unroll
-            for (int c = 0; c < kC; ++c) t[c] = own[c];
-            atomicAdd(&acc[kTaps * kC + lane], warp_reduce_scatter32(t));
-        }
-        for (int tap = 0; tap < kTaps; ++tap) {
-            const Vox u = vx.moved(tap, d);
-            float p[32];
-            if (OUT) {
-                load_act32(S, (size_t)u.act(d), d.ny, p);
-#pragma unroll
-                for (int c = 0; c < kC; ++c) p[c] *= s_own;
-            } else {
-                const float xs = __bfloat162float(__float2bfloat16_rn(sv[u.act(d)]));  // the forward's BF16 input
-#pragma unroll
-                for (int c = 0; c < kC; ++c) p[c] = own[c] * xs;
-            }
-            atomicAdd(&acc[tap * kC + lane], warp_reduce_scatter32(p));
-        }
-    }
-    __syncthreads();
-    for (int i = tid; i < kTaps * kC; i += blockDim.x) atomicAdd(&dW[i], acc[i]);
-    if (!OUT && tid < kC) atomicAdd(&db[tid], acc[kTaps * kC + tid]);
 }
 
 // Adam (Kingma and Ba, 2015) on the FP32 parameters
@@ -1395,15 +1470,21 @@ void enqueue_backward(ss_dn *n, const float *t, const float *ya, cudaStream_t s,
         k_dn_wgrad_tc<<<wgrid, kWgThreads, kSmemWg, s>>>(dZ, A, n->wpart, n->d, n->err);
         k_dn_wgrad_reduce<<<(kWgPartial + 255) / 256, 256, 0, s>>>(n->wpart, wgrid, dW, db);
     };
-    const unsigned pg = (unsigned)(n->ntiles < 8 * n->sms ? n->ntiles : 8 * n->sms);
+    // the 1-channel layers' weight gradients on the tensor cores, fixed-order sums over the CTAs
+    const int w1grid = n->ntiles < kW1CtasPerSm * n->sms ? n->ntiles : kW1CtasPerSm * n->sms;
+    auto wgrad1 = [&](bool out_layer, float *dW, float *db) {
+        if (out_layer) k_dn_wgrad1_tc<true><<<w1grid, kW1Threads, kW1Smem, s>>>(n->dy, n->A3, n->wpart, n->d, n->err);
+        else k_dn_wgrad1_tc<false><<<w1grid, kW1Threads, kW1Smem, s>>>(n->xa, n->D1, n->wpart, n->d, n->err);
+        k_dn_wgrad1_reduce<<<(kW1Partial * 32 + 255) / 256, 256, 0, s>>>(n->wpart, w1grid, dW, db);
+    };
     k_dn_out_bwd<<<b, 128, 0, s>>>(n->dy, n->P, n->A3, n->D1, n->d, n->nvox);
-    k_dn_wgrad_c1<true><<<pg, 128, 0, s>>>(n->A3, n->dy, n->G + kOffWout, nullptr, n->d, n->ntiles);
+    wgrad1(true, n->G + kOffWout, nullptr);
     wgrad(n->D1, n->A2, n->G + kOffW3, n->G + kOffB3);
     launch_conv<2>(n, n->D1, n->Wm3, nullptr, n->A2, n->D2, s);
     wgrad(n->D2, n->A1, n->G + kOffW2, n->G + kOffB2);
     launch_conv<2>(n, n->D2, n->Wm2, nullptr, n->A1, n->D1, s);
-    k_dn_wgrad_c1<false><<<pg, 128, 0, s>>>(n->D1, n->xa, n->G + kOffWin, n->G + kOffBin, n->d, n->ntiles);
-    n->launches += 10;
+    wgrad1(false, n->G + kOffWin, n->G + kOffBin);
+    n->launches += 12;
 }
 
 int check_err(ss_dn *n) {
