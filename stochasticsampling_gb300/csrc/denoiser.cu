@@ -5,31 +5,38 @@
 //
 // Activations are BF16 in the layout [x][phi][4 chunks][y][8 channels]:
 // along a line (x, phi) each 8-channel chunk is a contiguous plane of ny
-// rows of 16 B, so the 128 voxels of one tile are four 2 KB blocks.  The
-// 32 -> 32 convolutions are implicit GEMMs on the 5th-generation tensor
-// cores: per tile (x, phi, 128 consecutive y), D[128 x 32] = sum over the 27
-// taps of A_tap[128 x 32] W_tap[32 x 32]^T, BF16 operands in shared memory,
-// FP32 accumulator in tensor memory, one elected thread issuing tcgen05.mma.
-// A CTA walks along phi through its runs of tiles and loads each input line
-// (x + dx, phi) once per run (with one halo row at either end, periodic in
-// y) into a ring of 18 line buffers; the 27 taps are descriptor offsets into
-// those lines (the y shift is a 16-byte row offset).  The 3 lines of one
-// input position feed the output tiles phi - 1, phi and phi + 1, so each
-// (dx, dy, K half) is one MMA of M = 128, N = 96 (K = 16) with the three
-// dphi taps' weights stacked along N.  The kernel is warp-specialised: one
-// thread streams the lines with bulk copies, one thread issues the MMAs into
-// a ring of 8 accumulators in tensor memory, and four warps drain finished
-// accumulators with tcgen05.ld (one voxel's 32 channels per thread), add the
-// bias and apply ReLU (or the ReLU derivative of a reference tensor, for the
-// backward pass) while the next positions' MMAs run.
+// rows of 16 B, so the 128 voxels of one tile are four 2 KB blocks.  Every
+// layer runs on the 5th-generation tensor cores (BF16 operands in shared
+// memory, FP32 accumulators in tensor memory):
+//  - k_conv32: the 32 -> 32 convolutions (and, with the weights of output
+//    channel 0 alone, the 32 -> 1 output layer) as implicit GEMMs.  A tile
+//    is two output rows (x, x + 1) x 128 y at one phi; a CTA walks along phi
+//    through its runs of tiles; each input position (the 4 lines x - 1 ..
+//    x + 2 at one phi, with one halo row at either end, periodic in y) lands
+//    in a ring of position buffers by bulk copies from a producer warp, and
+//    the taps are descriptor offsets into those lines (the y shift is a
+//    16-byte row offset).  A position feeds the output tiles phi - 1, phi and
+//    phi + 1, so each (row, dx, dy, K half) is one MMA of M = 128, N = 96
+//    (K = 16) with the three dphi taps' weights stacked along N.  The MMA
+//    warp runs its loop warp-uniformly with one elected lane issuing into
+//    two rings of 8 accumulators; eight epilogue warps drain finished
+//    accumulators with tcgen05.ld (one voxel's 32 channels per thread) and
+//    apply bias and ReLU, the ReLU derivative of a reference tensor (the
+//    backward pass) or the residual (the output layer).
+//  - k_dn_in_tc: the 1 -> 32 input layer, one small GEMM per tile with the
+//    27 taps as K; k_dn_wgrad_tc / k_dn_wgrad1_tc: the weight gradients, GEMMs
+//    over the voxels with the accumulators resident in tensor memory and
+//    fixed-order sums over the CTAs.
+// The CUDA cores keep the layout transposes, the output layer's backward,
+// the loss, Adam and the weight packing.
 //
-// Shared-memory operand layouts (K-major, no swizzle).  A line: for each of
+// Shared-memory operand layouts (no swizzle).  A line (K-major): for each of
 // its 4 K chunks (8 channels, 16 bytes) the rows at a 16-byte stride, so row
 // groups are 128 B apart (stride offset) and K chunks 2176 B (leading
-// offset).  Weights: per tap 32 rows x 4 chunks in 8 x 16 B core matrices,
-// leading offset 128 B, stride offset 512 B.  Every wait is bounded: on a
-// timeout the kernel records an error, waits for its own copies and MMAs,
-// frees its tensor memory and returns.
+// offset).  Weights (K-major): per tap 32 rows x 4 chunks in 8 x 16 B core
+// matrices, leading offset 128 B, stride offset 512 B.  Every wait is
+// bounded: on a timeout a kernel records an error, waits for its own copies
+// and MMAs, frees its tensor memory and returns.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
