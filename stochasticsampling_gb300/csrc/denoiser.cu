@@ -107,25 +107,6 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-// A voxel (x, y, p) and its linear index in the activation layout
-// [x][phi][y] (every internal grid; the network's input and output are in
-// the histogram layout [x][y][phi], converted by k_dn_transpose).
-// moved(tap) is the periodic neighbour at tap = (dx + 1) 9 + (dy + 1) 3 + (dp + 1).
-struct Vox {
-    int x, y, p;
-    __device__ __forceinline__ static Vox from_act(int a, Dims d) {
-        return Vox{a / (d.ny * d.np), a % d.ny, (a / d.ny) % d.np};
-    }
-    __device__ __forceinline__ Vox moved(int tap, Dims d) const {
-        int a = x + tap / 9 - 1, b = y + (tap / 3) % 3 - 1, c = p + tap % 3 - 1;
-        a = a < 0 ? a + d.nx : (a >= d.nx ? a - d.nx : a);
-        b = b < 0 ? b + d.ny : (b >= d.ny ? b - d.ny : b);
-        c = c < 0 ? c + d.np : (c >= d.np ? c - d.np : c);
-        return Vox{a, b, c};
-    }
-    __device__ __forceinline__ int act(Dims d) const { return (x * d.np + p) * d.ny + y; }
-};
-
 // i in [-n, 2n) wrapped into [0, n)
 __device__ __forceinline__ int wrap_idx(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
@@ -946,12 +927,14 @@ __global__ void k_pack_weights(const float *__restrict__ W, uint8_t *__restrict_
 }
 
 // the 1 -> 32 input layer's weights w[tap][co] as the B operand [32 co][32 taps]
-// of its GEMM (taps 27-31 zero)
+// of its GEMM (taps 27-31 zero); MIRROR: tap k holds w[26 - k] (the output
+// layer's weights for its backward through the same GEMM)
+template <bool MIRROR>
 __global__ void k_pack_in_weights(const float *__restrict__ W, uint8_t *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kC * kC) return;
     const int n = i / kC, k = i % kC;
-    const float w = k < kTaps ? W[k * kC + n] : 0.f;
+    const float w = k < kTaps ? W[(MIRROR ? kTaps - 1 - k : k) * kC + n] : 0.f;
     *reinterpret_cast<__nv_bfloat16 *>(out + core_offset(n, k)) = __float2bfloat16_rn(w);
 }
 
@@ -1022,20 +1005,6 @@ __device__ __forceinline__ void store_act32(__nv_bfloat16 *A, size_t v, int ny, 
         *reinterpret_cast<uint4 *>(A + at0 + c * plane) = make_uint4(q[0], q[1], q[2], q[3]);
     }
 }
-__device__ __forceinline__ void load_act32(const __nv_bfloat16 *A, size_t v, int ny, float (&a)[32]) {
-    const size_t at0 = act_at(v, 0, ny), plane = (size_t)ny * 8;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        const uint4 u = *reinterpret_cast<const uint4 *>(A + at0 + c * plane);
-        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162 *>(&w[j]);
-            a[8 * c + 2 * j] = __low2float(h);
-            a[8 * c + 2 * j + 1] = __high2float(h);
-        }
-    }
-}
 
 // FP32 grids between the histogram layout [x][y][phi] and the activation
 // layout [x][phi][y]: per plane x a transpose in 32 x 32 tiles
@@ -1068,6 +1037,10 @@ __global__ void k_dn_transpose(const float *__restrict__ src, float *__restrict_
 // there (K-major core matrices), one thread issues the MMAs, and every warp
 // reads its 32 rows of D back for the bias, the ReLU and the BF16 store.
 // Several CTAs per SM overlap one another's staging, MMAs and stores.
+// BWD: the output layer's backward into its input with the same GEMM,
+// dZ3[u][c] = (sum_tap w_out[tap][c] dy[nbr(u, 26 - tap)]) * (A3[u][c] > 0):
+// the input is dy, B the output weights at the mirrored taps (w_out[26 - k]
+// for tap k), and the epilogue applies ReLU'(A3) (ref) instead of bias and ReLU.
 constexpr int kInThreads = 128;
 constexpr int kInCtasPerSm = 8;  // 8 x 32 tensor-memory columns per SM
 
@@ -1076,9 +1049,12 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
     return *reinterpret_cast<uint32_t *>(&h);
 }
 
-__global__ void __launch_bounds__(kInThreads) k_dn_in_tc(const float *__restrict__ x,
+// (the backward's epilogue needs more registers: 6 blocks per SM instead of 8, no spills)
+template <bool BWD>
+__global__ void __launch_bounds__(kInThreads, BWD ? 6 : kInCtasPerSm) k_dn_in_tc(const float *__restrict__ x,
                                                          const uint8_t *__restrict__ Wpi,
                                                          const float *__restrict__ bias,
+                                                         const __nv_bfloat16 *__restrict__ ref,
                                                          __nv_bfloat16 *__restrict__ A1, Dims d,
                                                          unsigned *__restrict__ err) {
     __shared__ __align__(1024) uint8_t sA[kTileM * kC * 2];  // [128][32] BF16, core matrices
@@ -1090,7 +1066,7 @@ __global__ void __launch_bounds__(kInThreads) k_dn_in_tc(const float *__restrict
     const int tid = threadIdx.x, warp = tid >> 5;
     for (int i = tid; i < kC * kC * 2 / 16; i += kInThreads)
         reinterpret_cast<uint4 *>(sW)[i] = reinterpret_cast<const uint4 *>(Wpi)[i];
-    if (tid < kC) sb[tid] = bias[tid];
+    if (!BWD && tid < kC) sb[tid] = bias[tid];
     const uint32_t mb = smem_u32(&mbar);
     if (tid == 0) {
         mbar_init(mb, 1);
@@ -1148,9 +1124,25 @@ __global__ void __launch_bounds__(kInThreads) k_dn_in_tc(const float *__restrict
         tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), r);  // warp w: rows (voxels) 32 w ..
         tc_before_sync();
         float a[32];
+        const size_t line = (size_t)xx * d.np + p;
+        if (BWD) {
+            // ReLU'(A3) at this voxel: its 4 chunk planes, two BF16 channels per word
 #pragma unroll
-        for (int c = 0; c < kC; ++c) a[c] = fmaxf(__uint_as_float(r[c]) + sb[c], 0.f);
-        store_act32(A1, ((size_t)xx * d.np + p) * d.ny + y0 + tid, d.ny, a);
+            for (int c = 0; c < 4; ++c) {
+                const uint4 u = *reinterpret_cast<const uint4 *>(ref + ((line * 4 + c) * d.ny + y0 + tid) * 8);
+                const uint32_t w4[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    a[8 * c + 2 * j] = __uint_as_float(w4[j] << 16) > 0.f ? __uint_as_float(r[8 * c + 2 * j]) : 0.f;
+                    a[8 * c + 2 * j + 1] =
+                        __uint_as_float(w4[j] & 0xFFFF0000u) > 0.f ? __uint_as_float(r[8 * c + 2 * j + 1]) : 0.f;
+                }
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < kC; ++c) a[c] = fmaxf(__uint_as_float(r[c]) + sb[c], 0.f);
+        }
+        store_act32(A1, line * d.ny + y0 + tid, d.ny, a);
     }
     if (!ok && tid == 0) {
         atomicOr(err, kErrTimeout);
@@ -1242,32 +1234,6 @@ __global__ void k_dn_loss_moment(const float *__restrict__ y, const float *__res
     }
 }
 
-// backward of the output layer into its input: dZ3[u][c] = (sum_tap
-// w_out[tap][c] dy[nbr(u, 26 - tap)]) * (A3[u][c] > 0)
-__global__ void __launch_bounds__(128) k_dn_out_bwd(const float *__restrict__ dy, const float *__restrict__ P,
-                                                    const __nv_bfloat16 *__restrict__ A3,
-                                                    __nv_bfloat16 *__restrict__ dZ3, Dims d, int nvox) {
-    __shared__ float sw[kTaps * kC];
-    // the weights the forward used (BF16, on the tensor cores)
-    for (int i = threadIdx.x; i < kTaps * kC; i += blockDim.x) sw[i] = __bfloat162float(__float2bfloat16_rn(P[kOffWout + i]));
-    __syncthreads();
-    const int u = blockIdx.x * blockDim.x + threadIdx.x;  // activation index
-    if (u >= nvox) return;
-    const Vox vx = Vox::from_act(u, d);
-    float g[32];
-#pragma unroll
-    for (int c = 0; c < kC; ++c) g[c] = 0.f;
-    for (int t = 0; t < kTaps; ++t) {
-        const float dv = dy[vx.moved(kTaps - 1 - t, d).act(d)];
-#pragma unroll
-        for (int c = 0; c < kC; ++c) g[c] = fmaf(sw[t * kC + c], dv, g[c]);
-    }
-    float a[32];
-    load_act32(A3, (size_t)u, d.ny, a);
-#pragma unroll
-    for (int c = 0; c < kC; ++c) g[c] = a[c] > 0.f ? g[c] : 0.f;
-    store_act32(dZ3, (size_t)u, d.ny, g);
-}
 
 // Adam (Kingma and Ba, 2015) on the FP32 parameters
 __global__ void k_dn_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
@@ -1384,7 +1350,7 @@ struct ss_dn {
     // dy, yb, xa, ta: FP32 grids in the activation layout
     float *P = nullptr, *G = nullptr, *M = nullptr, *S = nullptr, *dy = nullptr, *yb = nullptr, *xa = nullptr,
           *ta = nullptr;
-    uint8_t *Wp2 = nullptr, *Wp3 = nullptr, *Wm2 = nullptr, *Wm3 = nullptr, *Wpo = nullptr, *Wpi = nullptr;
+    uint8_t *Wp2 = nullptr, *Wp3 = nullptr, *Wm2 = nullptr, *Wm3 = nullptr, *Wpo = nullptr, *Wpi = nullptr, *Wpob = nullptr;
     __nv_bfloat16 *A1 = nullptr, *A2 = nullptr, *A3 = nullptr, *D1 = nullptr, *D2 = nullptr;
     float *wpart = nullptr;  // the weight gradients' per-CTA partial sums
     double *sums = nullptr;
@@ -1432,8 +1398,9 @@ void pack_all(ss_dn *n, cudaStream_t s) {
     k_pack_weights<true><<<b, 256, 0, s>>>(n->P + kOffW2, n->Wm2);
     k_pack_weights<true><<<b, 256, 0, s>>>(n->P + kOffW3, n->Wm3);
     k_pack_out_weights<<<b, 256, 0, s>>>(n->P + kOffWout, n->Wpo);
-    k_pack_in_weights<<<(kC * kC + 255) / 256, 256, 0, s>>>(n->P + kOffWin, n->Wpi);
-    n->launches += 6;
+    k_pack_in_weights<false><<<(kC * kC + 255) / 256, 256, 0, s>>>(n->P + kOffWin, n->Wpi);
+    k_pack_in_weights<true><<<(kC * kC + 255) / 256, 256, 0, s>>>(n->P + kOffWout, n->Wpob);
+    n->launches += 7;
 }
 
 template <bool TO_ACT>
@@ -1446,7 +1413,7 @@ void transpose(ss_dn *n, const float *src, float *dst, cudaStream_t s) {
 void enqueue_forward_act(ss_dn *n, const float *x, float *ya, cudaStream_t s) {
     transpose<true>(n, x, n->xa, s);
     const int tiles = n->d.nx * n->d.np * (n->d.ny / kTileM), in_grid = tiles < kInCtasPerSm * n->sms ? tiles : kInCtasPerSm * n->sms;
-    k_dn_in_tc<<<in_grid, kInThreads, 0, s>>>(n->xa, n->Wpi, n->P + kOffBin, n->A1, n->d, n->err);
+    k_dn_in_tc<false><<<in_grid, kInThreads, 0, s>>>(n->xa, n->Wpi, n->P + kOffBin, nullptr, n->A1, n->d, n->err);
     launch_conv<0>(n, n->A1, n->Wp2, n->P + kOffB2, nullptr, n->A2, s);
     launch_conv<0>(n, n->A2, n->Wp3, n->P + kOffB3, nullptr, n->A3, s);
     // the 32 -> 1 output layer on the tensor cores (BF16 weights), + the residual
@@ -1463,7 +1430,6 @@ void enqueue_forward(ss_dn *n, const float *x, float *y, cudaStream_t s) {
 // loss of y against t, then the gradients of every parameter (accumulated into G)
 // (after enqueue_forward_act: n->xa holds the input, ya the output, both in the activation layout)
 void enqueue_backward(ss_dn *n, const float *t, const float *ya, cudaStream_t s, bool grads) {
-    const unsigned b = (unsigned)((n->nvox + 127) / 128);
     transpose<true>(n, t, n->ta, s);
     if (n->moment_weight > 0.f)
         k_dn_loss_moment<<<2 * n->sms, 128, 2 * n->d.np * sizeof(float), s>>>(
@@ -1484,7 +1450,9 @@ void enqueue_backward(ss_dn *n, const float *t, const float *ya, cudaStream_t s,
         else k_dn_wgrad1_tc<false><<<w1grid, kW1Threads, kW1Smem, s>>>(n->xa, n->D1, n->wpart, n->d, n->err);
         k_dn_wgrad1_reduce<<<(kW1Partial * 32 + 255) / 256, 256, 0, s>>>(n->wpart, w1grid, dW, db);
     };
-    k_dn_out_bwd<<<b, 128, 0, s>>>(n->dy, n->P, n->A3, n->D1, n->d, n->nvox);
+    // the output layer's backward into dZ3 (in D1): the input layer's GEMM on dy with mirrored weights
+    const int tiles = n->d.nx * n->d.np * (n->d.ny / kTileM), in_grid = tiles < kInCtasPerSm * n->sms ? tiles : kInCtasPerSm * n->sms;
+    k_dn_in_tc<true><<<in_grid, kInThreads, 0, s>>>(n->dy, n->Wpob, nullptr, n->A3, n->D1, n->d, n->err);
     wgrad1(true, n->G + kOffWout, nullptr);
     wgrad(n->D1, n->A2, n->G + kOffW3, n->G + kOffB3);
     launch_conv<2>(n, n->D1, n->Wm3, nullptr, n->A2, n->D2, s);
@@ -1508,7 +1476,7 @@ void destroy_dn(ss_dn *n) {
     if (n->stream) cudaStreamSynchronize(n->stream);
     cudaFree(n->P); cudaFree(n->G); cudaFree(n->M); cudaFree(n->S); cudaFree(n->dy); cudaFree(n->yb);
     cudaFree(n->xa); cudaFree(n->ta);
-    cudaFree(n->Wp2); cudaFree(n->Wp3); cudaFree(n->Wm2); cudaFree(n->Wm3); cudaFree(n->Wpo); cudaFree(n->Wpi);
+    cudaFree(n->Wp2); cudaFree(n->Wp3); cudaFree(n->Wm2); cudaFree(n->Wm3); cudaFree(n->Wpo); cudaFree(n->Wpi); cudaFree(n->Wpob);
     cudaFree(n->A1); cudaFree(n->A2); cudaFree(n->A3); cudaFree(n->D1); cudaFree(n->D2);
     cudaFree(n->sums); cudaFree(n->err); cudaFree(n->wpart);
     if (n->own_stream && n->stream) cudaStreamDestroy(n->stream);
@@ -1550,6 +1518,7 @@ int ss_dn_create(uint32_t nx, uint32_t ny, uint32_t np, uint64_t seed, void *str
     A((void **)&n->Wp2, kBAll); A((void **)&n->Wp3, kBAll); A((void **)&n->Wm2, kBAll); A((void **)&n->Wm3, kBAll);
     A((void **)&n->Wpo, kBAll);
     A((void **)&n->Wpi, kC * kC * 2);
+    A((void **)&n->Wpob, kC * kC * 2);
     A((void **)&n->A1, ab); A((void **)&n->A2, ab); A((void **)&n->A3, ab); A((void **)&n->D1, ab);
     A((void **)&n->D2, ab);
     A((void **)&n->sums, 2 * sizeof(double)); A((void **)&n->err, sizeof(unsigned));
