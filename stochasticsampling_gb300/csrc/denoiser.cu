@@ -27,8 +27,9 @@
 //    27 taps as K; k_dn_wgrad_tc / k_dn_wgrad1_tc: the weight gradients, GEMMs
 //    over the voxels with the accumulators resident in tensor memory and
 //    fixed-order sums over the CTAs.
-// The CUDA cores keep the layout transposes, the output layer's backward,
-// the loss, Adam and the weight packing.
+// The same GEMM, on dy with mirrored weights, is the output layer's backward.
+// The CUDA cores keep the layout transposes, the loss, Adam and the weight
+// packing.
 //
 // Shared-memory operand layouts (no swizzle).  A line (K-major): for each of
 // its 4 K chunks (8 channels, 16 bytes) the rows at a 16-byte stride, so row
