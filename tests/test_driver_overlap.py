@@ -190,3 +190,22 @@ def test_a_later_run_reuses_the_page_locked_buffers():
     driver.run_simulation(_settings(outputs, 4), sim, Sink(), overlap=True)
     assert len(sim.holders) == n
     assert all(sim.output_buffers[s][k] is v for (s, k), v in held.items())
+
+
+def test_a_failing_step_leaves_no_transfer_in_flight():
+    """A step that raises in the middle of the run: the error reaches the
+    caller, and the transfers begun before it are waited for (the slots are
+    free, the host buffers no longer written by the device)."""
+    class Failing(FakeSim):
+        def do_timestep(self):
+            if self.t == 5:
+                raise RuntimeError("step failed")
+            super().do_timestep()
+
+    sim, sink = Failing(), Sink()
+    with pytest.raises(RuntimeError, match="step failed"):
+        driver.run_simulation(_settings(OUTPUTS["every_kind"], 12), sim, sink, overlap=True)
+    assert not sim.inflight
+    # the entries completed before the failure reached the sink in step order
+    steps = [e["timestep"] for e in sink.entries]
+    assert steps == sorted(steps)
